@@ -1,0 +1,108 @@
+"""Seeded synthetic scenes for the FLIP step (host-side input generation).
+
+The reference has no datasets or benchmark inputs; its own demo seeds fluid
+bodies with 8 particles per cell, one per 2x2x2 sub-cell, jittered inside the
+sub-cell (src/engine/fluidsimulation.cpp:4522-4562).  The scenes here do the
+same with numpy's PCG64 generator, so a seed gives identical particles on
+every host.  Particles are returned as float32 (N, 3) position and velocity
+arrays in the layout `FluidSimulation::loadMarkerParticleData` takes
+(src/engine/fluidsimulation.h:102-106: packed xyz floats, 12 bytes each).
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+
+import numpy as np
+
+
+@dataclass
+class Scene:
+    isize: int
+    jsize: int
+    ksize: int
+    dx: float
+    positions: np.ndarray          # (N, 3) float32
+    velocities: np.ndarray         # (N, 3) float32
+    gravity: tuple = (0.0, -9.81, 0.0)
+    pic_ratio: float = 0.05        # FLIP blend 0.95
+    cfl: int = 5
+    frame_dt: float = 1.0 / 120.0
+    tolerance: float = 1e-6
+    steps: int = 10
+    name: str = ""
+    meta: dict = field(default_factory=dict)
+
+    @property
+    def num_particles(self) -> int:
+        return int(self.positions.shape[0])
+
+
+def _jittered_cells(cells: np.ndarray, dx: float, rng: np.random.Generator) -> np.ndarray:
+    """8 particles per cell, one per 2x2x2 sub-cell, uniform inside the sub-cell."""
+    sub = np.array([[a, b, c] for c in (0, 1) for b in (0, 1) for a in (0, 1)], dtype=np.float64)
+    n = cells.shape[0]
+    base = (cells[:, None, :].astype(np.float64) + 0.5 * sub[None, :, :]) * dx
+    jitter = rng.random((n, 8, 3)) * (0.5 * dx)
+    return (base + jitter).reshape(-1, 3).astype(np.float32)
+
+
+def _box_cells(isize, jsize, ksize, dx, lo, hi) -> np.ndarray:
+    i0, j0, k0 = [int(np.ceil(l / dx - 1e-9)) for l in lo]
+    i1 = min(int(np.floor(hi[0] / dx + 1e-9)), isize)
+    j1 = min(int(np.floor(hi[1] / dx + 1e-9)), jsize)
+    k1 = min(int(np.floor(hi[2] / dx + 1e-9)), ksize)
+    k, j, i = np.meshgrid(np.arange(k0, k1), np.arange(j0, j1), np.arange(i0, i1), indexing="ij")
+    return np.stack([i.ravel(), j.ravel(), k.ravel()], axis=1)
+
+
+def _sphere_cells(isize, jsize, ksize, dx, centre, radius) -> np.ndarray:
+    k, j, i = np.meshgrid(np.arange(ksize), np.arange(jsize), np.arange(isize), indexing="ij")
+    c = np.stack([i.ravel(), j.ravel(), k.ravel()], axis=1)
+    p = (c + 0.5) * dx
+    d2 = ((p - np.asarray(centre)) ** 2).sum(axis=1)
+    return c[d2 < radius * radius]
+
+
+def dam_break(n: int = 64, *, seed: int = 0, fill=(0.4, 0.6, 1.0), sphere: bool = False,
+              jsize: int | None = None, ksize: int | None = None, dx: float | None = None,
+              steps: int = 10, pic_ratio: float = 0.05, tolerance: float = 1e-6) -> Scene:
+    """Dam break in an n^3 (or n x jsize x ksize) box of side n*dx.
+
+    The fluid block spans x in [0, fill[0]], y in [0, fill[1]], z in [0, fill[2]]
+    of a unit-length domain edge; cells entirely inside it get 8 particles.
+    With `sphere`, a ball of radius 0.15 centred at (0.7, 0.7, 0.5) moving at
+    (0, -2, 0) is added.  Particles in the outer three cells sit inside the
+    domain walls and are removed by the first step, as in the reference.
+    """
+    jsize = n if jsize is None else jsize
+    ksize = n if ksize is None else ksize
+    dx = 1.0 / n if dx is None else dx
+    rng = np.random.default_rng(seed)
+    cells = _box_cells(n, jsize, ksize, dx, (0.0, 0.0, 0.0), fill)
+    pos = _jittered_cells(cells, dx, rng)
+    vel = np.zeros_like(pos)
+    if sphere:
+        sc = _sphere_cells(n, jsize, ksize, dx, (0.7, 0.7, 0.5), 0.15)
+        sp = _jittered_cells(sc, dx, rng)
+        sv = np.zeros_like(sp)
+        sv[:, 1] = -2.0
+        pos = np.concatenate([pos, sp])
+        vel = np.concatenate([vel, sv])
+    return Scene(n, jsize, ksize, dx, pos, vel, steps=steps, pic_ratio=pic_ratio,
+                 tolerance=tolerance, name=f"dam{'+sphere' if sphere else ''}_{n}x{jsize}x{ksize}")
+
+
+def plain_64(seed: int = 0) -> Scene:
+    """Plain dam break, 64^3, dx=1/64, 10 steps of 1/120 s."""
+    return dam_break(64, seed=seed, steps=10)
+
+
+def plain_128(seed: int = 0) -> Scene:
+    """Dam break plus falling sphere, 128^3, dx=1/128, 60 steps of 1/120 s."""
+    return dam_break(128, seed=seed, sphere=True, steps=60)
+
+
+def mixed_256(seed: int = 0) -> Scene:
+    """256x128x128 at dx=1/128 (domain 2 x 1 x 1), fluid in the lower 45%."""
+    return dam_break(256, jsize=128, ksize=128, dx=1.0 / 128, seed=seed,
+                     fill=(2.0, 0.45, 1.0), steps=30, pic_ratio=0.02)

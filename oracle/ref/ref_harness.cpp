@@ -1,0 +1,321 @@
+// Test-only harness around the reference FLIP engine (jklae/FLIPEngine3D,
+// src/engine/*).  It is compiled by oracle/build_ref.sh from the reference's
+// own sources into oracle/_ref/libflipref.so and is used ONLY by the tests and
+// by the golden-fixture generator to pin the C++ restatement in oracle/.
+// Nothing in the product library links or loads it.
+//
+// This translation unit redefines private/protected as public (after the
+// standard headers) so
+// it can (a) set the pressure tolerance, which the reference keeps private with
+// no setter (src/engine/fluidsimulation.h:1657), and (b) run one substep stage
+// by stage, in the order of FluidSimulation::_stepFluid
+// (src/engine/fluidsimulation.cpp:5471-5508), dumping the state between stages.
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <fstream>
+#include <iostream>
+#include <limits>
+#include <map>
+#include <mutex>
+#include <condition_variable>
+#include <queue>
+#include <sstream>
+#include <string>
+#include <thread>
+#include <vector>
+
+// Standard headers above are included before the access override below.
+#define private public
+#define protected public
+#include "fluidsimulation.h"
+#include "pressuresolver.h"
+#include "pcgsolver/pcgsolver.h"
+#include "pcgsolver/sparsematrix.h"
+
+namespace {
+
+struct RefSim {
+    FluidSimulation *sim = nullptr;
+    std::string status;
+};
+
+template <class T>
+void copyArray(Array3d<T> &a, T *out) {
+    int n = a.width * a.height * a.depth;
+    T *raw = a.getRawArray();
+    std::memcpy(out, raw, sizeof(T) * (size_t)n);
+}
+
+void copyBool(Array3d<bool> &a, uint8_t *out) {
+    int n = a.width * a.height * a.depth;
+    bool *raw = a.getRawArray();
+    for (int i = 0; i < n; i++) out[i] = raw[i] ? 1 : 0;
+}
+
+}  // namespace
+
+// Buffers filled by ref_update_staged.  Any pointer may be null.
+struct RefStageDump {
+    float *phi;          // I*J*K   liquid SDF after post-processing
+    float *u_p2g, *v_p2g, *w_p2g;           // after P2G + extrapolation
+    uint8_t *vu_p2g, *vv_p2g, *vw_p2g;      // valid masks after P2G (pre-extrapolation)
+    float *u_force, *v_force, *w_force;     // after body force
+    float *pressure;     // I*J*K   PCG solution scattered to cells (0 elsewhere)
+    double *rhs;         // I*J*K   negative divergence (0 elsewhere)
+    float *u_press, *v_press, *w_press;     // after pressure apply + extrapolation
+    float *u_final, *v_final, *w_final;     // after constrain
+    float *u_saved, *v_saved, *w_saved;     // saved field after constrain
+    float *vel_g2p;      // 3*N_before velocities after PIC/FLIP update (pre-advection)
+    float *pos_adv;      // 3*N_before positions after RK3+collision (pre-removal)
+    int *n_before;       // particle count at the start of the step
+    int *pcg_iters;
+    double *pcg_error;
+};
+
+extern "C" {
+
+void *ref_create(int isize, int jsize, int ksize, double dx) {
+    RefSim *r = new RefSim();
+    r->sim = new FluidSimulation(isize, jsize, ksize, dx);
+    r->sim->disableSurfaceReconstruction();
+    r->sim->_logfile.disableConsole();
+    return r;
+}
+
+void ref_destroy(void *h) {
+    RefSim *r = (RefSim *)h;
+    delete r->sim;
+    delete r;
+}
+
+void ref_set_threads(void *h, int n) { ((RefSim *)h)->sim->setMaxThreadCount(n); }
+void ref_set_pic_ratio(void *h, double ratio) { ((RefSim *)h)->sim->setPICFLIPRatio(ratio); }
+void ref_add_body_force(void *h, double x, double y, double z) { ((RefSim *)h)->sim->addBodyForce(x, y, z); }
+void ref_set_cfl(void *h, int c) { ((RefSim *)h)->sim->setCFLConditionNumber(c); }
+void ref_set_pressure_tol(void *h, double tol) { ((RefSim *)h)->sim->_pressureSolveTolerance = tol; }
+void ref_set_pressure_maxiter(void *h, int n) { ((RefSim *)h)->sim->_maxPressureSolveIterations = n; }
+
+void ref_load_particles(void *h, int n, const float *pos, const float *vel) {
+    FluidSimulationMarkerParticleData d;
+    d.size = n;
+    d.positions = (char *)pos;
+    d.velocities = (char *)vel;
+    ((RefSim *)h)->sim->loadMarkerParticleData(d);
+}
+
+void ref_initialize(void *h) { ((RefSim *)h)->sim->initialize(); }
+void ref_update(void *h, double dt) { ((RefSim *)h)->sim->update(dt); }
+
+int ref_num_particles(void *h) { return (int)((RefSim *)h)->sim->getNumMarkerParticles(); }
+
+void ref_get_particles(void *h, float *pos, float *vel) {
+    FluidSimulation *s = ((RefSim *)h)->sim;
+    if (pos) s->getMarkerParticlePositionData((char *)pos);
+    if (vel) s->getMarkerParticleVelocityData((char *)vel);
+}
+
+int ref_frame_substeps(void *h) { return ((RefSim *)h)->sim->getFrameStatsData().substeps; }
+
+void ref_get_liquid_phi(void *h, float *out) { copyArray(((RefSim *)h)->sim->_liquidSDF._phi, out); }
+void ref_get_solid_phi(void *h, float *out) { copyArray(((RefSim *)h)->sim->_solidSDF._phi, out); }
+
+void ref_get_mac(void *h, float *u, float *v, float *w) {
+    MACVelocityField &m = ((RefSim *)h)->sim->_MACVelocity;
+    copyArray(m._u, u);
+    copyArray(m._v, v);
+    copyArray(m._w, w);
+}
+
+void ref_get_weights(void *h, float *wu, float *wv, float *ww, float *wc) {
+    FluidSimulation *s = ((RefSim *)h)->sim;
+    s->_updateWeightGrid();
+    copyArray(s->_weightGrid.U, wu);
+    copyArray(s->_weightGrid.V, wv);
+    copyArray(s->_weightGrid.W, ww);
+    copyArray(s->_weightGrid.center, wc);
+}
+
+void ref_get_near_solid(void *h, int *dims, uint8_t *out) {
+    FluidSimulation *s = ((RefSim *)h)->sim;
+    dims[0] = s->_nearSolidGrid.width;
+    dims[1] = s->_nearSolidGrid.height;
+    dims[2] = s->_nearSolidGrid.depth;
+    if (out) copyBool(s->_nearSolidGrid, out);
+}
+
+const char *ref_pressure_status(void *h) {
+    RefSim *r = (RefSim *)h;
+    r->status = r->sim->_pressureSolverStatus;
+    return r->status.c_str();
+}
+
+// One frame of exactly one substep of length dt, run stage by stage in the
+// order of FluidSimulation::update (src/engine/fluidsimulation.cpp:5755-5845)
+// and _stepFluid (:5471-5508), with state dumps between the stages.  Returns
+// -1 (and does nothing) if the CFL condition would split the frame.
+int ref_update_staged(void *h, double dt, RefStageDump *d) {
+    FluidSimulation *s = ((RefSim *)h)->sim;
+    if (!s->_isSimulationInitialized) return -2;
+
+    s->_timingData = FluidSimulation::TimingData();
+    double epsdt = 1e-6;
+    s->_isZeroLengthDeltaTime = dt < epsdt;
+    dt = std::max(dt, epsdt);
+    s->_isCurrentFrameFinished = false;
+    s->_currentFrameDeltaTime = dt;
+    s->_currentFrameDeltaTimeRemaining = dt;
+    s->_currentFrameTimeStepNumber = 0;
+    s->_isSkippedFrame = s->_isZeroLengthDeltaTime && s->_outputData.isInitialized;
+
+    double step = fmin(s->_calculateNextTimeStep(dt), s->_currentFrameDeltaTimeRemaining);
+    if (step < dt) return -1;
+    s->_currentFrameTimeStep = step;
+    s->_currentFrameDeltaTimeRemaining -= step;
+    s->_isLastFrameTimeStep = true;
+
+    int I = s->_isize, J = s->_jsize, K = s->_ksize;
+    if (d->n_before) *d->n_before = (int)s->_markerParticles.size();
+
+    // _stepFluid, stage by stage
+    s->_launchUpdateObstacleObjectsThread(step);
+    s->_joinUpdateObstacleObjectsThread();
+    s->_launchUpdateLiquidLevelSetThread();
+    s->_joinUpdateLiquidLevelSetThread();
+    if (d->phi) copyArray(s->_liquidSDF._phi, d->phi);
+
+    // _advectVelocityField, split so the pre-extrapolation valid mask is visible
+    s->_validVelocities.reset();
+    s->_MACVelocity.clear();
+    if (!s->_markerParticles.empty()) {
+        VelocityAdvectorParameters params;
+        params.particles = &s->_markerParticles;
+        params.vfield = &s->_MACVelocity;
+        params.validVelocities = &s->_validVelocities;
+        params.particleRadius = s->_liquidSDFParticleRadius;
+        s->_velocityAdvector.advect(params);
+        if (d->vu_p2g) {
+            copyBool(s->_validVelocities.validU, d->vu_p2g);
+            copyBool(s->_validVelocities.validV, d->vv_p2g);
+            copyBool(s->_validVelocities.validW, d->vw_p2g);
+        }
+        s->_extrapolateFluidVelocities(s->_MACVelocity, s->_validVelocities);
+    }
+    if (d->u_p2g) ref_get_mac(h, d->u_p2g, d->v_p2g, d->w_p2g);
+
+    s->_saveVelocityField();
+    s->_applyBodyForcesToVelocityField(step);
+    if (d->u_force) ref_get_mac(h, d->u_force, d->v_force, d->w_force);
+
+    // _pressureSolve with PressureSolver::solve expanded so the solution
+    // vector is visible (src/engine/pressuresolver.cpp:44-76)
+    s->_updateWeightGrid();
+    PressureSolverParameters params;
+    params.cellwidth = s->_dx;
+    params.deltaTime = step;
+    params.tolerance = s->_pressureSolveTolerance;
+    params.acceptableTolerance = s->_pressureSolveAcceptableTolerance;
+    params.maxIterations = s->_maxPressureSolveIterations;
+    params.velocityField = &s->_MACVelocity;
+    params.validVelocities = &s->_validVelocities;
+    params.liquidSDF = &s->_liquidSDF;
+    params.solidSDF = &s->_solidSDF;
+    params.weightGrid = &s->_weightGrid;
+    params.isSurfaceTensionEnabled = false;
+
+    PressureSolver ps;
+    ps._initialize(params);
+    ps._conditionSolidVelocityField();
+    ps._initializeSurfaceTensionClusterData();
+    std::vector<double> rhs(ps._matSize, 0);
+    ps._calculateNegativeDivergenceVector(rhs);
+    double maxAbsCoeff = 0.0;
+    for (size_t i = 0; i < rhs.size(); i++) maxAbsCoeff = fmax(maxAbsCoeff, fabs(rhs[i]));
+    std::vector<double> soln(ps._matSize, 0);
+    int iters = 0;
+    double err = 0.0;
+    if (maxAbsCoeff < ps._pressureSolveTolerance) {
+        ps._solverStatus = "Pressure Solver Iterations: 0\nEstimated Error: 0.0";
+    } else {
+        SparseMatrixd matrix(ps._matSize, 7);
+        ps._calculateMatrixCoefficients(matrix);
+        PCGSolver<double> solver;
+        solver.setSolverParameters(ps._pressureSolveTolerance, ps._maxCGIterations);
+        bool ok = solver.solve(matrix, rhs, soln, err, iters);
+        bool accept = ok || (iters == ps._maxCGIterations && err < ps._pressureSolveAcceptableTolerance);
+        if (accept) ps._applySolutionToVelocityField(soln);
+        ps._solverStatus = accept ? "ok" : "***Pressure Solver FAILED";
+    }
+    s->_pressureSolverStatus = ps.getSolverStatus();
+    if (d->pcg_iters) *d->pcg_iters = iters;
+    if (d->pcg_error) *d->pcg_error = err;
+    if (d->pressure || d->rhs) {
+        if (d->pressure) std::fill(d->pressure, d->pressure + (size_t)I * J * K, 0.0f);
+        if (d->rhs) std::fill(d->rhs, d->rhs + (size_t)I * J * K, 0.0);
+        for (int idx = 0; idx < ps._matSize; idx++) {
+            GridIndex g = ps._pressureCells[idx];
+            size_t flat = (size_t)g.i + (size_t)I * ((size_t)g.j + (size_t)J * g.k);
+            if (d->pressure) d->pressure[flat] = (float)soln[idx];
+            if (d->rhs) d->rhs[flat] = rhs[idx];
+        }
+    }
+    s->_extrapolateFluidVelocities(s->_MACVelocity, s->_validVelocities);
+    if (d->u_press) ref_get_mac(h, d->u_press, d->v_press, d->w_press);
+
+    s->_constrainVelocityFields();
+    if (d->u_final) ref_get_mac(h, d->u_final, d->v_final, d->w_final);
+    if (d->u_saved) {
+        copyArray(s->_savedVelocityField._u, d->u_saved);
+        copyArray(s->_savedVelocityField._v, d->v_saved);
+        copyArray(s->_savedVelocityField._w, d->w_saved);
+    }
+
+    s->_updateMarkerParticleVelocities();
+    if (d->vel_g2p) {
+        for (size_t i = 0; i < s->_markerParticles.size(); i++) {
+            vmath::vec3 v = s->_markerParticles[i].velocity;
+            d->vel_g2p[3 * i + 0] = v.x;
+            d->vel_g2p[3 * i + 1] = v.y;
+            d->vel_g2p[3 * i + 2] = v.z;
+        }
+    }
+    s->_deleteSavedVelocityField();
+
+    // _advanceMarkerParticles with the pre-removal positions exposed
+    {
+        std::vector<vmath::vec3> positions;
+        positions.reserve(s->_markerParticles.size());
+        for (size_t i = 0; i < s->_markerParticles.size(); i++) positions.push_back(s->_markerParticles[i].position);
+        std::vector<vmath::vec3> output(positions.size());
+        int nthreads = (int)fmin(ThreadUtils::getMaxThreadCount(), positions.size());
+        std::vector<int> intervals = ThreadUtils::splitRangeIntoIntervals(0, positions.size(), nthreads);
+        for (int t = 0; t < nthreads; t++) {
+            s->_advanceMarkerParticlesThread(step, intervals[t], intervals[t + 1], &positions, &output);
+        }
+        for (size_t i = 0; i < s->_markerParticles.size(); i++) {
+            s->_markerParticles[i].position = output[i];
+            if (d->pos_adv) {
+                d->pos_adv[3 * i + 0] = output[i].x;
+                d->pos_adv[3 * i + 1] = output[i].y;
+                d->pos_adv[3 * i + 2] = output[i].z;
+            }
+        }
+        s->_removeMarkerParticles(s->_currentFrameDeltaTime);
+    }
+    s->_updateFluidObjects();
+    s->_outputSimulationData();
+    s->_currentFrameTimeStepNumber++;
+
+    s->_outputData.frameData.frame = s->_currentFrame;
+    s->_outputData.frameData.substeps = s->_currentFrameTimeStepNumber;
+    s->_outputData.frameData.deltaTime = dt;
+    s->_outputData.frameData.fluidParticles = (int)s->_markerParticles.size();
+    s->_outputData.isInitialized = true;
+    s->_currentFrame++;
+    s->_isCurrentFrameFinished = true;
+    return 0;
+}
+
+}  // extern "C"

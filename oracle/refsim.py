@@ -1,0 +1,209 @@
+"""ctypes binding of oracle/_ref/libflipref.so (test-only checker).
+
+The library is the reference engine itself (jklae/FLIPEngine3D src/engine),
+compiled by oracle/build_ref.sh; it exists only where the reference sources
+are present.  Tests and tests/golden/make_golden.py use it to pin the C++
+restatement in oracle/; the product never imports this module.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+
+import numpy as np
+
+_HERE = Path(__file__).resolve().parent
+_LIB_PATHS = {"ref": _HERE / "_ref" / "libflipref.so", "orc": _HERE / "_build" / "libflip_oracle.so"}
+_libs = {}
+
+
+def available(prefix: str = "ref") -> bool:
+    return _LIB_PATHS[prefix].exists()
+
+
+class _Dump(C.Structure):
+    _fields_ = [(n, C.c_void_p) for n in (
+        "phi", "u_p2g", "v_p2g", "w_p2g", "vu_p2g", "vv_p2g", "vw_p2g",
+        "u_force", "v_force", "w_force", "pressure", "rhs",
+        "u_press", "v_press", "w_press", "u_final", "v_final", "w_final",
+        "u_saved", "v_saved", "w_saved", "vel_g2p", "pos_adv",
+        "n_before", "pcg_iters", "pcg_error")]
+
+
+class _Prefixed:
+    """Attribute access with the symbol prefix ('ref_' or 'orc_') added."""
+
+    def __init__(self, cdll, prefix):
+        self._cdll, self._prefix = cdll, prefix
+
+    def __getattr__(self, name):
+        return getattr(self._cdll, name.replace("ref_", self._prefix + "_", 1))
+
+
+def lib(prefix: str = "ref"):
+    if prefix not in _libs:
+        path = _LIB_PATHS[prefix]
+        if not path.exists():
+            raise FileNotFoundError(f"{path} missing: build it first")
+        L = _Prefixed(C.CDLL(str(path)), prefix)
+        L.ref_create.restype = C.c_void_p
+        L.ref_create.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double]
+        for name, args in {
+            "ref_destroy": [C.c_void_p], "ref_set_threads": [C.c_void_p, C.c_int],
+            "ref_set_pic_ratio": [C.c_void_p, C.c_double],
+            "ref_add_body_force": [C.c_void_p, C.c_double, C.c_double, C.c_double],
+            "ref_set_cfl": [C.c_void_p, C.c_int], "ref_set_pressure_tol": [C.c_void_p, C.c_double],
+            "ref_set_pressure_maxiter": [C.c_void_p, C.c_int],
+            "ref_load_particles": [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p],
+            "ref_initialize": [C.c_void_p], "ref_update": [C.c_void_p, C.c_double],
+            "ref_get_particles": [C.c_void_p, C.c_void_p, C.c_void_p],
+            "ref_get_liquid_phi": [C.c_void_p, C.c_void_p], "ref_get_solid_phi": [C.c_void_p, C.c_void_p],
+            "ref_get_mac": [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p],
+            "ref_get_weights": [C.c_void_p] + [C.c_void_p] * (4 if prefix == "ref" else 3),
+            "ref_get_near_solid": [C.c_void_p, C.c_void_p, C.c_void_p],
+        }.items():
+            getattr(L, name).argtypes = args
+            getattr(L, name).restype = None
+        L.ref_num_particles.argtypes = [C.c_void_p]
+        L.ref_num_particles.restype = C.c_int
+        L.ref_frame_substeps.argtypes = [C.c_void_p]
+        L.ref_frame_substeps.restype = C.c_int
+        if prefix == "ref":
+            L.ref_pressure_status.argtypes = [C.c_void_p]
+            L.ref_pressure_status.restype = C.c_char_p
+        else:
+            L.ref_last_pcg_iters.argtypes = [C.c_void_p]
+            L.ref_last_pcg_iters.restype = C.c_int
+            L.ref_last_pcg_error.argtypes = [C.c_void_p]
+            L.ref_last_pcg_error.restype = C.c_double
+        L.ref_update_staged.argtypes = [C.c_void_p, C.c_double, C.POINTER(_Dump)]
+        L.ref_update_staged.restype = C.c_int
+        _libs[prefix] = L
+    return _libs[prefix]
+
+
+def _p(a):
+    return a.ctypes.data_as(C.c_void_p) if a is not None else None
+
+
+class RefSimulation:
+    """The reference FluidSimulation driven headless, as a test checker."""
+
+    PREFIX = "ref"
+
+    def __init__(self, isize, jsize, ksize, dx, *, threads=1):
+        self.L = lib(self.PREFIX)
+        self.dims = (isize, jsize, ksize)
+        self.dx = dx
+        self.h = self.L.ref_create(isize, jsize, ksize, dx)
+        self.L.ref_set_threads(self.h, threads)
+
+    def close(self):
+        if self.h:
+            self.L.ref_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def setup(self, scene, tolerance=None):
+        self.L.ref_set_pic_ratio(self.h, scene.pic_ratio)
+        self.L.ref_add_body_force(self.h, *scene.gravity)
+        self.L.ref_set_cfl(self.h, scene.cfl)
+        self.L.ref_set_pressure_tol(self.h, scene.tolerance if tolerance is None else tolerance)
+        pos = np.ascontiguousarray(scene.positions, dtype=np.float32)
+        vel = np.ascontiguousarray(scene.velocities, dtype=np.float32)
+        self.L.ref_load_particles(self.h, pos.shape[0], _p(pos), _p(vel))
+        self.L.ref_initialize(self.h)
+        return self
+
+    def update(self, dt):
+        self.L.ref_update(self.h, dt)
+
+    def particles(self):
+        n = self.L.ref_num_particles(self.h)
+        pos = np.zeros((n, 3), np.float32)
+        vel = np.zeros((n, 3), np.float32)
+        self.L.ref_get_particles(self.h, _p(pos), _p(vel))
+        return pos, vel
+
+    def solid_phi(self):
+        I, J, K = self.dims
+        a = np.zeros((K + 1, J + 1, I + 1), np.float32)
+        self.L.ref_get_solid_phi(self.h, _p(a))
+        return a
+
+    def liquid_phi(self):
+        I, J, K = self.dims
+        a = np.zeros((K, J, I), np.float32)
+        self.L.ref_get_liquid_phi(self.h, _p(a))
+        return a
+
+    def weights(self):
+        I, J, K = self.dims
+        wu = np.zeros((K, J, I + 1), np.float32)
+        wv = np.zeros((K, J + 1, I), np.float32)
+        ww = np.zeros((K + 1, J, I), np.float32)
+        if self.PREFIX == "ref":
+            wc = np.zeros((K, J, I), np.float32)
+            self.L.ref_get_weights(self.h, _p(wu), _p(wv), _p(ww), _p(wc))
+        else:
+            self.L.ref_get_weights(self.h, _p(wu), _p(wv), _p(ww))
+        return wu, wv, ww
+
+    def near_solid(self):
+        dims = np.zeros(3, np.int32)
+        self.L.ref_get_near_solid(self.h, _p(dims), None)
+        out = np.zeros((dims[2], dims[1], dims[0]), np.uint8)
+        self.L.ref_get_near_solid(self.h, _p(dims), _p(out))
+        return out
+
+    def pressure_status(self):
+        return self.L.ref_pressure_status(self.h).decode()
+
+    def update_staged(self, dt):
+        """One single-substep frame with the state between stages returned."""
+        I, J, K = self.dims
+        n = self.L.ref_num_particles(self.h)
+        su, sv, sw = (K, J, I + 1), (K, J + 1, I), (K + 1, J, I)
+        out = {}
+
+        def mk(name, shape, dtype=np.float32):
+            out[name] = np.zeros(shape, dtype)
+            return out[name]
+
+        d = _Dump()
+        d.phi = _p(mk("phi", (K, J, I)))
+        for stage in ("p2g", "force", "press", "final", "saved"):
+            setattr(d, "u_" + stage, _p(mk("u_" + stage, su)))
+            setattr(d, "v_" + stage, _p(mk("v_" + stage, sv)))
+            setattr(d, "w_" + stage, _p(mk("w_" + stage, sw)))
+        d.vu_p2g = _p(mk("vu_p2g", su, np.uint8))
+        d.vv_p2g = _p(mk("vv_p2g", sv, np.uint8))
+        d.vw_p2g = _p(mk("vw_p2g", sw, np.uint8))
+        d.pressure = _p(mk("pressure", (K, J, I)))
+        d.rhs = _p(mk("rhs", (K, J, I), np.float64))
+        d.vel_g2p = _p(mk("vel_g2p", (n, 3)))
+        d.pos_adv = _p(mk("pos_adv", (n, 3)))
+        d.n_before = _p(mk("n_before", (1,), np.int32))
+        d.pcg_iters = _p(mk("pcg_iters", (1,), np.int32))
+        d.pcg_error = _p(mk("pcg_error", (1,), np.float64))
+        rc = self.L.ref_update_staged(self.h, dt, C.byref(d))
+        if rc != 0:
+            raise RuntimeError(f"ref_update_staged returned {rc}")
+        out["positions"], out["velocities"] = self.particles()
+        return out
+
+
+class OracleSimulation(RefSimulation):
+    """The C++ restatement in oracle/flip_oracle.cpp (same interface)."""
+
+    PREFIX = "orc"
+
+    def pressure_status(self):
+        return (f"Pressure Solver Iterations: {self.L.ref_last_pcg_iters(self.h)}\n"
+                f"Estimated Error: {self.L.ref_last_pcg_error(self.h)}")
