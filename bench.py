@@ -1,0 +1,309 @@
+#!/usr/bin/env python3
+"""FLIP step benchmark on GB300: Mparticle-steps/s at 128^3.
+
+Workload (N=1): the 128^3 plain FLIP dam break (dx = 1/128, fluid box
+x<0.4, y<0.6, 8 jittered particles per cell, seed 0) plus a falling sphere
+(r = 0.15 at (0.7, 0.7, 0.5), v = (0, -2, 0)), FLIP blend 0.95, gravity
+-9.81, CFL 5, PCG tolerance 1e-6; one step = one update(1/120) frame.
+Inputs are synthetic (no dataset exists for this path).  Under torchrun each
+rank runs its own replica of the scene on its own GPU (weak scaling, no
+collective on the data path); the timing is max over ranks.
+
+  value  device time of K frames (CUDA events on the library's stream,
+         L2 flushed between frames outside the events), particles at the
+         start of each frame summed over frames and ranks.
+  e2e    the same metric through the public API with host buffers: each
+         frame is update(dt) plus getMarkerParticlePositionData() into host
+         memory (host wall clock, device synchronised).
+  --impl reference   the reference CPU path (the reference engine when it was
+         compiled here, else the C++ oracle restating it) on a bounded sample
+         of the same workload, rank 0 only.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+FRAME_DT = 1.0 / 120.0
+METRIC = "Mparticle-steps/s at 128^3 (plain FLIP step, dam break + sphere)"
+UNIT = "Mparticle-steps/s"
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d.get("hbm_gbs", 6800.0)), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (FileNotFoundError, OSError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], 0.0, set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = max(smax, float(f[2]))
+            except ValueError:
+                continue
+            for name, val in zip(names, f[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": smax, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def algorithmic_bytes(n_particles, n_cells, n_fluid, iters):
+    """Per-substep algorithmic HBM bytes of the FLIP step: 120 B per particle
+    (binning 48, SDF/P2G reads 24, G2P+RK3 read+write 48), 256 B per grid
+    cell (SDF, flags, faces, 2x extrapolation, save, force, RHS, apply,
+    2x constrain, G2P grid reads, weights) and 132 B per pressure cell per
+    PCG iteration (stencil 24, two sweeps 56, three axpys 36, two dots 16)."""
+    return 120.0 * n_particles + 256.0 * n_cells, 132.0 * n_fluid * iters
+
+
+def run_gpu(args, rank, world):
+    import torch
+
+    import flipengine3d_gb300 as fg
+    from flipengine3d_gb300.scenes import plain_128
+
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    sc = plain_128()
+    stream = torch.cuda.Stream()
+    sim = fg.FluidSimulation.from_scene(sc)
+    sim.setStream(stream.cuda_stream)
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")   # 256 MB > 129 MB L2
+
+    for _ in range(args.warmup):
+        sim.update(FRAME_DT)
+    torch.cuda.synchronize()
+
+    # device-timed frames
+    sim.set_stage_timing(True)
+    launches0 = sim.launch_count()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    particles = 0
+    iters, cells = [], []
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clocks:
+        for k in range(args.steps):
+            with torch.cuda.stream(stream):
+                flush.zero_()
+            particles += sim.getNumMarkerParticles()
+            ev[k][0].record(stream)
+            sim.update(FRAME_DT)
+            ev[k][1].record(stream)
+            st = sim.getFrameStatsData()
+            iters.append(st.pressure_iterations)
+            cells.append(st.pressure_cells)
+        torch.cuda.synchronize()
+    launches = sim.launch_count() - launches0
+    ms = sum(a.elapsed_time(b) for a, b in ev)
+    stage_ms, substeps = sim.stage_times()
+    sim.set_stage_timing(False)
+
+    # end to end through the public API with host buffers
+    d2h = 0
+    torch.cuda.synchronize()
+    e2e_particles = 0
+    t0 = time.perf_counter()
+    for k in range(args.steps):
+        e2e_particles += sim.getNumMarkerParticles()
+        sim.update(FRAME_DT)
+        pos = sim.getMarkerParticlePositionData()
+        d2h += pos.nbytes
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+
+    t = torch.tensor([ms, e2e_s], dtype=torch.float64, device="cuda")
+    tot = torch.tensor([particles, e2e_particles], dtype=torch.float64, device="cuda")
+    if world > 1:
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        torch.distributed.all_reduce(tot, op=torch.distributed.ReduceOp.SUM)
+    ms_max, e2e_max = float(t[0]), float(t[1])
+    if rank != 0:
+        return None
+    value = float(tot[0]) / (ms_max / 1e3) / 1e6
+    e2e_value = float(tot[1]) / e2e_max / 1e6
+
+    # roofline of the dominant stage
+    peak, peak_kind = peaks()
+    n_cells = sc.isize * sc.jsize * sc.ksize
+    n_avg = particles / args.steps
+    dominant = max(stage_ms, key=stage_ms.get)
+    base_b, pcg_b = algorithmic_bytes(n_avg, n_cells, np.mean(cells), np.mean(iters))
+    stage_bytes = {
+        "pressure": pcg_b * substeps,
+        "advect": 48.0 * n_avg * substeps + 24.0 * n_cells * substeps,
+        "binning": 48.0 * n_avg * substeps,
+        "p2g": 24.0 * n_avg * substeps + (15.0 + 48.0) * n_cells * substeps,
+        "liquid_sdf": 12.0 * n_avg * substeps + 5.0 * n_cells * substeps,
+        "constrain": (48.0 + 24.0) * n_cells * substeps,
+        "force": 24.0 * n_cells * substeps,
+    }
+    achieved = stage_bytes[dominant] / (stage_ms[dominant] / 1e3) / 1e9
+    step_achieved = (base_b + pcg_b) * substeps / (sum(stage_ms.values()) / 1e3) / 1e9
+
+    cpu = cpu_baseline(args) if not args.no_cpu_baseline else None
+    line = {
+        "metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(ms_max / args.steps, 4), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32 (FP64 dots/refinement)",
+        "data": "synthetic: seeded dam break + sphere, 8 jittered particles per cell",
+        "config": {"workload": "plain FLIP 128x128x128, dx=1/128, dam break + sphere, FLIP blend 0.95, "
+                               "PCG tol 1e-6, dt=1/120", "particles": int(n_avg), "grid": [sc.isize, sc.jsize, sc.ksize],
+                   "pressure_cells": int(np.mean(cells)), "pcg_iterations_mean": float(np.mean(iters)),
+                   "l2": "flushed between timed frames (256 MB write, outside the events)",
+                   "parallelism": f"replicas x{world}"},
+        "e2e": {"value": round(e2e_value, 4), "unit": UNIT, "h2d_bytes_per_step": 8,
+                "d2h_bytes_per_step": int(d2h / args.steps),
+                "path": "FluidSimulation.update(dt) + getMarkerParticlePositionData() via the C ABI"},
+        "roofline": {"bound": "hbm", "kernel": f"stage:{dominant}", "achieved": round(achieved, 1),
+                     "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": None,
+                     "peak_source": peak_kind,
+                     "step_achieved_gbs": round(step_achieved, 1),
+                     "stage_ms_per_step": {k: round(v / args.steps, 3) for k, v in stage_ms.items()}},
+        "cpu_baseline": cpu,
+        "gpu_launches": int(launches),
+        "clocks": clocks.summary(),
+    }
+    return line
+
+
+def cpu_sample_sim(args, threads):
+    """The reference CPU path on one bounded sample of the workload."""
+    from flipengine3d_gb300.scenes import plain_128
+    from oracle import refsim
+    sc = plain_128()
+    if refsim.available("ref"):
+        kind, cls = "reference", refsim.RefSimulation
+    else:
+        kind, cls = "port", refsim.OracleSimulation
+        threads = 1
+    sim = cls(sc.isize, sc.jsize, sc.ksize, sc.dx, threads=threads).setup(sc)
+    return sc, sim, kind, threads
+
+
+def cpu_baseline(args):
+    threads = os.cpu_count() or 1
+    sc, sim, kind, threads = cpu_sample_sim(args, threads)
+    sim.update(FRAME_DT)                       # first frame builds the solid level set: untimed
+    n = sim.particles()[0].shape[0]
+    t0 = time.perf_counter()
+    sim.update(FRAME_DT)
+    dt = time.perf_counter() - t0
+    return {"value": round(n / dt / 1e6, 5), "unit": UNIT, "cores": threads, "kind": kind,
+            "sample": f"1 timed frame of the 128^3 workload ({n} particles) after 1 untimed frame, {dt:.1f} s"}
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return None
+    threads = os.cpu_count() or 1
+    sc, sim, kind, threads = cpu_sample_sim(args, threads)
+    steps = max(1, min(args.steps, args.reference_max_steps))
+    warm = max(0, min(args.warmup, 1))
+    for _ in range(warm):
+        sim.update(FRAME_DT)
+    total, t = 0, 0.0
+    for _ in range(steps):
+        n = sim.particles()[0].shape[0]
+        t0 = time.perf_counter()
+        sim.update(FRAME_DT)
+        t += time.perf_counter() - t0
+        total += n
+    value = total / t / 1e6
+    sample = (f"{steps} timed frame(s) of the 128^3 workload after {warm} untimed, "
+              f"{'reference engine' if kind == 'reference' else 'C++ oracle restating it'}, {threads} thread(s)")
+    return {"metric": METRIC, "value": round(value, 5), "unit": UNIT, "n_gpus": world, "steps": steps,
+            "warmup": warm, "ms_per_step": round(t / steps * 1e3, 2), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32/f64", "data": "synthetic: seeded dam break + sphere",
+            "config": {"workload": "plain FLIP 128x128x128, dx=1/128, dam break + sphere, FLIP blend 0.95, "
+                                   "PCG tol 1e-6, dt=1/120"},
+            "impl": "reference",
+            "cpu_baseline": {"value": round(value, 5), "unit": UNIT, "cores": threads, "kind": kind, "sample": sample},
+            "e2e": {"value": round(value, 5), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--reference-max-steps", type=int, default=3)
+    args = ap.parse_args()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if world > 1 and args.impl == "gb300":
+        import torch
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        torch.distributed.init_process_group("nccl")
+    if args.impl == "reference":
+        line = run_reference(args, rank, world)
+    else:
+        line = run_gpu(args, rank, world)
+    if line is not None:
+        print(json.dumps(line), flush=True)
+    if world > 1 and args.impl == "gb300":
+        import torch
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

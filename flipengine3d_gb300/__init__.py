@@ -1,0 +1,8 @@
+"""GB300-native FLIP step behind the reference's FluidSimulation API.
+
+The compute lives in libflip3d_gb300.so (hand-written CUDA for sm_103a,
+flipengine3d_gb300/csrc); `FluidSimulation` mirrors the reference class over
+its C ABI (include/flip3d.h).
+"""
+from .fluidsimulation import FluidSimulation, FlipCudaError, compute_domain_solid, load_library  # noqa: F401
+from . import scenes  # noqa: F401

@@ -1,0 +1,67 @@
+// Shared device helpers for the GB300 FLIP step.
+//
+// Index and position conventions follow the reference engine so that cell
+// keys, block frames and flags come out bit-identical:
+//   flat index            i + ni*(j + nj*k)               (array3d.h:425-433)
+//   position -> index     floor((double)p * (1.0/dx))     (grid3d.h:56-61)
+//   index -> position     (float)((double)(float)i * dx)  (grid3d.h:75-81)
+//   cell centre           (float)((double)(float)i*dx + 0.5*dx)  (grid3d.h:99-104)
+// The library is compiled with --fmad=false: float expressions that must be
+// bit-exact (SDF distances, P2G kernel weights, extrapolation means) are
+// evaluated unfused, as the reference's x86-64 build does.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace flip {
+
+struct Dims {
+    int ni, nj, nk;
+    __host__ __device__ long long size() const { return (long long)ni * nj * nk; }
+    __host__ __device__ long long idx(int i, int j, int k) const {
+        return (long long)i + (long long)ni * ((long long)j + (long long)nj * k);
+    }
+    __host__ __device__ bool in(int i, int j, int k) const {
+        return i >= 0 && j >= 0 && k >= 0 && i < ni && j < nj && k < nk;
+    }
+};
+
+// floor((double)p * inv) without FP64 in the common case: the float product
+// is within 1.3e-7 relative of the exact one, so away from integer
+// boundaries its floor is the exact floor; near them fall back to FP64.
+__device__ __forceinline__ int exact_floor(float p, double inv, float invf) {
+    float q = __fmul_rn(p, invf);
+    float fq = floorf(q);
+    float frac = __fsub_rn(q, fq);
+    float tolf = 1e-3f + 4e-7f * fabsf(q);
+    if (frac > tolf && frac < 1.0f - tolf) return (int)fq;
+    return (int)floor((double)p * inv);
+}
+
+__device__ __forceinline__ float idx_to_pos(int i, double dx) { return (float)((double)(float)i * dx); }
+__device__ __forceinline__ float cell_centre(int i, double dx) { return (float)((double)(float)i * dx + 0.5 * dx); }
+
+// order-preserving float <-> uint32 encoding for deterministic atomicMin
+__device__ __forceinline__ unsigned int f2ord(float f) {
+    unsigned int b = __float_as_uint(f);
+    return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+}
+__device__ __forceinline__ float ord2f(unsigned int u) {
+    unsigned int b = (u & 0x80000000u) ? (u & 0x7fffffffu) : ~u;
+    return __uint_as_float(b);
+}
+
+// Particle key flags (bits above the 28-bit cell index).
+constexpr unsigned int KEY_CELL_MASK = 0x0fffffffu;
+constexpr unsigned int KEY_SOLID = 0x80000000u;    // removed: inside the solid
+constexpr unsigned int KEY_FAST = 0x40000000u;     // over the extreme-speed limit
+constexpr unsigned int KEY_NONE = 0xffffffffu;     // no particle
+
+inline unsigned int div_up(long long a, int b) { return (unsigned int)((a + b - 1) / b); }
+
+// Count of kernel launches issued by this library (all contexts); each
+// launcher adds the number of kernels it enqueues.
+long long &launch_counter();
+#define FLIP_COUNT(n) (::flip::launch_counter() += (n))
+
+}  // namespace flip

@@ -1,0 +1,888 @@
+// Host side of the GB300 FLIP step: the context behind the C ABI in
+// include/flip3d.h, device memory, the frame/substep loop of
+// FluidSimulation::update (src/engine/fluidsimulation.cpp:5755-5845) and the
+// stage sequence of _stepFluid (:5471-5508), each stage a CUDA kernel.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/flip3d.h"
+#include "flip_kernels.cuh"
+#include "solid_setup.h"
+
+namespace flip {
+long long &launch_counter() {
+    static long long n = 0;
+    return n;
+}
+}  // namespace flip
+
+using namespace flip;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const std::string &msg) {
+    g_err = msg;
+    return code;
+}
+
+#define CK(call)                                                                                  \
+    do {                                                                                          \
+        cudaError_t e_ = (call);                                                                  \
+        if (e_ != cudaSuccess) return fail(FLIP_E_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+template <class T>
+int dalloc(T **p, size_t count) {
+    if (count == 0) count = 1;
+    cudaError_t e = cudaMalloc((void **)p, count * sizeof(T));
+    if (e != cudaSuccess) return fail(FLIP_E_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    return FLIP_OK;
+}
+
+}  // namespace
+
+struct flip_ctx {
+    int I, J, K;
+    double dx;
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    bool ownStream = false;
+
+    // parameters (reference defaults, fluidsimulation.h:1519-1700)
+    double picRatio = 0.05;
+    std::vector<float> bodyForces;   // xyz triples
+    double cfl = 5.0;
+    double tol = 1e-9, accTol = 1.0;
+    int maxIter = 1000;
+    int minFrameSteps = 1, maxFrameSteps = 6;
+    int maxPerCell = 250;
+    double maxRemovePct = 0.0005;
+    int maxRemoveAbs = 35;
+
+    // state
+    bool initialized = false;
+    std::vector<float> queuePos, queueVel;
+    const float *queueDevPos = nullptr, *queueDevVel = nullptr;
+    int queueDevN = 0;
+    int n = 0, capacity = 0;
+    int frame = 0, stepNumber = 0;
+    double frameDt = 0, frameRemaining = 0;
+    bool outputInitialized = false;
+    bool solidBuilt = false;
+    flip_frame_stats stats{};
+    double maxSpeed = 0.0;
+
+    DomainBox box;
+    StepConsts c{};
+
+    // device buffers
+    ParticleSoA pa{}, pb{};
+    unsigned int *keys = nullptr;
+    int *cellCount = nullptr, *cellStart = nullptr, *cursor = nullptr, *slots = nullptr;
+    int *survivors = nullptr, *newStart = nullptr, *scanScratch = nullptr, *scanTotal = nullptr;
+    float *phi = nullptr, *solidPhi = nullptr, *wu = nullptr, *wv = nullptr, *ww = nullptr;
+    uint8_t *solidCC = nullptr, *nearSolid = nullptr;
+    float *u = nullptr, *v = nullptr, *w = nullptr, *su = nullptr, *sv = nullptr, *sw = nullptr;
+    uint8_t *vu = nullptr, *vv = nullptr, *vw = nullptr, *status = nullptr;
+    PressureBuffers pr{};
+    unsigned int *speedHist = nullptr, *maxVelSqBits = nullptr;
+    float *maxSpeedSq = nullptr;
+    // pinned host mailbox for per-substep scalars
+    struct Mail {
+        int levelRange[3];
+        double bmax;
+        double rho;
+        unsigned int rmaxBits;
+        int total;
+        unsigned int velSqBits;
+    } *mail = nullptr;
+    std::vector<void *> allocations;
+
+    long long launchesAtCreate = 0;
+
+    // stage timing
+    bool timing = false;
+    bool endMarkPending = false;
+    cudaEvent_t ev[FLIP_NUM_STAGES + 1] = {};
+    double stageMs[FLIP_NUM_STAGES] = {};
+    long long timedSubsteps = 0;
+    void mark(int stage) {
+        if (timing) cudaEventRecord(ev[stage], stream);
+    }
+
+    long long nu() const { return (long long)(I + 1) * J * K; }
+    long long nv() const { return (long long)I * (J + 1) * K; }
+    long long nw() const { return (long long)I * J * (K + 1); }
+    long long nc() const { return (long long)I * J * K; }
+
+    template <class T>
+    int alloc(T **p, size_t count) {
+        int rc = dalloc(p, count);
+        if (rc == FLIP_OK) allocations.push_back((void *)*p);
+        return rc;
+    }
+};
+
+namespace {
+
+int sync(flip_ctx *x) {
+    cudaError_t e = cudaStreamSynchronize(x->stream);
+    if (e != cudaSuccess) return fail(FLIP_E_CUDA, std::string("stream: ") + cudaGetErrorString(e));
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return fail(FLIP_E_CUDA, std::string("launch: ") + cudaGetErrorString(e));
+    return FLIP_OK;
+}
+
+float3 body_force(const flip_ctx *x) {
+    // _getConstantBodyForce (fluidsimulation.cpp:3363-3370): float sum
+    float bx = 0.f, by = 0.f, bz = 0.f;
+    for (size_t q = 0; q + 2 < x->bodyForces.size(); q += 3) {
+        bx += x->bodyForces[q];
+        by += x->bodyForces[q + 1];
+        bz += x->bodyForces[q + 2];
+    }
+    return make_float3(bx, by, bz);
+}
+
+int alloc_grids(flip_ctx *x) {
+    int rc;
+    long long nc = x->nc();
+    if ((rc = x->alloc(&x->cellCount, nc + 1))) return rc;
+    if ((rc = x->alloc(&x->cellStart, nc + 1))) return rc;
+    if ((rc = x->alloc(&x->cursor, nc + 1))) return rc;
+    if ((rc = x->alloc(&x->survivors, nc + 1))) return rc;
+    if ((rc = x->alloc(&x->newStart, nc + 1))) return rc;
+    if ((rc = x->alloc(&x->scanScratch, scan_scratch_ints((int)nc) + 4))) return rc;
+    if ((rc = x->alloc(&x->scanTotal, 4))) return rc;
+    if ((rc = x->alloc(&x->phi, nc))) return rc;
+    if ((rc = x->alloc(&x->solidPhi, (size_t)(x->I + 1) * (x->J + 1) * (x->K + 1)))) return rc;
+    if ((rc = x->alloc(&x->solidCC, nc))) return rc;
+    if ((rc = x->alloc(&x->wu, x->nu())) || (rc = x->alloc(&x->wv, x->nv())) || (rc = x->alloc(&x->ww, x->nw())))
+        return rc;
+    if ((rc = x->alloc(&x->u, x->nu())) || (rc = x->alloc(&x->v, x->nv())) || (rc = x->alloc(&x->w, x->nw())))
+        return rc;
+    if ((rc = x->alloc(&x->su, x->nu())) || (rc = x->alloc(&x->sv, x->nv())) || (rc = x->alloc(&x->sw, x->nw())))
+        return rc;
+    if ((rc = x->alloc(&x->vu, x->nu())) || (rc = x->alloc(&x->vv, x->nv())) || (rc = x->alloc(&x->vw, x->nw())))
+        return rc;
+    if ((rc = x->alloc(&x->status, x->nu() + x->nv() + x->nw()))) return rc;
+    PressureBuffers &p = x->pr;
+    if ((rc = x->alloc(&p.fluid, nc))) return rc;
+    if ((rc = x->alloc(&p.A, nc)) || (rc = x->alloc(&p.L, nc))) return rc;
+    if ((rc = x->alloc(&p.Adiag, nc)) || (rc = x->alloc(&p.b, nc)) || (rc = x->alloc(&p.invdiagD, nc)) ||
+        (rc = x->alloc(&p.x, nc)))
+        return rc;
+    if ((rc = x->alloc(&p.r, nc)) || (rc = x->alloc(&p.z, nc)) || (rc = x->alloc(&p.s, nc)) ||
+        (rc = x->alloc(&p.q, nc)) || (rc = x->alloc(&p.pressure, nc)))
+        return rc;
+    p.nPartials = pressure_partials(x->c);
+    if ((rc = x->alloc(&p.partials, p.nPartials + 32))) return rc;
+    if ((rc = x->alloc(&p.scal, 8)) || (rc = x->alloc(&p.rmaxBits, 4)) || (rc = x->alloc(&p.levelRange, 4)))
+        return rc;
+    if ((rc = x->alloc(&x->speedHist, 8)) || (rc = x->alloc(&x->maxVelSqBits, 4)) || (rc = x->alloc(&x->maxSpeedSq, 4)))
+        return rc;
+    CK(cudaMemsetAsync(x->phi, 0, nc * sizeof(float), x->stream));
+    CK(cudaMemsetAsync(x->u, 0, x->nu() * 4, x->stream));
+    CK(cudaMemsetAsync(x->v, 0, x->nv() * 4, x->stream));
+    CK(cudaMemsetAsync(x->w, 0, x->nw() * 4, x->stream));
+    return FLIP_OK;
+}
+
+int alloc_particles(flip_ctx *x, int cap) {
+    int rc;
+    x->capacity = cap;
+    ParticleSoA *bufs[2] = {&x->pa, &x->pb};
+    for (ParticleSoA *b : bufs) {
+        if ((rc = x->alloc(&b->px, cap)) || (rc = x->alloc(&b->py, cap)) || (rc = x->alloc(&b->pz, cap)) ||
+            (rc = x->alloc(&b->vx, cap)) || (rc = x->alloc(&b->vy, cap)) || (rc = x->alloc(&b->vz, cap)) ||
+            (rc = x->alloc(&b->id, cap)))
+            return rc;
+    }
+    if ((rc = x->alloc(&x->keys, cap)) || (rc = x->alloc(&x->slots, cap))) return rc;
+    return FLIP_OK;
+}
+
+// Counting sort of the particles in `pa` by cell, with removal flags in
+// keys; survivors land in `pb` ordered (cell, id); then the buffers swap.
+int rebin(flip_ctx *x) {
+    cudaStream_t s = x->stream;
+    int nc = (int)x->nc();
+    CK(cudaMemsetAsync(x->cellCount, 0, (size_t)(nc + 1) * sizeof(int), s));
+    CK(cudaMemsetAsync(x->cursor, 0, (size_t)(nc + 1) * sizeof(int), s));
+    CK(cudaMemsetAsync(x->maxVelSqBits, 0, sizeof(unsigned int), s));
+    launch_bin_count(x->keys, x->n, x->cellCount, s);
+    launch_scan_cells(x->cellCount, nc, x->cellStart, x->scanScratch, x->scanTotal, s);
+    launch_bin_scatter(x->keys, x->n, x->cellStart, x->cursor, x->slots, s);
+    launch_cell_sort_select(x->cellStart, nc, x->slots, x->pa.id, x->keys, x->maxPerCell, x->survivors, s);
+    launch_scan_cells(x->survivors, nc, x->newStart, x->scanScratch, x->scanTotal, s);
+    launch_gather_particles(x->pa, x->pb, x->cellStart, x->slots, x->newStart, nc, x->maxVelSqBits, s);
+    CK(cudaMemcpyAsync(&x->mail->total, x->scanTotal, sizeof(int), cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(&x->mail->velSqBits, x->maxVelSqBits, sizeof(unsigned int), cudaMemcpyDeviceToHost, s));
+    if (x->endMarkPending) {
+        x->mark(FLIP_NUM_STAGES);
+        x->endMarkPending = false;
+    }
+    int rc = sync(x);
+    if (rc) return rc;
+    std::swap(x->pa, x->pb);
+    std::swap(x->cellStart, x->newStart);
+    x->n = x->mail->total;
+    float vsq;
+    std::memcpy(&vsq, &x->mail->velSqBits, 4);
+    x->maxSpeed = std::sqrt((double)vsq);
+    return FLIP_OK;
+}
+
+int rebin_marked(flip_ctx *x) {
+    // rebin() synchronises; record the end mark before its final sync
+    x->endMarkPending = true;
+    return rebin(x);
+}
+
+int collect_stage_times(flip_ctx *x) {
+    if (!x->timing) return FLIP_OK;
+    CK(cudaEventSynchronize(x->ev[FLIP_NUM_STAGES]));
+    for (int q = 0; q < FLIP_NUM_STAGES; q++) {
+        float ms = 0.f;
+        CK(cudaEventElapsedTime(&ms, x->ev[q], x->ev[q + 1]));
+        x->stageMs[q] += ms;
+    }
+    x->timedSubsteps++;
+    return FLIP_OK;
+}
+
+int build_solid(flip_ctx *x) {
+    x->box.compute(x->I, x->J, x->K, x->dx, x->cfl);
+    cudaStream_t s = x->stream;
+    CK(cudaMemcpyAsync(x->solidPhi, x->box.nodal.data(), x->box.nodal.size() * 4, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(x->wu, x->box.wu.data(), x->box.wu.size() * 4, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(x->wv, x->box.wv.data(), x->box.wv.size() * 4, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(x->ww, x->box.ww.data(), x->box.ww.size() * 4, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(x->solidCC, x->box.solidCentre.data(), x->box.solidCentre.size(), cudaMemcpyHostToDevice, s));
+    int rc = x->alloc(&x->nearSolid, x->box.near.size());
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(x->nearSolid, x->box.near.data(), x->box.near.size(), cudaMemcpyHostToDevice, s));
+    StepConsts &c = x->c;
+    c.nsi = x->box.nsi; c.nsj = x->box.nsj; c.nsk = x->box.nsk;
+    c.nearCell = x->box.nearCell;
+    c.invNearCell = 1.0 / x->box.nearCell;
+    c.invNearCellf = (float)c.invNearCell;
+    // collision boundary: the domain box shrunk again by 0.1 dx
+    double v2 = -((double)0.1f * x->dx), h2 = 0.5 * v2;
+    c.bposx = x->box.px - (float)h2; c.bposy = x->box.py - (float)h2; c.bposz = x->box.pz - (float)h2;
+    c.bw = x->box.ex + v2; c.bh = x->box.ey + v2; c.bd = x->box.ez + v2;
+    rc = sync(x);
+    if (rc) return rc;
+    x->solidBuilt = true;
+    return FLIP_OK;
+}
+
+template <class T>
+void dl(flip_ctx *x, T *dst, const T *src, long long count) {
+    if (dst) cudaMemcpyAsync(dst, src, count * sizeof(T), cudaMemcpyDeviceToHost, x->stream);
+}
+
+// Particles of the current arrays in the reference's order (by id).
+int particles_in_order(flip_ctx *x, std::vector<float> *pos, std::vector<float> *vel) {
+    int n = x->n;
+    std::vector<float> px(n), py(n), pz(n), vx(n), vy(n), vz(n);
+    std::vector<unsigned int> id(n);
+    dl(x, px.data(), x->pa.px, n); dl(x, py.data(), x->pa.py, n); dl(x, pz.data(), x->pa.pz, n);
+    dl(x, vx.data(), x->pa.vx, n); dl(x, vy.data(), x->pa.vy, n); dl(x, vz.data(), x->pa.vz, n);
+    dl(x, id.data(), x->pa.id, n);
+    int rc = sync(x);
+    if (rc) return rc;
+    std::vector<int> order(n);
+    for (int q = 0; q < n; q++) order[q] = q;
+    std::sort(order.begin(), order.end(), [&](int a, int b) { return id[a] < id[b]; });
+    if (pos) pos->resize(3 * (size_t)n);
+    if (vel) vel->resize(3 * (size_t)n);
+    for (int q = 0; q < n; q++) {
+        int o = order[q];
+        if (pos) { (*pos)[3 * q] = px[o]; (*pos)[3 * q + 1] = py[o]; (*pos)[3 * q + 2] = pz[o]; }
+        if (vel) { (*vel)[3 * q] = vx[o]; (*vel)[3 * q + 1] = vy[o]; (*vel)[3 * q + 2] = vz[o]; }
+    }
+    return FLIP_OK;
+}
+
+// PressureSolver::solve (pressuresolver.cpp:44-76) with PCGSolver::solve
+// (pcgsolver.h:248-302): returns FLIP_OK when the velocity field was
+// updated (or nothing needed solving), FLIP_E_SOLVER_NOCONV when the solve
+// failed and the field was left as it was.
+int pressure_solve(flip_ctx *x, double dt, bool *applied, flip_stage_dump *d) {
+    cudaStream_t s = x->stream;
+    StepConsts &c = x->c;
+    PressureBuffers &p = x->pr;
+    *applied = false;
+    x->stats.pressure_iterations = 0;
+    x->stats.pressure_error = 0.0;
+    launch_pressure_build(c, x->phi, x->wu, x->wv, x->ww, x->u, x->v, x->w, dt, p, s);
+    CK(cudaMemcpyAsync(x->mail->levelRange, p.levelRange, 3 * sizeof(int), cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(&x->mail->bmax, p.scal + 2, sizeof(double), cudaMemcpyDeviceToHost, s));
+    int rc = sync(x);
+    if (rc) return rc;
+    if (d && d->rhs) {
+        CK(cudaMemcpy(d->rhs, p.b, x->nc() * sizeof(double), cudaMemcpyDeviceToHost));
+    }
+    int lo = x->mail->levelRange[0], hi = x->mail->levelRange[1];
+    x->stats.pressure_cells = x->mail->levelRange[2];
+    double bmax = x->mail->bmax;
+    if (hi < lo || bmax < x->tol) return FLIP_OK;   // empty system or nothing to project
+    double ptol = std::max(x->tol, 1e-30) * bmax;
+
+    launch_mic0_factor(c, x->phi, x->wu, x->wv, x->ww, dt, p, lo, hi, s);
+    launch_init_residual(c, p, s);
+    launch_precondition(c, p, p.r, p.z, lo, hi, s);
+    launch_dot_zr(c, p, s);
+    CK(cudaMemcpyAsync(&x->mail->rho, p.scal + 1, sizeof(double), cudaMemcpyDeviceToHost, s));
+    rc = sync(x);
+    if (rc) return rc;
+    double rho = x->mail->rho;
+    bool ok = false;
+    int iterations = 0;
+    double resid = bmax;
+    if (rho == 0 || rho != rho) {
+        ok = false;
+    } else {
+        launch_copy_zs(c, p, s);
+        launch_set_rho(p, s);
+        int it;
+        for (it = 0; it < x->maxIter; it++) {
+            launch_spmv_dot(c, p, s);
+            launch_update_xr(c, p, s);
+            if ((it + 1) % 25 == 0) launch_true_residual(c, x->phi, x->wu, x->wv, x->ww, dt, p, s);
+            CK(cudaMemcpyAsync(&x->mail->rmaxBits, p.rmaxBits, sizeof(unsigned int), cudaMemcpyDeviceToHost, s));
+            rc = sync(x);
+            if (rc) return rc;
+            float rm;
+            std::memcpy(&rm, &x->mail->rmaxBits, 4);
+            resid = rm;
+            if (resid <= ptol) {
+                iterations = it + 1;
+                ok = true;
+                break;
+            }
+            launch_precondition(c, p, p.r, p.z, lo, hi, s);
+            launch_dot_zr(c, p, s);
+            launch_update_s(c, p, s);
+            launch_set_rho(p, s);
+        }
+        if (!ok) iterations = it;
+    }
+    x->stats.pressure_iterations = iterations;
+    x->stats.pressure_error = resid;
+    bool accept = ok || (iterations == x->maxIter && resid < x->accTol);
+    launch_pressure_to_float(c, p, s);
+    if (d && d->pressure) {
+        rc = sync(x);
+        if (rc) return rc;
+        CK(cudaMemcpy(d->pressure, p.pressure, x->nc() * sizeof(float), cudaMemcpyDeviceToHost));
+    }
+    if (!accept) return FLIP_E_SOLVER_NOCONV;
+    launch_apply_pressure(c, x->phi, x->wu, x->wv, x->ww, p, dt, x->u, x->v, x->w, x->vu, x->vv, x->vw, s);
+    *applied = true;
+    return FLIP_OK;
+}
+
+int dump_mac(flip_ctx *x, float *a, float *b, float *e, const float *u, const float *v, const float *w) {
+    if (!a) return FLIP_OK;
+    int rc = sync(x);
+    if (rc) return rc;
+    CK(cudaMemcpy(a, u, x->nu() * 4, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(b, v, x->nv() * 4, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(e, w, x->nw() * 4, cudaMemcpyDeviceToHost));
+    return FLIP_OK;
+}
+
+// _stepFluid (fluidsimulation.cpp:5471-5508)
+int step_fluid(flip_ctx *x, double dt, flip_stage_dump *d) {
+    cudaStream_t s = x->stream;
+    StepConsts &c = x->c;
+    int rc;
+    if (d && d->n_before) *d->n_before = x->n;
+    if (!x->solidBuilt && x->n > 0) {
+        if ((rc = build_solid(x))) return rc;
+    }
+    int layers = (int)std::ceil(x->cfl) + 2;
+    x->mark(FLIP_STAGE_LIQUID_SDF);
+    // liquid level set (particlelevelset.cpp:161-196)
+    if (x->n > 0 && x->solidBuilt) {
+        launch_liquid_sdf(x->pa, x->cellStart, c, x->solidCC, x->phi, s);
+    } else {
+        std::vector<float> fill(x->nc(), (float)(3.0 * x->dx));
+        float eps = (float)(0.005 * x->dx);
+        for (auto &f : fill) if (std::abs(f) < eps) f = f > 0 ? eps : -eps;
+        CK(cudaMemcpyAsync(x->phi, fill.data(), fill.size() * 4, cudaMemcpyHostToDevice, s));
+        CK(cudaStreamSynchronize(s));
+    }
+    if (d && d->phi) {
+        if ((rc = sync(x))) return rc;
+        CK(cudaMemcpy(d->phi, x->phi, x->nc() * 4, cudaMemcpyDeviceToHost));
+    }
+    // advect velocity field: P2G + extrapolation (fluidsimulation.cpp:3253-3285)
+    x->mark(FLIP_STAGE_P2G);
+    if (x->n > 0) {
+        launch_p2g(x->pa, x->cellStart, c, x->u, x->v, x->w, x->vu, x->vv, x->vw, s);
+        if (d && d->vu_p2g) {
+            if ((rc = sync(x))) return rc;
+            CK(cudaMemcpy(d->vu_p2g, x->vu, x->nu(), cudaMemcpyDeviceToHost));
+            CK(cudaMemcpy(d->vv_p2g, x->vv, x->nv(), cudaMemcpyDeviceToHost));
+            CK(cudaMemcpy(d->vw_p2g, x->vw, x->nw(), cudaMemcpyDeviceToHost));
+        }
+        launch_extrapolate(c, x->u, x->v, x->w, x->vu, x->vv, x->vw, x->status, layers, s);
+    } else {
+        CK(cudaMemsetAsync(x->u, 0, x->nu() * 4, s));
+        CK(cudaMemsetAsync(x->v, 0, x->nv() * 4, s));
+        CK(cudaMemsetAsync(x->w, 0, x->nw() * 4, s));
+        CK(cudaMemsetAsync(x->vu, 0, x->nu(), s));
+        CK(cudaMemsetAsync(x->vv, 0, x->nv(), s));
+        CK(cudaMemsetAsync(x->vw, 0, x->nw(), s));
+    }
+    if (d && (rc = dump_mac(x, d->u_p2g, d->v_p2g, d->w_p2g, x->u, x->v, x->w))) return rc;
+    // save + constant body force (fluidsimulation.cpp:3287-3297, 3450-3489)
+    x->mark(FLIP_STAGE_FORCE);
+    float3 bf = body_force(x);
+    const float feps = 1e-6f;
+    launch_save_and_force(c, x->u, x->v, x->w, x->su, x->sv, x->sw, (float)(bf.x * dt), (float)(bf.y * dt),
+                          (float)(bf.z * dt), std::fabs(bf.x) > feps, std::fabs(bf.y) > feps, std::fabs(bf.z) > feps, s);
+    if (d && (rc = dump_mac(x, d->u_force, d->v_force, d->w_force, x->u, x->v, x->w))) return rc;
+    // pressure (fluidsimulation.cpp:3732-3773)
+    if (!x->solidBuilt) {
+        if ((rc = build_solid(x))) return rc;
+    }
+    bool applied = false;
+    x->mark(FLIP_STAGE_PRESSURE);
+    rc = pressure_solve(x, dt, &applied, d);
+    if (rc != FLIP_OK && rc != FLIP_E_SOLVER_NOCONV) return rc;
+    x->stats.pressure_status = rc;
+    if (d && d->pcg_iters) *d->pcg_iters = x->stats.pressure_iterations;
+    if (d && d->pcg_error) *d->pcg_error = x->stats.pressure_error;
+    x->mark(FLIP_STAGE_CONSTRAIN);
+    launch_extrapolate(c, x->u, x->v, x->w, x->vu, x->vv, x->vw, x->status, layers, s);
+    if (d && (rc = dump_mac(x, d->u_press, d->v_press, d->w_press, x->u, x->v, x->w))) return rc;
+    // constrain saved and current fields (fluidsimulation.cpp:3937-3950)
+    launch_constrain(c, x->u, x->v, x->w, x->su, x->sv, x->sw, x->wu, x->wv, x->ww, s);
+    if (d && (rc = dump_mac(x, d->u_final, d->v_final, d->w_final, x->u, x->v, x->w))) return rc;
+    if (d && (rc = dump_mac(x, d->u_saved, d->v_saved, d->w_saved, x->su, x->sv, x->sw))) return rc;
+    if (x->n == 0) {
+        x->mark(FLIP_STAGE_ADVECT);
+        x->mark(FLIP_STAGE_BINNING);
+        x->mark(FLIP_NUM_STAGES);
+        return collect_stage_times(x);
+    }
+    // particle velocities, advection, removal (fluidsimulation.cpp:4172-4390)
+    x->mark(FLIP_STAGE_ADVECT);
+    double speedStep = x->cfl * x->dx / x->frameDt;
+    CK(cudaMemsetAsync(x->speedHist, 0, 8 * sizeof(unsigned int), s));
+    launch_advect(x->pa, x->n, c, x->u, x->v, x->w, x->su, x->sv, x->sw, x->solidPhi, x->nearSolid,
+                  (float)x->picRatio, (float)(1 - x->picRatio), dt, x->keys, x->speedHist, speedStep, s);
+    if (d && (d->vel_g2p || d->pos_adv)) {
+        std::vector<float> pos, vel;
+        if ((rc = particles_in_order(x, &pos, &vel))) return rc;
+        if (d->vel_g2p) std::memcpy(d->vel_g2p, vel.data(), vel.size() * 4);
+        if (d->pos_adv) std::memcpy(d->pos_adv, pos.data(), pos.size() * 4);
+    }
+    launch_speed_limit(x->speedHist, x->n, x->maxFrameSteps, speedStep, x->maxRemovePct, x->maxRemoveAbs,
+                       x->maxSpeedSq, s);
+    launch_mark_fast(x->pa, x->n, x->maxSpeedSq, x->keys, s);
+    x->mark(FLIP_STAGE_BINNING);
+    rc = rebin_marked(x);
+    if (rc) return rc;
+    return collect_stage_times(x);
+}
+
+// _calculateNextTimeStep (fluidsimulation.cpp:5593-5613)
+double next_time_step(flip_ctx *x, double dt) {
+    double maxu;
+    if (x->frame == 0 && x->stepNumber == 0) {
+        float3 bf = body_force(x);
+        float len = std::sqrt(bf.x * bf.x + bf.y * bf.y + bf.z * bf.z);
+        maxu = 0.0 + len * dt;
+    } else {
+        maxu = x->maxSpeed;
+    }
+    maxu = std::fmax(0.0, maxu);
+    return x->cfl * x->dx / (maxu + 1e-6);
+}
+
+int do_update(flip_ctx *x, double dt, flip_stage_dump *d) {
+    if (!x->initialized) return fail(FLIP_E_RUNTIME, "Error: FluidSimulation must be initialized before update.");
+    if (dt < 0.0) return fail(FLIP_E_DOMAIN, "Error: delta time must be greater than or equal to 0.");
+    double epsdt = 1e-6;
+    bool zeroLength = dt < epsdt;
+    dt = std::max(dt, epsdt);
+    x->frameDt = dt;
+    x->frameRemaining = dt;
+    x->stepNumber = 0;
+    bool skipped = zeroLength && x->outputInitialized;
+    double substep = dt / (double)x->minFrameSteps;
+    double eps = 1e-9;
+    int worst = FLIP_OK;
+    do {
+        double step = std::fmin(next_time_step(x, dt), x->frameRemaining);
+        if (d && step < dt) return fail(FLIP_E_RUNTIME, "staged update: the frame needs more than one substep");
+        double done = x->frameDt - x->frameRemaining;
+        double limit = (x->stepNumber + 1) * substep;
+        if (done + step > limit) step = std::fmin(substep, x->frameRemaining);
+        if (x->stepNumber == x->maxFrameSteps - 1) step = x->frameRemaining;
+        x->frameRemaining -= step;
+        if (!skipped) {
+            int rc = step_fluid(x, step, d);
+            if (rc == FLIP_E_SOLVER_NOCONV) worst = rc;
+            else if (rc != FLIP_OK) return rc;
+            if (x->stats.pressure_status == FLIP_E_SOLVER_NOCONV) worst = FLIP_E_SOLVER_NOCONV;
+        }
+        d = nullptr;
+        x->stepNumber++;
+    } while (x->frameRemaining > eps);
+    x->stats.frame = x->frame;
+    x->stats.substeps = x->stepNumber;
+    x->stats.delta_time = dt;
+    x->stats.fluid_particles = x->n;
+    x->stats.pressure_status = worst;
+    x->outputInitialized = true;
+    x->frame++;
+    return FLIP_OK;
+}
+
+int do_initialize(flip_ctx *x) {
+    if (x->initialized) return FLIP_OK;
+    cudaStream_t s = x->stream;
+    int rc;
+    // _loadMarkerParticles (fluidsimulation.cpp:2773-2786): keep points in
+    // [0, I dx) x [0, J dx) x [0, K dx)
+    std::vector<float> hp, hv;
+    if (x->queueDevN > 0) {
+        hp.resize(3 * (size_t)x->queueDevN);
+        hv.resize(3 * (size_t)x->queueDevN);
+        CK(cudaMemcpy(hp.data(), x->queueDevPos, hp.size() * 4, cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(hv.data(), x->queueDevVel, hv.size() * 4, cudaMemcpyDeviceToHost));
+    }
+    hp.insert(hp.begin(), x->queuePos.begin(), x->queuePos.end());
+    hv.insert(hv.begin(), x->queueVel.begin(), x->queueVel.end());
+    double W = x->I * x->dx, H = x->J * x->dx, D = x->K * x->dx;
+    int total = (int)(hp.size() / 3);
+    std::vector<float> sx, sy, sz, svx, svy, svz;
+    for (int q = 0; q < total; q++) {
+        float a = hp[3 * q] * 1.0f, b = hp[3 * q + 1] * 1.0f, e = hp[3 * q + 2] * 1.0f;
+        if (a >= 0.0f && b >= 0.0f && e >= 0.0f && a < 0.0 + W && b < 0.0 + H && e < 0.0 + D) {
+            sx.push_back(a); sy.push_back(b); sz.push_back(e);
+            svx.push_back(hv[3 * q]); svy.push_back(hv[3 * q + 1]); svz.push_back(hv[3 * q + 2]);
+        }
+    }
+    x->queuePos.clear(); x->queueVel.clear(); x->queueDevN = 0;
+    x->n = (int)sx.size();
+    if ((rc = alloc_particles(x, std::max(x->n, 1)))) return rc;
+    if (x->n > 0) {
+        std::vector<unsigned int> ids(x->n);
+        for (int q = 0; q < x->n; q++) ids[q] = (unsigned int)q;
+        CK(cudaMemcpyAsync(x->pa.px, sx.data(), x->n * 4, cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(x->pa.py, sy.data(), x->n * 4, cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(x->pa.pz, sz.data(), x->n * 4, cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(x->pa.vx, svx.data(), x->n * 4, cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(x->pa.vy, svy.data(), x->n * 4, cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(x->pa.vz, svz.data(), x->n * 4, cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(x->pa.id, ids.data(), x->n * 4, cudaMemcpyHostToDevice, s));
+        launch_keys_from_positions(x->pa, x->n, x->c, x->keys, s);
+        int saveMax = x->maxPerCell;
+        x->maxPerCell = 0x7fffffff;          // loading keeps every particle
+        rc = rebin(x);
+        x->maxPerCell = saveMax;
+        if (rc) return rc;
+    } else {
+        CK(cudaMemsetAsync(x->cellStart, 0, (x->nc() + 1) * sizeof(int), s));
+    }
+    x->initialized = true;
+    return sync(x);
+}
+
+}  // namespace
+
+// ====================================================================== C ABI
+extern "C" {
+
+const char *flip_last_error(void) { return g_err.c_str(); }
+
+int flip_create(int isize, int jsize, int ksize, double dx, flip_ctx **out) {
+    if (!out) return fail(FLIP_E_NULL, "null output pointer");
+    *out = nullptr;
+    if (isize <= 0 || jsize <= 0 || ksize <= 0 || !(dx > 0.0))
+        return fail(FLIP_E_DOMAIN, "Error: dimensions and cell size must be greater than 0.");
+    if ((long long)isize * jsize * ksize >= (1LL << 28))
+        return fail(FLIP_E_DOMAIN, "grid too large for 28-bit cell keys");
+    int ndev = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess || ndev == 0)
+        return fail(FLIP_E_CUDA, std::string("no CUDA device: ") + cudaGetErrorString(e));
+    flip_ctx *x = new flip_ctx();
+    x->I = isize; x->J = jsize; x->K = ksize; x->dx = dx;
+    cudaGetDevice(&x->device);
+    if (cudaStreamCreateWithFlags(&x->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        delete x;
+        return fail(FLIP_E_CUDA, "cudaStreamCreate failed");
+    }
+    x->ownStream = true;
+    if (cudaMallocHost((void **)&x->mail, sizeof(flip_ctx::Mail)) != cudaSuccess) {
+        cudaStreamDestroy(x->stream);
+        delete x;
+        return fail(FLIP_E_NOMEM, "cudaMallocHost failed");
+    }
+    StepConsts &c = x->c;
+    c.I = isize; c.J = jsize; c.K = ksize;
+    c.dx = dx; c.invdx = 1.0 / dx; c.invdxf = (float)(1.0 / dx); c.dxf = (float)dx;
+    c.radius = 0.5 * 1.0 * dx * std::sqrt(3.0);
+    c.cfl = x->cfl;
+    c.maxPerCell = x->maxPerCell;
+    int rc = alloc_grids(x);
+    if (rc) {
+        flip_destroy(x);
+        return rc;
+    }
+    x->launchesAtCreate = launch_counter();
+    *out = x;
+    return FLIP_OK;
+}
+
+int flip_destroy(flip_ctx *x) {
+    if (!x) return FLIP_E_NULL;
+    cudaStreamSynchronize(x->stream);
+    for (int q = 0; q <= FLIP_NUM_STAGES; q++)
+        if (x->ev[q]) cudaEventDestroy(x->ev[q]);
+    for (void *p : x->allocations) cudaFree(p);
+    if (x->mail) cudaFreeHost(x->mail);
+    if (x->ownStream) cudaStreamDestroy(x->stream);
+    delete x;
+    return FLIP_OK;
+}
+
+int flip_set_stream(flip_ctx *x, void *stream) {
+    if (!x) return FLIP_E_NULL;
+    cudaStreamSynchronize(x->stream);
+    if (stream) {
+        if (x->ownStream) cudaStreamDestroy(x->stream);
+        x->stream = (cudaStream_t)stream;
+        x->ownStream = false;
+    }
+    return FLIP_OK;
+}
+
+int flip_set_pic_flip_ratio(flip_ctx *x, double r) {
+    if (!x) return FLIP_E_NULL;
+    if (r < 0.0 || r > 1.0) return fail(FLIP_E_DOMAIN, "Error: PICFLIP ratio must be in range [0.0, 1.0].");
+    x->picRatio = r;
+    return FLIP_OK;
+}
+int flip_get_pic_flip_ratio(flip_ctx *x, double *r) {
+    if (!x || !r) return FLIP_E_NULL;
+    *r = x->picRatio;
+    return FLIP_OK;
+}
+int flip_add_body_force(flip_ctx *x, double fx, double fy, double fz) {
+    if (!x) return FLIP_E_NULL;
+    x->bodyForces.push_back((float)fx);
+    x->bodyForces.push_back((float)fy);
+    x->bodyForces.push_back((float)fz);
+    return FLIP_OK;
+}
+int flip_reset_body_force(flip_ctx *x) {
+    if (!x) return FLIP_E_NULL;
+    x->bodyForces.clear();
+    return FLIP_OK;
+}
+int flip_set_cfl_condition_number(flip_ctx *x, int n) {
+    if (!x) return FLIP_E_NULL;
+    if (n < 1) return fail(FLIP_E_DOMAIN, "Error: CFL must be greater than or equal to 1.");
+    if (x->solidBuilt) return fail(FLIP_E_RUNTIME, "CFL number is fixed once the simulation has stepped");
+    x->cfl = n;
+    x->c.cfl = n;
+    return FLIP_OK;
+}
+int flip_set_pressure_tolerance(flip_ctx *x, double tol) {
+    if (!x) return FLIP_E_NULL;
+    if (!(tol > 0.0)) return fail(FLIP_E_DOMAIN, "tolerance must be positive");
+    x->tol = tol;
+    return FLIP_OK;
+}
+int flip_set_max_pressure_iterations(flip_ctx *x, int n) {
+    if (!x) return FLIP_E_NULL;
+    if (n < 1) return fail(FLIP_E_DOMAIN, "iterations must be positive");
+    x->maxIter = n;
+    return FLIP_OK;
+}
+int flip_load_marker_particle_data(flip_ctx *x, int n, const float *pos, const float *vel) {
+    if (!x) return FLIP_E_NULL;
+    if (n < 0) return fail(FLIP_E_DOMAIN, "negative particle count");
+    if (n == 0) return FLIP_OK;
+    if (!pos || !vel) return FLIP_E_NULL;
+    if (x->initialized) return fail(FLIP_E_RUNTIME, "particles are loaded before initialize()");
+    x->queuePos.insert(x->queuePos.end(), pos, pos + 3 * (size_t)n);
+    x->queueVel.insert(x->queueVel.end(), vel, vel + 3 * (size_t)n);
+    return FLIP_OK;
+}
+int flip_load_marker_particle_data_device(flip_ctx *x, int n, const float *dpos, const float *dvel) {
+    if (!x) return FLIP_E_NULL;
+    if (n < 0) return fail(FLIP_E_DOMAIN, "negative particle count");
+    if (n == 0) return FLIP_OK;
+    if (!dpos || !dvel) return FLIP_E_NULL;
+    if (x->initialized) return fail(FLIP_E_RUNTIME, "particles are loaded before initialize()");
+    if (x->queueDevN) return fail(FLIP_E_RUNTIME, "one device particle load per simulation");
+    x->queueDevPos = dpos; x->queueDevVel = dvel; x->queueDevN = n;
+    return FLIP_OK;
+}
+int flip_initialize(flip_ctx *x) {
+    if (!x) return FLIP_E_NULL;
+    return do_initialize(x);
+}
+int flip_is_initialized(flip_ctx *x, int *yes) {
+    if (!x || !yes) return FLIP_E_NULL;
+    *yes = x->initialized ? 1 : 0;
+    return FLIP_OK;
+}
+int flip_update(flip_ctx *x, double dt) {
+    if (!x) return FLIP_E_NULL;
+    return do_update(x, dt, nullptr);
+}
+int flip_update_staged(flip_ctx *x, double dt, flip_stage_dump *d) {
+    if (!x || !d) return FLIP_E_NULL;
+    return do_update(x, dt, d);
+}
+int flip_get_num_marker_particles(flip_ctx *x, int *n) {
+    if (!x || !n) return FLIP_E_NULL;
+    *n = x->n;
+    return FLIP_OK;
+}
+int flip_get_marker_particle_position_data(flip_ctx *x, float *out) {
+    if (!x || !out) return FLIP_E_NULL;
+    std::vector<float> pos;
+    int rc = particles_in_order(x, &pos, nullptr);
+    if (rc) return rc;
+    std::memcpy(out, pos.data(), pos.size() * 4);
+    return FLIP_OK;
+}
+int flip_get_marker_particle_velocity_data(flip_ctx *x, float *out) {
+    if (!x || !out) return FLIP_E_NULL;
+    std::vector<float> vel;
+    int rc = particles_in_order(x, nullptr, &vel);
+    if (rc) return rc;
+    std::memcpy(out, vel.data(), vel.size() * 4);
+    return FLIP_OK;
+}
+static int range_get(flip_ctx *x, int start, int end, float *out, bool vel) {
+    if (!x || !out) return FLIP_E_NULL;
+    if (start < 0 || end > x->n || start > end) return fail(FLIP_E_DOMAIN, "Error: invalid range.");
+    std::vector<float> a;
+    int rc = vel ? particles_in_order(x, nullptr, &a) : particles_in_order(x, &a, nullptr);
+    if (rc) return rc;
+    std::memcpy(out, a.data() + 3 * (size_t)start, 3 * (size_t)(end - start) * 4);
+    return FLIP_OK;
+}
+int flip_get_marker_particle_position_data_range(flip_ctx *x, int start, int end, float *out) {
+    return range_get(x, start, end, out, false);
+}
+int flip_get_marker_particle_velocity_data_range(flip_ctx *x, int start, int end, float *out) {
+    return range_get(x, start, end, out, true);
+}
+int flip_get_marker_particle_data_device(flip_ctx *x, float *dpos, float *dvel) {
+    if (!x) return FLIP_E_NULL;
+    cudaStream_t s = x->stream;
+    int n = x->n;
+    if (dpos) {
+        CK(cudaMemcpyAsync(dpos, x->pa.px, n * 4, cudaMemcpyDeviceToDevice, s));
+        CK(cudaMemcpyAsync(dpos + n, x->pa.py, n * 4, cudaMemcpyDeviceToDevice, s));
+        CK(cudaMemcpyAsync(dpos + 2 * (size_t)n, x->pa.pz, n * 4, cudaMemcpyDeviceToDevice, s));
+    }
+    if (dvel) {
+        CK(cudaMemcpyAsync(dvel, x->pa.vx, n * 4, cudaMemcpyDeviceToDevice, s));
+        CK(cudaMemcpyAsync(dvel + n, x->pa.vy, n * 4, cudaMemcpyDeviceToDevice, s));
+        CK(cudaMemcpyAsync(dvel + 2 * (size_t)n, x->pa.vz, n * 4, cudaMemcpyDeviceToDevice, s));
+    }
+    return FLIP_OK;
+}
+int flip_get_frame_stats(flip_ctx *x, flip_frame_stats *out) {
+    if (!x || !out) return FLIP_E_NULL;
+    *out = x->stats;
+    return FLIP_OK;
+}
+int flip_get_current_frame(flip_ctx *x, int *frame) {
+    if (!x || !frame) return FLIP_E_NULL;
+    *frame = x->frame;
+    return FLIP_OK;
+}
+int flip_get_liquid_sdf(flip_ctx *x, float *phi) {
+    if (!x || !phi) return FLIP_E_NULL;
+    int rc = sync(x);
+    if (rc) return rc;
+    CK(cudaMemcpy(phi, x->phi, x->nc() * 4, cudaMemcpyDeviceToHost));
+    return FLIP_OK;
+}
+int flip_get_solid_sdf(flip_ctx *x, float *nodal) {
+    if (!x || !nodal) return FLIP_E_NULL;
+    if (!x->solidBuilt) {
+        int rc = build_solid(x);
+        if (rc) return rc;
+    }
+    std::memcpy(nodal, x->box.nodal.data(), x->box.nodal.size() * 4);
+    return FLIP_OK;
+}
+int flip_get_mac_velocity(flip_ctx *x, float *u, float *v, float *w) {
+    if (!x || !u || !v || !w) return FLIP_E_NULL;
+    return dump_mac(x, u, v, w, x->u, x->v, x->w);
+}
+int flip_get_face_weights(flip_ctx *x, float *wu, float *wv, float *ww) {
+    if (!x || !wu || !wv || !ww) return FLIP_E_NULL;
+    if (!x->solidBuilt) {
+        int rc = build_solid(x);
+        if (rc) return rc;
+    }
+    std::memcpy(wu, x->box.wu.data(), x->box.wu.size() * 4);
+    std::memcpy(wv, x->box.wv.data(), x->box.wv.size() * 4);
+    std::memcpy(ww, x->box.ww.data(), x->box.ww.size() * 4);
+    return FLIP_OK;
+}
+int flip_compute_domain_solid(int isize, int jsize, int ksize, double dx, int cfl, float *nodal, float *wu,
+                              float *wv, float *ww, int *nearDims, uint8_t *nearOut) {
+    if (isize <= 0 || jsize <= 0 || ksize <= 0 || !(dx > 0.0) || cfl < 1)
+        return fail(FLIP_E_DOMAIN, "bad grid or CFL number");
+    DomainBox b;
+    b.compute(isize, jsize, ksize, dx, cfl);
+    if (nodal) std::memcpy(nodal, b.nodal.data(), b.nodal.size() * 4);
+    if (wu) std::memcpy(wu, b.wu.data(), b.wu.size() * 4);
+    if (wv) std::memcpy(wv, b.wv.data(), b.wv.size() * 4);
+    if (ww) std::memcpy(ww, b.ww.data(), b.ww.size() * 4);
+    if (nearDims) { nearDims[0] = b.nsi; nearDims[1] = b.nsj; nearDims[2] = b.nsk; }
+    if (nearOut) std::memcpy(nearOut, b.near.data(), b.near.size());
+    return FLIP_OK;
+}
+
+int flip_set_stage_timing(flip_ctx *x, int enable) {
+    if (!x) return FLIP_E_NULL;
+    CK(cudaStreamSynchronize(x->stream));
+    if (enable && !x->ev[0]) {
+        for (int q = 0; q <= FLIP_NUM_STAGES; q++) CK(cudaEventCreate(&x->ev[q]));
+    }
+    x->timing = enable != 0;
+    for (int q = 0; q < FLIP_NUM_STAGES; q++) x->stageMs[q] = 0.0;
+    x->timedSubsteps = 0;
+    return FLIP_OK;
+}
+
+int flip_get_stage_times(flip_ctx *x, double *ms, long long *substeps) {
+    if (!x || !ms) return FLIP_E_NULL;
+    for (int q = 0; q < FLIP_NUM_STAGES; q++) ms[q] = x->stageMs[q];
+    if (substeps) *substeps = x->timedSubsteps;
+    return FLIP_OK;
+}
+
+int flip_get_launch_count(flip_ctx *x, long long *count) {
+    if (!x || !count) return FLIP_E_NULL;
+    *count = launch_counter() - x->launchesAtCreate;
+    return FLIP_OK;
+}
+
+}  // extern "C"

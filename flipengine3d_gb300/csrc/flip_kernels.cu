@@ -1,0 +1,741 @@
+// FLIP step kernels for GB300 (sm_103a): particle binning, liquid SDF, P2G,
+// extrapolation, body force, constrain, and the fused PIC/FLIP + RK3 +
+// collision particle update.  Every kernel is an HBM-bound gather/stencil;
+// nothing here is a dense contraction, so no tensor cores are involved.
+#include <cstdio>
+
+#include "flip_kernels.cuh"
+
+namespace flip {
+
+namespace {
+
+constexpr int TPB = 256;
+
+struct F3 { float x, y, z; };
+__device__ __forceinline__ F3 f3(float x, float y, float z) { F3 r; r.x = x; r.y = y; r.z = z; return r; }
+__device__ __forceinline__ F3 add(F3 a, F3 b) { return f3(__fadd_rn(a.x, b.x), __fadd_rn(a.y, b.y), __fadd_rn(a.z, b.z)); }
+__device__ __forceinline__ F3 sub(F3 a, F3 b) { return f3(__fsub_rn(a.x, b.x), __fsub_rn(a.y, b.y), __fsub_rn(a.z, b.z)); }
+__device__ __forceinline__ F3 mul(float s, F3 v) { return f3(__fmul_rn(v.x, s), __fmul_rn(v.y, s), __fmul_rn(v.z, s)); }
+__device__ __forceinline__ float dot3(F3 a, F3 b) {
+    return __fadd_rn(__fadd_rn(__fmul_rn(a.x, b.x), __fmul_rn(a.y, b.y)), __fmul_rn(a.z, b.z));
+}
+__device__ __forceinline__ float len3(F3 a) { return __fsqrt_rn(dot3(a, a)); }
+// vmath operator/ : multiply by (float)(1.0 / s)  (src/engine/vmath.cpp:100-103)
+__device__ __forceinline__ F3 normalize3(F3 v) {
+    float inv = (float)(1.0 / (double)len3(v));
+    return mul(inv, v);
+}
+
+// ------------------------------------------------------------------ binning
+__global__ void k_keys(ParticleSoA p, int n, StepConsts c, unsigned int *keys) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    int i = exact_floor(p.px[t], c.invdx, c.invdxf);
+    int j = exact_floor(p.py[t], c.invdx, c.invdxf);
+    int k = exact_floor(p.pz[t], c.invdx, c.invdxf);
+    Dims d{c.I, c.J, c.K};
+    keys[t] = d.in(i, j, k) ? (unsigned int)d.idx(i, j, k) : KEY_SOLID;
+}
+
+__global__ void k_bin_count(const unsigned int *keys, int n, int *count) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    unsigned int k = keys[t];
+    if (k & KEY_SOLID) return;
+    atomicAdd(&count[k & KEY_CELL_MASK], 1);
+}
+
+// Exclusive scan of n ints: 4096 per block, then the block totals.
+constexpr int SCAN_T = 1024, SCAN_PER = 4, SCAN_TILE = SCAN_T * SCAN_PER;
+
+__device__ int block_scan_excl(int v, int *sh, int *total) {
+    int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) sh[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        int w = (lane < (int)(blockDim.x >> 5)) ? sh[lane] : 0;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            int y = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane >= o) w += y;
+        }
+        sh[lane] = w;
+    }
+    __syncthreads();
+    int base = warp > 0 ? sh[warp - 1] : 0;
+    if (total) *total = sh[(blockDim.x >> 5) - 1];
+    int r = base + x - v;
+    __syncthreads();
+    return r;
+}
+
+__global__ void k_scan_tiles(const int *in, int n, int *out, int *tileSums) {
+    __shared__ int sh[32];
+    long long base = (long long)blockIdx.x * SCAN_TILE + threadIdx.x * SCAN_PER;
+    int v[SCAN_PER];
+    int sum = 0;
+#pragma unroll
+    for (int q = 0; q < SCAN_PER; q++) {
+        long long g = base + q;
+        v[q] = g < n ? in[g] : 0;
+        sum += v[q];
+    }
+    int total;
+    int ex = block_scan_excl(sum, sh, &total);
+#pragma unroll
+    for (int q = 0; q < SCAN_PER; q++) {
+        long long g = base + q;
+        if (g < n) out[g] = ex;
+        ex += v[q];
+    }
+    if (threadIdx.x == 0) tileSums[blockIdx.x] = total;
+}
+
+__global__ void k_scan_sums(int *tileSums, int ntiles, int *grandTotal) {
+    __shared__ int sh[32];
+    int v[SCAN_PER];
+    int sum = 0;
+#pragma unroll
+    for (int q = 0; q < SCAN_PER; q++) {
+        int g = threadIdx.x * SCAN_PER + q;
+        v[q] = g < ntiles ? tileSums[g] : 0;
+        sum += v[q];
+    }
+    int total;
+    int ex = block_scan_excl(sum, sh, &total);
+#pragma unroll
+    for (int q = 0; q < SCAN_PER; q++) {
+        int g = threadIdx.x * SCAN_PER + q;
+        if (g < ntiles) tileSums[g] = ex;
+        ex += v[q];
+    }
+    if (threadIdx.x == 0) *grandTotal = total;
+}
+
+__global__ void k_scan_add(int *out, int n, const int *tileSums, const int *grandTotal) {
+    long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (g < n) out[g] += tileSums[g / SCAN_TILE];
+    if (g == n) out[n] = *grandTotal;
+}
+
+__global__ void k_bin_scatter(const unsigned int *keys, int n, const int *start, int *cursor, int *slots) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    unsigned int k = keys[t];
+    if (k & KEY_SOLID) return;
+    int c = (int)(k & KEY_CELL_MASK);
+    int pos = start[c] + atomicAdd(&cursor[c], 1);
+    slots[pos] = t;
+}
+
+// Per cell: order the slots by particle id (the reference's order), then
+// apply the 250-per-cell limit (first by id) and the extreme-speed removal,
+// as _removeMarkerParticles does (src/engine/fluidsimulation.cpp:4324-4353).
+// Kept slots are compacted to the front of the cell's segment.
+__global__ void k_cell_sort_select(const int *start, int ncells, int *slots, const unsigned int *ids,
+                                   const unsigned int *keys, int maxPerCell, int *survivors) {
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= ncells) return;
+    int b = start[c], e = start[c + 1];
+    for (int a = b + 1; a < e; a++) {
+        int s = slots[a];
+        unsigned int key = ids[s];
+        int q = a - 1;
+        while (q >= b && ids[slots[q]] > key) {
+            slots[q + 1] = slots[q];
+            q--;
+        }
+        slots[q + 1] = s;
+    }
+    int kept = 0;
+    for (int a = b; a < e; a++) {
+        int s = slots[a];
+        int rank = a - b;
+        if (rank >= maxPerCell) continue;
+        if (keys[s] & KEY_FAST) continue;
+        slots[b + kept] = s;
+        kept++;
+    }
+    survivors[c] = kept;
+}
+
+__global__ void k_gather(ParticleSoA src, ParticleSoA dst, const int *start, const int *slots,
+                         const int *newStart, int ncells, unsigned int *maxSpeedSqBits) {
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    float best = 0.0f;
+    if (c < ncells) {
+        int b = start[c];
+        int o = newStart[c], e = newStart[c + 1];
+        for (int q = 0; q < e - o; q++) {
+            int s = slots[b + q];
+            float vx = src.vx[s], vy = src.vy[s], vz = src.vz[s];
+            dst.px[o + q] = src.px[s];
+            dst.py[o + q] = src.py[s];
+            dst.pz[o + q] = src.pz[s];
+            dst.vx[o + q] = vx;
+            dst.vy[o + q] = vy;
+            dst.vz[o + q] = vz;
+            dst.id[o + q] = src.id[s];
+            float sq = __fadd_rn(__fadd_rn(__fmul_rn(vx, vx), __fmul_rn(vy, vy)), __fmul_rn(vz, vz));
+            best = fmaxf(best, sq);
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) best = fmaxf(best, __shfl_xor_sync(0xffffffffu, best, o));
+    if ((threadIdx.x & 31) == 0 && best > 0.0f) atomicMax(maxSpeedSqBits, __float_as_uint(best));
+}
+
+// --------------------------------------------------------------- liquid SDF
+// One CTA per 10^3-cell block of the reference (particlelevelset.h:140-142):
+// every particle whose search box reaches the block updates the block's
+// cells with min(|c - p| - r) in the block's own float frame
+// (particlelevelset.cpp:582-629).  Min is order-free, so the result is
+// bit-identical to the reference.  Then the solid post-process
+// (particlelevelset.cpp:172-196).
+constexpr int BW = 10;
+
+// Does the reference's count pass put particle p in block (bx,by,bz)'s list?
+// (particlelevelset.cpp:477-532, velocityadvector.cpp:272-329)
+__device__ __forceinline__ bool in_block_list(float px, float py, float pz, float sr, float blockdxf,
+                                              double invBlock, int bx, int by, int bz) {
+    int ci = (int)floor((double)px * invBlock), cj = (int)floor((double)py * invBlock),
+        ck = (int)floor((double)pz * invBlock);
+    float bpx = (float)((double)(float)ci * (double)blockdxf);
+    float bpy = (float)((double)(float)cj * (double)blockdxf);
+    float bpz = (float)((double)(float)ck * (double)blockdxf);
+    if (__fsub_rn(px, sr) > bpx && __fsub_rn(py, sr) > bpy && __fsub_rn(pz, sr) > bpz &&
+        __fadd_rn(px, sr) < __fadd_rn(bpx, blockdxf) && __fadd_rn(py, sr) < __fadd_rn(bpy, blockdxf) &&
+        __fadd_rn(pz, sr) < __fadd_rn(bpz, blockdxf)) {
+        return ci == bx && cj == by && ck == bz;
+    }
+    int i0 = (int)floor((double)__fsub_rn(px, sr) * invBlock), i1 = (int)floor((double)__fadd_rn(px, sr) * invBlock);
+    int j0 = (int)floor((double)__fsub_rn(py, sr) * invBlock), j1 = (int)floor((double)__fadd_rn(py, sr) * invBlock);
+    int k0 = (int)floor((double)__fsub_rn(pz, sr) * invBlock), k1 = (int)floor((double)__fadd_rn(pz, sr) * invBlock);
+    return bx >= i0 && bx <= i1 && by >= j0 && by <= j1 && bz >= k0 && bz <= k1;
+}
+
+__global__ void __launch_bounds__(TPB) k_liquid_sdf(ParticleSoA p, const int *cellStart, StepConsts c,
+                                                    const uint8_t *solidCC, float *phi) {
+    __shared__ unsigned int smin[BW * BW * BW];
+    __shared__ float centre[BW];
+    const int bx = blockIdx.x, by = blockIdx.y, bz = blockIdx.z;
+    const double dx = c.dx;
+    const float maxd = (float)(3.0 * dx);
+    for (int q = threadIdx.x; q < BW * BW * BW; q += blockDim.x) smin[q] = f2ord(maxd);
+    if (threadIdx.x < BW) centre[threadIdx.x] = cell_centre(threadIdx.x, dx);
+    __syncthreads();
+
+    const float r = (float)c.radius;
+    const float sr = __fmul_rn(2.0f, r);
+    const float blockdxf = (float)(BW * dx);
+    const double invBlock = 1.0 / (double)blockdxf;
+    const double blockdxD = (double)BW * dx;
+    const float offx = (float)((double)(float)bx * blockdxD), offy = (float)((double)(float)by * blockdxD),
+                offz = (float)((double)(float)bz * blockdxD);
+    Dims cells{c.I, c.J, c.K};
+    int x0 = max(bx * BW - 2, 0), x1 = min(bx * BW + BW + 1, c.I - 1);
+    int y0 = max(by * BW - 2, 0), y1 = min(by * BW + BW + 1, c.J - 1);
+    int z0 = max(bz * BW - 2, 0), z1 = min(bz * BW + BW + 1, c.K - 1);
+    int ny = y1 - y0 + 1, nrows = ny * (z1 - z0 + 1);
+    int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
+    for (int row = warp; row < nrows; row += nwarps) {
+        int cy = y0 + row % ny, cz = z0 + row / ny;
+        int pb = cellStart[cells.idx(x0, cy, cz)], pe = cellStart[cells.idx(x1, cy, cz) + 1];
+        for (int t = pb + lane; t < pe; t += 32) {
+            float px = p.px[t], py = p.py[t], pz = p.pz[t];
+            if (!in_block_list(px, py, pz, sr, blockdxf, invBlock, bx, by, bz)) continue;
+            float lx = __fsub_rn(px, offx), ly = __fsub_rn(py, offy), lz = __fsub_rn(pz, offz);
+            int a0 = max((int)floor((double)__fsub_rn(lx, sr) * c.invdx), 0);
+            int b0 = max((int)floor((double)__fsub_rn(ly, sr) * c.invdx), 0);
+            int c0 = max((int)floor((double)__fsub_rn(lz, sr) * c.invdx), 0);
+            int a1 = min((int)floor((double)__fadd_rn(lx, sr) * c.invdx), BW - 1);
+            int b1 = min((int)floor((double)__fadd_rn(ly, sr) * c.invdx), BW - 1);
+            int c1 = min((int)floor((double)__fadd_rn(lz, sr) * c.invdx), BW - 1);
+            for (int cc = c0; cc <= c1; cc++) {
+                float dz = __fsub_rn(centre[cc], lz);
+                for (int bb = b0; bb <= b1; bb++) {
+                    float dy = __fsub_rn(centre[bb], ly);
+                    for (int aa = a0; aa <= a1; aa++) {
+                        float ddx = __fsub_rn(centre[aa], lx);
+                        float d2 = __fadd_rn(__fadd_rn(__fmul_rn(ddx, ddx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+                        float dist = __fsub_rn(__fsqrt_rn(d2), r);
+                        atomicMin(&smin[aa + BW * (bb + BW * cc)], f2ord(dist));
+                    }
+                }
+            }
+        }
+    }
+    __syncthreads();
+    const float eps = (float)(0.005 * dx);
+    const double half = 0.5 * dx;
+    const float neg = (float)(-0.5f * dx);
+    for (int q = threadIdx.x; q < BW * BW * BW; q += blockDim.x) {
+        int a = q % BW, b = (q / BW) % BW, cz = q / (BW * BW);
+        int gi = bx * BW + a, gj = by * BW + b, gk = bz * BW + cz;
+        if (!cells.in(gi, gj, gk)) continue;
+        long long ci = cells.idx(gi, gj, gk);
+        float val = ord2f(smin[q]);
+        if ((double)val < half && solidCC[ci]) val = neg;
+        if (fabsf(val) < eps) val = val > 0 ? eps : -eps;
+        phi[ci] = val;
+    }
+}
+
+// ---------------------------------------------------------------------- P2G
+// Gather form of VelocityAdvector (velocityadvector.cpp:38-459): one thread
+// per face; candidate particles come from the 18 cells that can hold a
+// particle within r of the face; each particle's weight is evaluated in the
+// reference's 10^3-block frame.  Sums run in a fixed (cell, id) order, so
+// the result is deterministic (no float atomics).
+__global__ void __launch_bounds__(TPB) k_p2g(ParticleSoA p, const int *cellStart, StepConsts c, int dir,
+                                             float *G, uint8_t *valid) {
+    const int ni = c.I + (dir == 0), nj = c.J + (dir == 1), nk = c.K + (dir == 2);
+    long long f = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= (long long)ni * nj * nk) return;
+    int fi = (int)(f % ni), fj = (int)((f / ni) % nj), fk = (int)(f / ((long long)ni * nj));
+    const double dx = c.dx;
+    const float r = (float)c.radius;
+    const float rsq = __fmul_rn(r, r);
+    const float sr = (float)(c.radius + (double)1e-6f);
+    const float r2 = rsq, r4 = __fmul_rn(r2, r2), r6 = __fmul_rn(r4, r2);
+    // same expression trees as the reference's coefficient set-up
+    const float coef1 = __fmul_rn(4.0f / 9.0f, __fdiv_rn(1.0f, __fmul_rn(__fmul_rn(__fmul_rn(__fmul_rn(__fmul_rn(r, r), r), r), r), r)));
+    const float coef2 = __fmul_rn(17.0f / 9.0f, __fdiv_rn(1.0f, __fmul_rn(__fmul_rn(__fmul_rn(r, r), r), r)));
+    const float coef3 = __fmul_rn(22.0f / 9.0f, __fdiv_rn(1.0f, __fmul_rn(r, r)));
+    (void)r4; (void)r6;
+    const float halfdx = (float)(0.5 * dx);
+    const float ox = dir == 0 ? 0.0f : halfdx, oy = dir == 1 ? 0.0f : halfdx, oz = dir == 2 ? 0.0f : halfdx;
+    const float blockdxf = (float)(dx * BW);
+    const double invBlock = 1.0 / (double)blockdxf;
+    const int bx = fi / BW, by = fj / BW, bz = fk / BW;
+    const double blockdxD = (double)BW * dx;
+    const float offx = (float)((double)(float)bx * blockdxD), offy = (float)((double)(float)by * blockdxD),
+                offz = (float)((double)(float)bz * blockdxD);
+    const int la = fi - bx * BW, lb = fj - by * BW, lc = fk - bz * BW;
+    const float gx = idx_to_pos(la, dx), gy = idx_to_pos(lb, dx), gz = idx_to_pos(lc, dx);
+    // candidate cells of the cell grid
+    int cx0 = dir == 0 ? fi - 1 : fi - 1, cx1 = dir == 0 ? fi : fi + 1;
+    int cy0 = fj - 1, cy1 = dir == 1 ? fj : fj + 1;
+    int cz0 = fk - 1, cz1 = dir == 2 ? fk : fk + 1;
+    cx0 = max(cx0, 0); cy0 = max(cy0, 0); cz0 = max(cz0, 0);
+    cx1 = min(cx1, c.I - 1); cy1 = min(cy1, c.J - 1); cz1 = min(cz1, c.K - 1);
+    Dims cells{c.I, c.J, c.K};
+    float sc = 0.0f, wt = 0.0f;
+    for (int cz = cz0; cz <= cz1; cz++)
+        for (int cy = cy0; cy <= cy1; cy++) {
+            int pb = cellStart[cells.idx(cx0, cy, cz)], pe = cellStart[cells.idx(cx1, cy, cz) + 1];
+            for (int t = pb; t < pe; t++) {
+                float px = __fsub_rn(p.px[t], ox), py = __fsub_rn(p.py[t], oy), pz = __fsub_rn(p.pz[t], oz);
+                float lx = __fsub_rn(px, offx), ly = __fsub_rn(py, offy), lz = __fsub_rn(pz, offz);
+                float ddx = __fsub_rn(gx, lx), ddy = __fsub_rn(gy, ly), ddz = __fsub_rn(gz, lz);
+                float d2 = __fadd_rn(__fadd_rn(__fmul_rn(ddx, ddx), __fmul_rn(ddy, ddy)), __fmul_rn(ddz, ddz));
+                if (!(d2 < rsq)) continue;
+                // the face must lie inside the particle's clamped local box
+                int a0 = (int)floor((double)__fsub_rn(lx, sr) * c.invdx), a1 = (int)floor((double)__fadd_rn(lx, sr) * c.invdx);
+                int b0 = (int)floor((double)__fsub_rn(ly, sr) * c.invdx), b1 = (int)floor((double)__fadd_rn(ly, sr) * c.invdx);
+                int c0 = (int)floor((double)__fsub_rn(lz, sr) * c.invdx), c1 = (int)floor((double)__fadd_rn(lz, sr) * c.invdx);
+                if (la < a0 || la > a1 || lb < b0 || lb > b1 || lc < c0 || lc > c1) continue;
+                if (!in_block_list(px, py, pz, sr, blockdxf, invBlock, bx, by, bz)) continue;
+                float vel = dir == 0 ? p.vx[t] : dir == 1 ? p.vy[t] : p.vz[t];
+                float w3 = __fmul_rn(__fmul_rn(__fmul_rn(coef1, d2), d2), d2);
+                float w2 = __fmul_rn(__fmul_rn(coef2, d2), d2);
+                float w1 = __fmul_rn(coef3, d2);
+                float wgt = __fsub_rn(__fadd_rn(__fsub_rn(1.0f, w3), w2), w1);
+                sc = __fadd_rn(sc, __fmul_rn(wgt, vel));
+                wt = __fadd_rn(wt, wgt);
+            }
+        }
+    const float eps = 1e-6f;
+    bool ok = wt > eps;
+    if (ok) sc = __fdiv_rn(sc, wt);
+    G[f] = sc;
+    valid[f] = ok ? 1 : 0;
+}
+
+// ------------------------------------------------------------ extrapolation
+// Layered BFS of GridUtils::extrapolateGrid (gridutils.cpp:32-228) done in
+// place, one launch per layer.  Status: 0 = valid input, l+1 = filled by
+// layer l, 254 = grid border (fixed, counts as known), 255 = unknown.
+constexpr uint8_t ST_BORDER = 254, ST_UNKNOWN = 255;
+
+__global__ void k_extrap_init(StepConsts c, const uint8_t *vu, const uint8_t *vv, const uint8_t *vw,
+                              uint8_t *status) {
+    long long nu = (long long)(c.I + 1) * c.J * c.K, nv = (long long)c.I * (c.J + 1) * c.K;
+    long long nw = (long long)c.I * c.J * (c.K + 1);
+    long long f = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= nu + nv + nw) return;
+    int dir = f < nu ? 0 : (f < nu + nv ? 1 : 2);
+    long long l = dir == 0 ? f : (dir == 1 ? f - nu : f - nu - nv);
+    const uint8_t *valid = dir == 0 ? vu : (dir == 1 ? vv : vw);
+    int ni = c.I + (dir == 0), nj = c.J + (dir == 1), nk = c.K + (dir == 2);
+    int i = (int)(l % ni), j = (int)((l / ni) % nj), k = (int)(l / ((long long)ni * nj));
+    uint8_t s;
+    if (i == 0 || j == 0 || k == 0 || i == ni - 1 || j == nj - 1 || k == nk - 1) s = ST_BORDER;
+    else s = valid[l] ? 0 : ST_UNKNOWN;
+    status[f] = s;
+}
+
+__global__ void k_extrap_layer(StepConsts c, float *u, float *v, float *w, uint8_t *status, int layer) {
+    long long nu = (long long)(c.I + 1) * c.J * c.K, nv = (long long)c.I * (c.J + 1) * c.K;
+    long long nw = (long long)c.I * c.J * (c.K + 1);
+    long long f = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= nu + nv + nw) return;
+    if (status[f] != ST_UNKNOWN) return;
+    int dir = f < nu ? 0 : (f < nu + nv ? 1 : 2);
+    long long base = dir == 0 ? 0 : (dir == 1 ? nu : nu + nv);
+    long long l = f - base;
+    float *G = dir == 0 ? u : (dir == 1 ? v : w);
+    int ni = c.I + (dir == 0), nj = c.J + (dir == 1);
+    long long sx = 1, sy = ni, sz = (long long)ni * nj;
+    // unknown cells are never on the border, so all six neighbours exist
+    const long long nb[6] = {l + sx, l - sx, l + sy, l - sy, l + sz, l - sz};
+    bool frontier = false;
+#pragma unroll
+    for (int q = 0; q < 6; q++) frontier |= status[base + nb[q]] == (uint8_t)layer;
+    if (!frontier) return;
+    float sum = 0.0f;
+    int count = 0;
+#pragma unroll
+    for (int q = 0; q < 6; q++) {
+        uint8_t s = status[base + nb[q]];
+        if (s == ST_BORDER || s <= (uint8_t)layer) {
+            sum = __fadd_rn(sum, G[nb[q]]);
+            count++;
+        }
+    }
+    G[l] = __fdiv_rn(sum, (float)count);
+    status[f] = (uint8_t)(layer + 1);
+}
+
+// -------------------------------------------------- save + body force, constrain
+__global__ void k_save_force(long long nu, long long nv, long long nw, float *u, float *v, float *w, float *su,
+                             float *sv, float *sw, float fx, float fy, float fz, int ax, int ay, int az) {
+    long long f = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (f < nu) {
+        float x = u[f]; su[f] = x; if (ax) u[f] = __fadd_rn(x, fx);
+    } else if (f < nu + nv) {
+        long long l = f - nu; float x = v[l]; sv[l] = x; if (ay) v[l] = __fadd_rn(x, fy);
+    } else if (f < nu + nv + nw) {
+        long long l = f - nu - nv; float x = w[l]; sw[l] = x; if (az) w[l] = __fadd_rn(x, fz);
+    }
+}
+
+// Faces with zero fluid weight take the solid velocity, which is zero for the
+// static domain walls; partly solid faces blend with the wall friction (zero
+// for the domain), which leaves them unchanged
+// (src/engine/fluidsimulation.cpp:3884-3950).
+__global__ void k_constrain(long long nu, long long nv, long long nw, float *u, float *v, float *w, float *su,
+                            float *sv, float *sw, const float *wu, const float *wv, const float *ww) {
+    long long f = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (f < nu) {
+        if (wu[f] == 0.0f) { u[f] = 0.0f; su[f] = 0.0f; }
+    } else if (f < nu + nv) {
+        long long l = f - nu;
+        if (wv[l] == 0.0f) { v[l] = 0.0f; sv[l] = 0.0f; }
+    } else if (f < nu + nv + nw) {
+        long long l = f - nu - nv;
+        if (ww[l] == 0.0f) { w[l] = 0.0f; sw[l] = 0.0f; }
+    }
+}
+
+// ---------------------------------------------------------- particle update
+// MAC trilinear sample in FP64, exactly as MACVelocityField::_interpolateLinearU/V/W
+// (macvelocityfield.cpp:519-613) and Interpolation::trilinearInterpolate
+// (interpolation.cpp:61-70).
+__device__ __forceinline__ double trilerp(const double p[8], double x, double y, double z) {
+    return p[0] * (1 - x) * (1 - y) * (1 - z) + p[1] * x * (1 - y) * (1 - z) + p[2] * (1 - x) * y * (1 - z) +
+           p[3] * (1 - x) * (1 - y) * z + p[4] * x * (1 - y) * z + p[5] * (1 - x) * y * z +
+           p[6] * x * y * (1 - z) + p[7] * x * y * z;
+}
+
+__device__ double interp_face(const float *G, int ni, int nj, int nk, int dir, double x, double y, double z,
+                              double dx, double inv) {
+    if (dir != 0) x -= 0.5 * dx;
+    if (dir != 1) y -= 0.5 * dx;
+    if (dir != 2) z -= 0.5 * dx;
+    int i = (int)floor(x * inv), j = (int)floor(y * inv), k = (int)floor(z * inv);
+    double ix = (x - (double)i * dx) * inv, iy = (y - (double)j * dx) * inv, iz = (z - (double)k * dx) * inv;
+    double q[8];
+    const int off[8][3] = {{0, 0, 0}, {1, 0, 0}, {0, 1, 0}, {0, 0, 1}, {1, 0, 1}, {0, 1, 1}, {1, 1, 0}, {1, 1, 1}};
+#pragma unroll
+    for (int t = 0; t < 8; t++) {
+        int a = i + off[t][0], b = j + off[t][1], cc = k + off[t][2];
+        bool in = a >= 0 && b >= 0 && cc >= 0 && a < ni && b < nj && cc < nk;
+        q[t] = in ? (double)__ldg(&G[(long long)a + (long long)ni * ((long long)b + (long long)nj * cc)]) : 0.0;
+    }
+    return trilerp(q, ix, iy, iz);
+}
+
+__device__ F3 eval_vel(const StepConsts &c, const float *u, const float *v, const float *w, F3 p) {
+    double x = p.x, y = p.y, z = p.z;
+    double dx = c.dx;
+    if (!(x >= 0 && y >= 0 && z >= 0 && x < dx * c.I && y < dx * c.J && z < dx * c.K)) return f3(0.0f, 0.0f, 0.0f);
+    return f3((float)interp_face(u, c.I + 1, c.J, c.K, 0, x, y, z, dx, c.invdx),
+              (float)interp_face(v, c.I, c.J + 1, c.K, 1, x, y, z, dx, c.invdx),
+              (float)interp_face(w, c.I, c.J, c.K + 1, 2, x, y, z, dx, c.invdx));
+}
+
+// Interpolation::trilinearInterpolate(vec3, dx, grid) on the nodal solid SDF
+// (interpolation.cpp:72-113): the cell offset is a float difference.
+__device__ float solid_at(const StepConsts &c, const float *S, F3 p) {
+    int i = (int)floor((double)p.x * c.invdx), j = (int)floor((double)p.y * c.invdx), k = (int)floor((double)p.z * c.invdx);
+    double ix = (double)__fsub_rn(p.x, idx_to_pos(i, c.dx)) * c.invdx;
+    double iy = (double)__fsub_rn(p.y, idx_to_pos(j, c.dx)) * c.invdx;
+    double iz = (double)__fsub_rn(p.z, idx_to_pos(k, c.dx)) * c.invdx;
+    int ni = c.I + 1, nj = c.J + 1, nk = c.K + 1;
+    double q[8];
+    const int off[8][3] = {{0, 0, 0}, {1, 0, 0}, {0, 1, 0}, {0, 0, 1}, {1, 0, 1}, {0, 1, 1}, {1, 1, 0}, {1, 1, 1}};
+#pragma unroll
+    for (int t = 0; t < 8; t++) {
+        int a = i + off[t][0], b = j + off[t][1], cc = k + off[t][2];
+        bool in = a >= 0 && b >= 0 && cc >= 0 && a < ni && b < nj && cc < nk;
+        q[t] = in ? (double)__ldg(&S[(long long)a + (long long)ni * ((long long)b + (long long)nj * cc)]) : 0.0;
+    }
+    return (float)trilerp(q, ix, iy, iz);
+}
+
+// Interpolation::trilinearInterpolateGradient (interpolation.cpp:197-258)
+__device__ F3 solid_grad(const StepConsts &c, const float *S, F3 p) {
+    int i = (int)floor((double)p.x * c.invdx), j = (int)floor((double)p.y * c.invdx), k = (int)floor((double)p.z * c.invdx);
+    double ix = (double)__fsub_rn(p.x, idx_to_pos(i, c.dx)) * c.invdx;
+    double iy = (double)__fsub_rn(p.y, idx_to_pos(j, c.dx)) * c.invdx;
+    double iz = (double)__fsub_rn(p.z, idx_to_pos(k, c.dx)) * c.invdx;
+    int ni = c.I + 1, nj = c.J + 1, nk = c.K + 1;
+    auto at = [&](int a, int b, int cc) -> float {
+        a += i; b += j; cc += k;
+        bool in = a >= 0 && b >= 0 && cc >= 0 && a < ni && b < nj && cc < nk;
+        return in ? __ldg(&S[(long long)a + (long long)ni * ((long long)b + (long long)nj * cc)]) : 0.0f;
+    };
+    float v000 = at(0, 0, 0), v100 = at(1, 0, 0), v010 = at(0, 1, 0), v001 = at(0, 0, 1);
+    float v101 = at(1, 0, 1), v011 = at(0, 1, 1), v110 = at(1, 1, 0), v111 = at(1, 1, 1);
+    auto bil = [](double a, double b, double cc, double d, double x, double y) {
+        double l1 = (1 - x) * a + x * b;
+        double l2 = (1 - x) * cc + x * d;
+        return (1 - y) * l1 + y * l2;
+    };
+    float gx = (float)bil(__fsub_rn(v100, v000), __fsub_rn(v110, v010), __fsub_rn(v101, v001), __fsub_rn(v111, v011), iy, iz);
+    float gy = (float)bil(__fsub_rn(v010, v000), __fsub_rn(v110, v100), __fsub_rn(v011, v001), __fsub_rn(v111, v101), ix, iz);
+    float gz = (float)bil(__fsub_rn(v001, v000), __fsub_rn(v101, v100), __fsub_rn(v011, v010), __fsub_rn(v111, v110), ix, iy);
+    return f3(gx, gy, gz);
+}
+
+__device__ __forceinline__ bool box_inside(const StepConsts &c, F3 p) {
+    return p.x >= c.bposx && p.y >= c.bposy && p.z >= c.bposz && (double)p.x < (double)c.bposx + c.bw &&
+           (double)p.y < (double)c.bposy + c.bh && (double)p.z < (double)c.bposz + c.bd;
+}
+// AABB::getNearestPointInsideAABB (aabb.cpp:497-518), eps 1e-6
+__device__ __forceinline__ F3 box_nearest(const StepConsts &c, F3 p) {
+    if (box_inside(c, p)) return p;
+    float mxx = __fadd_rn(c.bposx, (float)c.bw);
+    float mxy = __fadd_rn(c.bposy, (float)c.bh);
+    float mxz = __fadd_rn(c.bposz, (float)c.bd);
+    p.x = fmaxf(p.x, c.bposx); p.y = fmaxf(p.y, c.bposy); p.z = fmaxf(p.z, c.bposz);
+    p.x = (float)fmin((double)p.x, (double)mxx - 1e-6);
+    p.y = (float)fmin((double)p.y, (double)mxy - 1e-6);
+    p.z = (float)fmin((double)p.z, (double)mxz - 1e-6);
+    return p;
+}
+
+__device__ __forceinline__ bool near_solid(const StepConsts &c, const uint8_t *ns, F3 p) {
+    int i = (int)floor((double)p.x * c.invNearCell), j = (int)floor((double)p.y * c.invNearCell),
+        k = (int)floor((double)p.z * c.invNearCell);
+    if (i < 0 || j < 0 || k < 0 || i >= c.nsi || j >= c.nsj || k >= c.nsk) return false;
+    return ns[(long long)i + (long long)c.nsi * ((long long)j + (long long)c.nsj * k)] != 0;
+}
+
+// FluidSimulation::_resolveCollision (src/engine/fluidsimulation.cpp:4221-4296)
+__device__ F3 resolve_collision(const StepConsts &c, const float *S, const uint8_t *ns, F3 oldp, F3 newp) {
+    int gi = (int)floor((double)newp.x * c.invdx), gj = (int)floor((double)newp.y * c.invdx),
+        gk = (int)floor((double)newp.z * c.invdx);
+    if (!(gi >= 0 && gj >= 0 && gk >= 0 && gi < c.I && gj < c.J && gk < c.K)) newp = box_nearest(c, newp);
+    if (!near_solid(c, ns, oldp) && !near_solid(c, ns, newp)) return newp;
+    const float eps = 1e-6f;
+    const float stepDist = __fmul_rn(0.5f, (float)c.dx);
+    float travel = len3(sub(newp, oldp));
+    if (travel < eps) return newp;
+    int nsteps = (int)ceilf(__fdiv_rn(travel, stepDist));
+    F3 dir = normalize3(sub(newp, oldp));
+    F3 last = oldp, cur = oldp;
+    bool found = false;
+    float cphi = 0.0f;
+    for (int s = 0; s < nsteps; s++) {
+        if (s == nsteps - 1) cur = newp;
+        else cur = add(oldp, mul(__fmul_rn((float)(s + 1), stepDist), dir));
+        float ph = solid_at(c, S, cur);
+        if (ph < 0.0f || !box_inside(c, cur)) { cphi = ph; found = true; break; }
+        last = cur;
+    }
+    if (!found) return newp;
+    F3 res;
+    const float maxDist = (float)(c.cfl * c.dx);
+    F3 g = solid_grad(c, S, cur);
+    if (len3(g) > eps) {
+        g = normalize3(g);
+        res = sub(cur, mul((float)((double)cphi - (double)0.1f * c.dx), g));
+        float rphi = solid_at(c, S, res);
+        float rd = len3(sub(res, cur));
+        if (rphi < 0 || rd > maxDist) res = last;
+    } else {
+        res = last;
+    }
+    if (!box_inside(c, res)) {
+        F3 orig = res;
+        res = box_nearest(c, res);
+        float rphi = solid_at(c, S, res);
+        float rd = len3(sub(res, orig));
+        if (rphi < 0.0f || rd > maxDist) res = last;
+    }
+    return res;
+}
+
+// Fused particle update: PIC/FLIP velocity (fluidsimulation.cpp:4082-4092),
+// Ralston RK3 (4191-4198), collision (4221-4296), then the removal tests and
+// the new cell key for the next binning.
+__global__ void __launch_bounds__(TPB) k_advect(ParticleSoA p, int n, StepConsts c, const float *u, const float *v,
+                                                const float *w, const float *su, const float *sv, const float *sw,
+                                                const float *S, const uint8_t *ns, float picRatio, float flipRatio,
+                                                double dt, unsigned int *keys, unsigned int *hist, double speedStep) {
+    __shared__ unsigned int shist[8];
+    if (threadIdx.x < 8) shist[threadIdx.x] = 0;
+    __syncthreads();
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < n) {
+        F3 p0 = f3(p.px[t], p.py[t], p.pz[t]);
+        F3 v0 = f3(p.vx[t], p.vy[t], p.vz[t]);
+        F3 vpic = eval_vel(c, u, v, w, p0);
+        F3 vold = eval_vel(c, su, sv, sw, p0);
+        F3 vflip = sub(add(v0, vpic), vold);
+        F3 vn = add(mul(picRatio, vpic), mul(flipRatio, vflip));
+        F3 k1 = eval_vel(c, u, v, w, p0);
+        F3 k2 = eval_vel(c, u, v, w, add(p0, mul((float)(0.5 * dt), k1)));
+        F3 k3 = eval_vel(c, u, v, w, add(p0, mul((float)(0.75 * dt), k2)));
+        F3 sum = add(add(mul(2.0f, k1), mul(3.0f, k2)), mul(4.0f, k3));
+        F3 p1 = add(p0, mul((float)(dt / 9.0f), sum));
+        p1 = resolve_collision(c, S, ns, p0, p1);
+        p.px[t] = p1.x; p.py[t] = p1.y; p.pz[t] = p1.z;
+        p.vx[t] = vn.x; p.vy[t] = vn.y; p.vz[t] = vn.z;
+        double speed = (double)len3(vn);
+        int bin = (int)fmin(floor(speed / speedStep), 5.0);
+        atomicAdd(&shist[bin], 1u);
+        unsigned int key;
+        if (solid_at(c, S, p1) < 0.0f) {
+            key = KEY_SOLID;
+        } else {
+            int i = (int)floor((double)p1.x * c.invdx), j = (int)floor((double)p1.y * c.invdx),
+                k = (int)floor((double)p1.z * c.invdx);
+            Dims d{c.I, c.J, c.K};
+            key = d.in(i, j, k) ? (unsigned int)d.idx(i, j, k) : KEY_SOLID;
+        }
+        keys[t] = key;
+    }
+    __syncthreads();
+    if (threadIdx.x < 6 && shist[threadIdx.x]) atomicAdd(&hist[threadIdx.x], shist[threadIdx.x]);
+}
+
+// _getMarkerParticleSpeedLimit (fluidsimulation.cpp:4298-4322), one thread
+__global__ void k_speed_limit(const unsigned int *hist, int n, int bins, double step, double maxPct, int maxAbs,
+                              float *maxSpeedSq) {
+    int maxRemoval = (int)fmin((double)(int)((double)n * maxPct), (double)maxAbs);
+    double maxspeed = bins * step;
+    int cur = 0;
+    for (int i = bins - 1; i > 0; i--) {
+        if (cur + (int)hist[i] > maxRemoval) break;
+        cur += (int)hist[i];
+        maxspeed = i * step;
+    }
+    float ms = (float)maxspeed;
+    *maxSpeedSq = __fmul_rn(ms, ms);
+}
+
+__global__ void k_mark_fast(ParticleSoA p, int n, const float *maxSpeedSq, unsigned int *keys) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    unsigned int k = keys[t];
+    if (k & KEY_SOLID) return;
+    F3 v = f3(p.vx[t], p.vy[t], p.vz[t]);
+    if ((double)dot3(v, v) > (double)*maxSpeedSq) keys[t] = k | KEY_FAST;
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ launchers
+void launch_keys_from_positions(const ParticleSoA &p, int n, const StepConsts &c, unsigned int *keys, cudaStream_t s) {
+    if (n > 0) { FLIP_COUNT(1); k_keys<<<div_up(n, TPB), TPB, 0, s>>>(p, n, c, keys); }
+}
+void launch_bin_count(const unsigned int *keys, int n, int *cellCount, cudaStream_t s) {
+    if (n > 0) { FLIP_COUNT(1); k_bin_count<<<div_up(n, TPB), TPB, 0, s>>>(keys, n, cellCount); }
+}
+int scan_scratch_ints(int ncells) { return (int)div_up(ncells + 1, SCAN_TILE) + 2; }
+void launch_scan_cells(const int *count, int ncells, int *start, int *scratch, int *total, cudaStream_t s) {
+    int ntiles = (int)div_up(ncells, SCAN_TILE);
+    { FLIP_COUNT(1); k_scan_tiles<<<ntiles, SCAN_T, 0, s>>>(count, ncells, start, scratch); }
+    { FLIP_COUNT(1); k_scan_sums<<<1, SCAN_T, 0, s>>>(scratch, ntiles, total); }
+    { FLIP_COUNT(1); k_scan_add<<<div_up(ncells + 1, TPB), TPB, 0, s>>>(start, ncells, scratch, total); }
+}
+void launch_bin_scatter(const unsigned int *keys, int n, const int *cellStart, int *cursor, int *slots, cudaStream_t s) {
+    if (n > 0) { FLIP_COUNT(1); k_bin_scatter<<<div_up(n, TPB), TPB, 0, s>>>(keys, n, cellStart, cursor, slots); }
+}
+void launch_cell_sort_select(const int *cellStart, int ncells, int *slots, const unsigned int *ids,
+                             const unsigned int *keys, int maxPerCell, int *survivorCount, cudaStream_t s) {
+    { FLIP_COUNT(1); k_cell_sort_select<<<div_up(ncells, TPB), TPB, 0, s>>>(cellStart, ncells, slots, ids, keys, maxPerCell, survivorCount); }
+}
+void launch_gather_particles(const ParticleSoA &src, ParticleSoA dst, const int *cellStart, const int *slots,
+                             const int *newStart, int ncells, unsigned int *maxSpeedSqBits, cudaStream_t s) {
+    { FLIP_COUNT(1); k_gather<<<div_up(ncells, TPB), TPB, 0, s>>>(src, dst, cellStart, slots, newStart, ncells, maxSpeedSqBits); }
+}
+void launch_liquid_sdf(const ParticleSoA &p, const int *cellStart, const StepConsts &c, const uint8_t *solidCC,
+                       float *phi, cudaStream_t s) {
+    dim3 grid(div_up(c.I, BW), div_up(c.J, BW), div_up(c.K, BW));
+    { FLIP_COUNT(1); k_liquid_sdf<<<grid, TPB, 0, s>>>(p, cellStart, c, solidCC, phi); }
+}
+void launch_p2g(const ParticleSoA &p, const int *cellStart, const StepConsts &c, float *u, float *v, float *w,
+                uint8_t *vu, uint8_t *vv, uint8_t *vw, cudaStream_t s) {
+    long long nu = (long long)(c.I + 1) * c.J * c.K, nv = (long long)c.I * (c.J + 1) * c.K,
+              nw = (long long)c.I * c.J * (c.K + 1);
+    { FLIP_COUNT(1); k_p2g<<<div_up(nu, TPB), TPB, 0, s>>>(p, cellStart, c, 0, u, vu); }
+    { FLIP_COUNT(1); k_p2g<<<div_up(nv, TPB), TPB, 0, s>>>(p, cellStart, c, 1, v, vv); }
+    { FLIP_COUNT(1); k_p2g<<<div_up(nw, TPB), TPB, 0, s>>>(p, cellStart, c, 2, w, vw); }
+}
+void launch_extrapolate(const StepConsts &c, float *u, float *v, float *w, const uint8_t *vu, const uint8_t *vv,
+                        const uint8_t *vw, uint8_t *status, int layers, cudaStream_t s) {
+    long long tot = (long long)(c.I + 1) * c.J * c.K + (long long)c.I * (c.J + 1) * c.K +
+                    (long long)c.I * c.J * (c.K + 1);
+    { FLIP_COUNT(1); k_extrap_init<<<div_up(tot, TPB), TPB, 0, s>>>(c, vu, vv, vw, status); }
+    for (int l = 0; l < layers; l++) { FLIP_COUNT(1); k_extrap_layer<<<div_up(tot, TPB), TPB, 0, s>>>(c, u, v, w, status, l); }
+}
+void launch_save_and_force(const StepConsts &c, float *u, float *v, float *w, float *su, float *sv, float *sw,
+                           float fx, float fy, float fz, bool ax, bool ay, bool az, cudaStream_t s) {
+    long long nu = (long long)(c.I + 1) * c.J * c.K, nv = (long long)c.I * (c.J + 1) * c.K,
+              nw = (long long)c.I * c.J * (c.K + 1);
+    { FLIP_COUNT(1); k_save_force<<<div_up(nu + nv + nw, TPB), TPB, 0, s>>>(nu, nv, nw, u, v, w, su, sv, sw, fx, fy, fz, ax, ay, az); }
+}
+void launch_constrain(const StepConsts &c, float *u, float *v, float *w, float *su, float *sv, float *sw,
+                      const float *wu, const float *wv, const float *ww, cudaStream_t s) {
+    long long nu = (long long)(c.I + 1) * c.J * c.K, nv = (long long)c.I * (c.J + 1) * c.K,
+              nw = (long long)c.I * c.J * (c.K + 1);
+    { FLIP_COUNT(1); k_constrain<<<div_up(nu + nv + nw, TPB), TPB, 0, s>>>(nu, nv, nw, u, v, w, su, sv, sw, wu, wv, ww); }
+}
+void launch_advect(ParticleSoA p, int n, const StepConsts &c, const float *u, const float *v, const float *w,
+                   const float *su, const float *sv, const float *sw, const float *solidPhi,
+                   const uint8_t *nearSolid, float picRatio, float flipRatio, double dt, unsigned int *keys,
+                   unsigned int *speedHist, double speedStep, cudaStream_t s) {
+    if (n <= 0) return;
+    FLIP_COUNT(1);
+    k_advect<<<div_up(n, TPB), TPB, 0, s>>>(p, n, c, u, v, w, su, sv, sw, solidPhi, nearSolid, picRatio,
+                                            flipRatio, dt, keys, speedHist, speedStep);
+}
+void launch_speed_limit(const unsigned int *hist, int n, int bins, double speedStep, double maxPct, int maxAbs,
+                        float *maxSpeedSq, cudaStream_t s) {
+    { FLIP_COUNT(1); k_speed_limit<<<1, 1, 0, s>>>(hist, n, bins, speedStep, maxPct, maxAbs, maxSpeedSq); }
+}
+void launch_mark_fast(const ParticleSoA &p, int n, const float *maxSpeedSq, unsigned int *keys, cudaStream_t s) {
+    if (n > 0) { FLIP_COUNT(1); k_mark_fast<<<div_up(n, TPB), TPB, 0, s>>>(p, n, maxSpeedSq, keys); }
+}
+
+}  // namespace flip

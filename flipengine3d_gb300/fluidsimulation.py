@@ -1,0 +1,354 @@
+"""Python mirror of the reference's FluidSimulation API over the C ABI.
+
+Method names, argument meaning and error behaviour follow
+jklae/FLIPEngine3D src/engine/fluidsimulation.h (FLIP Fluids 1.0.9b):
+`std::runtime_error` becomes RuntimeError, `std::domain_error` ValueError,
+`std::out_of_range` IndexError.  All work runs in libflip3d_gb300.so on the
+GPU; there is no CPU path: without the built library or a CUDA device the
+constructor raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+from . import build as _build
+
+FLIP_OK = 0
+FLIP_E_RUNTIME = -1
+FLIP_E_DOMAIN = -2
+FLIP_E_OUT_OF_RANGE = -3
+FLIP_E_SOLVER_NOCONV = -4
+FLIP_E_DEVICE_TIMEOUT = -5
+FLIP_E_CUDA = -6
+FLIP_E_NOMEM = -7
+FLIP_E_NULL = -8
+
+
+class FlipCudaError(RuntimeError):
+    """A CUDA runtime failure inside the library."""
+
+
+class FrameStats(C.Structure):
+    _fields_ = [("frame", C.c_int), ("substeps", C.c_int), ("delta_time", C.c_double),
+                ("fluid_particles", C.c_int), ("pressure_iterations", C.c_int),
+                ("pressure_error", C.c_double), ("pressure_status", C.c_int), ("pressure_cells", C.c_int)]
+
+
+STAGE_NAMES = ("liquid_sdf", "p2g", "force", "pressure", "constrain", "advect", "binning")
+
+
+class StageDump(C.Structure):
+    _fields_ = [(n, C.c_void_p) for n in (
+        "phi", "u_p2g", "v_p2g", "w_p2g", "vu_p2g", "vv_p2g", "vw_p2g",
+        "u_force", "v_force", "w_force", "pressure", "rhs",
+        "u_press", "v_press", "w_press", "u_final", "v_final", "w_final",
+        "u_saved", "v_saved", "w_saved", "vel_g2p", "pos_adv",
+        "n_before", "pcg_iters", "pcg_error")]
+
+
+_lib = None
+
+# (name, argtypes) of every exported entry point, as declared in include/flip3d.h
+_P, _I, _D = C.c_void_p, C.c_int, C.c_double
+SIGNATURES = {
+    "flip_create": [_I, _I, _I, _D, C.POINTER(C.c_void_p)],
+    "flip_destroy": [_P],
+    "flip_set_stream": [_P, _P],
+    "flip_set_pic_flip_ratio": [_P, _D],
+    "flip_get_pic_flip_ratio": [_P, C.POINTER(C.c_double)],
+    "flip_add_body_force": [_P, _D, _D, _D],
+    "flip_reset_body_force": [_P],
+    "flip_set_cfl_condition_number": [_P, _I],
+    "flip_set_pressure_tolerance": [_P, _D],
+    "flip_set_max_pressure_iterations": [_P, _I],
+    "flip_load_marker_particle_data": [_P, _I, _P, _P],
+    "flip_load_marker_particle_data_device": [_P, _I, _P, _P],
+    "flip_initialize": [_P],
+    "flip_is_initialized": [_P, C.POINTER(C.c_int)],
+    "flip_update": [_P, _D],
+    "flip_update_staged": [_P, _D, C.POINTER(StageDump)],
+    "flip_get_num_marker_particles": [_P, C.POINTER(C.c_int)],
+    "flip_get_marker_particle_position_data": [_P, _P],
+    "flip_get_marker_particle_velocity_data": [_P, _P],
+    "flip_get_marker_particle_position_data_range": [_P, _I, _I, _P],
+    "flip_get_marker_particle_velocity_data_range": [_P, _I, _I, _P],
+    "flip_get_marker_particle_data_device": [_P, _P, _P],
+    "flip_get_frame_stats": [_P, C.POINTER(FrameStats)],
+    "flip_get_current_frame": [_P, C.POINTER(C.c_int)],
+    "flip_get_liquid_sdf": [_P, _P],
+    "flip_get_solid_sdf": [_P, _P],
+    "flip_get_mac_velocity": [_P, _P, _P, _P],
+    "flip_get_face_weights": [_P, _P, _P, _P],
+    "flip_compute_domain_solid": [_I, _I, _I, _D, _I, _P, _P, _P, _P, _P, _P],
+    "flip_set_stage_timing": [_P, _I],
+    "flip_get_stage_times": [_P, _P, C.POINTER(C.c_longlong)],
+    "flip_get_launch_count": [_P, C.POINTER(C.c_longlong)],
+}
+
+
+def load_library(path: str | Path | None = None):
+    """Load libflip3d_gb300.so (built by flipengine3d_gb300.build)."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = Path(path) if path else _build.library_path()
+    if not p.exists():
+        raise FileNotFoundError(f"{p} is missing: run flipengine3d_gb300.build.build_library() "
+                                "(or __graft_entry__.build()) first")
+    lib = C.CDLL(str(p))
+    for name, args in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = C.c_int
+    lib.flip_last_error.argtypes = []
+    lib.flip_last_error.restype = C.c_char_p
+    if path is None:
+        _lib = lib
+    return lib
+
+
+def _check(lib, rc: int):
+    if rc == FLIP_OK:
+        return
+    msg = (lib.flip_last_error() or b"").decode(errors="replace")
+    if rc == FLIP_E_RUNTIME:
+        raise RuntimeError(msg)
+    if rc == FLIP_E_DOMAIN:
+        raise ValueError(msg)
+    if rc == FLIP_E_OUT_OF_RANGE:
+        raise IndexError(msg)
+    if rc == FLIP_E_CUDA or rc == FLIP_E_NOMEM:
+        raise FlipCudaError(msg)
+    raise RuntimeError(f"flip error {rc}: {msg}")
+
+
+def _ptr(a):
+    return None if a is None else C.c_void_p(a.ctypes.data)
+
+
+def compute_domain_solid(isize, jsize, ksize, dx, cfl=5):
+    """Static domain-wall set-up (no device needed): nodal solid SDF, face
+    weights and the coarse near-solid grid, arrays shaped (k, j, i)."""
+    lib = load_library()
+    I, J, K = isize, jsize, ksize
+    nodal = np.zeros((K + 1, J + 1, I + 1), np.float32)
+    wu = np.zeros((K, J, I + 1), np.float32)
+    wv = np.zeros((K, J + 1, I), np.float32)
+    ww = np.zeros((K + 1, J, I), np.float32)
+    dims = np.zeros(3, np.int32)
+    _check(lib, lib.flip_compute_domain_solid(I, J, K, dx, cfl, None, None, None, None, _ptr(dims), None))
+    near = np.zeros((dims[2], dims[1], dims[0]), np.uint8)
+    _check(lib, lib.flip_compute_domain_solid(I, J, K, dx, cfl, _ptr(nodal), _ptr(wu), _ptr(wv), _ptr(ww),
+                                              _ptr(dims), _ptr(near)))
+    return nodal, (wu, wv, ww), near
+
+
+class FluidSimulation:
+    """FluidSimulation(isize, jsize, ksize, dx) on one GB300 (current device)."""
+
+    def __init__(self, isize: int, jsize: int, ksize: int, dx: float):
+        self._lib = load_library()
+        self._h = C.c_void_p()
+        _check(self._lib, self._lib.flip_create(int(isize), int(jsize), int(ksize), float(dx), C.byref(self._h)))
+        self.dims = (int(isize), int(jsize), int(ksize))
+        self.dx = float(dx)
+
+    # -- lifetime
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            self._lib.flip_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _c(self, rc):
+        _check(self._lib, rc)
+
+    # -- reference API
+    def setStream(self, cuda_stream_handle: int):
+        self._c(self._lib.flip_set_stream(self._h, C.c_void_p(int(cuda_stream_handle))))
+
+    def setPICFLIPRatio(self, r: float):
+        self._c(self._lib.flip_set_pic_flip_ratio(self._h, float(r)))
+
+    def getPICFLIPRatio(self) -> float:
+        v = C.c_double()
+        self._c(self._lib.flip_get_pic_flip_ratio(self._h, C.byref(v)))
+        return v.value
+
+    def addBodyForce(self, fx, fy=None, fz=None):
+        if fy is None:
+            fx, fy, fz = fx
+        self._c(self._lib.flip_add_body_force(self._h, float(fx), float(fy), float(fz)))
+
+    def resetBodyForce(self):
+        self._c(self._lib.flip_reset_body_force(self._h))
+
+    def setCFLConditionNumber(self, n: int):
+        self._c(self._lib.flip_set_cfl_condition_number(self._h, int(n)))
+
+    def setPressureSolveTolerance(self, tol: float):
+        self._c(self._lib.flip_set_pressure_tolerance(self._h, float(tol)))
+
+    def setMaxPressureSolveIterations(self, n: int):
+        self._c(self._lib.flip_set_max_pressure_iterations(self._h, int(n)))
+
+    def loadMarkerParticleData(self, positions, velocities):
+        pos = np.ascontiguousarray(positions, dtype=np.float32).reshape(-1, 3)
+        vel = np.ascontiguousarray(velocities, dtype=np.float32).reshape(-1, 3)
+        if pos.shape != vel.shape:
+            raise ValueError("positions and velocities differ in size")
+        self._c(self._lib.flip_load_marker_particle_data(self._h, pos.shape[0], _ptr(pos), _ptr(vel)))
+
+    def loadMarkerParticleDataDevice(self, n: int, d_positions: int, d_velocities: int):
+        self._c(self._lib.flip_load_marker_particle_data_device(self._h, int(n), C.c_void_p(d_positions),
+                                                                C.c_void_p(d_velocities)))
+
+    def initialize(self):
+        self._c(self._lib.flip_initialize(self._h))
+
+    def isInitialized(self) -> bool:
+        v = C.c_int()
+        self._c(self._lib.flip_is_initialized(self._h, C.byref(v)))
+        return bool(v.value)
+
+    def update(self, dt: float):
+        self._c(self._lib.flip_update(self._h, float(dt)))
+
+    def getNumMarkerParticles(self) -> int:
+        v = C.c_int()
+        self._c(self._lib.flip_get_num_marker_particles(self._h, C.byref(v)))
+        return v.value
+
+    def getMarkerParticlePositionData(self) -> np.ndarray:
+        out = np.zeros((self.getNumMarkerParticles(), 3), np.float32)
+        self._c(self._lib.flip_get_marker_particle_position_data(self._h, _ptr(out)))
+        return out
+
+    def getMarkerParticleVelocityData(self) -> np.ndarray:
+        out = np.zeros((self.getNumMarkerParticles(), 3), np.float32)
+        self._c(self._lib.flip_get_marker_particle_velocity_data(self._h, _ptr(out)))
+        return out
+
+    def getMarkerParticlePositionDataRange(self, start: int, end: int) -> np.ndarray:
+        out = np.zeros((max(end - start, 0), 3), np.float32)
+        self._c(self._lib.flip_get_marker_particle_position_data_range(self._h, int(start), int(end), _ptr(out)))
+        return out
+
+    def getMarkerParticleVelocityDataRange(self, start: int, end: int) -> np.ndarray:
+        out = np.zeros((max(end - start, 0), 3), np.float32)
+        self._c(self._lib.flip_get_marker_particle_velocity_data_range(self._h, int(start), int(end), _ptr(out)))
+        return out
+
+    def getMarkerParticleDataDevice(self, d_positions: int, d_velocities: int):
+        self._c(self._lib.flip_get_marker_particle_data_device(self._h, C.c_void_p(d_positions),
+                                                               C.c_void_p(d_velocities)))
+
+    def getCurrentFrame(self) -> int:
+        v = C.c_int()
+        self._c(self._lib.flip_get_current_frame(self._h, C.byref(v)))
+        return v.value
+
+    def getFrameStatsData(self) -> FrameStats:
+        s = FrameStats()
+        self._c(self._lib.flip_get_frame_stats(self._h, C.byref(s)))
+        return s
+
+    def getIsomesh(self):
+        """Surface meshing is outside this library: an empty (vertices, triangles) pair."""
+        return np.zeros((0, 3), np.float32), np.zeros((0, 3), np.int32)
+
+    # -- state readback for tests
+    def liquid_sdf(self) -> np.ndarray:
+        I, J, K = self.dims
+        a = np.zeros((K, J, I), np.float32)
+        self._c(self._lib.flip_get_liquid_sdf(self._h, _ptr(a)))
+        return a
+
+    def solid_sdf(self) -> np.ndarray:
+        I, J, K = self.dims
+        a = np.zeros((K + 1, J + 1, I + 1), np.float32)
+        self._c(self._lib.flip_get_solid_sdf(self._h, _ptr(a)))
+        return a
+
+    def mac_velocity(self):
+        I, J, K = self.dims
+        u = np.zeros((K, J, I + 1), np.float32)
+        v = np.zeros((K, J + 1, I), np.float32)
+        w = np.zeros((K + 1, J, I), np.float32)
+        self._c(self._lib.flip_get_mac_velocity(self._h, _ptr(u), _ptr(v), _ptr(w)))
+        return u, v, w
+
+    def set_stage_timing(self, enable: bool = True):
+        self._c(self._lib.flip_set_stage_timing(self._h, 1 if enable else 0))
+
+    def stage_times(self):
+        """(dict stage -> summed device ms, substeps summed)"""
+        ms = np.zeros(len(STAGE_NAMES), np.float64)
+        n = C.c_longlong()
+        self._c(self._lib.flip_get_stage_times(self._h, _ptr(ms), C.byref(n)))
+        return dict(zip(STAGE_NAMES, ms.tolist())), n.value
+
+    def launch_count(self) -> int:
+        v = C.c_longlong()
+        self._c(self._lib.flip_get_launch_count(self._h, C.byref(v)))
+        return v.value
+
+    def update_staged(self, dt: float) -> dict:
+        """One single-substep frame; returns the state between the stages."""
+        I, J, K = self.dims
+        n = self.getNumMarkerParticles()
+        su, sv, sw = (K, J, I + 1), (K, J + 1, I), (K + 1, J, I)
+        out = {}
+
+        def mk(name, shape, dtype=np.float32):
+            out[name] = np.zeros(shape, dtype)
+            return _ptr(out[name])
+
+        d = StageDump()
+        d.phi = mk("phi", (K, J, I))
+        for stage in ("p2g", "force", "press", "final", "saved"):
+            setattr(d, "u_" + stage, mk("u_" + stage, su))
+            setattr(d, "v_" + stage, mk("v_" + stage, sv))
+            setattr(d, "w_" + stage, mk("w_" + stage, sw))
+        d.vu_p2g = mk("vu_p2g", su, np.uint8)
+        d.vv_p2g = mk("vv_p2g", sv, np.uint8)
+        d.vw_p2g = mk("vw_p2g", sw, np.uint8)
+        d.pressure = mk("pressure", (K, J, I))
+        d.rhs = mk("rhs", (K, J, I), np.float64)
+        d.vel_g2p = mk("vel_g2p", (n, 3))
+        d.pos_adv = mk("pos_adv", (n, 3))
+        d.n_before = mk("n_before", (1,), np.int32)
+        d.pcg_iters = mk("pcg_iters", (1,), np.int32)
+        d.pcg_error = mk("pcg_error", (1,), np.float64)
+        self._c(self._lib.flip_update_staged(self._h, float(dt), C.byref(d)))
+        out["positions"] = self.getMarkerParticlePositionData()
+        out["velocities"] = self.getMarkerParticleVelocityData()
+        return out
+
+    @classmethod
+    def from_scene(cls, scene, tolerance=None):
+        """Set up a seeded scene (flipengine3d_gb300.scenes) the way the
+        reference's headless driver does: PIC ratio, gravity, CFL,
+        tolerance, particles, initialize."""
+        sim = cls(scene.isize, scene.jsize, scene.ksize, scene.dx)
+        sim.setPICFLIPRatio(scene.pic_ratio)
+        sim.addBodyForce(*scene.gravity)
+        sim.setCFLConditionNumber(scene.cfl)
+        sim.setPressureSolveTolerance(scene.tolerance if tolerance is None else tolerance)
+        sim.loadMarkerParticleData(scene.positions, scene.velocities)
+        sim.initialize()
+        return sim

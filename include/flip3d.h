@@ -1,0 +1,184 @@
+/*
+ * flip3d.h -- C ABI of the GB300 FLIP step (libflip3d_gb300.so).
+ *
+ * Drop-in for the hot path of jklae/FLIPEngine3D's C++ class FluidSimulation
+ * (src/engine/fluidsimulation.h:117-1130; the FLIP Fluids engine 1.0.9b):
+ * construct, add body forces, set the PIC/FLIP ratio, load marker particles,
+ * initialize, update(dt), read particles back.  Plain pointers and sizes
+ * only.  Every call returns a status code; the header-only C++ shim in
+ * include/FluidSimulation.hpp turns them back into the reference's
+ * exception types.
+ *
+ * Threading: a context is not re-entrant; calls on one context must not
+ * overlap.  All device work of a context is ordered on one CUDA stream
+ * (its own, or the one given by flip_set_stream).
+ */
+#ifndef FLIP3D_H
+#define FLIP3D_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes.  The first three mirror the exception classes the reference
+ * throws (fluidsimulation.cpp: runtime_error 5756-5759, domain_error
+ * 1891-1896/5761-5765, out_of_range 2058-2063). */
+#define FLIP_OK 0
+#define FLIP_E_RUNTIME (-1)        /* e.g. update() before initialize()          */
+#define FLIP_E_DOMAIN (-2)         /* argument out of its domain                 */
+#define FLIP_E_OUT_OF_RANGE (-3)   /* bad particle index range                   */
+#define FLIP_E_SOLVER_NOCONV (-4)  /* pressure solve failed (reported, not fatal) */
+#define FLIP_E_DEVICE_TIMEOUT (-5) /* a bounded device wait gave up              */
+#define FLIP_E_CUDA (-6)           /* CUDA runtime error (no device, launch...)  */
+#define FLIP_E_NOMEM (-7)          /* device allocation failed                   */
+#define FLIP_E_NULL (-8)           /* null context or pointer                    */
+
+typedef struct flip_ctx flip_ctx;
+
+/* Frame statistics, the part of FluidSimulationFrameStats
+ * (fluidsimulation.h:78-100) the hot path produces. */
+typedef struct flip_frame_stats {
+    int frame;
+    int substeps;
+    double delta_time;
+    int fluid_particles;
+    int pressure_iterations;  /* of the last substep */
+    double pressure_error;    /* |r|inf of the last substep */
+    int pressure_status;      /* FLIP_OK or FLIP_E_SOLVER_NOCONV */
+    int pressure_cells;       /* rows of the last substep's pressure system */
+} flip_frame_stats;
+
+/* Stages of one substep, for flip_get_stage_times. */
+#define FLIP_STAGE_LIQUID_SDF 0   /* liquid level set + solid post-process      */
+#define FLIP_STAGE_P2G 1          /* P2G splat + velocity extrapolation        */
+#define FLIP_STAGE_FORCE 2        /* save field + body force                   */
+#define FLIP_STAGE_PRESSURE 3     /* system build, MIC(0), PCG, pressure apply */
+#define FLIP_STAGE_CONSTRAIN 4    /* extrapolation + constrain                 */
+#define FLIP_STAGE_ADVECT 5       /* PIC/FLIP, RK3, collision, removal tests   */
+#define FLIP_STAGE_BINNING 6      /* counting sort by cell + removal           */
+#define FLIP_NUM_STAGES 7
+
+/* Stage dump of one single-substep frame (test and debug interface); any
+ * pointer may be NULL.  Face grids are (I+1)*J*K, I*(J+1)*K, I*J*(K+1); cell
+ * grids I*J*K; flat index i + ni*(j + nj*k).  Particle arrays are 3*n floats
+ * in the reference's particle order. */
+typedef struct flip_stage_dump {
+    float *phi;
+    float *u_p2g, *v_p2g, *w_p2g;
+    uint8_t *vu_p2g, *vv_p2g, *vw_p2g;
+    float *u_force, *v_force, *w_force;
+    float *pressure;
+    double *rhs;
+    float *u_press, *v_press, *w_press;
+    float *u_final, *v_final, *w_final;
+    float *u_saved, *v_saved, *w_saved;
+    float *vel_g2p;
+    float *pos_adv;
+    int *n_before;
+    int *pcg_iters;
+    double *pcg_error;
+} flip_stage_dump;
+
+/* FluidSimulation(int isize, int jsize, int ksize, double dx)
+ * (fluidsimulation.h:127, fluidsimulation.cpp:49-52).  Binds the current
+ * CUDA device.  FLIP_E_DOMAIN for non-positive sizes. */
+int flip_create(int isize, int jsize, int ksize, double dx, flip_ctx **out);
+int flip_destroy(flip_ctx *ctx);
+
+/* Order the context's device work on an existing cudaStream_t (NULL: the
+ * context's own stream). */
+int flip_set_stream(flip_ctx *ctx, void *cuda_stream);
+
+/* setPICFLIPRatio (fluidsimulation.cpp:1891-1903): r in [0,1] is the PIC
+ * fraction; FLIP blend 0.95 is r = 0.05 (the default). */
+int flip_set_pic_flip_ratio(flip_ctx *ctx, double ratio);
+int flip_get_pic_flip_ratio(flip_ctx *ctx, double *ratio);
+
+/* addBodyForce(double fx, double fy, double fz) (fluidsimulation.cpp:1582-1590) */
+int flip_add_body_force(flip_ctx *ctx, double fx, double fy, double fz);
+/* resetBodyForce (fluidsimulation.cpp:1598-1603) */
+int flip_reset_body_force(flip_ctx *ctx);
+
+/* setCFLConditionNumber (fluidsimulation.h:844) */
+int flip_set_cfl_condition_number(flip_ctx *ctx, int n);
+
+/* Pressure-solve controls.  The reference keeps these private
+ * (fluidsimulation.h:1657-1659: tolerance 1e-9, acceptable 1.0, 1000
+ * iterations); they are exposed here so the workload's tolerance can be set. */
+int flip_set_pressure_tolerance(flip_ctx *ctx, double tol);
+int flip_set_max_pressure_iterations(flip_ctx *ctx, int n);
+
+/* loadMarkerParticleData(FluidSimulationMarkerParticleData)
+ * (fluidsimulation.cpp:2488-2509): n packed xyz float triples each, copied
+ * on the call, applied at flip_initialize (particles outside the domain box
+ * are dropped, fluidsimulation.cpp:2773-2786). */
+int flip_load_marker_particle_data(flip_ctx *ctx, int n, const float *positions, const float *velocities);
+/* Same, from device memory (no host copy). */
+int flip_load_marker_particle_data_device(flip_ctx *ctx, int n, const float *d_positions,
+                                          const float *d_velocities);
+
+/* initialize() (fluidsimulation.cpp:82-88) */
+int flip_initialize(flip_ctx *ctx);
+int flip_is_initialized(flip_ctx *ctx, int *yes);
+
+/* update(double dt) (fluidsimulation.cpp:5755-5845): one frame, split into
+ * 1..6 CFL substeps.  FLIP_E_RUNTIME before initialize, FLIP_E_DOMAIN for
+ * dt < 0.  A failed pressure solve is reported through the frame stats, as
+ * the reference only records it in its status string. */
+int flip_update(flip_ctx *ctx, double dt);
+/* As flip_update for a frame that is exactly one substep, filling the stage
+ * dump (FLIP_E_RUNTIME if the CFL condition would split the frame). */
+int flip_update_staged(flip_ctx *ctx, double dt, flip_stage_dump *dump);
+
+/* getNumMarkerParticles (fluidsimulation.cpp:2050-2052) */
+int flip_get_num_marker_particles(flip_ctx *ctx, int *n);
+/* getMarkerParticlePositionData / VelocityData (fluidsimulation.cpp:2408-2420):
+ * 3*n floats in the reference's particle order. */
+int flip_get_marker_particle_position_data(flip_ctx *ctx, float *out);
+int flip_get_marker_particle_velocity_data(flip_ctx *ctx, float *out);
+/* ...DataRange (fluidsimulation.cpp:2314-2336): FLIP_E_DOMAIN on a bad range. */
+int flip_get_marker_particle_position_data_range(flip_ctx *ctx, int start, int end, float *out);
+int flip_get_marker_particle_velocity_data_range(flip_ctx *ctx, int start, int end, float *out);
+/* Device-side readback (cell order, not the reference's order): positions
+ * and velocities as 3 planes of n floats each. */
+int flip_get_marker_particle_data_device(flip_ctx *ctx, float *d_positions, float *d_velocities);
+
+/* getFrameStatsData (fluidsimulation.cpp:2302-2304), getCurrentFrame (:94-96) */
+int flip_get_frame_stats(flip_ctx *ctx, flip_frame_stats *out);
+int flip_get_current_frame(flip_ctx *ctx, int *frame);
+
+/* Grid state readback for tests (sizes as in flip_stage_dump). */
+int flip_get_liquid_sdf(flip_ctx *ctx, float *phi);
+int flip_get_solid_sdf(flip_ctx *ctx, float *nodal_phi);   /* (I+1)*(J+1)*(K+1) */
+int flip_get_mac_velocity(flip_ctx *ctx, float *u, float *v, float *w);
+int flip_get_face_weights(flip_ctx *ctx, float *wu, float *wv, float *ww);
+
+/* Static wall set-up of initialize()/the first step, without a device: the
+ * domain-box solid level set on the (I+1)*(J+1)*(K+1) nodes, the fluid face
+ * weights and the coarse near-solid grid (dims written to near_dims[3];
+ * `near` may be NULL to query them).  Restates _updateSolidLevelSet /
+ * _updateWeightGrid / _updateNearSolidGrid for the domain walls
+ * (fluidsimulation.cpp:3028-3126, 3690-3730). */
+int flip_compute_domain_solid(int isize, int jsize, int ksize, double dx, int cfl, float *nodal_phi, float *wu,
+                              float *wv, float *ww, int *near_dims, uint8_t *near);
+
+/* Per-stage device time: CUDA events recorded on the context's stream at the
+ * stage boundaries of every substep, summed.  flip_set_stage_timing enables
+ * or disables the events and resets the sums; flip_get_stage_times writes
+ * FLIP_NUM_STAGES milliseconds and the number of substeps summed. */
+int flip_set_stage_timing(flip_ctx *ctx, int enable);
+int flip_get_stage_times(flip_ctx *ctx, double *ms, long long *substeps);
+
+/* Number of this library's kernel launches issued so far on the context. */
+int flip_get_launch_count(flip_ctx *ctx, long long *count);
+
+/* Last error message of the calling thread (static storage). */
+const char *flip_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FLIP3D_H */

@@ -1,0 +1,59 @@
+"""Generate tests/golden/*.npz from the reference engine itself.
+
+Runs jklae/FLIPEngine3D's FluidSimulation (compiled from its sources by
+oracle/build_ref.sh into oracle/_ref/libflipref.so) headless on small seeded
+scenes and stores the state after each stage of the first frame plus the
+particles after later frames.  Inputs are not stored: the scenes are
+regenerated from flipengine3d_gb300.scenes with the recorded arguments.
+
+    python tests/golden/make_golden.py        # needs the reference sources
+"""
+from __future__ import annotations
+
+import json
+import sys
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parents[2]
+sys.path.insert(0, str(ROOT))
+
+from flipengine3d_gb300.scenes import dam_break  # noqa: E402
+from oracle.refsim import RefSimulation  # noqa: E402
+
+OUT = Path(__file__).resolve().parent
+
+# name -> (dam_break kwargs, frames, reduction partitions, pressure tolerance)
+CASES = {
+    "dam16": (dict(n=16, seed=0), 3, 1, 1e-9),
+    "sphere13x17x11": (dict(n=13, jsize=17, ksize=11, dx=1.0 / 13, seed=5, sphere=True, fill=(0.5, 0.5, 0.6)), 3, 1, 1e-9),
+    "dam12_loose": (dict(n=12, seed=2, fill=(0.6, 0.9, 1.0)), 2, 1, 1e-6),
+}
+STAGE_KEYS = ("phi", "vu_p2g", "vv_p2g", "vw_p2g", "u_p2g", "v_p2g", "w_p2g", "pressure", "u_final", "v_final",
+              "w_final", "vel_g2p", "pos_adv")
+
+
+def make(name, kwargs, frames, threads, tol):
+    sc = dam_break(**kwargs)
+    ref = RefSimulation(sc.isize, sc.jsize, sc.ksize, sc.dx, threads=threads).setup(sc, tolerance=tol)
+    st = ref.update_staged(sc.frame_dt)
+    data = {k: st[k] for k in STAGE_KEYS}
+    data["pcg_iters"] = st["pcg_iters"]
+    data["pcg_error"] = st["pcg_error"]
+    data["positions_1"], data["velocities_1"] = st["positions"], st["velocities"]
+    for f in range(2, frames + 1):
+        ref.update(sc.frame_dt)
+    pos, vel = ref.particles()
+    data[f"positions_{frames}"], data[f"velocities_{frames}"] = pos, vel
+    meta = dict(scene=kwargs, frames=frames, threads=threads, tolerance=tol, dt=sc.frame_dt,
+                gravity=list(sc.gravity), pic_ratio=sc.pic_ratio, cfl=sc.cfl,
+                seeded=int(sc.num_particles), source="jklae/FLIPEngine3D src/engine via oracle/build_ref.sh")
+    np.savez_compressed(OUT / f"{name}.npz", meta=np.array(json.dumps(meta)), **data)
+    print(name, "particles", sc.num_particles, "->", pos.shape[0], "iters", int(st["pcg_iters"][0]),
+          f"{(OUT / f'{name}.npz').stat().st_size / 1024:.0f} KB")
+
+
+if __name__ == "__main__":
+    for name, (kw, frames, thr, tol) in CASES.items():
+        make(name, kw, frames, thr, tol)

@@ -1,0 +1,97 @@
+"""GPU parity: the sm_103a library against the reference's outputs.
+
+Bars (the benchmark spec): liquid SDF and cell/face flags bit-exact; face velocities,
+pressure and particle positions within 1e-5 relative (max-abs error over
+max-abs value) after one step.  Checked against the golden fixtures the
+reference engine produced and against the CPU oracle on further scenes.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from conftest import golden_cases, load_golden, rel_err
+from flipengine3d_gb300 import FluidSimulation
+from flipengine3d_gb300.scenes import dam_break
+from oracle import refsim
+
+pytestmark = pytest.mark.gpu
+
+RTOL = 1e-5          # face velocities, pressure, particle positions after one step
+RTOL_MULTI = 1e-4    # after several frames (differences grow through advection)
+FACES = ("u", "v", "w")
+
+
+def check_first_frame(st, ref, label):
+    assert np.array_equal(st["phi"], ref["phi"]), f"{label}: liquid SDF not bit-exact"
+    for f in FACES:
+        assert np.array_equal(st[f"v{f}_p2g"], ref[f"v{f}_p2g"]), f"{label}: P2G valid mask {f} differs"
+        assert rel_err(st[f"{f}_p2g"], ref[f"{f}_p2g"]) <= RTOL, f"{label}: P2G {f}"
+        assert rel_err(st[f"{f}_final"], ref[f"{f}_final"]) <= RTOL, f"{label}: final {f}"
+    assert rel_err(st["pressure"], ref["pressure"]) <= RTOL, f"{label}: pressure {rel_err(st['pressure'], ref['pressure']):.3g}"
+    assert rel_err(st["vel_g2p"], ref["vel_g2p"]) <= RTOL, f"{label}: PIC/FLIP velocities"
+    assert rel_err(st["pos_adv"], ref["pos_adv"]) <= RTOL, f"{label}: advected positions"
+
+
+@pytest.mark.parametrize("case", golden_cases())
+def test_first_frame_matches_reference_golden(gpu, case):
+    meta, g = load_golden(case)
+    sc = dam_break(**meta["scene"])
+    with FluidSimulation.from_scene(sc, tolerance=meta["tolerance"]) as sim:
+        st = sim.update_staged(meta["dt"])
+        check_first_frame(st, g, case)
+        assert st["positions"].shape == g["positions_1"].shape
+        assert rel_err(st["positions"], g["positions_1"]) <= RTOL
+        for _ in range(2, meta["frames"] + 1):
+            sim.update(meta["dt"])
+        f = meta["frames"]
+        pos = sim.getMarkerParticlePositionData()
+        assert pos.shape == g[f"positions_{f}"].shape
+        assert rel_err(pos, g[f"positions_{f}"]) <= RTOL_MULTI
+
+
+@pytest.mark.parametrize("kw", [
+    dict(n=32, seed=1),
+    dict(n=40, seed=2, sphere=True),
+    dict(n=27, jsize=35, ksize=22, dx=1 / 27, seed=3, fill=(0.6, 0.5, 0.9)),
+])
+def test_first_frame_matches_oracle(gpu, kw):
+    sc = dam_break(**kw)
+    orc = refsim.OracleSimulation(sc.isize, sc.jsize, sc.ksize, sc.dx).setup(sc, tolerance=1e-9)
+    ref = orc.update_staged(sc.frame_dt)
+    with FluidSimulation.from_scene(sc, tolerance=1e-9) as sim:
+        st = sim.update_staged(sc.frame_dt)
+        check_first_frame(st, ref, str(kw))
+        assert st["positions"].shape == ref["positions"].shape
+        assert rel_err(st["positions"], ref["positions"]) <= RTOL
+        assert rel_err(st["velocities"], ref["velocities"]) <= RTOL
+        assert abs(int(st["pcg_iters"][0]) - int(ref["pcg_iters"][0])) <= max(5, int(ref["pcg_iters"][0]) // 2)
+
+
+def test_multi_frame_tracks_oracle(gpu):
+    sc = dam_break(24, seed=9, sphere=True)
+    orc = refsim.OracleSimulation(sc.isize, sc.jsize, sc.ksize, sc.dx).setup(sc, tolerance=1e-9)
+    with FluidSimulation.from_scene(sc, tolerance=1e-9) as sim:
+        for f in range(5):
+            sim.update(sc.frame_dt)
+            orc.update(sc.frame_dt)
+            pos = sim.getMarkerParticlePositionData()
+            rpos, _ = orc.particles()
+            assert pos.shape == rpos.shape, f"frame {f}: particle count"
+            assert rel_err(pos, rpos) <= RTOL_MULTI, f"frame {f}"
+            assert np.array_equal(sim.liquid_sdf() < 0, orc.liquid_phi() < 0), f"frame {f}: fluid cells"
+
+
+def test_substepped_frame_matches_oracle(gpu):
+    """A frame long enough for the CFL condition to split it into substeps."""
+    sc = dam_break(20, seed=4, sphere=True)
+    orc = refsim.OracleSimulation(sc.isize, sc.jsize, sc.ksize, sc.dx).setup(sc, tolerance=1e-9)
+    with FluidSimulation.from_scene(sc, tolerance=1e-9) as sim:
+        for dt in (1 / 120, 1 / 15):
+            sim.update(dt)
+            orc.update(dt)
+        assert sim.getFrameStatsData().substeps == orc.L.ref_frame_substeps(orc.h) > 1
+        pos = sim.getMarkerParticlePositionData()
+        rpos, _ = orc.particles()
+        assert pos.shape == rpos.shape
+        assert rel_err(pos, rpos) <= RTOL_MULTI

@@ -1,0 +1,76 @@
+"""The CPU oracle, pinned: against the golden fixtures made by the reference
+engine (always), and against the reference engine itself where its sources
+are present (oracle/_ref built by oracle/build_ref.sh)."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from conftest import golden_cases, load_golden
+from flipengine3d_gb300.scenes import dam_break
+from oracle import refsim
+
+STAGES = ("phi", "vu_p2g", "vv_p2g", "vw_p2g", "u_p2g", "v_p2g", "w_p2g", "pressure", "u_final", "v_final",
+          "w_final", "vel_g2p", "pos_adv")
+
+
+@pytest.mark.parametrize("case", golden_cases())
+def test_oracle_matches_golden_bit_exact(built, case):
+    meta, g = load_golden(case)
+    sc = dam_break(**meta["scene"])
+    orc = refsim.OracleSimulation(sc.isize, sc.jsize, sc.ksize, sc.dx, threads=meta["threads"])
+    orc.setup(sc, tolerance=meta["tolerance"])
+    st = orc.update_staged(meta["dt"])
+    for k in STAGES:
+        assert np.array_equal(st[k], g[k]), f"{case}: stage {k} differs from the reference"
+    assert int(st["pcg_iters"][0]) == int(g["pcg_iters"][0])
+    assert np.array_equal(st["positions"], g["positions_1"])
+    assert np.array_equal(st["velocities"], g["velocities_1"])
+    for _ in range(2, meta["frames"] + 1):
+        orc.update(meta["dt"])
+    pos, vel = orc.particles()
+    f = meta["frames"]
+    assert np.array_equal(pos, g[f"positions_{f}"])
+    assert np.array_equal(vel, g[f"velocities_{f}"])
+
+
+needs_ref = pytest.mark.skipif(not refsim.available("ref"), reason="reference checker (oracle/_ref) not built")
+
+
+@needs_ref
+@pytest.mark.parametrize("kw,threads,frames", [
+    (dict(n=21, seed=11, sphere=True), 1, 3),
+    (dict(n=18, jsize=23, ksize=14, dx=1 / 18, seed=4, fill=(0.7, 0.5, 0.8)), 3, 2),
+])
+def test_oracle_matches_reference_engine(built, kw, threads, frames):
+    sc = dam_break(**kw)
+    a = refsim.RefSimulation(sc.isize, sc.jsize, sc.ksize, sc.dx, threads=threads).setup(sc, tolerance=1e-9)
+    b = refsim.OracleSimulation(sc.isize, sc.jsize, sc.ksize, sc.dx, threads=threads).setup(sc, tolerance=1e-9)
+    A = a.update_staged(sc.frame_dt)
+    B = b.update_staged(sc.frame_dt)
+    for k in STAGES + ("rhs", "positions", "velocities"):
+        assert np.array_equal(A[k], B[k]), k
+    for _ in range(frames - 1):
+        a.update(sc.frame_dt)
+        b.update(sc.frame_dt)
+    pa, va = a.particles()
+    pb, vb = b.particles()
+    assert np.array_equal(pa, pb) and np.array_equal(va, vb)
+    assert np.array_equal(a.solid_phi(), b.solid_phi())
+    assert all(np.array_equal(x, y) for x, y in zip(a.weights()[:3], b.weights()))
+    assert np.array_equal(a.near_solid(), b.near_solid())
+
+
+@needs_ref
+def test_oracle_matches_reference_empty_and_outside(built):
+    """No particles inside the domain: both load nothing and step quietly."""
+    n = 10
+    sc = dam_break(n, seed=0)
+    sc.positions = (sc.positions + 5.0).astype(np.float32)      # all outside the domain box
+    a = refsim.RefSimulation(n, n, n, sc.dx).setup(sc)
+    b = refsim.OracleSimulation(n, n, n, sc.dx).setup(sc)
+    for _ in range(2):
+        a.update(sc.frame_dt)
+        b.update(sc.frame_dt)
+    assert a.particles()[0].shape[0] == 0 and b.particles()[0].shape[0] == 0
+    assert np.array_equal(a.liquid_phi(), b.liquid_phi())
