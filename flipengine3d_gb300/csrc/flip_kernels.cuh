@@ -96,8 +96,11 @@ void launch_update_xr(const StepConsts &c, PressureBuffers &pb, cudaStream_t s);
 void launch_init_residual(const StepConsts &c, PressureBuffers &pb, cudaStream_t s);  // r = b, |r|inf
 void launch_set_rho(PressureBuffers &pb, cudaStream_t s);                             // scal[3] = scal[1]
 void launch_copy_zs(const StepConsts &c, PressureBuffers &pb, cudaStream_t s);        // s = z
+// out = b - A x with FP64 rows (x FP64), |out|inf into *rmaxOut
 void launch_true_residual(const StepConsts &c, const float *phi, const float *wu, const float *wv,
-                          const float *ww, double dt, PressureBuffers &pb, cudaStream_t s);
+                          const float *ww, double dt, PressureBuffers &pb, float *out, unsigned int *rmaxOut,
+                          cudaStream_t s);
+void launch_copy_qr(const StepConsts &c, PressureBuffers &pb, cudaStream_t s);        // r = q
 void launch_update_s(const StepConsts &c, PressureBuffers &pb, cudaStream_t s);       // beta = scal[1]/scal[3]
 void launch_pressure_to_float(const StepConsts &c, PressureBuffers &pb, cudaStream_t s);
 void launch_apply_pressure(const StepConsts &c, const float *phi, const float *wu, const float *wv,

@@ -457,12 +457,18 @@ void launch_copy_zs(const StepConsts &c, PressureBuffers &pb, cudaStream_t s) {
     { FLIP_COUNT(1); k_copy_float<<<div_up(n, TPB), TPB, 0, s>>>(n, pb.z, pb.s); }
 }
 
+void launch_copy_qr(const StepConsts &c, PressureBuffers &pb, cudaStream_t s) {
+    long long n = (long long)c.I * c.J * c.K;
+    { FLIP_COUNT(1); k_copy_float<<<div_up(n, TPB), TPB, 0, s>>>(n, pb.q, pb.r); }
+}
+
 void launch_true_residual(const StepConsts &c, const float *phi, const float *wu, const float *wv,
-                          const float *ww, double dt, PressureBuffers &pb, cudaStream_t s) {
+                          const float *ww, double dt, PressureBuffers &pb, float *out, unsigned int *rmaxOut,
+                          cudaStream_t s) {
     long long n = (long long)c.I * c.J * c.K;
     double mf = dt / (c.dx * c.dx);
-    cudaMemsetAsync(pb.rmaxBits, 0, sizeof(unsigned int), s);
-    { FLIP_COUNT(1); k_true_residual<<<div_up(n, TPB), TPB, 0, s>>>(c, phi, pb.fluid, wu, wv, ww, mf, pb.b, pb.x, pb.r, pb.rmaxBits); }
+    cudaMemsetAsync(rmaxOut, 0, sizeof(unsigned int), s);
+    { FLIP_COUNT(1); k_true_residual<<<div_up(n, TPB), TPB, 0, s>>>(c, phi, pb.fluid, wu, wv, ww, mf, pb.b, pb.x, out, rmaxOut); }
 }
 
 void launch_update_s(const StepConsts &c, PressureBuffers &pb, cudaStream_t s) {

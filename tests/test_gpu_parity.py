@@ -87,7 +87,7 @@ def test_substepped_frame_matches_oracle(gpu):
     sc = dam_break(20, seed=4, sphere=True)
     orc = refsim.OracleSimulation(sc.isize, sc.jsize, sc.ksize, sc.dx).setup(sc, tolerance=1e-9)
     with FluidSimulation.from_scene(sc, tolerance=1e-9) as sim:
-        for dt in (1 / 120, 1 / 15):
+        for dt in (1 / 120, 0.4):
             sim.update(dt)
             orc.update(dt)
         assert sim.getFrameStatsData().substeps == orc.L.ref_frame_substeps(orc.h) > 1
