@@ -69,7 +69,10 @@ def build_library(force: bool = False, verbose: bool = False) -> Path:
         for r in ex.map(_run, jobs):
             if verbose and r.stderr:
                 print(r.stderr)
-    objs = sorted(str(p) for p in objdir.glob("*.o"))
+    wanted = {objdir / (src.stem + ".o") for src in list(CSRC.glob("*.cu")) + list(CSRC.glob("*.cpp"))}
+    for stale in set(objdir.glob("*.o")) - wanted:   # objects of removed sources
+        stale.unlink()
+    objs = sorted(str(p) for p in wanted)
     out = library_path()
     if force or jobs or not out.exists():
         _run([nvcc, *ARCH, "-shared", "-o", str(out), *objs, "-lcudart"])

@@ -29,13 +29,16 @@ struct Dims {
 // floor((double)p * inv) without FP64 in the common case: the float product
 // is within 1.3e-7 relative of the exact one, so away from integer
 // boundaries its floor is the exact floor; near them fall back to FP64.
+// Kept out of line so the compiler cannot if-convert it into every call.
+static __device__ __noinline__ int floor_fp64(float p, double inv) { return (int)floor((double)p * inv); }
+
 __device__ __forceinline__ int exact_floor(float p, double inv, float invf) {
     float q = __fmul_rn(p, invf);
     float fq = floorf(q);
     float frac = __fsub_rn(q, fq);
     float tolf = 1e-3f + 4e-7f * fabsf(q);
     if (frac > tolf && frac < 1.0f - tolf) return (int)fq;
-    return (int)floor((double)p * inv);
+    return floor_fp64(p, inv);
 }
 
 __device__ __forceinline__ float idx_to_pos(int i, double dx) { return (float)((double)(float)i * dx); }

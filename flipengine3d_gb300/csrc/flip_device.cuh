@@ -1,0 +1,135 @@
+// Launch interface of the FLIP step kernels (host side of the CUDA code).
+#pragma once
+#include <cstdint>
+#include <string>
+#include <cuda_runtime.h>
+
+#include "flip_common.cuh"
+
+namespace flip {
+
+// Particles, structure of arrays, kept sorted by cell (ascending id inside a
+// cell).  `id` is the particle's rank in the reference's load order, which
+// the reference preserves through every removal.
+struct ParticleSoA {
+    float *px, *py, *pz, *vx, *vy, *vz;
+    unsigned int *id;
+};
+
+struct StepConsts {
+    int I, J, K;
+    double dx, invdx;
+    float invdxf;
+    float dxf;
+    float gxmax, gymax, gzmax;   // largest float coordinate with (double)x < I dx (J dx, K dx)
+    double radius;               // liquid SDF / P2G particle radius, 0.5*sqrt(3)*dx
+    double cfl;
+    int maxPerCell;
+    // near-solid coarse grid
+    int nsi, nsj, nsk;
+    double nearCell, invNearCell;
+    float invNearCellf;
+    // collision boundary AABB (domain inset, then the solid buffer)
+    float bposx, bposy, bposz;
+    double bw, bh, bd;
+    // position tables (device): node n at (float)((double)(float)n * dx);
+    // 10-cell block n at (float)((double)(float)n * 10 dx) and at
+    // (float)((double)(float)n * (double)(float)(10 dx)), index n + 1
+    const float *nodePos;
+    const float *blockPos;
+    const float *blockPosF;
+};
+
+// -- binning (flip_kernels.cu)
+void launch_keys_from_positions(const ParticleSoA &p, int n, const StepConsts &c, unsigned int *keys, cudaStream_t s);
+void launch_bin_count(const unsigned int *keys, int n, int *cellCount, cudaStream_t s);
+void launch_scan_cells(const int *count, int ncells, int *start, int *blockSums, int *total, cudaStream_t s);
+int scan_scratch_ints(int ncells);
+void launch_bin_scatter(const unsigned int *keys, int n, const int *cellStart, int *cursor, int *slots, cudaStream_t s);
+void launch_cell_sort_select(const int *cellStart, int ncells, int *slots, const unsigned int *ids,
+                             const unsigned int *keys, int maxPerCell, int *survivorCount, cudaStream_t s);
+void launch_gather_particles(const ParticleSoA &src, ParticleSoA dst, const int *cellStart, const int *slots,
+                             const int *newStart, int ncells, unsigned int *maxSpeedSqBits, cudaStream_t s);
+
+// -- grid stages
+void launch_liquid_sdf(const ParticleSoA &p, const int *cellStart, const StepConsts &c, const uint8_t *solidCC,
+                       float *phi, cudaStream_t s);
+void launch_p2g(const ParticleSoA &p, const int *cellStart, const StepConsts &c, float *u, float *v, float *w,
+                uint8_t *vu, uint8_t *vv, uint8_t *vw, cudaStream_t s);
+void launch_extrapolate(const StepConsts &c, float *u, float *v, float *w, const uint8_t *vu, const uint8_t *vv,
+                        const uint8_t *vw, uint8_t *status, int layers, cudaStream_t s);
+void launch_save_and_force(const StepConsts &c, float *u, float *v, float *w, float *su, float *sv, float *sw,
+                           float fx, float fy, float fz, bool ax, bool ay, bool az, cudaStream_t s);
+void launch_constrain(const StepConsts &c, float *u, float *v, float *w, float *su, float *sv, float *sw,
+                      const float *wu, const float *wv, const float *ww, cudaStream_t s);
+
+// -- particle update: PIC/FLIP, RK3, collision, removal tests, new keys
+void launch_advect(ParticleSoA p, int n, const StepConsts &c, const float *u, const float *v, const float *w,
+                   const float *su, const float *sv, const float *sw, const float *solidPhi,
+                   const uint8_t *nearSolid, float picRatio, float flipRatio, double dt, unsigned int *keys,
+                   unsigned int *speedHist, double speedStep, cudaStream_t s);
+void launch_speed_limit(const unsigned int *hist, int n, int bins, double speedStep, double maxPct, int maxAbs,
+                        float *maxSpeedSq, cudaStream_t s);
+void launch_mark_fast(const ParticleSoA &p, int n, const float *maxSpeedSq, unsigned int *keys, cudaStream_t s);
+
+// -- pressure projection (flip_pcg.cu); dense cell-grid vectors, cells
+// outside the system hold zeros
+struct PressureBuffers {
+    uint8_t *fluid;        // interior cell with phi < 0 (a row of the system)
+    double4 *Ad;           // rows {diag, to +x, to +y, to +z}, FP64
+    double *b;             // right-hand side (negative divergence)
+    double *invdiagD;      // MIC(0) inverse pivots, FP64
+    float4 *L;             // {invdiag, Lx, Ly, Lz} for the FP32 sweeps
+    double *x, *r, *q;     // solution, residual, A s
+    float *z, *s;          // preconditioned residual, search direction
+    double *partials;      // per-block partial sums (deterministic reduction)
+    double *scal;          // [0]=s.q [1]=z.r (new rho) [2]=|b|inf [3]=rho
+    unsigned long long *rmaxBits;  // |r|inf as double bits
+    int *levelRange;       // [0]=min(i+j+k) [1]=max(i+j+k) [2]=system size
+    float *pressure;       // float copy of x for the velocity update
+    int nPartials;
+};
+struct PressureArgs {
+    const float *phi, *wu, *wv, *ww;
+    float *u, *v, *w;
+    uint8_t *vu, *vv, *vw;
+    double dt, tol, accTol;
+    int maxIter;
+    float *dumpPressure;   // host, optional
+    double *dumpRhs;       // host, optional
+};
+struct PressureMail {      // pinned host scalars
+    int levelRange[3];
+    double bmax, rho;
+    unsigned long long rmaxBits;
+    int sweepErr;
+};
+struct PressureResult {
+    int iterations;
+    double residual;
+    bool applied;
+    int cells;
+};
+
+// Pipelined wavefront sweeps (flip_sweep.cu)
+struct SweepState {
+    int2 *range;             // per tile [first, last] step holding a system cell
+    unsigned int *progress;  // per tile progress word
+    unsigned int *ticket;    // tile ticket counter
+    int *err;                // set when a bounded wait gave up
+    unsigned int epoch;
+    long long launches;
+};
+int sweep_tiles(int J, int K, int *ntj, int *ntk);
+void launch_sweep_ranges(const StepConsts &c, const uint8_t *fluid, SweepState &sw, cudaStream_t s);
+// z = M^-1 r with the MIC(0) factor L: forward then backward sweep
+void launch_sweeps(const StepConsts &c, const float4 *L, const double *r, float *z, SweepState &sw, cudaStream_t s);
+
+int pressure_partials(const StepConsts &c);
+// PressureSolver::solve (pressuresolver.cpp:44-76) on the device.  Returns
+// FLIP_OK (velocities updated, or nothing to solve), FLIP_E_SOLVER_NOCONV
+// (left unchanged), FLIP_E_DEVICE_TIMEOUT or FLIP_E_CUDA.
+int pressure_project(const StepConsts &c, const PressureArgs &a, PressureBuffers &pb, SweepState &sw,
+                     PressureMail *mail, cudaStream_t s, PressureResult *res, std::string *errMsg);
+
+}  // namespace flip

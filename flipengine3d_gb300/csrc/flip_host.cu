@@ -91,6 +91,7 @@ struct flip_ctx {
     float *u = nullptr, *v = nullptr, *w = nullptr, *su = nullptr, *sv = nullptr, *sw = nullptr;
     uint8_t *vu = nullptr, *vv = nullptr, *vw = nullptr, *status = nullptr;
     PressureBuffers pr{};
+    SweepState sweep{};
     unsigned int *speedHist = nullptr, *maxVelSqBits = nullptr;
     float *maxSpeedSq = nullptr;
     // pinned host mailbox for per-substep scalars
@@ -101,7 +102,9 @@ struct flip_ctx {
         unsigned int rmaxBits;
         int total;
         unsigned int velSqBits;
+        int sweepErr;
     } *mail = nullptr;
+    PressureMail *pmail = nullptr;
     std::vector<void *> allocations;
 
     long long launchesAtCreate = 0;
@@ -173,18 +176,44 @@ int alloc_grids(flip_ctx *x) {
         return rc;
     if ((rc = x->alloc(&x->status, x->nu() + x->nv() + x->nw()))) return rc;
     PressureBuffers &p = x->pr;
-    if ((rc = x->alloc(&p.fluid, nc))) return rc;
-    if ((rc = x->alloc(&p.A, nc)) || (rc = x->alloc(&p.L, nc))) return rc;
-    if ((rc = x->alloc(&p.Adiag, nc)) || (rc = x->alloc(&p.b, nc)) || (rc = x->alloc(&p.invdiagD, nc)) ||
-        (rc = x->alloc(&p.x, nc)))
-        return rc;
-    if ((rc = x->alloc(&p.r, nc)) || (rc = x->alloc(&p.z, nc)) || (rc = x->alloc(&p.s, nc)) ||
-        (rc = x->alloc(&p.q, nc)) || (rc = x->alloc(&p.pressure, nc)))
+    if ((rc = x->alloc(&p.fluid, nc)) || (rc = x->alloc(&p.Ad, nc)) || (rc = x->alloc(&p.L, nc)) ||
+        (rc = x->alloc(&p.b, nc)) || (rc = x->alloc(&p.invdiagD, nc)) || (rc = x->alloc(&p.x, nc)) ||
+        (rc = x->alloc(&p.r, nc)) || (rc = x->alloc(&p.q, nc)) || (rc = x->alloc(&p.z, nc)) ||
+        (rc = x->alloc(&p.s, nc)) || (rc = x->alloc(&p.pressure, nc)))
         return rc;
     p.nPartials = pressure_partials(x->c);
-    if ((rc = x->alloc(&p.partials, p.nPartials + 32))) return rc;
-    if ((rc = x->alloc(&p.scal, 8)) || (rc = x->alloc(&p.rmaxBits, 4)) || (rc = x->alloc(&p.levelRange, 4)))
+    if ((rc = x->alloc(&p.partials, p.nPartials + 32)) || (rc = x->alloc(&p.scal, 8)) ||
+        (rc = x->alloc(&p.rmaxBits, 2)) || (rc = x->alloc(&p.levelRange, 4)))
         return rc;
+    {
+        int ntj, ntk;
+        int nt = sweep_tiles(x->J, x->K, &ntj, &ntk);
+        if ((rc = x->alloc(&x->sweep.range, nt)) || (rc = x->alloc(&x->sweep.progress, nt)) ||
+            (rc = x->alloc(&x->sweep.ticket, 4)) || (rc = x->alloc(&x->sweep.err, 4)))
+            return rc;
+        CK(cudaMemsetAsync(x->sweep.progress, 0, nt * sizeof(unsigned int), x->stream));
+        CK(cudaMemsetAsync(x->sweep.err, 0, 4 * sizeof(int), x->stream));
+    }
+    {
+        // position tables (see StepConsts)
+        int nmax = std::max(x->I, std::max(x->J, x->K)) + 16;
+        int nb = nmax / 10 + 4;
+        std::vector<float> node(nmax), blk(nb), blkf(nb);
+        for (int q = 0; q < nmax; q++) node[q] = (float)((double)(float)q * x->dx);
+        float bdx = (float)(10 * x->dx);
+        for (int q = 0; q < nb; q++) {
+            blk[q] = (float)((double)(float)(q - 1) * (10.0 * x->dx));
+            blkf[q] = (float)((double)(float)(q - 1) * (double)bdx);
+        }
+        float *dn, *db, *dbf;
+        if ((rc = x->alloc(&dn, nmax)) || (rc = x->alloc(&db, nb)) || (rc = x->alloc(&dbf, nb))) return rc;
+        CK(cudaMemcpy(dn, node.data(), nmax * 4, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(db, blk.data(), nb * 4, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(dbf, blkf.data(), nb * 4, cudaMemcpyHostToDevice));
+        x->c.nodePos = dn;
+        x->c.blockPos = db;
+        x->c.blockPosF = dbf;
+    }
     if ((rc = x->alloc(&x->speedHist, 8)) || (rc = x->alloc(&x->maxVelSqBits, 4)) || (rc = x->alloc(&x->maxSpeedSq, 4)))
         return rc;
     CK(cudaMemsetAsync(x->phi, 0, nc * sizeof(float), x->stream));
@@ -311,104 +340,26 @@ int particles_in_order(flip_ctx *x, std::vector<float> *pos, std::vector<float> 
     return FLIP_OK;
 }
 
-// PressureSolver::solve (pressuresolver.cpp:44-76) with PCGSolver::solve
-// (pcgsolver.h:248-302): returns FLIP_OK when the velocity field was
-// updated (or nothing needed solving), FLIP_E_SOLVER_NOCONV when the solve
-// failed and the field was left as it was.
+// PressureSolver::solve (pressuresolver.cpp:44-76) on the device: FLIP_OK
+// when the velocities were updated or nothing needed solving,
+// FLIP_E_SOLVER_NOCONV when the solve failed and they were left as they were.
 int pressure_solve(flip_ctx *x, double dt, bool *applied, flip_stage_dump *d) {
-    cudaStream_t s = x->stream;
-    StepConsts &c = x->c;
-    PressureBuffers &p = x->pr;
-    *applied = false;
-    x->stats.pressure_iterations = 0;
-    x->stats.pressure_error = 0.0;
-    launch_pressure_build(c, x->phi, x->wu, x->wv, x->ww, x->u, x->v, x->w, dt, p, s);
-    CK(cudaMemcpyAsync(x->mail->levelRange, p.levelRange, 3 * sizeof(int), cudaMemcpyDeviceToHost, s));
-    CK(cudaMemcpyAsync(&x->mail->bmax, p.scal + 2, sizeof(double), cudaMemcpyDeviceToHost, s));
-    int rc = sync(x);
-    if (rc) return rc;
-    if (d && d->rhs) {
-        CK(cudaMemcpy(d->rhs, p.b, x->nc() * sizeof(double), cudaMemcpyDeviceToHost));
-    }
-    int lo = x->mail->levelRange[0], hi = x->mail->levelRange[1];
-    x->stats.pressure_cells = x->mail->levelRange[2];
-    double bmax = x->mail->bmax;
-    if (hi < lo || bmax < x->tol) return FLIP_OK;   // empty system or nothing to project
-    double ptol = std::max(x->tol, 1e-30) * bmax;
-
-    launch_mic0_factor(c, x->phi, x->wu, x->wv, x->ww, dt, p, lo, hi, s);
-    launch_init_residual(c, p, s);
-    launch_precondition(c, p, p.r, p.z, lo, hi, s);
-    launch_dot_zr(c, p, s);
-    CK(cudaMemcpyAsync(&x->mail->rho, p.scal + 1, sizeof(double), cudaMemcpyDeviceToHost, s));
-    rc = sync(x);
-    if (rc) return rc;
-    double rho = x->mail->rho;
-    bool ok = false;
-    int iterations = 0;
-    double resid = bmax;
-    if (rho == 0 || rho != rho) {
-        ok = false;
-    } else {
-        launch_copy_zs(c, p, s);
-        launch_set_rho(p, s);
-        // FP32 PCG on the FP32 rows with the solution in FP64; the FP64 true
-        // residual b - A x is checked every 25 iterations and whenever the
-        // FP32 recurrence reports convergence.  If the recurrence was wrong,
-        // CG restarts from the true residual (iterative refinement).
-        unsigned int *trueBits = p.rmaxBits + 1;
-        int it;
-        for (it = 0; it < x->maxIter; it++) {
-            launch_spmv_dot(c, p, s);
-            launch_update_xr(c, p, s);
-            CK(cudaMemcpyAsync(&x->mail->rmaxBits, p.rmaxBits, sizeof(unsigned int), cudaMemcpyDeviceToHost, s));
-            rc = sync(x);
-            if (rc) return rc;
-            float rm;
-            std::memcpy(&rm, &x->mail->rmaxBits, 4);
-            bool claim = rm <= ptol, periodic = (it + 1) % 25 == 0;
-            resid = rm;
-            if (claim || periodic) {
-                launch_true_residual(c, x->phi, x->wu, x->wv, x->ww, dt, p, p.q, trueBits, s);
-                CK(cudaMemcpyAsync(&x->mail->rmaxBits, trueBits, sizeof(unsigned int), cudaMemcpyDeviceToHost, s));
-                rc = sync(x);
-                if (rc) return rc;
-                std::memcpy(&rm, &x->mail->rmaxBits, 4);
-                resid = rm;
-                if (resid <= ptol) {
-                    iterations = it + 1;
-                    ok = true;
-                    break;
-                }
-                if (claim) {
-                    launch_copy_qr(c, p, s);
-                    launch_precondition(c, p, p.r, p.z, lo, hi, s);
-                    launch_dot_zr(c, p, s);
-                    launch_copy_zs(c, p, s);
-                    launch_set_rho(p, s);
-                    continue;
-                }
-            }
-            launch_precondition(c, p, p.r, p.z, lo, hi, s);
-            launch_dot_zr(c, p, s);
-            launch_update_s(c, p, s);
-            launch_set_rho(p, s);
-        }
-        if (!ok) iterations = it;
-    }
-    x->stats.pressure_iterations = iterations;
-    x->stats.pressure_error = resid;
-    bool accept = ok || (iterations == x->maxIter && resid < x->accTol);
-    launch_pressure_to_float(c, p, s);
-    if (d && d->pressure) {
-        rc = sync(x);
-        if (rc) return rc;
-        CK(cudaMemcpy(d->pressure, p.pressure, x->nc() * sizeof(float), cudaMemcpyDeviceToHost));
-    }
-    if (!accept) return FLIP_E_SOLVER_NOCONV;
-    launch_apply_pressure(c, x->phi, x->wu, x->wv, x->ww, p, dt, x->u, x->v, x->w, x->vu, x->vv, x->vw, s);
-    *applied = true;
-    return FLIP_OK;
+    PressureArgs a;
+    a.phi = x->phi; a.wu = x->wu; a.wv = x->wv; a.ww = x->ww;
+    a.u = x->u; a.v = x->v; a.w = x->w;
+    a.vu = x->vu; a.vv = x->vv; a.vw = x->vw;
+    a.dt = dt; a.tol = x->tol; a.accTol = x->accTol; a.maxIter = x->maxIter;
+    a.dumpPressure = d ? d->pressure : nullptr;
+    a.dumpRhs = d ? d->rhs : nullptr;
+    PressureResult res{};
+    std::string msg;
+    int rc = pressure_project(x->c, a, x->pr, x->sweep, x->pmail, x->stream, &res, &msg);
+    x->stats.pressure_iterations = res.iterations;
+    x->stats.pressure_error = res.residual;
+    x->stats.pressure_cells = res.cells;
+    *applied = res.applied;
+    if (rc != FLIP_OK && rc != FLIP_E_SOLVER_NOCONV) return fail(rc, msg);
+    return rc;
 }
 
 int dump_mac(flip_ctx *x, float *a, float *b, float *e, const float *u, const float *v, const float *w) {
@@ -649,7 +600,8 @@ int flip_create(int isize, int jsize, int ksize, double dx, flip_ctx **out) {
         return fail(FLIP_E_CUDA, "cudaStreamCreate failed");
     }
     x->ownStream = true;
-    if (cudaMallocHost((void **)&x->mail, sizeof(flip_ctx::Mail)) != cudaSuccess) {
+    if (cudaMallocHost((void **)&x->mail, sizeof(flip_ctx::Mail)) != cudaSuccess ||
+        cudaMallocHost((void **)&x->pmail, sizeof(PressureMail)) != cudaSuccess) {
         cudaStreamDestroy(x->stream);
         delete x;
         return fail(FLIP_E_NOMEM, "cudaMallocHost failed");
@@ -658,6 +610,14 @@ int flip_create(int isize, int jsize, int ksize, double dx, flip_ctx **out) {
     c.I = isize; c.J = jsize; c.K = ksize;
     c.dx = dx; c.invdx = 1.0 / dx; c.invdxf = (float)(1.0 / dx); c.dxf = (float)dx;
     c.radius = 0.5 * 1.0 * dx * std::sqrt(3.0);
+    auto below = [](double bound) {   // largest float v with (double)v < bound
+        float v = (float)bound;
+        while ((double)v >= bound) v = std::nextafter(v, 0.0f);
+        return v;
+    };
+    c.gxmax = below(dx * isize);
+    c.gymax = below(dx * jsize);
+    c.gzmax = below(dx * ksize);
     c.cfl = x->cfl;
     c.maxPerCell = x->maxPerCell;
     int rc = alloc_grids(x);
@@ -677,6 +637,7 @@ int flip_destroy(flip_ctx *x) {
         if (x->ev[q]) cudaEventDestroy(x->ev[q]);
     for (void *p : x->allocations) cudaFree(p);
     if (x->mail) cudaFreeHost(x->mail);
+    if (x->pmail) cudaFreeHost(x->pmail);
     if (x->ownStream) cudaStreamDestroy(x->stream);
     delete x;
     return FLIP_OK;

@@ -203,20 +203,20 @@ constexpr int BW = 10;
 // Does the reference's count pass put particle p in block (bx,by,bz)'s list?
 // (particlelevelset.cpp:477-532, velocityadvector.cpp:272-329)
 __device__ __forceinline__ bool in_block_list(float px, float py, float pz, float sr, float blockdxf,
-                                              double invBlock, int bx, int by, int bz) {
-    int ci = (int)floor((double)px * invBlock), cj = (int)floor((double)py * invBlock),
-        ck = (int)floor((double)pz * invBlock);
-    float bpx = (float)((double)(float)ci * (double)blockdxf);
-    float bpy = (float)((double)(float)cj * (double)blockdxf);
-    float bpz = (float)((double)(float)ck * (double)blockdxf);
+                                              double invBlock, float invBlockf, const float *blockPosF,
+                                              int bx, int by, int bz) {
+    int ci = exact_floor(px, invBlock, invBlockf), cj = exact_floor(py, invBlock, invBlockf),
+        ck = exact_floor(pz, invBlock, invBlockf);
+    // (float)((double)(float)n * (double)blockdxf), tabulated from n = -1
+    float bpx = blockPosF[ci + 1], bpy = blockPosF[cj + 1], bpz = blockPosF[ck + 1];
     if (__fsub_rn(px, sr) > bpx && __fsub_rn(py, sr) > bpy && __fsub_rn(pz, sr) > bpz &&
         __fadd_rn(px, sr) < __fadd_rn(bpx, blockdxf) && __fadd_rn(py, sr) < __fadd_rn(bpy, blockdxf) &&
         __fadd_rn(pz, sr) < __fadd_rn(bpz, blockdxf)) {
         return ci == bx && cj == by && ck == bz;
     }
-    int i0 = (int)floor((double)__fsub_rn(px, sr) * invBlock), i1 = (int)floor((double)__fadd_rn(px, sr) * invBlock);
-    int j0 = (int)floor((double)__fsub_rn(py, sr) * invBlock), j1 = (int)floor((double)__fadd_rn(py, sr) * invBlock);
-    int k0 = (int)floor((double)__fsub_rn(pz, sr) * invBlock), k1 = (int)floor((double)__fadd_rn(pz, sr) * invBlock);
+    int i0 = exact_floor(__fsub_rn(px, sr), invBlock, invBlockf), i1 = exact_floor(__fadd_rn(px, sr), invBlock, invBlockf);
+    int j0 = exact_floor(__fsub_rn(py, sr), invBlock, invBlockf), j1 = exact_floor(__fadd_rn(py, sr), invBlock, invBlockf);
+    int k0 = exact_floor(__fsub_rn(pz, sr), invBlock, invBlockf), k1 = exact_floor(__fadd_rn(pz, sr), invBlock, invBlockf);
     return bx >= i0 && bx <= i1 && by >= j0 && by <= j1 && bz >= k0 && bz <= k1;
 }
 
@@ -235,9 +235,10 @@ __global__ void __launch_bounds__(TPB) k_liquid_sdf(ParticleSoA p, const int *ce
     const float sr = __fmul_rn(2.0f, r);
     const float blockdxf = (float)(BW * dx);
     const double invBlock = 1.0 / (double)blockdxf;
+    const float invBlockf = (float)invBlock;
     const double blockdxD = (double)BW * dx;
-    const float offx = (float)((double)(float)bx * blockdxD), offy = (float)((double)(float)by * blockdxD),
-                offz = (float)((double)(float)bz * blockdxD);
+    const float offx = c.blockPos[bx + 1], offy = c.blockPos[by + 1],
+                offz = c.blockPos[bz + 1];
     Dims cells{c.I, c.J, c.K};
     int x0 = max(bx * BW - 2, 0), x1 = min(bx * BW + BW + 1, c.I - 1);
     int y0 = max(by * BW - 2, 0), y1 = min(by * BW + BW + 1, c.J - 1);
@@ -249,14 +250,14 @@ __global__ void __launch_bounds__(TPB) k_liquid_sdf(ParticleSoA p, const int *ce
         int pb = cellStart[cells.idx(x0, cy, cz)], pe = cellStart[cells.idx(x1, cy, cz) + 1];
         for (int t = pb + lane; t < pe; t += 32) {
             float px = p.px[t], py = p.py[t], pz = p.pz[t];
-            if (!in_block_list(px, py, pz, sr, blockdxf, invBlock, bx, by, bz)) continue;
+            if (!in_block_list(px, py, pz, sr, blockdxf, invBlock, invBlockf, c.blockPosF, bx, by, bz)) continue;
             float lx = __fsub_rn(px, offx), ly = __fsub_rn(py, offy), lz = __fsub_rn(pz, offz);
-            int a0 = max((int)floor((double)__fsub_rn(lx, sr) * c.invdx), 0);
-            int b0 = max((int)floor((double)__fsub_rn(ly, sr) * c.invdx), 0);
-            int c0 = max((int)floor((double)__fsub_rn(lz, sr) * c.invdx), 0);
-            int a1 = min((int)floor((double)__fadd_rn(lx, sr) * c.invdx), BW - 1);
-            int b1 = min((int)floor((double)__fadd_rn(ly, sr) * c.invdx), BW - 1);
-            int c1 = min((int)floor((double)__fadd_rn(lz, sr) * c.invdx), BW - 1);
+            int a0 = max(exact_floor(__fsub_rn(lx, sr), c.invdx, c.invdxf), 0);
+            int b0 = max(exact_floor(__fsub_rn(ly, sr), c.invdx, c.invdxf), 0);
+            int c0 = max(exact_floor(__fsub_rn(lz, sr), c.invdx, c.invdxf), 0);
+            int a1 = min(exact_floor(__fadd_rn(lx, sr), c.invdx, c.invdxf), BW - 1);
+            int b1 = min(exact_floor(__fadd_rn(ly, sr), c.invdx, c.invdxf), BW - 1);
+            int c1 = min(exact_floor(__fadd_rn(lz, sr), c.invdx, c.invdxf), BW - 1);
             for (int cc = c0; cc <= c1; cc++) {
                 float dz = __fsub_rn(centre[cc], lz);
                 for (int bb = b0; bb <= b1; bb++) {
@@ -313,12 +314,13 @@ __global__ void __launch_bounds__(TPB) k_p2g(ParticleSoA p, const int *cellStart
     const float ox = dir == 0 ? 0.0f : halfdx, oy = dir == 1 ? 0.0f : halfdx, oz = dir == 2 ? 0.0f : halfdx;
     const float blockdxf = (float)(dx * BW);
     const double invBlock = 1.0 / (double)blockdxf;
+    const float invBlockf = (float)invBlock;
     const int bx = fi / BW, by = fj / BW, bz = fk / BW;
     const double blockdxD = (double)BW * dx;
-    const float offx = (float)((double)(float)bx * blockdxD), offy = (float)((double)(float)by * blockdxD),
-                offz = (float)((double)(float)bz * blockdxD);
+    const float offx = c.blockPos[bx + 1], offy = c.blockPos[by + 1],
+                offz = c.blockPos[bz + 1];
     const int la = fi - bx * BW, lb = fj - by * BW, lc = fk - bz * BW;
-    const float gx = idx_to_pos(la, dx), gy = idx_to_pos(lb, dx), gz = idx_to_pos(lc, dx);
+    const float gx = c.nodePos[la], gy = c.nodePos[lb], gz = c.nodePos[lc];
     // candidate cells of the cell grid
     int cx0 = dir == 0 ? fi - 1 : fi - 1, cx1 = dir == 0 ? fi : fi + 1;
     int cy0 = fj - 1, cy1 = dir == 1 ? fj : fj + 1;
@@ -337,11 +339,11 @@ __global__ void __launch_bounds__(TPB) k_p2g(ParticleSoA p, const int *cellStart
                 float d2 = __fadd_rn(__fadd_rn(__fmul_rn(ddx, ddx), __fmul_rn(ddy, ddy)), __fmul_rn(ddz, ddz));
                 if (!(d2 < rsq)) continue;
                 // the face must lie inside the particle's clamped local box
-                int a0 = (int)floor((double)__fsub_rn(lx, sr) * c.invdx), a1 = (int)floor((double)__fadd_rn(lx, sr) * c.invdx);
-                int b0 = (int)floor((double)__fsub_rn(ly, sr) * c.invdx), b1 = (int)floor((double)__fadd_rn(ly, sr) * c.invdx);
-                int c0 = (int)floor((double)__fsub_rn(lz, sr) * c.invdx), c1 = (int)floor((double)__fadd_rn(lz, sr) * c.invdx);
+                int a0 = exact_floor(__fsub_rn(lx, sr), c.invdx, c.invdxf), a1 = exact_floor(__fadd_rn(lx, sr), c.invdx, c.invdxf);
+                int b0 = exact_floor(__fsub_rn(ly, sr), c.invdx, c.invdxf), b1 = exact_floor(__fadd_rn(ly, sr), c.invdx, c.invdxf);
+                int c0 = exact_floor(__fsub_rn(lz, sr), c.invdx, c.invdxf), c1 = exact_floor(__fadd_rn(lz, sr), c.invdx, c.invdxf);
                 if (la < a0 || la > a1 || lb < b0 || lb > b1 || lc < c0 || lc > c1) continue;
-                if (!in_block_list(px, py, pz, sr, blockdxf, invBlock, bx, by, bz)) continue;
+                if (!in_block_list(px, py, pz, sr, blockdxf, invBlock, invBlockf, c.blockPosF, bx, by, bz)) continue;
                 float vel = dir == 0 ? p.vx[t] : dir == 1 ? p.vy[t] : p.vz[t];
                 float w3 = __fmul_rn(__fmul_rn(__fmul_rn(coef1, d2), d2), d2);
                 float w2 = __fmul_rn(__fmul_rn(coef2, d2), d2);
@@ -445,83 +447,104 @@ __global__ void k_constrain(long long nu, long long nv, long long nw, float *u, 
 }
 
 // ---------------------------------------------------------- particle update
-// MAC trilinear sample in FP64, exactly as MACVelocityField::_interpolateLinearU/V/W
-// (macvelocityfield.cpp:519-613) and Interpolation::trilinearInterpolate
-// (interpolation.cpp:61-70).
-__device__ __forceinline__ double trilerp(const double p[8], double x, double y, double z) {
-    return p[0] * (1 - x) * (1 - y) * (1 - z) + p[1] * x * (1 - y) * (1 - z) + p[2] * (1 - x) * y * (1 - z) +
-           p[3] * (1 - x) * (1 - y) * z + p[4] * x * (1 - y) * z + p[5] * (1 - x) * y * z +
-           p[6] * x * y * (1 - z) + p[7] * x * y * z;
+// Trilinear weights of Interpolation::trilinearInterpolate (interpolation.cpp:
+// 61-70) with vertex order {000,100,010,001,101,011,110,111}, in FP32.
+__device__ __forceinline__ float trilerp_f(const float q[8], float x, float y, float z) {
+    float x1 = 1.0f - x, y1 = 1.0f - y, z1 = 1.0f - z;
+    float r = q[0] * (x1 * y1 * z1);
+    r = __fmaf_rn(q[1], x * y1 * z1, r);
+    r = __fmaf_rn(q[2], x1 * y * z1, r);
+    r = __fmaf_rn(q[3], x1 * y1 * z, r);
+    r = __fmaf_rn(q[4], x * y1 * z, r);
+    r = __fmaf_rn(q[5], x1 * y * z, r);
+    r = __fmaf_rn(q[6], x * y * z1, r);
+    r = __fmaf_rn(q[7], x * y * z, r);
+    return r;
 }
 
-__device__ double interp_face(const float *G, int ni, int nj, int nk, int dir, double x, double y, double z,
-                              double dx, double inv) {
-    if (dir != 0) x -= 0.5 * dx;
-    if (dir != 1) y -= 0.5 * dx;
-    if (dir != 2) z -= 0.5 * dx;
-    int i = (int)floor(x * inv), j = (int)floor(y * inv), k = (int)floor(z * inv);
-    double ix = (x - (double)i * dx) * inv, iy = (y - (double)j * dx) * inv, iz = (z - (double)k * dx) * inv;
-    double q[8];
-    const int off[8][3] = {{0, 0, 0}, {1, 0, 0}, {0, 1, 0}, {0, 0, 1}, {1, 0, 1}, {0, 1, 1}, {1, 1, 0}, {1, 1, 1}};
-#pragma unroll
-    for (int t = 0; t < 8; t++) {
-        int a = i + off[t][0], b = j + off[t][1], cc = k + off[t][2];
-        bool in = a >= 0 && b >= 0 && cc >= 0 && a < ni && b < nj && cc < nk;
-        q[t] = in ? (double)__ldg(&G[(long long)a + (long long)ni * ((long long)b + (long long)nj * cc)]) : 0.0;
-    }
-    return trilerp(q, ix, iy, iz);
+__device__ __forceinline__ float grid_at(const float *G, int ni, int nj, int nk, int a, int b, int cc) {
+    bool in = a >= 0 && b >= 0 && cc >= 0 && a < ni && b < nj && cc < nk;
+    return in ? __ldg(&G[(long long)a + (long long)ni * ((long long)b + (long long)nj * cc)]) : 0.0f;
+}
+
+// MAC velocity component at a point, as MACVelocityField::_interpolateLinearU/V/W
+// (macvelocityfield.cpp:519-613) but in FP32.  The cell coordinate is
+// x*(1/dx) - 1/2 in one fused step, which is exact for power-of-two dx and
+// within half an ulp otherwise; the reference evaluates the same in FP64.
+__device__ __forceinline__ float interp_face(const float *G, int ni, int nj, int nk, int dir, float x, float y,
+                                             float z, float invdxf) {
+    float fx = dir == 0 ? __fmul_rn(x, invdxf) : __fmaf_rn(x, invdxf, -0.5f);
+    float fy = dir == 1 ? __fmul_rn(y, invdxf) : __fmaf_rn(y, invdxf, -0.5f);
+    float fz = dir == 2 ? __fmul_rn(z, invdxf) : __fmaf_rn(z, invdxf, -0.5f);
+    float gi = floorf(fx), gj = floorf(fy), gk = floorf(fz);
+    int i = (int)gi, j = (int)gj, k = (int)gk;
+    float q[8] = {grid_at(G, ni, nj, nk, i, j, k),         grid_at(G, ni, nj, nk, i + 1, j, k),
+                  grid_at(G, ni, nj, nk, i, j + 1, k),     grid_at(G, ni, nj, nk, i, j, k + 1),
+                  grid_at(G, ni, nj, nk, i + 1, j, k + 1), grid_at(G, ni, nj, nk, i, j + 1, k + 1),
+                  grid_at(G, ni, nj, nk, i + 1, j + 1, k), grid_at(G, ni, nj, nk, i + 1, j + 1, k + 1)};
+    return trilerp_f(q, fx - gi, fy - gj, fz - gk);
+}
+
+// isPositionInGrid (grid3d.h:133-135): x >= 0 && x < I dx, with the upper
+// bound pre-rounded so the float compare equals the reference's FP64 one.
+__device__ __forceinline__ bool in_grid(const StepConsts &c, F3 p) {
+    return p.x >= 0.0f && p.y >= 0.0f && p.z >= 0.0f && p.x <= c.gxmax && p.y <= c.gymax && p.z <= c.gzmax;
 }
 
 __device__ F3 eval_vel(const StepConsts &c, const float *u, const float *v, const float *w, F3 p) {
-    double x = p.x, y = p.y, z = p.z;
-    double dx = c.dx;
-    if (!(x >= 0 && y >= 0 && z >= 0 && x < dx * c.I && y < dx * c.J && z < dx * c.K)) return f3(0.0f, 0.0f, 0.0f);
-    return f3((float)interp_face(u, c.I + 1, c.J, c.K, 0, x, y, z, dx, c.invdx),
-              (float)interp_face(v, c.I, c.J + 1, c.K, 1, x, y, z, dx, c.invdx),
-              (float)interp_face(w, c.I, c.J, c.K + 1, 2, x, y, z, dx, c.invdx));
+    if (!in_grid(c, p)) return f3(0.0f, 0.0f, 0.0f);
+    return f3(interp_face(u, c.I + 1, c.J, c.K, 0, p.x, p.y, p.z, c.invdxf),
+              interp_face(v, c.I, c.J + 1, c.K, 1, p.x, p.y, p.z, c.invdxf),
+              interp_face(w, c.I, c.J, c.K + 1, 2, p.x, p.y, p.z, c.invdxf));
 }
 
-// Interpolation::trilinearInterpolate(vec3, dx, grid) on the nodal solid SDF
-// (interpolation.cpp:72-113): the cell offset is a float difference.
+// Nodal solid SDF at a point (Interpolation::trilinearInterpolate(vec3, dx,
+// grid), interpolation.cpp:72-113).  FP32 weights; when the value is within
+// rounding of zero the sign is settled by the reference's FP64 evaluation.
 __device__ float solid_at(const StepConsts &c, const float *S, F3 p) {
-    int i = (int)floor((double)p.x * c.invdx), j = (int)floor((double)p.y * c.invdx), k = (int)floor((double)p.z * c.invdx);
-    double ix = (double)__fsub_rn(p.x, idx_to_pos(i, c.dx)) * c.invdx;
-    double iy = (double)__fsub_rn(p.y, idx_to_pos(j, c.dx)) * c.invdx;
-    double iz = (double)__fsub_rn(p.z, idx_to_pos(k, c.dx)) * c.invdx;
+    int i = exact_floor(p.x, c.invdx, c.invdxf), j = exact_floor(p.y, c.invdx, c.invdxf),
+        k = exact_floor(p.z, c.invdx, c.invdxf);
+    float dxl = __fsub_rn(p.x, c.nodePos[max(i, 0)]), dyl = __fsub_rn(p.y, c.nodePos[max(j, 0)]),
+          dzl = __fsub_rn(p.z, c.nodePos[max(k, 0)]);
     int ni = c.I + 1, nj = c.J + 1, nk = c.K + 1;
-    double q[8];
-    const int off[8][3] = {{0, 0, 0}, {1, 0, 0}, {0, 1, 0}, {0, 0, 1}, {1, 0, 1}, {0, 1, 1}, {1, 1, 0}, {1, 1, 1}};
+    float q[8] = {grid_at(S, ni, nj, nk, i, j, k),         grid_at(S, ni, nj, nk, i + 1, j, k),
+                  grid_at(S, ni, nj, nk, i, j + 1, k),     grid_at(S, ni, nj, nk, i, j, k + 1),
+                  grid_at(S, ni, nj, nk, i + 1, j, k + 1), grid_at(S, ni, nj, nk, i, j + 1, k + 1),
+                  grid_at(S, ni, nj, nk, i + 1, j + 1, k), grid_at(S, ni, nj, nk, i + 1, j + 1, k + 1)};
+    float v = trilerp_f(q, dxl * c.invdxf, dyl * c.invdxf, dzl * c.invdxf);
+    float mag = 0.0f;
 #pragma unroll
-    for (int t = 0; t < 8; t++) {
-        int a = i + off[t][0], b = j + off[t][1], cc = k + off[t][2];
-        bool in = a >= 0 && b >= 0 && cc >= 0 && a < ni && b < nj && cc < nk;
-        q[t] = in ? (double)__ldg(&S[(long long)a + (long long)ni * ((long long)b + (long long)nj * cc)]) : 0.0;
-    }
-    return (float)trilerp(q, ix, iy, iz);
+    for (int t = 0; t < 8; t++) mag += fabsf(q[t]);
+    if (fabsf(v) > 1e-6f * mag) return v;
+    double qd[8];
+#pragma unroll
+    for (int t = 0; t < 8; t++) qd[t] = q[t];
+    double ix = (double)dxl * c.invdx, iy = (double)dyl * c.invdx, iz = (double)dzl * c.invdx;
+    return (float)(qd[0] * (1 - ix) * (1 - iy) * (1 - iz) + qd[1] * ix * (1 - iy) * (1 - iz) +
+                   qd[2] * (1 - ix) * iy * (1 - iz) + qd[3] * (1 - ix) * (1 - iy) * iz + qd[4] * ix * (1 - iy) * iz +
+                   qd[5] * (1 - ix) * iy * iz + qd[6] * ix * iy * (1 - iz) + qd[7] * ix * iy * iz);
 }
 
-// Interpolation::trilinearInterpolateGradient (interpolation.cpp:197-258)
+// Interpolation::trilinearInterpolateGradient (interpolation.cpp:197-258), FP32
 __device__ F3 solid_grad(const StepConsts &c, const float *S, F3 p) {
-    int i = (int)floor((double)p.x * c.invdx), j = (int)floor((double)p.y * c.invdx), k = (int)floor((double)p.z * c.invdx);
-    double ix = (double)__fsub_rn(p.x, idx_to_pos(i, c.dx)) * c.invdx;
-    double iy = (double)__fsub_rn(p.y, idx_to_pos(j, c.dx)) * c.invdx;
-    double iz = (double)__fsub_rn(p.z, idx_to_pos(k, c.dx)) * c.invdx;
+    int i = exact_floor(p.x, c.invdx, c.invdxf), j = exact_floor(p.y, c.invdx, c.invdxf),
+        k = exact_floor(p.z, c.invdx, c.invdxf);
+    float ix = __fsub_rn(p.x, c.nodePos[max(i, 0)]) * c.invdxf;
+    float iy = __fsub_rn(p.y, c.nodePos[max(j, 0)]) * c.invdxf;
+    float iz = __fsub_rn(p.z, c.nodePos[max(k, 0)]) * c.invdxf;
     int ni = c.I + 1, nj = c.J + 1, nk = c.K + 1;
-    auto at = [&](int a, int b, int cc) -> float {
-        a += i; b += j; cc += k;
-        bool in = a >= 0 && b >= 0 && cc >= 0 && a < ni && b < nj && cc < nk;
-        return in ? __ldg(&S[(long long)a + (long long)ni * ((long long)b + (long long)nj * cc)]) : 0.0f;
-    };
-    float v000 = at(0, 0, 0), v100 = at(1, 0, 0), v010 = at(0, 1, 0), v001 = at(0, 0, 1);
-    float v101 = at(1, 0, 1), v011 = at(0, 1, 1), v110 = at(1, 1, 0), v111 = at(1, 1, 1);
-    auto bil = [](double a, double b, double cc, double d, double x, double y) {
-        double l1 = (1 - x) * a + x * b;
-        double l2 = (1 - x) * cc + x * d;
+    float v000 = grid_at(S, ni, nj, nk, i, j, k), v100 = grid_at(S, ni, nj, nk, i + 1, j, k);
+    float v010 = grid_at(S, ni, nj, nk, i, j + 1, k), v001 = grid_at(S, ni, nj, nk, i, j, k + 1);
+    float v101 = grid_at(S, ni, nj, nk, i + 1, j, k + 1), v011 = grid_at(S, ni, nj, nk, i, j + 1, k + 1);
+    float v110 = grid_at(S, ni, nj, nk, i + 1, j + 1, k), v111 = grid_at(S, ni, nj, nk, i + 1, j + 1, k + 1);
+    auto bil = [](float a, float b, float cc, float d, float x, float y) {
+        float l1 = (1 - x) * a + x * b;
+        float l2 = (1 - x) * cc + x * d;
         return (1 - y) * l1 + y * l2;
     };
-    float gx = (float)bil(__fsub_rn(v100, v000), __fsub_rn(v110, v010), __fsub_rn(v101, v001), __fsub_rn(v111, v011), iy, iz);
-    float gy = (float)bil(__fsub_rn(v010, v000), __fsub_rn(v110, v100), __fsub_rn(v011, v001), __fsub_rn(v111, v101), ix, iz);
-    float gz = (float)bil(__fsub_rn(v001, v000), __fsub_rn(v101, v100), __fsub_rn(v011, v010), __fsub_rn(v111, v110), ix, iy);
+    float gx = bil(v100 - v000, v110 - v010, v101 - v001, v111 - v011, iy, iz);
+    float gy = bil(v010 - v000, v110 - v100, v011 - v001, v111 - v101, ix, iz);
+    float gz = bil(v001 - v000, v101 - v100, v011 - v010, v111 - v110, ix, iy);
     return f3(gx, gy, gz);
 }
 
@@ -543,16 +566,16 @@ __device__ __forceinline__ F3 box_nearest(const StepConsts &c, F3 p) {
 }
 
 __device__ __forceinline__ bool near_solid(const StepConsts &c, const uint8_t *ns, F3 p) {
-    int i = (int)floor((double)p.x * c.invNearCell), j = (int)floor((double)p.y * c.invNearCell),
-        k = (int)floor((double)p.z * c.invNearCell);
+    int i = exact_floor(p.x, c.invNearCell, c.invNearCellf), j = exact_floor(p.y, c.invNearCell, c.invNearCellf),
+        k = exact_floor(p.z, c.invNearCell, c.invNearCellf);
     if (i < 0 || j < 0 || k < 0 || i >= c.nsi || j >= c.nsj || k >= c.nsk) return false;
     return ns[(long long)i + (long long)c.nsi * ((long long)j + (long long)c.nsj * k)] != 0;
 }
 
 // FluidSimulation::_resolveCollision (src/engine/fluidsimulation.cpp:4221-4296)
 __device__ F3 resolve_collision(const StepConsts &c, const float *S, const uint8_t *ns, F3 oldp, F3 newp) {
-    int gi = (int)floor((double)newp.x * c.invdx), gj = (int)floor((double)newp.y * c.invdx),
-        gk = (int)floor((double)newp.z * c.invdx);
+    int gi = exact_floor(newp.x, c.invdx, c.invdxf), gj = exact_floor(newp.y, c.invdx, c.invdxf),
+        gk = exact_floor(newp.z, c.invdx, c.invdxf);
     if (!(gi >= 0 && gj >= 0 && gk >= 0 && gi < c.I && gj < c.J && gk < c.K)) newp = box_nearest(c, newp);
     if (!near_solid(c, ns, oldp) && !near_solid(c, ns, newp)) return newp;
     const float eps = 1e-6f;
@@ -612,7 +635,7 @@ __global__ void __launch_bounds__(TPB) k_advect(ParticleSoA p, int n, StepConsts
         F3 vold = eval_vel(c, su, sv, sw, p0);
         F3 vflip = sub(add(v0, vpic), vold);
         F3 vn = add(mul(picRatio, vpic), mul(flipRatio, vflip));
-        F3 k1 = eval_vel(c, u, v, w, p0);
+        F3 k1 = vpic;
         F3 k2 = eval_vel(c, u, v, w, add(p0, mul((float)(0.5 * dt), k1)));
         F3 k3 = eval_vel(c, u, v, w, add(p0, mul((float)(0.75 * dt), k2)));
         F3 sum = add(add(mul(2.0f, k1), mul(3.0f, k2)), mul(4.0f, k3));
@@ -620,15 +643,20 @@ __global__ void __launch_bounds__(TPB) k_advect(ParticleSoA p, int n, StepConsts
         p1 = resolve_collision(c, S, ns, p0, p1);
         p.px[t] = p1.x; p.py[t] = p1.y; p.pz[t] = p1.z;
         p.vx[t] = vn.x; p.vy[t] = vn.y; p.vz[t] = vn.z;
-        double speed = (double)len3(vn);
-        int bin = (int)fmin(floor(speed / speedStep), 5.0);
+        float speed = len3(vn);
+        // floor(speed / step) as the reference's FP64 division gives it
+        float qf = __fmul_rn(speed, (float)(1.0 / speedStep));
+        float fl = floorf(qf);
+        int bin = (qf - fl > 1e-3f && qf - fl < 1.0f - 1e-3f) ? (int)fminf(fl, 5.0f)
+                                                               : (int)fmin(floor((double)speed / speedStep), 5.0);
+        if (speed != speed) bin = 5;
         atomicAdd(&shist[bin], 1u);
         unsigned int key;
         if (solid_at(c, S, p1) < 0.0f) {
             key = KEY_SOLID;
         } else {
-            int i = (int)floor((double)p1.x * c.invdx), j = (int)floor((double)p1.y * c.invdx),
-                k = (int)floor((double)p1.z * c.invdx);
+            int i = exact_floor(p1.x, c.invdx, c.invdxf), j = exact_floor(p1.y, c.invdx, c.invdxf),
+                k = exact_floor(p1.z, c.invdx, c.invdxf);
             Dims d{c.I, c.J, c.K};
             key = d.in(i, j, k) ? (unsigned int)d.idx(i, j, k) : KEY_SOLID;
         }
@@ -659,7 +687,7 @@ __global__ void k_mark_fast(ParticleSoA p, int n, const float *maxSpeedSq, unsig
     unsigned int k = keys[t];
     if (k & KEY_SOLID) return;
     F3 v = f3(p.vx[t], p.vy[t], p.vz[t]);
-    if ((double)dot3(v, v) > (double)*maxSpeedSq) keys[t] = k | KEY_FAST;
+    if (dot3(v, v) > *maxSpeedSq) keys[t] = k | KEY_FAST;
 }
 
 }  // namespace

@@ -1,0 +1,513 @@
+// Variational pressure projection for GB300 (sm_103a).
+//
+// The system is the reference's (pressuresolver.cpp:580-808): a 7-point
+// matrix over the interior cells with phi < 0, ghost-fluid diagonal terms at
+// air neighbours, face weights from the solid level set.  Its rows are built
+// in FP64 exactly as the reference builds them and kept as {diag, +x, +y, +z}.
+// Preconditioner: the reference's MIC(0) (pcgsolver.h:70-185, tau 0.97,
+// pivot floor 0.25) restated for 7-point rows; the factorisation runs as an
+// i+j+k wavefront in FP64 and the two triangular sweeps as the pipelined
+// FP32 wavefront of flip_sweep.cu.  CG (pcgsolver.h:248-302): the
+// Laplacian apply, the solution, the residual and the dot products are
+// FP64, so the recurrence tracks b - A x to FP64 rounding; the FP32 parts
+// (preconditioner, search direction) only steer the iteration.  Every 25
+// iterations, and whenever the recurrence reports convergence, the residual
+// is recomputed as b - A x (iterative refinement), and convergence is
+// decided on it, with the reference's test |r|inf <= tol * |b|inf.
+#include <cmath>
+#include <cstring>
+#include <string>
+
+#include "../../include/flip3d.h"
+#include "flip_kernels.cuh"
+
+namespace flip {
+
+namespace {
+
+constexpr int TPB = 256;
+
+__device__ __forceinline__ bool sys_cell(const StepConsts &c, const float *phi, int i, int j, int k) {
+    if (i < 1 || j < 1 || k < 1 || i > c.I - 2 || j > c.J - 2 || k > c.K - 2) return false;
+    return phi[(long long)i + (long long)c.I * ((long long)j + (long long)c.J * k)] < 0.0f;
+}
+
+__global__ void k_flags(StepConsts c, const float *phi, uint8_t *fluid, int *levelRange) {
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    Dims d{c.I, c.J, c.K};
+    bool f = false;
+    int lv = 0;
+    if (t < d.size()) {
+        int i = (int)(t % c.I), j = (int)((t / c.I) % c.J), k = (int)(t / ((long long)c.I * c.J));
+        f = sys_cell(c, phi, i, j, k);
+        fluid[t] = f ? 1 : 0;
+        lv = i + j + k;
+    }
+    // warp-aggregated min/max/count of the system cells' levels
+    unsigned int m = __ballot_sync(0xffffffffu, f);
+    if (!m) return;
+    int lo = f ? lv : 0x7fffffff, hi = f ? lv : -1;
+    for (int o = 16; o > 0; o >>= 1) {
+        lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+        hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicMin(&levelRange[0], lo);
+        atomicMax(&levelRange[1], hi);
+        atomicAdd(&levelRange[2], __popc(m));
+    }
+}
+
+// One matrix row in FP64, as _calculateMatrixCoefficientsThread builds it
+// (pressuresolver.cpp:723-808).  Off-diagonal entries exist only towards
+// neighbours that are rows of the system; a liquid neighbour outside the
+// interior contributes neither an entry nor a ghost-fluid term (the
+// reference's key map drops it).
+__device__ double4 row_coeffs(const StepConsts &c, const float *phi, const float *wu, const float *wv,
+                              const float *ww, double mf, int i, int j, int k) {
+    Dims du{c.I + 1, c.J, c.K}, dv{c.I, c.J + 1, c.K}, dw{c.I, c.J, c.K + 1}, dc{c.I, c.J, c.K};
+    double vR = wu[du.idx(i + 1, j, k)], vL = wu[du.idx(i, j, k)];
+    double vT = wv[dv.idx(i, j + 1, k)], vB = wv[dv.idx(i, j, k)];
+    double vF = ww[dw.idx(i, j, k + 1)], vK = ww[dw.idx(i, j, k)];
+    double pc = phi[dc.idx(i, j, k)];
+    double diag = (vR + vL + vT + vB + vF + vK) * mf;
+    double xp = 0.0, yp = 0.0, zp = 0.0;
+    const double maxtheta = 25.0, eps = 1e-9;
+    const int nb[6][3] = {{i + 1, j, k}, {i - 1, j, k}, {i, j + 1, k}, {i, j - 1, k}, {i, j, k + 1}, {i, j, k - 1}};
+    const double vol[6] = {vR, vL, vT, vB, vF, vK};
+#pragma unroll
+    for (int q = 0; q < 6; q++) {
+        double pn = phi[dc.idx(nb[q][0], nb[q][1], nb[q][2])];
+        if (pn < 0.0) {
+            if (sys_cell(c, phi, nb[q][0], nb[q][1], nb[q][2])) {
+                if (q == 0) xp = -vol[q] * mf;
+                else if (q == 2) yp = -vol[q] * mf;
+                else if (q == 4) zp = -vol[q] * mf;
+            }
+        } else {
+            double theta = pn / (pc + eps);
+            theta = fmax(-maxtheta, fmin(theta, maxtheta));
+            diag -= vol[q] * mf * theta;
+        }
+    }
+    return make_double4(fmax(diag, 0.0), xp, yp, zp);
+}
+
+// RHS (pressuresolver.cpp:580-669; the domain walls do not move) and the rows.
+__global__ void k_build(StepConsts c, const float *phi, const float *wu, const float *wv, const float *ww,
+                        const float *u, const float *v, const float *w, double mf, PressureBuffers pb) {
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    Dims d{c.I, c.J, c.K};
+    double bmag = 0.0;
+    if (t < d.size()) {
+        pb.x[t] = 0.0;
+        pb.r[t] = 0.0;
+        pb.q[t] = 0.0;
+        pb.z[t] = 0.0f;
+        pb.s[t] = 0.0f;
+        pb.invdiagD[t] = 0.0;
+        pb.L[t] = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (!pb.fluid[t]) {
+            pb.Ad[t] = make_double4(0.0, 0.0, 0.0, 0.0);
+            pb.b[t] = 0.0;
+        } else {
+            int i = (int)(t % c.I), j = (int)((t / c.I) % c.J), k = (int)(t / ((long long)c.I * c.J));
+            Dims du{c.I + 1, c.J, c.K}, dv{c.I, c.J + 1, c.K}, dw{c.I, c.J, c.K + 1};
+            double vR = wu[du.idx(i + 1, j, k)], vL = wu[du.idx(i, j, k)];
+            double vT = wv[dv.idx(i, j + 1, k)], vB = wv[dv.idx(i, j, k)];
+            double vF = ww[dw.idx(i, j, k + 1)], vK = ww[dw.idx(i, j, k)];
+            double factor = 1.0 / c.dx;
+            double div = 0.0;
+            div += -factor * vR * (double)u[du.idx(i + 1, j, k)];
+            div += factor * vL * (double)u[du.idx(i, j, k)];
+            div += -factor * vT * (double)v[dv.idx(i, j + 1, k)];
+            div += factor * vB * (double)v[dv.idx(i, j, k)];
+            div += -factor * vF * (double)w[dw.idx(i, j, k + 1)];
+            div += factor * vK * (double)w[dw.idx(i, j, k)];
+            pb.b[t] = div;
+            bmag = fabs(div);
+            pb.Ad[t] = row_coeffs(c, phi, wu, wv, ww, mf, i, j, k);
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) bmag = fmax(bmag, __shfl_xor_sync(0xffffffffu, bmag, o));
+    if ((threadIdx.x & 31) == 0 && bmag > 0.0)
+        atomicMax((unsigned long long *)pb.scal + 2, (unsigned long long)__double_as_longlong(bmag));
+}
+
+// MIC(0) pivots of one wavefront i+j+k = level, FP64.  For 7-point rows the
+// column-oriented elimination of factorModifiedIncompleteColesky0 reduces to:
+//   d_c = A_cc - sum over earlier neighbours k (ascending index) of
+//         L_ck^2 + 0.97 L_ck (sum of k's other later-neighbour entries L_mk),
+//   L_mk = A_mk / sqrt(pivot_k); a pivot below 0.25 A_kk falls back to A_kk.
+__global__ void k_mic0_level(StepConsts c, const uint8_t *fluid, const double4 *Ad, double *invD, int level) {
+    int jj = blockIdx.x * blockDim.x + threadIdx.x;
+    int nj = c.J - 2, nk = c.K - 2;
+    if (jj >= nj * nk) return;
+    int j = 1 + jj % nj, k = 1 + jj / nj;
+    int i = level - j - k;
+    if (i < 1 || i > c.I - 2) return;
+    const long long sy = c.I, sz = (long long)c.I * c.J;
+    long long t = i + sy * j + sz * k;
+    if (!fluid[t]) return;
+    double ad = Ad[t].x;
+    double d = ad;
+    const long long back[3] = {t - sz, t - sy, t - 1};   // ascending: -z, -y, -x
+#pragma unroll
+    for (int q = 0; q < 3; q++) {
+        long long kk = back[q];
+        if (!fluid[kk]) continue;
+        double4 ak = Ad[kk];
+        if (ak.x == 0.0) continue;
+        double inv = invD[kk];
+        double Lck = (q == 0 ? ak.w : (q == 1 ? ak.z : ak.y)) * inv;
+        // k's later neighbours, ascending +x, +y, +z, without c itself
+        double miss = 0.0;
+        if (q != 2 && fluid[kk + 1]) miss += ak.y * inv;
+        if (q != 1 && fluid[kk + sy]) miss += ak.z * inv;
+        if (q != 0 && fluid[kk + sz]) miss += ak.w * inv;
+        d -= Lck * Lck;
+        d -= 0.97 * Lck * miss;
+    }
+    double inv;
+    if (ad == 0.0) inv = 0.0;
+    else if (d < 0.25 * ad) inv = 1 / sqrt(ad);
+    else inv = 1 / sqrt(d);
+    invD[t] = inv;
+}
+
+__global__ void k_mic0_finalize(long long n, const uint8_t *fluid, const double4 *Ad, const double *invD, float4 *L) {
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    double inv = invD[t];
+    if (!fluid[t] || inv == 0.0) {
+        L[t] = make_float4(0.f, 0.f, 0.f, 0.f);
+        return;
+    }
+    double4 a = Ad[t];
+    L[t] = make_float4((float)inv, (float)(a.y * inv), (float)(a.z * inv), (float)(a.w * inv));
+}
+
+template <class T>
+__device__ __forceinline__ T block_sum(T v, T *sh) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) sh[warp] = v;
+    __syncthreads();
+    T s = 0;
+    if (threadIdx.x == 0)
+        for (int q = 0; q < (int)(blockDim.x >> 5); q++) s += sh[q];
+    __syncthreads();
+    return s;
+}
+
+__device__ __forceinline__ void block_max_to(double v, unsigned long long *out) {
+    if (v != v) v = __longlong_as_double(0x7ff0000000000000ll);   // NaN never reads as converged
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    if ((threadIdx.x & 31) == 0 && v > 0.0) atomicMax(out, (unsigned long long)__double_as_longlong(v));
+}
+
+// q = A s (FP64), block partials of s.q
+__global__ void k_spmv(StepConsts c, const uint8_t *fluid, const double4 *Ad, const float *s, double *q,
+                       double *partials) {
+    __shared__ double sh[32];
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    long long n = (long long)c.I * c.J * c.K;
+    double part = 0.0;
+    if (t < n && fluid[t]) {
+        const long long sy = c.I, sz = (long long)c.I * c.J;
+        double4 a = Ad[t];
+        double acc = a.x * (double)s[t];
+        acc = fma(a.y, (double)s[t + 1], acc);
+        acc = fma(a.z, (double)s[t + sy], acc);
+        acc = fma(a.w, (double)s[t + sz], acc);
+        acc = fma(Ad[t - 1].y, (double)s[t - 1], acc);
+        acc = fma(Ad[t - sy].z, (double)s[t - sy], acc);
+        acc = fma(Ad[t - sz].w, (double)s[t - sz], acc);
+        q[t] = acc;
+        part = (double)s[t] * acc;
+    }
+    double b = block_sum(part, sh);
+    if (threadIdx.x == 0) partials[blockIdx.x] = b;
+}
+
+__global__ void k_dot_zr(long long n, const float *z, const double *r, double *partials) {
+    __shared__ double sh[32];
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    double part = t < n ? (double)z[t] * r[t] : 0.0;
+    double s = block_sum(part, sh);
+    if (threadIdx.x == 0) partials[blockIdx.x] = s;
+}
+
+// fixed-order sum of the block partials (deterministic)
+__global__ void k_sum_partials(const double *partials, int n, double *out) {
+    __shared__ double sh[32];
+    double v = 0.0;
+    for (int q = threadIdx.x; q < n; q += blockDim.x) v += partials[q];
+    double s = block_sum(v, sh);
+    if (threadIdx.x == 0) *out = s;
+}
+
+// x += alpha s, r -= alpha q with alpha = rho / s.q passed on as float, as
+// BLAS::addScaled(float alpha, ...) does (blaswrapper.h:129-158); |r|inf
+__global__ void k_update_xr(long long n, const uint8_t *fluid, double *x, double *r, const float *s,
+                            const double *q, const double *scal, unsigned long long *rmaxBits) {
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const double alpha = (double)(float)(scal[3] / scal[0]);
+    double m = 0.0;
+    if (t < n && fluid[t]) {
+        x[t] = fma(alpha, (double)s[t], x[t]);
+        double rv = fma(-alpha, q[t], r[t]);
+        r[t] = rv;
+        m = fabs(rv);
+    }
+    block_max_to(m, rmaxBits);
+}
+
+// r = b - A x (residual replacement); |r|inf
+__global__ void k_true_residual(StepConsts c, const uint8_t *fluid, const double4 *Ad, const double *b,
+                                const double *x, double *r, unsigned long long *rmaxBits) {
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    long long n = (long long)c.I * c.J * c.K;
+    double m = 0.0;
+    if (t < n && fluid[t]) {
+        const long long sy = c.I, sz = (long long)c.I * c.J;
+        double4 a = Ad[t];
+        double ax = a.x * x[t];
+        ax = fma(a.y, x[t + 1], ax);
+        ax = fma(a.z, x[t + sy], ax);
+        ax = fma(a.w, x[t + sz], ax);
+        ax = fma(Ad[t - 1].y, x[t - 1], ax);
+        ax = fma(Ad[t - sy].z, x[t - sy], ax);
+        ax = fma(Ad[t - sz].w, x[t - sz], ax);
+        double rv = b[t] - ax;
+        r[t] = rv;
+        m = fabs(rv);
+    }
+    block_max_to(m, rmaxBits);
+}
+
+__global__ void k_init_r(long long n, const double *b, double *r, unsigned long long *rmaxBits) {
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    double m = 0.0;
+    if (t < n) {
+        r[t] = b[t];
+        m = fabs(b[t]);
+    }
+    block_max_to(m, rmaxBits);
+}
+
+// s = z + beta s, beta = rho_new / rho as float (pcgsolver.h:295-298)
+__global__ void k_update_s(long long n, const uint8_t *fluid, const float *z, float *s, const double *scal) {
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const float beta = (float)(scal[1] / scal[3]);
+    if (t < n && fluid[t]) s[t] = __fmaf_rn(beta, s[t], z[t]);
+}
+
+__global__ void k_copy_zs(long long n, const float *z, float *s) {
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < n) s[t] = z[t];
+}
+
+__global__ void k_set_rho(double *scal) { scal[3] = scal[1]; }
+
+__global__ void k_x_to_float(long long n, const double *x, float *p) {
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < n) p[t] = (float)x[t];
+}
+
+// _applyPressureToVelocityFieldThread (pressuresolver.cpp:896-1046) without
+// surface tension.  Liquid means phi < 0 over all cells (FluidMaterialGrid,
+// :849-858); the faces i == 0 and i == I-1 (and the v/w analogues) are
+// skipped as the reference skips them.
+__global__ void k_apply_pressure(StepConsts c, const float *phi, const float *wu, const float *wv, const float *ww,
+                                 const float *P, float factor, float *u, float *v, float *w, uint8_t *vu,
+                                 uint8_t *vv, uint8_t *vw) {
+    long long nu = (long long)(c.I + 1) * c.J * c.K, nv = (long long)c.I * (c.J + 1) * c.K;
+    long long nw = (long long)c.I * c.J * (c.K + 1);
+    long long f = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= nu + nv + nw) return;
+    int dir = f < nu ? 0 : (f < nu + nv ? 1 : 2);
+    long long l = dir == 0 ? f : (dir == 1 ? f - nu : f - nu - nv);
+    int ni = c.I + (dir == 0), nj = c.J + (dir == 1);
+    int i = (int)(l % ni), j = (int)((l / ni) % nj), k = (int)(l / ((long long)ni * nj));
+    float *G = dir == 0 ? u : (dir == 1 ? v : w);
+    uint8_t *V = dir == 0 ? vu : (dir == 1 ? vv : vw);
+    const float *W = dir == 0 ? wu : (dir == 1 ? wv : ww);
+    V[l] = 0;
+    int g = dir == 0 ? i : (dir == 1 ? j : k);
+    int gmax = dir == 0 ? c.I : (dir == 1 ? c.J : c.K);
+    if (g == 0 || g == gmax - 1) return;
+    Dims dc{c.I, c.J, c.K};
+    int ai = i - (dir == 0), aj = j - (dir == 1), ak = k - (dir == 2);
+    bool fb = dc.in(i, j, k) && phi[dc.idx(i, j, k)] < 0.0f;
+    bool fa = phi[dc.idx(ai, aj, ak)] < 0.0f;
+    bool border = (g == gmax) ? fa : (fb || fa);
+    if (!(W[l] > 0.0f && border)) {
+        G[l] = 0.0f;
+        return;
+    }
+    float p1, p2;
+    const float eps = 1e-6f;
+    const double maxtheta = 25.0;
+    if (fa && fb) {
+        p1 = P[dc.idx(ai, aj, ak)];
+        p2 = P[dc.idx(i, j, k)];
+    } else {
+        float phi1 = phi[dc.idx(ai, aj, ak)], phi2 = phi[dc.idx(i, j, k)];
+        if (fa) {
+            float tp = (float)fmax(-maxtheta, fmin((double)__fdiv_rn(phi2, __fadd_rn(phi1, eps)), maxtheta));
+            p1 = P[dc.idx(ai, aj, ak)];
+            p2 = __fmul_rn(tp, p1);
+        } else {
+            float tp = (float)fmax(-maxtheta, fmin((double)__fdiv_rn(phi1, __fadd_rn(phi2, eps)), maxtheta));
+            p2 = P[dc.idx(i, j, k)];
+            p1 = __fmul_rn(tp, p2);
+        }
+    }
+    G[l] = __fadd_rn(G[l], __fmul_rn(-factor, __fsub_rn(p2, p1)));
+    V[l] = 1;
+}
+
+int cuda_fail(cudaError_t e, std::string *msg) {
+    if (msg) *msg = std::string("pressure solve: ") + cudaGetErrorString(e);
+    return FLIP_E_CUDA;
+}
+
+}  // namespace
+
+int pressure_partials(const StepConsts &c) { return (int)div_up((long long)c.I * c.J * c.K, TPB); }
+
+#define PCK(call)                                     \
+    do {                                              \
+        cudaError_t e_ = (call);                      \
+        if (e_ != cudaSuccess) return cuda_fail(e_, errMsg); \
+    } while (0)
+
+int pressure_project(const StepConsts &c, const PressureArgs &a, PressureBuffers &pb, SweepState &sw,
+                     PressureMail *mail, cudaStream_t s, PressureResult *res, std::string *errMsg) {
+    const long long n = (long long)c.I * c.J * c.K;
+    const unsigned nb = div_up(n, TPB);
+    const double mf = a.dt / (c.dx * c.dx);
+    res->iterations = 0;
+    res->residual = 0.0;
+    res->applied = false;
+    res->cells = 0;
+    auto sync = [&]() -> cudaError_t {
+        cudaError_t e = cudaStreamSynchronize(s);
+        return e != cudaSuccess ? e : cudaGetLastError();
+    };
+
+    int lr[3] = {0x7fffffff, -1, 0};
+    PCK(cudaMemcpyAsync(pb.levelRange, lr, sizeof(lr), cudaMemcpyHostToDevice, s));
+    PCK(cudaMemsetAsync(pb.scal, 0, 8 * sizeof(double), s));
+    { FLIP_COUNT(1); k_flags<<<nb, TPB, 0, s>>>(c, a.phi, pb.fluid, pb.levelRange); }
+    { FLIP_COUNT(1); k_build<<<nb, TPB, 0, s>>>(c, a.phi, a.wu, a.wv, a.ww, a.u, a.v, a.w, mf, pb); }
+    PCK(cudaMemcpyAsync(mail->levelRange, pb.levelRange, 3 * sizeof(int), cudaMemcpyDeviceToHost, s));
+    PCK(cudaMemcpyAsync(&mail->bmax, pb.scal + 2, sizeof(double), cudaMemcpyDeviceToHost, s));
+    PCK(sync());
+    if (a.dumpRhs) PCK(cudaMemcpy(a.dumpRhs, pb.b, n * sizeof(double), cudaMemcpyDeviceToHost));
+    const int lo = mail->levelRange[0], hi = mail->levelRange[1];
+    res->cells = mail->levelRange[2];
+    const double bmax = mail->bmax;
+    if (hi < lo || bmax < a.tol) {   // no system, or nothing to project (pressuresolver.cpp:53-56)
+        if (a.dumpPressure) std::memset(a.dumpPressure, 0, n * sizeof(float));
+        return FLIP_OK;
+    }
+    const double ptol = fmax(a.tol, 1e-30) * bmax;
+
+    // MIC(0) factor, one launch per wavefront
+    const int np = (c.J - 2) * (c.K - 2);
+    for (int lv = lo; lv <= hi; lv++) {
+        FLIP_COUNT(1);
+        k_mic0_level<<<div_up(np, TPB), TPB, 0, s>>>(c, pb.fluid, pb.Ad, pb.invdiagD, lv);
+    }
+    { FLIP_COUNT(1); k_mic0_finalize<<<nb, TPB, 0, s>>>(n, pb.fluid, pb.Ad, pb.invdiagD, pb.L); }
+    launch_sweep_ranges(c, pb.fluid, sw, s);
+
+    unsigned long long *rmax = pb.rmaxBits;
+    auto read_rmax = [&](double *out, int *sweepErr) -> cudaError_t {
+        cudaError_t e = cudaMemcpyAsync(&mail->rmaxBits, rmax, sizeof(unsigned long long), cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(&mail->sweepErr, sw.err, sizeof(int), cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = sync();
+        if (e != cudaSuccess) return e;
+        std::memcpy(out, &mail->rmaxBits, sizeof(double));
+        *sweepErr = mail->sweepErr;
+        return cudaSuccess;
+    };
+    auto precondition = [&]() {
+        launch_sweeps(c, pb.L, pb.r, pb.z, sw, s);
+        { FLIP_COUNT(1); k_dot_zr<<<nb, TPB, 0, s>>>(n, pb.z, pb.r, pb.partials); }
+        { FLIP_COUNT(1); k_sum_partials<<<1, 1024, 0, s>>>(pb.partials, pb.nPartials, pb.scal + 1); }
+    };
+    auto residual = [&]() {
+        PCK(cudaMemsetAsync(rmax, 0, sizeof(unsigned long long), s));
+        { FLIP_COUNT(1); k_true_residual<<<nb, TPB, 0, s>>>(c, pb.fluid, pb.Ad, pb.b, pb.x, pb.r, rmax); }
+        return FLIP_OK;
+    };
+
+    PCK(cudaMemsetAsync(rmax, 0, sizeof(unsigned long long), s));
+    { FLIP_COUNT(1); k_init_r<<<nb, TPB, 0, s>>>(n, pb.b, pb.r, rmax); }
+    precondition();
+    PCK(cudaMemcpyAsync(&mail->rho, pb.scal + 1, sizeof(double), cudaMemcpyDeviceToHost, s));
+    PCK(sync());
+    const double rho0 = mail->rho;
+    bool ok = false;
+    int iterations = 0;
+    double resid = bmax;
+    int sweepErr = 0;
+    if (!(rho0 == 0 || rho0 != rho0)) {
+        { FLIP_COUNT(1); k_copy_zs<<<nb, TPB, 0, s>>>(n, pb.z, pb.s); }
+        { FLIP_COUNT(1); k_set_rho<<<1, 1, 0, s>>>(pb.scal); }
+        int it;
+        for (it = 0; it < a.maxIter; it++) {
+            { FLIP_COUNT(1); k_spmv<<<nb, TPB, 0, s>>>(c, pb.fluid, pb.Ad, pb.s, pb.q, pb.partials); }
+            { FLIP_COUNT(1); k_sum_partials<<<1, 1024, 0, s>>>(pb.partials, pb.nPartials, pb.scal + 0); }
+            PCK(cudaMemsetAsync(rmax, 0, sizeof(unsigned long long), s));
+            { FLIP_COUNT(1); k_update_xr<<<nb, TPB, 0, s>>>(n, pb.fluid, pb.x, pb.r, pb.s, pb.q, pb.scal, rmax); }
+            const bool periodic = (it + 1) % 25 == 0;
+            if (periodic) residual();
+            PCK(read_rmax(&resid, &sweepErr));
+            if (sweepErr) break;
+            if (resid <= ptol && !periodic) {   // confirm on b - A x
+                residual();
+                PCK(read_rmax(&resid, &sweepErr));
+                if (sweepErr) break;
+            }
+            if (resid <= ptol) {
+                iterations = it + 1;
+                ok = true;
+                break;
+            }
+            precondition();
+            { FLIP_COUNT(1); k_update_s<<<nb, TPB, 0, s>>>(n, pb.fluid, pb.z, pb.s, pb.scal); }
+            { FLIP_COUNT(1); k_set_rho<<<1, 1, 0, s>>>(pb.scal); }
+        }
+        if (!ok) iterations = it;
+    }
+    if (sweepErr) {
+        int ntj, ntk;
+        cudaMemsetAsync(sw.err, 0, sizeof(int), s);
+        cudaMemsetAsync(sw.progress, 0, sweep_tiles(c.J, c.K, &ntj, &ntk) * sizeof(unsigned int), s);
+        sw.epoch = 0;
+        sync();
+        if (errMsg) *errMsg = "a wavefront sweep gave up waiting for a neighbouring tile";
+        return FLIP_E_DEVICE_TIMEOUT;
+    }
+    res->iterations = iterations;
+    res->residual = resid;
+    const bool accept = ok || (iterations == a.maxIter && resid < a.accTol);   // pressuresolver.cpp:810-840
+    { FLIP_COUNT(1); k_x_to_float<<<nb, TPB, 0, s>>>(n, pb.x, pb.pressure); }
+    if (a.dumpPressure) {
+        PCK(sync());
+        PCK(cudaMemcpy(a.dumpPressure, pb.pressure, n * sizeof(float), cudaMemcpyDeviceToHost));
+    }
+    if (!accept) return FLIP_E_SOLVER_NOCONV;
+    long long tot = (long long)(c.I + 1) * c.J * c.K + (long long)c.I * (c.J + 1) * c.K + (long long)c.I * c.J * (c.K + 1);
+    float factor = (float)(a.dt / c.dx);
+    { FLIP_COUNT(1); k_apply_pressure<<<div_up(tot, TPB), TPB, 0, s>>>(c, a.phi, a.wu, a.wv, a.ww, pb.pressure, factor,
+                                                                    a.u, a.v, a.w, a.vu, a.vv, a.vw); }
+    res->applied = true;
+    return FLIP_OK;
+}
+
+}  // namespace flip
