@@ -82,6 +82,7 @@ struct PressureBuffers {
     float4 *L;             // {invdiag, Lx, Ly, Lz} for the FP32 sweeps
     double *x, *r, *q;     // solution, residual, A s
     float *z, *s;          // preconditioned residual, search direction
+    float *rf;             // r rounded to FP32, the forward sweep's right-hand side
     double *partials;      // per-block partial sums (deterministic reduction)
     double *scal;          // [0]=s.q [1]=z.r (new rho) [2]=|b|inf [3]=rho
     unsigned long long *rmaxBits;  // |r|inf as double bits
@@ -114,16 +115,17 @@ struct PressureResult {
 // Pipelined wavefront sweeps (flip_sweep.cu)
 struct SweepState {
     int2 *range;             // per tile [first, last] step holding a system cell
-    unsigned int *progress;  // per tile progress word
+    unsigned long long *xchg;  // tile edge exchange words {epoch, value}
     unsigned int *ticket;    // tile ticket counter
     int *err;                // set when a bounded wait gave up
     unsigned int epoch;
     long long launches;
 };
 int sweep_tiles(int J, int K, int *ntj, int *ntk);
+long long sweep_exchange_words(int I, int J, int K);
 void launch_sweep_ranges(const StepConsts &c, const uint8_t *fluid, SweepState &sw, cudaStream_t s);
 // z = M^-1 r with the MIC(0) factor L: forward then backward sweep
-void launch_sweeps(const StepConsts &c, const float4 *L, const double *r, float *z, SweepState &sw, cudaStream_t s);
+void launch_sweeps(const StepConsts &c, const float4 *L, const float *rf, float *z, SweepState &sw, cudaStream_t s);
 
 int pressure_partials(const StepConsts &c);
 // PressureSolver::solve (pressuresolver.cpp:44-76) on the device.  Returns
@@ -132,4 +134,12 @@ int pressure_partials(const StepConsts &c);
 int pressure_project(const StepConsts &c, const PressureArgs &a, PressureBuffers &pb, SweepState &sw,
                      PressureMail *mail, cudaStream_t s, PressureResult *res, std::string *errMsg);
 
+}  // namespace flip
+
+namespace flip {
+// Packed xyz positions/velocities (either may be null) of the n particles in
+// the reference's order; flags/rank hold idSpace+1 ints, scratch
+// scan_scratch_ints(idSpace) ints.
+void launch_readback_order(const ParticleSoA &p, int n, int idSpace, int *flags, int *rank, int *scratch,
+                           int *total, float *pos, float *vel, cudaStream_t s);
 }  // namespace flip

@@ -84,6 +84,8 @@ struct flip_ctx {
     // device buffers
     ParticleSoA pa{}, pb{};
     unsigned int *keys = nullptr;
+    int idSpace = 0;   // ids are ranks in the load order, below idSpace
+    int *idFlags = nullptr, *idRank = nullptr, *idScratch = nullptr, *idTotal = nullptr;
     int *cellCount = nullptr, *cellStart = nullptr, *cursor = nullptr, *slots = nullptr;
     int *survivors = nullptr, *newStart = nullptr, *scanScratch = nullptr, *scanTotal = nullptr;
     float *phi = nullptr, *solidPhi = nullptr, *wu = nullptr, *wv = nullptr, *ww = nullptr;
@@ -179,7 +181,7 @@ int alloc_grids(flip_ctx *x) {
     if ((rc = x->alloc(&p.fluid, nc)) || (rc = x->alloc(&p.Ad, nc)) || (rc = x->alloc(&p.L, nc)) ||
         (rc = x->alloc(&p.b, nc)) || (rc = x->alloc(&p.invdiagD, nc)) || (rc = x->alloc(&p.x, nc)) ||
         (rc = x->alloc(&p.r, nc)) || (rc = x->alloc(&p.q, nc)) || (rc = x->alloc(&p.z, nc)) ||
-        (rc = x->alloc(&p.s, nc)) || (rc = x->alloc(&p.pressure, nc)))
+        (rc = x->alloc(&p.s, nc)) || (rc = x->alloc(&p.rf, nc)) || (rc = x->alloc(&p.pressure, nc)))
         return rc;
     p.nPartials = pressure_partials(x->c);
     if ((rc = x->alloc(&p.partials, p.nPartials + 32)) || (rc = x->alloc(&p.scal, 8)) ||
@@ -188,10 +190,11 @@ int alloc_grids(flip_ctx *x) {
     {
         int ntj, ntk;
         int nt = sweep_tiles(x->J, x->K, &ntj, &ntk);
-        if ((rc = x->alloc(&x->sweep.range, nt)) || (rc = x->alloc(&x->sweep.progress, nt)) ||
+        long long nw = sweep_exchange_words(x->I, x->J, x->K);
+        if ((rc = x->alloc(&x->sweep.range, nt)) || (rc = x->alloc(&x->sweep.xchg, nw)) ||
             (rc = x->alloc(&x->sweep.ticket, 4)) || (rc = x->alloc(&x->sweep.err, 4)))
             return rc;
-        CK(cudaMemsetAsync(x->sweep.progress, 0, nt * sizeof(unsigned int), x->stream));
+        CK(cudaMemsetAsync(x->sweep.xchg, 0, nw * sizeof(unsigned long long), x->stream));
         CK(cudaMemsetAsync(x->sweep.err, 0, 4 * sizeof(int), x->stream));
     }
     {
@@ -226,14 +229,19 @@ int alloc_grids(flip_ctx *x) {
 int alloc_particles(flip_ctx *x, int cap) {
     int rc;
     x->capacity = cap;
+    x->idSpace = cap;
     ParticleSoA *bufs[2] = {&x->pa, &x->pb};
-    for (ParticleSoA *b : bufs) {
-        if ((rc = x->alloc(&b->px, cap)) || (rc = x->alloc(&b->py, cap)) || (rc = x->alloc(&b->pz, cap)) ||
-            (rc = x->alloc(&b->vx, cap)) || (rc = x->alloc(&b->vy, cap)) || (rc = x->alloc(&b->vz, cap)) ||
-            (rc = x->alloc(&b->id, cap)))
-            return rc;
+    for (ParticleSoA *b : bufs) {   // one block per buffer: 6 float planes then the ids
+        float *base;
+        if ((rc = x->alloc(&base, 7 * (size_t)cap))) return rc;
+        b->px = base; b->py = base + cap; b->pz = base + 2 * (size_t)cap;
+        b->vx = base + 3 * (size_t)cap; b->vy = base + 4 * (size_t)cap; b->vz = base + 5 * (size_t)cap;
+        b->id = (unsigned int *)(base + 6 * (size_t)cap);
     }
     if ((rc = x->alloc(&x->keys, cap)) || (rc = x->alloc(&x->slots, cap))) return rc;
+    if ((rc = x->alloc(&x->idFlags, cap + 1)) || (rc = x->alloc(&x->idRank, cap + 1)) ||
+        (rc = x->alloc(&x->idScratch, scan_scratch_ints(cap) + 4)) || (rc = x->alloc(&x->idTotal, 4)))
+        return rc;
     return FLIP_OK;
 }
 
@@ -318,26 +326,24 @@ void dl(flip_ctx *x, T *dst, const T *src, long long count) {
 }
 
 // Particles of the current arrays in the reference's order (by id).
-int particles_in_order(flip_ctx *x, std::vector<float> *pos, std::vector<float> *vel) {
+// Particles [start, end) of the reference's order into host memory (packed
+// xyz), reordered on the device: the idle particle buffer is the staging area.
+int particles_to_host(flip_ctx *x, float *pos, float *vel, int start, int end) {
     int n = x->n;
-    std::vector<float> px(n), py(n), pz(n), vx(n), vy(n), vz(n);
-    std::vector<unsigned int> id(n);
-    dl(x, px.data(), x->pa.px, n); dl(x, py.data(), x->pa.py, n); dl(x, pz.data(), x->pa.pz, n);
-    dl(x, vx.data(), x->pa.vx, n); dl(x, vy.data(), x->pa.vy, n); dl(x, vz.data(), x->pa.vz, n);
-    dl(x, id.data(), x->pa.id, n);
-    int rc = sync(x);
-    if (rc) return rc;
-    std::vector<int> order(n);
-    for (int q = 0; q < n; q++) order[q] = q;
-    std::sort(order.begin(), order.end(), [&](int a, int b) { return id[a] < id[b]; });
-    if (pos) pos->resize(3 * (size_t)n);
-    if (vel) vel->resize(3 * (size_t)n);
-    for (int q = 0; q < n; q++) {
-        int o = order[q];
-        if (pos) { (*pos)[3 * q] = px[o]; (*pos)[3 * q + 1] = py[o]; (*pos)[3 * q + 2] = pz[o]; }
-        if (vel) { (*vel)[3 * q] = vx[o]; (*vel)[3 * q + 1] = vy[o]; (*vel)[3 * q + 2] = vz[o]; }
-    }
-    return FLIP_OK;
+    if (n == 0 || end <= start) return FLIP_OK;
+    float *dpos = x->pb.px, *dvel = x->pb.px + 3 * (size_t)x->capacity;
+    launch_readback_order(x->pa, n, x->idSpace, x->idFlags, x->idRank, x->idScratch, x->idTotal,
+                          pos ? dpos : nullptr, vel ? dvel : nullptr, x->stream);
+    size_t off = 3 * (size_t)start, bytes = 3 * (size_t)(end - start) * sizeof(float);
+    if (pos) CK(cudaMemcpyAsync(pos, dpos + off, bytes, cudaMemcpyDeviceToHost, x->stream));
+    if (vel) CK(cudaMemcpyAsync(vel, dvel + off, bytes, cudaMemcpyDeviceToHost, x->stream));
+    return sync(x);
+}
+
+int particles_in_order(flip_ctx *x, std::vector<float> *pos, std::vector<float> *vel) {
+    if (pos) pos->resize(3 * (size_t)x->n);
+    if (vel) vel->resize(3 * (size_t)x->n);
+    return particles_to_host(x, pos ? pos->data() : nullptr, vel ? vel->data() : nullptr, 0, x->n);
 }
 
 // PressureSolver::solve (pressuresolver.cpp:44-76) on the device: FLIP_OK
@@ -741,28 +747,16 @@ int flip_get_num_marker_particles(flip_ctx *x, int *n) {
 }
 int flip_get_marker_particle_position_data(flip_ctx *x, float *out) {
     if (!x || !out) return FLIP_E_NULL;
-    std::vector<float> pos;
-    int rc = particles_in_order(x, &pos, nullptr);
-    if (rc) return rc;
-    std::memcpy(out, pos.data(), pos.size() * 4);
-    return FLIP_OK;
+    return particles_to_host(x, out, nullptr, 0, x->n);
 }
 int flip_get_marker_particle_velocity_data(flip_ctx *x, float *out) {
     if (!x || !out) return FLIP_E_NULL;
-    std::vector<float> vel;
-    int rc = particles_in_order(x, nullptr, &vel);
-    if (rc) return rc;
-    std::memcpy(out, vel.data(), vel.size() * 4);
-    return FLIP_OK;
+    return particles_to_host(x, nullptr, out, 0, x->n);
 }
 static int range_get(flip_ctx *x, int start, int end, float *out, bool vel) {
     if (!x || !out) return FLIP_E_NULL;
     if (start < 0 || end > x->n || start > end) return fail(FLIP_E_DOMAIN, "Error: invalid range.");
-    std::vector<float> a;
-    int rc = vel ? particles_in_order(x, nullptr, &a) : particles_in_order(x, &a, nullptr);
-    if (rc) return rc;
-    std::memcpy(out, a.data() + 3 * (size_t)start, 3 * (size_t)(end - start) * 4);
-    return FLIP_OK;
+    return vel ? particles_to_host(x, nullptr, out, start, end) : particles_to_host(x, out, nullptr, start, end);
 }
 int flip_get_marker_particle_position_data_range(flip_ctx *x, int start, int end, float *out) {
     return range_get(x, start, end, out, false);

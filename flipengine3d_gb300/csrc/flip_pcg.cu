@@ -7,7 +7,7 @@
 // Preconditioner: the reference's MIC(0) (pcgsolver.h:70-185, tau 0.97,
 // pivot floor 0.25) restated for 7-point rows; the factorisation runs as an
 // i+j+k wavefront in FP64 and the two triangular sweeps as the pipelined
-// FP32 wavefront of flip_sweep.cu.  CG (pcgsolver.h:248-302): the
+// FP32 wavefront of flip_wavefront.cu.  CG (pcgsolver.h:248-302): the
 // Laplacian apply, the solution, the residual and the dot products are
 // FP64, so the recurrence tracks b - A x to FP64 rounding; the FP32 parts
 // (preconditioner, search direction) only steer the iteration.  Every 25
@@ -102,6 +102,7 @@ __global__ void k_build(StepConsts c, const float *phi, const float *wu, const f
     if (t < d.size()) {
         pb.x[t] = 0.0;
         pb.r[t] = 0.0;
+        pb.rf[t] = 0.0f;
         pb.q[t] = 0.0;
         pb.z[t] = 0.0f;
         pb.s[t] = 0.0f;
@@ -249,7 +250,7 @@ __global__ void k_sum_partials(const double *partials, int n, double *out) {
 
 // x += alpha s, r -= alpha q with alpha = rho / s.q passed on as float, as
 // BLAS::addScaled(float alpha, ...) does (blaswrapper.h:129-158); |r|inf
-__global__ void k_update_xr(long long n, const uint8_t *fluid, double *x, double *r, const float *s,
+__global__ void k_update_xr(long long n, const uint8_t *fluid, double *x, double *r, float *rf, const float *s,
                             const double *q, const double *scal, unsigned long long *rmaxBits) {
     long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const double alpha = (double)(float)(scal[3] / scal[0]);
@@ -258,6 +259,7 @@ __global__ void k_update_xr(long long n, const uint8_t *fluid, double *x, double
         x[t] = fma(alpha, (double)s[t], x[t]);
         double rv = fma(-alpha, q[t], r[t]);
         r[t] = rv;
+        rf[t] = (float)rv;
         m = fabs(rv);
     }
     block_max_to(m, rmaxBits);
@@ -265,7 +267,7 @@ __global__ void k_update_xr(long long n, const uint8_t *fluid, double *x, double
 
 // r = b - A x (residual replacement); |r|inf
 __global__ void k_true_residual(StepConsts c, const uint8_t *fluid, const double4 *Ad, const double *b,
-                                const double *x, double *r, unsigned long long *rmaxBits) {
+                                const double *x, double *r, float *rf, unsigned long long *rmaxBits) {
     long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     long long n = (long long)c.I * c.J * c.K;
     double m = 0.0;
@@ -281,16 +283,18 @@ __global__ void k_true_residual(StepConsts c, const uint8_t *fluid, const double
         ax = fma(Ad[t - sz].w, x[t - sz], ax);
         double rv = b[t] - ax;
         r[t] = rv;
+        rf[t] = (float)rv;
         m = fabs(rv);
     }
     block_max_to(m, rmaxBits);
 }
 
-__global__ void k_init_r(long long n, const double *b, double *r, unsigned long long *rmaxBits) {
+__global__ void k_init_r(long long n, const double *b, double *r, float *rf, unsigned long long *rmaxBits) {
     long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     double m = 0.0;
     if (t < n) {
         r[t] = b[t];
+        rf[t] = (float)b[t];
         m = fabs(b[t]);
     }
     block_max_to(m, rmaxBits);
@@ -435,18 +439,18 @@ int pressure_project(const StepConsts &c, const PressureArgs &a, PressureBuffers
         return cudaSuccess;
     };
     auto precondition = [&]() {
-        launch_sweeps(c, pb.L, pb.r, pb.z, sw, s);
+        launch_sweeps(c, pb.L, pb.rf, pb.z, sw, s);
         { FLIP_COUNT(1); k_dot_zr<<<nb, TPB, 0, s>>>(n, pb.z, pb.r, pb.partials); }
         { FLIP_COUNT(1); k_sum_partials<<<1, 1024, 0, s>>>(pb.partials, pb.nPartials, pb.scal + 1); }
     };
     auto residual = [&]() {
         PCK(cudaMemsetAsync(rmax, 0, sizeof(unsigned long long), s));
-        { FLIP_COUNT(1); k_true_residual<<<nb, TPB, 0, s>>>(c, pb.fluid, pb.Ad, pb.b, pb.x, pb.r, rmax); }
+        { FLIP_COUNT(1); k_true_residual<<<nb, TPB, 0, s>>>(c, pb.fluid, pb.Ad, pb.b, pb.x, pb.r, pb.rf, rmax); }
         return FLIP_OK;
     };
 
     PCK(cudaMemsetAsync(rmax, 0, sizeof(unsigned long long), s));
-    { FLIP_COUNT(1); k_init_r<<<nb, TPB, 0, s>>>(n, pb.b, pb.r, rmax); }
+    { FLIP_COUNT(1); k_init_r<<<nb, TPB, 0, s>>>(n, pb.b, pb.r, pb.rf, rmax); }
     precondition();
     PCK(cudaMemcpyAsync(&mail->rho, pb.scal + 1, sizeof(double), cudaMemcpyDeviceToHost, s));
     PCK(sync());
@@ -463,7 +467,7 @@ int pressure_project(const StepConsts &c, const PressureArgs &a, PressureBuffers
             { FLIP_COUNT(1); k_spmv<<<nb, TPB, 0, s>>>(c, pb.fluid, pb.Ad, pb.s, pb.q, pb.partials); }
             { FLIP_COUNT(1); k_sum_partials<<<1, 1024, 0, s>>>(pb.partials, pb.nPartials, pb.scal + 0); }
             PCK(cudaMemsetAsync(rmax, 0, sizeof(unsigned long long), s));
-            { FLIP_COUNT(1); k_update_xr<<<nb, TPB, 0, s>>>(n, pb.fluid, pb.x, pb.r, pb.s, pb.q, pb.scal, rmax); }
+            { FLIP_COUNT(1); k_update_xr<<<nb, TPB, 0, s>>>(n, pb.fluid, pb.x, pb.r, pb.rf, pb.s, pb.q, pb.scal, rmax); }
             const bool periodic = (it + 1) % 25 == 0;
             if (periodic) residual();
             PCK(read_rmax(&resid, &sweepErr));
@@ -485,9 +489,8 @@ int pressure_project(const StepConsts &c, const PressureArgs &a, PressureBuffers
         if (!ok) iterations = it;
     }
     if (sweepErr) {
-        int ntj, ntk;
         cudaMemsetAsync(sw.err, 0, sizeof(int), s);
-        cudaMemsetAsync(sw.progress, 0, sweep_tiles(c.J, c.K, &ntj, &ntk) * sizeof(unsigned int), s);
+        cudaMemsetAsync(sw.xchg, 0, sweep_exchange_words(c.I, c.J, c.K) * sizeof(unsigned long long), s);
         sw.epoch = 0;
         sync();
         if (errMsg) *errMsg = "a wavefront sweep gave up waiting for a neighbouring tile";
