@@ -1,0 +1,148 @@
+// FluidSimulation.hpp -- header-only C++ face of libflip3d_gb300.so.
+//
+// The same class name, constructor and method names as the reference's
+// FluidSimulation (src/engine/fluidsimulation.h:117-1130) for the calls its
+// driver makes on the FLIP step (src/FluidManager.cpp:9-13,47-84), so a
+// caller can switch by changing the include and the namespace.  Status
+// codes of the C ABI come back as the exception types the reference throws:
+// std::runtime_error (update before initialize, fluidsimulation.cpp:5756),
+// std::domain_error (bad arguments, :1891-1896, :5761-5765) and
+// std::out_of_range (bad readback range, :2058-2063).  The reference leaves
+// a failed pressure solve silent; here it is reported in
+// getFrameStatsData().pressureStatus and update() does not throw for it.
+// CUDA failures and bounded device waits that gave up throw flip3d::Error.
+#ifndef FLIP3D_FLUIDSIMULATION_HPP
+#define FLIP3D_FLUIDSIMULATION_HPP
+
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "flip3d.h"
+
+namespace flip3d {
+
+struct Error : std::runtime_error {
+    int code;
+    Error(int c, const std::string &m) : std::runtime_error(m), code(c) {}
+};
+
+inline void check(int rc) {
+    if (rc == FLIP_OK) return;
+    std::string msg = flip_last_error();
+    switch (rc) {
+        case FLIP_E_RUNTIME: throw std::runtime_error(msg);
+        case FLIP_E_DOMAIN: throw std::domain_error(msg);
+        case FLIP_E_OUT_OF_RANGE: throw std::out_of_range(msg);
+        default: throw Error(rc, msg);
+    }
+}
+
+// fluidsimulation.h:102-106: size entries of 3 floats (12 bytes) each
+struct FluidSimulationMarkerParticleData {
+    int size = 0;
+    char *positions = nullptr;
+    char *velocities = nullptr;
+};
+
+// the part of FluidSimulationFrameStats (fluidsimulation.h:78-100) the FLIP step produces
+struct FluidSimulationFrameStats {
+    int frame = 0;
+    int substeps = 0;
+    double deltaTime = 0.0;
+    int fluidParticles = 0;
+    int pressureIterations = 0;
+    double pressureError = 0.0;
+    int pressureStatus = FLIP_OK;
+};
+
+// Surface reconstruction is not part of this library: getIsomesh() returns
+// an empty mesh, as the reference does with reconstruction disabled.
+struct TriangleMesh {
+    std::vector<float> vertices;
+    std::vector<int> triangles;
+};
+
+class FluidSimulation {
+public:
+    FluidSimulation(int isize, int jsize, int ksize, double dx) { check(flip_create(isize, jsize, ksize, dx, &ctx_)); }
+    ~FluidSimulation() { flip_destroy(ctx_); }
+    FluidSimulation(const FluidSimulation &) = delete;
+    FluidSimulation &operator=(const FluidSimulation &) = delete;
+
+    void initialize() { check(flip_initialize(ctx_)); }
+    bool isInitialized() {
+        int v = 0;
+        check(flip_is_initialized(ctx_, &v));
+        return v != 0;
+    }
+    void update(double dt) {
+        int rc = flip_update(ctx_, dt);
+        if (rc != FLIP_E_SOLVER_NOCONV) check(rc);
+    }
+    int getCurrentFrame() {
+        int f = 0;
+        check(flip_get_current_frame(ctx_, &f));
+        return f;
+    }
+    void addBodyForce(double fx, double fy, double fz) { check(flip_add_body_force(ctx_, fx, fy, fz)); }
+    void resetBodyForce() { check(flip_reset_body_force(ctx_)); }
+    void setCFLConditionNumber(int n) { check(flip_set_cfl_condition_number(ctx_, n)); }
+    void setPICFLIPRatio(double r) { check(flip_set_pic_flip_ratio(ctx_, r)); }
+    double getPICFLIPRatio() {
+        double r = 0.0;
+        check(flip_get_pic_flip_ratio(ctx_, &r));
+        return r;
+    }
+    // No effect: the step runs on the GPU; kept for drivers that call them.
+    void setMaxThreadCount(int) {}
+    void disableSurfaceReconstruction() {}
+    TriangleMesh &getIsomesh() { return mesh_; }
+
+    void loadMarkerParticleData(FluidSimulationMarkerParticleData data) {
+        check(flip_load_marker_particle_data(ctx_, data.size, reinterpret_cast<const float *>(data.positions),
+                                             reinterpret_cast<const float *>(data.velocities)));
+    }
+    unsigned int getNumMarkerParticles() {
+        int n = 0;
+        check(flip_get_num_marker_particles(ctx_, &n));
+        return (unsigned int)n;
+    }
+    unsigned int getMarkerParticlePositionDataSize() { return 3 * sizeof(float) * getNumMarkerParticles(); }
+    unsigned int getMarkerParticleVelocityDataSize() { return 3 * sizeof(float) * getNumMarkerParticles(); }
+    void getMarkerParticlePositionData(char *data) {
+        check(flip_get_marker_particle_position_data(ctx_, reinterpret_cast<float *>(data)));
+    }
+    void getMarkerParticleVelocityData(char *data) {
+        check(flip_get_marker_particle_velocity_data(ctx_, reinterpret_cast<float *>(data)));
+    }
+    void getMarkerParticlePositionDataRange(int start, int end, char *data) {
+        check(flip_get_marker_particle_position_data_range(ctx_, start, end, reinterpret_cast<float *>(data)));
+    }
+    void getMarkerParticleVelocityDataRange(int start, int end, char *data) {
+        check(flip_get_marker_particle_velocity_data_range(ctx_, start, end, reinterpret_cast<float *>(data)));
+    }
+    FluidSimulationFrameStats getFrameStatsData() {
+        flip_frame_stats s{};
+        check(flip_get_frame_stats(ctx_, &s));
+        FluidSimulationFrameStats o;
+        o.frame = s.frame;
+        o.substeps = s.substeps;
+        o.deltaTime = s.delta_time;
+        o.fluidParticles = s.fluid_particles;
+        o.pressureIterations = s.pressure_iterations;
+        o.pressureError = s.pressure_error;
+        o.pressureStatus = s.pressure_status;
+        return o;
+    }
+
+    flip_ctx *handle() { return ctx_; }
+
+private:
+    flip_ctx *ctx_ = nullptr;
+    TriangleMesh mesh_;
+};
+
+}  // namespace flip3d
+
+#endif
