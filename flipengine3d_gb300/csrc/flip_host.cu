@@ -582,6 +582,10 @@ int do_initialize(flip_ctx *x) {
 
 }  // namespace
 
+namespace flip {
+int record_error(int code, const std::string &msg) { return fail(code, msg); }
+}  // namespace flip
+
 // ====================================================================== C ABI
 extern "C" {
 

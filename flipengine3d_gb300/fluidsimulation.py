@@ -86,6 +86,7 @@ SIGNATURES = {
     "flip_set_stage_timing": [_P, _I],
     "flip_get_stage_times": [_P, _P, C.POINTER(C.c_longlong)],
     "flip_get_launch_count": [_P, C.POINTER(C.c_longlong)],
+    "flip_order_particles_by_id_noalloc": [_P, _P, _P, _P, _I, _I, _P, _P],
 }
 
 
@@ -144,6 +145,21 @@ def compute_domain_solid(isize, jsize, ksize, dx, cfl=5):
     _check(lib, lib.flip_compute_domain_solid(I, J, K, dx, cfl, _ptr(nodal), _ptr(wu), _ptr(wv), _ptr(ww),
                                               _ptr(dims), _ptr(near)))
     return nodal, (wu, wv, ww), near
+
+
+def order_particles_by_id_noalloc(d_px: int, d_py: int, d_pz: int, d_ids: int, n: int, id_space: int,
+                                  d_out_xyz: int, cuda_stream_handle: int = 0) -> None:
+    """Positions of n particles, in ascending id order, into caller memory
+    (3*n floats, packed xyz); the library allocates nothing.  All pointers
+    are device addresses (int); ids are distinct unsigned 32-bit values below
+    id_space <= FLIP_NOALLOC_MAX_IDS.  Runs on the given stream."""
+    lib = load_library()
+    _check(lib, lib.flip_order_particles_by_id_noalloc(C.c_void_p(d_px), C.c_void_p(d_py), C.c_void_p(d_pz),
+                                                       C.c_void_p(d_ids), int(n), int(id_space),
+                                                       C.c_void_p(d_out_xyz), C.c_void_p(cuda_stream_handle)))
+
+
+FLIP_NOALLOC_MAX_IDS = 1 << 20
 
 
 class FluidSimulation:

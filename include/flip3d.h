@@ -175,6 +175,29 @@ int flip_get_stage_times(flip_ctx *ctx, double *ms, long long *substeps);
 /* Number of this library's kernel launches issued so far on the context. */
 int flip_get_launch_count(flip_ctx *ctx, long long *count);
 
+/* Particle positions in ascending id order, written into caller memory,
+ * with no allocation by the library.  No counterpart in the reference: it
+ * is the context readback's ordering (flip_get_marker_particle_position_data)
+ * for callers that cannot call cudaMalloc, such as hosts whose device memory
+ * all comes from their own allocator or pool, or frame loops in which a
+ * cudaMalloc's implicit device synchronisation is not acceptable.  Inputs
+ * are device arrays of n particles (x, y, z planes and ids, in any order);
+ * ids must be distinct and below id_space (ids at or above it are skipped).
+ * The output holds 3*n floats, packed xyz, the particle with the smallest
+ * id first.  id_space may be at most FLIP_NOALLOC_MAX_IDS; a larger one is
+ * rejected with FLIP_E_OUT_OF_RANGE.  The work runs on `stream` (a
+ * cudaStream_t; NULL for the default stream) in a device array of about
+ * 4 MiB that the library holds from load until exit on every device that
+ * uses it.  The first call on a device looks that array's address up (once
+ * per device, with the device current) and should come before any stream
+ * capture.  Every call shares the array: calls whose work overlaps on the
+ * GPU (different streams, or different threads without ordering) race, so
+ * order them. */
+#define FLIP_NOALLOC_MAX_IDS (1 << 20)
+int flip_order_particles_by_id_noalloc(const float *d_px, const float *d_py, const float *d_pz,
+                                       const unsigned int *d_ids, int n, int id_space, float *d_out_xyz,
+                                       void *stream);
+
 /* Last error message of the calling thread (static storage). */
 const char *flip_last_error(void);
 
