@@ -36,7 +36,16 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
 FRAME_DT = 1.0 / 120.0
-METRIC = "Mparticle-steps/s at 128^3 (plain FLIP step, dam break + sphere)"
+METRIC = "Mparticle-steps/s at 128^3 (plain FLIP step, dam break + sphere)"  # the plain_128 workload
+SCENES = {
+    "plain_128": "plain FLIP 128x128x128, dx=1/128, dam break + sphere, FLIP blend 0.95, PCG tol 1e-6, dt=1/120",
+    "plain_64": "plain FLIP 64x64x64, dx=1/64, dam break, FLIP blend 0.95, PCG tol 1e-6, dt=1/120",
+}
+
+
+def make_scene(name):
+    from flipengine3d_gb300 import scenes
+    return getattr(scenes, name)()
 UNIT = "Mparticle-steps/s"
 
 
@@ -103,6 +112,22 @@ class ClockSampler:
         return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": smax, "reasons": sorted(reasons), "samples": len(sm)}
 
 
+SWEEP_BYTES_PER_ROW = 24.0
+TRAFFIC_FILE = ROOT / "profiles" / "k_wavefront_plain128.txt"
+
+
+def sweep_traffic_per_launch():
+    """DRAM bytes (read + write) per sweep launch from the committed ncu
+    summary of this workload, or None when there is none."""
+    try:
+        for line in TRAFFIC_FILE.read_text().splitlines():
+            if line.startswith("traffic_bytes_per_launch:"):
+                return int(float(line.split(":", 1)[1]))
+    except OSError:
+        pass
+    return None
+
+
 def algorithmic_bytes(n_particles, n_cells, n_fluid, iters):
     """Per-substep algorithmic HBM bytes of the FLIP step: 120 B per particle
     (binning 48, SDF/P2G reads 24, G2P+RK3 read+write 48), 256 B per grid
@@ -116,11 +141,9 @@ def run_gpu(args, rank, world):
     import torch
 
     import flipengine3d_gb300 as fg
-    from flipengine3d_gb300.scenes import plain_128
-
     local = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(local)
-    sc = plain_128()
+    sc = make_scene(args.scene)
     stream = torch.cuda.Stream()
     sim = fg.FluidSimulation.from_scene(sc)
     sim.setStream(stream.cuda_stream)
@@ -154,6 +177,7 @@ def run_gpu(args, rank, world):
     launches = sim.launch_count() - launches0
     ms = sum(a.elapsed_time(b) for a, b in ev)
     stage_ms, substeps = sim.stage_times()
+    sweep_ms, sweep_launches, sweep_rows = sim.sweep_times()
     sim.set_stage_timing(False)
 
     # end to end through the public API with host buffers
@@ -180,22 +204,15 @@ def run_gpu(args, rank, world):
     value = float(tot[0]) / (ms_max / 1e3) / 1e6
     e2e_value = float(tot[1]) / e2e_max / 1e6
 
-    # roofline of the dominant stage
+    # roofline of the dominant kernel: the MIC(0) sweeps, event-timed per
+    # launch on the simulation's stream inside the library
     peak, peak_kind = peaks()
     n_cells = sc.isize * sc.jsize * sc.ksize
     n_avg = particles / args.steps
-    dominant = max(stage_ms, key=stage_ms.get)
     base_b, pcg_b = algorithmic_bytes(n_avg, n_cells, np.mean(cells), np.mean(iters))
-    stage_bytes = {
-        "pressure": pcg_b * substeps,
-        "advect": 48.0 * n_avg * substeps + 24.0 * n_cells * substeps,
-        "binning": 48.0 * n_avg * substeps,
-        "p2g": 24.0 * n_avg * substeps + (15.0 + 48.0) * n_cells * substeps,
-        "liquid_sdf": 12.0 * n_avg * substeps + 5.0 * n_cells * substeps,
-        "constrain": (48.0 + 24.0) * n_cells * substeps,
-        "force": 24.0 * n_cells * substeps,
-    }
-    achieved = stage_bytes[dominant] / (stage_ms[dominant] / 1e3) / 1e9
+    sweep_bytes_per_launch = SWEEP_BYTES_PER_ROW * sweep_rows / max(sweep_launches, 1)
+    sweep_s_per_launch = sweep_ms / 1e3 / max(sweep_launches, 1)
+    achieved = sweep_bytes_per_launch / sweep_s_per_launch / 1e9 if sweep_launches else 0.0
     step_achieved = (base_b + pcg_b) * substeps / (sum(stage_ms.values()) / 1e3) / 1e9
 
     cpu = cpu_baseline(args) if not args.no_cpu_baseline else None
@@ -204,17 +221,21 @@ def run_gpu(args, rank, world):
         "warmup": args.warmup, "ms_per_step": round(ms_max / args.steps, 4), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32 (FP64 dots/refinement)",
         "data": "synthetic: seeded dam break + sphere, 8 jittered particles per cell",
-        "config": {"workload": "plain FLIP 128x128x128, dx=1/128, dam break + sphere, FLIP blend 0.95, "
-                               "PCG tol 1e-6, dt=1/120", "particles": int(n_avg), "grid": [sc.isize, sc.jsize, sc.ksize],
+        "config": {"workload": SCENES[args.scene], "particles": int(n_avg), "grid": [sc.isize, sc.jsize, sc.ksize],
                    "pressure_cells": int(np.mean(cells)), "pcg_iterations_mean": float(np.mean(iters)),
                    "l2": "flushed between timed frames (256 MB write, outside the events)",
                    "parallelism": f"replicas x{world}"},
         "e2e": {"value": round(e2e_value, 4), "unit": UNIT, "h2d_bytes_per_step": 8,
                 "d2h_bytes_per_step": int(d2h / args.steps),
                 "path": "FluidSimulation.update(dt) + getMarkerParticlePositionData() via the C ABI"},
-        "roofline": {"bound": "hbm", "kernel": f"stage:{dominant}", "achieved": round(achieved, 1),
-                     "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": None,
+        "roofline": {"bound": "hbm", "kernel": "k_wavefront (MIC(0) forward + backward sweeps)",
+                     "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
+                     "frac": round(achieved / peak, 5), "traffic": sweep_traffic_per_launch(),
                      "peak_source": peak_kind,
+                     "bytes_per_launch": round(sweep_bytes_per_launch), "launches": int(sweep_launches),
+                     "avg_launch_us": round(sweep_s_per_launch * 1e6, 2),
+                     "share_of_step": round(sweep_ms / ms, 4) if ms else None,
+                     "bytes_rule": f"{SWEEP_BYTES_PER_ROW:g} B per pressure row per sweep (factor row 16, rhs 4, result 4)",
                      "step_achieved_gbs": round(step_achieved, 1),
                      "stage_ms_per_step": {k: round(v / args.steps, 3) for k, v in stage_ms.items()}},
         "cpu_baseline": cpu,
@@ -226,9 +247,8 @@ def run_gpu(args, rank, world):
 
 def cpu_sample_sim(args, threads):
     """The reference CPU path on one bounded sample of the workload."""
-    from flipengine3d_gb300.scenes import plain_128
     from oracle import refsim
-    sc = plain_128()
+    sc = make_scene(args.scene)
     if refsim.available("ref"):
         kind, cls = "reference", refsim.RefSimulation
     else:
@@ -247,7 +267,7 @@ def cpu_baseline(args):
     sim.update(FRAME_DT)
     dt = time.perf_counter() - t0
     return {"value": round(n / dt / 1e6, 5), "unit": UNIT, "cores": threads, "kind": kind,
-            "sample": f"1 timed frame of the 128^3 workload ({n} particles) after 1 untimed frame, {dt:.1f} s"}
+            "sample": f"1 timed frame of the {args.scene} workload ({n} particles) after 1 untimed frame, {dt:.1f} s"}
 
 
 def run_reference(args, rank, world):
@@ -267,13 +287,12 @@ def run_reference(args, rank, world):
         t += time.perf_counter() - t0
         total += n
     value = total / t / 1e6
-    sample = (f"{steps} timed frame(s) of the 128^3 workload after {warm} untimed, "
+    sample = (f"{steps} timed frame(s) of the {args.scene} workload after {warm} untimed, "
               f"{'reference engine' if kind == 'reference' else 'C++ oracle restating it'}, {threads} thread(s)")
     return {"metric": METRIC, "value": round(value, 5), "unit": UNIT, "n_gpus": world, "steps": steps,
             "warmup": warm, "ms_per_step": round(t / steps * 1e3, 2), "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32/f64", "data": "synthetic: seeded dam break + sphere",
-            "config": {"workload": "plain FLIP 128x128x128, dx=1/128, dam break + sphere, FLIP blend 0.95, "
-                                   "PCG tol 1e-6, dt=1/120"},
+            "config": {"workload": SCENES[args.scene]},
             "impl": "reference",
             "cpu_baseline": {"value": round(value, 5), "unit": UNIT, "cores": threads, "kind": kind, "sample": sample},
             "e2e": {"value": round(value, 5), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -287,6 +306,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--reference-max-steps", type=int, default=3)
+    ap.add_argument("--scene", default="plain_128", choices=sorted(SCENES),
+                    help="plain_128 is the benchmark workload; plain_64 is the small case for profiling")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

@@ -84,7 +84,7 @@ struct PressureBuffers {
     float *z, *s;          // preconditioned residual, search direction
     float *rf;             // r rounded to FP32, the forward sweep's right-hand side
     double *partials;      // per-block partial sums (deterministic reduction)
-    double *scal;          // [0]=s.q [1]=z.r (new rho) [2]=|b|inf [3]=rho
+    double *scal;          // [0]=s.q [1]=z.r (new rho) [2]=|b|inf [3]=rho [4]=alpha [5]=beta
     unsigned long long *rmaxBits;  // |r|inf as double bits
     int *levelRange;       // [0]=min(i+j+k) [1]=max(i+j+k) [2]=system size
     float *pressure;       // float copy of x for the velocity update
@@ -98,6 +98,14 @@ struct PressureArgs {
     int maxIter;
     float *dumpPressure;   // host, optional
     double *dumpRhs;       // host, optional
+    struct SweepTiming *sweepTiming;   // optional: event-timed sweep launches
+};
+// Device time of the preconditioner sweeps, summed over launches.
+struct SweepTiming {
+    cudaEvent_t ev[2];
+    double ms;
+    long long launches;     // sweep kernels (forward and backward count one each)
+    long long cellSweeps;   // sum over launches of the system rows swept
 };
 struct PressureMail {      // pinned host scalars
     int levelRange[3];

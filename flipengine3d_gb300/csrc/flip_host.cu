@@ -117,6 +117,7 @@ struct flip_ctx {
     cudaEvent_t ev[FLIP_NUM_STAGES + 1] = {};
     double stageMs[FLIP_NUM_STAGES] = {};
     long long timedSubsteps = 0;
+    SweepTiming sweepTiming{};
     void mark(int stage) {
         if (timing) cudaEventRecord(ev[stage], stream);
     }
@@ -357,6 +358,7 @@ int pressure_solve(flip_ctx *x, double dt, bool *applied, flip_stage_dump *d) {
     a.dt = dt; a.tol = x->tol; a.accTol = x->accTol; a.maxIter = x->maxIter;
     a.dumpPressure = d ? d->pressure : nullptr;
     a.dumpRhs = d ? d->rhs : nullptr;
+    a.sweepTiming = x->timing ? &x->sweepTiming : nullptr;
     PressureResult res{};
     std::string msg;
     int rc = pressure_project(x->c, a, x->pr, x->sweep, x->pmail, x->stream, &res, &msg);
@@ -645,6 +647,8 @@ int flip_destroy(flip_ctx *x) {
     cudaStreamSynchronize(x->stream);
     for (int q = 0; q <= FLIP_NUM_STAGES; q++)
         if (x->ev[q]) cudaEventDestroy(x->ev[q]);
+    for (int q = 0; q < 2; q++)
+        if (x->sweepTiming.ev[q]) cudaEventDestroy(x->sweepTiming.ev[q]);
     for (void *p : x->allocations) cudaFree(p);
     if (x->mail) cudaFreeHost(x->mail);
     if (x->pmail) cudaFreeHost(x->pmail);
@@ -845,10 +849,22 @@ int flip_set_stage_timing(flip_ctx *x, int enable) {
     CK(cudaStreamSynchronize(x->stream));
     if (enable && !x->ev[0]) {
         for (int q = 0; q <= FLIP_NUM_STAGES; q++) CK(cudaEventCreate(&x->ev[q]));
+        for (int q = 0; q < 2; q++) CK(cudaEventCreate(&x->sweepTiming.ev[q]));
     }
     x->timing = enable != 0;
     for (int q = 0; q < FLIP_NUM_STAGES; q++) x->stageMs[q] = 0.0;
     x->timedSubsteps = 0;
+    x->sweepTiming.ms = 0.0;
+    x->sweepTiming.launches = 0;
+    x->sweepTiming.cellSweeps = 0;
+    return FLIP_OK;
+}
+
+int flip_get_sweep_times(flip_ctx *x, double *ms, long long *launches, long long *cell_sweeps) {
+    if (!x || !ms) return FLIP_E_NULL;
+    *ms = x->sweepTiming.ms;
+    if (launches) *launches = x->sweepTiming.launches;
+    if (cell_sweeps) *cell_sweeps = x->sweepTiming.cellSweeps;
     return FLIP_OK;
 }
 

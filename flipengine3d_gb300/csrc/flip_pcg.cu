@@ -14,6 +14,7 @@
 // iterations, and whenever the recurrence reports convergence, the residual
 // is recomputed as b - A x (iterative refinement), and convergence is
 // decided on it, with the reference's test |r|inf <= tol * |b|inf.
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <string>
@@ -26,6 +27,7 @@ namespace flip {
 namespace {
 
 constexpr int TPB = 256;
+constexpr int RBLOCKS = 152 * 4;   // grid of the reduction kernels: 4 CTAs per SM
 
 __device__ __forceinline__ bool sys_cell(const StepConsts &c, const float *phi, int i, int j, int k) {
     if (i < 1 || j < 1 || k < 1 || i > c.I - 2 || j > c.J - 2 || k > c.K - 2) return false;
@@ -93,6 +95,23 @@ __device__ double4 row_coeffs(const StepConsts &c, const float *phi, const float
     return make_double4(fmax(diag, 0.0), xp, yp, zp);
 }
 
+// Max of non-negative values over the block, then one atomic per block.
+// With nanAsInf a NaN reads as +inf (a residual norm that never passes for
+// converged); otherwise NaNs are ignored, as fmax ignores them.
+__device__ __forceinline__ void block_max_to(double v, unsigned long long *out, bool nanAsInf = true) {
+    __shared__ double sh[32];
+    if (v != v) v = nanAsInf ? __longlong_as_double(0x7ff0000000000000ll) : 0.0;
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) sh[warp] = v;
+    __syncthreads();
+    if (warp == 0) {
+        v = lane < (int)(blockDim.x >> 5) ? sh[lane] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+        if (lane == 0 && v > 0.0) atomicMax(out, (unsigned long long)__double_as_longlong(v));
+    }
+}
+
 // RHS (pressuresolver.cpp:580-669; the domain walls do not move) and the rows.
 __global__ void k_build(StepConsts c, const float *phi, const float *wu, const float *wv, const float *ww,
                         const float *u, const float *v, const float *w, double mf, PressureBuffers pb) {
@@ -130,9 +149,7 @@ __global__ void k_build(StepConsts c, const float *phi, const float *wu, const f
             pb.Ad[t] = row_coeffs(c, phi, wu, wv, ww, mf, i, j, k);
         }
     }
-    for (int o = 16; o > 0; o >>= 1) bmag = fmax(bmag, __shfl_xor_sync(0xffffffffu, bmag, o));
-    if ((threadIdx.x & 31) == 0 && bmag > 0.0)
-        atomicMax((unsigned long long *)pb.scal + 2, (unsigned long long)__double_as_longlong(bmag));
+    block_max_to(bmag, (unsigned long long *)pb.scal + 2, false);
 }
 
 // MIC(0) pivots of one wavefront i+j+k = level, FP64.  For 7-point rows the
@@ -201,21 +218,22 @@ __device__ __forceinline__ T block_sum(T v, T *sh) {
     return s;
 }
 
-__device__ __forceinline__ void block_max_to(double v, unsigned long long *out) {
-    if (v != v) v = __longlong_as_double(0x7ff0000000000000ll);   // NaN never reads as converged
-    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
-    if ((threadIdx.x & 31) == 0 && v > 0.0) atomicMax(out, (unsigned long long)__double_as_longlong(v));
-}
+
+// The reductions below run on a fixed grid of RBLOCKS CTAs with grid-stride
+// loops: each thread sums its cells in a fixed order, each CTA writes one
+// partial, and k_sum_partials adds the partials in a fixed order, so every
+// sum is deterministic and the FP64 reduction work is per thread, not per
+// cell.
 
 // q = A s (FP64), block partials of s.q
 __global__ void k_spmv(StepConsts c, const uint8_t *fluid, const double4 *Ad, const float *s, double *q,
                        double *partials) {
     __shared__ double sh[32];
-    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    long long n = (long long)c.I * c.J * c.K;
+    const long long n = (long long)c.I * c.J * c.K;
+    const long long sy = c.I, sz = (long long)c.I * c.J;
     double part = 0.0;
-    if (t < n && fluid[t]) {
-        const long long sy = c.I, sz = (long long)c.I * c.J;
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+        if (!fluid[t]) continue;
         double4 a = Ad[t];
         double acc = a.x * (double)s[t];
         acc = fma(a.y, (double)s[t + 1], acc);
@@ -225,42 +243,51 @@ __global__ void k_spmv(StepConsts c, const uint8_t *fluid, const double4 *Ad, co
         acc = fma(Ad[t - sy].z, (double)s[t - sy], acc);
         acc = fma(Ad[t - sz].w, (double)s[t - sz], acc);
         q[t] = acc;
-        part = (double)s[t] * acc;
+        part = fma((double)s[t], acc, part);
     }
     double b = block_sum(part, sh);
     if (threadIdx.x == 0) partials[blockIdx.x] = b;
 }
 
-__global__ void k_dot_zr(long long n, const float *z, const double *r, double *partials) {
+__global__ void k_dot_zr(long long n, const uint8_t *fluid, const float *z, const double *r, double *partials) {
     __shared__ double sh[32];
-    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    double part = t < n ? (double)z[t] * r[t] : 0.0;
+    double part = 0.0;
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x)
+        if (fluid[t]) part = fma((double)z[t], r[t], part);
     double s = block_sum(part, sh);
     if (threadIdx.x == 0) partials[blockIdx.x] = s;
 }
 
-// fixed-order sum of the block partials (deterministic)
-__global__ void k_sum_partials(const double *partials, int n, double *out) {
+// Fixed-order sum of the block partials (deterministic) into scal[slot];
+// then the step length that depends on it, once for all threads: for s.q
+// (slot 0) alpha = rho / s.q, for z.r (slot 1) beta = rho_new / rho, each
+// rounded to float as BLAS::addScaled takes it (blaswrapper.h:129-158).
+__global__ void k_sum_partials(const double *partials, int n, double *scal, int slot) {
     __shared__ double sh[32];
     double v = 0.0;
     for (int q = threadIdx.x; q < n; q += blockDim.x) v += partials[q];
     double s = block_sum(v, sh);
-    if (threadIdx.x == 0) *out = s;
+    if (threadIdx.x == 0) {
+        scal[slot] = s;
+        if (slot == 0) scal[4] = (double)(float)(scal[3] / s);
+        else scal[5] = scal[3] != 0.0 ? (double)(float)(s / scal[3]) : 0.0;
+    }
 }
 
 // x += alpha s, r -= alpha q with alpha = rho / s.q passed on as float, as
 // BLAS::addScaled(float alpha, ...) does (blaswrapper.h:129-158); |r|inf
 __global__ void k_update_xr(long long n, const uint8_t *fluid, double *x, double *r, float *rf, const float *s,
                             const double *q, const double *scal, unsigned long long *rmaxBits) {
-    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    const double alpha = (double)(float)(scal[3] / scal[0]);
+    const double alpha = scal[4];
     double m = 0.0;
-    if (t < n && fluid[t]) {
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+        if (!fluid[t]) continue;
         x[t] = fma(alpha, (double)s[t], x[t]);
         double rv = fma(-alpha, q[t], r[t]);
         r[t] = rv;
         rf[t] = (float)rv;
-        m = fabs(rv);
+        double av = fabs(rv);
+        m = (av != av || av > m) ? av : m;   // a NaN sticks
     }
     block_max_to(m, rmaxBits);
 }
@@ -268,11 +295,11 @@ __global__ void k_update_xr(long long n, const uint8_t *fluid, double *x, double
 // r = b - A x (residual replacement); |r|inf
 __global__ void k_true_residual(StepConsts c, const uint8_t *fluid, const double4 *Ad, const double *b,
                                 const double *x, double *r, float *rf, unsigned long long *rmaxBits) {
-    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    long long n = (long long)c.I * c.J * c.K;
+    const long long n = (long long)c.I * c.J * c.K;
+    const long long sy = c.I, sz = (long long)c.I * c.J;
     double m = 0.0;
-    if (t < n && fluid[t]) {
-        const long long sy = c.I, sz = (long long)c.I * c.J;
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+        if (!fluid[t]) continue;
         double4 a = Ad[t];
         double ax = a.x * x[t];
         ax = fma(a.y, x[t + 1], ax);
@@ -284,18 +311,19 @@ __global__ void k_true_residual(StepConsts c, const uint8_t *fluid, const double
         double rv = b[t] - ax;
         r[t] = rv;
         rf[t] = (float)rv;
-        m = fabs(rv);
+        double av = fabs(rv);
+        m = (av != av || av > m) ? av : m;
     }
     block_max_to(m, rmaxBits);
 }
 
 __global__ void k_init_r(long long n, const double *b, double *r, float *rf, unsigned long long *rmaxBits) {
-    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     double m = 0.0;
-    if (t < n) {
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
         r[t] = b[t];
         rf[t] = (float)b[t];
-        m = fabs(b[t]);
+        double av = fabs(b[t]);
+        m = (av != av || av > m) ? av : m;
     }
     block_max_to(m, rmaxBits);
 }
@@ -303,7 +331,7 @@ __global__ void k_init_r(long long n, const double *b, double *r, float *rf, uns
 // s = z + beta s, beta = rho_new / rho as float (pcgsolver.h:295-298)
 __global__ void k_update_s(long long n, const uint8_t *fluid, const float *z, float *s, const double *scal) {
     long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    const float beta = (float)(scal[1] / scal[3]);
+    const float beta = (float)scal[5];
     if (t < n && fluid[t]) s[t] = __fmaf_rn(beta, s[t], z[t]);
 }
 
@@ -379,7 +407,7 @@ int cuda_fail(cudaError_t e, std::string *msg) {
 
 }  // namespace
 
-int pressure_partials(const StepConsts &c) { return (int)div_up((long long)c.I * c.J * c.K, TPB); }
+int pressure_partials(const StepConsts &c) { return std::min((int)div_up((long long)c.I * c.J * c.K, TPB), RBLOCKS); }
 
 #define PCK(call)                                     \
     do {                                              \
@@ -391,6 +419,7 @@ int pressure_project(const StepConsts &c, const PressureArgs &a, PressureBuffers
                      PressureMail *mail, cudaStream_t s, PressureResult *res, std::string *errMsg) {
     const long long n = (long long)c.I * c.J * c.K;
     const unsigned nb = div_up(n, TPB);
+    const unsigned rb = (unsigned)pb.nPartials;   // reduction grid
     const double mf = a.dt / (c.dx * c.dx);
     res->iterations = 0;
     res->residual = 0.0;
@@ -429,31 +458,49 @@ int pressure_project(const StepConsts &c, const PressureArgs &a, PressureBuffers
     launch_sweep_ranges(c, pb.fluid, sw, s);
 
     unsigned long long *rmax = pb.rmaxBits;
+    bool sweepPending = false;
+    auto tally = [&]() {   // add the last timed sweep pair once its events are complete
+        if (!sweepPending) return;
+        float ms = 0.0f;
+        if (cudaEventElapsedTime(&ms, a.sweepTiming->ev[0], a.sweepTiming->ev[1]) == cudaSuccess) {
+            a.sweepTiming->ms += ms;
+            a.sweepTiming->launches += 2;
+            a.sweepTiming->cellSweeps += 2LL * res->cells;
+        }
+        sweepPending = false;
+    };
     auto read_rmax = [&](double *out, int *sweepErr) -> cudaError_t {
         cudaError_t e = cudaMemcpyAsync(&mail->rmaxBits, rmax, sizeof(unsigned long long), cudaMemcpyDeviceToHost, s);
         if (e == cudaSuccess) e = cudaMemcpyAsync(&mail->sweepErr, sw.err, sizeof(int), cudaMemcpyDeviceToHost, s);
         if (e == cudaSuccess) e = sync();
         if (e != cudaSuccess) return e;
+        tally();
         std::memcpy(out, &mail->rmaxBits, sizeof(double));
         *sweepErr = mail->sweepErr;
         return cudaSuccess;
     };
     auto precondition = [&]() {
+        if (a.sweepTiming) cudaEventRecord(a.sweepTiming->ev[0], s);
         launch_sweeps(c, pb.L, pb.rf, pb.z, sw, s);
-        { FLIP_COUNT(1); k_dot_zr<<<nb, TPB, 0, s>>>(n, pb.z, pb.r, pb.partials); }
-        { FLIP_COUNT(1); k_sum_partials<<<1, 1024, 0, s>>>(pb.partials, pb.nPartials, pb.scal + 1); }
+        if (a.sweepTiming) {
+            cudaEventRecord(a.sweepTiming->ev[1], s);
+            sweepPending = true;
+        }
+        { FLIP_COUNT(1); k_dot_zr<<<rb, TPB, 0, s>>>(n, pb.fluid, pb.z, pb.r, pb.partials); }
+        { FLIP_COUNT(1); k_sum_partials<<<1, 1024, 0, s>>>(pb.partials, pb.nPartials, pb.scal, 1); }
     };
     auto residual = [&]() {
         PCK(cudaMemsetAsync(rmax, 0, sizeof(unsigned long long), s));
-        { FLIP_COUNT(1); k_true_residual<<<nb, TPB, 0, s>>>(c, pb.fluid, pb.Ad, pb.b, pb.x, pb.r, pb.rf, rmax); }
+        { FLIP_COUNT(1); k_true_residual<<<rb, TPB, 0, s>>>(c, pb.fluid, pb.Ad, pb.b, pb.x, pb.r, pb.rf, rmax); }
         return FLIP_OK;
     };
 
     PCK(cudaMemsetAsync(rmax, 0, sizeof(unsigned long long), s));
-    { FLIP_COUNT(1); k_init_r<<<nb, TPB, 0, s>>>(n, pb.b, pb.r, pb.rf, rmax); }
+    { FLIP_COUNT(1); k_init_r<<<rb, TPB, 0, s>>>(n, pb.b, pb.r, pb.rf, rmax); }
     precondition();
     PCK(cudaMemcpyAsync(&mail->rho, pb.scal + 1, sizeof(double), cudaMemcpyDeviceToHost, s));
     PCK(sync());
+    tally();
     const double rho0 = mail->rho;
     bool ok = false;
     int iterations = 0;
@@ -464,10 +511,10 @@ int pressure_project(const StepConsts &c, const PressureArgs &a, PressureBuffers
         { FLIP_COUNT(1); k_set_rho<<<1, 1, 0, s>>>(pb.scal); }
         int it;
         for (it = 0; it < a.maxIter; it++) {
-            { FLIP_COUNT(1); k_spmv<<<nb, TPB, 0, s>>>(c, pb.fluid, pb.Ad, pb.s, pb.q, pb.partials); }
-            { FLIP_COUNT(1); k_sum_partials<<<1, 1024, 0, s>>>(pb.partials, pb.nPartials, pb.scal + 0); }
+            { FLIP_COUNT(1); k_spmv<<<rb, TPB, 0, s>>>(c, pb.fluid, pb.Ad, pb.s, pb.q, pb.partials); }
+            { FLIP_COUNT(1); k_sum_partials<<<1, 1024, 0, s>>>(pb.partials, pb.nPartials, pb.scal, 0); }
             PCK(cudaMemsetAsync(rmax, 0, sizeof(unsigned long long), s));
-            { FLIP_COUNT(1); k_update_xr<<<nb, TPB, 0, s>>>(n, pb.fluid, pb.x, pb.r, pb.rf, pb.s, pb.q, pb.scal, rmax); }
+            { FLIP_COUNT(1); k_update_xr<<<rb, TPB, 0, s>>>(n, pb.fluid, pb.x, pb.r, pb.rf, pb.s, pb.q, pb.scal, rmax); }
             const bool periodic = (it + 1) % 25 == 0;
             if (periodic) residual();
             PCK(read_rmax(&resid, &sweepErr));
@@ -495,6 +542,10 @@ int pressure_project(const StepConsts &c, const PressureArgs &a, PressureBuffers
         sync();
         if (errMsg) *errMsg = "a wavefront sweep gave up waiting for a neighbouring tile";
         return FLIP_E_DEVICE_TIMEOUT;
+    }
+    if (sweepPending) {
+        PCK(sync());
+        tally();
     }
     res->iterations = iterations;
     res->residual = resid;

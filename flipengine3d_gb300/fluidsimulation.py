@@ -86,6 +86,7 @@ SIGNATURES = {
     "flip_set_stage_timing": [_P, _I],
     "flip_get_stage_times": [_P, _P, C.POINTER(C.c_longlong)],
     "flip_get_launch_count": [_P, C.POINTER(C.c_longlong)],
+    "flip_get_sweep_times": [_P, C.POINTER(C.c_double), C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)],
     "flip_order_particles_by_id_noalloc": [_P, _P, _P, _P, _I, _I, _P, _P],
 }
 
@@ -317,6 +318,15 @@ class FluidSimulation:
         n = C.c_longlong()
         self._c(self._lib.flip_get_stage_times(self._h, _ptr(ms), C.byref(n)))
         return dict(zip(STAGE_NAMES, ms.tolist())), n.value
+
+    def sweep_times(self):
+        """(summed device ms of the MIC(0) sweep kernels, kernels timed,
+        pressure rows swept summed over them), while stage timing is on."""
+        ms = C.c_double()
+        n = C.c_longlong()
+        cells = C.c_longlong()
+        self._c(self._lib.flip_get_sweep_times(self._h, C.byref(ms), C.byref(n), C.byref(cells)))
+        return ms.value, n.value, cells.value
 
     def launch_count(self) -> int:
         v = C.c_longlong()

@@ -171,6 +171,11 @@ int flip_compute_domain_solid(int isize, int jsize, int ksize, double dx, int cf
  * FLIP_NUM_STAGES milliseconds and the number of substeps summed. */
 int flip_set_stage_timing(flip_ctx *ctx, int enable);
 int flip_get_stage_times(flip_ctx *ctx, double *ms, long long *substeps);
+/* While stage timing is on: device time of the MIC(0) preconditioner sweeps
+ * (the kernels of solveLower / solveLowerTransposeInPlace, pcgsolver.h:192-221),
+ * summed; the number of sweep kernels timed; and the sum over them of the
+ * pressure rows each swept. */
+int flip_get_sweep_times(flip_ctx *ctx, double *ms, long long *launches, long long *cell_sweeps);
 
 /* Number of this library's kernel launches issued so far on the context. */
 int flip_get_launch_count(flip_ctx *ctx, long long *count);
