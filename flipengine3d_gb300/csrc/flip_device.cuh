@@ -74,15 +74,48 @@ void launch_mark_fast(const ParticleSoA &p, int n, const float *maxSpeedSq, unsi
 
 // -- pressure projection (flip_pcg.cu); dense cell-grid vectors, cells
 // outside the system hold zeros
+// Sweep layout: the vectors of the MIC(0) sweeps (factor rows, right-hand
+// side, result) are stored step-major.  The interior pencils are cut into
+// tiles of SWEEP_TJ (j) x SWEEP_TK (k); pencil (l, w) of a tile holds cell i
+// at forward step tf = i - 1 + l + w, and entry (tile, tf, w, l) lives at
+// ((tile * T + tf) * SWEEP_TJ * SWEEP_TK + w * SWEEP_TJ + l), T = I - 2 +
+// SWEEP_TJ - 1 + SWEEP_TK - 1.  A chunk of consecutive steps of a tile is one
+// contiguous block, in either sweep direction.  Entries that hold no interior
+// cell stay zero.
+constexpr int SWEEP_TJ = 32, SWEEP_TK = 8, SWEEP_NP = SWEEP_TJ * SWEEP_TK;
+struct SweepLayout {
+    int ntj, ntk, T;
+};
+inline SweepLayout sweep_layout(int I, int J, int K) {
+    SweepLayout g;
+    g.ntj = (J - 2 + SWEEP_TJ - 1) / SWEEP_TJ;
+    g.ntk = (K - 2 + SWEEP_TK - 1) / SWEEP_TK;
+    g.T = (I - 2) + (SWEEP_TJ - 1) + (SWEEP_TK - 1);
+    return g;
+}
+inline long long sweep_layout_size(int I, int J, int K) {
+    SweepLayout g = sweep_layout(I, J, K);
+    return (long long)g.ntj * g.ntk * g.T * SWEEP_NP;
+}
+// entry of interior cell (i, j, k)
+__device__ __forceinline__ long long sweep_index(const SweepLayout &g, int i, int j, int k) {
+    const int jj = j - 1, kk = k - 1;
+    const int l = jj % SWEEP_TJ, w = kk % SWEEP_TK;
+    const int tile = jj / SWEEP_TJ + g.ntj * (kk / SWEEP_TK);
+    return ((long long)tile * g.T + (i - 1 + l + w)) * SWEEP_NP + w * SWEEP_TJ + l;
+}
+
 struct PressureBuffers {
     uint8_t *fluid;        // interior cell with phi < 0 (a row of the system)
     double4 *Ad;           // rows {diag, to +x, to +y, to +z}, FP64
     double *b;             // right-hand side (negative divergence)
     double *invdiagD;      // MIC(0) inverse pivots, FP64
-    float4 *L;             // {invdiag, Lx, Ly, Lz} for the FP32 sweeps
+    float4 *L;             // {invdiag, Lx, Ly, Lz} for the FP32 sweeps, sweep layout
     double *x, *r, *q;     // solution, residual, A s
-    float *z, *s;          // preconditioned residual, search direction
-    float *rf;             // r rounded to FP32, the forward sweep's right-hand side
+    float *z;              // preconditioned residual, sweep layout
+    float *s;              // search direction
+    float *rf;             // r rounded to FP32, the forward sweep's right-hand side, sweep layout
+    SweepLayout sl;
     double *partials;      // per-block partial sums (deterministic reduction)
     double *scal;          // [0]=s.q [1]=z.r (new rho) [2]=|b|inf [3]=rho [4]=alpha [5]=beta
     unsigned long long *rmaxBits;  // |r|inf as double bits
@@ -120,10 +153,11 @@ struct PressureResult {
     int cells;
 };
 
-// Pipelined wavefront sweeps (flip_sweep.cu)
+// Pipelined wavefront sweeps (flip_wavefront.cu)
 struct SweepState {
     int2 *range;             // per tile [first, last] step holding a system cell
     unsigned long long *xchg;  // tile edge exchange words {epoch, value}
+    long long xchgWords;       // words allocated for xchg
     unsigned int *ticket;    // tile ticket counter
     int *err;                // set when a bounded wait gave up
     unsigned int epoch;

@@ -179,11 +179,17 @@ int alloc_grids(flip_ctx *x) {
         return rc;
     if ((rc = x->alloc(&x->status, x->nu() + x->nv() + x->nw()))) return rc;
     PressureBuffers &p = x->pr;
-    if ((rc = x->alloc(&p.fluid, nc)) || (rc = x->alloc(&p.Ad, nc)) || (rc = x->alloc(&p.L, nc)) ||
+    const long long nsl = sweep_layout_size(x->I, x->J, x->K);
+    p.sl = sweep_layout(x->I, x->J, x->K);
+    if ((rc = x->alloc(&p.fluid, nc)) || (rc = x->alloc(&p.Ad, nc)) || (rc = x->alloc(&p.L, nsl)) ||
         (rc = x->alloc(&p.b, nc)) || (rc = x->alloc(&p.invdiagD, nc)) || (rc = x->alloc(&p.x, nc)) ||
-        (rc = x->alloc(&p.r, nc)) || (rc = x->alloc(&p.q, nc)) || (rc = x->alloc(&p.z, nc)) ||
-        (rc = x->alloc(&p.s, nc)) || (rc = x->alloc(&p.rf, nc)) || (rc = x->alloc(&p.pressure, nc)))
+        (rc = x->alloc(&p.r, nc)) || (rc = x->alloc(&p.q, nc)) || (rc = x->alloc(&p.z, nsl)) ||
+        (rc = x->alloc(&p.s, nc)) || (rc = x->alloc(&p.rf, nsl)) || (rc = x->alloc(&p.pressure, nc)))
         return rc;
+    // entries of the sweep layout that hold no interior cell stay zero
+    CK(cudaMemsetAsync(p.L, 0, nsl * sizeof(float4), x->stream));
+    CK(cudaMemsetAsync(p.rf, 0, nsl * sizeof(float), x->stream));
+    CK(cudaMemsetAsync(p.z, 0, nsl * sizeof(float), x->stream));
     p.nPartials = pressure_partials(x->c);
     if ((rc = x->alloc(&p.partials, p.nPartials + 32)) || (rc = x->alloc(&p.scal, 8)) ||
         (rc = x->alloc(&p.rmaxBits, 2)) || (rc = x->alloc(&p.levelRange, 4)))
@@ -192,6 +198,7 @@ int alloc_grids(flip_ctx *x) {
         int ntj, ntk;
         int nt = sweep_tiles(x->J, x->K, &ntj, &ntk);
         long long nw = sweep_exchange_words(x->I, x->J, x->K);
+        x->sweep.xchgWords = nw;
         if ((rc = x->alloc(&x->sweep.range, nt)) || (rc = x->alloc(&x->sweep.xchg, nw)) ||
             (rc = x->alloc(&x->sweep.ticket, 4)) || (rc = x->alloc(&x->sweep.err, 4)))
             return rc;

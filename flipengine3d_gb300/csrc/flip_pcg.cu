@@ -121,12 +121,9 @@ __global__ void k_build(StepConsts c, const float *phi, const float *wu, const f
     if (t < d.size()) {
         pb.x[t] = 0.0;
         pb.r[t] = 0.0;
-        pb.rf[t] = 0.0f;
         pb.q[t] = 0.0;
-        pb.z[t] = 0.0f;
         pb.s[t] = 0.0f;
         pb.invdiagD[t] = 0.0;
-        pb.L[t] = make_float4(0.f, 0.f, 0.f, 0.f);
         if (!pb.fluid[t]) {
             pb.Ad[t] = make_double4(0.0, 0.0, 0.0, 0.0);
             pb.b[t] = 0.0;
@@ -193,16 +190,25 @@ __global__ void k_mic0_level(StepConsts c, const uint8_t *fluid, const double4 *
     invD[t] = inv;
 }
 
-__global__ void k_mic0_finalize(long long n, const uint8_t *fluid, const double4 *Ad, const double *invD, float4 *L) {
+// the FP32 factor rows of the interior cells, into the sweep layout
+__global__ void k_mic0_finalize(StepConsts c, SweepLayout g, const uint8_t *fluid, const double4 *Ad,
+                                const double *invD, float4 *L) {
     long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= n) return;
-    double inv = invD[t];
-    if (!fluid[t] || inv == 0.0) {
-        L[t] = make_float4(0.f, 0.f, 0.f, 0.f);
-        return;
+    if (t >= (long long)c.I * c.J * c.K) return;
+    const int i = (int)(t % c.I), j = (int)((t / c.I) % c.J), k = (int)(t / ((long long)c.I * c.J));
+    if (i < 1 || j < 1 || k < 1 || i > c.I - 2 || j > c.J - 2 || k > c.K - 2) return;
+    const double inv = invD[t];
+    float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (fluid[t] && inv != 0.0) {
+        const double4 a = Ad[t];
+        v = make_float4((float)inv, (float)(a.y * inv), (float)(a.z * inv), (float)(a.w * inv));
     }
-    double4 a = Ad[t];
-    L[t] = make_float4((float)inv, (float)(a.y * inv), (float)(a.z * inv), (float)(a.w * inv));
+    L[sweep_index(g, i, j, k)] = v;
+}
+
+__device__ __forceinline__ long long sweep_index_of(const StepConsts &c, const SweepLayout &g, long long t) {
+    const int i = (int)(t % c.I), j = (int)((t / c.I) % c.J), k = (int)(t / ((long long)c.I * c.J));
+    return sweep_index(g, i, j, k);
 }
 
 template <class T>
@@ -249,11 +255,13 @@ __global__ void k_spmv(StepConsts c, const uint8_t *fluid, const double4 *Ad, co
     if (threadIdx.x == 0) partials[blockIdx.x] = b;
 }
 
-__global__ void k_dot_zr(long long n, const uint8_t *fluid, const float *z, const double *r, double *partials) {
+__global__ void k_dot_zr(StepConsts c, SweepLayout g, const uint8_t *fluid, const float *z, const double *r,
+                         double *partials) {
     __shared__ double sh[32];
+    const long long n = (long long)c.I * c.J * c.K;
     double part = 0.0;
     for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x)
-        if (fluid[t]) part = fma((double)z[t], r[t], part);
+        if (fluid[t]) part = fma((double)z[sweep_index_of(c, g, t)], r[t], part);
     double s = block_sum(part, sh);
     if (threadIdx.x == 0) partials[blockIdx.x] = s;
 }
@@ -276,8 +284,9 @@ __global__ void k_sum_partials(const double *partials, int n, double *scal, int 
 
 // x += alpha s, r -= alpha q with alpha = rho / s.q passed on as float, as
 // BLAS::addScaled(float alpha, ...) does (blaswrapper.h:129-158); |r|inf
-__global__ void k_update_xr(long long n, const uint8_t *fluid, double *x, double *r, float *rf, const float *s,
-                            const double *q, const double *scal, unsigned long long *rmaxBits) {
+__global__ void k_update_xr(StepConsts c, SweepLayout g, const uint8_t *fluid, double *x, double *r, float *rf,
+                            const float *s, const double *q, const double *scal, unsigned long long *rmaxBits) {
+    const long long n = (long long)c.I * c.J * c.K;
     const double alpha = scal[4];
     double m = 0.0;
     for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
@@ -285,7 +294,7 @@ __global__ void k_update_xr(long long n, const uint8_t *fluid, double *x, double
         x[t] = fma(alpha, (double)s[t], x[t]);
         double rv = fma(-alpha, q[t], r[t]);
         r[t] = rv;
-        rf[t] = (float)rv;
+        rf[sweep_index_of(c, g, t)] = (float)rv;
         double av = fabs(rv);
         m = (av != av || av > m) ? av : m;   // a NaN sticks
     }
@@ -293,7 +302,7 @@ __global__ void k_update_xr(long long n, const uint8_t *fluid, double *x, double
 }
 
 // r = b - A x (residual replacement); |r|inf
-__global__ void k_true_residual(StepConsts c, const uint8_t *fluid, const double4 *Ad, const double *b,
+__global__ void k_true_residual(StepConsts c, SweepLayout g, const uint8_t *fluid, const double4 *Ad, const double *b,
                                 const double *x, double *r, float *rf, unsigned long long *rmaxBits) {
     const long long n = (long long)c.I * c.J * c.K;
     const long long sy = c.I, sz = (long long)c.I * c.J;
@@ -310,18 +319,22 @@ __global__ void k_true_residual(StepConsts c, const uint8_t *fluid, const double
         ax = fma(Ad[t - sz].w, x[t - sz], ax);
         double rv = b[t] - ax;
         r[t] = rv;
-        rf[t] = (float)rv;
+        rf[sweep_index_of(c, g, t)] = (float)rv;
         double av = fabs(rv);
         m = (av != av || av > m) ? av : m;
     }
     block_max_to(m, rmaxBits);
 }
 
-__global__ void k_init_r(long long n, const double *b, double *r, float *rf, unsigned long long *rmaxBits) {
+__global__ void k_init_r(StepConsts c, SweepLayout g, const double *b, double *r, float *rf,
+                         unsigned long long *rmaxBits) {
+    const long long n = (long long)c.I * c.J * c.K;
     double m = 0.0;
     for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
         r[t] = b[t];
-        rf[t] = (float)b[t];
+        const int i = (int)(t % c.I), j = (int)((t / c.I) % c.J), k = (int)(t / ((long long)c.I * c.J));
+        if (i >= 1 && j >= 1 && k >= 1 && i <= c.I - 2 && j <= c.J - 2 && k <= c.K - 2)
+            rf[sweep_index(g, i, j, k)] = (float)b[t];
         double av = fabs(b[t]);
         m = (av != av || av > m) ? av : m;
     }
@@ -329,15 +342,16 @@ __global__ void k_init_r(long long n, const double *b, double *r, float *rf, uns
 }
 
 // s = z + beta s, beta = rho_new / rho as float (pcgsolver.h:295-298)
-__global__ void k_update_s(long long n, const uint8_t *fluid, const float *z, float *s, const double *scal) {
+__global__ void k_update_s(StepConsts c, SweepLayout g, const uint8_t *fluid, const float *z, float *s,
+                           const double *scal) {
     long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const float beta = (float)scal[5];
-    if (t < n && fluid[t]) s[t] = __fmaf_rn(beta, s[t], z[t]);
+    if (t < (long long)c.I * c.J * c.K && fluid[t]) s[t] = __fmaf_rn(beta, s[t], z[sweep_index_of(c, g, t)]);
 }
 
-__global__ void k_copy_zs(long long n, const float *z, float *s) {
+__global__ void k_copy_zs(StepConsts c, SweepLayout g, const uint8_t *fluid, const float *z, float *s) {
     long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t < n) s[t] = z[t];
+    if (t < (long long)c.I * c.J * c.K) s[t] = fluid[t] ? z[sweep_index_of(c, g, t)] : 0.0f;
 }
 
 __global__ void k_set_rho(double *scal) { scal[3] = scal[1]; }
@@ -447,6 +461,10 @@ int pressure_project(const StepConsts &c, const PressureArgs &a, PressureBuffers
         return FLIP_OK;
     }
     const double ptol = fmax(a.tol, 1e-30) * bmax;
+    if (sw.xchgWords < sweep_exchange_words(c.I, c.J, c.K)) {   // the sweeps' exchange array must cover every step
+        if (errMsg) *errMsg = "sweep exchange array smaller than the grid needs";
+        return FLIP_E_RUNTIME;
+    }
 
     // MIC(0) factor, one launch per wavefront
     const int np = (c.J - 2) * (c.K - 2);
@@ -454,7 +472,7 @@ int pressure_project(const StepConsts &c, const PressureArgs &a, PressureBuffers
         FLIP_COUNT(1);
         k_mic0_level<<<div_up(np, TPB), TPB, 0, s>>>(c, pb.fluid, pb.Ad, pb.invdiagD, lv);
     }
-    { FLIP_COUNT(1); k_mic0_finalize<<<nb, TPB, 0, s>>>(n, pb.fluid, pb.Ad, pb.invdiagD, pb.L); }
+    { FLIP_COUNT(1); k_mic0_finalize<<<nb, TPB, 0, s>>>(c, pb.sl, pb.fluid, pb.Ad, pb.invdiagD, pb.L); }
     launch_sweep_ranges(c, pb.fluid, sw, s);
 
     unsigned long long *rmax = pb.rmaxBits;
@@ -486,17 +504,17 @@ int pressure_project(const StepConsts &c, const PressureArgs &a, PressureBuffers
             cudaEventRecord(a.sweepTiming->ev[1], s);
             sweepPending = true;
         }
-        { FLIP_COUNT(1); k_dot_zr<<<rb, TPB, 0, s>>>(n, pb.fluid, pb.z, pb.r, pb.partials); }
+        { FLIP_COUNT(1); k_dot_zr<<<rb, TPB, 0, s>>>(c, pb.sl, pb.fluid, pb.z, pb.r, pb.partials); }
         { FLIP_COUNT(1); k_sum_partials<<<1, 1024, 0, s>>>(pb.partials, pb.nPartials, pb.scal, 1); }
     };
     auto residual = [&]() {
         PCK(cudaMemsetAsync(rmax, 0, sizeof(unsigned long long), s));
-        { FLIP_COUNT(1); k_true_residual<<<rb, TPB, 0, s>>>(c, pb.fluid, pb.Ad, pb.b, pb.x, pb.r, pb.rf, rmax); }
+        { FLIP_COUNT(1); k_true_residual<<<rb, TPB, 0, s>>>(c, pb.sl, pb.fluid, pb.Ad, pb.b, pb.x, pb.r, pb.rf, rmax); }
         return FLIP_OK;
     };
 
     PCK(cudaMemsetAsync(rmax, 0, sizeof(unsigned long long), s));
-    { FLIP_COUNT(1); k_init_r<<<rb, TPB, 0, s>>>(n, pb.b, pb.r, pb.rf, rmax); }
+    { FLIP_COUNT(1); k_init_r<<<rb, TPB, 0, s>>>(c, pb.sl, pb.b, pb.r, pb.rf, rmax); }
     precondition();
     PCK(cudaMemcpyAsync(&mail->rho, pb.scal + 1, sizeof(double), cudaMemcpyDeviceToHost, s));
     PCK(sync());
@@ -507,14 +525,14 @@ int pressure_project(const StepConsts &c, const PressureArgs &a, PressureBuffers
     double resid = bmax;
     int sweepErr = 0;
     if (!(rho0 == 0 || rho0 != rho0)) {
-        { FLIP_COUNT(1); k_copy_zs<<<nb, TPB, 0, s>>>(n, pb.z, pb.s); }
+        { FLIP_COUNT(1); k_copy_zs<<<nb, TPB, 0, s>>>(c, pb.sl, pb.fluid, pb.z, pb.s); }
         { FLIP_COUNT(1); k_set_rho<<<1, 1, 0, s>>>(pb.scal); }
         int it;
         for (it = 0; it < a.maxIter; it++) {
             { FLIP_COUNT(1); k_spmv<<<rb, TPB, 0, s>>>(c, pb.fluid, pb.Ad, pb.s, pb.q, pb.partials); }
             { FLIP_COUNT(1); k_sum_partials<<<1, 1024, 0, s>>>(pb.partials, pb.nPartials, pb.scal, 0); }
             PCK(cudaMemsetAsync(rmax, 0, sizeof(unsigned long long), s));
-            { FLIP_COUNT(1); k_update_xr<<<rb, TPB, 0, s>>>(n, pb.fluid, pb.x, pb.r, pb.rf, pb.s, pb.q, pb.scal, rmax); }
+            { FLIP_COUNT(1); k_update_xr<<<rb, TPB, 0, s>>>(c, pb.sl, pb.fluid, pb.x, pb.r, pb.rf, pb.s, pb.q, pb.scal, rmax); }
             const bool periodic = (it + 1) % 25 == 0;
             if (periodic) residual();
             PCK(read_rmax(&resid, &sweepErr));
@@ -530,7 +548,7 @@ int pressure_project(const StepConsts &c, const PressureArgs &a, PressureBuffers
                 break;
             }
             precondition();
-            { FLIP_COUNT(1); k_update_s<<<nb, TPB, 0, s>>>(n, pb.fluid, pb.z, pb.s, pb.scal); }
+            { FLIP_COUNT(1); k_update_s<<<nb, TPB, 0, s>>>(c, pb.sl, pb.fluid, pb.z, pb.s, pb.scal); }
             { FLIP_COUNT(1); k_set_rho<<<1, 1, 0, s>>>(pb.scal); }
         }
         if (!ok) iterations = it;

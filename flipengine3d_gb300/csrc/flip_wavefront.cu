@@ -9,33 +9,36 @@
 // (upper) neighbours only, so the cells of a plane i + j + k = const are
 // independent: the exact wavefront order.
 //
-// Mapping.  A CTA owns a tile of 32 (j) x 8 (k) pencils along i: lane = j,
-// warp = k.  In the forward sweep thread (l, w) processes i = 1 + t - l - w
-// at step t, so its j-1 neighbour (lane l-1) and k-1 neighbour (warp w-1)
-// finished that i at step t-1: j terms arrive by warp shuffle, k terms
-// through shared memory after the per-step barrier (the backward sweep is the
-// mirror image).  In the forward sweep a cell hands its neighbours the
-// finished products L_c * y_c rather than y_c: each product is rounded once,
-// by whichever thread forms it, so the bits are the reference's and the
-// receiver saves the coupling load and the multiply.
+// Mapping.  A CTA owns a tile of 32 (j) x 8 (k) pencils along i.  Its eight
+// compute warps hold one pencil per thread (lane = j, warp = k); in the
+// forward sweep thread (l, w) processes i = 1 + t - l - w at step t, so its
+// j-1 neighbour (lane l-1) and k-1 neighbour (warp w-1) finished that i at
+// step t-1: j terms arrive by warp shuffle, k terms through shared memory
+// after the per-step barrier (the backward sweep is the mirror image).  In
+// the forward sweep a cell hands its neighbours the finished products
+// L_c * y_c rather than y_c: each product is rounded once, by whichever
+// thread forms it, so the bits are the reference's.
 //
-// Lean steps.  A pencil's cells outside the interior (the skewed start and
-// end of the wavefront, and pencils past the grid's edge) are read at the
-// nearest boundary cell, whose factor row and right-hand side are zero, so
-// every step runs the same unpredicated arithmetic and only the store is
-// masked.  Steps run in chunks of 8; the next chunk's rows, right-hand side
-// and edge words are loaded while the current one computes.
+// Data movement.  The factor rows, the right-hand side and the result live
+// in the step-major sweep layout (flip_device.cuh), so the 8 steps of a
+// chunk of a tile are one contiguous block in either direction.  A helper
+// warp moves whole chunks with bulk asynchronous copies into a ring of
+// shared-memory slots (an mbarrier per slot counts the bytes in), writes
+// finished chunks back with bulk stores, and fetches the terms that the
+// neighbouring tiles publish for the chunk's edge cells.  The compute warps
+// only read operands from the slot and run the arithmetic; cells outside
+// the grid read zero rows, so a step is unpredicated.
 //
-// Tile edges.  The lanes on a tile's downstream edges publish each term they
-// form as one 64-bit word {sweep epoch, value} in an exchange array; the
-// neighbouring tile polls exactly the words it needs until their epoch is the
-// current sweep's.  A single naturally aligned 64-bit store is seen whole or
-// not at all, so no fence, flag or progress counter sits between the
-// producing step and the consuming one.  Cells that the producing tile does
-// not compute (outside its range of system cells) contribute zero and are not
+// Tile edges.  The threads on a tile's downstream edges publish each term
+// they form as one 64-bit word {sweep epoch, value}, indexed by step, in an
+// exchange array; the neighbour's helper warp polls exactly the words its
+// chunk needs until their epoch is the current sweep's.  A single naturally
+// aligned 64-bit store is seen whole or not at all, so no fence, flag or
+// progress counter sits between the producing step and the consuming one.
+// Cells that the producing tile does not compute contribute zero and are not
 // polled.  Tiles take tickets in dependency order, so a tile only waits for
-// tiles that are already running.  Every wait is bounded: on timeout the tile
-// raises the error flag and stops, and the host reports
+// tiles that are already running.  Every wait is bounded: on timeout the
+// tile raises the error flag and stops, and the host reports
 // FLIP_E_DEVICE_TIMEOUT; no wait can spin forever.
 #include "flip_device.cuh"
 
@@ -43,24 +46,40 @@ namespace flip {
 
 namespace {
 
-constexpr int TJ = 32, TK = 8, CH = 8;
-constexpr int NTHREADS = TJ * TK;
+constexpr int TJ = SWEEP_TJ, TK = SWEEP_TK, NP = SWEEP_NP, CH = 8, NBUF = 4;
+constexpr int NCOMP = NP, NTHREADS = NCOMP + 32;
 constexpr unsigned int SPIN_LIMIT = 1u << 22;   // poll rounds of <= ~250 ns: about a second
 
 struct SweepArgs {
-    const float4 *L;
-    const float *rin;              // forward: r rounded to FP32; backward: unused (reads out)
-    float *out;                    // forward: y; backward: z, in place over y
-    int I, J, K;
+    const float4 *L;               // factor rows, sweep layout
+    const float *rin;              // right-hand side, sweep layout (backward: the forward result)
+    float *out;                    // result, sweep layout (backward: in place over the forward result)
+    int J, K, NI, T;
     int ntj, ntk;
     const int2 *range;             // per tile: first/last step (forward numbering) holding a system cell
-    unsigned long long *xchg;      // per tile: TK j-edge rows, then TJ k-edge rows, of I words
+    unsigned long long *xchg;      // per tile: T x TK j-edge words, then T x TJ k-edge words
     unsigned int *ticket;
     unsigned int ticketBase;
     unsigned int epoch;
     int *err;
 };
 
+struct Slot {
+    float4 L[CH][NP];   // rows in layout order: forward row q = step q, backward row q = step CH-1-q
+    float r[CH][NP];
+    float o[CH][NP];
+    float eJ[CH][TK];   // by step: term from the j neighbour tile for the edge lane of each warp
+    float eK[CH][TJ];   // by step: term from the k neighbour tile for each lane of the edge warp
+};
+struct SweepSmem {
+    Slot slot[NBUF];
+    float p[2][TK][TJ];   // forward: L_w y of each pencil's last cell; backward: its z
+    unsigned long long full[NBUF], done[NBUF];
+    int abort;
+    int tile;
+};
+
+__device__ __forceinline__ unsigned smem_addr(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
 __device__ __forceinline__ unsigned long long ld_word(const unsigned long long *p) {
     unsigned long long v;
     asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
@@ -72,26 +91,74 @@ __device__ __forceinline__ void st_word(unsigned long long *p, unsigned long lon
 __device__ __forceinline__ unsigned long long pack(unsigned int epoch, float v) {
     return ((unsigned long long)epoch << 32) | __float_as_uint(v);
 }
-__device__ __forceinline__ float word_value(unsigned long long v) { return __uint_as_float((unsigned int)v); }
+__device__ __forceinline__ void mb_init(unsigned long long *b, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(b)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mb_arrive(unsigned long long *b) {
+    asm volatile("{\n .reg .b64 st;\n mbarrier.arrive.shared::cta.b64 st, [%0];\n}" ::"r"(smem_addr(b)) : "memory");
+}
+__device__ __forceinline__ void mb_expect_tx(unsigned long long *b, unsigned bytes) {
+    asm volatile("mbarrier.expect_tx.relaxed.cta.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(b)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mb_test(unsigned long long *b, unsigned parity) {
+    unsigned ok;
+    asm volatile("{\n .reg .pred p;\n mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+                 : "=r"(ok) : "r"(smem_addr(b)), "r"(parity) : "memory");
+    return ok != 0;
+}
+// Bounded wait for a phase of an mbarrier; false on abort or timeout.
+__device__ bool mb_wait(unsigned long long *b, unsigned parity, int *abortFlag, int *err) {
+    for (unsigned int spin = 0; spin < SPIN_LIMIT; spin++) {
+        if (mb_test(b, parity)) return true;
+        if (*(volatile int *)abortFlag) return false;
+        if (spin > 16) __nanosleep(32);
+    }
+    *(volatile int *)abortFlag = 1;
+    atomicExch(err, 1);
+    return false;
+}
+// bulk copy global -> shared, completion counted in bytes on mbarrier b
+__device__ __forceinline__ void bulk_load(void *dst, const void *src, unsigned bytes, unsigned long long *b) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                 ::"r"(smem_addr(dst)), "l"(src), "r"(bytes), "r"(smem_addr(b)) : "memory");
+}
+__device__ __forceinline__ void bulk_store(void *dst, const void *src, unsigned bytes) {
+    asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(dst), "r"(smem_addr(src)),
+                 "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void bulk_wait_read_all() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
+__device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+// named barrier of the compute warps, plain and with an OR vote
+__device__ __forceinline__ bool compute_sync_or(bool v) {
+    unsigned r;
+    asm volatile("{\n .reg .pred pi, po;\n setp.ne.u32 pi, %1, 0;\n bar.red.or.pred po, 1, %2, pi;\n selp.u32 %0, 1, 0, po;\n}"
+                 : "=r"(r) : "r"((unsigned)v), "n"(NCOMP) : "memory");
+    return r != 0;
+}
+__device__ __forceinline__ void compute_sync() { asm volatile("bar.sync 1, %0;" ::"n"(NCOMP) : "memory"); }
 
 template <bool FWD>
 __global__ void __launch_bounds__(NTHREADS, 1) k_wavefront(SweepArgs a) {
-    // forward: L_w * y of each pencil's last cell (the k+1 neighbour's term);
-    // backward: z of each pencil's last cell
-    __shared__ float shP[2][TK][TJ];
-    __shared__ int shTile;
-    const int l = threadIdx.x & 31, w = threadIdx.x >> 5;
+    extern __shared__ __align__(128) unsigned char smemRaw[];
+    SweepSmem &sm = *reinterpret_cast<SweepSmem *>(smemRaw);
     const int ntiles = a.ntj * a.ntk;
     if (threadIdx.x == 0) {
         int t = (int)(atomicAdd(a.ticket, 1u) - a.ticketBase);
-        shTile = FWD ? t : ntiles - 1 - t;
+        sm.tile = FWD ? t : ntiles - 1 - t;
+        sm.abort = 0;
+        for (int b = 0; b < NBUF; b++) {
+            mb_init(&sm.full[b], 32);      // the helper warp's lanes, plus the bytes of the chunk
+            mb_init(&sm.done[b], NCOMP);
+        }
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncthreads();
-    const int tile = shTile;
+    const int tile = sm.tile;
     if (tile < 0 || tile >= ntiles) return;
     const int tj = tile % a.ntj, tk = tile / a.ntj;
-    const int NI = a.I - 2;
-    const int T = NI + (TJ - 1) + (TK - 1);
+    const int NI = a.NI, T = a.T;
     auto steps_of = [&](int tl) {   // [first, last] step of a tile in this sweep's numbering
         const int2 rg = a.range[tl];
         return FWD ? rg : make_int2((T - 1) - rg.y, (T - 1) - rg.x);
@@ -99,160 +166,197 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_wavefront(SweepArgs a) {
     const int2 own = steps_of(tile);
     const int tlo = own.x, thi = own.y;
     if (thi < tlo) return;   // no system cell in the tile: nothing to compute or publish
+    const int nChunks = (thi - tlo) / CH + 1;
+    const int j0 = 1 + tj * TJ, k0 = 1 + tk * TK;
+    // cell of pencil (lane lr, warp ww) at step t
+    auto cell = [&](int lr, int ww, int t) {
+        return FWD ? 1 + t - lr - ww : NI - t + (TJ - 1 - lr) + (TK - 1 - ww);
+    };
+    auto pencil_in = [&](int lr, int ww) { return j0 + lr <= a.J - 2 && k0 + ww <= a.K - 2; };
+    const size_t wordsPerTile = (size_t)T * (TJ + TK);
+    const unsigned int ep = a.epoch;
+    // the chunk of steps [tb, tb + rows) as one block of the layout
+    auto chunk_rows = [&](int n) { return min(CH, thi + 1 - (tlo + n * CH)); };
+    auto chunk_row0 = [&](int rows) { return FWD ? 0 : CH - rows; };
+    auto chunk_tf0 = [&](int tb, int rows) { return FWD ? tb : T - tb - rows; };
+    const size_t tileBase = (size_t)tile * T * NP;
 
-    const int j = 1 + tj * TJ + l, k = 1 + tk * TK + w;
-    const bool active = j <= a.J - 2 && k <= a.K - 2;
-    const long long row = (long long)a.I * (min(j, a.J - 1) + (long long)a.J * min(k, a.K - 1));
-    const float4 *Lrow = a.L + row;
-    const float *Rrow = FWD ? a.rin + row : a.out + row;
-    float *Orow = a.out + row;
-    // cell of step t: i0 + t (forward) or i0 - t (backward)
-    const int i0 = FWD ? 1 - l - w : NI + (TJ - 1 - l) + (TK - 1 - w);
-    // steps at which the cell is interior and inside the tile's range
-    int v0 = FWD ? l + w : i0 - NI;
+    if (threadIdx.x >= NCOMP) {
+        // ================================================== helper warp
+        const int lane = threadIdx.x - NCOMP;
+        const int srcJ = FWD ? (tj > 0 ? tile - 1 : -1) : (tj < a.ntj - 1 ? tile + 1 : -1);
+        const int srcK = FWD ? (tk > 0 ? tile - a.ntj : -1) : (tk < a.ntk - 1 ? tile + a.ntj : -1);
+        const int2 rgJ = srcJ >= 0 ? steps_of(srcJ) : make_int2(1, 0);
+        const int2 rgK = srcK >= 0 ? steps_of(srcK) : make_int2(1, 0);
+        const int laneJ = FWD ? 0 : TJ - 1, warpK = FWD ? 0 : TK - 1;
+        const unsigned long long *srcJw = a.xchg + (srcJ >= 0 ? srcJ : 0) * wordsPerTile;
+        const unsigned long long *srcKw = a.xchg + (srcK >= 0 ? srcK : 0) * wordsPerTile + (size_t)T * TK;
+        bool ok = true;
+        int lastIssued = -1;   // last chunk whose operand copies were started
+        for (int m = 0; m < nChunks + NBUF && ok; m++) {
+            const int b = m % NBUF;
+            Slot &sl = sm.slot[b];
+            if (m >= NBUF) {   // write chunk m - NBUF back once its results are in
+                const int n = m - NBUF;
+                if (!mb_wait(&sm.done[b], (n / NBUF) & 1, &sm.abort, a.err)) { ok = false; break; }
+                if (lane == 0) {
+                    const int rows = chunk_rows(n), tb = tlo + n * CH;
+                    bulk_store(a.out + tileBase + (size_t)chunk_tf0(tb, rows) * NP, &sl.o[chunk_row0(rows)][0],
+                               (unsigned)(rows * NP * sizeof(float)));
+                    bulk_commit();
+                }
+            }
+            if (m >= nChunks) continue;
+            const int tb = tlo + m * CH, rows = chunk_rows(m);
+            if (lane == 0) {   // operands of chunk m
+                const unsigned bl = (unsigned)(rows * NP * sizeof(float4)), br = (unsigned)(rows * NP * sizeof(float));
+                const size_t e0 = tileBase + (size_t)chunk_tf0(tb, rows) * NP;
+                mb_expect_tx(&sm.full[b], bl + br);
+                bulk_load(&sl.L[chunk_row0(rows)][0], a.L + e0, bl, &sm.full[b]);
+                bulk_load(&sl.r[chunk_row0(rows)][0], a.rin + e0, br, &sm.full[b]);
+            }
+            lastIssued = m;
+            // edge terms: the consumer cell is computed and the producer's
+            // cell (TJ-1 or TK-1 steps later there) too
+            float vK[CH], vJ[2];
+            unsigned long long wK[CH], wJ[2];
+            unsigned int needK = 0, needJ = 0;
+#pragma unroll
+            for (int s = 0; s < CH; s++) {
+                const int te = tb + s, i = cell(lane, warpK, te);
+                const bool need = srcK >= 0 && s < rows && pencil_in(lane, warpK) && i >= 1 && i <= NI &&
+                                  te + (TK - 1) >= rgK.x && te + (TK - 1) <= rgK.y;
+                wK[s] = need ? ld_word(srcKw + (size_t)(te + TK - 1) * TJ + lane) : 0ull;
+                needK |= need ? 1u << s : 0u;
+            }
+#pragma unroll
+            for (int q = 0; q < 2; q++) {
+                const int e = lane + 32 * q, es = e >> 3, ew = e & 7, te = tb + es, i = cell(laneJ, ew, te);
+                const bool need = srcJ >= 0 && es < rows && pencil_in(laneJ, ew) && i >= 1 && i <= NI &&
+                                  te + (TJ - 1) >= rgJ.x && te + (TJ - 1) <= rgJ.y;
+                wJ[q] = need ? ld_word(srcJw + (size_t)(te + TJ - 1) * TK + ew) : 0ull;
+                needJ |= need ? 1u << q : 0u;
+            }
+            for (unsigned int spin = 0;; spin++) {
+                unsigned int missK = 0, missJ = 0;
+#pragma unroll
+                for (int s = 0; s < CH; s++)
+                    missK |= ((needK >> s) & 1u) && (unsigned int)(wK[s] >> 32) != ep ? 1u << s : 0u;
+#pragma unroll
+                for (int q = 0; q < 2; q++)
+                    missJ |= ((needJ >> q) & 1u) && (unsigned int)(wJ[q] >> 32) != ep ? 1u << q : 0u;
+                if (!(missK | missJ)) break;
+                if (spin >= SPIN_LIMIT) {
+                    *(volatile int *)&sm.abort = 1;
+                    atomicExch(a.err, 1);
+                    ok = false;   // still arrive below, so that the chunk's copies can be waited for
+                    break;
+                }
+                if (*(volatile int *)&sm.abort) { ok = false; break; }
+                if (spin > 8) __nanosleep(64);
+#pragma unroll
+                for (int s = 0; s < CH; s++)
+                    if ((missK >> s) & 1u) wK[s] = ld_word(srcKw + (size_t)(tb + s + TK - 1) * TJ + lane);
+#pragma unroll
+                for (int q = 0; q < 2; q++) {
+                    const int e = lane + 32 * q, es = e >> 3, ew = e & 7;
+                    if ((missJ >> q) & 1u) wJ[q] = ld_word(srcJw + (size_t)(tb + es + TJ - 1) * TK + ew);
+                }
+            }
+#pragma unroll
+            for (int s = 0; s < CH; s++) vK[s] = __uint_as_float((unsigned int)wK[s]);
+#pragma unroll
+            for (int q = 0; q < 2; q++) vJ[q] = __uint_as_float((unsigned int)wJ[q]);
+#pragma unroll
+            for (int s = 0; s < CH; s++) sl.eK[s][lane] = vK[s];
+#pragma unroll
+            for (int q = 0; q < 2; q++) {
+                const int e = lane + 32 * q;
+                sl.eJ[e >> 3][e & 7] = vJ[q];
+            }
+            if (lane == 0) bulk_wait_read_all();   // the slot's results of chunk m - NBUF are out
+            __syncwarp();
+            mb_arrive(&sm.full[b]);
+        }
+        if (!ok) {
+            // Stopping early: the operand copies already started must land
+            // before the CTA's shared memory is released.  Their phases have
+            // all arrivals, so each completes once its bytes are in.
+            for (int m = max(0, lastIssued - NBUF + 1); m <= lastIssued; m++)
+                for (unsigned int spin = 0; spin < SPIN_LIMIT && !mb_test(&sm.full[m % NBUF], (m / NBUF) & 1); spin++)
+                    __nanosleep(32);
+        }
+        if (lane == 0) bulk_wait_all();   // every write-back complete before the CTA ends
+        return;
+    }
+
+    // ====================================================== compute warps
+    const int l = threadIdx.x & 31, w = threadIdx.x >> 5;
+    int v0 = FWD ? l + w : (TJ - 1 - l) + (TK - 1 - w);   // steps at which the own cell is interior
     int v1 = v0 + NI - 1;
-    if (!active) { v0 = 1; v1 = 0; }
+    if (!pencil_in(l, w)) { v0 = 1; v1 = 0; }
     v0 = max(v0, tlo);
     v1 = min(v1, thi);
-
-    const int srcJ = FWD ? (tj > 0 ? tile - 1 : -1) : (tj < a.ntj - 1 ? tile + 1 : -1);
-    const int srcK = FWD ? (tk > 0 ? tile - a.ntj : -1) : (tk < a.ntk - 1 ? tile + a.ntj : -1);
-    const bool rdJ = (FWD ? l == 0 : l == TJ - 1) && srcJ >= 0;   // reads the j neighbour tile
-    const bool rdK = (FWD ? w == 0 : w == TK - 1) && srcK >= 0;   // reads the k neighbour tile
     const bool pubJ = FWD ? (l == TJ - 1 && tj < a.ntj - 1) : (l == 0 && tj > 0);
     const bool pubK = FWD ? (w == TK - 1 && tk < a.ntk - 1) : (w == 0 && tk > 0);
-    const size_t rowsPerTile = (size_t)(TJ + TK) * a.I;
-    unsigned long long *pubJrow = a.xchg + tile * rowsPerTile + (size_t)w * a.I;
-    unsigned long long *pubKrow = a.xchg + tile * rowsPerTile + (size_t)(TK + l) * a.I;
-    const unsigned long long *srcJrow = a.xchg + (rdJ ? srcJ : 0) * rowsPerTile + (size_t)w * a.I;
-    const unsigned long long *srcKrow = a.xchg + (rdK ? srcK : 0) * rowsPerTile + (size_t)(TK + l) * a.I;
-    // steps whose edge word must come from the neighbour: this cell is
-    // computed and the neighbour's cell (TJ-1 or TK-1 steps later there) too
-    int nJ0 = 1, nJ1 = 0, nK0 = 1, nK1 = 0;
-    if (rdJ) {
-        const int2 rg = steps_of(srcJ);
-        nJ0 = max(v0, rg.x - (TJ - 1));
-        nJ1 = min(v1, rg.y - (TJ - 1));
-    }
-    if (rdK) {
-        const int2 rg = steps_of(srcK);
-        nK0 = max(v0, rg.x - (TK - 1));
-        nK1 = min(v1, rg.y - (TK - 1));
-    }
-    const unsigned int ep = a.epoch;
-
-    struct Chunk {
-        float4 L[CH];
-        float r[CH];
-        unsigned long long eJ[CH], eK[CH];
-        unsigned int needJ, needK;   // bit s: the edge word of step s comes from the neighbour
-    };
-    auto cell = [&](int t) { return FWD ? i0 + t : i0 - t; };
-    auto load = [&](Chunk &d, int tb) {
-        d.needJ = 0;
-        d.needK = 0;
-#pragma unroll
-        for (int s = 0; s < CH; s++) {
-            const int t = tb + s;
-            const int i = cell(t);
-            const int ic = min(max(i, 0), a.I - 1);
-            d.L[s] = __ldg(Lrow + ic);
-            d.r[s] = __ldg(Rrow + ic);
-            const bool nj = t >= nJ0 && t <= nJ1, nk = t >= nK0 && t <= nK1;
-            d.eJ[s] = nj ? ld_word(srcJrow + i) : 0ull;
-            d.eK[s] = nk ? ld_word(srcKrow + i) : 0ull;
-            d.needJ |= nj ? 1u << s : 0u;
-            d.needK |= nk ? 1u << s : 0u;
-        }
-    };
-    // Re-poll the edge words of the chunk that are not yet of this sweep;
-    // false when the wait gave up (or another tile raised the error flag).
-    auto settle = [&](Chunk &d, int tb) -> bool {
-        if (!(d.needJ | d.needK)) return true;
-        unsigned int spin = 0;
-        for (;;) {
-            unsigned int missJ = 0, missK = 0;
-#pragma unroll
-            for (int s = 0; s < CH; s++) {
-                missJ |= ((d.needJ >> s) & 1u) && (unsigned int)(d.eJ[s] >> 32) != ep ? 1u << s : 0u;
-                missK |= ((d.needK >> s) & 1u) && (unsigned int)(d.eK[s] >> 32) != ep ? 1u << s : 0u;
-            }
-            if (!(missJ | missK)) return true;
-            if (++spin > SPIN_LIMIT || *(volatile int *)a.err) return false;
-            if (spin > 8) __nanosleep(64);
-#pragma unroll
-            for (int s = 0; s < CH; s++) {
-                const int i = cell(tb + s);
-                if ((missJ >> s) & 1u) d.eJ[s] = ld_word(srcJrow + i);
-                if ((missK >> s) & 1u) d.eK[s] = ld_word(srcKrow + i);
-            }
-        }
-    };
-
-    shP[0][w][l] = 0.0f;
-    shP[1][w][l] = 0.0f;
+    unsigned long long *pubJw = a.xchg + tile * wordsPerTile + w;                     // [t][TK]
+    unsigned long long *pubKw = a.xchg + tile * wordsPerTile + (size_t)T * TK + l;    // [t][TJ]
+    sm.p[0][w][l] = 0.0f;
+    sm.p[1][w][l] = 0.0f;
     // forward: this pencil's terms from its last cell, L_x y (own next cell)
     // and L_y y (lane l+1); backward: z of its last cell
     float px = 0.0f, pz = 0.0f, zPrev = 0.0f;
-    auto run = [&](Chunk &cur, Chunk &nxt, int tb) -> bool {
-        const bool fine = settle(cur, tb);
-        if (__syncthreads_or(!fine)) {
-            if (!fine) atomicExch(a.err, 1);
-            return false;
+    for (int n = 0; n < nChunks; n++) {
+        const int b = n % NBUF, tb = tlo + n * CH;
+        const bool fine = mb_wait(&sm.full[b], (n / NBUF) & 1, &sm.abort, a.err);
+        if (compute_sync_or(!fine)) {
+            *(volatile int *)&sm.abort = 1;
+            return;
         }
-        if (tb + CH <= thi) load(nxt, tb + CH);
+        Slot &sl = sm.slot[b];
         const int par = tb & 1;
 #pragma unroll
         for (int s = 0; s < CH; s++) {
             const int t = tb + s;
+            const int q = FWD ? s : CH - 1 - s;
             const int cb = (s & 1) ^ par, pb = cb ^ 1;   // buffers of steps t and t-1
-            const float4 Lc = cur.L[s];
+            const float4 Lc = sl.L[q][threadIdx.x];
+            const float rr = sl.r[q][threadIdx.x];
+            const bool valid = t >= v0 && t <= v1;
             float res;
             if (FWD) {
                 float pJ = __shfl_up_sync(0xffffffffu, pz, 1);
-                if (l == 0) pJ = word_value(cur.eJ[s]);
-                const float pK = w > 0 ? shP[pb][w - 1][l] : word_value(cur.eK[s]);
-                float acc = __fsub_rn(cur.r[s], pK);
+                if (l == 0) pJ = sl.eJ[s][w];
+                const float pK = w > 0 ? sm.p[pb][w - 1][l] : sl.eK[s][l];
+                float acc = __fsub_rn(rr, pK);
                 acc = __fsub_rn(acc, pJ);
                 acc = __fsub_rn(acc, px);
                 res = __fmul_rn(acc, Lc.x);
                 px = __fmul_rn(Lc.y, res);
                 pz = __fmul_rn(Lc.z, res);
                 const float pw = __fmul_rn(Lc.w, res);
-                shP[cb][w][l] = pw;
-                const bool valid = t >= v0 && t <= v1;
-                const int i = cell(t);
-                if (valid) Orow[i] = res;
-                if (valid && pubJ) st_word(pubJrow + i, pack(ep, pz));
-                if (valid && pubK) st_word(pubKrow + i, pack(ep, pw));
+                sm.p[cb][w][l] = pw;
+                if (valid && pubJ) st_word(pubJw + (size_t)t * TK, pack(ep, pz));
+                if (valid && pubK) st_word(pubKw + (size_t)t * TJ, pack(ep, pw));
             } else {
                 float zJ = __shfl_down_sync(0xffffffffu, zPrev, 1);
-                if (l == TJ - 1) zJ = word_value(cur.eJ[s]);
-                const float zK = w < TK - 1 ? shP[pb][w + 1][l] : word_value(cur.eK[s]);
-                float acc = __fsub_rn(cur.r[s], __fmul_rn(Lc.y, zPrev));
+                if (l == TJ - 1) zJ = sl.eJ[s][w];
+                const float zK = w < TK - 1 ? sm.p[pb][w + 1][l] : sl.eK[s][l];
+                float acc = __fsub_rn(rr, __fmul_rn(Lc.y, zPrev));
                 acc = __fsub_rn(acc, __fmul_rn(Lc.z, zJ));
                 acc = __fsub_rn(acc, __fmul_rn(Lc.w, zK));
                 res = __fmul_rn(acc, Lc.x);
                 zPrev = res;
-                shP[cb][w][l] = res;
-                const bool valid = t >= v0 && t <= v1;
-                const int i = cell(t);
-                if (valid) Orow[i] = res;
-                if (valid && pubJ) st_word(pubJrow + i, pack(ep, res));
-                if (valid && pubK) st_word(pubKrow + i, pack(ep, res));
+                sm.p[cb][w][l] = res;
+                if (valid && pubJ) st_word(pubJw + (size_t)t * TK, pack(ep, res));
+                if (valid && pubK) st_word(pubKw + (size_t)t * TJ, pack(ep, res));
             }
+            sl.o[q][threadIdx.x] = res;
             if (t == thi) break;
-            __syncthreads();
+            compute_sync();
         }
-        return true;
-    };
-
-    Chunk A, B;
-    load(A, tlo);
-    for (int tb = tlo; tb <= thi; tb += 2 * CH) {
-        if (!run(A, B, tb)) return;
-        if (tb + CH > thi) break;
-        if (!run(B, A, tb + CH)) return;
+        fence_proxy_async();   // the results are read by the bulk store
+        mb_arrive(&sm.done[b]);
     }
 }
 
@@ -288,9 +392,10 @@ int sweep_tiles(int J, int K, int *ntj, int *ntk) {
     *ntk = (K - 2 + TK - 1) / TK;
     return *ntj * *ntk;
 }
+// per tile: TK j-edge words and TJ k-edge words for each of its T steps
 long long sweep_exchange_words(int I, int J, int K) {
-    int ntj, ntk;
-    return (long long)sweep_tiles(J, K, &ntj, &ntk) * (TJ + TK) * I;
+    const SweepLayout g = sweep_layout(I, J, K);
+    return (long long)g.ntj * g.ntk * (TJ + TK) * g.T;
 }
 
 void launch_sweep_ranges(const StepConsts &c, const uint8_t *fluid, SweepState &sw, cudaStream_t s) {
@@ -304,25 +409,37 @@ void launch_sweep_ranges(const StepConsts &c, const uint8_t *fluid, SweepState &
 }
 
 void launch_sweeps(const StepConsts &c, const float4 *L, const float *rf, float *z, SweepState &sw, cudaStream_t s) {
-    int ntj, ntk;
-    int n = sweep_tiles(c.J, c.K, &ntj, &ntk);
+    const SweepLayout g = sweep_layout(c.I, c.J, c.K);
+    const int n = g.ntj * g.ntk;
+    static unsigned long long smemSet = 0;   // devices on which the slots' shared memory is opted in
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 64 && !((smemSet >> dev) & 1ull)) {
+        cudaFuncSetAttribute(k_wavefront<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SweepSmem));
+        cudaFuncSetAttribute(k_wavefront<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SweepSmem));
+        smemSet |= 1ull << dev;
+    }
     if (sw.epoch >= 0xfffffff0u) {   // epochs are about to wrap: forget every old word
         cudaMemsetAsync(sw.xchg, 0, sweep_exchange_words(c.I, c.J, c.K) * sizeof(unsigned long long), s);
         sw.epoch = 0;
     }
     SweepArgs a;
-    a.L = L; a.rin = rf; a.out = z;
-    a.I = c.I; a.J = c.J; a.K = c.K;
-    a.ntj = ntj; a.ntk = ntk;
+    a.L = L;
+    a.J = c.J; a.K = c.K; a.NI = c.I - 2; a.T = g.T;
+    a.ntj = g.ntj; a.ntk = g.ntk;
     a.range = sw.range; a.xchg = sw.xchg; a.ticket = sw.ticket; a.err = sw.err;
+    // forward: y from r
+    a.rin = rf; a.out = z;
     a.epoch = ++sw.epoch;
     a.ticketBase = (unsigned int)(sw.launches * n);
     sw.launches++;
-    { FLIP_COUNT(1); k_wavefront<true><<<n, NTHREADS, 0, s>>>(a); }
+    { FLIP_COUNT(1); k_wavefront<true><<<n, NTHREADS, sizeof(SweepSmem), s>>>(a); }
+    // backward: z from y, in place
+    a.rin = z; a.out = z;
     a.epoch = ++sw.epoch;
     a.ticketBase = (unsigned int)(sw.launches * n);
     sw.launches++;
-    { FLIP_COUNT(1); k_wavefront<false><<<n, NTHREADS, 0, s>>>(a); }
+    { FLIP_COUNT(1); k_wavefront<false><<<n, NTHREADS, sizeof(SweepSmem), s>>>(a); }
 }
 
 }  // namespace flip
