@@ -105,6 +105,18 @@ __device__ __forceinline__ long long sweep_index(const SweepLayout &g, int i, in
     return ((long long)tile * g.T + (i - 1 + l + w)) * SWEEP_NP + w * SWEEP_TJ + l;
 }
 
+// Device-side control of the PCG loop: the convergence test runs on the
+// device, so the host enqueues iterations in batches and reads this once per
+// batch; every kernel of an iteration returns at once when done is set.
+struct PcgCtl {
+    int done;      // converged
+    int iters;     // iterations to convergence
+    int claim;     // the recurrence residual passed the test; b - A x must confirm
+    int pad;
+    double resid;  // last residual norm tested
+};
+constexpr int PCG_BATCH = 8;   // iterations enqueued between host checks
+
 struct PressureBuffers {
     uint8_t *fluid;        // interior cell with phi < 0 (a row of the system)
     double4 *Ad;           // rows {diag, to +x, to +y, to +z}, FP64
@@ -118,7 +130,8 @@ struct PressureBuffers {
     SweepLayout sl;
     double *partials;      // per-block partial sums (deterministic reduction)
     double *scal;          // [0]=s.q [1]=z.r (new rho) [2]=|b|inf [3]=rho [4]=alpha [5]=beta
-    unsigned long long *rmaxBits;  // |r|inf as double bits
+    unsigned long long *rmaxBits;  // [0] |r|inf of the recurrence, [1] of b - A x, as double bits
+    PcgCtl *ctl;
     int *levelRange;       // [0]=min(i+j+k) [1]=max(i+j+k) [2]=system size
     float *pressure;       // float copy of x for the velocity update
     int nPartials;
@@ -135,7 +148,7 @@ struct PressureArgs {
 };
 // Device time of the preconditioner sweeps, summed over launches.
 struct SweepTiming {
-    cudaEvent_t ev[2];
+    cudaEvent_t ev[2 * (PCG_BATCH + 1)];   // a pair per sweep pair of a batch, plus the first
     double ms;
     long long launches;     // sweep kernels (forward and backward count one each)
     long long cellSweeps;   // sum over launches of the system rows swept
@@ -143,7 +156,7 @@ struct SweepTiming {
 struct PressureMail {      // pinned host scalars
     int levelRange[3];
     double bmax, rho;
-    unsigned long long rmaxBits;
+    PcgCtl ctl;
     int sweepErr;
 };
 struct PressureResult {
@@ -167,7 +180,9 @@ int sweep_tiles(int J, int K, int *ntj, int *ntk);
 long long sweep_exchange_words(int I, int J, int K);
 void launch_sweep_ranges(const StepConsts &c, const uint8_t *fluid, SweepState &sw, cudaStream_t s);
 // z = M^-1 r with the MIC(0) factor L: forward then backward sweep
-void launch_sweeps(const StepConsts &c, const float4 *L, const float *rf, float *z, SweepState &sw, cudaStream_t s);
+// The launches return at once when *skip is set (a converged solve).
+void launch_sweeps(const StepConsts &c, const float4 *L, const float *rf, float *z, SweepState &sw, const int *skip,
+                   cudaStream_t s);
 
 int pressure_partials(const StepConsts &c);
 // PressureSolver::solve (pressuresolver.cpp:44-76) on the device.  Returns

@@ -192,7 +192,7 @@ int alloc_grids(flip_ctx *x) {
     CK(cudaMemsetAsync(p.z, 0, nsl * sizeof(float), x->stream));
     p.nPartials = pressure_partials(x->c);
     if ((rc = x->alloc(&p.partials, p.nPartials + 32)) || (rc = x->alloc(&p.scal, 8)) ||
-        (rc = x->alloc(&p.rmaxBits, 2)) || (rc = x->alloc(&p.levelRange, 4)))
+        (rc = x->alloc(&p.rmaxBits, 2)) || (rc = x->alloc(&p.levelRange, 4)) || (rc = x->alloc(&p.ctl, 1)))
         return rc;
     {
         int ntj, ntk;
@@ -654,7 +654,7 @@ int flip_destroy(flip_ctx *x) {
     cudaStreamSynchronize(x->stream);
     for (int q = 0; q <= FLIP_NUM_STAGES; q++)
         if (x->ev[q]) cudaEventDestroy(x->ev[q]);
-    for (int q = 0; q < 2; q++)
+    for (int q = 0; q < 2 * (PCG_BATCH + 1); q++)
         if (x->sweepTiming.ev[q]) cudaEventDestroy(x->sweepTiming.ev[q]);
     for (void *p : x->allocations) cudaFree(p);
     if (x->mail) cudaFreeHost(x->mail);
@@ -856,7 +856,7 @@ int flip_set_stage_timing(flip_ctx *x, int enable) {
     CK(cudaStreamSynchronize(x->stream));
     if (enable && !x->ev[0]) {
         for (int q = 0; q <= FLIP_NUM_STAGES; q++) CK(cudaEventCreate(&x->ev[q]));
-        for (int q = 0; q < 2; q++) CK(cudaEventCreate(&x->sweepTiming.ev[q]));
+        for (int q = 0; q < 2 * (PCG_BATCH + 1); q++) CK(cudaEventCreate(&x->sweepTiming.ev[q]));
     }
     x->timing = enable != 0;
     for (int q = 0; q < FLIP_NUM_STAGES; q++) x->stageMs[q] = 0.0;

@@ -196,8 +196,11 @@ __global__ void k_gather(ParticleSoA src, ParticleSoA dst, const int *start, con
 // every particle whose search box reaches the block updates the block's
 // cells with min(|c - p| - r) in the block's own float frame
 // (particlelevelset.cpp:582-629).  Min is order-free, so the result is
-// bit-identical to the reference.  Then the solid post-process
-// (particlelevelset.cpp:172-196).
+// bit-identical to the reference.  Rounded square root and the subtraction
+// of r are both monotone, so min over particles of fl(fl(sqrt(d2)) - r)
+// equals fl(fl(sqrt(min d2)) - r): the particle loop keeps the smallest
+// squared distance per cell and each cell takes one square root at the end.
+// Then the solid post-process (particlelevelset.cpp:172-196).
 constexpr int BW = 10;
 
 // Does the reference's count pass put particle p in block (bx,by,bz)'s list?
@@ -222,12 +225,12 @@ __device__ __forceinline__ bool in_block_list(float px, float py, float pz, floa
 
 __global__ void __launch_bounds__(TPB) k_liquid_sdf(ParticleSoA p, const int *cellStart, StepConsts c,
                                                     const uint8_t *solidCC, float *phi) {
-    __shared__ unsigned int smin[BW * BW * BW];
+    __shared__ unsigned int smin[BW * BW * BW];   // bits of the smallest squared distance (>= 0)
     __shared__ float centre[BW];
     const int bx = blockIdx.x, by = blockIdx.y, bz = blockIdx.z;
     const double dx = c.dx;
     const float maxd = (float)(3.0 * dx);
-    for (int q = threadIdx.x; q < BW * BW * BW; q += blockDim.x) smin[q] = f2ord(maxd);
+    for (int q = threadIdx.x; q < BW * BW * BW; q += blockDim.x) smin[q] = 0x7f800000u;   // +inf
     if (threadIdx.x < BW) centre[threadIdx.x] = cell_centre(threadIdx.x, dx);
     __syncthreads();
 
@@ -259,14 +262,15 @@ __global__ void __launch_bounds__(TPB) k_liquid_sdf(ParticleSoA p, const int *ce
             int b1 = min(exact_floor(__fadd_rn(ly, sr), c.invdx, c.invdxf), BW - 1);
             int c1 = min(exact_floor(__fadd_rn(lz, sr), c.invdx, c.invdxf), BW - 1);
             for (int cc = c0; cc <= c1; cc++) {
-                float dz = __fsub_rn(centre[cc], lz);
+                const float dz = __fsub_rn(centre[cc], lz);
+                const float dz2 = __fmul_rn(dz, dz);
                 for (int bb = b0; bb <= b1; bb++) {
-                    float dy = __fsub_rn(centre[bb], ly);
+                    const float dy = __fsub_rn(centre[bb], ly);
+                    const float dy2 = __fmul_rn(dy, dy);
                     for (int aa = a0; aa <= a1; aa++) {
-                        float ddx = __fsub_rn(centre[aa], lx);
-                        float d2 = __fadd_rn(__fadd_rn(__fmul_rn(ddx, ddx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
-                        float dist = __fsub_rn(__fsqrt_rn(d2), r);
-                        atomicMin(&smin[aa + BW * (bb + BW * cc)], f2ord(dist));
+                        const float ddx = __fsub_rn(centre[aa], lx);
+                        const float d2 = __fadd_rn(__fadd_rn(__fmul_rn(ddx, ddx), dy2), dz2);
+                        atomicMin(&smin[aa + BW * (bb + BW * cc)], __float_as_uint(d2));
                     }
                 }
             }
@@ -281,7 +285,8 @@ __global__ void __launch_bounds__(TPB) k_liquid_sdf(ParticleSoA p, const int *ce
         int gi = bx * BW + a, gj = by * BW + b, gk = bz * BW + cz;
         if (!cells.in(gi, gj, gk)) continue;
         long long ci = cells.idx(gi, gj, gk);
-        float val = ord2f(smin[q]);
+        const unsigned int m = smin[q];
+        float val = m == 0x7f800000u ? maxd : fminf(maxd, __fsub_rn(__fsqrt_rn(__uint_as_float(m)), r));
         if ((double)val < half && solidCC[ci]) val = neg;
         if (fabsf(val) < eps) val = val > 0 ? eps : -eps;
         phi[ci] = val;

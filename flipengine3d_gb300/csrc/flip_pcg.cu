@@ -233,8 +233,9 @@ __device__ __forceinline__ T block_sum(T v, T *sh) {
 
 // q = A s (FP64), block partials of s.q
 __global__ void k_spmv(StepConsts c, const uint8_t *fluid, const double4 *Ad, const float *s, double *q,
-                       double *partials) {
+                       double *partials, const PcgCtl *ctl) {
     __shared__ double sh[32];
+    if (ctl->done) return;
     const long long n = (long long)c.I * c.J * c.K;
     const long long sy = c.I, sz = (long long)c.I * c.J;
     double part = 0.0;
@@ -256,8 +257,9 @@ __global__ void k_spmv(StepConsts c, const uint8_t *fluid, const double4 *Ad, co
 }
 
 __global__ void k_dot_zr(StepConsts c, SweepLayout g, const uint8_t *fluid, const float *z, const double *r,
-                         double *partials) {
+                         double *partials, const PcgCtl *ctl) {
     __shared__ double sh[32];
+    if (ctl->done) return;
     const long long n = (long long)c.I * c.J * c.K;
     double part = 0.0;
     for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x)
@@ -270,22 +272,32 @@ __global__ void k_dot_zr(StepConsts c, SweepLayout g, const uint8_t *fluid, cons
 // then the step length that depends on it, once for all threads: for s.q
 // (slot 0) alpha = rho / s.q, for z.r (slot 1) beta = rho_new / rho, each
 // rounded to float as BLAS::addScaled takes it (blaswrapper.h:129-158).
-__global__ void k_sum_partials(const double *partials, int n, double *scal, int slot) {
+// For s.q it also clears the iteration's residual norms.
+__global__ void k_sum_partials(const double *partials, int n, double *scal, int slot, const PcgCtl *ctl,
+                               unsigned long long *rmaxBits) {
     __shared__ double sh[32];
+    if (ctl->done) return;
     double v = 0.0;
     for (int q = threadIdx.x; q < n; q += blockDim.x) v += partials[q];
     double s = block_sum(v, sh);
     if (threadIdx.x == 0) {
         scal[slot] = s;
-        if (slot == 0) scal[4] = (double)(float)(scal[3] / s);
-        else scal[5] = scal[3] != 0.0 ? (double)(float)(s / scal[3]) : 0.0;
+        if (slot == 0) {
+            scal[4] = (double)(float)(scal[3] / s);
+            rmaxBits[0] = 0ull;
+            rmaxBits[1] = 0ull;
+        } else {
+            scal[5] = scal[3] != 0.0 ? (double)(float)(s / scal[3]) : 0.0;
+        }
     }
 }
 
 // x += alpha s, r -= alpha q with alpha = rho / s.q passed on as float, as
 // BLAS::addScaled(float alpha, ...) does (blaswrapper.h:129-158); |r|inf
 __global__ void k_update_xr(StepConsts c, SweepLayout g, const uint8_t *fluid, double *x, double *r, float *rf,
-                            const float *s, const double *q, const double *scal, unsigned long long *rmaxBits) {
+                            const float *s, const double *q, const double *scal, unsigned long long *rmaxBits,
+                            const PcgCtl *ctl) {
+    if (ctl->done) return;
     const long long n = (long long)c.I * c.J * c.K;
     const double alpha = scal[4];
     double m = 0.0;
@@ -301,9 +313,13 @@ __global__ void k_update_xr(StepConsts c, SweepLayout g, const uint8_t *fluid, d
     block_max_to(m, rmaxBits);
 }
 
-// r = b - A x (residual replacement); |r|inf
+// r = b - A x (residual replacement); |r|inf.  Inside the loop: skipped
+// once converged, and with onlyOnClaim unless the recurrence just claimed
+// convergence.
 __global__ void k_true_residual(StepConsts c, SweepLayout g, const uint8_t *fluid, const double4 *Ad, const double *b,
-                                const double *x, double *r, float *rf, unsigned long long *rmaxBits) {
+                                const double *x, double *r, float *rf, unsigned long long *rmaxBits,
+                                const PcgCtl *ctl, int onlyOnClaim) {
+    if (ctl && (ctl->done || (onlyOnClaim && !ctl->claim))) return;
     const long long n = (long long)c.I * c.J * c.K;
     const long long sy = c.I, sz = (long long)c.I * c.J;
     double m = 0.0;
@@ -343,7 +359,8 @@ __global__ void k_init_r(StepConsts c, SweepLayout g, const double *b, double *r
 
 // s = z + beta s, beta = rho_new / rho as float (pcgsolver.h:295-298)
 __global__ void k_update_s(StepConsts c, SweepLayout g, const uint8_t *fluid, const float *z, float *s,
-                           const double *scal) {
+                           const double *scal, const PcgCtl *ctl) {
+    if (ctl->done) return;
     long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const float beta = (float)scal[5];
     if (t < (long long)c.I * c.J * c.K && fluid[t]) s[t] = __fmaf_rn(beta, s[t], z[sweep_index_of(c, g, t)]);
@@ -354,7 +371,39 @@ __global__ void k_copy_zs(StepConsts c, SweepLayout g, const uint8_t *fluid, con
     if (t < (long long)c.I * c.J * c.K) s[t] = fluid[t] ? z[sweep_index_of(c, g, t)] : 0.0f;
 }
 
-__global__ void k_set_rho(double *scal) { scal[3] = scal[1]; }
+__global__ void k_set_rho(double *scal, const PcgCtl *ctl) {
+    if (!ctl->done) scal[3] = scal[1];
+}
+
+// The reference's convergence test |r|inf <= tol |b|inf (pcgsolver.h:
+// 263-288) on the device.  After the update of iteration it: on the
+// iterations where r was recomputed as b - A x (every 25th) that norm
+// decides; otherwise a pass of the recurrence's norm is only a claim, which
+// k_confirm settles on b - A x.
+__global__ void k_check(PcgCtl *ctl, const unsigned long long *rmaxBits, double ptol, int it, int periodic) {
+    if (ctl->done) return;
+    const double resid = __longlong_as_double((long long)rmaxBits[periodic ? 1 : 0]);
+    ctl->resid = resid;
+    ctl->claim = 0;
+    if (resid <= ptol) {
+        if (periodic) {
+            ctl->done = 1;
+            ctl->iters = it + 1;
+        } else {
+            ctl->claim = 1;
+        }
+    }
+}
+__global__ void k_confirm(PcgCtl *ctl, const unsigned long long *rmaxBits, double ptol, int it) {
+    if (ctl->done || !ctl->claim) return;
+    const double resid = __longlong_as_double((long long)rmaxBits[1]);
+    ctl->resid = resid;
+    ctl->claim = 0;
+    if (resid <= ptol) {
+        ctl->done = 1;
+        ctl->iters = it + 1;
+    }
+}
 
 __global__ void k_x_to_float(long long n, const double *x, float *p) {
     long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -476,49 +525,31 @@ int pressure_project(const StepConsts &c, const PressureArgs &a, PressureBuffers
     launch_sweep_ranges(c, pb.fluid, sw, s);
 
     unsigned long long *rmax = pb.rmaxBits;
-    bool sweepPending = false;
-    auto tally = [&]() {   // add the last timed sweep pair once its events are complete
-        if (!sweepPending) return;
+    SweepTiming *tm = a.sweepTiming;
+    // sweep pairs timed but not yet added: event pair index q
+    auto tally_pair = [&](int q) {
         float ms = 0.0f;
-        if (cudaEventElapsedTime(&ms, a.sweepTiming->ev[0], a.sweepTiming->ev[1]) == cudaSuccess) {
-            a.sweepTiming->ms += ms;
-            a.sweepTiming->launches += 2;
-            a.sweepTiming->cellSweeps += 2LL * res->cells;
+        if (cudaEventElapsedTime(&ms, tm->ev[2 * q], tm->ev[2 * q + 1]) == cudaSuccess) {
+            tm->ms += ms;
+            tm->launches += 2;
+            tm->cellSweeps += 2LL * res->cells;
         }
-        sweepPending = false;
     };
-    auto read_rmax = [&](double *out, int *sweepErr) -> cudaError_t {
-        cudaError_t e = cudaMemcpyAsync(&mail->rmaxBits, rmax, sizeof(unsigned long long), cudaMemcpyDeviceToHost, s);
-        if (e == cudaSuccess) e = cudaMemcpyAsync(&mail->sweepErr, sw.err, sizeof(int), cudaMemcpyDeviceToHost, s);
-        if (e == cudaSuccess) e = sync();
-        if (e != cudaSuccess) return e;
-        tally();
-        std::memcpy(out, &mail->rmaxBits, sizeof(double));
-        *sweepErr = mail->sweepErr;
-        return cudaSuccess;
-    };
-    auto precondition = [&]() {
-        if (a.sweepTiming) cudaEventRecord(a.sweepTiming->ev[0], s);
-        launch_sweeps(c, pb.L, pb.rf, pb.z, sw, s);
-        if (a.sweepTiming) {
-            cudaEventRecord(a.sweepTiming->ev[1], s);
-            sweepPending = true;
-        }
-        { FLIP_COUNT(1); k_dot_zr<<<rb, TPB, 0, s>>>(c, pb.sl, pb.fluid, pb.z, pb.r, pb.partials); }
-        { FLIP_COUNT(1); k_sum_partials<<<1, 1024, 0, s>>>(pb.partials, pb.nPartials, pb.scal, 1); }
-    };
-    auto residual = [&]() {
-        PCK(cudaMemsetAsync(rmax, 0, sizeof(unsigned long long), s));
-        { FLIP_COUNT(1); k_true_residual<<<rb, TPB, 0, s>>>(c, pb.sl, pb.fluid, pb.Ad, pb.b, pb.x, pb.r, pb.rf, rmax); }
-        return FLIP_OK;
+    auto precondition = [&](int q) {   // z = M^-1 r, then rho_new = z.r
+        if (tm) cudaEventRecord(tm->ev[2 * q], s);
+        launch_sweeps(c, pb.L, pb.rf, pb.z, sw, &pb.ctl->done, s);
+        if (tm) cudaEventRecord(tm->ev[2 * q + 1], s);
+        { FLIP_COUNT(1); k_dot_zr<<<rb, TPB, 0, s>>>(c, pb.sl, pb.fluid, pb.z, pb.r, pb.partials, pb.ctl); }
+        { FLIP_COUNT(1); k_sum_partials<<<1, 1024, 0, s>>>(pb.partials, pb.nPartials, pb.scal, 1, pb.ctl, rmax); }
     };
 
-    PCK(cudaMemsetAsync(rmax, 0, sizeof(unsigned long long), s));
+    PCK(cudaMemsetAsync(pb.ctl, 0, sizeof(PcgCtl), s));
+    PCK(cudaMemsetAsync(rmax, 0, 2 * sizeof(unsigned long long), s));
     { FLIP_COUNT(1); k_init_r<<<rb, TPB, 0, s>>>(c, pb.sl, pb.b, pb.r, pb.rf, rmax); }
-    precondition();
+    precondition(0);
     PCK(cudaMemcpyAsync(&mail->rho, pb.scal + 1, sizeof(double), cudaMemcpyDeviceToHost, s));
     PCK(sync());
-    tally();
+    if (tm) tally_pair(0);
     const double rho0 = mail->rho;
     bool ok = false;
     int iterations = 0;
@@ -526,32 +557,48 @@ int pressure_project(const StepConsts &c, const PressureArgs &a, PressureBuffers
     int sweepErr = 0;
     if (!(rho0 == 0 || rho0 != rho0)) {
         { FLIP_COUNT(1); k_copy_zs<<<nb, TPB, 0, s>>>(c, pb.sl, pb.fluid, pb.z, pb.s); }
-        { FLIP_COUNT(1); k_set_rho<<<1, 1, 0, s>>>(pb.scal); }
-        int it;
-        for (it = 0; it < a.maxIter; it++) {
-            { FLIP_COUNT(1); k_spmv<<<rb, TPB, 0, s>>>(c, pb.fluid, pb.Ad, pb.s, pb.q, pb.partials); }
-            { FLIP_COUNT(1); k_sum_partials<<<1, 1024, 0, s>>>(pb.partials, pb.nPartials, pb.scal, 0); }
-            PCK(cudaMemsetAsync(rmax, 0, sizeof(unsigned long long), s));
-            { FLIP_COUNT(1); k_update_xr<<<rb, TPB, 0, s>>>(c, pb.sl, pb.fluid, pb.x, pb.r, pb.rf, pb.s, pb.q, pb.scal, rmax); }
-            const bool periodic = (it + 1) % 25 == 0;
-            if (periodic) residual();
-            PCK(read_rmax(&resid, &sweepErr));
-            if (sweepErr) break;
-            if (resid <= ptol && !periodic) {   // confirm on b - A x
-                residual();
-                PCK(read_rmax(&resid, &sweepErr));
-                if (sweepErr) break;
+        { FLIP_COUNT(1); k_set_rho<<<1, 1, 0, s>>>(pb.scal, pb.ctl); }
+        // Iterations go to the device PCG_BATCH at a time; the convergence
+        // test runs there, and the kernels of iterations after convergence
+        // return at once.  The host reads the outcome once per batch.
+        for (int it0 = 0; it0 < a.maxIter;) {
+            const int nit = std::min(PCG_BATCH, a.maxIter - it0);
+            for (int k = 0; k < nit; k++) {
+                const int it = it0 + k;
+                const int periodic = (it + 1) % 25 == 0;
+                { FLIP_COUNT(1); k_spmv<<<rb, TPB, 0, s>>>(c, pb.fluid, pb.Ad, pb.s, pb.q, pb.partials, pb.ctl); }
+                { FLIP_COUNT(1); k_sum_partials<<<1, 1024, 0, s>>>(pb.partials, pb.nPartials, pb.scal, 0, pb.ctl, rmax); }
+                { FLIP_COUNT(1); k_update_xr<<<rb, TPB, 0, s>>>(c, pb.sl, pb.fluid, pb.x, pb.r, pb.rf, pb.s, pb.q, pb.scal, rmax, pb.ctl); }
+                if (periodic) {
+                    FLIP_COUNT(1);
+                    k_true_residual<<<rb, TPB, 0, s>>>(c, pb.sl, pb.fluid, pb.Ad, pb.b, pb.x, pb.r, pb.rf, rmax + 1, pb.ctl, 0);
+                }
+                { FLIP_COUNT(1); k_check<<<1, 1, 0, s>>>(pb.ctl, rmax, ptol, it, periodic); }
+                if (!periodic) {   // confirm a claim on b - A x
+                    { FLIP_COUNT(1); k_true_residual<<<rb, TPB, 0, s>>>(c, pb.sl, pb.fluid, pb.Ad, pb.b, pb.x, pb.r, pb.rf, rmax + 1, pb.ctl, 1); }
+                    { FLIP_COUNT(1); k_confirm<<<1, 1, 0, s>>>(pb.ctl, rmax, ptol, it); }
+                }
+                precondition(1 + k);
+                { FLIP_COUNT(1); k_update_s<<<nb, TPB, 0, s>>>(c, pb.sl, pb.fluid, pb.z, pb.s, pb.scal, pb.ctl); }
+                { FLIP_COUNT(1); k_set_rho<<<1, 1, 0, s>>>(pb.scal, pb.ctl); }
             }
-            if (resid <= ptol) {
-                iterations = it + 1;
+            PCK(cudaMemcpyAsync(&mail->ctl, pb.ctl, sizeof(PcgCtl), cudaMemcpyDeviceToHost, s));
+            PCK(cudaMemcpyAsync(&mail->sweepErr, sw.err, sizeof(int), cudaMemcpyDeviceToHost, s));
+            PCK(sync());
+            sweepErr = mail->sweepErr;
+            resid = mail->ctl.resid;
+            if (tm)   // the sweep pairs that ran: all before convergence
+                for (int k = 0; k < nit; k++)
+                    if (!mail->ctl.done || it0 + k < mail->ctl.iters - 1) tally_pair(1 + k);
+            if (sweepErr) break;
+            if (mail->ctl.done) {
                 ok = true;
+                iterations = mail->ctl.iters;
                 break;
             }
-            precondition();
-            { FLIP_COUNT(1); k_update_s<<<nb, TPB, 0, s>>>(c, pb.sl, pb.fluid, pb.z, pb.s, pb.scal); }
-            { FLIP_COUNT(1); k_set_rho<<<1, 1, 0, s>>>(pb.scal); }
+            it0 += nit;
         }
-        if (!ok) iterations = it;
+        if (!ok) iterations = a.maxIter;
     }
     if (sweepErr) {
         cudaMemsetAsync(sw.err, 0, sizeof(int), s);
@@ -560,10 +607,6 @@ int pressure_project(const StepConsts &c, const PressureArgs &a, PressureBuffers
         sync();
         if (errMsg) *errMsg = "a wavefront sweep gave up waiting for a neighbouring tile";
         return FLIP_E_DEVICE_TIMEOUT;
-    }
-    if (sweepPending) {
-        PCK(sync());
-        tally();
     }
     res->iterations = iterations;
     res->residual = resid;

@@ -62,6 +62,7 @@ struct SweepArgs {
     unsigned int ticketBase;
     unsigned int epoch;
     int *err;
+    const int *skip;   // nonzero: return at once
 };
 
 struct Slot {
@@ -145,8 +146,12 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_wavefront(SweepArgs a) {
     SweepSmem &sm = *reinterpret_cast<SweepSmem *>(smemRaw);
     const int ntiles = a.ntj * a.ntk;
     if (threadIdx.x == 0) {
-        int t = (int)(atomicAdd(a.ticket, 1u) - a.ticketBase);
-        sm.tile = FWD ? t : ntiles - 1 - t;
+        if (*(volatile const int *)a.skip || *(volatile int *)a.err) {
+            sm.tile = -1;   // converged, or an earlier sweep gave up: nothing to do
+        } else {
+            int t = (int)(atomicAdd(a.ticket, 1u) - a.ticketBase);
+            sm.tile = FWD ? t : ntiles - 1 - t;
+        }
         sm.abort = 0;
         for (int b = 0; b < NBUF; b++) {
             mb_init(&sm.full[b], 32);      // the helper warp's lanes, plus the bytes of the chunk
@@ -252,7 +257,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_wavefront(SweepArgs a) {
                     ok = false;   // still arrive below, so that the chunk's copies can be waited for
                     break;
                 }
-                if (*(volatile int *)&sm.abort) { ok = false; break; }
+                if (*(volatile int *)&sm.abort || *(volatile int *)a.err) { ok = false; break; }
                 if (spin > 8) __nanosleep(64);
 #pragma unroll
                 for (int s = 0; s < CH; s++)
@@ -408,7 +413,8 @@ void launch_sweep_ranges(const StepConsts &c, const uint8_t *fluid, SweepState &
     sw.launches = 0;
 }
 
-void launch_sweeps(const StepConsts &c, const float4 *L, const float *rf, float *z, SweepState &sw, cudaStream_t s) {
+void launch_sweeps(const StepConsts &c, const float4 *L, const float *rf, float *z, SweepState &sw, const int *skip,
+                   cudaStream_t s) {
     const SweepLayout g = sweep_layout(c.I, c.J, c.K);
     const int n = g.ntj * g.ntk;
     static unsigned long long smemSet = 0;   // devices on which the slots' shared memory is opted in
@@ -427,7 +433,7 @@ void launch_sweeps(const StepConsts &c, const float4 *L, const float *rf, float 
     a.L = L;
     a.J = c.J; a.K = c.K; a.NI = c.I - 2; a.T = g.T;
     a.ntj = g.ntj; a.ntk = g.ntk;
-    a.range = sw.range; a.xchg = sw.xchg; a.ticket = sw.ticket; a.err = sw.err;
+    a.range = sw.range; a.xchg = sw.xchg; a.ticket = sw.ticket; a.err = sw.err; a.skip = skip;
     // forward: y from r
     a.rin = rf; a.out = z;
     a.epoch = ++sw.epoch;
