@@ -216,6 +216,10 @@ def run_gpu(args, rank, world):
     step_achieved = (base_b + pcg_b) * substeps / (sum(stage_ms.values()) / 1e3) / 1e9
 
     cpu = cpu_baseline(args) if not args.no_cpu_baseline else None
+    batched = served = None
+    if not args.no_batched and world == 1:
+        sim.close()   # free the plain scene's memory first
+        batched, served = run_batched_and_served(args, value)
     line = {
         "metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(ms_max / args.steps, 4), "higher_is_better": True,
@@ -239,10 +243,89 @@ def run_gpu(args, rank, world):
                      "step_achieved_gbs": round(step_achieved, 1),
                      "stage_ms_per_step": {k: round(v / args.steps, 3) for k, v in stage_ms.items()}},
         "cpu_baseline": cpu,
+        "batched": batched,
+        "served": served,
         "gpu_launches": int(launches),
         "clocks": clocks.summary(),
     }
     return line
+
+
+def mixed_scenes(count, seed=1):
+    """The mixed-size scene set: cubic grids with edges drawn from
+    {32, 48, 64, 80, 96} (dx = 1/edge), each a dam break whose x extent
+    (the fill fraction) is drawn from [0.2, 0.6], y <= 0.6, full z, 8 jittered
+    particles per cell, FLIP blend 0.95."""
+    from flipengine3d_gb300.scenes import dam_break
+    rng = np.random.default_rng(seed)
+    edges = rng.choice([32, 48, 64, 80, 96], size=count)
+    fills = rng.uniform(0.2, 0.6, size=count)
+    return [dam_break(int(e), seed=seed * 1000 + q, fill=(float(f), 0.6, 1.0)) for q, (e, f) in enumerate(zip(edges, fills))]
+
+
+def run_batched_and_served(args, plain_value):
+    """Many resident scenes on one GPU through the C++ runtime (one CUDA
+    stream per scene, args.workers host threads).  Batched: every scene one
+    step per round (update_all), wall-clock timed over args.batch_steps
+    rounds.  Served: Poisson arrivals of one-step requests for random resident
+    scenes, latency from submission to completion."""
+    import torch
+
+    import flipengine3d_gb300 as fg
+    scs = mixed_scenes(args.batch_scenes)
+    rt = fg.FluidRuntime(workers=args.workers, reserve_bytes=2 << 30)
+    sims, rejected = [], 0
+    for sc in scs:   # admission by free HBM
+        need = fg.estimate_device_bytes(sc.isize, sc.jsize, sc.ksize, sc.num_particles)
+        if not rt.admit(need):
+            rejected += 1
+            continue
+        sims.append((sc, fg.FluidSimulation.from_scene(sc)))
+    handles = [s for _, s in sims]
+    dt = FRAME_DT
+    for _ in range(max(args.warmup, 1)):
+        rt.update_all(handles, dt)
+    torch.cuda.synchronize()
+    parts = 0
+    t0 = time.perf_counter()
+    for _ in range(args.batch_steps):
+        parts += sum(s.getNumMarkerParticles() for s in handles)
+        rt.update_all(handles, dt)
+    torch.cuda.synchronize()
+    tb = time.perf_counter() - t0
+    bval = parts / tb / 1e6
+    batched = {"value": round(bval, 3), "unit": UNIT, "scenes": len(handles), "rejected_at_admission": rejected,
+               "particles": int(parts / args.batch_steps), "steps": args.batch_steps,
+               "ms_per_step": round(tb / args.batch_steps * 1e3, 2), "workers": args.workers,
+               "vs_plain": round(bval / plain_value, 3) if plain_value else None,
+               "timing": "wall clock around update_all (all scenes one frame), device synchronised",
+               "config": "mixed sizes: edges from {32,48,64,80,96} (seed 1), dam x-fill U[0.2,0.6], y<=0.6, "
+                         "8 particles per cell, FLIP blend 0.95, PCG tol 1e-6, dt=1/120; one stream per scene"}
+    # served: Poisson arrivals
+    rng = np.random.default_rng(7)
+    gaps = rng.exponential(1.0 / args.arrival_rate, size=args.requests)
+    picks = rng.integers(0, len(handles), size=args.requests)
+    sizes = [s.getNumMarkerParticles() for s in handles]
+    ids = []
+    t0 = time.perf_counter()
+    due = t0
+    for g, q in zip(gaps, picks):
+        due += g
+        while time.perf_counter() < due:
+            pass
+        ids.append(rt.submit(handles[q], dt))
+    lat = np.array([rt.wait(i)[0] for i in ids])
+    ts = time.perf_counter() - t0
+    served = {"p50_ms": round(float(np.percentile(lat, 50)), 2), "p99_ms": round(float(np.percentile(lat, 99)), 2),
+              "requests": args.requests, "arrival_rate_hz": args.arrival_rate,
+              "value": round(float(sum(sizes[q] for q in picks)) / ts / 1e6, 3), "unit": UNIT,
+              "resident_scenes": len(handles), "workers": args.workers,
+              "note": "latency = submission to completion (queueing included); one-step requests on the "
+                      "batched scene set"}
+    rt.close()
+    for s in handles:
+        s.close()
+    return batched, served
 
 
 def cpu_sample_sim(args, threads):
@@ -306,6 +389,12 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--reference-max-steps", type=int, default=3)
+    ap.add_argument("--no-batched", action="store_true", help="skip the batched and served measurements")
+    ap.add_argument("--batch-scenes", type=int, default=64)
+    ap.add_argument("--batch-steps", type=int, default=5)
+    ap.add_argument("--workers", type=int, default=16)
+    ap.add_argument("--requests", type=int, default=800)
+    ap.add_argument("--arrival-rate", type=float, default=2000.0)
     ap.add_argument("--scene", default="plain_128", choices=sorted(SCENES),
                     help="plain_128 is the benchmark workload; plain_64 is the small case for profiling")
     args = ap.parse_args()

@@ -185,6 +185,7 @@ void launch_sweeps(const StepConsts &c, const float4 *L, const float *rf, float 
                    cudaStream_t s);
 
 int pressure_partials(const StepConsts &c);
+int pressure_partials_for(int I, int J, int K);
 // PressureSolver::solve (pressuresolver.cpp:44-76) on the device.  Returns
 // FLIP_OK (velocities updated, or nothing to solve), FLIP_E_SOLVER_NOCONV
 // (left unchanged), FLIP_E_DEVICE_TIMEOUT or FLIP_E_CUDA.

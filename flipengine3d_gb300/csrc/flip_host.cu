@@ -14,8 +14,11 @@
 #include "solid_setup.h"
 
 namespace flip {
+// Kernel launches issued by the calling thread; each context adds the
+// launches of its own calls (LaunchTally), so contexts driven from
+// different threads keep separate counts.
 long long &launch_counter() {
-    static long long n = 0;
+    static thread_local long long n = 0;
     return n;
 }
 }  // namespace flip
@@ -109,7 +112,8 @@ struct flip_ctx {
     PressureMail *pmail = nullptr;
     std::vector<void *> allocations;
 
-    long long launchesAtCreate = 0;
+    long long launches = 0;      // kernel launches of this context's calls
+    long long deviceBytes = 0;   // device memory allocated for this context
 
     // stage timing
     bool timing = false;
@@ -130,8 +134,21 @@ struct flip_ctx {
     template <class T>
     int alloc(T **p, size_t count) {
         int rc = dalloc(p, count);
-        if (rc == FLIP_OK) allocations.push_back((void *)*p);
+        if (rc == FLIP_OK) {
+            allocations.push_back((void *)*p);
+            deviceBytes += (long long)(count * sizeof(T));
+        }
         return rc;
+    }
+};
+
+// adds the launches made during one call to the context's count
+struct LaunchTally {
+    flip_ctx *x;
+    long long start;
+    explicit LaunchTally(flip_ctx *c) : x(c), start(flip::launch_counter()) {}
+    ~LaunchTally() {
+        if (x) x->launches += flip::launch_counter() - start;
     }
 };
 
@@ -644,7 +661,6 @@ int flip_create(int isize, int jsize, int ksize, double dx, flip_ctx **out) {
         flip_destroy(x);
         return rc;
     }
-    x->launchesAtCreate = launch_counter();
     *out = x;
     return FLIP_OK;
 }
@@ -720,6 +736,7 @@ int flip_set_max_pressure_iterations(flip_ctx *x, int n) {
 }
 int flip_load_marker_particle_data(flip_ctx *x, int n, const float *pos, const float *vel) {
     if (!x) return FLIP_E_NULL;
+    LaunchTally tally(x);
     if (n < 0) return fail(FLIP_E_DOMAIN, "negative particle count");
     if (n == 0) return FLIP_OK;
     if (!pos || !vel) return FLIP_E_NULL;
@@ -730,6 +747,7 @@ int flip_load_marker_particle_data(flip_ctx *x, int n, const float *pos, const f
 }
 int flip_load_marker_particle_data_device(flip_ctx *x, int n, const float *dpos, const float *dvel) {
     if (!x) return FLIP_E_NULL;
+    LaunchTally tally(x);
     if (n < 0) return fail(FLIP_E_DOMAIN, "negative particle count");
     if (n == 0) return FLIP_OK;
     if (!dpos || !dvel) return FLIP_E_NULL;
@@ -740,6 +758,7 @@ int flip_load_marker_particle_data_device(flip_ctx *x, int n, const float *dpos,
 }
 int flip_initialize(flip_ctx *x) {
     if (!x) return FLIP_E_NULL;
+    LaunchTally tally(x);
     return do_initialize(x);
 }
 int flip_is_initialized(flip_ctx *x, int *yes) {
@@ -749,10 +768,12 @@ int flip_is_initialized(flip_ctx *x, int *yes) {
 }
 int flip_update(flip_ctx *x, double dt) {
     if (!x) return FLIP_E_NULL;
+    LaunchTally tally(x);
     return do_update(x, dt, nullptr);
 }
 int flip_update_staged(flip_ctx *x, double dt, flip_stage_dump *d) {
     if (!x || !d) return FLIP_E_NULL;
+    LaunchTally tally(x);
     return do_update(x, dt, d);
 }
 int flip_get_num_marker_particles(flip_ctx *x, int *n) {
@@ -762,10 +783,12 @@ int flip_get_num_marker_particles(flip_ctx *x, int *n) {
 }
 int flip_get_marker_particle_position_data(flip_ctx *x, float *out) {
     if (!x || !out) return FLIP_E_NULL;
+    LaunchTally tally(x);
     return particles_to_host(x, out, nullptr, 0, x->n);
 }
 int flip_get_marker_particle_velocity_data(flip_ctx *x, float *out) {
     if (!x || !out) return FLIP_E_NULL;
+    LaunchTally tally(x);
     return particles_to_host(x, nullptr, out, 0, x->n);
 }
 static int range_get(flip_ctx *x, int start, int end, float *out, bool vel) {
@@ -774,9 +797,11 @@ static int range_get(flip_ctx *x, int start, int end, float *out, bool vel) {
     return vel ? particles_to_host(x, nullptr, out, start, end) : particles_to_host(x, out, nullptr, start, end);
 }
 int flip_get_marker_particle_position_data_range(flip_ctx *x, int start, int end, float *out) {
+    LaunchTally tally(x);
     return range_get(x, start, end, out, false);
 }
 int flip_get_marker_particle_velocity_data_range(flip_ctx *x, int start, int end, float *out) {
+    LaunchTally tally(x);
     return range_get(x, start, end, out, true);
 }
 int flip_get_marker_particle_data_device(flip_ctx *x, float *dpos, float *dvel) {
@@ -882,9 +907,36 @@ int flip_get_stage_times(flip_ctx *x, double *ms, long long *substeps) {
     return FLIP_OK;
 }
 
+int flip_get_device_bytes(flip_ctx *x, long long *bytes) {
+    if (!x || !bytes) return FLIP_E_NULL;
+    *bytes = x->deviceBytes;
+    return FLIP_OK;
+}
+
+// The allocations of alloc_grids and alloc_particles, summed without a device.
+int flip_estimate_device_bytes(int isize, int jsize, int ksize, int particles, long long *bytes) {
+    if (!bytes) return FLIP_E_NULL;
+    if (isize <= 0 || jsize <= 0 || ksize <= 0 || particles < 0)
+        return fail(FLIP_E_DOMAIN, "bad grid or particle count");
+    const long long I = isize, J = jsize, K = ksize, nc = I * J * K;
+    const long long faces = (I + 1) * J * K + I * (J + 1) * K + I * J * (K + 1);
+    const long long nsl = sweep_layout_size(isize, jsize, ksize);
+    const long long cap = std::max(particles, 1);
+    long long b = 0;
+    b += 5 * (nc + 1) * 4 + (scan_scratch_ints((int)nc) + 4) * 4 + 16;   // binning
+    b += nc * 4 + (I + 1) * (J + 1) * (K + 1) * 4 + nc;                  // phi, solid phi, solid cells
+    b += faces * (4 * 3 + 1 + 1);                                        // weights, velocity, saved, valid, status
+    b += nc * (1 + 32 + 8 * 5 + 4 + 4) + nsl * (16 + 4 + 4);              // pressure system
+    b += (pressure_partials_for(isize, jsize, ksize) + 32) * 8 + 64 + 16 + 32;
+    b += sweep_exchange_words(isize, jsize, ksize) * 8 + 4096;           // sweep exchange, ranges, tables
+    b += cap * (7 * 4 * 2 + 4 * 4) + (scan_scratch_ints((int)cap) + 4) * 4 + 64;   // particles
+    *bytes = b;
+    return FLIP_OK;
+}
+
 int flip_get_launch_count(flip_ctx *x, long long *count) {
     if (!x || !count) return FLIP_E_NULL;
-    *count = launch_counter() - x->launchesAtCreate;
+    *count = x->launches;
     return FLIP_OK;
 }
 

@@ -470,7 +470,10 @@ int cuda_fail(cudaError_t e, std::string *msg) {
 
 }  // namespace
 
-int pressure_partials(const StepConsts &c) { return std::min((int)div_up((long long)c.I * c.J * c.K, TPB), RBLOCKS); }
+int pressure_partials(const StepConsts &c) { return pressure_partials_for(c.I, c.J, c.K); }
+int pressure_partials_for(int I, int J, int K) {
+    return std::min((int)div_up((long long)I * J * K, TPB), RBLOCKS);
+}
 
 #define PCK(call)                                     \
     do {                                              \

@@ -40,6 +40,8 @@
 // tiles that are already running.  Every wait is bounded: on timeout the
 // tile raises the error flag and stops, and the host reports
 // FLIP_E_DEVICE_TIMEOUT; no wait can spin forever.
+#include <atomic>
+
 #include "flip_device.cuh"
 
 namespace flip {
@@ -417,13 +419,13 @@ void launch_sweeps(const StepConsts &c, const float4 *L, const float *rf, float 
                    cudaStream_t s) {
     const SweepLayout g = sweep_layout(c.I, c.J, c.K);
     const int n = g.ntj * g.ntk;
-    static unsigned long long smemSet = 0;   // devices on which the slots' shared memory is opted in
+    static std::atomic<unsigned long long> smemSet{0};   // devices on which the slots' shared memory is opted in
     int dev = 0;
     cudaGetDevice(&dev);
-    if (dev < 64 && !((smemSet >> dev) & 1ull)) {
+    if (dev < 64 && !((smemSet.load() >> dev) & 1ull)) {   // idempotent, so a race only repeats it
         cudaFuncSetAttribute(k_wavefront<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SweepSmem));
         cudaFuncSetAttribute(k_wavefront<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SweepSmem));
-        smemSet |= 1ull << dev;
+        smemSet.fetch_or(1ull << dev);
     }
     if (sw.epoch >= 0xfffffff0u) {   // epochs are about to wrap: forget every old word
         cudaMemsetAsync(sw.xchg, 0, sweep_exchange_words(c.I, c.J, c.K) * sizeof(unsigned long long), s);

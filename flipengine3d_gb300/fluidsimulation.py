@@ -88,6 +88,15 @@ SIGNATURES = {
     "flip_get_launch_count": [_P, C.POINTER(C.c_longlong)],
     "flip_get_sweep_times": [_P, C.POINTER(C.c_double), C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)],
     "flip_order_particles_by_id_noalloc": [_P, _P, _P, _P, _I, _I, _P, _P],
+    "flip_get_device_bytes": [_P, C.POINTER(C.c_longlong)],
+    "flip_estimate_device_bytes": [_I, _I, _I, _I, C.POINTER(C.c_longlong)],
+    "flip_runtime_create": [_I, C.c_longlong, C.POINTER(C.c_void_p)],
+    "flip_runtime_destroy": [_P],
+    "flip_runtime_submit": [_P, _P, _D, _I, C.POINTER(C.c_longlong)],
+    "flip_runtime_wait": [_P, C.c_longlong, C.POINTER(C.c_double), C.POINTER(C.c_int)],
+    "flip_runtime_update_all": [_P, C.POINTER(C.c_void_p), _I, _D],
+    "flip_runtime_admit": [_P, C.c_longlong, C.POINTER(C.c_int)],
+    "flip_runtime_pending": [_P, C.POINTER(C.c_int), C.POINTER(C.c_int)],
 }
 
 
@@ -161,6 +170,73 @@ def order_particles_by_id_noalloc(d_px: int, d_py: int, d_pz: int, d_ids: int, n
 
 
 FLIP_NOALLOC_MAX_IDS = 1 << 20
+
+
+def estimate_device_bytes(isize: int, jsize: int, ksize: int, particles: int) -> int:
+    """Device memory a scene of this size needs (no device used)."""
+    lib = load_library()
+    b = C.c_longlong()
+    _check(lib, lib.flip_estimate_device_bytes(int(isize), int(jsize), int(ksize), int(particles), C.byref(b)))
+    return b.value
+
+
+class FluidRuntime:
+    """Many scenes on one GPU (C++ runtime behind the C ABI): `workers` host
+    threads step FluidSimulation contexts concurrently, each on its own CUDA
+    stream.  submit()/wait() serve step requests as they arrive (continuous
+    batching; requests of one scene keep their order); update_all() steps a
+    set of scenes once each.  A scene must not be used directly while it has
+    requests in flight."""
+
+    def __init__(self, workers: int = 8, reserve_bytes: int = 0):
+        self._lib = load_library()
+        self._h = C.c_void_p()
+        _check(self._lib, self._lib.flip_runtime_create(int(workers), int(reserve_bytes), C.byref(self._h)))
+
+    def close(self):
+        if self._h:
+            self._lib.flip_runtime_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def submit(self, sim: "FluidSimulation", dt: float, steps: int = 1) -> int:
+        rid = C.c_longlong()
+        _check(self._lib, self._lib.flip_runtime_submit(self._h, sim._h, float(dt), int(steps), C.byref(rid)))
+        return rid.value
+
+    def wait(self, request_id: int):
+        """(latency in ms from submission, status code of the request's updates)"""
+        ms = C.c_double()
+        st = C.c_int()
+        _check(self._lib, self._lib.flip_runtime_wait(self._h, int(request_id), C.byref(ms), C.byref(st)))
+        return ms.value, st.value
+
+    def update_all(self, sims, dt: float) -> None:
+        arr = (C.c_void_p * len(sims))(*[s._h.value for s in sims])
+        rc = self._lib.flip_runtime_update_all(self._h, arr, len(sims), float(dt))
+        if rc != FLIP_E_SOLVER_NOCONV:
+            _check(self._lib, rc)
+
+    def admit(self, nbytes: int) -> bool:
+        ok = C.c_int()
+        _check(self._lib, self._lib.flip_runtime_admit(self._h, int(nbytes), C.byref(ok)))
+        return bool(ok.value)
+
+    def pending(self):
+        q, r = C.c_int(), C.c_int()
+        _check(self._lib, self._lib.flip_runtime_pending(self._h, C.byref(q), C.byref(r)))
+        return q.value, r.value
 
 
 class FluidSimulation:
@@ -327,6 +403,11 @@ class FluidSimulation:
         cells = C.c_longlong()
         self._c(self._lib.flip_get_sweep_times(self._h, C.byref(ms), C.byref(n), C.byref(cells)))
         return ms.value, n.value, cells.value
+
+    def device_bytes(self) -> int:
+        b = C.c_longlong()
+        self._c(self._lib.flip_get_device_bytes(self._h, C.byref(b)))
+        return b.value
 
     def launch_count(self) -> int:
         v = C.c_longlong()

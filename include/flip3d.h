@@ -180,6 +180,36 @@ int flip_get_sweep_times(flip_ctx *ctx, double *ms, long long *launches, long lo
 /* Number of this library's kernel launches issued so far on the context. */
 int flip_get_launch_count(flip_ctx *ctx, long long *count);
 
+/* Device memory of a context (flip_get_device_bytes), and the same figure
+ * for a scene not yet created (flip_estimate_device_bytes: grids, pressure
+ * system, particle storage for `particles`), for admission decisions.  No
+ * counterpart in the reference, which runs on the host. */
+int flip_get_device_bytes(flip_ctx *ctx, long long *bytes);
+int flip_estimate_device_bytes(int isize, int jsize, int ksize, int particles, long long *bytes);
+
+/* Many scenes on one GPU: a runtime with `workers` host threads steps
+ * contexts concurrently, each on its own stream.  No counterpart in the
+ * reference (FluidManager drives one FluidSimulation).
+ *   flip_runtime_submit: enqueue `steps` calls of update(dt) on a scene;
+ *     requests of one scene run in submission order, requests of different
+ *     scenes overlap on the GPU.  A scene must not be used by the caller
+ *     while it has requests in flight.
+ *   flip_runtime_wait: block until a request is done; its latency (from
+ *     submission, queueing included) in ms and its status (that of update).
+ *   flip_runtime_update_all: one update(dt) of every listed scene, together;
+ *     returns the first error.
+ *   flip_runtime_admit: 1 if `bytes` fit in the device's free memory less
+ *     the reserve given at creation.
+ *   flip_runtime_destroy finishes the submitted requests first. */
+typedef struct flip_runtime flip_runtime;
+int flip_runtime_create(int workers, long long reserve_bytes, flip_runtime **out);
+int flip_runtime_destroy(flip_runtime *rt);
+int flip_runtime_submit(flip_runtime *rt, flip_ctx *scene, double dt, int steps, long long *request_id);
+int flip_runtime_wait(flip_runtime *rt, long long request_id, double *latency_ms, int *status);
+int flip_runtime_update_all(flip_runtime *rt, flip_ctx **scenes, int n, double dt);
+int flip_runtime_admit(flip_runtime *rt, long long bytes, int *admitted);
+int flip_runtime_pending(flip_runtime *rt, int *queued, int *running);
+
 /* Particle positions in ascending id order, written into caller memory,
  * with no allocation by the library.  No counterpart in the reference: it
  * is the context readback's ordering (flip_get_marker_particle_position_data)

@@ -74,3 +74,18 @@ def test_domain_solid_setup_matches_oracle(built, dims):
     for a, b in zip(weights, orc.weights()):
         assert np.array_equal(a, b)
     assert np.array_equal(near, orc.near_solid())
+
+
+def test_runtime_and_estimate_checks_need_no_device(built):
+    lib = fs.load_library()
+    h = C.c_void_p()
+    assert lib.flip_runtime_create(0, 0, C.byref(h)) == fs.FLIP_E_DOMAIN
+    assert lib.flip_runtime_create(4, -1, C.byref(h)) == fs.FLIP_E_DOMAIN
+    assert lib.flip_runtime_submit(None, None, 0.01, 1, None) == fs.FLIP_E_NULL
+    b = C.c_longlong()
+    assert lib.flip_estimate_device_bytes(0, 8, 8, 10, C.byref(b)) == fs.FLIP_E_DOMAIN
+    small = fs.estimate_device_bytes(32, 32, 32, 100_000)
+    big = fs.estimate_device_bytes(128, 128, 128, 4_000_000)
+    assert 0 < small < big
+    # 128^3 with 4M particles: grids + system + particles, between 0.5 and 2 GB
+    assert 5e8 < big < 2e9
