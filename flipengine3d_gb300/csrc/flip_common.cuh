@@ -61,6 +61,16 @@ constexpr unsigned int KEY_FAST = 0x40000000u;     // over the extreme-speed lim
 constexpr unsigned int KEY_NONE = 0xffffffffu;     // no particle
 
 inline unsigned int div_up(long long a, int b) { return (unsigned int)((a + b - 1) / b); }
+// Grid coordinates of a flat index i + ni*(j + nj*k).  Grids hold fewer than
+// 2^31 entries (flip_create caps them), so 32-bit division suffices; 64-bit
+// division has no hardware instruction.
+__host__ __device__ __forceinline__ void unflatten(long long t, int ni, int nj, int &i, int &j, int &k) {
+    const unsigned u = (unsigned)t, a = (unsigned)ni, b = (unsigned)nj;
+    const unsigned q = u / a;
+    i = (int)(u - q * a);
+    j = (int)(q % b);
+    k = (int)(q / b);
+}
 
 // Count of kernel launches issued by this library (all contexts); each
 // launcher adds the number of kernels it enqueues.

@@ -304,7 +304,8 @@ __global__ void __launch_bounds__(TPB) k_p2g(ParticleSoA p, const int *cellStart
     const int ni = c.I + (dir == 0), nj = c.J + (dir == 1), nk = c.K + (dir == 2);
     long long f = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (f >= (long long)ni * nj * nk) return;
-    int fi = (int)(f % ni), fj = (int)((f / ni) % nj), fk = (int)(f / ((long long)ni * nj));
+    int fi, fj, fk;
+    unflatten(f, ni, nj, fi, fj, fk);
     const double dx = c.dx;
     const float r = (float)c.radius;
     const float rsq = __fmul_rn(r, r);
@@ -381,7 +382,8 @@ __global__ void k_extrap_init(StepConsts c, const uint8_t *vu, const uint8_t *vv
     long long l = dir == 0 ? f : (dir == 1 ? f - nu : f - nu - nv);
     const uint8_t *valid = dir == 0 ? vu : (dir == 1 ? vv : vw);
     int ni = c.I + (dir == 0), nj = c.J + (dir == 1), nk = c.K + (dir == 2);
-    int i = (int)(l % ni), j = (int)((l / ni) % nj), k = (int)(l / ((long long)ni * nj));
+    int i, j, k;
+    unflatten(l, ni, nj, i, j, k);
     uint8_t s;
     if (i == 0 || j == 0 || k == 0 || i == ni - 1 || j == nj - 1 || k == nk - 1) s = ST_BORDER;
     else s = valid[l] ? 0 : ST_UNKNOWN;

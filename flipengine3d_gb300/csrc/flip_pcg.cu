@@ -27,7 +27,7 @@ namespace flip {
 namespace {
 
 constexpr int TPB = 256;
-constexpr int RBLOCKS = 152 * 4;   // grid of the reduction kernels: 4 CTAs per SM
+constexpr int RBLOCKS = 152 * 8;   // grid of the reduction kernels: 8 CTAs of 256 threads per SM (full occupancy)
 
 __device__ __forceinline__ bool sys_cell(const StepConsts &c, const float *phi, int i, int j, int k) {
     if (i < 1 || j < 1 || k < 1 || i > c.I - 2 || j > c.J - 2 || k > c.K - 2) return false;
@@ -40,7 +40,8 @@ __global__ void k_flags(StepConsts c, const float *phi, uint8_t *fluid, int *lev
     bool f = false;
     int lv = 0;
     if (t < d.size()) {
-        int i = (int)(t % c.I), j = (int)((t / c.I) % c.J), k = (int)(t / ((long long)c.I * c.J));
+        int i, j, k;
+        unflatten(t, c.I, c.J, i, j, k);
         f = sys_cell(c, phi, i, j, k);
         fluid[t] = f ? 1 : 0;
         lv = i + j + k;
@@ -128,7 +129,8 @@ __global__ void k_build(StepConsts c, const float *phi, const float *wu, const f
             pb.Ad[t] = make_double4(0.0, 0.0, 0.0, 0.0);
             pb.b[t] = 0.0;
         } else {
-            int i = (int)(t % c.I), j = (int)((t / c.I) % c.J), k = (int)(t / ((long long)c.I * c.J));
+            int i, j, k;
+        unflatten(t, c.I, c.J, i, j, k);
             Dims du{c.I + 1, c.J, c.K}, dv{c.I, c.J + 1, c.K}, dw{c.I, c.J, c.K + 1};
             double vR = wu[du.idx(i + 1, j, k)], vL = wu[du.idx(i, j, k)];
             double vT = wv[dv.idx(i, j + 1, k)], vB = wv[dv.idx(i, j, k)];
@@ -195,7 +197,8 @@ __global__ void k_mic0_finalize(StepConsts c, SweepLayout g, const uint8_t *flui
                                 const double *invD, float4 *L) {
     long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= (long long)c.I * c.J * c.K) return;
-    const int i = (int)(t % c.I), j = (int)((t / c.I) % c.J), k = (int)(t / ((long long)c.I * c.J));
+    int i, j, k;
+    unflatten(t, c.I, c.J, i, j, k);
     if (i < 1 || j < 1 || k < 1 || i > c.I - 2 || j > c.J - 2 || k > c.K - 2) return;
     const double inv = invD[t];
     float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -207,7 +210,8 @@ __global__ void k_mic0_finalize(StepConsts c, SweepLayout g, const uint8_t *flui
 }
 
 __device__ __forceinline__ long long sweep_index_of(const StepConsts &c, const SweepLayout &g, long long t) {
-    const int i = (int)(t % c.I), j = (int)((t / c.I) % c.J), k = (int)(t / ((long long)c.I * c.J));
+    int i, j, k;
+    unflatten(t, c.I, c.J, i, j, k);
     return sweep_index(g, i, j, k);
 }
 
@@ -232,13 +236,14 @@ __device__ __forceinline__ T block_sum(T v, T *sh) {
 // cell.
 
 // q = A s (FP64), block partials of s.q
-__global__ void k_spmv(StepConsts c, const uint8_t *fluid, const double4 *Ad, const float *s, double *q,
-                       double *partials, const PcgCtl *ctl) {
+__global__ void k_spmv(StepConsts c, const uint8_t *__restrict__ fluid, const double4 *__restrict__ Ad,
+                       const float *__restrict__ s, double *__restrict__ q, double *partials, const PcgCtl *ctl) {
     __shared__ double sh[32];
     if (ctl->done) return;
     const long long n = (long long)c.I * c.J * c.K;
     const long long sy = c.I, sz = (long long)c.I * c.J;
     double part = 0.0;
+#pragma unroll 4
     for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
         if (!fluid[t]) continue;
         double4 a = Ad[t];
@@ -256,12 +261,13 @@ __global__ void k_spmv(StepConsts c, const uint8_t *fluid, const double4 *Ad, co
     if (threadIdx.x == 0) partials[blockIdx.x] = b;
 }
 
-__global__ void k_dot_zr(StepConsts c, SweepLayout g, const uint8_t *fluid, const float *z, const double *r,
-                         double *partials, const PcgCtl *ctl) {
+__global__ void k_dot_zr(StepConsts c, SweepLayout g, const uint8_t *__restrict__ fluid, const float *__restrict__ z,
+                         const double *__restrict__ r, double *partials, const PcgCtl *ctl) {
     __shared__ double sh[32];
     if (ctl->done) return;
     const long long n = (long long)c.I * c.J * c.K;
     double part = 0.0;
+#pragma unroll 4
     for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x)
         if (fluid[t]) part = fma((double)z[sweep_index_of(c, g, t)], r[t], part);
     double s = block_sum(part, sh);
@@ -294,13 +300,15 @@ __global__ void k_sum_partials(const double *partials, int n, double *scal, int 
 
 // x += alpha s, r -= alpha q with alpha = rho / s.q passed on as float, as
 // BLAS::addScaled(float alpha, ...) does (blaswrapper.h:129-158); |r|inf
-__global__ void k_update_xr(StepConsts c, SweepLayout g, const uint8_t *fluid, double *x, double *r, float *rf,
-                            const float *s, const double *q, const double *scal, unsigned long long *rmaxBits,
+__global__ void k_update_xr(StepConsts c, SweepLayout g, const uint8_t *__restrict__ fluid, double *__restrict__ x,
+                            double *__restrict__ r, float *__restrict__ rf, const float *__restrict__ s,
+                            const double *__restrict__ q, const double *scal, unsigned long long *rmaxBits,
                             const PcgCtl *ctl) {
     if (ctl->done) return;
     const long long n = (long long)c.I * c.J * c.K;
     const double alpha = scal[4];
     double m = 0.0;
+#pragma unroll 4
     for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
         if (!fluid[t]) continue;
         x[t] = fma(alpha, (double)s[t], x[t]);
@@ -323,6 +331,7 @@ __global__ void k_true_residual(StepConsts c, SweepLayout g, const uint8_t *flui
     const long long n = (long long)c.I * c.J * c.K;
     const long long sy = c.I, sz = (long long)c.I * c.J;
     double m = 0.0;
+#pragma unroll 4
     for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
         if (!fluid[t]) continue;
         double4 a = Ad[t];
@@ -346,9 +355,11 @@ __global__ void k_init_r(StepConsts c, SweepLayout g, const double *b, double *r
                          unsigned long long *rmaxBits) {
     const long long n = (long long)c.I * c.J * c.K;
     double m = 0.0;
+#pragma unroll 4
     for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
         r[t] = b[t];
-        const int i = (int)(t % c.I), j = (int)((t / c.I) % c.J), k = (int)(t / ((long long)c.I * c.J));
+        int i, j, k;
+    unflatten(t, c.I, c.J, i, j, k);
         if (i >= 1 && j >= 1 && k >= 1 && i <= c.I - 2 && j <= c.J - 2 && k <= c.K - 2)
             rf[sweep_index(g, i, j, k)] = (float)b[t];
         double av = fabs(b[t]);
@@ -424,7 +435,8 @@ __global__ void k_apply_pressure(StepConsts c, const float *phi, const float *wu
     int dir = f < nu ? 0 : (f < nu + nv ? 1 : 2);
     long long l = dir == 0 ? f : (dir == 1 ? f - nu : f - nu - nv);
     int ni = c.I + (dir == 0), nj = c.J + (dir == 1);
-    int i = (int)(l % ni), j = (int)((l / ni) % nj), k = (int)(l / ((long long)ni * nj));
+    int i, j, k;
+    unflatten(l, ni, nj, i, j, k);
     float *G = dir == 0 ? u : (dir == 1 ? v : w);
     uint8_t *V = dir == 0 ? vu : (dir == 1 ? vv : vw);
     const float *W = dir == 0 ? wu : (dir == 1 ? wv : ww);

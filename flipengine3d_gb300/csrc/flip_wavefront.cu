@@ -49,6 +49,9 @@ namespace flip {
 namespace {
 
 constexpr int TJ = SWEEP_TJ, TK = SWEEP_TK, NP = SWEEP_NP, CH = 8, NBUF = 4;
+// the helper warp's lanes take the CH x TK j-edge words two at a time and the
+// CH x TJ k-edge words one step each
+static_assert(CH * TK == 64 && TJ == 32, "edge-word mapping of the helper warp");
 constexpr int NCOMP = NP, NTHREADS = NCOMP + 32;
 constexpr unsigned int SPIN_LIMIT = 1u << 22;   // poll rounds of <= ~250 ns: about a second
 
@@ -379,7 +382,8 @@ __global__ void k_tile_range(const uint8_t *fluid, int I, int J, int K, int ntj,
     bool f = t < (long long)I * J * K && fluid[t];
     int tile = -1, step = 0;
     if (f) {
-        int i = (int)(t % I), j = (int)((t / I) % J), k = (int)(t / ((long long)I * J));
+        int i, j, k;
+        unflatten(t, I, J, i, j, k);
         tile = (j - 1) / TJ + ntj * ((k - 1) / TK);
         step = (i - 1) + (j - 1) % TJ + (k - 1) % TK;
     }
