@@ -34,6 +34,10 @@ import numpy as np
 
 ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
+# Hardware work queues for concurrent streams (read when the CUDA context is
+# created): the multi-scene runtime runs one stream per scene, and with the
+# default of 8 queues streams share queues and serialise.
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
 
 FRAME_DT = 1.0 / 120.0
 METRIC = "Mparticle-steps/s at 128^3 (plain FLIP step, dam break + sphere)"  # the plain_128 workload

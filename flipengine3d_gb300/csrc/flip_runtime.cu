@@ -162,11 +162,21 @@ int flip_runtime_wait(flip_runtime *rt, long long request_id, double *latency_ms
 int flip_runtime_update_all(flip_runtime *rt, flip_ctx **scenes, int n, double dt) {
     if (!rt || (n > 0 && !scenes)) return flip::record_error(FLIP_E_NULL, "null runtime or scene list");
     if (n < 0) return flip::record_error(FLIP_E_DOMAIN, "negative scene count");
-    std::vector<long long> ids(n);
+    // largest scenes first (longest-processing-time order), so that the big
+    // steps do not start last and stretch the round
+    std::vector<std::pair<long long, int>> order(n);
     for (int q = 0; q < n; q++) {
+        int np = 0;
+        flip_get_num_marker_particles(scenes[q], &np);
+        order[q] = {-(long long)np, q};
+    }
+    std::stable_sort(order.begin(), order.end());
+    std::vector<long long> ids(n);
+    for (int o = 0; o < n; o++) {
+        const int q = order[o].second;
         int rc = flip_runtime_submit(rt, scenes[q], dt, 1, &ids[q]);
         if (rc) {
-            for (int p = 0; p < q; p++) flip_runtime_wait(rt, ids[p], nullptr, nullptr);
+            for (int p = 0; p < o; p++) flip_runtime_wait(rt, ids[order[p].second], nullptr, nullptr);
             return rc;
         }
     }
