@@ -141,6 +141,18 @@ def algorithmic_bytes(n_particles, n_cells, n_fluid, iters):
     return 120.0 * n_particles + 256.0 * n_cells, 132.0 * n_fluid * iters
 
 
+def combine_ranks(ms, e2e_s, particles, e2e_particles, world, device):
+    """Whole-job figures of N replicas: the slowest rank's times (max) and the
+    particles of all ranks (sum).  One rank: the values themselves."""
+    import torch
+    t = torch.tensor([ms, e2e_s], dtype=torch.float64, device=device)
+    tot = torch.tensor([particles, e2e_particles], dtype=torch.float64, device=device)
+    if world > 1:
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        torch.distributed.all_reduce(tot, op=torch.distributed.ReduceOp.SUM)
+    return float(t[0]), float(t[1]), float(tot[0]), float(tot[1])
+
+
 def run_gpu(args, rank, world):
     import torch
 
@@ -197,16 +209,11 @@ def run_gpu(args, rank, world):
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t0
 
-    t = torch.tensor([ms, e2e_s], dtype=torch.float64, device="cuda")
-    tot = torch.tensor([particles, e2e_particles], dtype=torch.float64, device="cuda")
-    if world > 1:
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        torch.distributed.all_reduce(tot, op=torch.distributed.ReduceOp.SUM)
-    ms_max, e2e_max = float(t[0]), float(t[1])
+    ms_max, e2e_max, ptot, e2e_ptot = combine_ranks(ms, e2e_s, particles, e2e_particles, world, "cuda")
     if rank != 0:
         return None
-    value = float(tot[0]) / (ms_max / 1e3) / 1e6
-    e2e_value = float(tot[1]) / e2e_max / 1e6
+    value = ptot / (ms_max / 1e3) / 1e6
+    e2e_value = e2e_ptot / e2e_max / 1e6
 
     # roofline of the dominant kernel: the MIC(0) sweeps, event-timed per
     # launch on the simulation's stream inside the library
