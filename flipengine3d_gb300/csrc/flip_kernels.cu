@@ -247,11 +247,26 @@ __global__ void __launch_bounds__(TPB) k_liquid_sdf(ParticleSoA p, const int *ce
     int y0 = max(by * BW - 2, 0), y1 = min(by * BW + BW + 1, c.J - 1);
     int z0 = max(bz * BW - 2, 0), z1 = min(bz * BW + BW + 1, c.K - 1);
     int ny = y1 - y0 + 1, nrows = ny * (z1 - z0 + 1);
-    int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
-    for (int row = warp; row < nrows; row += nwarps) {
-        int cy = y0 + row % ny, cz = z0 + row / ny;
-        int pb = cellStart[cells.idx(x0, cy, cz)], pe = cellStart[cells.idx(x1, cy, cz) + 1];
-        for (int t = pb + lane; t < pe; t += 32) {
+    // A warp takes two rows of cells along x, 16 lanes each; a lane takes a
+    // contiguous run of its row's particles, so about one lane per cell.
+    // Lanes in step then sit in different cells (or rows), and their
+    // shared-memory atomics rarely meet on one cell, whereas the particles
+    // of one cell share their whole box.
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
+    const int sel = lane >> 4, hl = lane & 15;
+    for (int pair = warp; 2 * pair < nrows; pair += nwarps) {
+        const int row = 2 * pair + sel;
+        int pb = 0, pe = 0;
+        if (row < nrows) {
+            const int cy = y0 + row % ny, cz = z0 + row / ny;
+            pb = cellStart[cells.idx(x0, cy, cz)];
+            pe = cellStart[cells.idx(x1, cy, cz) + 1];
+        }
+        const int run = (pe - pb + 15) >> 4;   // particles per lane in this row
+        const int rounds = max(run, __shfl_xor_sync(0xffffffffu, run, 16));
+        for (int r = 0; r < rounds; r++) {
+            const int t = pb + hl * run + r;
+            if (r >= run || t >= pe) continue;
             float px = p.px[t], py = p.py[t], pz = p.pz[t];
             if (!in_block_list(px, py, pz, sr, blockdxf, invBlock, invBlockf, c.blockPosF, bx, by, bz)) continue;
             float lx = __fsub_rn(px, offx), ly = __fsub_rn(py, offy), lz = __fsub_rn(pz, offz);
