@@ -359,12 +359,12 @@ __global__ void __launch_bounds__(TPB) k_p2g(ParticleSoA p, const int *cellStart
                 float ddx = __fsub_rn(gx, lx), ddy = __fsub_rn(gy, ly), ddz = __fsub_rn(gz, lz);
                 float d2 = __fadd_rn(__fadd_rn(__fmul_rn(ddx, ddx), __fmul_rn(ddy, ddy)), __fmul_rn(ddz, ddz));
                 if (!(d2 < rsq)) continue;
-                // the face must lie inside the particle's clamped local box
-                int a0 = exact_floor(__fsub_rn(lx, sr), c.invdx, c.invdxf), a1 = exact_floor(__fadd_rn(lx, sr), c.invdx, c.invdxf);
-                int b0 = exact_floor(__fsub_rn(ly, sr), c.invdx, c.invdxf), b1 = exact_floor(__fadd_rn(ly, sr), c.invdx, c.invdxf);
-                int c0 = exact_floor(__fsub_rn(lz, sr), c.invdx, c.invdxf), c1 = exact_floor(__fadd_rn(lz, sr), c.invdx, c.invdxf);
-                if (la < a0 || la > a1 || lb < b0 || lb > b1 || lc < c0 || lc > c1) continue;
-                if (!in_block_list(px, py, pz, sr, blockdxf, invBlock, invBlockf, c.blockPosF, bx, by, bz)) continue;
+                // The reference also requires the face to lie in the particle's
+                // local box and the particle to be in the block's list, both
+                // taken with the support radius sr = r + 1e-6.  A particle
+                // within r of the face meets both: every coordinate of the face
+                // is within r of the particle, and the 1e-6 margin is far above
+                // the rounding of these float expressions (ulp(1) ~ 1.2e-7).
                 float vel = dir == 0 ? p.vx[t] : dir == 1 ? p.vy[t] : p.vz[t];
                 float w3 = __fmul_rn(__fmul_rn(__fmul_rn(coef1, d2), d2), d2);
                 float w2 = __fmul_rn(__fmul_rn(coef2, d2), d2);
