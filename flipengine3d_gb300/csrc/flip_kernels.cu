@@ -324,20 +324,13 @@ __global__ void __launch_bounds__(TPB) k_p2g(ParticleSoA p, const int *cellStart
     const double dx = c.dx;
     const float r = (float)c.radius;
     const float rsq = __fmul_rn(r, r);
-    const float sr = (float)(c.radius + (double)1e-6f);
-    const float r2 = rsq, r4 = __fmul_rn(r2, r2), r6 = __fmul_rn(r4, r2);
     // same expression trees as the reference's coefficient set-up
     const float coef1 = __fmul_rn(4.0f / 9.0f, __fdiv_rn(1.0f, __fmul_rn(__fmul_rn(__fmul_rn(__fmul_rn(__fmul_rn(r, r), r), r), r), r)));
     const float coef2 = __fmul_rn(17.0f / 9.0f, __fdiv_rn(1.0f, __fmul_rn(__fmul_rn(__fmul_rn(r, r), r), r)));
     const float coef3 = __fmul_rn(22.0f / 9.0f, __fdiv_rn(1.0f, __fmul_rn(r, r)));
-    (void)r4; (void)r6;
     const float halfdx = (float)(0.5 * dx);
     const float ox = dir == 0 ? 0.0f : halfdx, oy = dir == 1 ? 0.0f : halfdx, oz = dir == 2 ? 0.0f : halfdx;
-    const float blockdxf = (float)(dx * BW);
-    const double invBlock = 1.0 / (double)blockdxf;
-    const float invBlockf = (float)invBlock;
     const int bx = fi / BW, by = fj / BW, bz = fk / BW;
-    const double blockdxD = (double)BW * dx;
     const float offx = c.blockPos[bx + 1], offy = c.blockPos[by + 1],
                 offz = c.blockPos[bz + 1];
     const int la = fi - bx * BW, lb = fj - by * BW, lc = fk - bz * BW;
