@@ -112,7 +112,7 @@ struct PcgCtl {
     int done;      // converged
     int iters;     // iterations to convergence
     int claim;     // the recurrence residual passed the test; b - A x must confirm
-    int pad;
+    int it;        // index of the iteration being run
     double resid;  // last residual norm tested
 };
 constexpr int PCG_BATCH = 8;   // iterations enqueued between host checks
@@ -129,9 +129,14 @@ struct PressureBuffers {
     float *rf;             // r rounded to FP32, the forward sweep's right-hand side, sweep layout
     SweepLayout sl;
     double *partials;      // per-block partial sums (deterministic reduction)
-    double *scal;          // [0]=s.q [1]=z.r (new rho) [2]=|b|inf [3]=rho [4]=alpha [5]=beta
+    double *scal;          // [0]=s.q [1]=z.r (new rho) [2]=|b|inf [3]=rho [4]=alpha [5]=beta [6]=tol |b|inf
     unsigned long long *rmaxBits;  // [0] |r|inf of the recurrence, [1] of b - A x, as double bits
     PcgCtl *ctl;
+    // PCG_BATCH iterations captured as a CUDA graph, replayed per batch;
+    // [1] also records the sweep timing events
+    cudaGraphExec_t batchGraph[2] = {};
+    long long batchKernels[2] = {};
+    bool noGraphs = false;   // the stream cannot be captured: launch eagerly
     int *levelRange;       // [0]=min(i+j+k) [1]=max(i+j+k) [2]=system size
     float *pressure;       // float copy of x for the velocity update
     int nPartials;
@@ -155,7 +160,7 @@ struct SweepTiming {
 };
 struct PressureMail {      // pinned host scalars
     int levelRange[3];
-    double bmax, rho;
+    double bmax, rho, ptol;
     PcgCtl ctl;
     int sweepErr;
 };
@@ -171,10 +176,9 @@ struct SweepState {
     int2 *range;             // per tile [first, last] step holding a system cell
     unsigned long long *xchg;  // tile edge exchange words {epoch, value}
     long long xchgWords;       // words allocated for xchg
-    unsigned int *ticket;    // tile ticket counter
+    unsigned int *ticket;    // [0] tile tickets of the running sweep, [1] its epoch
     int *err;                // set when a bounded wait gave up
-    unsigned int epoch;
-    long long launches;
+    unsigned int epoch;      // host count of the epochs issued (wrap guard)
 };
 int sweep_tiles(int J, int K, int *ntj, int *ntk);
 long long sweep_exchange_words(int I, int J, int K);
@@ -183,6 +187,7 @@ void launch_sweep_ranges(const StepConsts &c, const uint8_t *fluid, SweepState &
 // The launches return at once when *skip is set (a converged solve).
 void launch_sweeps(const StepConsts &c, const float4 *L, const float *rf, float *z, SweepState &sw, const int *skip,
                    cudaStream_t s);
+void sweep_epoch_guard(const StepConsts &c, SweepState &sw, long long upcoming, cudaStream_t s);
 
 int pressure_partials(const StepConsts &c);
 int pressure_partials_for(int I, int J, int K);

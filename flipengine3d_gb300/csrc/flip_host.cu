@@ -221,6 +221,7 @@ int alloc_grids(flip_ctx *x) {
             return rc;
         CK(cudaMemsetAsync(x->sweep.xchg, 0, nw * sizeof(unsigned long long), x->stream));
         CK(cudaMemsetAsync(x->sweep.err, 0, 4 * sizeof(int), x->stream));
+        CK(cudaMemsetAsync(x->sweep.ticket, 0, 4 * sizeof(unsigned int), x->stream));
     }
     {
         // position tables (see StepConsts)
@@ -668,6 +669,8 @@ int flip_create(int isize, int jsize, int ksize, double dx, flip_ctx **out) {
 int flip_destroy(flip_ctx *x) {
     if (!x) return FLIP_E_NULL;
     cudaStreamSynchronize(x->stream);
+    for (int q = 0; q < 2; q++)   // the graphs refer to the timing events: first
+        if (x->pr.batchGraph[q]) cudaGraphExecDestroy(x->pr.batchGraph[q]);
     for (int q = 0; q <= FLIP_NUM_STAGES; q++)
         if (x->ev[q]) cudaEventDestroy(x->ev[q]);
     for (int q = 0; q < 2 * (PCG_BATCH + 1); q++)

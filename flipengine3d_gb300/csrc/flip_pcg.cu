@@ -321,13 +321,15 @@ __global__ void k_update_xr(StepConsts c, SweepLayout g, const uint8_t *__restri
     block_max_to(m, rmaxBits);
 }
 
-// r = b - A x (residual replacement); |r|inf.  Inside the loop: skipped
-// once converged, and with onlyOnClaim unless the recurrence just claimed
-// convergence.
+// r = b - A x (residual replacement); |r|inf.  Inside the loop it runs only
+// when needed: mode 0 on every 25th iteration (pcgsolver.h's periodic
+// recompute, here before the test), mode 1 when the recurrence just claimed
+// convergence; never once converged.
 __global__ void k_true_residual(StepConsts c, SweepLayout g, const uint8_t *fluid, const double4 *Ad, const double *b,
                                 const double *x, double *r, float *rf, unsigned long long *rmaxBits,
-                                const PcgCtl *ctl, int onlyOnClaim) {
-    if (ctl && (ctl->done || (onlyOnClaim && !ctl->claim))) return;
+                                const PcgCtl *ctl, int mode) {
+    if (ctl->done) return;
+    if (mode == 0 ? (ctl->it + 1) % 25 != 0 : !ctl->claim) return;
     const long long n = (long long)c.I * c.J * c.K;
     const long long sy = c.I, sz = (long long)c.I * c.J;
     double m = 0.0;
@@ -382,17 +384,22 @@ __global__ void k_copy_zs(StepConsts c, SweepLayout g, const uint8_t *fluid, con
     if (t < (long long)c.I * c.J * c.K) s[t] = fluid[t] ? z[sweep_index_of(c, g, t)] : 0.0f;
 }
 
-__global__ void k_set_rho(double *scal, const PcgCtl *ctl) {
-    if (!ctl->done) scal[3] = scal[1];
+__global__ void k_set_rho(double *scal, PcgCtl *ctl) {   // end of an iteration
+    if (ctl->done) return;
+    scal[3] = scal[1];
+    ctl->it += 1;
 }
+__global__ void k_init_rho(double *scal) { scal[3] = scal[1]; }
 
 // The reference's convergence test |r|inf <= tol |b|inf (pcgsolver.h:
 // 263-288) on the device.  After the update of iteration it: on the
 // iterations where r was recomputed as b - A x (every 25th) that norm
 // decides; otherwise a pass of the recurrence's norm is only a claim, which
 // k_confirm settles on b - A x.
-__global__ void k_check(PcgCtl *ctl, const unsigned long long *rmaxBits, double ptol, int it, int periodic) {
+__global__ void k_check(PcgCtl *ctl, const unsigned long long *rmaxBits, const double *scal) {
     if (ctl->done) return;
+    const int it = ctl->it, periodic = (it + 1) % 25 == 0;
+    const double ptol = scal[6];
     const double resid = __longlong_as_double((long long)rmaxBits[periodic ? 1 : 0]);
     ctl->resid = resid;
     ctl->claim = 0;
@@ -405,8 +412,10 @@ __global__ void k_check(PcgCtl *ctl, const unsigned long long *rmaxBits, double 
         }
     }
 }
-__global__ void k_confirm(PcgCtl *ctl, const unsigned long long *rmaxBits, double ptol, int it) {
+__global__ void k_confirm(PcgCtl *ctl, const unsigned long long *rmaxBits, const double *scal) {
     if (ctl->done || !ctl->claim) return;
+    const int it = ctl->it;
+    const double ptol = scal[6];
     const double resid = __longlong_as_double((long long)rmaxBits[1]);
     ctl->resid = resid;
     ctl->claim = 0;
@@ -475,8 +484,8 @@ __global__ void k_apply_pressure(StepConsts c, const float *phi, const float *wu
     V[l] = 1;
 }
 
-int cuda_fail(cudaError_t e, std::string *msg) {
-    if (msg) *msg = std::string("pressure solve: ") + cudaGetErrorString(e);
+int cuda_fail(cudaError_t e, const char *what, std::string *msg) {
+    if (msg) *msg = std::string("pressure solve: ") + what + ": " + cudaGetErrorString(e);
     return FLIP_E_CUDA;
 }
 
@@ -487,10 +496,10 @@ int pressure_partials_for(int I, int J, int K) {
     return std::min((int)div_up((long long)I * J * K, TPB), RBLOCKS);
 }
 
-#define PCK(call)                                     \
-    do {                                              \
-        cudaError_t e_ = (call);                      \
-        if (e_ != cudaSuccess) return cuda_fail(e_, errMsg); \
+#define PCK(call)                                               \
+    do {                                                        \
+        cudaError_t e_ = (call);                                \
+        if (e_ != cudaSuccess) return cuda_fail(e_, #call, errMsg); \
     } while (0)
 
 int pressure_project(const StepConsts &c, const PressureArgs &a, PressureBuffers &pb, SweepState &sw,
@@ -548,20 +557,47 @@ int pressure_project(const StepConsts &c, const PressureArgs &a, PressureBuffers
             tm->ms += ms;
             tm->launches += 2;
             tm->cellSweeps += 2LL * res->cells;
+        } else {
+            cudaGetLastError();   // a pair that was not recorded is not an error of the solve
         }
     };
-    auto precondition = [&](int q) {   // z = M^-1 r, then rho_new = z.r
-        if (tm) cudaEventRecord(tm->ev[2 * q], s);
+    bool capturing = false;
+    // inside a capture the events become graph nodes that record on every replay
+    auto record = [&](cudaEvent_t e) {
+        if (capturing) cudaEventRecordWithFlags(e, s, cudaEventRecordExternal);
+        else cudaEventRecord(e, s);
+    };
+    // z = M^-1 r, then rho_new = z.r; with `timed` the sweeps sit between
+    // event pair q (recorded as graph nodes when captured)
+    auto precondition = [&](int q, bool timed) {
+        if (timed) record(tm->ev[2 * q]);
         launch_sweeps(c, pb.L, pb.rf, pb.z, sw, &pb.ctl->done, s);
-        if (tm) cudaEventRecord(tm->ev[2 * q + 1], s);
+        if (timed) record(tm->ev[2 * q + 1]);
         { FLIP_COUNT(1); k_dot_zr<<<rb, TPB, 0, s>>>(c, pb.sl, pb.fluid, pb.z, pb.r, pb.partials, pb.ctl); }
         { FLIP_COUNT(1); k_sum_partials<<<1, 1024, 0, s>>>(pb.partials, pb.nPartials, pb.scal, 1, pb.ctl, rmax); }
     };
+    // one PCG iteration (pcgsolver.h:263-300); every launch is the same for
+    // every iteration, the iteration index lives on the device
+    auto iteration = [&](int k, bool timed) {
+        { FLIP_COUNT(1); k_spmv<<<rb, TPB, 0, s>>>(c, pb.fluid, pb.Ad, pb.s, pb.q, pb.partials, pb.ctl); }
+        { FLIP_COUNT(1); k_sum_partials<<<1, 1024, 0, s>>>(pb.partials, pb.nPartials, pb.scal, 0, pb.ctl, rmax); }
+        { FLIP_COUNT(1); k_update_xr<<<rb, TPB, 0, s>>>(c, pb.sl, pb.fluid, pb.x, pb.r, pb.rf, pb.s, pb.q, pb.scal, rmax, pb.ctl); }
+        { FLIP_COUNT(1); k_true_residual<<<rb, TPB, 0, s>>>(c, pb.sl, pb.fluid, pb.Ad, pb.b, pb.x, pb.r, pb.rf, rmax + 1, pb.ctl, 0); }
+        { FLIP_COUNT(1); k_check<<<1, 1, 0, s>>>(pb.ctl, rmax, pb.scal); }
+        { FLIP_COUNT(1); k_true_residual<<<rb, TPB, 0, s>>>(c, pb.sl, pb.fluid, pb.Ad, pb.b, pb.x, pb.r, pb.rf, rmax + 1, pb.ctl, 1); }
+        { FLIP_COUNT(1); k_confirm<<<1, 1, 0, s>>>(pb.ctl, rmax, pb.scal); }
+        precondition(1 + k, timed);
+        { FLIP_COUNT(1); k_update_s<<<nb, TPB, 0, s>>>(c, pb.sl, pb.fluid, pb.z, pb.s, pb.scal, pb.ctl); }
+        { FLIP_COUNT(1); k_set_rho<<<1, 1, 0, s>>>(pb.scal, pb.ctl); }
+    };
 
+    mail->ptol = ptol;
     PCK(cudaMemsetAsync(pb.ctl, 0, sizeof(PcgCtl), s));
     PCK(cudaMemsetAsync(rmax, 0, 2 * sizeof(unsigned long long), s));
+    PCK(cudaMemcpyAsync(pb.scal + 6, &mail->ptol, sizeof(double), cudaMemcpyHostToDevice, s));
     { FLIP_COUNT(1); k_init_r<<<rb, TPB, 0, s>>>(c, pb.sl, pb.b, pb.r, pb.rf, rmax); }
-    precondition(0);
+    sweep_epoch_guard(c, sw, 2, s);
+    precondition(0, tm != nullptr);
     PCK(cudaMemcpyAsync(&mail->rho, pb.scal + 1, sizeof(double), cudaMemcpyDeviceToHost, s));
     PCK(sync());
     if (tm) tally_pair(0);
@@ -572,30 +608,42 @@ int pressure_project(const StepConsts &c, const PressureArgs &a, PressureBuffers
     int sweepErr = 0;
     if (!(rho0 == 0 || rho0 != rho0)) {
         { FLIP_COUNT(1); k_copy_zs<<<nb, TPB, 0, s>>>(c, pb.sl, pb.fluid, pb.z, pb.s); }
-        { FLIP_COUNT(1); k_set_rho<<<1, 1, 0, s>>>(pb.scal, pb.ctl); }
-        // Iterations go to the device PCG_BATCH at a time; the convergence
-        // test runs there, and the kernels of iterations after convergence
-        // return at once.  The host reads the outcome once per batch.
+        { FLIP_COUNT(1); k_init_rho<<<1, 1, 0, s>>>(pb.scal); }
+        // Iterations go to the device PCG_BATCH at a time, as one CUDA graph
+        // (captured on first use, per context): the convergence test runs
+        // there and the kernels of iterations after convergence return at
+        // once.  The host reads the outcome once per batch.
+        const int gi = tm ? 1 : 0;
         for (int it0 = 0; it0 < a.maxIter;) {
             const int nit = std::min(PCG_BATCH, a.maxIter - it0);
-            for (int k = 0; k < nit; k++) {
-                const int it = it0 + k;
-                const int periodic = (it + 1) % 25 == 0;
-                { FLIP_COUNT(1); k_spmv<<<rb, TPB, 0, s>>>(c, pb.fluid, pb.Ad, pb.s, pb.q, pb.partials, pb.ctl); }
-                { FLIP_COUNT(1); k_sum_partials<<<1, 1024, 0, s>>>(pb.partials, pb.nPartials, pb.scal, 0, pb.ctl, rmax); }
-                { FLIP_COUNT(1); k_update_xr<<<rb, TPB, 0, s>>>(c, pb.sl, pb.fluid, pb.x, pb.r, pb.rf, pb.s, pb.q, pb.scal, rmax, pb.ctl); }
-                if (periodic) {
-                    FLIP_COUNT(1);
-                    k_true_residual<<<rb, TPB, 0, s>>>(c, pb.sl, pb.fluid, pb.Ad, pb.b, pb.x, pb.r, pb.rf, rmax + 1, pb.ctl, 0);
+            sweep_epoch_guard(c, sw, 2LL * nit, s);
+            if (nit == PCG_BATCH && !pb.batchGraph[gi] && !pb.noGraphs) {
+                long long &counter = launch_counter();
+                const long long before = counter;
+                const unsigned int epochBefore = sw.epoch;
+                if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+                    cudaGetLastError();   // e.g. the legacy default stream: no graphs, launch eagerly
+                    pb.noGraphs = true;
+                } else {
+                    cudaGraph_t graph = nullptr;
+                    capturing = true;
+                    for (int k = 0; k < PCG_BATCH; k++) iteration(k, tm != nullptr);
+                    capturing = false;
+                    PCK(cudaStreamEndCapture(s, &graph));
+                    cudaError_t e = cudaGraphInstantiate(&pb.batchGraph[gi], graph, 0);
+                    cudaGraphDestroy(graph);
+                    PCK(e);
+                    pb.batchKernels[gi] = counter - before;
+                    counter = before;   // counted when replayed
+                    sw.epoch = epochBefore;
                 }
-                { FLIP_COUNT(1); k_check<<<1, 1, 0, s>>>(pb.ctl, rmax, ptol, it, periodic); }
-                if (!periodic) {   // confirm a claim on b - A x
-                    { FLIP_COUNT(1); k_true_residual<<<rb, TPB, 0, s>>>(c, pb.sl, pb.fluid, pb.Ad, pb.b, pb.x, pb.r, pb.rf, rmax + 1, pb.ctl, 1); }
-                    { FLIP_COUNT(1); k_confirm<<<1, 1, 0, s>>>(pb.ctl, rmax, ptol, it); }
-                }
-                precondition(1 + k);
-                { FLIP_COUNT(1); k_update_s<<<nb, TPB, 0, s>>>(c, pb.sl, pb.fluid, pb.z, pb.s, pb.scal, pb.ctl); }
-                { FLIP_COUNT(1); k_set_rho<<<1, 1, 0, s>>>(pb.scal, pb.ctl); }
+            }
+            if (nit == PCG_BATCH && pb.batchGraph[gi]) {
+                PCK(cudaGraphLaunch(pb.batchGraph[gi], s));
+                launch_counter() += pb.batchKernels[gi];
+                sw.epoch += 2 * PCG_BATCH;
+            } else {
+                for (int k = 0; k < nit; k++) iteration(k, tm != nullptr);
             }
             PCK(cudaMemcpyAsync(&mail->ctl, pb.ctl, sizeof(PcgCtl), cudaMemcpyDeviceToHost, s));
             PCK(cudaMemcpyAsync(&mail->sweepErr, sw.err, sizeof(int), cudaMemcpyDeviceToHost, s));
@@ -618,6 +666,7 @@ int pressure_project(const StepConsts &c, const PressureArgs &a, PressureBuffers
     if (sweepErr) {
         cudaMemsetAsync(sw.err, 0, sizeof(int), s);
         cudaMemsetAsync(sw.xchg, 0, sweep_exchange_words(c.I, c.J, c.K) * sizeof(unsigned long long), s);
+        cudaMemsetAsync(sw.ticket, 0, 2 * sizeof(unsigned int), s);
         sw.epoch = 0;
         sync();
         if (errMsg) *errMsg = "a wavefront sweep gave up waiting for a neighbouring tile";

@@ -63,9 +63,7 @@ struct SweepArgs {
     int ntj, ntk;
     const int2 *range;             // per tile: first/last step (forward numbering) holding a system cell
     unsigned long long *xchg;      // per tile: T x TK j-edge words, then T x TJ k-edge words
-    unsigned int *ticket;
-    unsigned int ticketBase;
-    unsigned int epoch;
+    unsigned int *ticket;          // [0] tile tickets of this launch, [1] its epoch (set by k_sweep_prep)
     int *err;
     const int *skip;   // nonzero: return at once
 };
@@ -83,6 +81,7 @@ struct SweepSmem {
     unsigned long long full[NBUF], done[NBUF];
     int abort;
     int tile;
+    unsigned int epoch;
 };
 
 __device__ __forceinline__ unsigned smem_addr(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
@@ -154,10 +153,11 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_wavefront(SweepArgs a) {
         if (*(volatile const int *)a.skip || *(volatile int *)a.err) {
             sm.tile = -1;   // converged, or an earlier sweep gave up: nothing to do
         } else {
-            int t = (int)(atomicAdd(a.ticket, 1u) - a.ticketBase);
+            int t = (int)atomicAdd(&a.ticket[0], 1u);
             sm.tile = FWD ? t : ntiles - 1 - t;
         }
         sm.abort = 0;
+        sm.epoch = *(volatile unsigned int *)&a.ticket[1];
         for (int b = 0; b < NBUF; b++) {
             mb_init(&sm.full[b], 32);      // the helper warp's lanes, plus the bytes of the chunk
             mb_init(&sm.done[b], NCOMP);
@@ -184,7 +184,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_wavefront(SweepArgs a) {
     };
     auto pencil_in = [&](int lr, int ww) { return j0 + lr <= a.J - 2 && k0 + ww <= a.K - 2; };
     const size_t wordsPerTile = (size_t)T * (TJ + TK);
-    const unsigned int ep = a.epoch;
+    const unsigned int ep = sm.epoch;
     // the chunk of steps [tb, tb + rows) as one block of the layout
     auto chunk_rows = [&](int n) { return min(CH, thi + 1 - (tlo + n * CH)); };
     auto chunk_row0 = [&](int rows) { return FWD ? 0 : CH - rows; };
@@ -370,6 +370,14 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_wavefront(SweepArgs a) {
     }
 }
 
+// Before each sweep launch: a fresh epoch for its exchange words and the
+// tile tickets from zero.  Kept on the device so that a captured sequence of
+// sweeps replays with new epochs.
+__global__ void k_sweep_prep(unsigned int *ticket) {
+    ticket[0] = 0u;
+    ticket[1] += 1u;
+}
+
 __global__ void k_tile_range_init(int2 *range, int n) {
     int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t < n) range[t] = make_int2(0x7fffffff, -1);
@@ -415,8 +423,6 @@ void launch_sweep_ranges(const StepConsts &c, const uint8_t *fluid, SweepState &
     { FLIP_COUNT(1); k_tile_range_init<<<div_up(n, 256), 256, 0, s>>>(sw.range, n); }
     long long nc = (long long)c.I * c.J * c.K;
     { FLIP_COUNT(1); k_tile_range<<<div_up(nc, 256), 256, 0, s>>>(fluid, c.I, c.J, c.K, ntj, sw.range); }
-    cudaMemsetAsync(sw.ticket, 0, sizeof(unsigned int), s);
-    sw.launches = 0;
 }
 
 void launch_sweeps(const StepConsts &c, const float4 *L, const float *rf, float *z, SweepState &sw, const int *skip,
@@ -431,10 +437,6 @@ void launch_sweeps(const StepConsts &c, const float4 *L, const float *rf, float 
         cudaFuncSetAttribute(k_wavefront<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SweepSmem));
         smemSet.fetch_or(1ull << dev);
     }
-    if (sw.epoch >= 0xfffffff0u) {   // epochs are about to wrap: forget every old word
-        cudaMemsetAsync(sw.xchg, 0, sweep_exchange_words(c.I, c.J, c.K) * sizeof(unsigned long long), s);
-        sw.epoch = 0;
-    }
     SweepArgs a;
     a.L = L;
     a.J = c.J; a.K = c.K; a.NI = c.I - 2; a.T = g.T;
@@ -442,16 +444,22 @@ void launch_sweeps(const StepConsts &c, const float4 *L, const float *rf, float 
     a.range = sw.range; a.xchg = sw.xchg; a.ticket = sw.ticket; a.err = sw.err; a.skip = skip;
     // forward: y from r
     a.rin = rf; a.out = z;
-    a.epoch = ++sw.epoch;
-    a.ticketBase = (unsigned int)(sw.launches * n);
-    sw.launches++;
+    { FLIP_COUNT(1); k_sweep_prep<<<1, 1, 0, s>>>(sw.ticket); }
     { FLIP_COUNT(1); k_wavefront<true><<<n, NTHREADS, sizeof(SweepSmem), s>>>(a); }
     // backward: z from y, in place
     a.rin = z; a.out = z;
-    a.epoch = ++sw.epoch;
-    a.ticketBase = (unsigned int)(sw.launches * n);
-    sw.launches++;
+    { FLIP_COUNT(1); k_sweep_prep<<<1, 1, 0, s>>>(sw.ticket); }
     { FLIP_COUNT(1); k_wavefront<false><<<n, NTHREADS, sizeof(SweepSmem), s>>>(a); }
+    sw.epoch += 2;
+}
+
+// Epochs are 32-bit: before they wrap, forget every old word (outside any
+// capture: the host calls this between sweeps).
+void sweep_epoch_guard(const StepConsts &c, SweepState &sw, long long upcoming, cudaStream_t s) {
+    if ((long long)sw.epoch + upcoming < 0xfffffff0LL) return;
+    cudaMemsetAsync(sw.xchg, 0, sweep_exchange_words(c.I, c.J, c.K) * sizeof(unsigned long long), s);
+    cudaMemsetAsync(sw.ticket, 0, 2 * sizeof(unsigned int), s);
+    sw.epoch = 0;
 }
 
 }  // namespace flip
