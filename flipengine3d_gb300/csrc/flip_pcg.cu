@@ -16,6 +16,8 @@
 // decided on it, with the reference's test |r|inf <= tol * |b|inf.
 #include <algorithm>
 #include <cmath>
+
+#include <cooperative_groups.h>
 #include <cstring>
 #include <string>
 
@@ -23,6 +25,8 @@
 #include "flip_kernels.cuh"
 
 namespace flip {
+
+namespace cg = cooperative_groups;
 
 namespace {
 
@@ -156,10 +160,9 @@ __global__ void k_build(StepConsts c, const float *phi, const float *wu, const f
 //   d_c = A_cc - sum over earlier neighbours k (ascending index) of
 //         L_ck^2 + 0.97 L_ck (sum of k's other later-neighbour entries L_mk),
 //   L_mk = A_mk / sqrt(pivot_k); a pivot below 0.25 A_kk falls back to A_kk.
-__global__ void k_mic0_level(StepConsts c, const uint8_t *fluid, const double4 *Ad, double *invD, int level) {
-    int jj = blockIdx.x * blockDim.x + threadIdx.x;
-    int nj = c.J - 2, nk = c.K - 2;
-    if (jj >= nj * nk) return;
+__device__ __forceinline__ void mic0_cell(const StepConsts &c, const uint8_t *fluid, const double4 *Ad, double *invD,
+                                          int level, int jj) {
+    int nj = c.J - 2;
     int j = 1 + jj % nj, k = 1 + jj / nj;
     int i = level - j - k;
     if (i < 1 || i > c.I - 2) return;
@@ -190,6 +193,24 @@ __global__ void k_mic0_level(StepConsts c, const uint8_t *fluid, const double4 *
     else if (d < 0.25 * ad) inv = 1 / sqrt(ad);
     else inv = 1 / sqrt(d);
     invD[t] = inv;
+}
+
+__global__ void k_mic0_level(StepConsts c, const uint8_t *fluid, const double4 *Ad, double *invD, int level) {
+    int jj = blockIdx.x * blockDim.x + threadIdx.x;
+    if (jj < (c.J - 2) * (c.K - 2)) mic0_cell(c, fluid, Ad, invD, level, jj);
+}
+
+// All wavefronts lo..hi in one cooperative launch: the cells of a level in
+// parallel, a grid-wide barrier between levels (every block is resident, so
+// the barrier completes).
+__global__ void k_mic0_levels(StepConsts c, const uint8_t *fluid, const double4 *Ad, double *invD, int lo, int hi) {
+    cg::grid_group grid = cg::this_grid();
+    const int np = (c.J - 2) * (c.K - 2);
+    for (int lv = lo; lv <= hi; lv++) {
+        for (int jj = blockIdx.x * blockDim.x + threadIdx.x; jj < np; jj += gridDim.x * blockDim.x)
+            mic0_cell(c, fluid, Ad, invD, lv, jj);
+        grid.sync();
+    }
 }
 
 // the FP32 factor rows of the interior cells, into the sweep layout
@@ -539,9 +560,30 @@ int pressure_project(const StepConsts &c, const PressureArgs &a, PressureBuffers
         return FLIP_E_RUNTIME;
     }
 
-    // MIC(0) factor, one launch per wavefront
+    // MIC(0) factor, wavefront by wavefront: one cooperative launch over all
+    // levels where the device allows it, else one launch per level
     const int np = (c.J - 2) * (c.K - 2);
-    for (int lv = lo; lv <= hi; lv++) {
+    bool factored = false;
+    {
+        int dev = 0, coop = 0, perSM = 0, sms = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_mic0_levels, TPB, 0);
+        if (coop && perSM > 0) {
+            const int grid = std::max(1, std::min((int)div_up(np, TPB), perSM * sms));
+            int lo_ = lo, hi_ = hi;
+            StepConsts c_ = c;
+            const uint8_t *fl = pb.fluid;
+            const double4 *ad = pb.Ad;
+            double *inv = pb.invdiagD;
+            void *args[] = {&c_, &fl, &ad, &inv, &lo_, &hi_};
+            FLIP_COUNT(1);
+            factored = cudaLaunchCooperativeKernel((const void *)k_mic0_levels, grid, TPB, args, 0, s) == cudaSuccess;
+            if (!factored) cudaGetLastError();
+        }
+    }
+    for (int lv = lo; lv <= hi && !factored; lv++) {
         FLIP_COUNT(1);
         k_mic0_level<<<div_up(np, TPB), TPB, 0, s>>>(c, pb.fluid, pb.Ad, pb.invdiagD, lv);
     }
