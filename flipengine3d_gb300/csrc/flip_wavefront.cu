@@ -48,10 +48,12 @@ namespace flip {
 
 namespace {
 
-constexpr int TJ = SWEEP_TJ, TK = SWEEP_TK, NP = SWEEP_NP, CH = 8, NBUF = 4;
-// the helper warp's lanes take the CH x TK j-edge words two at a time and the
+constexpr int TJ = SWEEP_TJ, TK = SWEEP_TK, NP = SWEEP_NP, CH = 8;
+constexpr int NBUF = TK <= 8 ? 4 : 2;   // ring slots that fit in shared memory
+// the helper warp's lanes take the CH x TK j-edge words JQ at a time and the
 // CH x TJ k-edge words one step each
-static_assert(CH * TK == 64 && TJ == 32, "edge-word mapping of the helper warp");
+constexpr int JQ = CH * TK / 32;
+static_assert((CH * TK) % 32 == 0 && TJ == 32 && JQ <= 32, "edge-word mapping of the helper warp");
 constexpr int NCOMP = NP, NTHREADS = NCOMP + 32;
 constexpr unsigned int SPIN_LIMIT = 1u << 22;   // poll rounds of <= ~250 ns: about a second
 
@@ -228,8 +230,8 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_wavefront(SweepArgs a) {
             lastIssued = m;
             // edge terms: the consumer cell is computed and the producer's
             // cell (TJ-1 or TK-1 steps later there) too
-            float vK[CH], vJ[2];
-            unsigned long long wK[CH], wJ[2];
+            float vK[CH], vJ[JQ];
+            unsigned long long wK[CH], wJ[JQ];
             unsigned int needK = 0, needJ = 0;
 #pragma unroll
             for (int s = 0; s < CH; s++) {
@@ -240,8 +242,8 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_wavefront(SweepArgs a) {
                 needK |= need ? 1u << s : 0u;
             }
 #pragma unroll
-            for (int q = 0; q < 2; q++) {
-                const int e = lane + 32 * q, es = e >> 3, ew = e & 7, te = tb + es, i = cell(laneJ, ew, te);
+            for (int q = 0; q < JQ; q++) {
+                const int e = lane + 32 * q, es = e / TK, ew = e % TK, te = tb + es, i = cell(laneJ, ew, te);
                 const bool need = srcJ >= 0 && es < rows && pencil_in(laneJ, ew) && i >= 1 && i <= NI &&
                                   te + (TJ - 1) >= rgJ.x && te + (TJ - 1) <= rgJ.y;
                 wJ[q] = need ? ld_word(srcJw + (size_t)(te + TJ - 1) * TK + ew) : 0ull;
@@ -253,7 +255,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_wavefront(SweepArgs a) {
                 for (int s = 0; s < CH; s++)
                     missK |= ((needK >> s) & 1u) && (unsigned int)(wK[s] >> 32) != ep ? 1u << s : 0u;
 #pragma unroll
-                for (int q = 0; q < 2; q++)
+                for (int q = 0; q < JQ; q++)
                     missJ |= ((needJ >> q) & 1u) && (unsigned int)(wJ[q] >> 32) != ep ? 1u << q : 0u;
                 if (!(missK | missJ)) break;
                 if (spin >= SPIN_LIMIT) {
@@ -268,21 +270,21 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_wavefront(SweepArgs a) {
                 for (int s = 0; s < CH; s++)
                     if ((missK >> s) & 1u) wK[s] = ld_word(srcKw + (size_t)(tb + s + TK - 1) * TJ + lane);
 #pragma unroll
-                for (int q = 0; q < 2; q++) {
-                    const int e = lane + 32 * q, es = e >> 3, ew = e & 7;
+                for (int q = 0; q < JQ; q++) {
+                    const int e = lane + 32 * q, es = e / TK, ew = e % TK;
                     if ((missJ >> q) & 1u) wJ[q] = ld_word(srcJw + (size_t)(tb + es + TJ - 1) * TK + ew);
                 }
             }
 #pragma unroll
             for (int s = 0; s < CH; s++) vK[s] = __uint_as_float((unsigned int)wK[s]);
 #pragma unroll
-            for (int q = 0; q < 2; q++) vJ[q] = __uint_as_float((unsigned int)wJ[q]);
+            for (int q = 0; q < JQ; q++) vJ[q] = __uint_as_float((unsigned int)wJ[q]);
 #pragma unroll
             for (int s = 0; s < CH; s++) sl.eK[s][lane] = vK[s];
 #pragma unroll
-            for (int q = 0; q < 2; q++) {
+            for (int q = 0; q < JQ; q++) {
                 const int e = lane + 32 * q;
-                sl.eJ[e >> 3][e & 7] = vJ[q];
+                sl.eJ[e / TK][e % TK] = vJ[q];
             }
             if (lane == 0) bulk_wait_read_all();   // the slot's results of chunk m - NBUF are out
             __syncwarp();
