@@ -118,7 +118,7 @@ __device__ bool mb_wait(unsigned long long *b, unsigned parity, int *abortFlag, 
     for (unsigned int spin = 0; spin < SPIN_LIMIT; spin++) {
         if (mb_test(b, parity)) return true;
         if (*(volatile int *)abortFlag) return false;
-        if (spin > 16) __nanosleep(32);
+        if (spin > 1024) __nanosleep(32);
     }
     *(volatile int *)abortFlag = 1;
     atomicExch(err, 1);
@@ -265,7 +265,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_wavefront(SweepArgs a) {
                     break;
                 }
                 if (*(volatile int *)&sm.abort || *(volatile int *)a.err) { ok = false; break; }
-                if (spin > 8) __nanosleep(64);
+                if (spin > 1024) __nanosleep(64);
 #pragma unroll
                 for (int s = 0; s < CH; s++)
                     if ((missK >> s) & 1u) wK[s] = ld_word(srcKw + (size_t)(tb + s + TK - 1) * TJ + lane);
