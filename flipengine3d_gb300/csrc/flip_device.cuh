@@ -119,6 +119,10 @@ constexpr int PCG_BATCH = 8;   // iterations enqueued between host checks
 
 struct PressureBuffers {
     uint8_t *fluid;        // interior cell with phi < 0 (a row of the system)
+    // the rows as a list, in cell order (built once per solve by a scan):
+    // flat index and sweep-layout index of each row, and their number
+    int *fluidFlag, *fluidPos, *fluidScan, *nFluid;
+    int *fluidIdx, *fluidSk;
     double4 *Ad;           // rows {diag, to +x, to +y, to +z}, FP64
     double *b;             // right-hand side (negative divergence)
     double *invdiagD;      // MIC(0) inverse pivots, FP64

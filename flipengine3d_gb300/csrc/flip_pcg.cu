@@ -38,7 +38,7 @@ __device__ __forceinline__ bool sys_cell(const StepConsts &c, const float *phi, 
     return phi[(long long)i + (long long)c.I * ((long long)j + (long long)c.J * k)] < 0.0f;
 }
 
-__global__ void k_flags(StepConsts c, const float *phi, uint8_t *fluid, int *levelRange) {
+__global__ void k_flags(StepConsts c, const float *phi, uint8_t *fluid, int *fluidFlag, int *levelRange) {
     long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     Dims d{c.I, c.J, c.K};
     bool f = false;
@@ -48,6 +48,7 @@ __global__ void k_flags(StepConsts c, const float *phi, uint8_t *fluid, int *lev
         unflatten(t, c.I, c.J, i, j, k);
         f = sys_cell(c, phi, i, j, k);
         fluid[t] = f ? 1 : 0;
+        fluidFlag[t] = f ? 1 : 0;
         lv = i + j + k;
     }
     // warp-aggregated min/max/count of the system cells' levels
@@ -230,12 +231,6 @@ __global__ void k_mic0_finalize(StepConsts c, SweepLayout g, const uint8_t *flui
     L[sweep_index(g, i, j, k)] = v;
 }
 
-__device__ __forceinline__ long long sweep_index_of(const StepConsts &c, const SweepLayout &g, long long t) {
-    int i, j, k;
-    unflatten(t, c.I, c.J, i, j, k);
-    return sweep_index(g, i, j, k);
-}
-
 template <class T>
 __device__ __forceinline__ T block_sum(T v, T *sh) {
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
@@ -256,18 +251,28 @@ __device__ __forceinline__ T block_sum(T v, T *sh) {
 // sum is deterministic and the FP64 reduction work is per thread, not per
 // cell.
 
-// q = A s (FP64), block partials of s.q
-__global__ void k_spmv(StepConsts c, const uint8_t *__restrict__ fluid, const double4 *__restrict__ Ad,
+// the rows of the system as a list: flat index and sweep-layout index
+__global__ void k_compact_rows(StepConsts c, SweepLayout g, const uint8_t *fluid, const int *pos, int *idx, int *sk) {
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)c.I * c.J * c.K || !fluid[t]) return;
+    int i, j, k;
+    unflatten(t, c.I, c.J, i, j, k);
+    const int e = pos[t];
+    idx[e] = (int)t;
+    sk[e] = (int)sweep_index(g, i, j, k);
+}
+
+// q = A s (FP64) over the rows, block partials of s.q
+__global__ void k_spmv(StepConsts c, const int *__restrict__ rows, const int *nRows, const double4 *__restrict__ Ad,
                        const float *__restrict__ s, double *__restrict__ q, double *partials, const PcgCtl *ctl) {
     __shared__ double sh[32];
     if (ctl->done) return;
-    const long long n = (long long)c.I * c.J * c.K;
+    const int n = *nRows;
     const long long sy = c.I, sz = (long long)c.I * c.J;
     double part = 0.0;
-#pragma unroll 4
-    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
-        if (!fluid[t]) continue;
-        double4 a = Ad[t];
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
+        const long long t = rows[e];
+        const double4 a = Ad[t];
         double acc = a.x * (double)s[t];
         acc = fma(a.y, (double)s[t + 1], acc);
         acc = fma(a.z, (double)s[t + sy], acc);
@@ -282,15 +287,14 @@ __global__ void k_spmv(StepConsts c, const uint8_t *__restrict__ fluid, const do
     if (threadIdx.x == 0) partials[blockIdx.x] = b;
 }
 
-__global__ void k_dot_zr(StepConsts c, SweepLayout g, const uint8_t *__restrict__ fluid, const float *__restrict__ z,
-                         const double *__restrict__ r, double *partials, const PcgCtl *ctl) {
+__global__ void k_dot_zr(const int *__restrict__ rows, const int *__restrict__ rowsSk, const int *nRows,
+                         const float *__restrict__ z, const double *__restrict__ r, double *partials, const PcgCtl *ctl) {
     __shared__ double sh[32];
     if (ctl->done) return;
-    const long long n = (long long)c.I * c.J * c.K;
+    const int n = *nRows;
     double part = 0.0;
-#pragma unroll 4
-    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x)
-        if (fluid[t]) part = fma((double)z[sweep_index_of(c, g, t)], r[t], part);
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x)
+        part = fma((double)z[rowsSk[e]], r[rows[e]], part);
     double s = block_sum(part, sh);
     if (threadIdx.x == 0) partials[blockIdx.x] = s;
 }
@@ -321,22 +325,21 @@ __global__ void k_sum_partials(const double *partials, int n, double *scal, int 
 
 // x += alpha s, r -= alpha q with alpha = rho / s.q passed on as float, as
 // BLAS::addScaled(float alpha, ...) does (blaswrapper.h:129-158); |r|inf
-__global__ void k_update_xr(StepConsts c, SweepLayout g, const uint8_t *__restrict__ fluid, double *__restrict__ x,
-                            double *__restrict__ r, float *__restrict__ rf, const float *__restrict__ s,
-                            const double *__restrict__ q, const double *scal, unsigned long long *rmaxBits,
-                            const PcgCtl *ctl) {
+__global__ void k_update_xr(const int *__restrict__ rows, const int *__restrict__ rowsSk, const int *nRows,
+                            double *__restrict__ x, double *__restrict__ r, float *__restrict__ rf,
+                            const float *__restrict__ s, const double *__restrict__ q, const double *scal,
+                            unsigned long long *rmaxBits, const PcgCtl *ctl) {
     if (ctl->done) return;
-    const long long n = (long long)c.I * c.J * c.K;
+    const int n = *nRows;
     const double alpha = scal[4];
     double m = 0.0;
-#pragma unroll 4
-    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
-        if (!fluid[t]) continue;
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
+        const int t = rows[e];
         x[t] = fma(alpha, (double)s[t], x[t]);
-        double rv = fma(-alpha, q[t], r[t]);
+        const double rv = fma(-alpha, q[t], r[t]);
         r[t] = rv;
-        rf[sweep_index_of(c, g, t)] = (float)rv;
-        double av = fabs(rv);
+        rf[rowsSk[e]] = (float)rv;
+        const double av = fabs(rv);
         m = (av != av || av > m) ? av : m;   // a NaN sticks
     }
     block_max_to(m, rmaxBits);
@@ -346,18 +349,18 @@ __global__ void k_update_xr(StepConsts c, SweepLayout g, const uint8_t *__restri
 // when needed: mode 0 on every 25th iteration (pcgsolver.h's periodic
 // recompute, here before the test), mode 1 when the recurrence just claimed
 // convergence; never once converged.
-__global__ void k_true_residual(StepConsts c, SweepLayout g, const uint8_t *fluid, const double4 *Ad, const double *b,
-                                const double *x, double *r, float *rf, unsigned long long *rmaxBits,
-                                const PcgCtl *ctl, int mode) {
+__global__ void k_true_residual(StepConsts c, const int *__restrict__ rows, const int *__restrict__ rowsSk,
+                                const int *nRows, const double4 *__restrict__ Ad, const double *__restrict__ b,
+                                const double *__restrict__ x, double *__restrict__ r, float *__restrict__ rf,
+                                unsigned long long *rmaxBits, const PcgCtl *ctl, int mode) {
     if (ctl->done) return;
     if (mode == 0 ? (ctl->it + 1) % 25 != 0 : !ctl->claim) return;
-    const long long n = (long long)c.I * c.J * c.K;
+    const int n = *nRows;
     const long long sy = c.I, sz = (long long)c.I * c.J;
     double m = 0.0;
-#pragma unroll 4
-    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
-        if (!fluid[t]) continue;
-        double4 a = Ad[t];
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
+        const long long t = rows[e];
+        const double4 a = Ad[t];
         double ax = a.x * x[t];
         ax = fma(a.y, x[t + 1], ax);
         ax = fma(a.z, x[t + sy], ax);
@@ -365,10 +368,10 @@ __global__ void k_true_residual(StepConsts c, SweepLayout g, const uint8_t *flui
         ax = fma(Ad[t - 1].y, x[t - 1], ax);
         ax = fma(Ad[t - sy].z, x[t - sy], ax);
         ax = fma(Ad[t - sz].w, x[t - sz], ax);
-        double rv = b[t] - ax;
+        const double rv = b[t] - ax;
         r[t] = rv;
-        rf[sweep_index_of(c, g, t)] = (float)rv;
-        double av = fabs(rv);
+        rf[rowsSk[e]] = (float)rv;
+        const double av = fabs(rv);
         m = (av != av || av > m) ? av : m;
     }
     block_max_to(m, rmaxBits);
@@ -392,17 +395,22 @@ __global__ void k_init_r(StepConsts c, SweepLayout g, const double *b, double *r
 }
 
 // s = z + beta s, beta = rho_new / rho as float (pcgsolver.h:295-298)
-__global__ void k_update_s(StepConsts c, SweepLayout g, const uint8_t *fluid, const float *z, float *s,
-                           const double *scal, const PcgCtl *ctl) {
+__global__ void k_update_s(const int *__restrict__ rows, const int *__restrict__ rowsSk, const int *nRows,
+                           const float *__restrict__ z, float *__restrict__ s, const double *scal, const PcgCtl *ctl) {
     if (ctl->done) return;
-    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int n = *nRows;
     const float beta = (float)scal[5];
-    if (t < (long long)c.I * c.J * c.K && fluid[t]) s[t] = __fmaf_rn(beta, s[t], z[sweep_index_of(c, g, t)]);
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
+        const int t = rows[e];
+        s[t] = __fmaf_rn(beta, s[t], z[rowsSk[e]]);
+    }
 }
 
-__global__ void k_copy_zs(StepConsts c, SweepLayout g, const uint8_t *fluid, const float *z, float *s) {
-    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t < (long long)c.I * c.J * c.K) s[t] = fluid[t] ? z[sweep_index_of(c, g, t)] : 0.0f;
+// s = z on the rows (s is zero elsewhere)
+__global__ void k_copy_zs(const int *__restrict__ rows, const int *__restrict__ rowsSk, const int *nRows,
+                          const float *__restrict__ z, float *__restrict__ s) {
+    const int n = *nRows;
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) s[rows[e]] = z[rowsSk[e]];
 }
 
 __global__ void k_set_rho(double *scal, PcgCtl *ctl) {   // end of an iteration
@@ -541,7 +549,10 @@ int pressure_project(const StepConsts &c, const PressureArgs &a, PressureBuffers
     int lr[3] = {0x7fffffff, -1, 0};
     PCK(cudaMemcpyAsync(pb.levelRange, lr, sizeof(lr), cudaMemcpyHostToDevice, s));
     PCK(cudaMemsetAsync(pb.scal, 0, 8 * sizeof(double), s));
-    { FLIP_COUNT(1); k_flags<<<nb, TPB, 0, s>>>(c, a.phi, pb.fluid, pb.levelRange); }
+    { FLIP_COUNT(1); k_flags<<<nb, TPB, 0, s>>>(c, a.phi, pb.fluid, pb.fluidFlag, pb.levelRange); }
+    // the rows as a list in cell order (a scan keeps it deterministic)
+    launch_scan_cells(pb.fluidFlag, (int)n, pb.fluidPos, pb.fluidScan, pb.nFluid, s);
+    { FLIP_COUNT(1); k_compact_rows<<<nb, TPB, 0, s>>>(c, pb.sl, pb.fluid, pb.fluidPos, pb.fluidIdx, pb.fluidSk); }
     { FLIP_COUNT(1); k_build<<<nb, TPB, 0, s>>>(c, a.phi, a.wu, a.wv, a.ww, a.u, a.v, a.w, mf, pb); }
     PCK(cudaMemcpyAsync(mail->levelRange, pb.levelRange, 3 * sizeof(int), cudaMemcpyDeviceToHost, s));
     PCK(cudaMemcpyAsync(&mail->bmax, pb.scal + 2, sizeof(double), cudaMemcpyDeviceToHost, s));
@@ -615,21 +626,21 @@ int pressure_project(const StepConsts &c, const PressureArgs &a, PressureBuffers
         if (timed) record(tm->ev[2 * q]);
         launch_sweeps(c, pb.L, pb.rf, pb.z, sw, &pb.ctl->done, s);
         if (timed) record(tm->ev[2 * q + 1]);
-        { FLIP_COUNT(1); k_dot_zr<<<rb, TPB, 0, s>>>(c, pb.sl, pb.fluid, pb.z, pb.r, pb.partials, pb.ctl); }
+        { FLIP_COUNT(1); k_dot_zr<<<rb, TPB, 0, s>>>(pb.fluidIdx, pb.fluidSk, pb.nFluid, pb.z, pb.r, pb.partials, pb.ctl); }
         { FLIP_COUNT(1); k_sum_partials<<<1, 1024, 0, s>>>(pb.partials, pb.nPartials, pb.scal, 1, pb.ctl, rmax); }
     };
     // one PCG iteration (pcgsolver.h:263-300); every launch is the same for
     // every iteration, the iteration index lives on the device
     auto iteration = [&](int k, bool timed) {
-        { FLIP_COUNT(1); k_spmv<<<rb, TPB, 0, s>>>(c, pb.fluid, pb.Ad, pb.s, pb.q, pb.partials, pb.ctl); }
+        { FLIP_COUNT(1); k_spmv<<<rb, TPB, 0, s>>>(c, pb.fluidIdx, pb.nFluid, pb.Ad, pb.s, pb.q, pb.partials, pb.ctl); }
         { FLIP_COUNT(1); k_sum_partials<<<1, 1024, 0, s>>>(pb.partials, pb.nPartials, pb.scal, 0, pb.ctl, rmax); }
-        { FLIP_COUNT(1); k_update_xr<<<rb, TPB, 0, s>>>(c, pb.sl, pb.fluid, pb.x, pb.r, pb.rf, pb.s, pb.q, pb.scal, rmax, pb.ctl); }
-        { FLIP_COUNT(1); k_true_residual<<<rb, TPB, 0, s>>>(c, pb.sl, pb.fluid, pb.Ad, pb.b, pb.x, pb.r, pb.rf, rmax + 1, pb.ctl, 0); }
+        { FLIP_COUNT(1); k_update_xr<<<rb, TPB, 0, s>>>(pb.fluidIdx, pb.fluidSk, pb.nFluid, pb.x, pb.r, pb.rf, pb.s, pb.q, pb.scal, rmax, pb.ctl); }
+        { FLIP_COUNT(1); k_true_residual<<<rb, TPB, 0, s>>>(c, pb.fluidIdx, pb.fluidSk, pb.nFluid, pb.Ad, pb.b, pb.x, pb.r, pb.rf, rmax + 1, pb.ctl, 0); }
         { FLIP_COUNT(1); k_check<<<1, 1, 0, s>>>(pb.ctl, rmax, pb.scal); }
-        { FLIP_COUNT(1); k_true_residual<<<rb, TPB, 0, s>>>(c, pb.sl, pb.fluid, pb.Ad, pb.b, pb.x, pb.r, pb.rf, rmax + 1, pb.ctl, 1); }
+        { FLIP_COUNT(1); k_true_residual<<<rb, TPB, 0, s>>>(c, pb.fluidIdx, pb.fluidSk, pb.nFluid, pb.Ad, pb.b, pb.x, pb.r, pb.rf, rmax + 1, pb.ctl, 1); }
         { FLIP_COUNT(1); k_confirm<<<1, 1, 0, s>>>(pb.ctl, rmax, pb.scal); }
         precondition(1 + k, timed);
-        { FLIP_COUNT(1); k_update_s<<<nb, TPB, 0, s>>>(c, pb.sl, pb.fluid, pb.z, pb.s, pb.scal, pb.ctl); }
+        { FLIP_COUNT(1); k_update_s<<<rb, TPB, 0, s>>>(pb.fluidIdx, pb.fluidSk, pb.nFluid, pb.z, pb.s, pb.scal, pb.ctl); }
         { FLIP_COUNT(1); k_set_rho<<<1, 1, 0, s>>>(pb.scal, pb.ctl); }
     };
 
@@ -649,7 +660,7 @@ int pressure_project(const StepConsts &c, const PressureArgs &a, PressureBuffers
     double resid = bmax;
     int sweepErr = 0;
     if (!(rho0 == 0 || rho0 != rho0)) {
-        { FLIP_COUNT(1); k_copy_zs<<<nb, TPB, 0, s>>>(c, pb.sl, pb.fluid, pb.z, pb.s); }
+        { FLIP_COUNT(1); k_copy_zs<<<rb, TPB, 0, s>>>(pb.fluidIdx, pb.fluidSk, pb.nFluid, pb.z, pb.s); }
         { FLIP_COUNT(1); k_init_rho<<<1, 1, 0, s>>>(pb.scal); }
         // Iterations go to the device PCG_BATCH at a time, as one CUDA graph
         // (captured on first use, per context): the convergence test runs
