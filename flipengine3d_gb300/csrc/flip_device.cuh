@@ -1,5 +1,6 @@
 // Launch interface of the FLIP step kernels (host side of the CUDA code).
 #pragma once
+#include <algorithm>
 #include <cstdint>
 #include <string>
 #include <cuda_runtime.h>
@@ -75,33 +76,45 @@ void launch_mark_fast(const ParticleSoA &p, int n, const float *maxSpeedSq, unsi
 // -- pressure projection (flip_pcg.cu); dense cell-grid vectors, cells
 // outside the system hold zeros
 // Sweep layout: the vectors of the MIC(0) sweeps (factor rows, right-hand
-// side, result) are stored step-major.  The interior pencils are cut into
-// tiles of SWEEP_TJ (j) x SWEEP_TK (k); pencil (l, w) of a tile holds cell i
-// at forward step tf = i - 1 + l + w, and entry (tile, tf, w, l) lives at
-// ((tile * T + tf) * SWEEP_TJ * SWEEP_TK + w * SWEEP_TJ + l), T = I - 2 +
-// SWEEP_TJ - 1 + SWEEP_TK - 1.  A chunk of consecutive steps of a tile is one
-// contiguous block, in either sweep direction.  Entries that hold no interior
-// cell stay zero.
+// side, result) are stored step-major.  The interior pencils along i are cut
+// into tiles of SWEEP_TJ x SWEEP_TK: SWEEP_TJ along the tile's lane axis a
+// and SWEEP_TK along its warp axis b, where (a, b) = (j, k), or (k, j) when
+// `swap` is set (the orientation is chosen per solve).  Pencil (l, w) of a
+// tile holds cell i at forward step tf = i - 1 + l + w, and entry
+// (tile, tf, w, l) lives at ((tile * T + tf) * SWEEP_NP + w * SWEEP_TJ + l),
+// T = I - 2 + SWEEP_TJ - 1 + SWEEP_TK - 1.  A chunk of consecutive steps of a
+// tile is one contiguous block, in either sweep direction.  Entries that hold
+// no interior cell stay zero.
 constexpr int SWEEP_TJ = 32, SWEEP_TK = 8, SWEEP_NP = SWEEP_TJ * SWEEP_TK;
 struct SweepLayout {
-    int ntj, ntk, T;
+    int ntj, ntk, T;   // tiles along the lane and warp axes, steps per tile
+    int swap;          // 0: lanes along j, warps along k; 1: lanes along k, warps along j
+    int EA, EB;        // grid extents along the lane and warp axes
 };
-inline SweepLayout sweep_layout(int I, int J, int K) {
+inline SweepLayout sweep_layout(int I, int J, int K, int swap = 0) {
     SweepLayout g;
-    g.ntj = (J - 2 + SWEEP_TJ - 1) / SWEEP_TJ;
-    g.ntk = (K - 2 + SWEEP_TK - 1) / SWEEP_TK;
+    g.swap = swap;
+    g.EA = swap ? K : J;
+    g.EB = swap ? J : K;
+    g.ntj = (g.EA - 2 + SWEEP_TJ - 1) / SWEEP_TJ;
+    g.ntk = (g.EB - 2 + SWEEP_TK - 1) / SWEEP_TK;
     g.T = (I - 2) + (SWEEP_TJ - 1) + (SWEEP_TK - 1);
     return g;
 }
+// entries of either orientation: the arrays are allocated for the larger
 inline long long sweep_layout_size(int I, int J, int K) {
-    SweepLayout g = sweep_layout(I, J, K);
-    return (long long)g.ntj * g.ntk * g.T * SWEEP_NP;
+    long long best = 0;
+    for (int sw = 0; sw < 2; sw++) {
+        SweepLayout g = sweep_layout(I, J, K, sw);
+        best = std::max(best, (long long)g.ntj * g.ntk * g.T * SWEEP_NP);
+    }
+    return best;
 }
 // entry of interior cell (i, j, k)
-__device__ __forceinline__ long long sweep_index(const SweepLayout &g, int i, int j, int k) {
-    const int jj = j - 1, kk = k - 1;
-    const int l = jj % SWEEP_TJ, w = kk % SWEEP_TK;
-    const int tile = jj / SWEEP_TJ + g.ntj * (kk / SWEEP_TK);
+__host__ __device__ __forceinline__ long long sweep_index(const SweepLayout &g, int i, int j, int k) {
+    const int aa = (g.swap ? k : j) - 1, bb = (g.swap ? j : k) - 1;
+    const int l = aa % SWEEP_TJ, w = bb % SWEEP_TK;
+    const int tile = aa / SWEEP_TJ + g.ntj * (bb / SWEEP_TK);
     return ((long long)tile * g.T + (i - 1 + l + w)) * SWEEP_NP + w * SWEEP_TJ + l;
 }
 
@@ -131,17 +144,18 @@ struct PressureBuffers {
     float *z;              // preconditioned residual, sweep layout
     float *s;              // search direction
     float *rf;             // r rounded to FP32, the forward sweep's right-hand side, sweep layout
-    SweepLayout sl;
+    SweepLayout sl;        // the orientation of the current solve
+    long long nsl;         // entries allocated for the sweep layout
     double *partials;      // per-block partial sums (deterministic reduction)
     double *scal;          // [0]=s.q [1]=z.r (new rho) [2]=|b|inf [3]=rho [4]=alpha [5]=beta [6]=tol |b|inf
     unsigned long long *rmaxBits;  // [0] |r|inf of the recurrence, [1] of b - A x, as double bits
     PcgCtl *ctl;
     // PCG_BATCH iterations captured as a CUDA graph, replayed per batch;
     // [1] also records the sweep timing events
-    cudaGraphExec_t batchGraph[2] = {};
-    long long batchKernels[2] = {};
+    cudaGraphExec_t batchGraph[2][2] = {};   // [timed][orientation]
+    long long batchKernels[2][2] = {};
     bool noGraphs = false;   // the stream cannot be captured: launch eagerly
-    int *levelRange;       // [0]=min(i+j+k) [1]=max(i+j+k) [2]=system size
+    int *levelRange;       // [0]=min(i+j+k) [1]=max(i+j+k) [2]=system size [3..6]=min/max j, min/max k
     float *pressure;       // float copy of x for the velocity update
     int nPartials;
 };
@@ -154,6 +168,7 @@ struct PressureArgs {
     float *dumpPressure;   // host, optional
     double *dumpRhs;       // host, optional
     struct SweepTiming *sweepTiming;   // optional: event-timed sweep launches
+    int sweepOrientation;  // -1: chosen per solve; 0: lanes along j; 1: lanes along k
 };
 // Device time of the preconditioner sweeps, summed over launches.
 struct SweepTiming {
@@ -163,7 +178,7 @@ struct SweepTiming {
     long long cellSweeps;   // sum over launches of the system rows swept
 };
 struct PressureMail {      // pinned host scalars
-    int levelRange[3];
+    int levelRange[8];
     double bmax, rho, ptol;
     PcgCtl ctl;
     int sweepErr;
@@ -184,13 +199,14 @@ struct SweepState {
     int *err;                // set when a bounded wait gave up
     unsigned int epoch;      // host count of the epochs issued (wrap guard)
 };
-int sweep_tiles(int J, int K, int *ntj, int *ntk);
-long long sweep_exchange_words(int I, int J, int K);
-void launch_sweep_ranges(const StepConsts &c, const uint8_t *fluid, SweepState &sw, cudaStream_t s);
+int sweep_tiles_max(int I, int J, int K);           // tiles of the larger orientation
+long long sweep_exchange_words(int I, int J, int K);   // for the larger orientation
+void launch_sweep_ranges(const StepConsts &c, const SweepLayout &g, const uint8_t *fluid, SweepState &sw,
+                         cudaStream_t s);
 // z = M^-1 r with the MIC(0) factor L: forward then backward sweep
 // The launches return at once when *skip is set (a converged solve).
-void launch_sweeps(const StepConsts &c, const float4 *L, const float *rf, float *z, SweepState &sw, const int *skip,
-                   cudaStream_t s);
+void launch_sweeps(const StepConsts &c, const SweepLayout &g, const float4 *L, const float *rf, float *z,
+                   SweepState &sw, const int *skip, cudaStream_t s);
 void sweep_epoch_guard(const StepConsts &c, SweepState &sw, long long upcoming, cudaStream_t s);
 
 int pressure_partials(const StepConsts &c);

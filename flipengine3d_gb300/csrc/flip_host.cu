@@ -101,7 +101,7 @@ struct flip_ctx {
     float *maxSpeedSq = nullptr;
     // pinned host mailbox for per-substep scalars
     struct Mail {
-        int levelRange[3];
+        int levelRange[8];
         double bmax;
         double rho;
         unsigned int rmaxBits;
@@ -117,6 +117,7 @@ struct flip_ctx {
 
     // stage timing
     bool timing = false;
+    int sweepOrientation = -1;
     bool endMarkPending = false;
     cudaEvent_t ev[FLIP_NUM_STAGES + 1] = {};
     double stageMs[FLIP_NUM_STAGES] = {};
@@ -197,7 +198,8 @@ int alloc_grids(flip_ctx *x) {
     if ((rc = x->alloc(&x->status, x->nu() + x->nv() + x->nw()))) return rc;
     PressureBuffers &p = x->pr;
     const long long nsl = sweep_layout_size(x->I, x->J, x->K);
-    p.sl = sweep_layout(x->I, x->J, x->K);
+    p.sl = sweep_layout(x->I, x->J, x->K, 0);
+    p.nsl = nsl;
     if ((rc = x->alloc(&p.fluid, nc)) || (rc = x->alloc(&p.Ad, nc)) || (rc = x->alloc(&p.L, nsl)) ||
         (rc = x->alloc(&p.b, nc)) || (rc = x->alloc(&p.invdiagD, nc)) || (rc = x->alloc(&p.x, nc)) ||
         (rc = x->alloc(&p.r, nc)) || (rc = x->alloc(&p.q, nc)) || (rc = x->alloc(&p.z, nsl)) ||
@@ -213,11 +215,10 @@ int alloc_grids(flip_ctx *x) {
     CK(cudaMemsetAsync(p.z, 0, nsl * sizeof(float), x->stream));
     p.nPartials = pressure_partials(x->c);
     if ((rc = x->alloc(&p.partials, p.nPartials + 32)) || (rc = x->alloc(&p.scal, 8)) ||
-        (rc = x->alloc(&p.rmaxBits, 2)) || (rc = x->alloc(&p.levelRange, 4)) || (rc = x->alloc(&p.ctl, 1)))
+        (rc = x->alloc(&p.rmaxBits, 2)) || (rc = x->alloc(&p.levelRange, 8)) || (rc = x->alloc(&p.ctl, 1)))
         return rc;
     {
-        int ntj, ntk;
-        int nt = sweep_tiles(x->J, x->K, &ntj, &ntk);
+        int nt = sweep_tiles_max(x->I, x->J, x->K);
         long long nw = sweep_exchange_words(x->I, x->J, x->K);
         x->sweep.xchgWords = nw;
         if ((rc = x->alloc(&x->sweep.range, nt)) || (rc = x->alloc(&x->sweep.xchg, nw)) ||
@@ -388,6 +389,7 @@ int pressure_solve(flip_ctx *x, double dt, bool *applied, flip_stage_dump *d) {
     a.dumpPressure = d ? d->pressure : nullptr;
     a.dumpRhs = d ? d->rhs : nullptr;
     a.sweepTiming = x->timing ? &x->sweepTiming : nullptr;
+    a.sweepOrientation = x->sweepOrientation;
     PressureResult res{};
     std::string msg;
     int rc = pressure_project(x->c, a, x->pr, x->sweep, x->pmail, x->stream, &res, &msg);
@@ -674,7 +676,8 @@ int flip_destroy(flip_ctx *x) {
     if (!x) return FLIP_E_NULL;
     cudaStreamSynchronize(x->stream);
     for (int q = 0; q < 2; q++)   // the graphs refer to the timing events: first
-        if (x->pr.batchGraph[q]) cudaGraphExecDestroy(x->pr.batchGraph[q]);
+        for (int o = 0; o < 2; o++)
+            if (x->pr.batchGraph[q][o]) cudaGraphExecDestroy(x->pr.batchGraph[q][o]);
     for (int q = 0; q <= FLIP_NUM_STAGES; q++)
         if (x->ev[q]) cudaEventDestroy(x->ev[q]);
     for (int q = 0; q < 2 * (PCG_BATCH + 1); q++)
@@ -896,6 +899,19 @@ int flip_set_stage_timing(flip_ctx *x, int enable) {
     x->sweepTiming.ms = 0.0;
     x->sweepTiming.launches = 0;
     x->sweepTiming.cellSweeps = 0;
+    return FLIP_OK;
+}
+
+int flip_set_sweep_orientation(flip_ctx *x, int mode) {
+    if (!x) return FLIP_E_NULL;
+    if (mode < -1 || mode > 1) return FLIP_E_OUT_OF_RANGE;
+    x->sweepOrientation = mode;
+    return FLIP_OK;
+}
+
+int flip_get_sweep_orientation(flip_ctx *x, int *last) {
+    if (!x || !last) return FLIP_E_NULL;
+    *last = x->pr.sl.swap;
     return FLIP_OK;
 }
 

@@ -51,18 +51,34 @@ __global__ void k_flags(StepConsts c, const float *phi, uint8_t *fluid, int *flu
         fluidFlag[t] = f ? 1 : 0;
         lv = i + j + k;
     }
-    // warp-aggregated min/max/count of the system cells' levels
+    // warp-aggregated min/max/count of the system cells' levels, and their
+    // extent in j and k (for the sweep tile orientation)
     unsigned int m = __ballot_sync(0xffffffffu, f);
     if (!m) return;
+    int jk[4] = {0x7fffffff, -1, 0x7fffffff, -1};
+    if (f) {
+        int i, j, k;
+        unflatten(t, c.I, c.J, i, j, k);
+        jk[0] = jk[1] = j;
+        jk[2] = jk[3] = k;
+    }
     int lo = f ? lv : 0x7fffffff, hi = f ? lv : -1;
     for (int o = 16; o > 0; o >>= 1) {
         lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, o));
         hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+        jk[0] = min(jk[0], __shfl_xor_sync(0xffffffffu, jk[0], o));
+        jk[1] = max(jk[1], __shfl_xor_sync(0xffffffffu, jk[1], o));
+        jk[2] = min(jk[2], __shfl_xor_sync(0xffffffffu, jk[2], o));
+        jk[3] = max(jk[3], __shfl_xor_sync(0xffffffffu, jk[3], o));
     }
     if ((threadIdx.x & 31) == 0) {
         atomicMin(&levelRange[0], lo);
         atomicMax(&levelRange[1], hi);
         atomicAdd(&levelRange[2], __popc(m));
+        atomicMin(&levelRange[3], jk[0]);
+        atomicMax(&levelRange[4], jk[1]);
+        atomicMin(&levelRange[5], jk[2]);
+        atomicMax(&levelRange[6], jk[3]);
     }
 }
 
@@ -546,15 +562,13 @@ int pressure_project(const StepConsts &c, const PressureArgs &a, PressureBuffers
         return e != cudaSuccess ? e : cudaGetLastError();
     };
 
-    int lr[3] = {0x7fffffff, -1, 0};
-    PCK(cudaMemcpyAsync(pb.levelRange, lr, sizeof(lr), cudaMemcpyHostToDevice, s));
+    static const int lr[8] = {0x7fffffff, -1, 0, 0x7fffffff, -1, 0x7fffffff, -1, 0};
+    std::memcpy(mail->levelRange, lr, sizeof(lr));
+    PCK(cudaMemcpyAsync(pb.levelRange, mail->levelRange, sizeof(lr), cudaMemcpyHostToDevice, s));
     PCK(cudaMemsetAsync(pb.scal, 0, 8 * sizeof(double), s));
     { FLIP_COUNT(1); k_flags<<<nb, TPB, 0, s>>>(c, a.phi, pb.fluid, pb.fluidFlag, pb.levelRange); }
-    // the rows as a list in cell order (a scan keeps it deterministic)
-    launch_scan_cells(pb.fluidFlag, (int)n, pb.fluidPos, pb.fluidScan, pb.nFluid, s);
-    { FLIP_COUNT(1); k_compact_rows<<<nb, TPB, 0, s>>>(c, pb.sl, pb.fluid, pb.fluidPos, pb.fluidIdx, pb.fluidSk); }
     { FLIP_COUNT(1); k_build<<<nb, TPB, 0, s>>>(c, a.phi, a.wu, a.wv, a.ww, a.u, a.v, a.w, mf, pb); }
-    PCK(cudaMemcpyAsync(mail->levelRange, pb.levelRange, 3 * sizeof(int), cudaMemcpyDeviceToHost, s));
+    PCK(cudaMemcpyAsync(mail->levelRange, pb.levelRange, 7 * sizeof(int), cudaMemcpyDeviceToHost, s));
     PCK(cudaMemcpyAsync(&mail->bmax, pb.scal + 2, sizeof(double), cudaMemcpyDeviceToHost, s));
     PCK(sync());
     if (a.dumpRhs) PCK(cudaMemcpy(a.dumpRhs, pb.b, n * sizeof(double), cudaMemcpyDeviceToHost));
@@ -570,6 +584,30 @@ int pressure_project(const StepConsts &c, const PressureArgs &a, PressureBuffers
         if (errMsg) *errMsg = "sweep exchange array smaller than the grid needs";
         return FLIP_E_RUNTIME;
     }
+    // Sweep tile orientation for this solve: the one whose tiles the rows'
+    // extent crosses with the shorter chain of hops.  A hop across the lane
+    // axis delays the next tile by about TJ + chunk + handoff steps, across
+    // the warp axis by about TK + chunk + handoff.
+    {
+        const int jlo = mail->levelRange[3], jhi = mail->levelRange[4];
+        const int klo = mail->levelRange[5], khi = mail->levelRange[6];
+        auto hops = [](int lo_, int hi_, int w) { return (hi_ - 1) / w - (lo_ - 1) / w; };
+        const int lagA = SWEEP_TJ + 8 + 14, lagB = SWEEP_TK + 8 + 14;
+        const long long cost0 = (long long)hops(jlo, jhi, SWEEP_TJ) * lagA + (long long)hops(klo, khi, SWEEP_TK) * lagB;
+        const long long cost1 = (long long)hops(klo, khi, SWEEP_TJ) * lagA + (long long)hops(jlo, jhi, SWEEP_TK) * lagB;
+        int want = cost1 < cost0 ? 1 : (cost0 < cost1 ? 0 : pb.sl.swap);
+        if (a.sweepOrientation == 0 || a.sweepOrientation == 1) want = a.sweepOrientation;
+        if (want != pb.sl.swap) {
+            pb.sl = sweep_layout(c.I, c.J, c.K, want);
+            // entries that hold no interior cell in the new orientation must read zero
+            PCK(cudaMemsetAsync(pb.L, 0, pb.nsl * sizeof(float4), s));
+            PCK(cudaMemsetAsync(pb.rf, 0, pb.nsl * sizeof(float), s));
+            PCK(cudaMemsetAsync(pb.z, 0, pb.nsl * sizeof(float), s));
+        }
+    }
+    // the rows as a list in cell order (a scan keeps it deterministic)
+    launch_scan_cells(pb.fluidFlag, (int)n, pb.fluidPos, pb.fluidScan, pb.nFluid, s);
+    { FLIP_COUNT(1); k_compact_rows<<<nb, TPB, 0, s>>>(c, pb.sl, pb.fluid, pb.fluidPos, pb.fluidIdx, pb.fluidSk); }
 
     // MIC(0) factor, wavefront by wavefront: one cooperative launch over all
     // levels where the device allows it, else one launch per level
@@ -599,7 +637,7 @@ int pressure_project(const StepConsts &c, const PressureArgs &a, PressureBuffers
         k_mic0_level<<<div_up(np, TPB), TPB, 0, s>>>(c, pb.fluid, pb.Ad, pb.invdiagD, lv);
     }
     { FLIP_COUNT(1); k_mic0_finalize<<<nb, TPB, 0, s>>>(c, pb.sl, pb.fluid, pb.Ad, pb.invdiagD, pb.L); }
-    launch_sweep_ranges(c, pb.fluid, sw, s);
+    launch_sweep_ranges(c, pb.sl, pb.fluid, sw, s);
 
     unsigned long long *rmax = pb.rmaxBits;
     SweepTiming *tm = a.sweepTiming;
@@ -624,7 +662,7 @@ int pressure_project(const StepConsts &c, const PressureArgs &a, PressureBuffers
     // event pair q (recorded as graph nodes when captured)
     auto precondition = [&](int q, bool timed) {
         if (timed) record(tm->ev[2 * q]);
-        launch_sweeps(c, pb.L, pb.rf, pb.z, sw, &pb.ctl->done, s);
+        launch_sweeps(c, pb.sl, pb.L, pb.rf, pb.z, sw, &pb.ctl->done, s);
         if (timed) record(tm->ev[2 * q + 1]);
         { FLIP_COUNT(1); k_dot_zr<<<rb, TPB, 0, s>>>(pb.fluidIdx, pb.fluidSk, pb.nFluid, pb.z, pb.r, pb.partials, pb.ctl); }
         { FLIP_COUNT(1); k_sum_partials<<<1, 1024, 0, s>>>(pb.partials, pb.nPartials, pb.scal, 1, pb.ctl, rmax); }
@@ -666,11 +704,11 @@ int pressure_project(const StepConsts &c, const PressureArgs &a, PressureBuffers
         // (captured on first use, per context): the convergence test runs
         // there and the kernels of iterations after convergence return at
         // once.  The host reads the outcome once per batch.
-        const int gi = tm ? 1 : 0;
+        const int gi = tm ? 1 : 0, go = pb.sl.swap;
         for (int it0 = 0; it0 < a.maxIter;) {
             const int nit = std::min(PCG_BATCH, a.maxIter - it0);
             sweep_epoch_guard(c, sw, 2LL * nit, s);
-            if (nit == PCG_BATCH && !pb.batchGraph[gi] && !pb.noGraphs) {
+            if (nit == PCG_BATCH && !pb.batchGraph[gi][go] && !pb.noGraphs) {
                 long long &counter = launch_counter();
                 const long long before = counter;
                 const unsigned int epochBefore = sw.epoch;
@@ -683,17 +721,17 @@ int pressure_project(const StepConsts &c, const PressureArgs &a, PressureBuffers
                     for (int k = 0; k < PCG_BATCH; k++) iteration(k, tm != nullptr);
                     capturing = false;
                     PCK(cudaStreamEndCapture(s, &graph));
-                    cudaError_t e = cudaGraphInstantiate(&pb.batchGraph[gi], graph, 0);
+                    cudaError_t e = cudaGraphInstantiate(&pb.batchGraph[gi][go], graph, 0);
                     cudaGraphDestroy(graph);
                     PCK(e);
-                    pb.batchKernels[gi] = counter - before;
+                    pb.batchKernels[gi][go] = counter - before;
                     counter = before;   // counted when replayed
                     sw.epoch = epochBefore;
                 }
             }
-            if (nit == PCG_BATCH && pb.batchGraph[gi]) {
-                PCK(cudaGraphLaunch(pb.batchGraph[gi], s));
-                launch_counter() += pb.batchKernels[gi];
+            if (nit == PCG_BATCH && pb.batchGraph[gi][go]) {
+                PCK(cudaGraphLaunch(pb.batchGraph[gi][go], s));
+                launch_counter() += pb.batchKernels[gi][go];
                 sw.epoch += 2 * PCG_BATCH;
             } else {
                 for (int k = 0; k < nit; k++) iteration(k, tm != nullptr);

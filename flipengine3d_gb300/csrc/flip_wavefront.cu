@@ -61,7 +61,7 @@ struct SweepArgs {
     const float4 *L;               // factor rows, sweep layout
     const float *rin;              // right-hand side, sweep layout (backward: the forward result)
     float *out;                    // result, sweep layout (backward: in place over the forward result)
-    int J, K, NI, T;
+    int J, K, NI, T;               // J, K: grid extents along the tile's lane and warp axes
     int ntj, ntk;
     const int2 *range;             // per tile: first/last step (forward numbering) holding a system cell
     unsigned long long *xchg;      // per tile: T x TK j-edge words, then T x TJ k-edge words
@@ -146,7 +146,10 @@ __device__ __forceinline__ bool compute_sync_or(bool v) {
 }
 __device__ __forceinline__ void compute_sync() { asm volatile("bar.sync 1, %0;" ::"n"(NCOMP) : "memory"); }
 
-template <bool FWD>
+// SWAP: the tile's lanes run along k and its warps along j (else lanes along
+// j, warps along k).  The couplings that travel along each axis and the
+// order of the subtractions follow: forward -z, -y, -x; backward +x, +y, +z.
+template <bool FWD, bool SWAP>
 __global__ void __launch_bounds__(NTHREADS, 1) k_wavefront(SweepArgs a) {
     extern __shared__ __align__(128) unsigned char smemRaw[];
     SweepSmem &sm = *reinterpret_cast<SweepSmem *>(smemRaw);
@@ -337,26 +340,28 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_wavefront(SweepArgs a) {
             const bool valid = t >= v0 && t <= v1;
             float res;
             if (FWD) {
-                float pJ = __shfl_up_sync(0xffffffffu, pz, 1);
-                if (l == 0) pJ = sl.eJ[s][w];
-                const float pK = w > 0 ? sm.p[pb][w - 1][l] : sl.eK[s][l];
-                float acc = __fsub_rn(rr, pK);
-                acc = __fsub_rn(acc, pJ);
-                acc = __fsub_rn(acc, px);
+                // terms from the lane and warp neighbours: L of the neighbour
+                // towards this cell times its y (y-axis coupling L.z, z-axis L.w)
+                float pL = __shfl_up_sync(0xffffffffu, pz, 1);
+                if (l == 0) pL = sl.eJ[s][w];
+                const float pW = w > 0 ? sm.p[pb][w - 1][l] : sl.eK[s][l];
+                float acc = __fsub_rn(rr, SWAP ? pL : pW);   // -z
+                acc = __fsub_rn(acc, SWAP ? pW : pL);        // -y
+                acc = __fsub_rn(acc, px);                    // -x
                 res = __fmul_rn(acc, Lc.x);
                 px = __fmul_rn(Lc.y, res);
-                pz = __fmul_rn(Lc.z, res);
-                const float pw = __fmul_rn(Lc.w, res);
+                pz = __fmul_rn(SWAP ? Lc.w : Lc.z, res);     // for the next lane
+                const float pw = __fmul_rn(SWAP ? Lc.z : Lc.w, res);   // for the next warp
                 sm.p[cb][w][l] = pw;
                 if (valid && pubJ) st_word(pubJw + (size_t)t * TK, pack(ep, pz));
                 if (valid && pubK) st_word(pubKw + (size_t)t * TJ, pack(ep, pw));
             } else {
-                float zJ = __shfl_down_sync(0xffffffffu, zPrev, 1);
-                if (l == TJ - 1) zJ = sl.eJ[s][w];
-                const float zK = w < TK - 1 ? sm.p[pb][w + 1][l] : sl.eK[s][l];
-                float acc = __fsub_rn(rr, __fmul_rn(Lc.y, zPrev));
-                acc = __fsub_rn(acc, __fmul_rn(Lc.z, zJ));
-                acc = __fsub_rn(acc, __fmul_rn(Lc.w, zK));
+                float zL = __shfl_down_sync(0xffffffffu, zPrev, 1);
+                if (l == TJ - 1) zL = sl.eJ[s][w];
+                const float zW = w < TK - 1 ? sm.p[pb][w + 1][l] : sl.eK[s][l];
+                float acc = __fsub_rn(rr, __fmul_rn(Lc.y, zPrev));          // +x
+                acc = __fsub_rn(acc, __fmul_rn(Lc.z, SWAP ? zW : zL));      // +y
+                acc = __fsub_rn(acc, __fmul_rn(Lc.w, SWAP ? zL : zW));      // +z
                 res = __fmul_rn(acc, Lc.x);
                 zPrev = res;
                 sm.p[cb][w][l] = res;
@@ -387,15 +392,16 @@ __global__ void k_tile_range_init(int2 *range, int n) {
 
 // First and last forward step at which a tile meets a system cell
 // (lanes of a warp that fall into the same tile reduce before the atomics).
-__global__ void k_tile_range(const uint8_t *fluid, int I, int J, int K, int ntj, int2 *range) {
+__global__ void k_tile_range(const uint8_t *fluid, int I, int J, int K, SweepLayout g, int2 *range) {
     long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     bool f = t < (long long)I * J * K && fluid[t];
     int tile = -1, step = 0;
     if (f) {
         int i, j, k;
         unflatten(t, I, J, i, j, k);
-        tile = (j - 1) / TJ + ntj * ((k - 1) / TK);
-        step = (i - 1) + (j - 1) % TJ + (k - 1) % TK;
+        const int aa = (g.swap ? k : j) - 1, bb = (g.swap ? j : k) - 1;
+        tile = aa / TJ + g.ntj * (bb / TK);
+        step = (i - 1) + aa % TJ + bb % TK;
     }
     unsigned int grp = __match_any_sync(0xffffffffu, tile);
     int mn = __reduce_min_sync(grp, f ? step : 0x7fffffff);
@@ -408,50 +414,57 @@ __global__ void k_tile_range(const uint8_t *fluid, int I, int J, int K, int ntj,
 
 }  // namespace
 
-int sweep_tiles(int J, int K, int *ntj, int *ntk) {
-    *ntj = (J - 2 + TJ - 1) / TJ;
-    *ntk = (K - 2 + TK - 1) / TK;
-    return *ntj * *ntk;
+int sweep_tiles_max(int I, int J, int K) {
+    int best = 0;
+    for (int sw = 0; sw < 2; sw++) {
+        const SweepLayout g = sweep_layout(I, J, K, sw);
+        best = std::max(best, g.ntj * g.ntk);
+    }
+    return best;
 }
+
 // per tile: TK j-edge words and TJ k-edge words for each of its T steps
 long long sweep_exchange_words(int I, int J, int K) {
     const SweepLayout g = sweep_layout(I, J, K);
-    return (long long)g.ntj * g.ntk * (TJ + TK) * g.T;
+    return (long long)sweep_tiles_max(I, J, K) * (TJ + TK) * g.T;
 }
 
-void launch_sweep_ranges(const StepConsts &c, const uint8_t *fluid, SweepState &sw, cudaStream_t s) {
-    int ntj, ntk;
-    int n = sweep_tiles(c.J, c.K, &ntj, &ntk);
+void launch_sweep_ranges(const StepConsts &c, const SweepLayout &g, const uint8_t *fluid, SweepState &sw,
+                         cudaStream_t s) {
+    const int n = g.ntj * g.ntk;
     { FLIP_COUNT(1); k_tile_range_init<<<div_up(n, 256), 256, 0, s>>>(sw.range, n); }
     long long nc = (long long)c.I * c.J * c.K;
-    { FLIP_COUNT(1); k_tile_range<<<div_up(nc, 256), 256, 0, s>>>(fluid, c.I, c.J, c.K, ntj, sw.range); }
+    { FLIP_COUNT(1); k_tile_range<<<div_up(nc, 256), 256, 0, s>>>(fluid, c.I, c.J, c.K, g, sw.range); }
 }
 
-void launch_sweeps(const StepConsts &c, const float4 *L, const float *rf, float *z, SweepState &sw, const int *skip,
-                   cudaStream_t s) {
-    const SweepLayout g = sweep_layout(c.I, c.J, c.K);
+void launch_sweeps(const StepConsts &c, const SweepLayout &g, const float4 *L, const float *rf, float *z,
+                   SweepState &sw, const int *skip, cudaStream_t s) {
     const int n = g.ntj * g.ntk;
     static std::atomic<unsigned long long> smemSet{0};   // devices on which the slots' shared memory is opted in
     int dev = 0;
     cudaGetDevice(&dev);
     if (dev < 64 && !((smemSet.load() >> dev) & 1ull)) {   // idempotent, so a race only repeats it
-        cudaFuncSetAttribute(k_wavefront<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SweepSmem));
-        cudaFuncSetAttribute(k_wavefront<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SweepSmem));
+        cudaFuncSetAttribute(k_wavefront<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SweepSmem));
+        cudaFuncSetAttribute(k_wavefront<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SweepSmem));
+        cudaFuncSetAttribute(k_wavefront<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SweepSmem));
+        cudaFuncSetAttribute(k_wavefront<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SweepSmem));
         smemSet.fetch_or(1ull << dev);
     }
     SweepArgs a;
     a.L = L;
-    a.J = c.J; a.K = c.K; a.NI = c.I - 2; a.T = g.T;
+    a.J = g.EA; a.K = g.EB; a.NI = c.I - 2; a.T = g.T;   // extents along the lane and warp axes
     a.ntj = g.ntj; a.ntk = g.ntk;
     a.range = sw.range; a.xchg = sw.xchg; a.ticket = sw.ticket; a.err = sw.err; a.skip = skip;
     // forward: y from r
     a.rin = rf; a.out = z;
     { FLIP_COUNT(1); k_sweep_prep<<<1, 1, 0, s>>>(sw.ticket); }
-    { FLIP_COUNT(1); k_wavefront<true><<<n, NTHREADS, sizeof(SweepSmem), s>>>(a); }
+    if (g.swap) { FLIP_COUNT(1); k_wavefront<true, true><<<n, NTHREADS, sizeof(SweepSmem), s>>>(a); }
+    else { FLIP_COUNT(1); k_wavefront<true, false><<<n, NTHREADS, sizeof(SweepSmem), s>>>(a); }
     // backward: z from y, in place
     a.rin = z; a.out = z;
     { FLIP_COUNT(1); k_sweep_prep<<<1, 1, 0, s>>>(sw.ticket); }
-    { FLIP_COUNT(1); k_wavefront<false><<<n, NTHREADS, sizeof(SweepSmem), s>>>(a); }
+    if (g.swap) { FLIP_COUNT(1); k_wavefront<false, true><<<n, NTHREADS, sizeof(SweepSmem), s>>>(a); }
+    else { FLIP_COUNT(1); k_wavefront<false, false><<<n, NTHREADS, sizeof(SweepSmem), s>>>(a); }
     sw.epoch += 2;
 }
 

@@ -87,6 +87,8 @@ SIGNATURES = {
     "flip_get_stage_times": [_P, _P, C.POINTER(C.c_longlong)],
     "flip_get_launch_count": [_P, C.POINTER(C.c_longlong)],
     "flip_get_sweep_times": [_P, C.POINTER(C.c_double), C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)],
+    "flip_set_sweep_orientation": [_P, _I],
+    "flip_get_sweep_orientation": [_P, C.POINTER(C.c_int)],
     "flip_order_particles_by_id_noalloc": [_P, _P, _P, _P, _I, _I, _P, _P],
     "flip_get_device_bytes": [_P, C.POINTER(C.c_longlong)],
     "flip_estimate_device_bytes": [_I, _I, _I, _I, C.POINTER(C.c_longlong)],
@@ -403,6 +405,17 @@ class FluidSimulation:
         cells = C.c_longlong()
         self._c(self._lib.flip_get_sweep_times(self._h, C.byref(ms), C.byref(n), C.byref(cells)))
         return ms.value, n.value, cells.value
+
+    def set_sweep_orientation(self, mode: int):
+        """Preconditioner sweep tile orientation: -1 chosen per solve (the
+        default), 0 lanes along j, 1 lanes along k.  Results are the same."""
+        self._c(self._lib.flip_set_sweep_orientation(self._h, int(mode)))
+
+    def sweep_orientation(self) -> int:
+        """Orientation used by the last pressure solve."""
+        v = C.c_int()
+        self._c(self._lib.flip_get_sweep_orientation(self._h, C.byref(v)))
+        return v.value
 
     def device_bytes(self) -> int:
         b = C.c_longlong()

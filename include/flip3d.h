@@ -177,6 +177,14 @@ int flip_get_stage_times(flip_ctx *ctx, double *ms, long long *substeps);
  * pressure rows each swept. */
 int flip_get_sweep_times(flip_ctx *ctx, double *ms, long long *launches, long long *cell_sweeps);
 
+/* Orientation of the preconditioner sweep tiles: -1 (the default) picks it
+ * per solve from the extent of the pressure rows, 0 runs the tile lanes along
+ * j, 1 along k.  Results do not depend on it: both keep the reference's
+ * order of operations.  flip_get_sweep_orientation reports the orientation
+ * of the last solve.  No counterpart in the reference. */
+int flip_set_sweep_orientation(flip_ctx *ctx, int mode);
+int flip_get_sweep_orientation(flip_ctx *ctx, int *last);
+
 /* Number of this library's kernel launches issued so far on the context. */
 int flip_get_launch_count(flip_ctx *ctx, long long *count);
 

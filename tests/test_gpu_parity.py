@@ -54,6 +54,8 @@ def test_first_frame_matches_reference_golden(gpu, case):
     dict(n=32, seed=1),
     dict(n=40, seed=2, sphere=True),
     dict(n=27, jsize=35, ksize=22, dx=1 / 27, seed=3, fill=(0.6, 0.5, 0.9)),
+    # shallow and long in z: the sweep tiles run their lanes along k
+    dict(n=24, jsize=20, ksize=70, dx=1 / 24, seed=6, fill=(0.6, 0.25, 2.5)),
 ])
 def test_first_frame_matches_oracle(gpu, kw):
     sc = dam_break(**kw)
@@ -95,3 +97,27 @@ def test_substepped_frame_matches_oracle(gpu):
         rpos, _ = orc.particles()
         assert pos.shape == rpos.shape
         assert rel_err(pos, rpos) <= RTOL_MULTI
+
+
+def test_sweep_orientation_does_not_change_results(gpu):
+    """The preconditioner sweep tiles run their lanes along j or along k.
+    Both keep the reference's order of operations (pcgsolver.h:192-221), so
+    frames are bit-identical whichever runs."""
+    sc = dam_break(40, jsize=48, ksize=72, seed=5, sphere=True, fill=(0.5, 0.3, 1.6))
+    out = {}
+    for mode in (0, 1, -1):
+        with FluidSimulation.from_scene(sc, tolerance=1e-9) as sim:
+            sim.set_sweep_orientation(mode)
+            for _ in range(2):
+                sim.update(sc.frame_dt)
+            if mode >= 0:
+                assert sim.sweep_orientation() == mode
+            out[mode] = (sim.getMarkerParticlePositionData(), sim.getMarkerParticleVelocityData(),
+                         sim.getFrameStatsData().pressure_iterations)
+    for mode in (1, -1):
+        assert np.array_equal(out[mode][0], out[0][0]), f"orientation {mode}: positions"
+        assert np.array_equal(out[mode][1], out[0][1]), f"orientation {mode}: velocities"
+        assert out[mode][2] == out[0][2]
+    with FluidSimulation(8, 8, 8, 1 / 8) as sim:
+        with pytest.raises(IndexError):
+            sim.set_sweep_orientation(2)
