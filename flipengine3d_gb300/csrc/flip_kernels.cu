@@ -202,6 +202,7 @@ __global__ void k_gather(ParticleSoA src, ParticleSoA dst, const int *start, con
 // squared distance per cell and each cell takes one square root at the end.
 // Then the solid post-process (particlelevelset.cpp:172-196).
 constexpr int BW = 10;
+static_assert(BW <= 15, "the SDF kernel packs block-local cell coordinates in 4 bits");
 
 // Does the reference's count pass put particle p in block (bx,by,bz)'s list?
 // (particlelevelset.cpp:477-532, velocityadvector.cpp:272-329)
@@ -223,10 +224,17 @@ __device__ __forceinline__ bool in_block_list(float px, float py, float pz, floa
     return bx >= i0 && bx <= i1 && by >= j0 && by <= j1 && bz >= k0 && bz <= k1;
 }
 
-__global__ void __launch_bounds__(TPB) k_liquid_sdf(ParticleSoA p, const int *cellStart, StepConsts c,
-                                                    const uint8_t *solidCC, float *phi) {
+// 16 warps per 10^3 block: the block's ~200 rows of candidate particles
+// then take about 6 passes per warp, where 8 warps leave the blocks of a
+// small scene (one wave of CTAs) bound by the latency of their atomics.
+#ifndef SDF_TPB
+#define SDF_TPB 512
+#endif
+__global__ void __launch_bounds__(SDF_TPB) k_liquid_sdf(ParticleSoA p, const int *cellStart, StepConsts c,
+                                                        const uint8_t *solidCC, float *phi) {
     __shared__ unsigned int smin[BW * BW * BW];   // bits of the smallest squared distance (>= 0)
     __shared__ float centre[BW];
+    __shared__ float4 recs[SDF_TPB / 32][32];     // per warp: a pass's particles {lx, ly, lz, box}
     const int bx = blockIdx.x, by = blockIdx.y, bz = blockIdx.z;
     const double dx = c.dx;
     const float maxd = (float)(3.0 * dx);
@@ -239,7 +247,6 @@ __global__ void __launch_bounds__(TPB) k_liquid_sdf(ParticleSoA p, const int *ce
     const float blockdxf = (float)(BW * dx);
     const double invBlock = 1.0 / (double)blockdxf;
     const float invBlockf = (float)invBlock;
-    const double blockdxD = (double)BW * dx;
     const float offx = c.blockPos[bx + 1], offy = c.blockPos[by + 1],
                 offz = c.blockPos[bz + 1];
     Dims cells{c.I, c.J, c.K};
@@ -247,48 +254,86 @@ __global__ void __launch_bounds__(TPB) k_liquid_sdf(ParticleSoA p, const int *ce
     int y0 = max(by * BW - 2, 0), y1 = min(by * BW + BW + 1, c.J - 1);
     int z0 = max(bz * BW - 2, 0), z1 = min(bz * BW + BW + 1, c.K - 1);
     int ny = y1 - y0 + 1, nrows = ny * (z1 - z0 + 1);
-    // A warp takes two rows of cells along x, 16 lanes each; a lane takes a
-    // contiguous run of its row's particles, so about one lane per cell.
-    // Lanes in step then sit in different cells (or rows), and their
-    // shared-memory atomics rarely meet on one cell, whereas the particles
-    // of one cell share their whole box.
+    // A warp takes one row of cells along x at a time and its candidate
+    // particles 32 at a time.  Phase 1, a lane per particle: is it in this
+    // block's list, and which of the block's cells does its box cover.  Phase
+    // 2, a lane per (particle, column of the box along z): the warp's lanes
+    // are spread evenly over all columns of the pass's particles (a prefix
+    // sum of the column counts and a binary search), and each lane walks its
+    // column.  Lanes of one step are in distinct columns of one particle, or
+    // of different particles.
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
-    const int sel = lane >> 4, hl = lane & 15;
-    for (int pair = warp; 2 * pair < nrows; pair += nwarps) {
-        const int row = 2 * pair + sel;
-        int pb = 0, pe = 0;
-        if (row < nrows) {
-            const int cy = y0 + row % ny, cz = z0 + row / ny;
-            pb = cellStart[cells.idx(x0, cy, cz)];
-            pe = cellStart[cells.idx(x1, cy, cz) + 1];
-        }
-        const int run = (pe - pb + 15) >> 4;   // particles per lane in this row
-        const int rounds = max(run, __shfl_xor_sync(0xffffffffu, run, 16));
-        for (int r = 0; r < rounds; r++) {
-            const int t = pb + hl * run + r;
-            if (r >= run || t >= pe) continue;
-            float px = p.px[t], py = p.py[t], pz = p.pz[t];
-            if (!in_block_list(px, py, pz, sr, blockdxf, invBlock, invBlockf, c.blockPosF, bx, by, bz)) continue;
-            float lx = __fsub_rn(px, offx), ly = __fsub_rn(py, offy), lz = __fsub_rn(pz, offz);
-            int a0 = max(exact_floor(__fsub_rn(lx, sr), c.invdx, c.invdxf), 0);
-            int b0 = max(exact_floor(__fsub_rn(ly, sr), c.invdx, c.invdxf), 0);
-            int c0 = max(exact_floor(__fsub_rn(lz, sr), c.invdx, c.invdxf), 0);
-            int a1 = min(exact_floor(__fadd_rn(lx, sr), c.invdx, c.invdxf), BW - 1);
-            int b1 = min(exact_floor(__fadd_rn(ly, sr), c.invdx, c.invdxf), BW - 1);
-            int c1 = min(exact_floor(__fadd_rn(lz, sr), c.invdx, c.invdxf), BW - 1);
-            for (int cc = c0; cc <= c1; cc++) {
-                const float dz = __fsub_rn(centre[cc], lz);
-                const float dz2 = __fmul_rn(dz, dz);
-                for (int bb = b0; bb <= b1; bb++) {
-                    const float dy = __fsub_rn(centre[bb], ly);
-                    const float dy2 = __fmul_rn(dy, dy);
-                    for (int aa = a0; aa <= a1; aa++) {
-                        const float ddx = __fsub_rn(centre[aa], lx);
-                        const float d2 = __fadd_rn(__fadd_rn(__fmul_rn(ddx, ddx), dy2), dz2);
-                        atomicMin(&smin[aa + BW * (bb + BW * cc)], __float_as_uint(d2));
+    float4 *wrec = recs[warp];
+    // col / n = (col * ceil(2^11 / n)) >> 11, exact for n <= BW and col < n * BW;
+    // lane n holds the multiplier
+    const int divLane = lane > 0 ? (2048 + lane - 1) / lane : 0;
+    for (int row = warp; row < nrows; row += nwarps) {
+        const int cy = y0 + row % ny, cz = z0 + row / ny;
+        const int pb = cellStart[cells.idx(x0, cy, cz)];
+        const int pe = cellStart[cells.idx(x1, cy, cz) + 1];
+        for (int base = pb; base < pe; base += 32) {
+            const int t = base + lane;
+            int ncol = 0, na = 0;
+            float4 rec;
+            unsigned box = 0;
+            if (t < pe) {
+                const float px = p.px[t], py = p.py[t], pz = p.pz[t];
+                if (in_block_list(px, py, pz, sr, blockdxf, invBlock, invBlockf, c.blockPosF, bx, by, bz)) {
+                    const float lx = __fsub_rn(px, offx), ly = __fsub_rn(py, offy), lz = __fsub_rn(pz, offz);
+                    const int a0 = max(exact_floor(__fsub_rn(lx, sr), c.invdx, c.invdxf), 0);
+                    const int b0 = max(exact_floor(__fsub_rn(ly, sr), c.invdx, c.invdxf), 0);
+                    const int c0 = max(exact_floor(__fsub_rn(lz, sr), c.invdx, c.invdxf), 0);
+                    const int a1 = min(exact_floor(__fadd_rn(lx, sr), c.invdx, c.invdxf), BW - 1);
+                    const int b1 = min(exact_floor(__fadd_rn(ly, sr), c.invdx, c.invdxf), BW - 1);
+                    const int c1 = min(exact_floor(__fadd_rn(lz, sr), c.invdx, c.invdxf), BW - 1);
+                    if (a1 >= a0 && b1 >= b0 && c1 >= c0) {
+                        na = a1 - a0 + 1;
+                        ncol = na * (b1 - b0 + 1);
+                        box = (unsigned)a0 | (unsigned)na << 4 | (unsigned)b0 << 8 | (unsigned)c0 << 12 |
+                              (unsigned)c1 << 16;
+                        rec = make_float4(lx, ly, lz, 0.0f);
                     }
                 }
             }
+            const unsigned div = (unsigned)__shfl_sync(0xffffffffu, divLane, na);
+            if (ncol > 0) {
+                rec.w = __uint_as_float(box | div << 20);
+                wrec[lane] = rec;
+            }
+            int incl = ncol;   // inclusive prefix sum of the column counts over the lanes
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int v = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += v;
+            }
+            const int total = __shfl_sync(0xffffffffu, incl, 31);
+            __syncwarp();
+            for (int first = 0; first < total; first += 32) {
+                const int item = first + lane;
+                int L = 0;   // the smallest lane whose inclusive sum exceeds item
+#pragma unroll
+                for (int step = 16; step > 0; step >>= 1)
+                    if (__shfl_sync(0xffffffffu, incl, L + step - 1) <= item) L += step;
+                const int startL = __shfl_sync(0xffffffffu, incl, L) - __shfl_sync(0xffffffffu, ncol, L);
+                if (item < total) {
+                    const float4 pr = wrec[L];
+                    const unsigned w = __float_as_uint(pr.w);
+                    const int a0 = w & 15, na = (w >> 4) & 15, b0 = (w >> 8) & 15;
+                    const int c0 = (w >> 12) & 15, c1 = (w >> 16) & 15;
+                    const int col = item - startL;
+                    const int bq = (col * (int)(w >> 20)) >> 11;   // col / na
+                    const int aa = a0 + col - bq * na, bb = b0 + bq;
+                    const float ddx = __fsub_rn(centre[aa], pr.x);
+                    const float dy = __fsub_rn(centre[bb], pr.y);
+                    const float dxy = __fadd_rn(__fmul_rn(ddx, ddx), __fmul_rn(dy, dy));
+                    unsigned int *dst = &smin[aa + BW * (bb + BW * c0)];
+                    for (int cc = c0; cc <= c1; cc++, dst += BW * BW) {
+                        const float dz = __fsub_rn(centre[cc], pr.z);
+                        atomicMin(dst, __float_as_uint(__fadd_rn(dxy, __fmul_rn(dz, dz))));
+                    }
+                }
+            }
+            __syncwarp();
         }
     }
     __syncthreads();
@@ -735,7 +780,7 @@ void launch_gather_particles(const ParticleSoA &src, ParticleSoA dst, const int 
 void launch_liquid_sdf(const ParticleSoA &p, const int *cellStart, const StepConsts &c, const uint8_t *solidCC,
                        float *phi, cudaStream_t s) {
     dim3 grid(div_up(c.I, BW), div_up(c.J, BW), div_up(c.K, BW));
-    { FLIP_COUNT(1); k_liquid_sdf<<<grid, TPB, 0, s>>>(p, cellStart, c, solidCC, phi); }
+    { FLIP_COUNT(1); k_liquid_sdf<<<grid, SDF_TPB, 0, s>>>(p, cellStart, c, solidCC, phi); }
 }
 void launch_p2g(const ParticleSoA &p, const int *cellStart, const StepConsts &c, float *u, float *v, float *w,
                 uint8_t *vu, uint8_t *vv, uint8_t *vw, cudaStream_t s) {

@@ -261,11 +261,40 @@ __device__ __forceinline__ T block_sum(T v, T *sh) {
 }
 
 
-// The reductions below run on a fixed grid of RBLOCKS CTAs with grid-stride
-// loops: each thread sums its cells in a fixed order, each CTA writes one
-// partial, and k_sum_partials adds the partials in a fixed order, so every
-// sum is deterministic and the FP64 reduction work is per thread, not per
-// cell.
+// Each CTA of a reduction takes a ticket once its partial (or atomic) is
+// out; the CTA that takes the last one then sees all of them and finishes the
+// reduction, and resets the ticket for the next launch.  One launch instead
+// of a producer and a one-CTA consumer.
+__device__ __forceinline__ bool last_cta(unsigned int *ticket) {
+    __shared__ int amLast;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        amLast = atomicAdd(ticket, 1u) == gridDim.x - 1;
+        if (amLast) {
+            *ticket = 0u;
+            __threadfence();
+        }
+    }
+    __syncthreads();
+    return amLast;
+}
+// Sum of the launch's block partials in a fixed order (deterministic);
+// thread 0 holds the result.
+__device__ __forceinline__ double sum_partials_fixed(const double *partials, int n, double *sh) {
+    double v = 0.0;
+    for (int q = threadIdx.x; q < n; q += blockDim.x) v += __ldcg(partials + q);
+    return block_sum(v, sh);
+}
+__device__ __forceinline__ double bits_to_resid(const unsigned long long *p) {
+    return __longlong_as_double((long long)__ldcg(p));
+}
+
+// The reductions below run on a fixed grid per context (nPartials CTAs,
+// pressure_partials_for) with grid-stride loops: each thread sums its rows
+// in a fixed order, each CTA writes one partial, and the last CTA adds the
+// partials in a fixed order, so every sum is deterministic and the FP64
+// reduction work is per thread, not per row.
 
 // the rows of the system as a list: flat index and sweep-layout index
 __global__ void k_compact_rows(StepConsts c, SweepLayout g, const uint8_t *fluid, const int *pos, int *idx, int *sk) {
@@ -278,9 +307,12 @@ __global__ void k_compact_rows(StepConsts c, SweepLayout g, const uint8_t *fluid
     sk[e] = (int)sweep_index(g, i, j, k);
 }
 
-// q = A s (FP64) over the rows, block partials of s.q
+// q = A s (FP64) over the rows and s.q; the last CTA sums s.q and sets
+// alpha = rho / s.q, rounded to float as BLAS::addScaled takes it
+// (blaswrapper.h:129-158), and clears the iteration's residual norms.
 __global__ void k_spmv(StepConsts c, const int *__restrict__ rows, const int *nRows, const double4 *__restrict__ Ad,
-                       const float *__restrict__ s, double *__restrict__ q, double *partials, const PcgCtl *ctl) {
+                       const float *__restrict__ s, double *__restrict__ q, double *partials, double *scal,
+                       unsigned long long *rmaxBits, PcgCtl *ctl) {
     __shared__ double sh[32];
     if (ctl->done) return;
     const int n = *nRows;
@@ -301,10 +333,23 @@ __global__ void k_spmv(StepConsts c, const int *__restrict__ rows, const int *nR
     }
     double b = block_sum(part, sh);
     if (threadIdx.x == 0) partials[blockIdx.x] = b;
+    if (last_cta(&ctl->ticket[0])) {
+        const double sq = sum_partials_fixed(partials, gridDim.x, sh);
+        if (threadIdx.x == 0) {
+            scal[0] = sq;
+            scal[4] = (double)(float)(scal[3] / sq);
+            rmaxBits[0] = 0ull;
+            rmaxBits[1] = 0ull;
+        }
+    }
 }
 
+// rho_new = z.r.  The last CTA sums it; inside the loop (inLoop) it also
+// sets beta = rho_new / rho as float (pcgsolver.h:295-298) and ends the
+// iteration: rho = rho_new, next iteration index.
 __global__ void k_dot_zr(const int *__restrict__ rows, const int *__restrict__ rowsSk, const int *nRows,
-                         const float *__restrict__ z, const double *__restrict__ r, double *partials, const PcgCtl *ctl) {
+                         const float *__restrict__ z, const double *__restrict__ r, double *partials, double *scal,
+                         PcgCtl *ctl, int inLoop) {
     __shared__ double sh[32];
     if (ctl->done) return;
     const int n = *nRows;
@@ -313,38 +358,44 @@ __global__ void k_dot_zr(const int *__restrict__ rows, const int *__restrict__ r
         part = fma((double)z[rowsSk[e]], r[rows[e]], part);
     double s = block_sum(part, sh);
     if (threadIdx.x == 0) partials[blockIdx.x] = s;
+    if (last_cta(&ctl->ticket[1])) {
+        const double zr = sum_partials_fixed(partials, gridDim.x, sh);
+        if (threadIdx.x == 0) {
+            scal[1] = zr;
+            if (inLoop) {
+                scal[5] = scal[3] != 0.0 ? (double)(float)(zr / scal[3]) : 0.0;
+                ctl->it += 1;
+            }
+            scal[3] = zr;
+        }
+    }
 }
 
-// Fixed-order sum of the block partials (deterministic) into scal[slot];
-// then the step length that depends on it, once for all threads: for s.q
-// (slot 0) alpha = rho / s.q, for z.r (slot 1) beta = rho_new / rho, each
-// rounded to float as BLAS::addScaled takes it (blaswrapper.h:129-158).
-// For s.q it also clears the iteration's residual norms.
-__global__ void k_sum_partials(const double *partials, int n, double *scal, int slot, const PcgCtl *ctl,
-                               unsigned long long *rmaxBits) {
-    __shared__ double sh[32];
-    if (ctl->done) return;
-    double v = 0.0;
-    for (int q = threadIdx.x; q < n; q += blockDim.x) v += partials[q];
-    double s = block_sum(v, sh);
-    if (threadIdx.x == 0) {
-        scal[slot] = s;
-        if (slot == 0) {
-            scal[4] = (double)(float)(scal[3] / s);
-            rmaxBits[0] = 0ull;
-            rmaxBits[1] = 0ull;
+// The reference's convergence test |r|inf <= tol |b|inf (pcgsolver.h:
+// 263-288) on the device, by the last CTA of the kernel that produced the
+// norm.  On the iterations where r is recomputed as b - A x (every 25th)
+// that norm decides; otherwise a pass of the recurrence's norm is only a
+// claim, which the recompute of b - A x then settles (final).
+__device__ __forceinline__ void convergence_test(PcgCtl *ctl, double resid, double ptol, bool final) {
+    ctl->resid = resid;
+    ctl->claim = 0;
+    if (resid <= ptol) {
+        if (final) {
+            ctl->done = 1;
+            ctl->iters = ctl->it + 1;
         } else {
-            scal[5] = scal[3] != 0.0 ? (double)(float)(s / scal[3]) : 0.0;
+            ctl->claim = 1;
         }
     }
 }
 
 // x += alpha s, r -= alpha q with alpha = rho / s.q passed on as float, as
-// BLAS::addScaled(float alpha, ...) does (blaswrapper.h:129-158); |r|inf
+// BLAS::addScaled(float alpha, ...) does (blaswrapper.h:129-158); |r|inf,
+// tested by the last CTA except on the iterations of the periodic recompute
 __global__ void k_update_xr(const int *__restrict__ rows, const int *__restrict__ rowsSk, const int *nRows,
                             double *__restrict__ x, double *__restrict__ r, float *__restrict__ rf,
                             const float *__restrict__ s, const double *__restrict__ q, const double *scal,
-                            unsigned long long *rmaxBits, const PcgCtl *ctl) {
+                            unsigned long long *rmaxBits, PcgCtl *ctl) {
     if (ctl->done) return;
     const int n = *nRows;
     const double alpha = scal[4];
@@ -359,16 +410,18 @@ __global__ void k_update_xr(const int *__restrict__ rows, const int *__restrict_
         m = (av != av || av > m) ? av : m;   // a NaN sticks
     }
     block_max_to(m, rmaxBits);
+    if (last_cta(&ctl->ticket[2]) && threadIdx.x == 0 && (ctl->it + 1) % 25 != 0)
+        convergence_test(ctl, bits_to_resid(rmaxBits), scal[6], false);
 }
 
-// r = b - A x (residual replacement); |r|inf.  Inside the loop it runs only
-// when needed: mode 0 on every 25th iteration (pcgsolver.h's periodic
-// recompute, here before the test), mode 1 when the recurrence just claimed
-// convergence; never once converged.
+// r = b - A x (residual replacement); |r|inf, which the last CTA tests as
+// final.  Inside the loop it runs only when needed: mode 0 on every 25th
+// iteration (pcgsolver.h's periodic recompute, here before the test), mode
+// 1 when the recurrence just claimed convergence; never once converged.
 __global__ void k_true_residual(StepConsts c, const int *__restrict__ rows, const int *__restrict__ rowsSk,
                                 const int *nRows, const double4 *__restrict__ Ad, const double *__restrict__ b,
                                 const double *__restrict__ x, double *__restrict__ r, float *__restrict__ rf,
-                                unsigned long long *rmaxBits, const PcgCtl *ctl, int mode) {
+                                unsigned long long *rmaxBits, const double *scal, PcgCtl *ctl, int mode) {
     if (ctl->done) return;
     if (mode == 0 ? (ctl->it + 1) % 25 != 0 : !ctl->claim) return;
     const int n = *nRows;
@@ -391,6 +444,7 @@ __global__ void k_true_residual(StepConsts c, const int *__restrict__ rows, cons
         m = (av != av || av > m) ? av : m;
     }
     block_max_to(m, rmaxBits);
+    if (last_cta(&ctl->ticket[3 + mode]) && threadIdx.x == 0) convergence_test(ctl, bits_to_resid(rmaxBits), scal[6], true);
 }
 
 __global__ void k_init_r(StepConsts c, SweepLayout g, const double *b, double *r, float *rf,
@@ -427,47 +481,6 @@ __global__ void k_copy_zs(const int *__restrict__ rows, const int *__restrict__ 
                           const float *__restrict__ z, float *__restrict__ s) {
     const int n = *nRows;
     for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) s[rows[e]] = z[rowsSk[e]];
-}
-
-__global__ void k_set_rho(double *scal, PcgCtl *ctl) {   // end of an iteration
-    if (ctl->done) return;
-    scal[3] = scal[1];
-    ctl->it += 1;
-}
-__global__ void k_init_rho(double *scal) { scal[3] = scal[1]; }
-
-// The reference's convergence test |r|inf <= tol |b|inf (pcgsolver.h:
-// 263-288) on the device.  After the update of iteration it: on the
-// iterations where r was recomputed as b - A x (every 25th) that norm
-// decides; otherwise a pass of the recurrence's norm is only a claim, which
-// k_confirm settles on b - A x.
-__global__ void k_check(PcgCtl *ctl, const unsigned long long *rmaxBits, const double *scal) {
-    if (ctl->done) return;
-    const int it = ctl->it, periodic = (it + 1) % 25 == 0;
-    const double ptol = scal[6];
-    const double resid = __longlong_as_double((long long)rmaxBits[periodic ? 1 : 0]);
-    ctl->resid = resid;
-    ctl->claim = 0;
-    if (resid <= ptol) {
-        if (periodic) {
-            ctl->done = 1;
-            ctl->iters = it + 1;
-        } else {
-            ctl->claim = 1;
-        }
-    }
-}
-__global__ void k_confirm(PcgCtl *ctl, const unsigned long long *rmaxBits, const double *scal) {
-    if (ctl->done || !ctl->claim) return;
-    const int it = ctl->it;
-    const double ptol = scal[6];
-    const double resid = __longlong_as_double((long long)rmaxBits[1]);
-    ctl->resid = resid;
-    ctl->claim = 0;
-    if (resid <= ptol) {
-        ctl->done = 1;
-        ctl->iters = it + 1;
-    }
 }
 
 __global__ void k_x_to_float(long long n, const double *x, float *p) {
@@ -538,7 +551,14 @@ int cuda_fail(cudaError_t e, const char *what, std::string *msg) {
 
 int pressure_partials(const StepConsts &c) { return pressure_partials_for(c.I, c.J, c.K); }
 int pressure_partials_for(int I, int J, int K) {
-    return std::min((int)div_up((long long)I * J * K, TPB), RBLOCKS);
+// One reduction CTA per 1024 grid cells (the system has at most that many
+// rows), at most RBLOCKS: a smaller grid for a small scene costs its threads a
+// few more rows each but spares the GPU's CTA dispatch, which many scenes
+// running at once share.
+#ifndef PCG_CELLS_PER_CTA
+#define PCG_CELLS_PER_CTA 1024
+#endif
+    return std::min((int)div_up((long long)I * J * K, PCG_CELLS_PER_CTA), RBLOCKS);
 }
 
 #define PCK(call)                                               \
@@ -664,22 +684,17 @@ int pressure_project(const StepConsts &c, const PressureArgs &a, PressureBuffers
         if (timed) record(tm->ev[2 * q]);
         launch_sweeps(c, pb.sl, pb.L, pb.rf, pb.z, sw, &pb.ctl->done, s);
         if (timed) record(tm->ev[2 * q + 1]);
-        { FLIP_COUNT(1); k_dot_zr<<<rb, TPB, 0, s>>>(pb.fluidIdx, pb.fluidSk, pb.nFluid, pb.z, pb.r, pb.partials, pb.ctl); }
-        { FLIP_COUNT(1); k_sum_partials<<<1, 1024, 0, s>>>(pb.partials, pb.nPartials, pb.scal, 1, pb.ctl, rmax); }
+        { FLIP_COUNT(1); k_dot_zr<<<rb, TPB, 0, s>>>(pb.fluidIdx, pb.fluidSk, pb.nFluid, pb.z, pb.r, pb.partials, pb.scal, pb.ctl, q > 0); }
     };
     // one PCG iteration (pcgsolver.h:263-300); every launch is the same for
     // every iteration, the iteration index lives on the device
     auto iteration = [&](int k, bool timed) {
-        { FLIP_COUNT(1); k_spmv<<<rb, TPB, 0, s>>>(c, pb.fluidIdx, pb.nFluid, pb.Ad, pb.s, pb.q, pb.partials, pb.ctl); }
-        { FLIP_COUNT(1); k_sum_partials<<<1, 1024, 0, s>>>(pb.partials, pb.nPartials, pb.scal, 0, pb.ctl, rmax); }
+        { FLIP_COUNT(1); k_spmv<<<rb, TPB, 0, s>>>(c, pb.fluidIdx, pb.nFluid, pb.Ad, pb.s, pb.q, pb.partials, pb.scal, rmax, pb.ctl); }
         { FLIP_COUNT(1); k_update_xr<<<rb, TPB, 0, s>>>(pb.fluidIdx, pb.fluidSk, pb.nFluid, pb.x, pb.r, pb.rf, pb.s, pb.q, pb.scal, rmax, pb.ctl); }
-        { FLIP_COUNT(1); k_true_residual<<<rb, TPB, 0, s>>>(c, pb.fluidIdx, pb.fluidSk, pb.nFluid, pb.Ad, pb.b, pb.x, pb.r, pb.rf, rmax + 1, pb.ctl, 0); }
-        { FLIP_COUNT(1); k_check<<<1, 1, 0, s>>>(pb.ctl, rmax, pb.scal); }
-        { FLIP_COUNT(1); k_true_residual<<<rb, TPB, 0, s>>>(c, pb.fluidIdx, pb.fluidSk, pb.nFluid, pb.Ad, pb.b, pb.x, pb.r, pb.rf, rmax + 1, pb.ctl, 1); }
-        { FLIP_COUNT(1); k_confirm<<<1, 1, 0, s>>>(pb.ctl, rmax, pb.scal); }
+        { FLIP_COUNT(1); k_true_residual<<<rb, TPB, 0, s>>>(c, pb.fluidIdx, pb.fluidSk, pb.nFluid, pb.Ad, pb.b, pb.x, pb.r, pb.rf, rmax + 1, pb.scal, pb.ctl, 0); }
+        { FLIP_COUNT(1); k_true_residual<<<rb, TPB, 0, s>>>(c, pb.fluidIdx, pb.fluidSk, pb.nFluid, pb.Ad, pb.b, pb.x, pb.r, pb.rf, rmax + 1, pb.scal, pb.ctl, 1); }
         precondition(1 + k, timed);
         { FLIP_COUNT(1); k_update_s<<<rb, TPB, 0, s>>>(pb.fluidIdx, pb.fluidSk, pb.nFluid, pb.z, pb.s, pb.scal, pb.ctl); }
-        { FLIP_COUNT(1); k_set_rho<<<1, 1, 0, s>>>(pb.scal, pb.ctl); }
     };
 
     mail->ptol = ptol;
@@ -699,7 +714,6 @@ int pressure_project(const StepConsts &c, const PressureArgs &a, PressureBuffers
     int sweepErr = 0;
     if (!(rho0 == 0 || rho0 != rho0)) {
         { FLIP_COUNT(1); k_copy_zs<<<rb, TPB, 0, s>>>(pb.fluidIdx, pb.fluidSk, pb.nFluid, pb.z, pb.s); }
-        { FLIP_COUNT(1); k_init_rho<<<1, 1, 0, s>>>(pb.scal); }
         // Iterations go to the device PCG_BATCH at a time, as one CUDA graph
         // (captured on first use, per context): the convergence test runs
         // there and the kernels of iterations after convergence return at

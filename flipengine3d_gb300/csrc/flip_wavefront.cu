@@ -49,7 +49,11 @@ namespace flip {
 namespace {
 
 constexpr int TJ = SWEEP_TJ, TK = SWEEP_TK, NP = SWEEP_NP, CH = 8;
-constexpr int NBUF = TK <= 8 ? 4 : 2;   // ring slots that fit in shared memory
+#ifndef SWEEP_NBUF
+#define SWEEP_NBUF (SWEEP_TK <= 8 ? 4 : 2)   // ring slots that fit in shared memory
+#endif
+constexpr int NBUF = SWEEP_NBUF;
+static_assert(NBUF >= 2, "the ring needs a slot in flight beside the one in use");
 // the helper warp's lanes take the CH x TK j-edge words JQ at a time and the
 // CH x TJ k-edge words one step each
 constexpr int JQ = CH * TK / 32;
