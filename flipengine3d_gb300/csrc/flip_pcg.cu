@@ -551,12 +551,11 @@ int cuda_fail(cudaError_t e, const char *what, std::string *msg) {
 
 int pressure_partials(const StepConsts &c) { return pressure_partials_for(c.I, c.J, c.K); }
 int pressure_partials_for(int I, int J, int K) {
-// One reduction CTA per 1024 grid cells (the system has at most that many
-// rows), at most RBLOCKS: a smaller grid for a small scene costs its threads a
-// few more rows each but spares the GPU's CTA dispatch, which many scenes
-// running at once share.
+// One reduction CTA per 4096 grid cells, at most RBLOCKS.  A liquid fills a
+// fraction of the grid, so a thread takes a few rows; a smaller grid spares
+// the GPU's CTA dispatch, which many scenes running at once share.
 #ifndef PCG_CELLS_PER_CTA
-#define PCG_CELLS_PER_CTA 1024
+#define PCG_CELLS_PER_CTA 4096
 #endif
     return std::min((int)div_up((long long)I * J * K, PCG_CELLS_PER_CTA), RBLOCKS);
 }
