@@ -274,25 +274,52 @@ def mixed_scenes(count, seed=1):
     return [dam_break(int(e), seed=seed * 1000 + q, fill=(float(f), 0.6, 1.0)) for q, (e, f) in enumerate(zip(edges, fills))]
 
 
+def served_scene(q, seed=2):
+    """Scene q of the served set: a cubic grid with its edge drawn uniformly
+    from [32, 160] (dx = 1/edge), a dam break whose x extent is drawn from
+    [0.2, 0.6], y <= 0.6, full z, 4-8 jittered particles per cell (drawn per
+    scene), FLIP blend 0.95, PCG tolerance 1e-5."""
+    from flipengine3d_gb300.scenes import dam_break
+    rng = np.random.default_rng([seed, q])
+    edge = int(rng.integers(32, 161))
+    fill = float(rng.uniform(0.2, 0.6))
+    ppc = int(rng.integers(4, 9))
+    return dam_break(edge, seed=seed * 100000 + q, fill=(fill, 0.6, 1.0), ppc=ppc, tolerance=1e-5)
+
+
+def resident_scenes(rt, make, count, threads=16):
+    """Create `count` scenes through the runtime's admission by free HBM: the
+    host generates the particles on `threads` threads, and each scene is
+    admitted and made resident in order.  Returns (simulations, rejected)."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    import flipengine3d_gb300 as fg
+    sims, rejected = [], 0
+    with ThreadPoolExecutor(max_workers=threads) as ex:
+        for first in range(0, count, 2 * threads):   # a bounded number of scenes on the host at once
+            for sc in ex.map(make, range(first, min(count, first + 2 * threads))):
+                need = fg.estimate_device_bytes(sc.isize, sc.jsize, sc.ksize, sc.num_particles)
+                if not rt.admit(need):
+                    rejected += 1
+                    continue
+                sims.append(fg.FluidSimulation.from_scene(sc))
+    return sims, rejected
+
+
 def run_batched_and_served(args, plain_value):
     """Many resident scenes on one GPU through the C++ runtime (one CUDA
-    stream per scene, args.workers host threads).  Batched: every scene one
-    step per round (update_all), wall-clock timed over args.batch_steps
-    rounds.  Served: Poisson arrivals of one-step requests for random resident
+    stream per scene, args.workers host threads).  Batched: the mixed-size
+    set, every scene one step per round (update_all), wall-clock timed over
+    args.batch_steps rounds.  Served: the served set of args.served_scenes
+    resident scenes, Poisson arrivals of one-step requests for random
     scenes, latency from submission to completion."""
     import torch
 
     import flipengine3d_gb300 as fg
     scs = mixed_scenes(args.batch_scenes)
     rt = fg.FluidRuntime(workers=args.workers, reserve_bytes=2 << 30)
-    sims, rejected = [], 0
-    for sc in scs:   # admission by free HBM
-        need = fg.estimate_device_bytes(sc.isize, sc.jsize, sc.ksize, sc.num_particles)
-        if not rt.admit(need):
-            rejected += 1
-            continue
-        sims.append((sc, fg.FluidSimulation.from_scene(sc)))
-    handles = [s for _, s in sims]
+    handles, rejected = resident_scenes(rt, lambda q: scs[q], len(scs))
+    del scs
     dt = FRAME_DT
     for _ in range(max(args.warmup, 1)):
         rt.update_all(handles, dt)
@@ -312,7 +339,14 @@ def run_batched_and_served(args, plain_value):
                "timing": "wall clock around update_all (all scenes one frame), device synchronised",
                "config": "mixed sizes: edges from {32,48,64,80,96} (seed 1), dam x-fill U[0.2,0.6], y<=0.6, "
                          "8 particles per cell, FLIP blend 0.95, PCG tol 1e-6, dt=1/120; one stream per scene"}
-    # served: Poisson arrivals
+    for s in handles:
+        s.close()
+    torch.cuda.synchronize()
+    # served: Poisson arrivals over the served set
+    handles, srejected = resident_scenes(rt, served_scene, args.served_scenes)
+    for _ in range(max(args.warmup, 1)):
+        rt.update_all(handles, dt)
+    torch.cuda.synchronize()
     rng = np.random.default_rng(7)
     gaps = rng.exponential(1.0 / args.arrival_rate, size=args.requests)
     picks = rng.integers(0, len(handles), size=args.requests)
@@ -330,9 +364,11 @@ def run_batched_and_served(args, plain_value):
     served = {"p50_ms": round(float(np.percentile(lat, 50)), 2), "p99_ms": round(float(np.percentile(lat, 99)), 2),
               "requests": args.requests, "arrival_rate_hz": args.arrival_rate,
               "value": round(float(sum(sizes[q] for q in picks)) / ts / 1e6, 3), "unit": UNIT,
-              "resident_scenes": len(handles), "workers": args.workers,
-              "note": "latency = submission to completion (queueing included); one-step requests on the "
-                      "batched scene set"}
+              "resident_scenes": len(handles), "rejected_at_admission": srejected,
+              "resident_particles": int(sum(sizes)), "workers": args.workers,
+              "config": "edges uniform in [32,160] (seed 2), dam x-fill U[0.2,0.6], y<=0.6, 4-8 particles per "
+                        "cell, FLIP blend 0.95, PCG tol 1e-5, dt=1/120; one stream per scene",
+              "note": "latency = submission to completion (queueing included); one-step requests"}
     rt.close()
     for s in handles:
         s.close()
@@ -405,6 +441,7 @@ def main():
     ap.add_argument("--batch-steps", type=int, default=5)
     ap.add_argument("--workers", type=int, default=16)
     ap.add_argument("--requests", type=int, default=800)
+    ap.add_argument("--served-scenes", type=int, default=256)
     ap.add_argument("--arrival-rate", type=float, default=2000.0)
     ap.add_argument("--scene", default="plain_128", choices=sorted(SCENES),
                     help="plain_128 is the benchmark workload; plain_64 is the small case for profiling")

@@ -37,13 +37,19 @@ class Scene:
         return int(self.positions.shape[0])
 
 
-def _jittered_cells(cells: np.ndarray, dx: float, rng: np.random.Generator) -> np.ndarray:
-    """8 particles per cell, one per 2x2x2 sub-cell, uniform inside the sub-cell."""
+def _jittered_cells(cells: np.ndarray, dx: float, rng: np.random.Generator, ppc: int = 8) -> np.ndarray:
+    """8 particles per cell, one per 2x2x2 sub-cell, uniform inside the
+    sub-cell; with ppc < 8, a random ppc of the 8 sub-cells per cell (kept in
+    sub-cell order)."""
     sub = np.array([[a, b, c] for c in (0, 1) for b in (0, 1) for a in (0, 1)], dtype=np.float64)
     n = cells.shape[0]
     base = (cells[:, None, :].astype(np.float64) + 0.5 * sub[None, :, :]) * dx
     jitter = rng.random((n, 8, 3)) * (0.5 * dx)
-    return (base + jitter).reshape(-1, 3).astype(np.float32)
+    pts = base + jitter
+    if ppc < 8:
+        keep = np.sort(np.argsort(rng.random((n, 8)), axis=1)[:, :ppc], axis=1)
+        pts = np.take_along_axis(pts, keep[:, :, None], axis=1)
+    return pts.reshape(-1, 3).astype(np.float32)
 
 
 def _box_cells(isize, jsize, ksize, dx, lo, hi) -> np.ndarray:
@@ -65,7 +71,7 @@ def _sphere_cells(isize, jsize, ksize, dx, centre, radius) -> np.ndarray:
 
 def dam_break(n: int = 64, *, seed: int = 0, fill=(0.4, 0.6, 1.0), sphere: bool = False,
               jsize: int | None = None, ksize: int | None = None, dx: float | None = None,
-              steps: int = 10, pic_ratio: float = 0.05, tolerance: float = 1e-6) -> Scene:
+              steps: int = 10, pic_ratio: float = 0.05, tolerance: float = 1e-6, ppc: int = 8) -> Scene:
     """Dam break in an n^3 (or n x jsize x ksize) box of side n*dx.
 
     The fluid block spans x in [0, fill[0]], y in [0, fill[1]], z in [0, fill[2]]
@@ -73,17 +79,18 @@ def dam_break(n: int = 64, *, seed: int = 0, fill=(0.4, 0.6, 1.0), sphere: bool 
     With `sphere`, a ball of radius 0.15 centred at (0.7, 0.7, 0.5) moving at
     (0, -2, 0) is added.  Particles in the outer three cells sit inside the
     domain walls and are removed by the first step, as in the reference.
+    `ppc` (1-8) keeps that many of each cell's 8 particles.
     """
     jsize = n if jsize is None else jsize
     ksize = n if ksize is None else ksize
     dx = 1.0 / n if dx is None else dx
     rng = np.random.default_rng(seed)
     cells = _box_cells(n, jsize, ksize, dx, (0.0, 0.0, 0.0), fill)
-    pos = _jittered_cells(cells, dx, rng)
+    pos = _jittered_cells(cells, dx, rng, ppc)
     vel = np.zeros_like(pos)
     if sphere:
         sc = _sphere_cells(n, jsize, ksize, dx, (0.7, 0.7, 0.5), 0.15)
-        sp = _jittered_cells(sc, dx, rng)
+        sp = _jittered_cells(sc, dx, rng, ppc)
         sv = np.zeros_like(sp)
         sv[:, 1] = -2.0
         pos = np.concatenate([pos, sp])
