@@ -1,0 +1,101 @@
+"""GPU: the benchmark configurations at their full sizes.
+
+* 64^3 dam break, 10 frames: every frame against the oracle.
+* 128^3 dam break + sphere: the first frame against the oracle, then all 60
+  frames checked through properties that hold at any size.
+* 256x128x128 (FLIP blend 0.98, liquid in the lower 45%): the first frame
+  solved to 1e-9 on both sides, its pressure within 1e-6 relative of the
+  oracle's FP64 PCG (the configuration's own target); then 30 frames of
+  properties at the scene's tolerance.
+
+Bars as in test_gpu_parity: liquid SDF bit-exact; pressure, faces and
+positions within 1e-5 relative after one step; 1e-4 after several frames.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from conftest import rel_err
+from flipengine3d_gb300 import FluidSimulation
+from flipengine3d_gb300.scenes import mixed_256, plain_64, plain_128
+from oracle import refsim
+
+pytestmark = pytest.mark.gpu
+
+RTOL = 1e-5
+RTOL_MULTI = 1e-4
+
+
+def frame_properties(sim, sc, n_before, label):
+    """What a correct frame keeps, whatever the size: a converged solve, no
+    particle gained, every particle inside the domain box, finite state."""
+    st = sim.getFrameStatsData()
+    assert st.pressure_status == 0, f"{label}: pressure solve status {st.pressure_status}"
+    n = sim.getNumMarkerParticles()
+    assert 0 < n <= n_before, f"{label}: particle count {n_before} -> {n}"
+    pos = sim.getMarkerParticlePositionData()
+    vel = sim.getMarkerParticleVelocityData()
+    assert np.isfinite(pos).all() and np.isfinite(vel).all(), f"{label}: non-finite particle state"
+    ext = np.array([sc.isize, sc.jsize, sc.ksize]) * sc.dx
+    assert (pos >= 0).all() and (pos <= ext).all(), f"{label}: particle outside the domain"
+    return n
+
+
+def first_frame_vs_oracle(sim, sc, label, tol=None, prtol=RTOL):
+    orc = refsim.OracleSimulation(sc.isize, sc.jsize, sc.ksize, sc.dx).setup(sc, tolerance=tol)
+    ref = orc.update_staged(sc.frame_dt)
+    if tol is not None:
+        sim.setPressureSolveTolerance(tol)
+    st = sim.update_staged(sc.frame_dt)
+    sim.setPressureSolveTolerance(sc.tolerance)
+    assert np.array_equal(st["phi"], ref["phi"]), f"{label}: liquid SDF not bit-exact"
+    # The faces take dt/dx times a difference of FP32 pressures: pressures
+    # that differ by one float ulp at the largest |p| move a face by that
+    # much, which is the floor for two solvers whose pressures are not
+    # bit-identical.  Early frames of a large domain have small face speeds,
+    # so the floor can exceed RTOL relative to them.
+    ulp_p = float(np.spacing(np.float32(np.abs(ref["pressure"]).max())))
+    for f in ("u", "v", "w"):
+        floor = 2.0 * ulp_p * (sc.frame_dt / sc.dx) / max(float(np.abs(ref[f"{f}_final"]).max()), 1e-30)
+        assert rel_err(st[f"{f}_final"], ref[f"{f}_final"]) <= max(RTOL, floor), f"{label}: final {f}"
+    perr = rel_err(st["pressure"], ref["pressure"])
+    assert perr <= prtol, f"{label}: pressure vs the FP64 PCG oracle {perr:.3g}"
+    assert st["positions"].shape == ref["positions"].shape
+    assert rel_err(st["positions"], ref["positions"]) <= RTOL, f"{label}: positions"
+    return orc
+
+
+def test_plain_64_ten_frames_track_the_oracle(gpu):
+    sc = plain_64()
+    with FluidSimulation.from_scene(sc) as sim:
+        orc = first_frame_vs_oracle(sim, sc, "64^3 frame 1")
+        n = sim.getNumMarkerParticles()
+        for f in range(2, sc.steps + 1):
+            sim.update(sc.frame_dt)
+            orc.update(sc.frame_dt)
+            n = frame_properties(sim, sc, n, f"64^3 frame {f}")
+            pos = sim.getMarkerParticlePositionData()
+            rpos, _ = orc.particles()
+            assert pos.shape == rpos.shape, f"64^3 frame {f}: particle count"
+            assert rel_err(pos, rpos) <= RTOL_MULTI, f"64^3 frame {f}"
+
+
+def test_plain_128_sixty_frames(gpu):
+    sc = plain_128()
+    with FluidSimulation.from_scene(sc) as sim:
+        first_frame_vs_oracle(sim, sc, "128^3 frame 1")
+        n = sim.getNumMarkerParticles()
+        for f in range(2, sc.steps + 1):
+            sim.update(sc.frame_dt)
+            n = frame_properties(sim, sc, n, f"128^3 frame {f}")
+
+
+def test_mixed_256_against_fp64_pcg_then_thirty_frames(gpu):
+    sc = mixed_256()
+    with FluidSimulation.from_scene(sc) as sim:
+        first_frame_vs_oracle(sim, sc, "256x128x128 frame 1", tol=1e-9, prtol=1e-6)
+        n = sim.getNumMarkerParticles()
+        for f in range(2, sc.steps + 1):
+            sim.update(sc.frame_dt)
+            n = frame_properties(sim, sc, n, f"256x128x128 frame {f}")
