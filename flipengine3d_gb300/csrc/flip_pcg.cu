@@ -230,6 +230,81 @@ __global__ void k_mic0_levels(StepConsts c, const uint8_t *fluid, const double4 
     }
 }
 
+// The pivot of cell c (mic0_cell) regrouped per earlier neighbour q:
+//   L_cq^2 + 0.97 L_cq miss_q = inv_q^2 (a_q^2 + 0.97 a_q (m1_q + m2_q)),
+// with a_q the coupling of q to c and m1_q, m2_q q's other later-neighbour
+// couplings (0 where mic0_cell skips them).  The bracket depends on the rows
+// only; this pass computes it for every cell and earlier neighbour, so a
+// level needs three multiply-subtracts and a reciprocal square root.  The
+// FP64 results differ from mic0_cell's order in the last bits; the factor
+// is used rounded to FP32.
+__global__ void k_mic0_weights(StepConsts c, const uint8_t *fluid, const double4 *Ad, double *W0, double *W1,
+                               double *W2) {
+    const long long n = (long long)c.I * c.J * c.K;
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    double w[3] = {0.0, 0.0, 0.0};
+    if (fluid[t]) {   // interior by construction
+        const long long sy = c.I, sz = (long long)c.I * c.J;
+        const long long back[3] = {t - sz, t - sy, t - 1};
+#pragma unroll
+        for (int q = 0; q < 3; q++) {
+            const long long kk = back[q];
+            if (!fluid[kk]) continue;
+            const double4 ak = Ad[kk];
+            if (ak.x == 0.0) continue;
+            const double a = q == 0 ? ak.w : (q == 1 ? ak.z : ak.y);
+            const double o1 = q == 2 ? ak.z : ak.y, o2 = q == 0 ? ak.z : ak.w;
+            const double m1 = fluid[q == 2 ? kk + sy : kk + 1] ? o1 : 0.0;
+            const double m2 = fluid[q == 0 ? kk + sy : kk + sz] ? o2 : 0.0;
+            w[q] = a * a + 0.97 * a * (m1 + m2);
+        }
+    }
+    W0[t] = w[0];
+    W1[t] = w[1];
+    W2[t] = w[2];
+}
+
+// All levels lo..hi in one cooperative launch, a thread per (j, k) pencil
+// (the grid covers every pencil).  At level lv a pencil's cell is
+// i = lv - j - k, one further along i than at the previous level, so the -x
+// neighbour's pivot is the thread's own from the level before, kept in a
+// register; after each grid barrier only the -y and -z neighbours' pivots
+// are read from memory.  A neighbour that is no row has inv 0 (k_build
+// clears invD), so its term vanishes without a branch.
+__global__ void __launch_bounds__(TPB) k_mic0_pencils(StepConsts c, const uint8_t *fluid, const double4 *Ad,
+                                                      const double *W0, const double *W1, const double *W2,
+                                                      double *invD, int lo, int hi) {
+    cg::grid_group grid = cg::this_grid();
+    const int nj = c.J - 2, np = nj * (c.K - 2);
+    const int jj = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool mine = jj < np;
+    const int j = 1 + (mine ? jj % nj : 0), k = 1 + (mine ? jj / nj : 0);
+    const int sy = c.I, sz = c.I * c.J;
+    double prevInv = 0.0;
+    for (int lv = lo; lv <= hi; lv++) {
+        const int i = lv - j - k;
+        double inv = 0.0;
+        if (mine && i >= 1 && i <= c.I - 2) {
+            const int t = i + sy * j + sz * k;
+            if (fluid[t]) {
+                const double ad = Ad[t].x;
+                const double nz = invD[t - sz], ny = invD[t - sy];
+                double d = ad;
+                d -= W0[t] * (nz * nz);
+                d -= W1[t] * (ny * ny);
+                d -= W2[t] * (prevInv * prevInv);
+                if (ad == 0.0) inv = 0.0;
+                else if (d < 0.25 * ad) inv = rsqrt(ad);
+                else inv = rsqrt(d);
+                invD[t] = inv;
+            }
+        }
+        prevInv = inv;
+        grid.sync();
+    }
+}
+
 // the FP32 factor rows of the interior cells, into the sweep layout
 __global__ void k_mic0_finalize(StepConsts c, SweepLayout g, const uint8_t *fluid, const double4 *Ad,
                                 const double *invD, float4 *L) {
@@ -447,13 +522,15 @@ __global__ void k_true_residual(StepConsts c, const int *__restrict__ rows, cons
     if (last_cta(&ctl->ticket[3 + mode]) && threadIdx.x == 0) convergence_test(ctl, bits_to_resid(rmaxBits), scal[6], true);
 }
 
-__global__ void k_init_r(StepConsts c, SweepLayout g, const double *b, double *r, float *rf,
+// r = b (and its FP32 copy in the sweep layout), x = 0, |b|inf
+__global__ void k_init_r(StepConsts c, SweepLayout g, const double *b, double *r, float *rf, double *x,
                          unsigned long long *rmaxBits) {
     const long long n = (long long)c.I * c.J * c.K;
     double m = 0.0;
 #pragma unroll 4
     for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
         r[t] = b[t];
+        x[t] = 0.0;
         int i, j, k;
     unflatten(t, c.I, c.J, i, j, k);
         if (i >= 1 && j >= 1 && k >= 1 && i <= c.I - 2 && j <= c.J - 2 && k <= c.K - 2)
@@ -637,15 +714,28 @@ int pressure_project(const StepConsts &c, const PressureArgs &a, PressureBuffers
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        int perSMp = 0;
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_mic0_levels, TPB, 0);
-        if (coop && perSM > 0) {
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSMp, k_mic0_pencils, TPB, 0);
+        int lo_ = lo, hi_ = hi;
+        StepConsts c_ = c;
+        const uint8_t *fl = pb.fluid;
+        const double4 *ad = pb.Ad;
+        double *inv = pb.invdiagD;
+        void *args[] = {&c_, &fl, &ad, &inv, &lo_, &hi_};
+        // a thread per pencil where one cooperative wave holds them all; the
+        // pivot weights go to q, r and x, which the loop set-up rewrites
+        if (coop && perSMp > 0 && div_up(np, TPB) <= (long long)perSMp * sms) {
+            const double *w0 = pb.q, *w1 = pb.r, *w2 = pb.x;
+            void *pargs[] = {&c_, &fl, &ad, &w0, &w1, &w2, &inv, &lo_, &hi_};
+            { FLIP_COUNT(1); k_mic0_weights<<<nb, TPB, 0, s>>>(c, pb.fluid, pb.Ad, pb.q, pb.r, pb.x); }
+            FLIP_COUNT(1);
+            factored = cudaLaunchCooperativeKernel((const void *)k_mic0_pencils, (int)div_up(np, TPB), TPB, pargs, 0,
+                                                   s) == cudaSuccess;
+            if (!factored) cudaGetLastError();
+        }
+        if (!factored && coop && perSM > 0) {
             const int grid = std::max(1, std::min((int)div_up(np, TPB), perSM * sms));
-            int lo_ = lo, hi_ = hi;
-            StepConsts c_ = c;
-            const uint8_t *fl = pb.fluid;
-            const double4 *ad = pb.Ad;
-            double *inv = pb.invdiagD;
-            void *args[] = {&c_, &fl, &ad, &inv, &lo_, &hi_};
             FLIP_COUNT(1);
             factored = cudaLaunchCooperativeKernel((const void *)k_mic0_levels, grid, TPB, args, 0, s) == cudaSuccess;
             if (!factored) cudaGetLastError();
@@ -700,7 +790,7 @@ int pressure_project(const StepConsts &c, const PressureArgs &a, PressureBuffers
     PCK(cudaMemsetAsync(pb.ctl, 0, sizeof(PcgCtl), s));
     PCK(cudaMemsetAsync(rmax, 0, 2 * sizeof(unsigned long long), s));
     PCK(cudaMemcpyAsync(pb.scal + 6, &mail->ptol, sizeof(double), cudaMemcpyHostToDevice, s));
-    { FLIP_COUNT(1); k_init_r<<<rb, TPB, 0, s>>>(c, pb.sl, pb.b, pb.r, pb.rf, rmax); }
+    { FLIP_COUNT(1); k_init_r<<<rb, TPB, 0, s>>>(c, pb.sl, pb.b, pb.r, pb.rf, pb.x, rmax); }
     sweep_epoch_guard(c, sw, 2, s);
     precondition(0, tm != nullptr);
     PCK(cudaMemcpyAsync(&mail->rho, pb.scal + 1, sizeof(double), cudaMemcpyDeviceToHost, s));
