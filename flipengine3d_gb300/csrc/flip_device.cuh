@@ -157,6 +157,8 @@ struct PressureBuffers {
     long long batchKernels[2][2] = {};
     bool noGraphs = false;   // the stream cannot be captured: launch eagerly
     int *levelRange;       // [0]=min(i+j+k) [1]=max(i+j+k) [2]=system size [3..6]=min/max j, min/max k
+    int *factorProgress;   // per factor tile: the last level it finished
+    unsigned int *factorTicket;
     float *pressure;       // float copy of x for the velocity update
     int nPartials;
 };
@@ -212,6 +214,7 @@ void sweep_epoch_guard(const StepConsts &c, SweepState &sw, long long upcoming, 
 
 int pressure_partials(const StepConsts &c);
 int pressure_partials_for(int I, int J, int K);
+int mic0_factor_tiles(int J, int K);   // tiles of the wavefront factorisation
 // PressureSolver::solve (pressuresolver.cpp:44-76) on the device.  Returns
 // FLIP_OK (velocities updated, or nothing to solve), FLIP_E_SOLVER_NOCONV
 // (left unchanged), FLIP_E_DEVICE_TIMEOUT or FLIP_E_CUDA.

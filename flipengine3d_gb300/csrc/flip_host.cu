@@ -215,7 +215,8 @@ int alloc_grids(flip_ctx *x) {
     CK(cudaMemsetAsync(p.z, 0, nsl * sizeof(float), x->stream));
     p.nPartials = pressure_partials(x->c);
     if ((rc = x->alloc(&p.partials, p.nPartials + 32)) || (rc = x->alloc(&p.scal, 8)) ||
-        (rc = x->alloc(&p.rmaxBits, 2)) || (rc = x->alloc(&p.levelRange, 8)) || (rc = x->alloc(&p.ctl, 1)))
+        (rc = x->alloc(&p.rmaxBits, 2)) || (rc = x->alloc(&p.levelRange, 8)) || (rc = x->alloc(&p.ctl, 1)) ||
+        (rc = x->alloc(&p.factorProgress, mic0_factor_tiles(x->J, x->K))) || (rc = x->alloc(&p.factorTicket, 1)))
         return rc;
     {
         int nt = sweep_tiles_max(x->I, x->J, x->K);
@@ -952,6 +953,7 @@ int flip_estimate_device_bytes(int isize, int jsize, int ksize, int particles, l
     b += nc * (1 + 32 + 8 * 5 + 4 + 4) + nsl * (16 + 4 + 4);              // pressure system
     b += (nc + 1) * 4 * 2 + nc * 4 * 2 + (scan_scratch_ints((int)nc) + 8) * 4;   // row list
     b += (pressure_partials_for(isize, jsize, ksize) + 32) * 8 + 64 + 16 + 32;
+    b += (mic0_factor_tiles(jsize, ksize) + 1) * 4 + 64;                  // factor tiles, ticket, control
     b += sweep_exchange_words(isize, jsize, ksize) * 8 + 4096;           // sweep exchange, ranges, tables
     b += cap * (7 * 4 * 2 + 4 * 4) + (scan_scratch_ints((int)cap) + 4) * 4 + 64;   // particles
     *bytes = b;

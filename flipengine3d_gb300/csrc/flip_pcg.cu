@@ -265,44 +265,139 @@ __global__ void k_mic0_weights(StepConsts c, const uint8_t *fluid, const double4
     W2[t] = w[2];
 }
 
-// All levels lo..hi in one cooperative launch, a thread per (j, k) pencil
-// (the grid covers every pencil).  At level lv a pencil's cell is
-// i = lv - j - k, one further along i than at the previous level, so the -x
-// neighbour's pivot is the thread's own from the level before, kept in a
-// register; after each grid barrier only the -y and -z neighbours' pivots
-// are read from memory.  A neighbour that is no row has inv 0 (k_build
-// clears invD), so its term vanishes without a branch.
-__global__ void __launch_bounds__(TPB) k_mic0_pencils(StepConsts c, const uint8_t *fluid, const double4 *Ad,
-                                                      const double *W0, const double *W1, const double *W2,
-                                                      double *invD, int lo, int hi) {
-    cg::grid_group grid = cg::this_grid();
-    const int nj = c.J - 2, np = nj * (c.K - 2);
-    const int jj = blockIdx.x * blockDim.x + threadIdx.x;
-    const bool mine = jj < np;
-    const int j = 1 + (mine ? jj % nj : 0), k = 1 + (mine ? jj / nj : 0);
+// The factor as a tiled wavefront, with no grid-wide barrier: a CTA per
+// tile of FT x FT (j, k) pencils, tiles taken by ticket in diagonal order
+// (a tile only waits on tiles with smaller tickets, which are running or
+// done).  Within a tile a level costs one __syncthreads: the -y and -z
+// neighbours' pivots of the level before sit in shared memory, the -x one
+// in a register.  Across tiles a tile publishes the last level it finished
+// every FCH levels (release), and a tile's edge threads read FCH levels of
+// the neighbouring pencil's pivots at once, after acquiring its progress.
+// Every wait is bounded: past the limit the tile sets *err and all tiles
+// that depend on it give up too (the solve reports a device timeout).
+// A level is bound by the latency of its FP64 chain (a dependent FP64
+// operation takes ~64 cycles on this GPU, rsqrt ~430), not by throughput:
+// tiles of 8, 12 and 16 pencils a side time the same.
+#ifndef MIC0_FT
+#define MIC0_FT 16
+#endif
+#ifndef MIC0_FCH
+#define MIC0_FCH 8
+#endif
+constexpr int FT = MIC0_FT, FCH = MIC0_FCH;
+static_assert(FT * FT >= 32 && FT * FT <= 1024, "a tile is one CTA");
+constexpr unsigned int FACTOR_SPIN_LIMIT = 1u << 22;
+constexpr int FACTOR_DONE = 0x7fffffff;   // progress of a tile with all its levels done
+
+__device__ __forceinline__ int ld_acquire(const int *p) {
+    int v;
+    asm volatile("ld.acquire.gpu.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_release(int *p, int v) {
+    asm volatile("st.release.gpu.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+__global__ void __launch_bounds__(FT *FT) k_mic0_tiles(StepConsts c, const uint8_t *fluid, const double4 *Ad,
+                                                       const double *W0, const double *W1, const double *W2,
+                                                       double *invD, int lo, int hi, unsigned int *ticket,
+                                                       int *progress, int *err) {
+    __shared__ double prev[2][FT][FT];
+    __shared__ int tileSh, abortSh;
+    const int ntj = (c.J - 2 + FT - 1) / FT, ntk = (c.K - 2 + FT - 1) / FT;
+    if (threadIdx.x == 0) {
+        // ticket -> tile in diagonal order (tj + tk, then tj)
+        int q = (int)atomicAdd(ticket, 1u), d = 0;
+        for (; d < ntj + ntk - 1; d++) {
+            const int n = min(d, ntj - 1) - max(0, d - ntk + 1) + 1;
+            if (q < n) break;
+            q -= n;
+        }
+        abortSh = d >= ntj + ntk - 1;   // more CTAs than tiles: the launch is wrong
+        if (abortSh) atomicExch(err, 1);
+        const int tj = max(0, d - ntk + 1) + q;
+        tileSh = tj + ntj * (d - tj);
+    }
+    __syncthreads();
+    if (abortSh) return;
+    const int tile = tileSh, tj = tile % ntj, tk = tile / ntj;
+    const int a = threadIdx.x % FT, b = threadIdx.x / FT;   // j and k within the tile
+    const int j = 1 + tj * FT + a, k = 1 + tk * FT + b;
+    const bool mine = j <= c.J - 2 && k <= c.K - 2;
     const int sy = c.I, sz = c.I * c.J;
-    double prevInv = 0.0;
-    for (int lv = lo; lv <= hi; lv++) {
-        const int i = lv - j - k;
-        double inv = 0.0;
-        if (mine && i >= 1 && i <= c.I - 2) {
+    // the levels holding cells of this tile, within lo..hi
+    const int jhi = min(c.J - 2, 1 + tj * FT + FT - 1), khi = min(c.K - 2, 1 + tk * FT + FT - 1);
+    const int lvStart = max(lo, 1 + (1 + tj * FT) + (1 + tk * FT));
+    const int lvEnd = min(hi, (c.I - 2) + jhi + khi);
+    const int left = tj > 0 ? tile - 1 : -1, down = tk > 0 ? tile - ntj : -1;
+    prev[0][b][a] = prev[1][b][a] = 0.0;
+    if (threadIdx.x == 0) st_release(&progress[tile], lvStart - 1);   // the levels below hold no cell of the tile
+    int cur = 0;
+    double own = 0.0;   // this pencil's pivot at the level before (the -x neighbour's)
+    for (int lvc = lvStart; lvc <= lvEnd; lvc += FCH) {
+        // the chunk's boundary values are the neighbours' levels lvc-1 .. lvc+FCH-2
+        if (threadIdx.x == 0) {
+            const int need = lvc + FCH - 2;
+            const int nbr[2] = {left, down};
+            for (int q = 0; q < 2 && !abortSh; q++) {
+                if (nbr[q] < 0) continue;
+                unsigned int spin = 0;
+                while (ld_acquire(&progress[nbr[q]]) < need) {
+                    if (++spin >= FACTOR_SPIN_LIMIT || ld_acquire(err)) {
+                        atomicExch(err, 1);
+                        abortSh = 1;
+                        break;
+                    }
+                    if (spin > 256) __nanosleep(128);
+                }
+            }
+        }
+        __syncthreads();
+        if (abortSh) return;
+        // the chunk's cells of this pencil are consecutive along i: their
+        // rows, flags and weights, and the edge pencils' pivots, load at once
+        double bY[FCH], bZ[FCH], pad[FCH], pw0[FCH], pw1[FCH], pw2[FCH];
+        bool pcell[FCH];
+#pragma unroll
+        for (int m = 0; m < FCH; m++) {
+            const int i = lvc + m - j - k;
+            const bool in = mine && i >= 1 && i <= c.I - 2 && lvc + m <= lvEnd;
             const int t = i + sy * j + sz * k;
-            if (fluid[t]) {
-                const double ad = Ad[t].x;
-                const double nz = invD[t - sz], ny = invD[t - sy];
+            pcell[m] = in && fluid[t];
+            pad[m] = pcell[m] ? Ad[t].x : 0.0;
+            pw0[m] = pcell[m] ? W0[t] : 0.0;
+            pw1[m] = pcell[m] ? W1[t] : 0.0;
+            pw2[m] = pcell[m] ? W2[t] : 0.0;
+            bY[m] = (pcell[m] && a == 0 && left >= 0) ? __ldcg(invD + t - sy) : 0.0;
+            bZ[m] = (pcell[m] && b == 0 && down >= 0) ? __ldcg(invD + t - sz) : 0.0;
+        }
+#pragma unroll
+        for (int m = 0; m < FCH; m++) {
+            const int lv = lvc + m;
+            if (lv > lvEnd) break;
+            double inv = 0.0;
+            if (pcell[m]) {
+                const int t = (lv - j - k) + sy * j + sz * k;
+                const double ad = pad[m];
+                const double nz = b > 0 ? prev[cur ^ 1][b - 1][a] : bZ[m];
+                const double ny = a > 0 ? prev[cur ^ 1][b][a - 1] : bY[m];
                 double d = ad;
-                d -= W0[t] * (nz * nz);
-                d -= W1[t] * (ny * ny);
-                d -= W2[t] * (prevInv * prevInv);
+                d -= pw0[m] * (nz * nz);
+                d -= pw1[m] * (ny * ny);
+                d -= pw2[m] * (own * own);
                 if (ad == 0.0) inv = 0.0;
                 else if (d < 0.25 * ad) inv = rsqrt(ad);
                 else inv = rsqrt(d);
                 invD[t] = inv;
             }
+            prev[cur][b][a] = inv;
+            own = inv;
+            cur ^= 1;
+            __syncthreads();
         }
-        prevInv = inv;
-        grid.sync();
+        if (threadIdx.x == 0) st_release(&progress[tile], min(lvc + FCH - 1, lvEnd));
     }
+    if (threadIdx.x == 0) st_release(&progress[tile], FACTOR_DONE);
 }
 
 // the FP32 factor rows of the interior cells, into the sweep layout
@@ -627,6 +722,7 @@ int cuda_fail(cudaError_t e, const char *what, std::string *msg) {
 }  // namespace
 
 int pressure_partials(const StepConsts &c) { return pressure_partials_for(c.I, c.J, c.K); }
+int mic0_factor_tiles(int J, int K) { return std::max(1, (J - 2 + FT - 1) / FT) * std::max(1, (K - 2 + FT - 1) / FT); }
 int pressure_partials_for(int I, int J, int K) {
 // One reduction CTA per 4096 grid cells, at most RBLOCKS.  A liquid fills a
 // fraction of the grid, so a thread takes a few rows; a smaller grid spares
@@ -714,25 +810,24 @@ int pressure_project(const StepConsts &c, const PressureArgs &a, PressureBuffers
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        int perSMp = 0;
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_mic0_levels, TPB, 0);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSMp, k_mic0_pencils, TPB, 0);
         int lo_ = lo, hi_ = hi;
         StepConsts c_ = c;
         const uint8_t *fl = pb.fluid;
         const double4 *ad = pb.Ad;
         double *inv = pb.invdiagD;
         void *args[] = {&c_, &fl, &ad, &inv, &lo_, &hi_};
-        // a thread per pencil where one cooperative wave holds them all; the
-        // pivot weights go to q, r and x, which the loop set-up rewrites
-        if (coop && perSMp > 0 && div_up(np, TPB) <= (long long)perSMp * sms) {
-            const double *w0 = pb.q, *w1 = pb.r, *w2 = pb.x;
-            void *pargs[] = {&c_, &fl, &ad, &w0, &w1, &w2, &inv, &lo_, &hi_};
+        // the tiled wavefront; the pivot weights go to q, r and x, which the
+        // loop set-up rewrites
+        {
+            const int ntiles = mic0_factor_tiles(c.J, c.K);
+            PCK(cudaMemsetAsync(pb.factorProgress, 0xff, ntiles * sizeof(int), s));
+            PCK(cudaMemsetAsync(pb.factorTicket, 0, sizeof(unsigned int), s));
             { FLIP_COUNT(1); k_mic0_weights<<<nb, TPB, 0, s>>>(c, pb.fluid, pb.Ad, pb.q, pb.r, pb.x); }
             FLIP_COUNT(1);
-            factored = cudaLaunchCooperativeKernel((const void *)k_mic0_pencils, (int)div_up(np, TPB), TPB, pargs, 0,
-                                                   s) == cudaSuccess;
-            if (!factored) cudaGetLastError();
+            k_mic0_tiles<<<ntiles, FT * FT, 0, s>>>(c, pb.fluid, pb.Ad, pb.q, pb.r, pb.x, pb.invdiagD, lo, hi,
+                                                    pb.factorTicket, pb.factorProgress, sw.err);
+            factored = cudaGetLastError() == cudaSuccess;
         }
         if (!factored && coop && perSM > 0) {
             const int grid = std::max(1, std::min((int)div_up(np, TPB), perSM * sms));
@@ -794,14 +889,15 @@ int pressure_project(const StepConsts &c, const PressureArgs &a, PressureBuffers
     sweep_epoch_guard(c, sw, 2, s);
     precondition(0, tm != nullptr);
     PCK(cudaMemcpyAsync(&mail->rho, pb.scal + 1, sizeof(double), cudaMemcpyDeviceToHost, s));
+    PCK(cudaMemcpyAsync(&mail->sweepErr, sw.err, sizeof(int), cudaMemcpyDeviceToHost, s));
     PCK(sync());
     if (tm) tally_pair(0);
     const double rho0 = mail->rho;
     bool ok = false;
     int iterations = 0;
     double resid = bmax;
-    int sweepErr = 0;
-    if (!(rho0 == 0 || rho0 != rho0)) {
+    int sweepErr = mail->sweepErr;   // the factor's or the first sweep's bounded wait gave up
+    if (!sweepErr && !(rho0 == 0 || rho0 != rho0)) {
         { FLIP_COUNT(1); k_copy_zs<<<rb, TPB, 0, s>>>(pb.fluidIdx, pb.fluidSk, pb.nFluid, pb.z, pb.s); }
         // Iterations go to the device PCG_BATCH at a time, as one CUDA graph
         // (captured on first use, per context): the convergence test runs
@@ -863,7 +959,7 @@ int pressure_project(const StepConsts &c, const PressureArgs &a, PressureBuffers
         cudaMemsetAsync(sw.ticket, 0, 2 * sizeof(unsigned int), s);
         sw.epoch = 0;
         sync();
-        if (errMsg) *errMsg = "a wavefront sweep gave up waiting for a neighbouring tile";
+        if (errMsg) *errMsg = "a wavefront (factor or sweep) gave up waiting for a neighbouring tile";
         return FLIP_E_DEVICE_TIMEOUT;
     }
     res->iterations = iterations;
