@@ -196,15 +196,18 @@ def run_gpu(args, rank, world):
     sweep_ms, sweep_launches, sweep_rows = sim.sweep_times()
     sim.set_stage_timing(False)
 
-    # end to end through the public API with host buffers
+    # end to end through the public API with host buffers: the positions go
+    # into one pinned host buffer, as a caller of the reference's
+    # getMarkerParticlePositionData(char *) passes its own buffer
     d2h = 0
+    host = torch.empty((sim.getNumMarkerParticles(), 3), dtype=torch.float32, pin_memory=True).numpy()
     torch.cuda.synchronize()
     e2e_particles = 0
     t0 = time.perf_counter()
     for k in range(args.steps):
         e2e_particles += sim.getNumMarkerParticles()
         sim.update(FRAME_DT)
-        pos = sim.getMarkerParticlePositionData()
+        pos = sim.getMarkerParticlePositionData(out=host)
         d2h += pos.nbytes
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t0
@@ -242,7 +245,7 @@ def run_gpu(args, rank, world):
                    "parallelism": f"replicas x{world}"},
         "e2e": {"value": round(e2e_value, 4), "unit": UNIT, "h2d_bytes_per_step": 8,
                 "d2h_bytes_per_step": int(d2h / args.steps),
-                "path": "FluidSimulation.update(dt) + getMarkerParticlePositionData() via the C ABI"},
+                "path": "FluidSimulation.update(dt) + getMarkerParticlePositionData(out=pinned host buffer) via the C ABI"},
         "roofline": {"bound": "hbm", "kernel": "k_wavefront (MIC(0) forward + backward sweeps)",
                      "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 5), "traffic": sweep_traffic_per_launch(),

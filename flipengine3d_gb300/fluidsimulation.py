@@ -328,15 +328,27 @@ class FluidSimulation:
         self._c(self._lib.flip_get_num_marker_particles(self._h, C.byref(v)))
         return v.value
 
-    def getMarkerParticlePositionData(self) -> np.ndarray:
-        out = np.zeros((self.getNumMarkerParticles(), 3), np.float32)
-        self._c(self._lib.flip_get_marker_particle_position_data(self._h, _ptr(out)))
-        return out
+    def _readback_buffer(self, out) -> np.ndarray:
+        n = self.getNumMarkerParticles()
+        if out is None:
+            return np.empty((n, 3), np.float32)
+        if (not isinstance(out, np.ndarray) or out.dtype != np.float32 or not out.flags["C_CONTIGUOUS"]
+                or out.size < 3 * n):
+            raise ValueError(f"out must be a C-contiguous float32 array with room for {n} x 3 values")
+        return out.reshape(-1)[: 3 * n].reshape(n, 3)
 
-    def getMarkerParticleVelocityData(self) -> np.ndarray:
-        out = np.zeros((self.getNumMarkerParticles(), 3), np.float32)
-        self._c(self._lib.flip_get_marker_particle_velocity_data(self._h, _ptr(out)))
-        return out
+    def getMarkerParticlePositionData(self, out: np.ndarray | None = None) -> np.ndarray:
+        """Positions in load order, 3 floats each (getMarkerParticlePositionData,
+        fluidsimulation.cpp:2408-2420).  `out`, like the reference's caller
+        buffer, is written in place (a pinned one avoids a staging copy)."""
+        buf = self._readback_buffer(out)
+        self._c(self._lib.flip_get_marker_particle_position_data(self._h, _ptr(buf)))
+        return buf
+
+    def getMarkerParticleVelocityData(self, out: np.ndarray | None = None) -> np.ndarray:
+        buf = self._readback_buffer(out)
+        self._c(self._lib.flip_get_marker_particle_velocity_data(self._h, _ptr(buf)))
+        return buf
 
     def getMarkerParticlePositionDataRange(self, start: int, end: int) -> np.ndarray:
         out = np.zeros((max(end - start, 0), 3), np.float32)

@@ -109,3 +109,21 @@ def test_launches_are_counted(gpu):
         before = sim.launch_count()
         sim.update(sc.frame_dt)
         assert sim.launch_count() > before + 20
+
+
+def test_readback_into_a_caller_buffer(gpu):
+    """getMarkerParticlePositionData(char *) writes into the caller's buffer;
+    the Python mirror takes one as `out` and rejects one that is too small."""
+    sc = dam_break(12, seed=1)
+    with FluidSimulation.from_scene(sc) as sim:
+        sim.update(sc.frame_dt)
+        n = sim.getNumMarkerParticles()
+        ref = sim.getMarkerParticlePositionData()
+        buf = np.full((n + 5, 3), -1.0, np.float32)
+        got = sim.getMarkerParticlePositionData(out=buf)
+        assert np.shares_memory(got, buf) and np.array_equal(got, ref)
+        assert np.all(buf[n:] == -1.0)
+        assert np.array_equal(sim.getMarkerParticleVelocityData(out=np.empty((n, 3), np.float32)),
+                              sim.getMarkerParticleVelocityData())
+        with pytest.raises(ValueError):
+            sim.getMarkerParticlePositionData(out=np.empty((n - 1, 3), np.float32))
