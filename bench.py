@@ -245,7 +245,9 @@ def run_gpu(args, rank, world):
                    "parallelism": f"replicas x{world}"},
         "e2e": {"value": round(e2e_value, 4), "unit": UNIT, "h2d_bytes_per_step": 8,
                 "d2h_bytes_per_step": int(d2h / args.steps),
-                "path": "FluidSimulation.update(dt) + getMarkerParticlePositionData(out=pinned host buffer) via the C ABI"},
+                "path": "FluidSimulation.update(dt) + getMarkerParticlePositionData(out=pinned host buffer) via the C ABI",
+                "timing": "wall clock over back-to-back frames (no L2 flush between them; the step's working set "
+                          "is larger than L2), where `value` flushes L2 between event-timed frames"},
         "roofline": {"bound": "hbm", "kernel": "k_wavefront (MIC(0) forward + backward sweeps)",
                      "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 5), "traffic": sweep_traffic_per_launch(),

@@ -141,6 +141,7 @@ struct PressureBuffers {
     double *b;             // right-hand side (negative divergence)
     double *invdiagD;      // MIC(0) inverse pivots, FP64
     float4 *L;             // {invdiag, Lx, Ly, Lz} for the FP32 sweeps, sweep layout
+    float4 *A2;            // per cell {hi, lo}: the rows as exact float pairs (hi + lo = the FP64 value to 48 bits)
     double *x, *r, *q;     // solution, residual, A s
     float *z;              // preconditioned residual, sweep layout
     float *s;              // search direction

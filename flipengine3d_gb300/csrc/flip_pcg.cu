@@ -148,6 +148,7 @@ __global__ void k_build(StepConsts c, const float *phi, const float *wu, const f
         pb.invdiagD[t] = 0.0;
         if (!pb.fluid[t]) {
             pb.Ad[t] = make_double4(0.0, 0.0, 0.0, 0.0);
+            pb.A2[2 * t] = pb.A2[2 * t + 1] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
             pb.b[t] = 0.0;
         } else {
             int i, j, k;
@@ -166,7 +167,12 @@ __global__ void k_build(StepConsts c, const float *phi, const float *wu, const f
             div += factor * vK * (double)w[dw.idx(i, j, k)];
             pb.b[t] = div;
             bmag = fabs(div);
-            pb.Ad[t] = row_coeffs(c, phi, wu, wv, ww, mf, i, j, k);
+            const double4 a = row_coeffs(c, phi, wu, wv, ww, mf, i, j, k);
+            pb.Ad[t] = a;
+            const float4 hi = make_float4((float)a.x, (float)a.y, (float)a.z, (float)a.w);
+            pb.A2[2 * t] = hi;
+            pb.A2[2 * t + 1] = make_float4((float)(a.x - (double)hi.x), (float)(a.y - (double)hi.y),
+                                           (float)(a.z - (double)hi.z), (float)(a.w - (double)hi.w));
         }
     }
     block_max_to(bmag, (unsigned long long *)pb.scal + 2, false);
@@ -477,10 +483,28 @@ __global__ void k_compact_rows(StepConsts c, SweepLayout g, const uint8_t *fluid
     sk[e] = (int)sweep_index(g, i, j, k);
 }
 
-// q = A s (FP64) over the rows and s.q; the last CTA sums s.q and sets
-// alpha = rho / s.q, rounded to float as BLAS::addScaled takes it
-// (blaswrapper.h:129-158), and clears the iteration's residual norms.
-__global__ void k_spmv(StepConsts c, const int *__restrict__ rows, const int *nRows, const double4 *__restrict__ Ad,
+// Double-float arithmetic on the FP32 pipe (this GPU's FP64 rate is ~1/64
+// of FP32): a coefficient a = hi + lo (floats, exact to 48 bits) times an
+// FP32 s is hi*s exactly as a rounded product plus its FMA-recovered error,
+// plus lo*s; sums carry their rounding errors in a second float (Knuth's
+// TwoSum).  A 7-term row sum is exact to ~2^-48 of its terms, where FP64 is
+// exact to ~2^-53.
+__device__ __forceinline__ void df_mul_add(float ah, float al, float sv, float &sh, float &sl) {
+    const float ph = __fmul_rn(ah, sv);
+    float pl = __fmaf_rn(ah, sv, -ph);   // exact error of ah * sv
+    pl = __fmaf_rn(al, sv, pl);
+    const float t = __fadd_rn(sh, ph);
+    const float bb = __fsub_rn(t, sh);
+    const float err = __fadd_rn(__fsub_rn(sh, __fsub_rn(t, bb)), __fsub_rn(ph, bb));   // exact error of sh + ph
+    sl = __fadd_rn(sl, __fadd_rn(err, pl));
+    sh = t;
+}
+
+// q = A s over the rows, in double-float, then stored in FP64; s.q in FP64.
+// The last CTA sums s.q and sets alpha = rho / s.q, rounded to float as
+// BLAS::addScaled takes it (blaswrapper.h:129-158), and clears the
+// iteration's residual norms.
+__global__ void k_spmv(StepConsts c, const int *__restrict__ rows, const int *nRows, const float4 *__restrict__ A2,
                        const float *__restrict__ s, double *__restrict__ q, double *partials, double *scal,
                        unsigned long long *rmaxBits, PcgCtl *ctl) {
     __shared__ double sh[32];
@@ -490,16 +514,19 @@ __global__ void k_spmv(StepConsts c, const int *__restrict__ rows, const int *nR
     double part = 0.0;
     for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
         const long long t = rows[e];
-        const double4 a = Ad[t];
-        double acc = a.x * (double)s[t];
-        acc = fma(a.y, (double)s[t + 1], acc);
-        acc = fma(a.z, (double)s[t + sy], acc);
-        acc = fma(a.w, (double)s[t + sz], acc);
-        acc = fma(Ad[t - 1].y, (double)s[t - 1], acc);
-        acc = fma(Ad[t - sy].z, (double)s[t - sy], acc);
-        acc = fma(Ad[t - sz].w, (double)s[t - sz], acc);
+        const float4 hi = A2[2 * t], lo = A2[2 * t + 1];
+        const float st = s[t];
+        float accH = 0.0f, accL = 0.0f;
+        df_mul_add(hi.x, lo.x, st, accH, accL);
+        df_mul_add(hi.y, lo.y, s[t + 1], accH, accL);
+        df_mul_add(hi.z, lo.z, s[t + sy], accH, accL);
+        df_mul_add(hi.w, lo.w, s[t + sz], accH, accL);
+        df_mul_add(A2[2 * (t - 1)].y, A2[2 * (t - 1) + 1].y, s[t - 1], accH, accL);
+        df_mul_add(A2[2 * (t - sy)].z, A2[2 * (t - sy) + 1].z, s[t - sy], accH, accL);
+        df_mul_add(A2[2 * (t - sz)].w, A2[2 * (t - sz) + 1].w, s[t - sz], accH, accL);
+        const double acc = (double)accH + (double)accL;
         q[t] = acc;
-        part = fma((double)s[t], acc, part);
+        part = fma((double)st, acc, part);
     }
     double b = block_sum(part, sh);
     if (threadIdx.x == 0) partials[blockIdx.x] = b;
@@ -873,7 +900,7 @@ int pressure_project(const StepConsts &c, const PressureArgs &a, PressureBuffers
     // one PCG iteration (pcgsolver.h:263-300); every launch is the same for
     // every iteration, the iteration index lives on the device
     auto iteration = [&](int k, bool timed) {
-        { FLIP_COUNT(1); k_spmv<<<rb, TPB, 0, s>>>(c, pb.fluidIdx, pb.nFluid, pb.Ad, pb.s, pb.q, pb.partials, pb.scal, rmax, pb.ctl); }
+        { FLIP_COUNT(1); k_spmv<<<rb, TPB, 0, s>>>(c, pb.fluidIdx, pb.nFluid, pb.A2, pb.s, pb.q, pb.partials, pb.scal, rmax, pb.ctl); }
         { FLIP_COUNT(1); k_update_xr<<<rb, TPB, 0, s>>>(pb.fluidIdx, pb.fluidSk, pb.nFluid, pb.x, pb.r, pb.rf, pb.s, pb.q, pb.scal, rmax, pb.ctl); }
         { FLIP_COUNT(1); k_true_residual<<<rb, TPB, 0, s>>>(c, pb.fluidIdx, pb.fluidSk, pb.nFluid, pb.Ad, pb.b, pb.x, pb.r, pb.rf, rmax + 1, pb.scal, pb.ctl, 0); }
         { FLIP_COUNT(1); k_true_residual<<<rb, TPB, 0, s>>>(c, pb.fluidIdx, pb.fluidSk, pb.nFluid, pb.Ad, pb.b, pb.x, pb.r, pb.rf, rmax + 1, pb.scal, pb.ctl, 1); }
