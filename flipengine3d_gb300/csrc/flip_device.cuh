@@ -142,7 +142,7 @@ struct PressureBuffers {
     double *invdiagD;      // MIC(0) inverse pivots, FP64
     float4 *L;             // {invdiag, Lx, Ly, Lz} for the FP32 sweeps, sweep layout
     float4 *A2;            // per cell {hi, lo}: the rows as exact float pairs (hi + lo = the FP64 value to 48 bits)
-    double *x, *r, *q;     // solution, residual, A s
+    float2 *x, *r, *q;     // solution, residual, A s: exact float pairs {hi, lo} (hi + lo to ~48 bits)
     float *z;              // preconditioned residual, sweep layout
     float *s;              // search direction
     float *rf;             // r rounded to FP32, the forward sweep's right-hand side, sweep layout

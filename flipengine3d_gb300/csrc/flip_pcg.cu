@@ -141,9 +141,9 @@ __global__ void k_build(StepConsts c, const float *phi, const float *wu, const f
     Dims d{c.I, c.J, c.K};
     double bmag = 0.0;
     if (t < d.size()) {
-        pb.x[t] = 0.0;
-        pb.r[t] = 0.0;
-        pb.q[t] = 0.0;
+        pb.x[t] = make_float2(0.0f, 0.0f);
+        pb.r[t] = make_float2(0.0f, 0.0f);
+        pb.q[t] = make_float2(0.0f, 0.0f);
         pb.s[t] = 0.0f;
         pb.invdiagD[t] = 0.0;
         if (!pb.fluid[t]) {
@@ -489,6 +489,30 @@ __global__ void k_compact_rows(StepConsts c, SweepLayout g, const uint8_t *fluid
 // plus lo*s; sums carry their rounding errors in a second float (Knuth's
 // TwoSum).  A 7-term row sum is exact to ~2^-48 of its terms, where FP64 is
 // exact to ~2^-53.
+__device__ __forceinline__ float2 df_from(double v) {
+    const float h = (float)v;
+    return make_float2(h, (float)(v - (double)h));
+}
+__device__ __forceinline__ double df_to(float2 v) { return (double)v.x + (double)v.y; }
+// (h, l) with h = fl(h + l): the pair in normalised form (|l| <= ulp(h) / 2)
+__device__ __forceinline__ float2 df_norm(float h, float l) {
+    const float s = __fadd_rn(h, l);
+    return make_float2(s, __fsub_rn(l, __fsub_rn(s, h)));
+}
+// a + b for pairs: TwoSum of the leading parts, the rest added to the error
+__device__ __forceinline__ float2 df_add(float2 a, float2 b) {
+    const float t = __fadd_rn(a.x, b.x);
+    const float bb = __fsub_rn(t, a.x);
+    const float err = __fadd_rn(__fsub_rn(a.x, __fsub_rn(t, bb)), __fsub_rn(b.x, bb));
+    return df_norm(t, __fadd_rn(err, __fadd_rn(a.y, b.y)));
+}
+// f * v for a float f and a pair v: the leading product exact as its
+// rounded value plus its FMA-recovered error
+__device__ __forceinline__ float2 df_scale(float f, float2 v) {
+    const float ph = __fmul_rn(f, v.x);
+    const float pl = __fmaf_rn(f, v.y, __fmaf_rn(f, v.x, -ph));
+    return make_float2(ph, pl);
+}
 __device__ __forceinline__ void df_mul_add(float ah, float al, float sv, float &sh, float &sl) {
     const float ph = __fmul_rn(ah, sv);
     float pl = __fmaf_rn(ah, sv, -ph);   // exact error of ah * sv
@@ -500,18 +524,18 @@ __device__ __forceinline__ void df_mul_add(float ah, float al, float sv, float &
     sh = t;
 }
 
-// q = A s over the rows, in double-float, then stored in FP64; s.q in FP64.
-// The last CTA sums s.q and sets alpha = rho / s.q, rounded to float as
-// BLAS::addScaled takes it (blaswrapper.h:129-158), and clears the
-// iteration's residual norms.
+// q = A s over the rows in double-float, stored as a pair; s.q summed in
+// double-float per thread and in FP64 across threads.  The last CTA sums s.q
+// and sets alpha = rho / s.q, rounded to float as BLAS::addScaled takes it
+// (blaswrapper.h:129-158), and clears the iteration's residual norms.
 __global__ void k_spmv(StepConsts c, const int *__restrict__ rows, const int *nRows, const float4 *__restrict__ A2,
-                       const float *__restrict__ s, double *__restrict__ q, double *partials, double *scal,
+                       const float *__restrict__ s, float2 *__restrict__ q, double *partials, double *scal,
                        unsigned long long *rmaxBits, PcgCtl *ctl) {
     __shared__ double sh[32];
     if (ctl->done) return;
     const int n = *nRows;
     const long long sy = c.I, sz = (long long)c.I * c.J;
-    double part = 0.0;
+    float2 dot = make_float2(0.0f, 0.0f);
     for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
         const long long t = rows[e];
         const float4 hi = A2[2 * t], lo = A2[2 * t + 1];
@@ -524,11 +548,11 @@ __global__ void k_spmv(StepConsts c, const int *__restrict__ rows, const int *nR
         df_mul_add(A2[2 * (t - 1)].y, A2[2 * (t - 1) + 1].y, s[t - 1], accH, accL);
         df_mul_add(A2[2 * (t - sy)].z, A2[2 * (t - sy) + 1].z, s[t - sy], accH, accL);
         df_mul_add(A2[2 * (t - sz)].w, A2[2 * (t - sz) + 1].w, s[t - sz], accH, accL);
-        const double acc = (double)accH + (double)accL;
-        q[t] = acc;
-        part = fma((double)st, acc, part);
+        const float2 qt = df_norm(accH, accL);
+        q[t] = qt;
+        dot = df_add(dot, df_scale(st, qt));
     }
-    double b = block_sum(part, sh);
+    double b = block_sum(df_to(dot), sh);
     if (threadIdx.x == 0) partials[blockIdx.x] = b;
     if (last_cta(&ctl->ticket[0])) {
         const double sq = sum_partials_fixed(partials, gridDim.x, sh);
@@ -545,15 +569,15 @@ __global__ void k_spmv(StepConsts c, const int *__restrict__ rows, const int *nR
 // sets beta = rho_new / rho as float (pcgsolver.h:295-298) and ends the
 // iteration: rho = rho_new, next iteration index.
 __global__ void k_dot_zr(const int *__restrict__ rows, const int *__restrict__ rowsSk, const int *nRows,
-                         const float *__restrict__ z, const double *__restrict__ r, double *partials, double *scal,
+                         const float *__restrict__ z, const float2 *__restrict__ r, double *partials, double *scal,
                          PcgCtl *ctl, int inLoop) {
     __shared__ double sh[32];
     if (ctl->done) return;
     const int n = *nRows;
-    double part = 0.0;
+    float2 dot = make_float2(0.0f, 0.0f);   // double-float per thread, FP64 across threads
     for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x)
-        part = fma((double)z[rowsSk[e]], r[rows[e]], part);
-    double s = block_sum(part, sh);
+        dot = df_add(dot, df_scale(z[rowsSk[e]], r[rows[e]]));
+    double s = block_sum(df_to(dot), sh);
     if (threadIdx.x == 0) partials[blockIdx.x] = s;
     if (last_cta(&ctl->ticket[1])) {
         const double zr = sum_partials_fixed(partials, gridDim.x, sh);
@@ -590,23 +614,23 @@ __device__ __forceinline__ void convergence_test(PcgCtl *ctl, double resid, doub
 // BLAS::addScaled(float alpha, ...) does (blaswrapper.h:129-158); |r|inf,
 // tested by the last CTA except on the iterations of the periodic recompute
 __global__ void k_update_xr(const int *__restrict__ rows, const int *__restrict__ rowsSk, const int *nRows,
-                            double *__restrict__ x, double *__restrict__ r, float *__restrict__ rf,
-                            const float *__restrict__ s, const double *__restrict__ q, const double *scal,
+                            float2 *__restrict__ x, float2 *__restrict__ r, float *__restrict__ rf,
+                            const float *__restrict__ s, const float2 *__restrict__ q, const double *scal,
                             unsigned long long *rmaxBits, PcgCtl *ctl) {
     if (ctl->done) return;
     const int n = *nRows;
-    const double alpha = scal[4];
-    double m = 0.0;
+    const float alpha = (float)scal[4];   // exact: alpha is a float value
+    float m = 0.0f;
     for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
         const int t = rows[e];
-        x[t] = fma(alpha, (double)s[t], x[t]);
-        const double rv = fma(-alpha, q[t], r[t]);
+        x[t] = df_add(x[t], df_scale(alpha, make_float2(s[t], 0.0f)));   // alpha s is exact as a pair
+        const float2 rv = df_add(r[t], df_scale(-alpha, q[t]));
         r[t] = rv;
-        rf[rowsSk[e]] = (float)rv;
-        const double av = fabs(rv);
+        rf[rowsSk[e]] = rv.x;   // normalised: the pair rounded to float
+        const float av = fabsf(rv.x);
         m = (av != av || av > m) ? av : m;   // a NaN sticks
     }
-    block_max_to(m, rmaxBits);
+    block_max_to((double)m, rmaxBits);
     if (last_cta(&ctl->ticket[2]) && threadIdx.x == 0 && (ctl->it + 1) % 25 != 0)
         convergence_test(ctl, bits_to_resid(rmaxBits), scal[6], false);
 }
@@ -617,7 +641,7 @@ __global__ void k_update_xr(const int *__restrict__ rows, const int *__restrict_
 // 1 when the recurrence just claimed convergence; never once converged.
 __global__ void k_true_residual(StepConsts c, const int *__restrict__ rows, const int *__restrict__ rowsSk,
                                 const int *nRows, const double4 *__restrict__ Ad, const double *__restrict__ b,
-                                const double *__restrict__ x, double *__restrict__ r, float *__restrict__ rf,
+                                const float2 *__restrict__ x, float2 *__restrict__ r, float *__restrict__ rf,
                                 unsigned long long *rmaxBits, const double *scal, PcgCtl *ctl, int mode) {
     if (ctl->done) return;
     if (mode == 0 ? (ctl->it + 1) % 25 != 0 : !ctl->claim) return;
@@ -627,16 +651,17 @@ __global__ void k_true_residual(StepConsts c, const int *__restrict__ rows, cons
     for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
         const long long t = rows[e];
         const double4 a = Ad[t];
-        double ax = a.x * x[t];
-        ax = fma(a.y, x[t + 1], ax);
-        ax = fma(a.z, x[t + sy], ax);
-        ax = fma(a.w, x[t + sz], ax);
-        ax = fma(Ad[t - 1].y, x[t - 1], ax);
-        ax = fma(Ad[t - sy].z, x[t - sy], ax);
-        ax = fma(Ad[t - sz].w, x[t - sz], ax);
+        double ax = a.x * df_to(x[t]);
+        ax = fma(a.y, df_to(x[t + 1]), ax);
+        ax = fma(a.z, df_to(x[t + sy]), ax);
+        ax = fma(a.w, df_to(x[t + sz]), ax);
+        ax = fma(Ad[t - 1].y, df_to(x[t - 1]), ax);
+        ax = fma(Ad[t - sy].z, df_to(x[t - sy]), ax);
+        ax = fma(Ad[t - sz].w, df_to(x[t - sz]), ax);
         const double rv = b[t] - ax;
-        r[t] = rv;
-        rf[rowsSk[e]] = (float)rv;
+        const float2 rp = df_from(rv);
+        r[t] = rp;
+        rf[rowsSk[e]] = rp.x;
         const double av = fabs(rv);
         m = (av != av || av > m) ? av : m;
     }
@@ -645,14 +670,14 @@ __global__ void k_true_residual(StepConsts c, const int *__restrict__ rows, cons
 }
 
 // r = b (and its FP32 copy in the sweep layout), x = 0, |b|inf
-__global__ void k_init_r(StepConsts c, SweepLayout g, const double *b, double *r, float *rf, double *x,
+__global__ void k_init_r(StepConsts c, SweepLayout g, const double *b, float2 *r, float *rf, float2 *x,
                          unsigned long long *rmaxBits) {
     const long long n = (long long)c.I * c.J * c.K;
     double m = 0.0;
 #pragma unroll 4
     for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
-        r[t] = b[t];
-        x[t] = 0.0;
+        r[t] = df_from(b[t]);
+        x[t] = make_float2(0.0f, 0.0f);
         int i, j, k;
     unflatten(t, c.I, c.J, i, j, k);
         if (i >= 1 && j >= 1 && k >= 1 && i <= c.I - 2 && j <= c.J - 2 && k <= c.K - 2)
@@ -682,9 +707,9 @@ __global__ void k_copy_zs(const int *__restrict__ rows, const int *__restrict__ 
     for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) s[rows[e]] = z[rowsSk[e]];
 }
 
-__global__ void k_x_to_float(long long n, const double *x, float *p) {
+__global__ void k_x_to_float(long long n, const float2 *x, float *p) {
     long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t < n) p[t] = (float)x[t];
+    if (t < n) p[t] = (float)df_to(x[t]);
 }
 
 // _applyPressureToVelocityFieldThread (pressuresolver.cpp:896-1046) without
@@ -850,9 +875,12 @@ int pressure_project(const StepConsts &c, const PressureArgs &a, PressureBuffers
             const int ntiles = mic0_factor_tiles(c.J, c.K);
             PCK(cudaMemsetAsync(pb.factorProgress, 0xff, ntiles * sizeof(int), s));
             PCK(cudaMemsetAsync(pb.factorTicket, 0, sizeof(unsigned int), s));
-            { FLIP_COUNT(1); k_mic0_weights<<<nb, TPB, 0, s>>>(c, pb.fluid, pb.Ad, pb.q, pb.r, pb.x); }
+            // scratch: the 8-byte pair arrays q, r, x as FP64 arrays
+            double *w0 = reinterpret_cast<double *>(pb.q), *w1 = reinterpret_cast<double *>(pb.r),
+                   *w2 = reinterpret_cast<double *>(pb.x);
+            { FLIP_COUNT(1); k_mic0_weights<<<nb, TPB, 0, s>>>(c, pb.fluid, pb.Ad, w0, w1, w2); }
             FLIP_COUNT(1);
-            k_mic0_tiles<<<ntiles, FT * FT, 0, s>>>(c, pb.fluid, pb.Ad, pb.q, pb.r, pb.x, pb.invdiagD, lo, hi,
+            k_mic0_tiles<<<ntiles, FT * FT, 0, s>>>(c, pb.fluid, pb.Ad, w0, w1, w2, pb.invdiagD, lo, hi,
                                                     pb.factorTicket, pb.factorProgress, sw.err);
             factored = cudaGetLastError() == cudaSuccess;
         }
