@@ -8,9 +8,12 @@
 // pivot floor 0.25) restated for 7-point rows; the factorisation runs as an
 // i+j+k wavefront in FP64 and the two triangular sweeps as the pipelined
 // FP32 wavefront of flip_wavefront.cu.  CG (pcgsolver.h:248-302): the
-// Laplacian apply, the solution, the residual and the dot products are
-// FP64, so the recurrence tracks b - A x to FP64 rounding; the FP32 parts
-// (preconditioner, search direction) only steer the iteration.  Every 25
+// Laplacian apply, the solution and the residual are double-float (exact
+// float pairs, ~48 bits, on the FP32 pipe; this GPU's FP64 rate is ~1/64 of
+// FP32) and the dot products are summed in double-float per thread and FP64
+// across threads, so the recurrence tracks b - A x to far below the
+// tolerance; the FP32 parts (preconditioner, search direction) only steer
+// the iteration.  Every 25
 // iterations, and whenever the recurrence reports convergence, the residual
 // is recomputed as b - A x (iterative refinement), and convergence is
 // decided on it, with the reference's test |r|inf <= tol * |b|inf.
