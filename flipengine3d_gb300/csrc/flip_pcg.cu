@@ -639,15 +639,16 @@ __global__ void k_update_xr(const int *__restrict__ rows, const int *__restrict_
 }
 
 // r = b - A x (residual replacement); |r|inf, which the last CTA tests as
-// final.  Inside the loop it runs only when needed: mode 0 on every 25th
-// iteration (pcgsolver.h's periodic recompute, here before the test), mode
-// 1 when the recurrence just claimed convergence; never once converged.
+// final.  Inside the loop it runs only when needed: on every 25th iteration
+// (pcgsolver.h's periodic recompute, here before the test) and when the
+// recurrence just claimed convergence (a claim is only made on the other
+// iterations, so one launch serves both); never once converged.
 __global__ void k_true_residual(StepConsts c, const int *__restrict__ rows, const int *__restrict__ rowsSk,
                                 const int *nRows, const double4 *__restrict__ Ad, const double *__restrict__ b,
                                 const float2 *__restrict__ x, float2 *__restrict__ r, float *__restrict__ rf,
-                                unsigned long long *rmaxBits, const double *scal, PcgCtl *ctl, int mode) {
+                                unsigned long long *rmaxBits, const double *scal, PcgCtl *ctl) {
     if (ctl->done) return;
-    if (mode == 0 ? (ctl->it + 1) % 25 != 0 : !ctl->claim) return;
+    if ((ctl->it + 1) % 25 != 0 && !ctl->claim) return;
     const int n = *nRows;
     const long long sy = c.I, sz = (long long)c.I * c.J;
     double m = 0.0;
@@ -669,7 +670,7 @@ __global__ void k_true_residual(StepConsts c, const int *__restrict__ rows, cons
         m = (av != av || av > m) ? av : m;
     }
     block_max_to(m, rmaxBits);
-    if (last_cta(&ctl->ticket[3 + mode]) && threadIdx.x == 0) convergence_test(ctl, bits_to_resid(rmaxBits), scal[6], true);
+    if (last_cta(&ctl->ticket[3]) && threadIdx.x == 0) convergence_test(ctl, bits_to_resid(rmaxBits), scal[6], true);
 }
 
 // r = b (and its FP32 copy in the sweep layout), x = 0, |b|inf
@@ -933,8 +934,7 @@ int pressure_project(const StepConsts &c, const PressureArgs &a, PressureBuffers
     auto iteration = [&](int k, bool timed) {
         { FLIP_COUNT(1); k_spmv<<<rb, TPB, 0, s>>>(c, pb.fluidIdx, pb.nFluid, pb.A2, pb.s, pb.q, pb.partials, pb.scal, rmax, pb.ctl); }
         { FLIP_COUNT(1); k_update_xr<<<rb, TPB, 0, s>>>(pb.fluidIdx, pb.fluidSk, pb.nFluid, pb.x, pb.r, pb.rf, pb.s, pb.q, pb.scal, rmax, pb.ctl); }
-        { FLIP_COUNT(1); k_true_residual<<<rb, TPB, 0, s>>>(c, pb.fluidIdx, pb.fluidSk, pb.nFluid, pb.Ad, pb.b, pb.x, pb.r, pb.rf, rmax + 1, pb.scal, pb.ctl, 0); }
-        { FLIP_COUNT(1); k_true_residual<<<rb, TPB, 0, s>>>(c, pb.fluidIdx, pb.fluidSk, pb.nFluid, pb.Ad, pb.b, pb.x, pb.r, pb.rf, rmax + 1, pb.scal, pb.ctl, 1); }
+        { FLIP_COUNT(1); k_true_residual<<<rb, TPB, 0, s>>>(c, pb.fluidIdx, pb.fluidSk, pb.nFluid, pb.Ad, pb.b, pb.x, pb.r, pb.rf, rmax + 1, pb.scal, pb.ctl); }
         precondition(1 + k, timed);
         { FLIP_COUNT(1); k_update_s<<<rb, TPB, 0, s>>>(pb.fluidIdx, pb.fluidSk, pb.nFluid, pb.z, pb.s, pb.scal, pb.ctl); }
     };
