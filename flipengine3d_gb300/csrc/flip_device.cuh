@@ -126,7 +126,7 @@ struct PcgCtl {
     int iters;     // iterations to convergence
     int claim;     // the recurrence residual passed the test; b - A x must confirm
     int it;        // index of the iteration being run
-    unsigned int ticket[5];   // per reduction kernel: CTAs done (the last one finishes it)
+    unsigned int ticket[4];   // per reduction kernel (spmv, dot_zr, update_xr, true residual): CTAs done
     double resid;  // last residual norm tested
 };
 constexpr int PCG_BATCH = 8;   // iterations enqueued between host checks
