@@ -386,9 +386,8 @@ def cpu_sample_sim(args, threads):
     sc = make_scene(args.scene)
     if refsim.available("ref"):
         kind, cls = "reference", refsim.RefSimulation
-    else:
+    else:   # the C++ restatement, threaded where the reference threads
         kind, cls = "port", refsim.OracleSimulation
-        threads = 1
     sim = cls(sc.isize, sc.jsize, sc.ksize, sc.dx, threads=threads).setup(sc)
     return sc, sim, kind, threads
 

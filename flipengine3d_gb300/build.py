@@ -23,7 +23,7 @@ LIBNAME = "libflip3d_gb300.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "--fmad=false", "-Xcompiler", "-fPIC,-ffp-contract=off",
               "-I", str(ROOT / "include")]
-CXX_FLAGS = ["-std=c++17", "-O2", "-fPIC", "-ffp-contract=off"]
+CXX_FLAGS = ["-std=c++17", "-O2", "-fPIC", "-ffp-contract=off", "-pthread"]
 
 
 def _nvcc() -> str:

@@ -1,10 +1,14 @@
 // CPU oracle for one FLIP step -- TEST INFRASTRUCTURE ONLY (the checker).
 //
-// A restatement, in plain single-threaded C++, of the hot path of the
-// reference engine (jklae/FLIPEngine3D, src/engine = FLIP Fluids 1.0.9b).
-// Every stage keeps the reference's arithmetic types and operation order so
-// that, on the same inputs and the same reduction partition count, its
-// results equal the reference engine's bit for bit.  Each function cites the
+// A restatement, in plain C++, of the hot path of the reference engine
+// (jklae/FLIPEngine3D, src/engine = FLIP Fluids 1.0.9b).  Every stage keeps
+// the reference's arithmetic types and operation order so that, on the same
+// inputs and the same reduction partition count, its results equal the
+// reference engine's bit for bit.  With more than one thread, the loops
+// whose iterations write disjoint outputs (blocks of the level set and of
+// P2G, particles, extrapolated cells, matrix rows, vector elements, dot
+// product partitions) run on threads, as the reference runs them; the
+// triangular sweeps and the factorisation stay sequential.  Each function cites the
 // reference file:line it restates.  Compile with -ffp-contract=off so no
 // multiply-add is fused on any host (the reference's x86-64 -O2 build fuses
 // none).
@@ -14,6 +18,7 @@
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <thread>
 #include <vector>
 
 namespace orc {
@@ -88,6 +93,22 @@ static std::vector<int> splitRange(int b, int e, int n) {
         cur = end;
     }
     return out;
+}
+
+// f(begin, end) over [0, n) in nt contiguous ranges, one thread each (the
+// caller takes the first); only for loops whose iterations are independent.
+template <class F>
+static void parallel_ranges(int n, int nt, F f) {
+    nt = std::max(1, std::min(nt, n));
+    if (nt == 1) {
+        if (n > 0) f(0, n);
+        return;
+    }
+    std::vector<int> iv = splitRange(0, n, nt);
+    std::vector<std::thread> ts;
+    for (int t = 1; t < nt; t++) ts.emplace_back(f, iv[t], iv[t + 1]);
+    f(iv[0], iv[1]);
+    for (auto &th : ts) th.join();
 }
 
 // ------------------------------------------------------ level-set helpers
@@ -406,11 +427,13 @@ struct Sim {
             V3 p = parts[n].p;
             blockLists(p, sr, blockdx, active, lists, n);
         }
-        for (int k = 0; k < bk; k++)
-            for (int j = 0; j < bj; j++)
-                for (int i = 0; i < bi; i++) {
-                    auto &L = lists[active.idx(i, j, k)];
-                    if (!active(i, j, k) || L.empty()) continue;
+        std::vector<int> work;   // blocks with particles, in block order
+        for (int id = 0; id < (int)active.a.size(); id++)
+            if (active.a[id] && !lists[id].empty()) work.push_back(id);
+        parallel_ranges((int)work.size(), nthreads, [&](int w0, int w1) {
+            for (int wq = w0; wq < w1; wq++) {
+                    const int id = work[wq], i = id % bi, j = (id / bi) % bj, k = id / (bi * bj);
+                    auto &L = lists[id];
                     float data[1000];
                     for (int q = 0; q < 1000; q++) data[q] = (float)(3.0 * dx);
                     V3 off = idxToPos(i, j, k, (double)bw * dx);
@@ -434,7 +457,8 @@ struct Sim {
                         int gi = i * bw + a, gj = j * bw + b, gk = k * bw + c;
                         if (phi.in(gi, gj, gk)) phi(gi, gj, gk) = data[q];
                     }
-                }
+            }
+        });
     }
 
     static void feather26(Grid<uint8_t> &g) {
@@ -528,11 +552,13 @@ struct Sim {
         float coef1 = (4.0f / 9.0f) * (1.0f / (r * r * r * r * r * r));
         float coef2 = (17.0f / 9.0f) * (1.0f / (r * r * r * r));
         float coef3 = (22.0f / 9.0f) * (1.0f / (r * r));
-        for (int k = 0; k < bk; k++)
-            for (int j = 0; j < bj; j++)
-                for (int i = 0; i < bi; i++) {
-                    auto &L = lists[active.idx(i, j, k)];
-                    if (!active(i, j, k) || L.empty()) continue;
+        std::vector<int> work;   // blocks with particles, in block order
+        for (int id = 0; id < (int)active.a.size(); id++)
+            if (active.a[id] && !lists[id].empty()) work.push_back(id);
+        parallel_ranges((int)work.size(), nthreads, [&](int w0, int w1) {
+            for (int wq = w0; wq < w1; wq++) {
+                    const int id = work[wq], i = id % bi, j = (id / bi) % bj, k = id / (bi * bj);
+                    auto &L = lists[id];
                     float sc[1000], wt[1000];
                     for (int q = 0; q < 1000; q++) sc[q] = wt[q] = 0.0f;
                     V3 boff = idxToPos(i, j, k, (double)cw * dx);
@@ -567,14 +593,15 @@ struct Sim {
                             if (wt[q] > eps) valid(gi, gj, gk) = 1;
                         }
                     }
-                }
+            }
+        });
     }
 
     // ------------------------------- extrapolation (gridutils.cpp:32-228)
     // Layered BFS: layer L fills unknown cells next to the cells known
     // before it with the mean of their finished neighbours; border cells of
     // the grid count as finished from the start.
-    static void extrapolate(Grid<float> &G, const Grid<uint8_t> &valid, int layers) {
+    static void extrapolate(Grid<float> &G, const Grid<uint8_t> &valid, int layers, int nt) {
         const uint8_t UNKNOWN = 0, WAITING = 1, KNOWN = 2, DONE = 3;
         Grid<uint8_t> st; st.init(G.ni, G.nj, G.nk, UNKNOWN);
         for (int k = 0; k < G.nk; k++)
@@ -595,15 +622,19 @@ struct Sim {
                             if (st(n.i, n.j, n.k) == UNKNOWN) { st(n.i, n.j, n.k) = WAITING; cells.push_back(n); }
                         st(i, j, k) = DONE;
                     }
-            for (auto &g : cells) {
-                float sum = 0.0f;
-                int count = 0;
-                GI nb[6] = {{g.i + 1, g.j, g.k}, {g.i - 1, g.j, g.k}, {g.i, g.j + 1, g.k},
-                            {g.i, g.j - 1, g.k}, {g.i, g.j, g.k + 1}, {g.i, g.j, g.k - 1}};
-                for (auto &n : nb)
-                    if (st(n.i, n.j, n.k) == DONE) { sum += G(n.i, n.j, n.k); count++; }
-                G(g.i, g.j, g.k) = sum / (float)count;
-            }
+            // the layer's cells read only DONE cells, which the layer does not write
+            parallel_ranges((int)cells.size(), nt, [&](int c0, int c1) {
+                for (int q = c0; q < c1; q++) {
+                    const GI g = cells[q];
+                    float sum = 0.0f;
+                    int count = 0;
+                    GI nb[6] = {{g.i + 1, g.j, g.k}, {g.i - 1, g.j, g.k}, {g.i, g.j + 1, g.k},
+                                {g.i, g.j - 1, g.k}, {g.i, g.j, g.k + 1}, {g.i, g.j, g.k - 1}};
+                    for (auto &n : nb)
+                        if (st(n.i, n.j, n.k) == DONE) { sum += G(n.i, n.j, n.k); count++; }
+                    G(g.i, g.j, g.k) = sum / (float)count;
+                }
+            });
             if (l != layers - 1)
                 for (auto &g : cells) st(g.i, g.j, g.k) = KNOWN;
         }
@@ -611,9 +642,9 @@ struct Sim {
 
     void extrapolateMAC() {
         int layers = (int)std::ceil(cfl) + 2;    // fluidsimulation.cpp:3775-3779
-        extrapolate(u, vu, layers);
-        extrapolate(v, vv, layers);
-        extrapolate(w, vw, layers);
+        extrapolate(u, vu, layers, nthreads);
+        extrapolate(v, vv, layers, nthreads);
+        extrapolate(w, vw, layers, nthreads);
     }
 
     // ----------------------------- body forces (fluidsimulation.cpp:3450-3489)
@@ -638,12 +669,16 @@ struct Sim {
             return s;
         }
         std::vector<int> iv = splitRange(0, n, nt);
+        std::vector<double> parts_(nt, 0.0);
+        parallel_ranges(nt, nt, [&](int t0, int t1) {   // one partition per thread
+            for (int t = t0; t < t1; t++) {
+                double part = 0;
+                for (int i = iv[t]; i < iv[t + 1]; i++) part += x[i] * y[i];
+                parts_[t] = part;
+            }
+        });
         double s = 0;
-        for (int t = 0; t < nt; t++) {
-            double part = 0;
-            for (int i = iv[t]; i < iv[t + 1]; i++) part += x[i] * y[i];
-            s += part;
-        }
+        for (int t = 0; t < nt; t++) s += parts_[t];
         return s;
     }
     static double absmax(const std::vector<double> &x) {
@@ -782,13 +817,17 @@ struct Sim {
             } while (i != 0);
         };
         auto spmv = [&](const std::vector<double> &x, std::vector<double> &out) {
-            for (int i = 0; i < n; i++) {
-                out[i] = 0;
-                for (int q = 0; q < A[i].nnz; q++) out[i] += A[i].val[q] * x[A[i].col[q]];
-            }
+            parallel_ranges(n, nthreads, [&](int i0, int i1) {
+                for (int i = i0; i < i1; i++) {
+                    out[i] = 0;
+                    for (int q = 0; q < A[i].nnz; q++) out[i] += A[i].val[q] * x[A[i].col[q]];
+                }
+            });
         };
         auto addScaled = [&](float alpha, const std::vector<double> &x, std::vector<double> &y) {
-            for (int i = 0; i < n; i++) y[i] += alpha * x[i];
+            parallel_ranges(n, nthreads, [&](int i0, int i1) {
+                for (int i = i0; i < i1; i++) y[i] += alpha * x[i];
+            });
         };
         // PCGSolver::solve (pcgsolver.h:248-302)
         std::vector<double> x(n, 0.0), r = b, z(n), s(n);
@@ -979,11 +1018,14 @@ struct Sim {
 
     // ------------------------------------------- G2P (fluidsimulation.cpp:4082-4092)
     void updateParticleVelocities() {
-        for (auto &pt : parts) {
-            V3 vPIC = evalVel(u, v, w, pt.p);
-            V3 vFLIP = (pt.v + vPIC) - evalVel(su, sv, sw, pt.p);
-            pt.v = (float)picRatio * vPIC + (float)(1 - picRatio) * vFLIP;
-        }
+        parallel_ranges((int)parts.size(), nthreads, [&](int p0, int p1) {
+            for (int q = p0; q < p1; q++) {
+                Particle &pt = parts[q];
+                V3 vPIC = evalVel(u, v, w, pt.p);
+                V3 vFLIP = (pt.v + vPIC) - evalVel(su, sv, sw, pt.p);
+                pt.v = (float)picRatio * vPIC + (float)(1 - picRatio) * vFLIP;
+            }
+        });
     }
 
     // ------------------------------------------- advection (4191-4296)
@@ -1069,8 +1111,9 @@ struct Sim {
     void advance(double dt, std::vector<V3> *posAdv) {
         Box boundary = collisionBox();
         std::vector<V3> out(parts.size());
-        for (size_t q = 0; q < parts.size(); q++) out[q] = rk3(parts[q].p, dt);
-        for (size_t q = 0; q < parts.size(); q++) out[q] = resolveCollision(parts[q].p, out[q], boundary);
+        parallel_ranges((int)parts.size(), nthreads, [&](int p0, int p1) {
+            for (int q = p0; q < p1; q++) out[q] = resolveCollision(parts[q].p, rk3(parts[q].p, dt), boundary);
+        });
         for (size_t q = 0; q < parts.size(); q++) parts[q].p = out[q];
         if (posAdv) *posAdv = out;
         removeParticles(frameDt);

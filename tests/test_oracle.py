@@ -74,3 +74,20 @@ def test_oracle_matches_reference_empty_and_outside(built):
         b.update(sc.frame_dt)
     assert a.particles()[0].shape[0] == 0 and b.particles()[0].shape[0] == 0
     assert np.array_equal(a.liquid_phi(), b.liquid_phi())
+
+
+def test_oracle_threads_do_not_change_results(built):
+    """The port's threaded loops write disjoint outputs computed the same way,
+    so below the reference's 500k-row dot partition the thread count changes
+    no bit."""
+    sc = dam_break(20, seed=6, sphere=True)
+    out = []
+    for threads in (1, 5):
+        o = refsim.OracleSimulation(sc.isize, sc.jsize, sc.ksize, sc.dx, threads=threads).setup(sc, tolerance=1e-9)
+        st = o.update_staged(sc.frame_dt)
+        o.update(sc.frame_dt)
+        out.append((st, o.particles()))
+    (a, pa), (b, pb) = out
+    for k in STAGES + ("rhs", "positions", "velocities"):
+        assert np.array_equal(a[k], b[k]), k
+    assert np.array_equal(pa[0], pb[0]) and np.array_equal(pa[1], pb[1])
