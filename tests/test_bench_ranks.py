@@ -50,3 +50,22 @@ def test_two_gloo_ranks_combine_max_time_and_summed_particles():
 
 def test_single_rank_is_identity():
     assert bench.combine_ranks(5.0, 1.5, 42, 40, 1, "cpu") == (5.0, 1.5, 42.0, 40.0)
+
+
+def test_reference_arm_line_keeps_the_contract(built):
+    """The reference arm on a small scene: one JSON-able line with the keys
+    the bench contract names, the same metric and unit as the GPU arm, and a
+    cpu_baseline and e2e block that describe this run."""
+    import json
+    args = argparse.Namespace(steps=1, warmup=0, reference_max_steps=1, scene="plain_64")
+    line = bench.run_reference(args, 0, 1)
+    json.dumps(line)
+    for key in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better",
+                "scaling", "vs_baseline", "dtype", "data", "config", "impl", "cpu_baseline", "e2e"):
+        assert key in line, key
+    assert line["impl"] == "reference" and line["metric"] == bench.METRICS["plain_64"]
+    assert line["unit"] == bench.UNIT and line["higher_is_better"] is True and line["value"] > 0
+    cb = line["cpu_baseline"]
+    assert cb["value"] == line["value"] and cb["kind"] in ("reference", "port") and cb["cores"] >= 1
+    assert line["e2e"] == {"value": line["value"], "unit": bench.UNIT, "h2d_bytes_per_step": 0,
+                           "d2h_bytes_per_step": 0}
