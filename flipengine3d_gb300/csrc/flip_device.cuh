@@ -137,7 +137,7 @@ struct PressureBuffers {
     // flat index and sweep-layout index of each row, and their number
     int *fluidFlag, *fluidPos, *fluidScan, *nFluid;
     int *fluidIdx, *fluidSk;
-    double4 *Ad;           // rows {diag, to +x, to +y, to +z}, FP64
+    double4_32a *Ad;           // rows {diag, to +x, to +y, to +z}, FP64
     double *b;             // right-hand side (negative divergence)
     double *invdiagD;      // MIC(0) inverse pivots, FP64
     float4 *L;             // {invdiag, Lx, Ly, Lz} for the FP32 sweeps, sweep layout

@@ -90,7 +90,7 @@ __global__ void k_flags(StepConsts c, const float *phi, uint8_t *fluid, int *flu
 // neighbours that are rows of the system; a liquid neighbour outside the
 // interior contributes neither an entry nor a ghost-fluid term (the
 // reference's key map drops it).
-__device__ double4 row_coeffs(const StepConsts &c, const float *phi, const float *wu, const float *wv,
+__device__ double4_32a row_coeffs(const StepConsts &c, const float *phi, const float *wu, const float *wv,
                               const float *ww, double mf, int i, int j, int k) {
     Dims du{c.I + 1, c.J, c.K}, dv{c.I, c.J + 1, c.K}, dw{c.I, c.J, c.K + 1}, dc{c.I, c.J, c.K};
     double vR = wu[du.idx(i + 1, j, k)], vL = wu[du.idx(i, j, k)];
@@ -117,7 +117,7 @@ __device__ double4 row_coeffs(const StepConsts &c, const float *phi, const float
             diag -= vol[q] * mf * theta;
         }
     }
-    return make_double4(fmax(diag, 0.0), xp, yp, zp);
+    return make_double4_32a(fmax(diag, 0.0), xp, yp, zp);
 }
 
 // Max of non-negative values over the block, then one atomic per block.
@@ -150,7 +150,7 @@ __global__ void k_build(StepConsts c, const float *phi, const float *wu, const f
         pb.s[t] = 0.0f;
         pb.invdiagD[t] = 0.0;
         if (!pb.fluid[t]) {
-            pb.Ad[t] = make_double4(0.0, 0.0, 0.0, 0.0);
+            pb.Ad[t] = make_double4_32a(0.0, 0.0, 0.0, 0.0);
             pb.A2[2 * t] = pb.A2[2 * t + 1] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
             pb.b[t] = 0.0;
         } else {
@@ -170,7 +170,7 @@ __global__ void k_build(StepConsts c, const float *phi, const float *wu, const f
             div += factor * vK * (double)w[dw.idx(i, j, k)];
             pb.b[t] = div;
             bmag = fabs(div);
-            const double4 a = row_coeffs(c, phi, wu, wv, ww, mf, i, j, k);
+            const double4_32a a = row_coeffs(c, phi, wu, wv, ww, mf, i, j, k);
             pb.Ad[t] = a;
             const float4 hi = make_float4((float)a.x, (float)a.y, (float)a.z, (float)a.w);
             pb.A2[2 * t] = hi;
@@ -186,7 +186,7 @@ __global__ void k_build(StepConsts c, const float *phi, const float *wu, const f
 //   d_c = A_cc - sum over earlier neighbours k (ascending index) of
 //         L_ck^2 + 0.97 L_ck (sum of k's other later-neighbour entries L_mk),
 //   L_mk = A_mk / sqrt(pivot_k); a pivot below 0.25 A_kk falls back to A_kk.
-__device__ __forceinline__ void mic0_cell(const StepConsts &c, const uint8_t *fluid, const double4 *Ad, double *invD,
+__device__ __forceinline__ void mic0_cell(const StepConsts &c, const uint8_t *fluid, const double4_32a *Ad, double *invD,
                                           int level, int jj) {
     int nj = c.J - 2;
     int j = 1 + jj % nj, k = 1 + jj / nj;
@@ -202,7 +202,7 @@ __device__ __forceinline__ void mic0_cell(const StepConsts &c, const uint8_t *fl
     for (int q = 0; q < 3; q++) {
         long long kk = back[q];
         if (!fluid[kk]) continue;
-        double4 ak = Ad[kk];
+        double4_32a ak = Ad[kk];
         if (ak.x == 0.0) continue;
         double inv = invD[kk];
         double Lck = (q == 0 ? ak.w : (q == 1 ? ak.z : ak.y)) * inv;
@@ -221,7 +221,7 @@ __device__ __forceinline__ void mic0_cell(const StepConsts &c, const uint8_t *fl
     invD[t] = inv;
 }
 
-__global__ void k_mic0_level(StepConsts c, const uint8_t *fluid, const double4 *Ad, double *invD, int level) {
+__global__ void k_mic0_level(StepConsts c, const uint8_t *fluid, const double4_32a *Ad, double *invD, int level) {
     int jj = blockIdx.x * blockDim.x + threadIdx.x;
     if (jj < (c.J - 2) * (c.K - 2)) mic0_cell(c, fluid, Ad, invD, level, jj);
 }
@@ -229,7 +229,7 @@ __global__ void k_mic0_level(StepConsts c, const uint8_t *fluid, const double4 *
 // All wavefronts lo..hi in one cooperative launch: the cells of a level in
 // parallel, a grid-wide barrier between levels (every block is resident, so
 // the barrier completes).
-__global__ void k_mic0_levels(StepConsts c, const uint8_t *fluid, const double4 *Ad, double *invD, int lo, int hi) {
+__global__ void k_mic0_levels(StepConsts c, const uint8_t *fluid, const double4_32a *Ad, double *invD, int lo, int hi) {
     cg::grid_group grid = cg::this_grid();
     const int np = (c.J - 2) * (c.K - 2);
     for (int lv = lo; lv <= hi; lv++) {
@@ -247,7 +247,7 @@ __global__ void k_mic0_levels(StepConsts c, const uint8_t *fluid, const double4 
 // level needs three multiply-subtracts and a reciprocal square root.  The
 // FP64 results differ from mic0_cell's order in the last bits; the factor
 // is used rounded to FP32.
-__global__ void k_mic0_weights(StepConsts c, const uint8_t *fluid, const double4 *Ad, double *W0, double *W1,
+__global__ void k_mic0_weights(StepConsts c, const uint8_t *fluid, const double4_32a *Ad, double *W0, double *W1,
                                double *W2) {
     const long long n = (long long)c.I * c.J * c.K;
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -260,7 +260,7 @@ __global__ void k_mic0_weights(StepConsts c, const uint8_t *fluid, const double4
         for (int q = 0; q < 3; q++) {
             const long long kk = back[q];
             if (!fluid[kk]) continue;
-            const double4 ak = Ad[kk];
+            const double4_32a ak = Ad[kk];
             if (ak.x == 0.0) continue;
             const double a = q == 0 ? ak.w : (q == 1 ? ak.z : ak.y);
             const double o1 = q == 2 ? ak.z : ak.y, o2 = q == 0 ? ak.z : ak.w;
@@ -307,7 +307,7 @@ __device__ __forceinline__ void st_release(int *p, int v) {
     asm volatile("st.release.gpu.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
-__global__ void __launch_bounds__(FT *FT) k_mic0_tiles(StepConsts c, const uint8_t *fluid, const double4 *Ad,
+__global__ void __launch_bounds__(FT *FT) k_mic0_tiles(StepConsts c, const uint8_t *fluid, const double4_32a *Ad,
                                                        const double *W0, const double *W1, const double *W2,
                                                        double *invD, int lo, int hi, unsigned int *ticket,
                                                        int *progress, int *err) {
@@ -410,7 +410,7 @@ __global__ void __launch_bounds__(FT *FT) k_mic0_tiles(StepConsts c, const uint8
 }
 
 // the FP32 factor rows of the interior cells, into the sweep layout
-__global__ void k_mic0_finalize(StepConsts c, SweepLayout g, const uint8_t *fluid, const double4 *Ad,
+__global__ void k_mic0_finalize(StepConsts c, SweepLayout g, const uint8_t *fluid, const double4_32a *Ad,
                                 const double *invD, float4 *L) {
     long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= (long long)c.I * c.J * c.K) return;
@@ -420,7 +420,7 @@ __global__ void k_mic0_finalize(StepConsts c, SweepLayout g, const uint8_t *flui
     const double inv = invD[t];
     float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
     if (fluid[t] && inv != 0.0) {
-        const double4 a = Ad[t];
+        const double4_32a a = Ad[t];
         v = make_float4((float)inv, (float)(a.y * inv), (float)(a.z * inv), (float)(a.w * inv));
     }
     L[sweep_index(g, i, j, k)] = v;
@@ -644,7 +644,7 @@ __global__ void k_update_xr(const int *__restrict__ rows, const int *__restrict_
 // recurrence just claimed convergence (a claim is only made on the other
 // iterations, so one launch serves both); never once converged.
 __global__ void k_true_residual(StepConsts c, const int *__restrict__ rows, const int *__restrict__ rowsSk,
-                                const int *nRows, const double4 *__restrict__ Ad, const double *__restrict__ b,
+                                const int *nRows, const double4_32a *__restrict__ Ad, const double *__restrict__ b,
                                 const float2 *__restrict__ x, float2 *__restrict__ r, float *__restrict__ rf,
                                 unsigned long long *rmaxBits, const double *scal, PcgCtl *ctl) {
     if (ctl->done) return;
@@ -654,7 +654,7 @@ __global__ void k_true_residual(StepConsts c, const int *__restrict__ rows, cons
     double m = 0.0;
     for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
         const long long t = rows[e];
-        const double4 a = Ad[t];
+        const double4_32a a = Ad[t];
         double ax = a.x * df_to(x[t]);
         ax = fma(a.y, df_to(x[t + 1]), ax);
         ax = fma(a.z, df_to(x[t + sy]), ax);
@@ -870,7 +870,7 @@ int pressure_project(const StepConsts &c, const PressureArgs &a, PressureBuffers
         int lo_ = lo, hi_ = hi;
         StepConsts c_ = c;
         const uint8_t *fl = pb.fluid;
-        const double4 *ad = pb.Ad;
+        const double4_32a *ad = pb.Ad;
         double *inv = pb.invdiagD;
         void *args[] = {&c_, &fl, &ad, &inv, &lo_, &hi_};
         // the tiled wavefront; the pivot weights go to q, r and x, which the
