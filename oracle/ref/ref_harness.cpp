@@ -40,6 +40,7 @@ namespace {
 struct RefSim {
     FluidSimulation *sim = nullptr;
     std::string status;
+    unsigned int particleFragmentBytes = 0;   // 0: the reference's default fragments
 };
 
 template <class T>
@@ -92,6 +93,22 @@ void ref_destroy(void *h) {
 }
 
 void ref_set_threads(void *h, int n) { ((RefSim *)h)->sim->setMaxThreadCount(n); }
+// The byte size of the marker-particle container's fragments
+// (FragmentedVector::setFragmentByteSize, fragmentedvector.h:59-64; default
+// 5e6).  Its element access computes the fragment as (int)(i * (1.0 / n))
+// with n elements per fragment (fragmentedvector.h:141-153, 295-302): for
+// some i that are multiples of n the product rounds below i / n and the
+// access lands on the first element of the previous fragment.  Fragments
+// larger than the particle count have no such index.  Set here for the
+// simulation's particle container and for the load queue's, which
+// loadMarkerParticleData fills and _loadMarkerParticles reads back
+// (fluidsimulation.cpp:2488-2509, 2773-2786).  Only before particles are
+// loaded.
+void ref_set_particle_fragment_bytes(void *h, unsigned int bytes) {
+    RefSim *r = (RefSim *)h;
+    r->particleFragmentBytes = bytes;
+    r->sim->_markerParticles.setFragmentByteSize(bytes);
+}
 void ref_set_pic_ratio(void *h, double ratio) { ((RefSim *)h)->sim->setPICFLIPRatio(ratio); }
 void ref_add_body_force(void *h, double x, double y, double z) { ((RefSim *)h)->sim->addBodyForce(x, y, z); }
 void ref_set_cfl(void *h, int c) { ((RefSim *)h)->sim->setCFLConditionNumber(c); }
@@ -99,11 +116,26 @@ void ref_set_pressure_tol(void *h, double tol) { ((RefSim *)h)->sim->_pressureSo
 void ref_set_pressure_maxiter(void *h, int n) { ((RefSim *)h)->sim->_maxPressureSolveIterations = n; }
 
 void ref_load_particles(void *h, int n, const float *pos, const float *vel) {
-    FluidSimulationMarkerParticleData d;
-    d.size = n;
-    d.positions = (char *)pos;
-    d.velocities = (char *)vel;
-    ((RefSim *)h)->sim->loadMarkerParticleData(d);
+    RefSim *r = (RefSim *)h;
+    if (r->particleFragmentBytes == 0) {
+        FluidSimulationMarkerParticleData d;
+        d.size = n;
+        d.positions = (char *)pos;
+        d.velocities = (char *)vel;
+        r->sim->loadMarkerParticleData(d);
+        return;
+    }
+    if (n == 0) return;
+    // loadMarkerParticleData (fluidsimulation.cpp:2488-2509) with the load
+    // queue's container in fragments of the chosen size
+    const vmath::vec3 *positions = (const vmath::vec3 *)pos;
+    const vmath::vec3 *velocities = (const vmath::vec3 *)vel;
+    FluidSimulation::MarkerParticleLoadData loadData;
+    loadData.particles.setFragmentByteSize(r->particleFragmentBytes);
+    loadData.particles.reserve(n);
+    for (int i = 0; i < n; i++) loadData.particles.push_back(MarkerParticle(positions[i], velocities[i]));
+    r->sim->_markerParticleLoadQueue.push_back(loadData);
+    r->sim->_isMarkerParticleLoadPending = true;
 }
 
 void ref_initialize(void *h) { ((RefSim *)h)->sim->initialize(); }

@@ -65,6 +65,9 @@ def lib(prefix: str = "ref"):
         }.items():
             getattr(L, name).argtypes = args
             getattr(L, name).restype = None
+        if prefix == "ref":
+            L.ref_set_particle_fragment_bytes.argtypes = [C.c_void_p, C.c_uint]
+            L.ref_set_particle_fragment_bytes.restype = None
         L.ref_num_particles.argtypes = [C.c_void_p]
         L.ref_num_particles.restype = C.c_int
         L.ref_frame_substeps.argtypes = [C.c_void_p]
@@ -92,12 +95,18 @@ class RefSimulation:
 
     PREFIX = "ref"
 
-    def __init__(self, isize, jsize, ksize, dx, *, threads=1):
+    def __init__(self, isize, jsize, ksize, dx, *, threads=1, one_particle_fragment=False):
+        """one_particle_fragment (reference only): hold the marker particles in
+        one fragment of the reference's FragmentedVector, whose element access
+        at some multiples of its default 208,333-element fragment returns the
+        previous fragment's first element (ref_harness.cpp)."""
         self.L = lib(self.PREFIX)
         self.dims = (isize, jsize, ksize)
         self.dx = dx
         self.h = self.L.ref_create(isize, jsize, ksize, dx)
         self.L.ref_set_threads(self.h, threads)
+        if one_particle_fragment and self.PREFIX == "ref":
+            self.L.ref_set_particle_fragment_bytes(self.h, 2_000_000_000)
 
     def close(self):
         if self.h:
