@@ -131,3 +131,20 @@ def test_reference_particle_container_aliases_fragment_starts(built):
     # each is a copy of an earlier fragment start (the readback reads through
     # the same index arithmetic, so a copy of a copy reaches back two)
     assert all(any(np.array_equal(pos[i], sc.positions[i - m * n]) for m in (1, 2)) for i in aliased)
+
+
+@needs_ref
+def test_oracle_tracks_reference_engine_ten_frames_at_64(built):
+    """The 64^3 configuration at full size (486k particles), all 10 frames:
+    particle positions and velocities bit-identical every frame."""
+    from flipengine3d_gb300.scenes import plain_64
+    sc = plain_64()
+    a = refsim.RefSimulation(sc.isize, sc.jsize, sc.ksize, sc.dx, threads=8, one_particle_fragment=True).setup(sc)
+    b = refsim.OracleSimulation(sc.isize, sc.jsize, sc.ksize, sc.dx, threads=8).setup(sc)
+    for f in range(sc.steps):
+        a.update(sc.frame_dt)
+        b.update(sc.frame_dt)
+        pa, va = a.particles()
+        pb, vb = b.particles()
+        assert pa.shape == pb.shape, f"frame {f + 1}: particle count"
+        assert np.array_equal(pa, pb) and np.array_equal(va, vb), f"frame {f + 1}"
