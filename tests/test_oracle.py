@@ -148,3 +148,17 @@ def test_oracle_tracks_reference_engine_ten_frames_at_64(built):
         pb, vb = b.particles()
         assert pa.shape == pb.shape, f"frame {f + 1}: particle count"
         assert np.array_equal(pa, pb) and np.array_equal(va, vb), f"frame {f + 1}"
+
+
+@needs_ref
+def test_oracle_matches_reference_engine_at_256x128x128(built):
+    """The largest configuration (256x128x128, ~15M particles, FLIP blend
+    0.98): every stage dump of the first frame bit-identical."""
+    from flipengine3d_gb300.scenes import mixed_256
+    sc = mixed_256()
+    a = refsim.RefSimulation(sc.isize, sc.jsize, sc.ksize, sc.dx, threads=8, one_particle_fragment=True).setup(sc)
+    b = refsim.OracleSimulation(sc.isize, sc.jsize, sc.ksize, sc.dx, threads=8).setup(sc)
+    A = a.update_staged(sc.frame_dt)
+    B = b.update_staged(sc.frame_dt)
+    for k in A:
+        assert A[k].shape == B[k].shape and np.array_equal(A[k], B[k]), k
