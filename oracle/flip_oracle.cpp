@@ -420,13 +420,10 @@ struct Sim {
             if (active.in(g.i, g.j, g.k)) active(g.i, g.j, g.k) = 1;
         }
         feather26(active);
-        std::vector<std::vector<int>> lists(active.a.size());
         float r = (float)sdfRadius;
         float sr = 2.0f * (float)sdfRadius;
-        for (int n = 0; n < (int)parts.size(); n++) {
-            V3 p = parts[n].p;
-            blockLists(p, sr, blockdx, active, lists, n);
-        }
+        std::vector<std::vector<int>> lists =
+            buildBlockLists(active, nthreads, [&](int n) { return parts[n].p; }, sr, blockdx);
         std::vector<int> work;   // blocks with particles, in block order
         for (int id = 0; id < (int)active.a.size(); id++)
             if (active.a[id] && !lists[id].empty()) work.push_back(id);
@@ -476,6 +473,33 @@ struct Sim {
 
     // Which active blocks a point's search box overlaps, as the reference's
     // count pass decides it (simple case: box strictly inside its own block).
+    // The block lists of all particles, each in ascending particle order (the
+    // reference's count pass runs on threads over contiguous particle ranges
+    // and concatenates them in range order, particlelevelset.cpp:435-580):
+    // the threads fill lists of their own and the ranges are joined in order.
+    template <class P>
+    std::vector<std::vector<int>> buildBlockLists(const Grid<uint8_t> &active, int nt, P pos, float sr,
+                                                  float blockdx) const {
+        const int np = (int)parts.size();
+        nt = std::max(1, std::min(nt, np));
+        std::vector<std::vector<std::vector<int>>> part(nt, std::vector<std::vector<int>>(active.a.size()));
+        std::vector<int> iv = splitRange(0, np, nt);
+        parallel_ranges(nt, nt, [&](int t0, int t1) {
+            for (int t = t0; t < t1; t++)
+                for (int n = iv[t]; n < iv[t + 1]; n++) blockLists(pos(n), sr, blockdx, active, part[t], n);
+        });
+        std::vector<std::vector<int>> lists(active.a.size());
+        parallel_ranges((int)lists.size(), nt, [&](int b0, int b1) {
+            for (int b = b0; b < b1; b++) {
+                size_t total = 0;
+                for (int t = 0; t < nt; t++) total += part[t][b].size();
+                lists[b].reserve(total);
+                for (int t = 0; t < nt; t++) lists[b].insert(lists[b].end(), part[t][b].begin(), part[t][b].end());
+            }
+        });
+        return lists;
+    }
+
     static void blockLists(V3 p, float sr, float blockdx, const Grid<uint8_t> &active,
                            std::vector<std::vector<int>> &lists, int n) {
         GI bi = posToIdx(p, blockdx);
@@ -545,8 +569,8 @@ struct Sim {
         float eps = 1e-6f;
         float sr = (float)(sdfRadius + eps);
         float blockdx = (float)chunkdx;
-        std::vector<std::vector<int>> lists(active.a.size());
-        for (int n = 0; n < (int)parts.size(); n++) blockLists(parts[n].p - off, sr, blockdx, active, lists, n);
+        std::vector<std::vector<int>> lists =
+            buildBlockLists(active, nthreads, [&](int n) { return parts[n].p - off; }, sr, blockdx);
         float r = (float)sdfRadius;
         float rsq = r * r;
         float coef1 = (4.0f / 9.0f) * (1.0f / (r * r * r * r * r * r));
