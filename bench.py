@@ -273,11 +273,22 @@ def mixed_scenes(count, seed=1):
     {32, 48, 64, 80, 96} (dx = 1/edge), each a dam break whose x extent
     (the fill fraction) is drawn from [0.2, 0.6], y <= 0.6, full z, 8 jittered
     particles per cell, FLIP blend 0.95."""
-    from flipengine3d_gb300.scenes import dam_break
+    return [mixed_scene(q, count, seed) for q in range(count)]
+
+
+def mixed_scene_params(count, seed=1):
+    """(edge, fill) of each scene of the mixed-size set, without its particles."""
     rng = np.random.default_rng(seed)
     edges = rng.choice([32, 48, 64, 80, 96], size=count)
     fills = rng.uniform(0.2, 0.6, size=count)
-    return [dam_break(int(e), seed=seed * 1000 + q, fill=(float(f), 0.6, 1.0)) for q, (e, f) in enumerate(zip(edges, fills))]
+    return [(int(e), float(f)) for e, f in zip(edges, fills)]
+
+
+def mixed_scene(q, count=64, seed=1):
+    """Scene q of the mixed-size set."""
+    from flipengine3d_gb300.scenes import dam_break
+    e, f = mixed_scene_params(count, seed)[q]
+    return dam_break(e, seed=seed * 1000 + q, fill=(f, 0.6, 1.0))
 
 
 def served_scene(q, seed=2):

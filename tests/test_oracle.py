@@ -162,3 +162,26 @@ def test_oracle_matches_reference_engine_at_256x128x128(built):
     B = b.update_staged(sc.frame_dt)
     for k in A:
         assert A[k].shape == B[k].shape and np.array_equal(A[k], B[k]), k
+
+
+@needs_ref
+@pytest.mark.parametrize("kind,edge_or_index", [("mixed", 32), ("mixed", 48), ("mixed", 80), ("served", 6),
+                                                ("served", 1)])
+def test_oracle_matches_reference_engine_on_the_multi_scene_sets(built, kind, edge_or_index):
+    """Scenes of the batched set (the first of each edge 32, 48, 80; fills
+    0.2-0.6) and of the served set (4-8 particles per cell, tolerance 1e-5):
+    two frames bit-identical."""
+    import bench
+    if kind == "mixed":
+        q = next(i for i, (e, _) in enumerate(bench.mixed_scene_params(64)) if e == edge_or_index)
+        sc = bench.mixed_scene(q)
+    else:
+        sc = bench.served_scene(edge_or_index)
+    a = refsim.RefSimulation(sc.isize, sc.jsize, sc.ksize, sc.dx, threads=4, one_particle_fragment=True).setup(sc)
+    b = refsim.OracleSimulation(sc.isize, sc.jsize, sc.ksize, sc.dx, threads=4).setup(sc)
+    for f in range(2):
+        a.update(sc.frame_dt)
+        b.update(sc.frame_dt)
+        pa, va = a.particles()
+        pb, vb = b.particles()
+        assert pa.shape == pb.shape and np.array_equal(pa, pb) and np.array_equal(va, vb), f"{sc.name} frame {f + 1}"
