@@ -9,14 +9,21 @@ Inputs are synthetic (no dataset exists for this path).  Under torchrun each
 rank runs its own replica of the scene on its own GPU (weak scaling, no
 collective on the data path); the timing is max over ranks.
 
-  value  device time of K frames (CUDA events on the library's stream,
-         L2 flushed between frames outside the events), particles at the
-         start of each frame summed over frames and ranks.
-  e2e    the same metric through the public API with host buffers: each
-         frame is update(dt) plus getMarkerParticlePositionData() into host
+  value  device time of frames W+1..W+K after W untimed warm-up frames
+         (CUDA events on the library's stream, L2 flushed between frames
+         outside the events), particles at the start of each frame summed
+         over frames and ranks.
+  e2e    the same metric over the same frames through the public API with
+         host buffers: a simulation loaded with the particles of frame W
+         (loadMarkerParticleData + setCurrentFrame, untimed), then per frame
+         update(dt) plus getMarkerParticlePositionData() into pinned host
          memory (host wall clock, device synchronised).
+  plain_60  frames 1-60 of the 128^3 configuration from its seeded start.
+  batched / served  the mixed-size and served scene sets (see
+         run_batched_and_served); batched is compared with the same scenes
+         stepped one after another through the plain step, same frames.
   --impl reference   the reference CPU path (the reference engine when it was
-         compiled here, else the C++ oracle restating it) on a bounded sample
+         compiled here, else the C++ oracle restating it) on frames W+1..W+K
          of the same workload, rank 0 only.
 """
 from __future__ import annotations
@@ -154,6 +161,27 @@ def combine_ranks(ms, e2e_s, particles, e2e_particles, world, device):
     return float(t[0]), float(t[1]), float(tot[0]), float(tot[1])
 
 
+def timed_frames(sim, stream, steps, flush=None):
+    """`steps` update(1/120) frames, each bracketed by CUDA events on the
+    simulation's stream (L2 flushed before each, outside the events).
+    Returns (ms, particles at the start of each frame, per-frame stats)."""
+    import torch
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    parts, frames = [], []
+    for k in range(steps):
+        if flush is not None:
+            with torch.cuda.stream(stream):
+                flush.zero_()
+        parts.append(sim.getNumMarkerParticles())
+        ev[k][0].record(stream)
+        sim.update(FRAME_DT)
+        ev[k][1].record(stream)
+        st = sim.getFrameStatsData()
+        frames.append((st.substeps, st.pressure_iterations, st.pressure_cells))
+    torch.cuda.synchronize()
+    return sum(a.elapsed_time(b) for a, b in ev), parts, frames
+
+
 def run_gpu(args, rank, world):
     import torch
 
@@ -169,51 +197,62 @@ def run_gpu(args, rank, world):
     for _ in range(args.warmup):
         sim.update(FRAME_DT)
     torch.cuda.synchronize()
+    # the state after warm-up: the e2e pass resumes from it, so both passes
+    # (and the reference arm, which warms up the same way) time the same frames
+    snap_pos = sim.getMarkerParticlePositionData().copy()
+    snap_vel = sim.getMarkerParticleVelocityData().copy()
+    start_frame = sim.getCurrentFrame()
 
     # device-timed frames
     sim.set_stage_timing(True)
     launches0 = sim.launch_count()
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-    particles = 0
-    iters, cells = [], []
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
     with ClockSampler(local) as clocks:
-        for k in range(args.steps):
-            with torch.cuda.stream(stream):
-                flush.zero_()
-            particles += sim.getNumMarkerParticles()
-            ev[k][0].record(stream)
-            sim.update(FRAME_DT)
-            ev[k][1].record(stream)
-            st = sim.getFrameStatsData()
-            iters.append(st.pressure_iterations)
-            cells.append(st.pressure_cells)
-        torch.cuda.synchronize()
+        ms, parts, frames = timed_frames(sim, stream, args.steps, flush)
     launches = sim.launch_count() - launches0
-    ms = sum(a.elapsed_time(b) for a, b in ev)
+    particles = sum(parts)
     stage_ms, substeps = sim.stage_times()
     sweep_ms, sweep_launches, sweep_rows = sim.sweep_times()
     sim.set_stage_timing(False)
+    sim.close()
 
-    # end to end through the public API with host buffers: the positions go
+    # end to end through the public API with host buffers, over the same
+    # frames: a fresh simulation loads the warmed-up particles from host
+    # memory (loadMarkerParticleData + initialize + setCurrentFrame, untimed),
+    # then each timed frame is update(dt) plus getMarkerParticlePositionData()
     # into one pinned host buffer, as a caller of the reference's
     # getMarkerParticlePositionData(char *) passes its own buffer
+    e2e_sim = fg.FluidSimulation(sc.isize, sc.jsize, sc.ksize, sc.dx)
+    e2e_sim.setPICFLIPRatio(sc.pic_ratio)
+    e2e_sim.addBodyForce(*sc.gravity)
+    e2e_sim.setCFLConditionNumber(sc.cfl)
+    e2e_sim.setPressureSolveTolerance(sc.tolerance)
+    e2e_sim.loadMarkerParticleData(snap_pos, snap_vel)
+    e2e_sim.initialize()
+    e2e_sim.setCurrentFrame(start_frame)
+    e2e_sim.setStream(stream.cuda_stream)
+    host = torch.empty((len(snap_pos), 3), dtype=torch.float32, pin_memory=True).numpy()
     d2h = 0
-    host = torch.empty((sim.getNumMarkerParticles(), 3), dtype=torch.float32, pin_memory=True).numpy()
+    e2e_parts, e2e_frames = [], []
     torch.cuda.synchronize()
-    e2e_particles = 0
     t0 = time.perf_counter()
     for k in range(args.steps):
-        e2e_particles += sim.getNumMarkerParticles()
-        sim.update(FRAME_DT)
-        pos = sim.getMarkerParticlePositionData(out=host)
+        e2e_parts.append(e2e_sim.getNumMarkerParticles())
+        e2e_sim.update(FRAME_DT)
+        pos = e2e_sim.getMarkerParticlePositionData(out=host)
         d2h += pos.nbytes
+        st = e2e_sim.getFrameStatsData()
+        e2e_frames.append((st.substeps, st.pressure_iterations, st.pressure_cells))
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t0
+    e2e_sim.close()
+    e2e_particles = sum(e2e_parts)
+    same_window = e2e_parts == parts and e2e_frames == frames
 
     ms_max, e2e_max, ptot, e2e_ptot = combine_ranks(ms, e2e_s, particles, e2e_particles, world, "cuda")
+    psub = sum(p * f[0] for p, f in zip(parts, frames)) * world
     if rank != 0:
         return None
     value = ptot / (ms_max / 1e3) / 1e6
@@ -224,6 +263,8 @@ def run_gpu(args, rank, world):
     peak, peak_kind = peaks()
     n_cells = sc.isize * sc.jsize * sc.ksize
     n_avg = particles / args.steps
+    iters = [f[1] for f in frames]
+    cells = [f[2] for f in frames]
     base_b, pcg_b = algorithmic_bytes(n_avg, n_cells, np.mean(cells), np.mean(iters))
     sweep_bytes_per_launch = SWEEP_BYTES_PER_ROW * sweep_rows / max(sweep_launches, 1)
     sweep_s_per_launch = sweep_ms / 1e3 / max(sweep_launches, 1)
@@ -231,24 +272,32 @@ def run_gpu(args, rank, world):
     step_achieved = (base_b + pcg_b) * substeps / (sum(stage_ms.values()) / 1e3) / 1e9
 
     cpu = cpu_baseline(args) if not args.no_cpu_baseline else None
+    plain60 = run_full_length(args, fg, stream, flush) if (not args.no_full_length and world == 1) else None
     batched = served = None
     if not args.no_batched and world == 1:
-        sim.close()   # free the plain scene's memory first
-        batched, served = run_batched_and_served(args, value)
+        batched, served = run_batched_and_served(args)
     line = {
         "metric": METRICS[args.scene], "value": round(value, 4), "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(ms_max / args.steps, 4), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32 (FP64 dots/refinement)",
         "data": "synthetic: seeded dam break + sphere, 8 jittered particles per cell",
         "config": {"workload": SCENES[args.scene], "particles": int(n_avg), "grid": [sc.isize, sc.jsize, sc.ksize],
+                   "frames_timed": [start_frame + 1, start_frame + args.steps],
+                   "substeps_per_frame": [f[0] for f in frames],
+                   "pcg_iterations_per_frame": iters,
                    "pressure_cells": int(np.mean(cells)), "pcg_iterations_mean": float(np.mean(iters)),
+                   "mparticle_substeps_per_s": round(psub / (ms_max / 1e3) / 1e6, 4),
                    "l2": "flushed between timed frames (256 MB write, outside the events)",
                    "parallelism": f"replicas x{world}"},
         "e2e": {"value": round(e2e_value, 4), "unit": UNIT, "h2d_bytes_per_step": 8,
                 "d2h_bytes_per_step": int(d2h / args.steps),
-                "path": "FluidSimulation.update(dt) + getMarkerParticlePositionData(out=pinned host buffer) via the C ABI",
-                "timing": "wall clock over back-to-back frames (no L2 flush between them; the step's working set "
-                          "is larger than L2), where `value` flushes L2 between event-timed frames"},
+                "frames_timed": [start_frame + 1, start_frame + args.steps],
+                "same_frames_as_value": same_window,
+                "path": "FluidSimulation.update(dt) + getMarkerParticlePositionData(out=pinned host buffer) via the C "
+                        "ABI, on a simulation loaded with the warmed-up particles (loadMarkerParticleData + "
+                        "setCurrentFrame, untimed)",
+                "timing": "wall clock over back-to-back frames, device synchronised at both ends (no L2 flush "
+                          "between frames; the step's working set is larger than L2)"},
         "roofline": {"bound": "hbm", "kernel": "k_wavefront (MIC(0) forward + backward sweeps)",
                      "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 5), "traffic": sweep_traffic_per_launch(),
@@ -258,50 +307,39 @@ def run_gpu(args, rank, world):
                      "share_of_step": round(sweep_ms / ms, 4) if ms else None,
                      "bytes_rule": f"{SWEEP_BYTES_PER_ROW:g} B per pressure row per sweep (factor row 16, rhs 4, result 4)",
                      "step_achieved_gbs": round(step_achieved, 1),
+                     "step_frac": round(step_achieved / peak, 5),
                      "stage_ms_per_step": {k: round(v / args.steps, 3) for k, v in stage_ms.items()}},
         "cpu_baseline": cpu,
+        "plain_60": plain60,
         "batched": batched,
         "served": served,
         "gpu_launches": int(launches),
+        "launches_per_frame": round(launches / args.steps, 1),
         "clocks": clocks.summary(),
     }
     return line
 
 
+def run_full_length(args, fg, stream, flush):
+    """The 128^3 configuration over its full length: frames 1-60 from the
+    seeded start, each event-timed as `value` is (L2 flushed between)."""
+    if args.scene != "plain_128":
+        return None
+    sc = make_scene(args.scene)
+    sim = fg.FluidSimulation.from_scene(sc)
+    sim.setStream(stream.cuda_stream)
+    ms, parts, frames = timed_frames(sim, stream, sc.steps, flush)
+    sim.close()
+    return {"value": round(sum(parts) / (ms / 1e3) / 1e6, 4), "unit": UNIT, "frames": sc.steps,
+            "ms_per_frame": round(ms / sc.steps, 3), "substeps": sum(f[0] for f in frames),
+            "pcg_iterations_mean": round(float(np.mean([f[1] for f in frames])), 2),
+            "particles_first_last": [parts[0], parts[-1]],
+            "timing": "frames 1-60 from the seeded start, CUDA events per frame, L2 flushed between frames"}
+
+
 def mixed_scenes(count, seed=1):
-    """The mixed-size scene set: cubic grids with edges drawn from
-    {32, 48, 64, 80, 96} (dx = 1/edge), each a dam break whose x extent
-    (the fill fraction) is drawn from [0.2, 0.6], y <= 0.6, full z, 8 jittered
-    particles per cell, FLIP blend 0.95."""
+    from flipengine3d_gb300.scenes import mixed_scene
     return [mixed_scene(q, count, seed) for q in range(count)]
-
-
-def mixed_scene_params(count, seed=1):
-    """(edge, fill) of each scene of the mixed-size set, without its particles."""
-    rng = np.random.default_rng(seed)
-    edges = rng.choice([32, 48, 64, 80, 96], size=count)
-    fills = rng.uniform(0.2, 0.6, size=count)
-    return [(int(e), float(f)) for e, f in zip(edges, fills)]
-
-
-def mixed_scene(q, count=64, seed=1):
-    """Scene q of the mixed-size set."""
-    from flipengine3d_gb300.scenes import dam_break
-    e, f = mixed_scene_params(count, seed)[q]
-    return dam_break(e, seed=seed * 1000 + q, fill=(f, 0.6, 1.0))
-
-
-def served_scene(q, seed=2):
-    """Scene q of the served set: a cubic grid with its edge drawn uniformly
-    from [32, 160] (dx = 1/edge), a dam break whose x extent is drawn from
-    [0.2, 0.6], y <= 0.6, full z, 4-8 jittered particles per cell (drawn per
-    scene), FLIP blend 0.95, PCG tolerance 1e-5."""
-    from flipengine3d_gb300.scenes import dam_break
-    rng = np.random.default_rng([seed, q])
-    edge = int(rng.integers(32, 161))
-    fill = float(rng.uniform(0.2, 0.6))
-    ppc = int(rng.integers(4, 9))
-    return dam_break(edge, seed=seed * 100000 + q, fill=(fill, 0.6, 1.0), ppc=ppc, tolerance=1e-5)
 
 
 def resident_scenes(rt, make, count, threads=16):
@@ -323,69 +361,119 @@ def resident_scenes(rt, make, count, threads=16):
     return sims, rejected
 
 
-def run_batched_and_served(args, plain_value):
+def run_batched_and_served(args):
     """Many resident scenes on one GPU through the C++ runtime (one CUDA
-    stream per scene, args.workers host threads).  Batched: the mixed-size
-    set, every scene one step per round (update_all), wall-clock timed over
-    args.batch_steps rounds.  Served: the served set of args.served_scenes
-    resident scenes, Poisson arrivals of one-step requests for random
-    scenes, latency from submission to completion."""
+    stream per scene, args.workers host threads).
+
+    Batched: the mixed-size set, stepped together (update_all) and, as the
+    comparison, the same set stepped one scene after another through the
+    plain single-scene step; both wall-clock timed over the same frames
+    (args.warmup untimed, then args.batch_steps).  Served: the served set of
+    args.served_scenes resident scenes; capacity = one-step requests per
+    second that update_all sustains over it; Poisson arrivals of one-step
+    requests for random scenes at fractions of that capacity and at the
+    configured rate, latency from submission to completion."""
     import torch
 
     import flipengine3d_gb300 as fg
-    scs = mixed_scenes(args.batch_scenes)
-    rt = fg.FluidRuntime(workers=args.workers, reserve_bytes=2 << 30)
-    handles, rejected = resident_scenes(rt, lambda q: scs[q], len(scs))
-    del scs
     dt = FRAME_DT
-    for _ in range(max(args.warmup, 1)):
-        rt.update_all(handles, dt)
-    torch.cuda.synchronize()
-    parts = 0
-    t0 = time.perf_counter()
-    for _ in range(args.batch_steps):
-        parts += sum(s.getNumMarkerParticles() for s in handles)
-        rt.update_all(handles, dt)
-    torch.cuda.synchronize()
-    tb = time.perf_counter() - t0
-    bval = parts / tb / 1e6
-    batched = {"value": round(bval, 3), "unit": UNIT, "scenes": len(handles), "rejected_at_admission": rejected,
-               "particles": int(parts / args.batch_steps), "steps": args.batch_steps,
-               "ms_per_step": round(tb / args.batch_steps * 1e3, 2), "workers": args.workers,
-               "vs_plain": round(bval / plain_value, 3) if plain_value else None,
-               "timing": "wall clock around update_all (all scenes one frame), device synchronised",
+    rt = fg.FluidRuntime(workers=args.workers, reserve_bytes=2 << 30)
+
+    def timed_rounds(handles, step_all):
+        for _ in range(args.warmup):
+            step_all(handles)
+        torch.cuda.synchronize()
+        parts, frames = 0, 0
+        t0 = time.perf_counter()
+        for _ in range(args.batch_steps):
+            parts += sum(s.getNumMarkerParticles() for s in handles)
+            step_all(handles)
+        torch.cuda.synchronize()
+        return parts, time.perf_counter() - t0
+
+    def sequential(handles):
+        for h in handles:
+            h.update(dt)
+
+    out = {}
+    for mode, step_all in (("plain_sequential", sequential), ("batched", lambda hs: rt.update_all(hs, dt))):
+        scs = mixed_scenes(args.batch_scenes)
+        handles, rejected = resident_scenes(rt, lambda q: scs[q], len(scs))
+        del scs
+        parts, t = timed_rounds(handles, step_all)
+        out[mode] = (parts, t, len(handles), rejected)
+        for h in handles:
+            h.close()
+        torch.cuda.synchronize()
+    (pp, pt, _, _), (bp, bt, nb, rejected) = out["plain_sequential"], out["batched"]
+    plain_seq = pp / pt / 1e6
+    bval = bp / bt / 1e6
+    batched = {"value": round(bval, 3), "unit": UNIT, "scenes": nb, "rejected_at_admission": rejected,
+               "particles": int(bp / args.batch_steps), "steps": args.batch_steps,
+               "frames_timed": [args.warmup + 1, args.warmup + args.batch_steps],
+               "ms_per_step": round(bt / args.batch_steps * 1e3, 2), "workers": args.workers,
+               "plain_sequential": {"value": round(plain_seq, 3), "unit": UNIT,
+                                    "ms_per_step": round(pt / args.batch_steps * 1e3, 2),
+                                    "how": "the same scenes and frames, each scene stepped in turn through the "
+                                           "plain single-scene update(dt) on one stream"},
+               "vs_plain": round(bval / plain_seq, 3) if plain_seq else None,
+               "timing": "wall clock around each round (all scenes one frame), device synchronised at both ends",
                "config": "mixed sizes: edges from {32,48,64,80,96} (seed 1), dam x-fill U[0.2,0.6], y<=0.6, "
                          "8 particles per cell, FLIP blend 0.95, PCG tol 1e-6, dt=1/120; one stream per scene"}
-    for s in handles:
-        s.close()
-    torch.cuda.synchronize()
-    # served: Poisson arrivals over the served set
+
+    # served: the served set resident; capacity, then Poisson arrivals
+    from flipengine3d_gb300.scenes import served_scene
     handles, srejected = resident_scenes(rt, served_scene, args.served_scenes)
     for _ in range(max(args.warmup, 1)):
         rt.update_all(handles, dt)
     torch.cuda.synchronize()
-    rng = np.random.default_rng(7)
-    gaps = rng.exponential(1.0 / args.arrival_rate, size=args.requests)
-    picks = rng.integers(0, len(handles), size=args.requests)
-    sizes = [s.getNumMarkerParticles() for s in handles]
-    ids = []
     t0 = time.perf_counter()
-    due = t0
-    for g, q in zip(gaps, picks):
-        due += g
-        while time.perf_counter() < due:
-            pass
-        ids.append(rt.submit(handles[q], dt))
-    lat = np.array([rt.wait(i)[0] for i in ids])
-    ts = time.perf_counter() - t0
-    served = {"p50_ms": round(float(np.percentile(lat, 50)), 2), "p99_ms": round(float(np.percentile(lat, 99)), 2),
-              "requests": args.requests, "arrival_rate_hz": args.arrival_rate,
-              "value": round(float(sum(sizes[q] for q in picks)) / ts / 1e6, 3), "unit": UNIT,
+    cap_rounds = 2
+    for _ in range(cap_rounds):
+        rt.update_all(handles, dt)
+    torch.cuda.synchronize()
+    capacity = cap_rounds * len(handles) / (time.perf_counter() - t0)   # one-step requests per second
+    sizes = [s.getNumMarkerParticles() for s in handles]
+    rng = np.random.default_rng(7)
+
+    def load_point(rate, requests):
+        gaps = rng.exponential(1.0 / rate, size=requests)
+        picks = rng.integers(0, len(handles), size=requests)
+        ids = []
+        t0 = time.perf_counter()
+        due = t0
+        for g, q in zip(gaps, picks):
+            due += g
+            while time.perf_counter() < due:
+                pass
+            ids.append(rt.submit(handles[q], dt))
+        lat = np.array([rt.wait(i)[0] for i in ids])
+        ts = time.perf_counter() - t0
+        return {"arrival_rate_hz": round(rate, 1), "requests": requests,
+                "p50_ms": round(float(np.percentile(lat, 50)), 2), "p99_ms": round(float(np.percentile(lat, 99)), 2),
+                "value": round(float(sum(sizes[q] for q in picks)) / ts / 1e6, 3),
+                "completed_per_s": round(requests / ts, 1)}
+
+    curve = []
+    for frac in (0.25, 0.5, 0.8, 1.0):
+        rate = frac * capacity
+        pt_ = load_point(rate, max(50, min(args.requests, int(rate * 2.0))))
+        pt_["load_fraction"] = frac
+        curve.append(pt_)
+    main = load_point(args.arrival_rate, args.requests)
+    at80 = next(c for c in curve if c["load_fraction"] == 0.8)
+    served = {"p50_ms": main["p50_ms"], "p99_ms": main["p99_ms"], "requests": args.requests,
+              "arrival_rate_hz": args.arrival_rate, "value": main["value"], "unit": UNIT,
+              "capacity_steps_s": round(capacity, 1),
+              "p50_ms_at_80pct": at80["p50_ms"], "p99_ms_at_80pct": at80["p99_ms"],
+              "saturation_curve": curve,
               "resident_scenes": len(handles), "rejected_at_admission": srejected,
               "resident_particles": int(sum(sizes)), "workers": args.workers,
               "config": "edges uniform in [32,160] (seed 2), dam x-fill U[0.2,0.6], y<=0.6, 4-8 particles per "
                         "cell, FLIP blend 0.95, PCG tol 1e-5, dt=1/120; one stream per scene",
-              "note": "latency = submission to completion (queueing included); one-step requests"}
+              "note": "latency = submission to completion (queueing included); one-step requests; capacity = "
+                      "requests/s that update_all over all resident scenes sustains; the configured rate is "
+                      "above capacity, so its latency is mostly queueing"}
     rt.close()
     for s in handles:
         s.close()
@@ -405,40 +493,54 @@ def cpu_sample_sim(args, threads):
 
 
 def cpu_baseline(args):
+    """The reference CPU path on the machine's host cores: the GPU arm's frames
+    after the same warm-up, a bounded number of them (args.cpu_frames)."""
     threads = os.cpu_count() or 1
     sc, sim, kind, threads = cpu_sample_sim(args, threads)
-    sim.update(FRAME_DT)                       # first frame builds the solid level set: untimed
-    n = sim.particles()[0].shape[0]
-    t0 = time.perf_counter()
-    sim.update(FRAME_DT)
-    dt = time.perf_counter() - t0
-    return {"value": round(n / dt / 1e6, 5), "unit": UNIT, "cores": threads, "kind": kind,
-            "sample": f"1 timed frame of the {args.scene} workload ({n} particles) after 1 untimed frame, {dt:.1f} s"}
+    for _ in range(args.warmup):
+        sim.update(FRAME_DT)
+    total, t = 0, 0.0
+    frames = max(1, min(args.steps, args.cpu_frames))
+    for _ in range(frames):
+        total += sim.particles()[0].shape[0]
+        t0 = time.perf_counter()
+        sim.update(FRAME_DT)
+        t += time.perf_counter() - t0
+    return {"value": round(total / t / 1e6, 5), "unit": UNIT, "cores": threads, "kind": kind,
+            "sample": f"frames {args.warmup + 1}-{args.warmup + frames} of the {args.scene} workload (the first "
+                      f"{frames} of the GPU arm's timed frames) after {args.warmup} untimed, {t:.1f} s"}
 
 
 def run_reference(args, rank, world):
+    """The reference CPU path on the GPU arm's frames: args.warmup untimed
+    frames, then args.steps timed ones (capped at args.reference_max_steps)."""
     if rank != 0:
         return None
     threads = os.cpu_count() or 1
     sc, sim, kind, threads = cpu_sample_sim(args, threads)
     steps = max(1, min(args.steps, args.reference_max_steps))
-    warm = max(0, min(args.warmup, 1))
-    for _ in range(warm):
+    for _ in range(args.warmup):
         sim.update(FRAME_DT)
-    total, t = 0, 0.0
+    total, psub, t = 0, 0, 0.0
+    substeps = []
     for _ in range(steps):
         n = sim.particles()[0].shape[0]
         t0 = time.perf_counter()
         sim.update(FRAME_DT)
         t += time.perf_counter() - t0
         total += n
+        substeps.append(int(sim.L.ref_frame_substeps(sim.h)))
+        psub += n * substeps[-1]
     value = total / t / 1e6
-    sample = (f"{steps} timed frame(s) of the {args.scene} workload after {warm} untimed, "
-              f"{'reference engine' if kind == 'reference' else 'C++ oracle restating it'}, {threads} thread(s)")
+    sample = (f"frames {args.warmup + 1}-{args.warmup + steps} of the {args.scene} workload after {args.warmup} "
+              f"untimed, {'reference engine' if kind == 'reference' else 'C++ oracle restating it'}, "
+              f"{threads} thread(s)")
     return {"metric": METRICS[args.scene], "value": round(value, 5), "unit": UNIT, "n_gpus": world, "steps": steps,
-            "warmup": warm, "ms_per_step": round(t / steps * 1e3, 2), "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32/f64", "data": "synthetic: seeded dam break + sphere",
-            "config": {"workload": SCENES[args.scene]},
+            "warmup": args.warmup, "ms_per_step": round(t / steps * 1e3, 2), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32/f64", "data": "synthetic: seeded dam break + sphere",
+            "config": {"workload": SCENES[args.scene], "frames_timed": [args.warmup + 1, args.warmup + steps],
+                       "substeps_per_frame": substeps,
+                       "mparticle_substeps_per_s": round(psub / t / 1e6, 5)},
             "impl": "reference",
             "cpu_baseline": {"value": round(value, 5), "unit": UNIT, "cores": threads, "kind": kind, "sample": sample},
             "e2e": {"value": round(value, 5), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -451,10 +553,12 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--reference-max-steps", type=int, default=3)
+    ap.add_argument("--reference-max-steps", type=int, default=60)
+    ap.add_argument("--cpu-frames", type=int, default=3, help="timed frames of the GPU arm's cpu_baseline")
+    ap.add_argument("--no-full-length", action="store_true", help="skip the 60-frame 128^3 timing")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched and served measurements")
     ap.add_argument("--batch-scenes", type=int, default=64)
-    ap.add_argument("--batch-steps", type=int, default=5)
+    ap.add_argument("--batch-steps", type=int, default=100)
     ap.add_argument("--workers", type=int, default=16)
     ap.add_argument("--requests", type=int, default=800)
     ap.add_argument("--served-scenes", type=int, default=256)

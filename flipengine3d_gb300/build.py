@@ -93,10 +93,15 @@ def build_oracle(force: bool = False) -> Path:
 
 
 def build_reference_checker() -> Path | None:
-    """oracle/_ref/libflipref.so from the reference sources, where present."""
+    """oracle/_ref/libflipref.so from the reference sources, where present.
+
+    oracle/build_ref.sh locates the sources (FLIP_REFERENCE_ROOT) and exits
+    with status 2 when they are absent, as on a host without the reference
+    tree; then nothing is built and None is returned."""
     script = ROOT / "oracle" / "build_ref.sh"
-    ref = Path(os.environ.get("FLIP_REFERENCE_ROOT", "/root/reference")) / "src" / "engine"
-    if not ref.is_dir():
+    r = subprocess.run(["bash", str(script)], capture_output=True, text=True)
+    if r.returncode == 2:
         return None
-    _run(["bash", str(script)])
+    if r.returncode != 0:
+        raise RuntimeError(f"oracle/build_ref.sh failed ({r.returncode}):\n{r.stdout}\n{r.stderr}")
     return ROOT / "oracle" / "_ref" / "libflipref.so"

@@ -194,6 +194,10 @@ struct PressureResult {
     int cells;
 };
 
+// Bounded device waits: poll rounds of at most ~250 ns each before a wait
+// gives up and raises the error flag (about a second).
+constexpr unsigned int DEFAULT_SPIN_LIMIT = 1u << 22;
+
 // Pipelined wavefront sweeps (flip_wavefront.cu)
 struct SweepState {
     int2 *range;             // per tile [first, last] step holding a system cell
@@ -202,6 +206,8 @@ struct SweepState {
     unsigned int *ticket;    // [0] tile tickets of the running sweep, [1] its epoch
     int *err;                // set when a bounded wait gave up
     unsigned int epoch;      // host count of the epochs issued (wrap guard)
+    unsigned int spinLimit = 0;   // poll rounds of the factor's and sweeps' waits (0: DEFAULT_SPIN_LIMIT)
+    int stall = 0;           // fault injection: the sweeps' edge waits await an epoch never published
 };
 int sweep_tiles_max(int I, int J, int K);           // tiles of the larger orientation
 long long sweep_exchange_words(int I, int J, int K);   // for the larger orientation
@@ -213,6 +219,9 @@ void launch_sweeps(const StepConsts &c, const SweepLayout &g, const float4 *L, c
                    SweepState &sw, const int *skip, cudaStream_t s);
 void sweep_epoch_guard(const StepConsts &c, SweepState &sw, long long upcoming, cudaStream_t s);
 
+void mic0_factor(const StepConsts &c, const uint8_t *fluid, const double4_32a *Ad, double *invD, double *W0,
+                 double *W1, double *W2, int *progress, unsigned int *ticket, int *err, unsigned int spinLimit,
+                 int lo, int hi, cudaStream_t s);
 int pressure_partials(const StepConsts &c);
 int pressure_partials_for(int I, int J, int K);
 int mic0_factor_tiles(int J, int K);   // tiles of the wavefront factorisation

@@ -10,7 +10,7 @@
 #include <vector>
 
 #include "../../include/flip3d.h"
-#include "flip_kernels.cuh"
+#include "flip_device.cuh"
 #include "solid_setup.h"
 
 namespace flip {
@@ -840,6 +840,36 @@ int flip_get_frame_stats(flip_ctx *x, flip_frame_stats *out) {
 int flip_get_current_frame(flip_ctx *x, int *frame) {
     if (!x || !frame) return FLIP_E_NULL;
     *frame = x->frame;
+    return FLIP_OK;
+}
+int flip_get_binned_particles(flip_ctx *x, float *pos, unsigned int *ids, int *cell_start) {
+    if (!x) return FLIP_E_NULL;
+    int rc = sync(x);
+    if (rc) return rc;
+    const size_t n = (size_t)x->n;
+    if (pos && n) {
+        CK(cudaMemcpy(pos, x->pa.px, n * 4, cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(pos + n, x->pa.py, n * 4, cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(pos + 2 * n, x->pa.pz, n * 4, cudaMemcpyDeviceToHost));
+    }
+    if (ids && n) CK(cudaMemcpy(ids, x->pa.id, n * 4, cudaMemcpyDeviceToHost));
+    if (cell_start) CK(cudaMemcpy(cell_start, x->cellStart, (x->nc() + 1) * sizeof(int), cudaMemcpyDeviceToHost));
+    return FLIP_OK;
+}
+int flip_set_device_wait_limit(flip_ctx *x, unsigned int polls) {
+    if (!x) return FLIP_E_NULL;
+    x->sweep.spinLimit = polls;
+    return FLIP_OK;
+}
+int flip_inject_sweep_stall(flip_ctx *x, int on) {
+    if (!x) return FLIP_E_NULL;
+    x->sweep.stall = on ? 1 : 0;
+    return FLIP_OK;
+}
+int flip_set_current_frame(flip_ctx *x, int frame) {
+    if (!x) return FLIP_E_NULL;
+    if (frame < 0) return fail(FLIP_E_DOMAIN, "Error: frame number must be greater than or equal to 0.");
+    x->frame = frame;
     return FLIP_OK;
 }
 int flip_get_liquid_sdf(flip_ctx *x, float *phi) {

@@ -4,7 +4,7 @@
 // nothing here is a dense contraction, so no tensor cores are involved.
 #include <cstdio>
 
-#include "flip_kernels.cuh"
+#include "flip_device.cuh"
 
 namespace flip {
 

@@ -7,7 +7,6 @@
 // device memory all comes from its own allocator, or who must not let a
 // cudaMalloc stall the device in the middle of a frame loop, can still order
 // the particles it holds.
-#include <mutex>
 #include <string>
 
 #include "../../include/flip3d.h"
@@ -111,26 +110,19 @@ __global__ void k_na_scatter(const float *px, const float *py, const float *pz, 
     out[o + 2] = pz[t];
 }
 
-// Device address of the scratch array for the current device, looked up
-// once per device.
-constexpr int NA_MAX_DEVICES = 64;
-std::mutex g_naMutex;
-int *g_naScratch[NA_MAX_DEVICES] = {};
-
-int scratch_for_current_device(int **out) {
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) return flip::record_error(FLIP_E_CUDA, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
-    if (dev < 0 || dev >= NA_MAX_DEVICES) return flip::record_error(FLIP_E_CUDA, "device ordinal beyond 63");
-    std::lock_guard<std::mutex> lock(g_naMutex);
-    if (!g_naScratch[dev]) {
-        int *ptr = nullptr;
-        e = cudaGetSymbolAddress((void **)&ptr, g_noalloc_scratch);
-        if (e != cudaSuccess || !ptr)
-            return flip::record_error(FLIP_E_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
-        g_naScratch[dev] = ptr;
-    }
-    *out = g_naScratch[dev];
+// Device address of the scratch array in the current context.  The address
+// belongs to the context that loaded this module, not to the device
+// ordinal: a host that makes its own driver contexts, or calls
+// cudaDeviceReset, gets a new one.  So it is looked up on every call; once
+// the module is loaded in the context the lookup allocates nothing.  Under
+// lazy module loading the array's 4 MiB are reserved at the first call in a
+// context, not when the library loads.
+int scratch_for_current_context(int **out) {
+    int *ptr = nullptr;
+    cudaError_t e = cudaGetSymbolAddress((void **)&ptr, g_noalloc_scratch);
+    if (e != cudaSuccess || !ptr)
+        return flip::record_error(FLIP_E_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+    *out = ptr;
     return FLIP_OK;
 }
 
@@ -148,7 +140,7 @@ extern "C" int flip_order_particles_by_id_noalloc(const float *d_px, const float
     if (n == 0) return FLIP_OK;
     if (!d_px || !d_py || !d_pz || !d_ids || !d_out_xyz) return flip::record_error(FLIP_E_NULL, "null device pointer");
     int *rank = nullptr;
-    int rc = scratch_for_current_device(&rank);
+    int rc = scratch_for_current_context(&rank);
     if (rc) return rc;
     int *sums = rank + FLIP_NOALLOC_MAX_IDS + 1;
     cudaStream_t s = (cudaStream_t)stream;

@@ -25,7 +25,7 @@
 #include <string>
 
 #include "../../include/flip3d.h"
-#include "flip_kernels.cuh"
+#include "flip_device.cuh"
 
 namespace flip {
 
@@ -295,7 +295,6 @@ __global__ void k_mic0_weights(StepConsts c, const uint8_t *fluid, const double4
 #endif
 constexpr int FT = MIC0_FT, FCH = MIC0_FCH;
 static_assert(FT * FT >= 32 && FT * FT <= 1024, "a tile is one CTA");
-constexpr unsigned int FACTOR_SPIN_LIMIT = 1u << 22;
 constexpr int FACTOR_DONE = 0x7fffffff;   // progress of a tile with all its levels done
 
 __device__ __forceinline__ int ld_acquire(const int *p) {
@@ -310,7 +309,7 @@ __device__ __forceinline__ void st_release(int *p, int v) {
 __global__ void __launch_bounds__(FT *FT) k_mic0_tiles(StepConsts c, const uint8_t *fluid, const double4_32a *Ad,
                                                        const double *W0, const double *W1, const double *W2,
                                                        double *invD, int lo, int hi, unsigned int *ticket,
-                                                       int *progress, int *err) {
+                                                       int *progress, int *err, unsigned int spinLimit) {
     __shared__ double prev[2][FT][FT];
     __shared__ int tileSh, abortSh;
     const int ntj = (c.J - 2 + FT - 1) / FT, ntk = (c.K - 2 + FT - 1) / FT;
@@ -352,7 +351,7 @@ __global__ void __launch_bounds__(FT *FT) k_mic0_tiles(StepConsts c, const uint8
                 if (nbr[q] < 0) continue;
                 unsigned int spin = 0;
                 while (ld_acquire(&progress[nbr[q]]) < need) {
-                    if (++spin >= FACTOR_SPIN_LIMIT || ld_acquire(err)) {
+                    if (++spin >= spinLimit || ld_acquire(err)) {
                         atomicExch(err, 1);
                         abortSh = 1;
                         break;
@@ -795,6 +794,44 @@ int pressure_partials_for(int I, int J, int K) {
         if (e_ != cudaSuccess) return cuda_fail(e_, #call, errMsg); \
     } while (0)
 
+// MIC(0) factor of the rows Ad over the cells flagged in `fluid`, whose
+// levels i+j+k lie in lo..hi: the inverse pivots invD (FP64).  The tiled
+// wavefront runs where it launches; otherwise one cooperative launch over all
+// levels, else one launch per level.  W0..W2: n doubles each of scratch;
+// progress: mic0_factor_tiles ints; err: set when a bounded wait gave up.
+void mic0_factor(const StepConsts &c, const uint8_t *fluid, const double4_32a *Ad, double *invD, double *W0,
+                 double *W1, double *W2, int *progress, unsigned int *ticket, int *err, unsigned int spinLimit,
+                 int lo, int hi, cudaStream_t s) {
+    const long long n = (long long)c.I * c.J * c.K;
+    const unsigned nb = div_up(n, TPB);
+    const int np = (c.J - 2) * (c.K - 2);
+    const int ntiles = mic0_factor_tiles(c.J, c.K);
+    cudaMemsetAsync(progress, 0xff, ntiles * sizeof(int), s);
+    cudaMemsetAsync(ticket, 0, sizeof(unsigned int), s);
+    { FLIP_COUNT(1); k_mic0_weights<<<nb, TPB, 0, s>>>(c, fluid, Ad, W0, W1, W2); }
+    FLIP_COUNT(1);
+    k_mic0_tiles<<<ntiles, FT * FT, 0, s>>>(c, fluid, Ad, W0, W1, W2, invD, lo, hi, ticket, progress, err, spinLimit);
+    if (cudaGetLastError() == cudaSuccess) return;
+    int dev = 0, coop = 0, perSM = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_mic0_levels, TPB, 0);
+    if (coop && perSM > 0) {
+        StepConsts c_ = c;
+        int lo_ = lo, hi_ = hi;
+        void *args[] = {&c_, &fluid, &Ad, &invD, &lo_, &hi_};
+        const int grid = std::max(1, std::min((int)div_up(np, TPB), perSM * sms));
+        FLIP_COUNT(1);
+        if (cudaLaunchCooperativeKernel((const void *)k_mic0_levels, grid, TPB, args, 0, s) == cudaSuccess) return;
+        cudaGetLastError();
+    }
+    for (int lv = lo; lv <= hi; lv++) {
+        FLIP_COUNT(1);
+        k_mic0_level<<<div_up(np, TPB), TPB, 0, s>>>(c, fluid, Ad, invD, lv);
+    }
+}
+
 int pressure_project(const StepConsts &c, const PressureArgs &a, PressureBuffers &pb, SweepState &sw,
                      PressureMail *mail, cudaStream_t s, PressureResult *res, std::string *errMsg) {
     const long long n = (long long)c.I * c.J * c.K;
@@ -857,48 +894,11 @@ int pressure_project(const StepConsts &c, const PressureArgs &a, PressureBuffers
     launch_scan_cells(pb.fluidFlag, (int)n, pb.fluidPos, pb.fluidScan, pb.nFluid, s);
     { FLIP_COUNT(1); k_compact_rows<<<nb, TPB, 0, s>>>(c, pb.sl, pb.fluid, pb.fluidPos, pb.fluidIdx, pb.fluidSk); }
 
-    // MIC(0) factor, wavefront by wavefront: one cooperative launch over all
-    // levels where the device allows it, else one launch per level
-    const int np = (c.J - 2) * (c.K - 2);
-    bool factored = false;
-    {
-        int dev = 0, coop = 0, perSM = 0, sms = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_mic0_levels, TPB, 0);
-        int lo_ = lo, hi_ = hi;
-        StepConsts c_ = c;
-        const uint8_t *fl = pb.fluid;
-        const double4_32a *ad = pb.Ad;
-        double *inv = pb.invdiagD;
-        void *args[] = {&c_, &fl, &ad, &inv, &lo_, &hi_};
-        // the tiled wavefront; the pivot weights go to q, r and x, which the
-        // loop set-up rewrites
-        {
-            const int ntiles = mic0_factor_tiles(c.J, c.K);
-            PCK(cudaMemsetAsync(pb.factorProgress, 0xff, ntiles * sizeof(int), s));
-            PCK(cudaMemsetAsync(pb.factorTicket, 0, sizeof(unsigned int), s));
-            // scratch: the 8-byte pair arrays q, r, x as FP64 arrays
-            double *w0 = reinterpret_cast<double *>(pb.q), *w1 = reinterpret_cast<double *>(pb.r),
-                   *w2 = reinterpret_cast<double *>(pb.x);
-            { FLIP_COUNT(1); k_mic0_weights<<<nb, TPB, 0, s>>>(c, pb.fluid, pb.Ad, w0, w1, w2); }
-            FLIP_COUNT(1);
-            k_mic0_tiles<<<ntiles, FT * FT, 0, s>>>(c, pb.fluid, pb.Ad, w0, w1, w2, pb.invdiagD, lo, hi,
-                                                    pb.factorTicket, pb.factorProgress, sw.err);
-            factored = cudaGetLastError() == cudaSuccess;
-        }
-        if (!factored && coop && perSM > 0) {
-            const int grid = std::max(1, std::min((int)div_up(np, TPB), perSM * sms));
-            FLIP_COUNT(1);
-            factored = cudaLaunchCooperativeKernel((const void *)k_mic0_levels, grid, TPB, args, 0, s) == cudaSuccess;
-            if (!factored) cudaGetLastError();
-        }
-    }
-    for (int lv = lo; lv <= hi && !factored; lv++) {
-        FLIP_COUNT(1);
-        k_mic0_level<<<div_up(np, TPB), TPB, 0, s>>>(c, pb.fluid, pb.Ad, pb.invdiagD, lv);
-    }
+    // MIC(0) factor; the pivot weights go to q, r and x (as FP64 arrays),
+    // which the loop set-up rewrites
+    mic0_factor(c, pb.fluid, pb.Ad, pb.invdiagD, reinterpret_cast<double *>(pb.q), reinterpret_cast<double *>(pb.r),
+                reinterpret_cast<double *>(pb.x), pb.factorProgress, pb.factorTicket, sw.err,
+                sw.spinLimit ? sw.spinLimit : DEFAULT_SPIN_LIMIT, lo, hi, s);
     { FLIP_COUNT(1); k_mic0_finalize<<<nb, TPB, 0, s>>>(c, pb.sl, pb.fluid, pb.Ad, pb.invdiagD, pb.L); }
     launch_sweep_ranges(c, pb.sl, pb.fluid, sw, s);
 

@@ -59,7 +59,9 @@ static_assert(NBUF >= 2, "the ring needs a slot in flight beside the one in use"
 constexpr int JQ = CH * TK / 32;
 static_assert((CH * TK) % 32 == 0 && TJ == 32 && JQ <= 32, "edge-word mapping of the helper warp");
 constexpr int NCOMP = NP, NTHREADS = NCOMP + 32;
-constexpr unsigned int SPIN_LIMIT = 1u << 22;   // poll rounds of <= ~250 ns: about a second
+// Waiting for this CTA's own bulk copies in flight (they complete by
+// themselves) keeps the default limit, whatever limit the edge waits have.
+constexpr unsigned int DRAIN_SPIN_LIMIT = DEFAULT_SPIN_LIMIT;
 
 struct SweepArgs {
     const float4 *L;               // factor rows, sweep layout
@@ -72,6 +74,8 @@ struct SweepArgs {
     unsigned int *ticket;          // [0] tile tickets of this launch, [1] its epoch (set by k_sweep_prep)
     int *err;
     const int *skip;   // nonzero: return at once
+    unsigned int spinLimit;    // poll rounds before a wait gives up
+    unsigned int epochSkew;    // 0; nonzero only to make the edge waits run out (fault injection)
 };
 
 struct Slot {
@@ -118,8 +122,8 @@ __device__ __forceinline__ bool mb_test(unsigned long long *b, unsigned parity) 
     return ok != 0;
 }
 // Bounded wait for a phase of an mbarrier; false on abort or timeout.
-__device__ bool mb_wait(unsigned long long *b, unsigned parity, int *abortFlag, int *err) {
-    for (unsigned int spin = 0; spin < SPIN_LIMIT; spin++) {
+__device__ bool mb_wait(unsigned long long *b, unsigned parity, int *abortFlag, int *err, unsigned int limit) {
+    for (unsigned int spin = 0; spin < limit; spin++) {
         if (mb_test(b, parity)) return true;
         if (*(volatile int *)abortFlag) return false;
         if (spin > 1024) __nanosleep(32);
@@ -193,7 +197,8 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_wavefront(SweepArgs a) {
     };
     auto pencil_in = [&](int lr, int ww) { return j0 + lr <= a.J - 2 && k0 + ww <= a.K - 2; };
     const size_t wordsPerTile = (size_t)T * (TJ + TK);
-    const unsigned int ep = sm.epoch;
+    const unsigned int ep = sm.epoch;          // published with this sweep's terms
+    const unsigned int epWait = ep + a.epochSkew;   // awaited in the neighbours' words
     // the chunk of steps [tb, tb + rows) as one block of the layout
     auto chunk_rows = [&](int n) { return min(CH, thi + 1 - (tlo + n * CH)); };
     auto chunk_row0 = [&](int rows) { return FWD ? 0 : CH - rows; };
@@ -217,7 +222,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_wavefront(SweepArgs a) {
             Slot &sl = sm.slot[b];
             if (m >= NBUF) {   // write chunk m - NBUF back once its results are in
                 const int n = m - NBUF;
-                if (!mb_wait(&sm.done[b], (n / NBUF) & 1, &sm.abort, a.err)) { ok = false; break; }
+                if (!mb_wait(&sm.done[b], (n / NBUF) & 1, &sm.abort, a.err, a.spinLimit)) { ok = false; break; }
                 if (lane == 0) {
                     const int rows = chunk_rows(n), tb = tlo + n * CH;
                     bulk_store(a.out + tileBase + (size_t)chunk_tf0(tb, rows) * NP, &sl.o[chunk_row0(rows)][0],
@@ -260,12 +265,12 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_wavefront(SweepArgs a) {
                 unsigned int missK = 0, missJ = 0;
 #pragma unroll
                 for (int s = 0; s < CH; s++)
-                    missK |= ((needK >> s) & 1u) && (unsigned int)(wK[s] >> 32) != ep ? 1u << s : 0u;
+                    missK |= ((needK >> s) & 1u) && (unsigned int)(wK[s] >> 32) != epWait ? 1u << s : 0u;
 #pragma unroll
                 for (int q = 0; q < JQ; q++)
-                    missJ |= ((needJ >> q) & 1u) && (unsigned int)(wJ[q] >> 32) != ep ? 1u << q : 0u;
+                    missJ |= ((needJ >> q) & 1u) && (unsigned int)(wJ[q] >> 32) != epWait ? 1u << q : 0u;
                 if (!(missK | missJ)) break;
-                if (spin >= SPIN_LIMIT) {
+                if (spin >= a.spinLimit) {
                     *(volatile int *)&sm.abort = 1;
                     atomicExch(a.err, 1);
                     ok = false;   // still arrive below, so that the chunk's copies can be waited for
@@ -302,7 +307,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_wavefront(SweepArgs a) {
             // before the CTA's shared memory is released.  Their phases have
             // all arrivals, so each completes once its bytes are in.
             for (int m = max(0, lastIssued - NBUF + 1); m <= lastIssued; m++)
-                for (unsigned int spin = 0; spin < SPIN_LIMIT && !mb_test(&sm.full[m % NBUF], (m / NBUF) & 1); spin++)
+                for (unsigned int spin = 0; spin < DRAIN_SPIN_LIMIT && !mb_test(&sm.full[m % NBUF], (m / NBUF) & 1); spin++)
                     __nanosleep(32);
         }
         if (lane == 0) bulk_wait_all();   // every write-back complete before the CTA ends
@@ -327,7 +332,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_wavefront(SweepArgs a) {
     float px = 0.0f, pz = 0.0f, zPrev = 0.0f;
     for (int n = 0; n < nChunks; n++) {
         const int b = n % NBUF, tb = tlo + n * CH;
-        const bool fine = mb_wait(&sm.full[b], (n / NBUF) & 1, &sm.abort, a.err);
+        const bool fine = mb_wait(&sm.full[b], (n / NBUF) & 1, &sm.abort, a.err, a.spinLimit);
         if (compute_sync_or(!fine)) {
             *(volatile int *)&sm.abort = 1;
             return;
@@ -459,6 +464,8 @@ void launch_sweeps(const StepConsts &c, const SweepLayout &g, const float4 *L, c
     a.J = g.EA; a.K = g.EB; a.NI = c.I - 2; a.T = g.T;   // extents along the lane and warp axes
     a.ntj = g.ntj; a.ntk = g.ntk;
     a.range = sw.range; a.xchg = sw.xchg; a.ticket = sw.ticket; a.err = sw.err; a.skip = skip;
+    a.spinLimit = sw.spinLimit ? sw.spinLimit : DEFAULT_SPIN_LIMIT;
+    a.epochSkew = sw.stall ? 1u : 0u;
     // forward: y from r
     a.rin = rf; a.out = z;
     { FLIP_COUNT(1); k_sweep_prep<<<1, 1, 0, s>>>(sw.ticket); }

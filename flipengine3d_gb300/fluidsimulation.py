@@ -31,6 +31,11 @@ class FlipCudaError(RuntimeError):
     """A CUDA runtime failure inside the library."""
 
 
+class FlipDeviceTimeout(RuntimeError):
+    """A bounded device wait gave up (FLIP_E_DEVICE_TIMEOUT); the simulation
+    stays usable and the next update() starts the frame afresh."""
+
+
 class FrameStats(C.Structure):
     _fields_ = [("frame", C.c_int), ("substeps", C.c_int), ("delta_time", C.c_double),
                 ("fluid_particles", C.c_int), ("pressure_iterations", C.c_int),
@@ -78,6 +83,10 @@ SIGNATURES = {
     "flip_get_marker_particle_data_device": [_P, _P, _P],
     "flip_get_frame_stats": [_P, C.POINTER(FrameStats)],
     "flip_get_current_frame": [_P, C.POINTER(C.c_int)],
+    "flip_set_current_frame": [_P, _I],
+    "flip_get_binned_particles": [_P, _P, _P, _P],
+    "flip_set_device_wait_limit": [_P, C.c_uint],
+    "flip_inject_sweep_stall": [_P, _I],
     "flip_get_liquid_sdf": [_P, _P],
     "flip_get_solid_sdf": [_P, _P],
     "flip_get_mac_velocity": [_P, _P, _P, _P],
@@ -90,6 +99,8 @@ SIGNATURES = {
     "flip_set_sweep_orientation": [_P, _I],
     "flip_get_sweep_orientation": [_P, C.POINTER(C.c_int)],
     "flip_order_particles_by_id_noalloc": [_P, _P, _P, _P, _I, _I, _P, _P],
+    "flip_mic0_factor": [_I, _I, _I, _P, _P, _P],
+    "flip_mic0_precondition": [_I, _I, _I, _P, _P, _P, _P, _I],
     "flip_get_device_bytes": [_P, C.POINTER(C.c_longlong)],
     "flip_estimate_device_bytes": [_I, _I, _I, _I, C.POINTER(C.c_longlong)],
     "flip_runtime_create": [_I, C.c_longlong, C.POINTER(C.c_void_p)],
@@ -135,6 +146,8 @@ def _check(lib, rc: int):
         raise IndexError(msg)
     if rc == FLIP_E_CUDA or rc == FLIP_E_NOMEM:
         raise FlipCudaError(msg)
+    if rc == FLIP_E_DEVICE_TIMEOUT:
+        raise FlipDeviceTimeout(msg)
     raise RuntimeError(f"flip error {rc}: {msg}")
 
 
@@ -172,6 +185,35 @@ def order_particles_by_id_noalloc(d_px: int, d_py: int, d_pz: int, d_ids: int, n
 
 
 FLIP_NOALLOC_MAX_IDS = 1 << 20
+
+
+def mic0_factor(fluid: np.ndarray, rows7: np.ndarray) -> np.ndarray:
+    """The pressure solve's MIC(0) factor (factorModifiedIncompleteColesky0,
+    pcgsolver.h:70-185) on the GPU for a 7-point system over the flagged
+    cells: fluid (K, J, I) uint8, rows7 (K, J, I, 4) float64 {diag, +x, +y,
+    +z}.  Returns the inverse pivots (K, J, I) float64, 0 off the system."""
+    lib = load_library()
+    K, J, I = fluid.shape
+    f = np.ascontiguousarray(fluid, np.uint8)
+    rows = np.ascontiguousarray(rows7, np.float64)
+    inv = np.zeros((K, J, I), np.float64)
+    _check(lib, lib.flip_mic0_factor(I, J, K, _ptr(f), _ptr(rows), _ptr(inv)))
+    return inv
+
+
+def mic0_precondition(fluid: np.ndarray, factor: np.ndarray, r: np.ndarray, orientation: int = 0) -> np.ndarray:
+    """z = M^-1 r by the pressure solve's wavefront sweeps (solveLower then
+    solveLowerTransposeInPlace, pcgsolver.h:192-221) on the GPU, in FP32:
+    factor (K, J, I, 4) float32 {invdiag, L+x, L+y, L+z}, r (K, J, I)
+    float32; orientation 0 or 1 picks the sweep tiles' lane axis."""
+    lib = load_library()
+    K, J, I = fluid.shape
+    f = np.ascontiguousarray(fluid, np.uint8)
+    L = np.ascontiguousarray(factor, np.float32)
+    rr = np.ascontiguousarray(r, np.float32)
+    z = np.zeros((K, J, I), np.float32)
+    _check(lib, lib.flip_mic0_precondition(I, J, K, _ptr(f), _ptr(L), _ptr(rr), _ptr(z), int(orientation)))
+    return z
 
 
 def estimate_device_bytes(isize: int, jsize: int, ksize: int, particles: int) -> int:
@@ -369,6 +411,12 @@ class FluidSimulation:
         self._c(self._lib.flip_get_current_frame(self._h, C.byref(v)))
         return v.value
 
+    def setCurrentFrame(self, frame: int):
+        """setCurrentFrame (fluidsimulation.cpp:98-103): resume numbering at
+        `frame`; above 0 the first substep takes its CFL speed from the
+        particles, as a run that reached this frame does."""
+        self._c(self._lib.flip_set_current_frame(self._h, int(frame)))
+
     def getFrameStatsData(self) -> FrameStats:
         s = FrameStats()
         self._c(self._lib.flip_get_frame_stats(self._h, C.byref(s)))
@@ -398,6 +446,25 @@ class FluidSimulation:
         w = np.zeros((K + 1, J, I), np.float32)
         self._c(self._lib.flip_get_mac_velocity(self._h, _ptr(u), _ptr(v), _ptr(w)))
         return u, v, w
+
+    def binned_particles(self):
+        """(positions (n, 3), ids (n,), cell_start (I*J*K + 1,)) as stored on
+        the device: sorted by cell, then by id within a cell."""
+        n = self.getNumMarkerParticles()
+        I, J, K = self.dims
+        pos = np.zeros((3, n), np.float32)
+        ids = np.zeros(n, np.uint32)
+        start = np.zeros(I * J * K + 1, np.int32)
+        self._c(self._lib.flip_get_binned_particles(self._h, _ptr(pos), _ptr(ids), _ptr(start)))
+        return pos.T.copy(), ids, start
+
+    def set_device_wait_limit(self, polls: int):
+        """Poll rounds before a bounded device wait gives up (0: default)."""
+        self._c(self._lib.flip_set_device_wait_limit(self._h, int(polls)))
+
+    def inject_sweep_stall(self, on: bool = True):
+        """Fault injection: the sweeps' edge waits await terms no tile publishes."""
+        self._c(self._lib.flip_inject_sweep_stall(self._h, 1 if on else 0))
 
     def set_stage_timing(self, enable: bool = True):
         self._c(self._lib.flip_set_stage_timing(self._h, 1 if enable else 0))

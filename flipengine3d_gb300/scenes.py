@@ -113,3 +113,40 @@ def mixed_256(seed: int = 0) -> Scene:
     """256x128x128 at dx=1/128 (domain 2 x 1 x 1), fluid in the lower 45%."""
     return dam_break(256, jsize=128, ksize=128, dx=1.0 / 128, seed=seed,
                      fill=(2.0, 0.45, 1.0), steps=30, pic_ratio=0.02)
+
+
+# -- the multi-scene sets: the batched (mixed-size) set and the served set
+
+def mixed_scene_params(count: int = 64, seed: int = 1):
+    """(edge, fill) of each scene of the mixed-size set, without its particles."""
+    rng = np.random.default_rng(seed)
+    edges = rng.choice([32, 48, 64, 80, 96], size=count)
+    fills = rng.uniform(0.2, 0.6, size=count)
+    return [(int(e), float(f)) for e, f in zip(edges, fills)]
+
+
+def mixed_scene(q: int, count: int = 64, seed: int = 1) -> Scene:
+    """Scene q of the mixed-size set: a cubic grid with its edge drawn from
+    {32, 48, 64, 80, 96} (dx = 1/edge), a dam break whose x extent (the fill
+    fraction) is drawn from [0.2, 0.6], y <= 0.6, full z, 8 jittered particles
+    per cell, FLIP blend 0.95, PCG tolerance 1e-6."""
+    e, f = mixed_scene_params(count, seed)[q]
+    return dam_break(e, seed=seed * 1000 + q, fill=(f, 0.6, 1.0))
+
+
+def served_scene_params(q: int, seed: int = 2):
+    """(edge, fill, particles per cell) of scene q of the served set."""
+    rng = np.random.default_rng([seed, q])
+    edge = int(rng.integers(32, 161))
+    fill = float(rng.uniform(0.2, 0.6))
+    ppc = int(rng.integers(4, 9))
+    return edge, fill, ppc
+
+
+def served_scene(q: int, seed: int = 2) -> Scene:
+    """Scene q of the served set: a cubic grid with its edge drawn uniformly
+    from [32, 160] (dx = 1/edge), a dam break whose x extent is drawn from
+    [0.2, 0.6], y <= 0.6, full z, 4-8 jittered particles per cell (drawn per
+    scene), FLIP blend 0.95, PCG tolerance 1e-5."""
+    edge, fill, ppc = served_scene_params(q, seed)
+    return dam_break(edge, seed=seed * 100000 + q, fill=(fill, 0.6, 1.0), ppc=ppc, tolerance=1e-5)

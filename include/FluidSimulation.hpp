@@ -85,6 +85,7 @@ public:
         check(flip_get_current_frame(ctx_, &f));
         return f;
     }
+    void setCurrentFrame(int frame) { check(flip_set_current_frame(ctx_, frame)); }
     void addBodyForce(double fx, double fy, double fz) { check(flip_add_body_force(ctx_, fx, fy, fz)); }
     void resetBodyForce() { check(flip_reset_body_force(ctx_)); }
     void setCFLConditionNumber(int n) { check(flip_set_cfl_condition_number(ctx_, n)); }

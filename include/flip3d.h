@@ -149,6 +149,12 @@ int flip_get_marker_particle_data_device(flip_ctx *ctx, float *d_positions, floa
 /* getFrameStatsData (fluidsimulation.cpp:2302-2304), getCurrentFrame (:94-96) */
 int flip_get_frame_stats(flip_ctx *ctx, flip_frame_stats *out);
 int flip_get_current_frame(flip_ctx *ctx, int *frame);
+/* setCurrentFrame (fluidsimulation.cpp:98-103): the frame number the next
+ * update() runs as.  With marker particles loaded from a saved state, a
+ * frame number above 0 makes the first substep's CFL speed the particles'
+ * own (fluidsimulation.cpp:5593-5599), so the run resumes as it left off.
+ * FLIP_E_DOMAIN for a negative frame. */
+int flip_set_current_frame(flip_ctx *ctx, int frame);
 
 /* Grid state readback for tests (sizes as in flip_stage_dump). */
 int flip_get_liquid_sdf(flip_ctx *ctx, float *phi);
@@ -184,6 +190,43 @@ int flip_get_sweep_times(flip_ctx *ctx, double *ms, long long *launches, long lo
  * of the last solve.  No counterpart in the reference. */
 int flip_set_sweep_orientation(flip_ctx *ctx, int mode);
 int flip_get_sweep_orientation(flip_ctx *ctx, int *last);
+
+/* The particles as binned on the device (test and debug interface): after
+ * initialize() and every update(), the particles are stored sorted by cell
+ * (flat index of floor(p / dx)) and, within a cell, by id, the rank in load
+ * order that the reference keeps through removals.  pos: 3 planes of n
+ * floats (x..., y..., z...); ids: n values; cell_start: I*J*K + 1 offsets
+ * of each cell's run.  Any pointer may be NULL. */
+int flip_get_binned_particles(flip_ctx *ctx, float *pos, unsigned int *ids, int *cell_start);
+
+/* Fault injection for the bounded device waits (test interface).  Every
+ * wait of the factor's and the sweeps' wavefronts gives up after `polls`
+ * poll rounds (0 restores the default, about a second) and the update
+ * returns FLIP_E_DEVICE_TIMEOUT; the context stays usable.  With the stall
+ * on, the sweeps' tiles await edge terms under an epoch no tile publishes,
+ * so any tile with an upstream neighbour tile waits until its limit runs
+ * out.  Nothing faults or hangs: each wait ends at its limit. */
+int flip_set_device_wait_limit(flip_ctx *ctx, unsigned int polls);
+int flip_inject_sweep_stall(flip_ctx *ctx, int on);
+
+/* The pressure solve's MIC(0) preconditioner alone, on a 7-point system the
+ * caller gives (unit interface; host arrays in flat cell order, device
+ * buffers allocated per call).  The system's rows are the cells flagged in
+ * `fluid`, which must lie strictly inside the I x J x K grid; rows holds
+ * {diag, to +x, to +y, to +z} per cell as doubles, zero towards unflagged
+ * neighbours.
+ *   flip_mic0_factor: the inverse pivots of factorModifiedIncompleteColesky0
+ *     (pcgsolver.h:70-185, tau 0.97, pivot floor 0.25) into invdiag (one
+ *     double per cell, 0 off the system), by the solve's wavefront kernels.
+ *   flip_mic0_precondition: z = M^-1 r by the solve's FP32 wavefront sweeps,
+ *     solveLower then solveLowerTransposeInPlace (pcgsolver.h:192-221), with
+ *     the factor given as {invdiag, L to +x, L to +y, L to +z} floats per cell;
+ *     orientation 0 or 1 picks the sweep tiles' lane axis (j or k).
+ * FLIP_E_DOMAIN for a flagged cell on the border, FLIP_E_DEVICE_TIMEOUT if a
+ * bounded wait gave up. */
+int flip_mic0_factor(int isize, int jsize, int ksize, const uint8_t *fluid, const double *rows, double *invdiag);
+int flip_mic0_precondition(int isize, int jsize, int ksize, const uint8_t *fluid, const float *factor,
+                           const float *r, float *z, int orientation);
 
 /* Number of this library's kernel launches issued so far on the context. */
 int flip_get_launch_count(flip_ctx *ctx, long long *count);
@@ -225,17 +268,20 @@ int flip_runtime_pending(flip_runtime *rt, int *queued, int *running);
  * all comes from their own allocator or pool, or frame loops in which a
  * cudaMalloc's implicit device synchronisation is not acceptable.  Inputs
  * are device arrays of n particles (x, y, z planes and ids, in any order);
- * ids must be distinct and below id_space (ids at or above it are skipped).
- * The output holds 3*n floats, packed xyz, the particle with the smallest
- * id first.  id_space may be at most FLIP_NOALLOC_MAX_IDS; a larger one is
- * rejected with FLIP_E_OUT_OF_RANGE.  The work runs on `stream` (a
- * cudaStream_t; NULL for the default stream) in a device array of about
- * 4 MiB that the library holds from load until exit on every device that
- * uses it.  The first call on a device looks that array's address up (once
- * per device, with the device current) and should come before any stream
- * capture.  Every call shares the array: calls whose work overlaps on the
- * GPU (different streams, or different threads without ordering) race, so
- * order them. */
+ * ids must be distinct and below id_space; an id at or above id_space is
+ * skipped.  The output receives packed xyz, the particle with the smallest
+ * id first, one row per distinct id below id_space: with m such ids, the
+ * first 3*m floats are written and the rest of the buffer is left as it was
+ * (m = n when every id is in range).  id_space may be at most
+ * FLIP_NOALLOC_MAX_IDS; a larger one is rejected with FLIP_E_OUT_OF_RANGE.
+ * The work runs on `stream` (a cudaStream_t; NULL for the default stream) in
+ * a device array of about 4 MiB that the library holds until exit on every
+ * device that uses it.  The array's address is looked up in the current
+ * context on every call (no allocation once the module is loaded); under
+ * lazy module loading the first call in a context loads the module, so make
+ * it before any stream capture.  Every call shares the array: calls whose
+ * work overlaps on the GPU (different streams, or different threads without
+ * ordering) race, so order them. */
 #define FLIP_NOALLOC_MAX_IDS (1 << 20)
 int flip_order_particles_by_id_noalloc(const float *d_px, const float *d_py, const float *d_pz,
                                        const unsigned int *d_ids, int n, int id_space, float *d_out_xyz,

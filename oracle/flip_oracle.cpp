@@ -213,6 +213,122 @@ static V3 closestOnTriangle(V3 p0, V3 v0, V3 v1, V3 v2) {
     return v0 + (float)s * e0 + (float)t * e1;
 }
 
+// ------------------------------------------------------------ MIC(0)-PCG
+// A row of the 7-point pressure matrix: columns ascending, diagonal included
+// (the reference's SparseMatrix rows, pcgsolver/sparsematrix.h:26-110).
+struct Row7 { int col[7]; double val[7]; int nnz; };
+
+// SparseColumnLowerFactor (pcgsolver.h:22-58): inverse diagonal and the
+// strictly lower part, column by column.
+template <class T>
+struct LowerFactor {
+    std::vector<T> invdiag;
+    std::vector<int> colstart, rowidx;
+    std::vector<T> lval;
+};
+
+// factorModifiedIncompleteColesky0 (pcgsolver.h:70-185), modification 0.97,
+// minimum diagonal ratio 0.25, on the lower triangle, column oriented.
+static void mic0_factor(const std::vector<Row7> &A, LowerFactor<double> &F) {
+    const int n = (int)A.size();
+    std::vector<double> adiag(n, 0.0);
+    F.invdiag.assign(n, 0.0);
+    F.colstart.assign(n + 1, 0);
+    F.rowidx.clear();
+    F.lval.clear();
+    for (int c = 0; c < n; c++) {
+        F.colstart[c] = (int)F.rowidx.size();
+        for (int q = 0; q < A[c].nnz; q++) {
+            if (A[c].col[q] > c) { F.rowidx.push_back(A[c].col[q]); F.lval.push_back(A[c].val[q]); }
+            else if (A[c].col[q] == c) { F.invdiag[c] = adiag[c] = A[c].val[q]; }
+        }
+    }
+    F.colstart[n] = (int)F.rowidx.size();
+    std::vector<double> &invdiag = F.invdiag, &lval = F.lval;
+    const std::vector<int> &colstart = F.colstart, &rowidx = F.rowidx;
+    const double mic = 0.97, minRatio = 0.25;
+    auto rowHas = [&](int row, int col) {
+        for (int q = 0; q < A[row].nnz; q++) if (A[row].col[q] == col) return true;
+        return false;
+    };
+    for (int k = 0; k < n; k++) {
+        if (adiag[k] == 0) continue;
+        if (invdiag[k] < minRatio * adiag[k]) invdiag[k] = 1 / std::sqrt(adiag[k]);
+        else invdiag[k] = 1 / std::sqrt(invdiag[k]);
+        for (int p = colstart[k]; p < colstart[k + 1]; p++) lval[p] *= invdiag[k];
+        for (int p = colstart[k]; p < colstart[k + 1]; p++) {
+            int j = rowidx[p];
+            double mult = lval[p];
+            double missing = 0;
+            int a = colstart[k];
+            while (a < colstart[k + 1] && rowidx[a] < j) {
+                if (!rowHas(j, rowidx[a])) missing += lval[a];
+                a++;
+            }
+            if (a < colstart[k + 1] && rowidx[a] == j) invdiag[j] -= mult * lval[a];
+            a++;
+            int bq = colstart[j];
+            while (a < colstart[k + 1] && bq < colstart[j + 1]) {
+                if (rowidx[bq] < rowidx[a]) bq++;
+                else if (rowidx[bq] == rowidx[a]) { lval[bq] -= mult * lval[a]; a++; bq++; }
+                else { missing += lval[a]; a++; }
+            }
+            while (a < colstart[k + 1]) { missing += lval[a]; a++; }
+            invdiag[j] -= mic * mult * missing;
+        }
+    }
+}
+
+// The preconditioner solve: solveLower then solveLowerTransposeInPlace
+// (pcgsolver.h:192-221), in the factor's arithmetic type T.
+template <class T>
+static void mic0_apply(const LowerFactor<T> &F, const std::vector<T> &rhs, std::vector<T> &res) {
+    const int n = (int)F.invdiag.size();
+    res = rhs;
+    for (int i = 0; i < n; i++) {
+        res[i] *= F.invdiag[i];
+        for (int q = F.colstart[i]; q < F.colstart[i + 1]; q++) res[F.rowidx[q]] -= F.lval[q] * res[i];
+    }
+    int i = n;
+    if (n == 0) return;
+    do {
+        i--;
+        for (int q = F.colstart[i]; q < F.colstart[i + 1]; q++) res[i] -= F.lval[q] * res[F.rowidx[q]];
+        res[i] *= F.invdiag[i];
+    } while (i != 0);
+}
+
+// The system of the unit entry points: rows = the flagged cells in flat
+// order; rows7[4c] the diagonal of cell c, rows7[4c+1..3] its couplings to
+// the +x, +y, +z neighbours (structural entries wherever that neighbour is
+// flagged, mirrored into the neighbour's row).
+static void unit_system(int I, int J, int K, const uint8_t *fluid, const double *rows7, std::vector<Row7> &A,
+                        std::vector<int> &cellOf, std::vector<int> &rowOf) {
+    const size_t nc = (size_t)I * J * K;
+    rowOf.assign(nc, -1);
+    cellOf.clear();
+    for (size_t t = 0; t < nc; t++)
+        if (fluid[t]) { rowOf[t] = (int)cellOf.size(); cellOf.push_back((int)t); }
+    const int n = (int)cellOf.size();
+    A.assign(n, Row7{});
+    const long long step[3] = {1, (long long)I, (long long)I * J};
+    for (int c = 0; c < n; c++) {
+        const long long t = cellOf[c];
+        int cols[7]; double vals[7]; int m = 0;
+        for (int q = 2; q >= 0; q--) {   // lower neighbours, ascending column: -z, -y, -x
+            const long long nb = t - step[q];
+            if (nb >= 0 && fluid[nb]) { cols[m] = rowOf[nb]; vals[m] = rows7[4 * nb + 1 + q]; m++; }
+        }
+        cols[m] = c; vals[m] = rows7[4 * t]; m++;
+        for (int q = 0; q < 3; q++) {    // upper neighbours, ascending: +x, +y, +z
+            const long long nb = t + step[q];
+            if (nb < (long long)nc && fluid[nb]) { cols[m] = rowOf[nb]; vals[m] = rows7[4 * t + 1 + q]; m++; }
+        }
+        for (int a = 0; a < m; a++) { A[c].col[a] = cols[a]; A[c].val[a] = vals[a]; }
+        A[c].nnz = m;
+    }
+}
+
 // ------------------------------------------------------------- simulation
 struct Sim {
     int I, J, K;
@@ -745,8 +861,7 @@ struct Sim {
         if (maxAbs < tol) return true;
 
         // matrix (:723-808): 7-point rows, columns ascending
-        struct Row { int col[7]; double val[7]; int nnz; };
-        std::vector<Row> A(n);
+        std::vector<Row7> A(n);
         double mf = dt / (dx * dx);
         const double maxtheta = 25.0, eps = 1e-9;
         for (int c = 0; c < n; c++) {
@@ -771,7 +886,7 @@ struct Sim {
             }
             diag = std::max(diag, 0.0);
             // insert sorted
-            Row &R = A[c];
+            Row7 &R = A[c];
             R.nnz = 0;
             int order[7]; double vals[7]; int m = 0;
             for (int q = 0; q < noff; q++) { order[m] = offcol[q]; vals[m] = offval[q]; m++; }
@@ -783,63 +898,9 @@ struct Sim {
             R.nnz = m;
         }
 
-        // MIC(0) (pcgsolver.h:70-185) on the lower triangle, column oriented
-        std::vector<double> invdiag(n, 0.0), adiag(n, 0.0);
-        std::vector<int> colstart(n + 1, 0);
-        std::vector<int> rowidx;
-        std::vector<double> lval;
-        for (int c = 0; c < n; c++) {
-            colstart[c] = (int)rowidx.size();
-            for (int q = 0; q < A[c].nnz; q++) {
-                if (A[c].col[q] > c) { rowidx.push_back(A[c].col[q]); lval.push_back(A[c].val[q]); }
-                else if (A[c].col[q] == c) { invdiag[c] = adiag[c] = A[c].val[q]; }
-            }
-        }
-        colstart[n] = (int)rowidx.size();
-        const double mic = 0.97, minRatio = 0.25;
-        auto rowHas = [&](int row, int col) {
-            for (int q = 0; q < A[row].nnz; q++) if (A[row].col[q] == col) return true;
-            return false;
-        };
-        for (int k = 0; k < n; k++) {
-            if (adiag[k] == 0) continue;
-            if (invdiag[k] < minRatio * adiag[k]) invdiag[k] = 1 / std::sqrt(adiag[k]);
-            else invdiag[k] = 1 / std::sqrt(invdiag[k]);
-            for (int p = colstart[k]; p < colstart[k + 1]; p++) lval[p] *= invdiag[k];
-            for (int p = colstart[k]; p < colstart[k + 1]; p++) {
-                int j = rowidx[p];
-                double mult = lval[p];
-                double missing = 0;
-                int a = colstart[k];
-                while (a < colstart[k + 1] && rowidx[a] < j) {
-                    if (!rowHas(j, rowidx[a])) missing += lval[a];
-                    a++;
-                }
-                if (a < colstart[k + 1] && rowidx[a] == j) invdiag[j] -= mult * lval[a];
-                a++;
-                int bq = colstart[j];
-                while (a < colstart[k + 1] && bq < colstart[j + 1]) {
-                    if (rowidx[bq] < rowidx[a]) bq++;
-                    else if (rowidx[bq] == rowidx[a]) { lval[bq] -= mult * lval[a]; a++; bq++; }
-                    else { missing += lval[a]; a++; }
-                }
-                while (a < colstart[k + 1]) { missing += lval[a]; a++; }
-                invdiag[j] -= mic * mult * missing;
-            }
-        }
-        auto precond = [&](const std::vector<double> &rhs, std::vector<double> &res) {
-            res = rhs;
-            for (int i = 0; i < n; i++) {
-                res[i] *= invdiag[i];
-                for (int q = colstart[i]; q < colstart[i + 1]; q++) res[rowidx[q]] -= lval[q] * res[i];
-            }
-            int i = n;
-            do {
-                i--;
-                for (int q = colstart[i]; q < colstart[i + 1]; q++) res[i] -= lval[q] * res[rowidx[q]];
-                res[i] *= invdiag[i];
-            } while (i != 0);
-        };
+        LowerFactor<double> F;
+        mic0_factor(A, F);
+        auto precond = [&](const std::vector<double> &rhs, std::vector<double> &res) { mic0_apply(F, rhs, res); };
         auto spmv = [&](const std::vector<double> &x, std::vector<double> &out) {
             parallel_ranges(n, nthreads, [&](int i0, int i1) {
                 for (int i = i0; i < i1; i++) {
@@ -1357,4 +1418,66 @@ int orc_last_pcg_iters(void *h) { return ((Sim *)h)->lastIters; }
 double orc_last_pcg_error(void *h) { return ((Sim *)h)->lastError; }
 int orc_frame_substeps(void *h) { return ((Sim *)h)->lastSubsteps; }
 
+}  // extern "C"
+
+using namespace orc;
+
+extern "C" {
+// The MIC(0) preconditioner on its own (unit checks of the factor and the
+// sweeps against the reference's routines).  invdiag: n doubles per cell
+// (0 off the system); lower: 3 doubles per cell, the scaled factor entries
+// of the cell's column towards its +x, +y, +z rows (0 where absent).
+int orc_mic0_factor(int I, int J, int K, const uint8_t *fluid, const double *rows7, double *invdiag, double *lower) {
+    std::vector<Row7> A;
+    std::vector<int> cellOf, rowOf;
+    unit_system(I, J, K, fluid, rows7, A, cellOf, rowOf);
+    LowerFactor<double> F;
+    mic0_factor(A, F);
+    const size_t nc = (size_t)I * J * K;
+    std::fill(invdiag, invdiag + nc, 0.0);
+    if (lower) std::fill(lower, lower + 3 * nc, 0.0);
+    const long long step[3] = {1, (long long)I, (long long)I * J};
+    for (size_t c = 0; c < cellOf.size(); c++) {
+        const long long t = cellOf[c];
+        invdiag[t] = F.invdiag[c];
+        if (!lower) continue;
+        for (int p = F.colstart[c]; p < F.colstart[c + 1]; p++) {
+            const long long row = cellOf[F.rowidx[p]];
+            for (int q = 0; q < 3; q++)
+                if (row == t + step[q]) lower[3 * t + q] = F.lval[p];
+        }
+    }
+    return (int)cellOf.size();
+}
+
+// z = M^-1 r in FP32 with the factor given per cell as {invdiag, L+x, L+y,
+// L+z} (floats), the sweeps in the reference's order.
+int orc_mic0_precondition_f32(int I, int J, int K, const uint8_t *fluid, const float *factor, const float *r,
+                              float *z) {
+    const size_t nc = (size_t)I * J * K;
+    std::vector<int> rowOf(nc, -1), cellOf;
+    for (size_t t = 0; t < nc; t++)
+        if (fluid[t]) { rowOf[t] = (int)cellOf.size(); cellOf.push_back((int)t); }
+    const int n = (int)cellOf.size();
+    LowerFactor<float> F;
+    F.invdiag.assign(n, 0.0f);
+    F.colstart.assign(n + 1, 0);
+    const long long step[3] = {1, (long long)I, (long long)I * J};
+    for (int c = 0; c < n; c++) {
+        const long long t = cellOf[c];
+        F.colstart[c] = (int)F.rowidx.size();
+        F.invdiag[c] = factor[4 * t];
+        for (int q = 0; q < 3; q++) {
+            const long long nb = t + step[q];
+            if (nb < (long long)nc && fluid[nb]) { F.rowidx.push_back(rowOf[nb]); F.lval.push_back(factor[4 * t + 1 + q]); }
+        }
+    }
+    F.colstart[n] = (int)F.rowidx.size();
+    std::vector<float> rhs(n), res;
+    for (int c = 0; c < n; c++) rhs[c] = r[cellOf[c]];
+    mic0_apply(F, rhs, res);
+    std::fill(z, z + nc, 0.0f);
+    for (int c = 0; c < n; c++) z[cellOf[c]] = res[c];
+    return n;
+}
 }  // extern "C"

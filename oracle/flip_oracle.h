@@ -58,6 +58,14 @@ int orc_last_pcg_iters(void *h);
 double orc_last_pcg_error(void *h);
 int orc_frame_substeps(void *h);
 
+// The MIC(0) preconditioner alone on a 7-point system over the flagged cells
+// (rows in flat cell order; rows7: {diag, +x, +y, +z} per cell).  Returns
+// the number of rows.  factor (precondition): {invdiag, L+x, L+y, L+z} floats
+// per cell.
+int orc_mic0_factor(int I, int J, int K, const uint8_t *fluid, const double *rows7, double *invdiag, double *lower);
+int orc_mic0_precondition_f32(int I, int J, int K, const uint8_t *fluid, const float *factor, const float *r,
+                              float *z);
+
 #ifdef __cplusplus
 }
 #endif

@@ -350,4 +350,86 @@ int ref_update_staged(void *h, double dt, RefStageDump *d) {
     return 0;
 }
 
+
+// The reference's MIC(0) routines alone (pcgsolver.h): the factor
+// factorModifiedIncompleteColesky0 on a SparseMatrixd built from a 7-point
+// system over the flagged cells (rows in flat cell order; rows7 = {diag, +x,
+// +y, +z} per cell, couplings mirrored into the neighbour's row), and the
+// sweeps solveLower + solveLowerTransposeInPlace instantiated for float on a
+// factor given per cell as {invdiag, L+x, L+y, L+z}.  Outputs per cell, 0 off
+// the system; lower: the scaled column entries towards +x, +y, +z.
+static void ref_unit_rows(int I, int J, int K, const uint8_t *fluid, std::vector<int> &cellOf, std::vector<int> &rowOf) {
+    const size_t nc = (size_t)I * J * K;
+    rowOf.assign(nc, -1);
+    cellOf.clear();
+    for (size_t t = 0; t < nc; t++)
+        if (fluid[t]) { rowOf[t] = (int)cellOf.size(); cellOf.push_back((int)t); }
+}
+
+int ref_mic0_factor(int I, int J, int K, const uint8_t *fluid, const double *rows7, double *invdiag, double *lower) {
+    std::vector<int> cellOf, rowOf;
+    ref_unit_rows(I, J, K, fluid, cellOf, rowOf);
+    const int n = (int)cellOf.size();
+    const size_t nc = (size_t)I * J * K;
+    const long long step[3] = {1, (long long)I, (long long)I * J};
+    SparseMatrixd A(n);
+    for (int c = 0; c < n; c++) {
+        const long long t = cellOf[c];
+        A.set(c, c, rows7[4 * t]);
+        for (int q = 0; q < 3; q++) {
+            const long long nb = t + step[q];
+            if (nb < (long long)nc && fluid[nb]) {
+                A.set(c, rowOf[nb], rows7[4 * t + 1 + q]);
+                A.set(rowOf[nb], c, rows7[4 * t + 1 + q]);
+            }
+        }
+    }
+    SparseColumnLowerFactor<double> F;
+    factorModifiedIncompleteColesky0(A, F);
+    std::fill(invdiag, invdiag + nc, 0.0);
+    if (lower) std::fill(lower, lower + 3 * nc, 0.0);
+    for (int c = 0; c < n; c++) {
+        const long long t = cellOf[c];
+        invdiag[t] = F.invdiag[c];
+        if (!lower) continue;
+        for (unsigned int p = F.colstart[c]; p < F.colstart[c + 1]; p++) {
+            const long long row = cellOf[F.rowindex[p]];
+            for (int q = 0; q < 3; q++)
+                if (row == t + step[q]) lower[3 * t + q] = F.value[p];
+        }
+    }
+    return n;
+}
+
+int ref_mic0_precondition_f32(int I, int J, int K, const uint8_t *fluid, const float *factor, const float *r,
+                              float *z) {
+    std::vector<int> cellOf, rowOf;
+    ref_unit_rows(I, J, K, fluid, cellOf, rowOf);
+    const int n = (int)cellOf.size();
+    const size_t nc = (size_t)I * J * K;
+    const long long step[3] = {1, (long long)I, (long long)I * J};
+    SparseColumnLowerFactor<float> F(n);
+    for (int c = 0; c < n; c++) {
+        const long long t = cellOf[c];
+        F.colstart[c] = (unsigned int)F.rowindex.size();
+        F.invdiag[c] = factor[4 * t];
+        for (int q = 0; q < 3; q++) {
+            const long long nb = t + step[q];
+            if (nb < (long long)nc && fluid[nb]) {
+                F.rowindex.push_back((unsigned int)rowOf[nb]);
+                F.value.push_back(factor[4 * t + 1 + q]);
+            }
+        }
+    }
+    F.colstart[n] = (unsigned int)F.rowindex.size();
+    std::fill(z, z + nc, 0.0f);
+    if (n == 0) return 0;
+    std::vector<float> rhs(n), res(n);
+    for (int c = 0; c < n; c++) rhs[c] = r[cellOf[c]];
+    solveLower(F, rhs, res);
+    solveLowerTransposeInPlace(F, res);
+    for (int c = 0; c < n; c++) z[cellOf[c]] = res[c];
+    return n;
+}
+
 }  // extern "C"

@@ -82,12 +82,109 @@ def lib(prefix: str = "ref"):
             L.ref_last_pcg_error.restype = C.c_double
         L.ref_update_staged.argtypes = [C.c_void_p, C.c_double, C.POINTER(_Dump)]
         L.ref_update_staged.restype = C.c_int
+        L.ref_mic0_factor.argtypes = [C.c_int, C.c_int, C.c_int] + [C.c_void_p] * 4
+        L.ref_mic0_factor.restype = C.c_int
+        L.ref_mic0_precondition_f32.argtypes = [C.c_int, C.c_int, C.c_int] + [C.c_void_p] * 4
+        L.ref_mic0_precondition_f32.restype = C.c_int
         _libs[prefix] = L
     return _libs[prefix]
 
 
 def _p(a):
     return a.ctypes.data_as(C.c_void_p) if a is not None else None
+
+
+def mic0_factor(fluid, rows7, prefix="ref"):
+    """The MIC(0) factor of the 7-point system over the flagged cells
+    (fluid: (K, J, I) uint8; rows7: (K, J, I, 4) float64 {diag, +x, +y, +z})
+    by the reference's factorModifiedIncompleteColesky0 ('ref') or the
+    oracle's restatement ('orc').  Returns (invdiag (K, J, I), lower
+    (K, J, I, 3)): the inverse pivots and the scaled factor entries towards
+    +x, +y, +z."""
+    L = lib(prefix)
+    K, J, I = fluid.shape
+    fluid = np.ascontiguousarray(fluid, np.uint8)
+    rows7 = np.ascontiguousarray(rows7, np.float64)
+    inv = np.zeros((K, J, I), np.float64)
+    low = np.zeros((K, J, I, 3), np.float64)
+    L.ref_mic0_factor(I, J, K, _p(fluid), _p(rows7), _p(inv), _p(low))
+    return inv, low
+
+
+def mic0_precondition_f32(fluid, factor, r, prefix="ref"):
+    """z = M^-1 r in FP32 by the reference's solveLower and
+    solveLowerTransposeInPlace instantiated for float ('ref') or the oracle's
+    restatement ('orc'); factor: (K, J, I, 4) float32 {invdiag, L+x, L+y, L+z}."""
+    L = lib(prefix)
+    K, J, I = fluid.shape
+    fluid = np.ascontiguousarray(fluid, np.uint8)
+    factor = np.ascontiguousarray(factor, np.float32)
+    r = np.ascontiguousarray(r, np.float32)
+    z = np.zeros((K, J, I), np.float32)
+    L.ref_mic0_precondition_f32(I, J, K, _p(fluid), _p(factor), _p(r), _p(z))
+    return z
+
+
+def _hash_uniform(seed, stream, shape):
+    """Uniform [0, 1) values from a splitmix64 hash of (seed, stream, index):
+    the same on every host and numpy version, so fixtures need not store the
+    inputs they were made from."""
+    n = int(np.prod(shape))
+    with np.errstate(over="ignore"):
+        x = (np.arange(n, dtype=np.uint64) + np.uint64((seed * 1000003 + stream) * 0x9E3779B97F4A7C15 % (1 << 64)))
+        x = (x + np.uint64(0x9E3779B97F4A7C15))
+        x = (x ^ (x >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+        x = (x ^ (x >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+        x = x ^ (x >> np.uint64(31))
+    return ((x >> np.uint64(11)).astype(np.float64) * (1.0 / (1 << 53))).reshape(shape)
+
+
+def random_mic0_system(shape, seed, weak_fraction=0.05, null_rows=2):
+    """A random 7-point system of the pressure solve's shape: flagged cells
+    (a union of balls, with holes) strictly inside the grid, negative
+    couplings between flagged neighbours, a diagonal that dominates them by
+    ghost-fluid terms towards unflagged neighbours, a fraction of weak rows
+    (diagonal well below the couplings' sum, so pivots fall under the 0.25
+    floor) and a few null rows (all zero).  Portable: the values depend on
+    (shape, seed) only.  Returns (fluid (K, J, I) uint8, rows7 (K, J, I, 4))."""
+    K, J, I = shape
+    kk, jj, ii = np.meshgrid(np.arange(K), np.arange(J), np.arange(I), indexing="ij")
+    inside = (ii >= 1) & (jj >= 1) & (kk >= 1) & (ii <= I - 2) & (jj <= J - 2) & (kk <= K - 2)
+    balls = _hash_uniform(seed, 0, (4, 4))
+    blob = np.zeros(shape, bool)
+    for b in balls:
+        c = b[:3] * np.array([K, J, I])
+        rad = (0.25 + 0.25 * b[3]) * min(shape)
+        blob |= (kk - c[0]) ** 2 + (jj - c[1]) ** 2 + (ii - c[2]) ** 2 <= rad * rad
+    fluid = inside & blob & (_hash_uniform(seed, 1, shape) > 0.08)
+    rows7 = np.zeros(shape + (4,), np.float64)
+    nbr = np.zeros(shape + (3,), np.float64)
+    offs = ((0, 0, 1), (0, 1, 0), (1, 0, 0))
+    for q, (dk, dj, di) in enumerate(offs):
+        shifted = np.zeros(shape, bool)
+        shifted[: K - dk, : J - dj, : I - di] = fluid[dk:, dj:, di:]
+        a = -(0.2 + 0.8 * _hash_uniform(seed, 2 + q, shape))
+        nbr[..., q] = np.where(fluid & shifted, a, 0.0)
+    rows7[..., 1:] = nbr
+    coupled = np.abs(nbr).sum(-1)
+    for q, (dk, dj, di) in enumerate(offs):   # the couplings mirrored from the lower neighbours
+        back = np.zeros(shape)
+        back[dk:, dj:, di:] = np.abs(nbr[: K - dk, : J - dj, : I - di, q])
+        coupled += back
+    diag = coupled + 2.0 * _hash_uniform(seed, 5, shape)
+    weak = _hash_uniform(seed, 6, shape) < weak_fraction
+    diag = np.where(weak, 0.3 * coupled + 1e-3, diag)
+    rows7[..., 0] = np.where(fluid, diag, 0.0)
+    cells = np.argwhere(fluid)
+    if len(cells):
+        picks = np.unique((_hash_uniform(seed, 7, (null_rows,)) * len(cells)).astype(np.int64))
+        for q in picks:
+            k, j, i = cells[q]
+            rows7[k, j, i] = 0.0
+            rows7[k, j, i - 1, 1] = 0.0
+            rows7[k, j - 1, i, 2] = 0.0
+            rows7[k - 1, j, i, 3] = 0.0
+    return fluid.astype(np.uint8), rows7
 
 
 class RefSimulation:

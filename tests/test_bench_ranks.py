@@ -57,8 +57,9 @@ def test_reference_arm_line_keeps_the_contract(built):
     the bench contract names, the same metric and unit as the GPU arm, and a
     cpu_baseline and e2e block that describe this run."""
     import json
-    args = argparse.Namespace(steps=1, warmup=0, reference_max_steps=1, scene="plain_64")
+    args = argparse.Namespace(steps=1, warmup=1, reference_max_steps=60, scene="plain_64")
     line = bench.run_reference(args, 0, 1)
+    assert line["config"]["frames_timed"] == [2, 2] and line["warmup"] == 1 and line["steps"] == 1
     json.dumps(line)
     for key in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better",
                 "scaling", "vs_baseline", "dtype", "data", "config", "impl", "cpu_baseline", "e2e"):

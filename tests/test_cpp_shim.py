@@ -44,3 +44,87 @@ def test_cpp_shim_compiles_and_maps_domain_errors(built, tmp_path):
     r = subprocess.run([str(exe)], capture_output=True, text=True, env={**os.environ})
     assert r.returncode == 0, (r.stdout, r.stderr)
     assert r.stdout.strip() == "7"
+
+
+DRIVER = r"""
+// FluidManager's sequence on the FLIP step (src/FluidManager.cpp:9-13,47-84),
+// with the fluid loaded as marker particles: construct, body force,
+// load particles, initialize, three update() frames, read positions back.
+#include <cstdio>
+#include <vector>
+#include "FluidSimulation.hpp"
+
+int main(int argc, char **argv) {
+    int I, J, K, n;
+    double dx, pic;
+    std::FILE *in = std::fopen(argv[1], "rb");
+    if (!in || std::fread(&I, 4, 1, in) != 1 || std::fread(&J, 4, 1, in) != 1 || std::fread(&K, 4, 1, in) != 1 ||
+        std::fread(&dx, 8, 1, in) != 1 || std::fread(&pic, 8, 1, in) != 1 || std::fread(&n, 4, 1, in) != 1)
+        return 2;
+    std::vector<float> pos(3 * (size_t)n), vel(3 * (size_t)n);
+    if (std::fread(pos.data(), 4, pos.size(), in) != pos.size() || std::fread(vel.data(), 4, vel.size(), in) != vel.size())
+        return 2;
+    std::fclose(in);
+    flip3d::FluidSimulation fluidsim(I, J, K, dx);
+    fluidsim.setPICFLIPRatio(pic);
+    fluidsim.addBodyForce(0.0, -9.81, 0.0);
+    flip3d::FluidSimulationMarkerParticleData data;
+    data.size = n;
+    data.positions = reinterpret_cast<char *>(pos.data());
+    data.velocities = reinterpret_cast<char *>(vel.data());
+    fluidsim.loadMarkerParticleData(data);
+    fluidsim.initialize();
+    for (int f = 0; f < 3; f++) fluidsim.update(1.0 / 120.0);
+    std::vector<char> out(fluidsim.getMarkerParticlePositionDataSize());
+    fluidsim.getMarkerParticlePositionData(out.data());
+    std::FILE *o = std::fopen(argv[2], "wb");
+    unsigned int m = fluidsim.getNumMarkerParticles();
+    std::fwrite(&m, 4, 1, o);
+    std::fwrite(out.data(), 1, out.size(), o);
+    std::fclose(o);
+    std::printf("%d %u\n", fluidsim.getCurrentFrame(), m);
+    return 0;
+}
+"""
+
+
+@pytest.mark.gpu
+def test_cpp_drop_in_steps_a_scene_like_the_oracle(gpu, tmp_path):
+    """The C++ face drives the GPU the way FluidManager drives the reference:
+    its three frames match the oracle's (reference defaults: tolerance 1e-9)."""
+    import numpy as np
+
+    from conftest import rel_err
+    from flipengine3d_gb300.scenes import dam_break
+    from oracle import refsim
+    gxx = shutil.which("g++")
+    if not gxx:
+        pytest.skip("g++ not available")
+    sc = dam_break(20, seed=31, sphere=True)
+    inp = tmp_path / "scene.bin"
+    with open(inp, "wb") as f:
+        np.array([sc.isize, sc.jsize, sc.ksize], np.int32).tofile(f)
+        np.array([sc.dx, sc.pic_ratio], np.float64).tofile(f)
+        np.array([len(sc.positions)], np.int32).tofile(f)
+        np.ascontiguousarray(sc.positions, np.float32).tofile(f)
+        np.ascontiguousarray(sc.velocities, np.float32).tofile(f)
+    src = tmp_path / "driver.cpp"
+    src.write_text(DRIVER)
+    exe = tmp_path / "driver"
+    libdir = build.library_path().parent
+    subprocess.run([gxx, "-std=c++17", "-O2", "-I", str(ROOT / "include"), str(src), "-o", str(exe),
+                    "-L", str(libdir), "-lflip3d_gb300", f"-Wl,-rpath,{libdir}"], check=True)
+    out = tmp_path / "positions.bin"
+    r = subprocess.run([str(exe), str(inp), str(out)], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, (r.stdout, r.stderr)
+    frame, m = (int(v) for v in r.stdout.split())
+    assert frame == 3
+    raw = np.fromfile(out, dtype=np.uint32, count=1)
+    pos = np.fromfile(out, dtype=np.float32, offset=4).reshape(-1, 3)
+    assert int(raw[0]) == m == len(pos)
+    orc = refsim.OracleSimulation(sc.isize, sc.jsize, sc.ksize, sc.dx).setup(sc, tolerance=1e-9)
+    for _ in range(3):
+        orc.update(sc.frame_dt)
+    rpos, _ = orc.particles()
+    assert pos.shape == rpos.shape
+    assert rel_err(pos, rpos) <= 1e-4

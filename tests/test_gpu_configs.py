@@ -1,8 +1,9 @@
 """GPU: the benchmark configurations at their full sizes.
 
 * 64^3 dam break, 10 frames: every frame against the oracle.
-* 128^3 dam break + sphere: the first frame against the oracle, then all 60
-  frames checked through properties that hold at any size.
+* 128^3 dam break + sphere: the first frame stage by stage and frames 2-12
+  against the oracle, then all 60 frames checked through properties that
+  hold at any size.
 * 256x128x128 (FLIP blend 0.98, liquid in the lower 45%): the first frame
   solved to 1e-9 on both sides, its pressure within 1e-6 relative of the
   oracle's FP64 PCG (the configuration's own target); then 30 frames of
@@ -12,6 +13,8 @@ Bars as in test_gpu_parity: liquid SDF bit-exact; pressure, faces and
 positions within 1e-5 relative after one step; 1e-4 after several frames.
 """
 from __future__ import annotations
+
+import os
 
 import numpy as np
 import pytest
@@ -25,6 +28,7 @@ pytestmark = pytest.mark.gpu
 
 RTOL = 1e-5
 RTOL_MULTI = 1e-4
+THREADS = os.cpu_count() or 1
 
 
 def frame_properties(sim, sc, n_before, label):
@@ -42,8 +46,8 @@ def frame_properties(sim, sc, n_before, label):
     return n
 
 
-def first_frame_vs_oracle(sim, sc, label, tol=None, prtol=RTOL):
-    orc = refsim.OracleSimulation(sc.isize, sc.jsize, sc.ksize, sc.dx).setup(sc, tolerance=tol)
+def first_frame_vs_oracle(sim, sc, label, tol=None, prtol=RTOL, threads=1):
+    orc = refsim.OracleSimulation(sc.isize, sc.jsize, sc.ksize, sc.dx, threads=threads).setup(sc, tolerance=tol)
     ref = orc.update_staged(sc.frame_dt)
     if tol is not None:
         sim.setPressureSolveTolerance(tol)
@@ -81,14 +85,27 @@ def test_plain_64_ten_frames_track_the_oracle(gpu):
             assert rel_err(pos, rpos) <= RTOL_MULTI, f"64^3 frame {f}"
 
 
+TRACKED_128 = 12   # frames of the 128^3 configuration compared with the oracle
+
+
 def test_plain_128_sixty_frames(gpu):
     sc = plain_128()
     with FluidSimulation.from_scene(sc) as sim:
-        first_frame_vs_oracle(sim, sc, "128^3 frame 1")
+        orc = first_frame_vs_oracle(sim, sc, "128^3 frame 1", threads=THREADS)
         n = sim.getNumMarkerParticles()
         for f in range(2, sc.steps + 1):
             sim.update(sc.frame_dt)
             n = frame_properties(sim, sc, n, f"128^3 frame {f}")
+            if f <= TRACKED_128:
+                orc.update(sc.frame_dt)
+                pos = sim.getMarkerParticlePositionData()
+                rpos, _ = orc.particles()
+                assert pos.shape == rpos.shape, f"128^3 frame {f}: particle count"
+                assert rel_err(pos, rpos) <= RTOL_MULTI, f"128^3 frame {f}: positions"
+                gi, oi = sim.getFrameStatsData().pressure_iterations, orc.L.ref_last_pcg_iters(orc.h)
+                assert abs(gi - oi) <= 1, f"128^3 frame {f}: PCG iterations {gi} vs {oi}"
+            elif f == TRACKED_128 + 1:
+                orc.close()
 
 
 def test_mixed_256_against_fp64_pcg_then_thirty_frames(gpu):

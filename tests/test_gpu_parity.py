@@ -40,6 +40,7 @@ def test_first_frame_matches_reference_golden(gpu, case):
     with FluidSimulation.from_scene(sc, tolerance=meta["tolerance"]) as sim:
         st = sim.update_staged(meta["dt"])
         check_first_frame(st, g, case)
+        assert int(st["pcg_iters"][0]) == int(g["pcg_iters"][0]), "PCG iterations differ from the reference's"
         assert st["positions"].shape == g["positions_1"].shape
         assert rel_err(st["positions"], g["positions_1"]) <= RTOL
         for _ in range(2, meta["frames"] + 1):
@@ -67,7 +68,8 @@ def test_first_frame_matches_oracle(gpu, kw):
         assert st["positions"].shape == ref["positions"].shape
         assert rel_err(st["positions"], ref["positions"]) <= RTOL
         assert rel_err(st["velocities"], ref["velocities"]) <= RTOL
-        assert abs(int(st["pcg_iters"][0]) - int(ref["pcg_iters"][0])) <= max(5, int(ref["pcg_iters"][0]) // 2)
+        # the same PCG iteration count as the oracle's FP64 PCG (pcgsolver.h:248-302)
+        assert int(st["pcg_iters"][0]) == int(ref["pcg_iters"][0]), (int(st["pcg_iters"][0]), int(ref["pcg_iters"][0]))
 
 
 def test_multi_frame_tracks_oracle(gpu):
@@ -82,6 +84,8 @@ def test_multi_frame_tracks_oracle(gpu):
             assert pos.shape == rpos.shape, f"frame {f}: particle count"
             assert rel_err(pos, rpos) <= RTOL_MULTI, f"frame {f}"
             assert np.array_equal(sim.liquid_sdf() < 0, orc.liquid_phi() < 0), f"frame {f}: fluid cells"
+            gi, oi = sim.getFrameStatsData().pressure_iterations, orc.L.ref_last_pcg_iters(orc.h)
+            assert abs(gi - oi) <= 1, f"frame {f}: PCG iterations {gi} vs the oracle's {oi}"
 
 
 def test_substepped_frame_matches_oracle(gpu):

@@ -171,12 +171,12 @@ def test_oracle_matches_reference_engine_on_the_multi_scene_sets(built, kind, ed
     """Scenes of the batched set (the first of each edge 32, 48, 80; fills
     0.2-0.6) and of the served set (4-8 particles per cell, tolerance 1e-5):
     two frames bit-identical."""
-    import bench
+    from flipengine3d_gb300 import scenes
     if kind == "mixed":
-        q = next(i for i, (e, _) in enumerate(bench.mixed_scene_params(64)) if e == edge_or_index)
-        sc = bench.mixed_scene(q)
+        q = next(i for i, (e, _) in enumerate(scenes.mixed_scene_params(64)) if e == edge_or_index)
+        sc = scenes.mixed_scene(q)
     else:
-        sc = bench.served_scene(edge_or_index)
+        sc = scenes.served_scene(edge_or_index)
     a = refsim.RefSimulation(sc.isize, sc.jsize, sc.ksize, sc.dx, threads=4, one_particle_fragment=True).setup(sc)
     b = refsim.OracleSimulation(sc.isize, sc.jsize, sc.ksize, sc.dx, threads=4).setup(sc)
     for f in range(2):
