@@ -70,3 +70,38 @@ def rel_err(a, b) -> float:
     b = np.asarray(b, np.float64)
     scale = max(np.abs(b).max(initial=0.0), 1e-30)
     return float(np.abs(a - b).max(initial=0.0) / scale)
+
+
+def aligned_rel_err(a, b, max_skips=3, tol=1e-4):
+    """rel_err of two particle arrays in particle order that may each lack a
+    few particles of the other (a particle on the solid boundary removed on
+    one side only).  Matches the rows in order, skipping a row of either
+    side where they disagree by more than `tol` (relative); returns (error
+    over the matched rows, skips), or (inf, skips) past max_skips."""
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    scale = max(np.abs(b).max(initial=0.0), 1e-30)
+    close = lambda x, y: float(np.abs(x - y).max()) / scale <= tol
+    i = j = skips = 0
+    err = 0.0
+    while True:
+        m = min(len(a) - i, len(b) - j)
+        d = np.abs(a[i:i + m] - b[j:j + m]).max(axis=1, initial=0.0) / scale if m else np.zeros(0)
+        bad = np.flatnonzero(d > tol)
+        k = int(bad[0]) if len(bad) else m
+        if k:
+            err = max(err, float(d[:k].max()))
+        i += k
+        j += k
+        if k == m:
+            skips += (len(a) - i) + (len(b) - j)
+            return (err if skips <= max_skips else float("inf")), skips
+        if i + 1 < len(a) and close(a[i + 1], b[j]):
+            i += 1
+        elif j + 1 < len(b) and close(a[i], b[j + 1]):
+            j += 1
+        else:
+            return float("inf"), skips
+        skips += 1
+        if skips > max_skips:
+            return float("inf"), skips

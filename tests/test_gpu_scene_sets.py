@@ -6,11 +6,20 @@ inside the runtime.
 * Served set: the first scene with an edge above 128 and 4 particles per
   cell (tolerance 1e-5).
 
-Each scene: two frames through update(), positions within 1e-5 relative of
-the oracle after the first frame and 1e-4 after the second, the same
-particle counts, PCG iteration counts within one of the oracle's; then the
-same scenes stepped together through the runtime (update_all) give the
-results of the scenes alone, bit for bit.
+Each scene, frame 1 stage by stage: liquid SDF bit-exact; pressure and
+PIC/FLIP velocities within 1e-5 relative; PCG iterations equal to the
+oracle's; the advected positions (before removal, all particles) within
+1e-5 relative but for at most BOUNDARY_SKIPS particles, each within two
+cells of the solid surface.  The collision step (fluidsimulation.cpp:
+4221-4296) pushes a particle out, or back to where it started, as soon as
+the solid level set at its new position is below zero; positions agree to
+1e-5 relative, not bit for bit, so at millions of particles one that lands
+within ~1e-7 of the surface can be pushed on one side only, and likewise be
+removed as inside the solid on one side only.  The survivors are therefore
+compared in particle order allowing BOUNDARY_SKIPS such particles.  Frame 2
+then starts both sides from the oracle's particles and is compared the
+same way.  Finally the same scenes stepped together through the runtime
+(update_all) give the results of each scene alone, bit for bit.
 """
 from __future__ import annotations
 
@@ -19,7 +28,7 @@ import os
 import numpy as np
 import pytest
 
-from conftest import rel_err
+from conftest import aligned_rel_err, rel_err
 from flipengine3d_gb300 import FluidRuntime, FluidSimulation
 from flipengine3d_gb300 import scenes
 from oracle import refsim
@@ -27,7 +36,7 @@ from oracle import refsim
 pytestmark = pytest.mark.gpu
 
 RTOL = 1e-5
-RTOL_MULTI = 1e-4
+BOUNDARY_SKIPS = 3
 FRAMES = 2
 THREADS = os.cpu_count() or 1
 
@@ -40,25 +49,84 @@ def chosen_scenes():
     return out
 
 
-def test_scene_sets_match_oracle_alone_and_in_the_runtime(gpu):
+def resumed(sc, pos, vel, frame):
+    """A simulation loaded with the given particles, continuing at `frame`."""
+    sim = FluidSimulation(sc.isize, sc.jsize, sc.ksize, sc.dx)
+    sim.setPICFLIPRatio(sc.pic_ratio)
+    sim.addBodyForce(*sc.gravity)
+    sim.setCFLConditionNumber(sc.cfl)
+    sim.setPressureSolveTolerance(sc.tolerance)
+    sim.loadMarkerParticleData(pos, vel)
+    sim.initialize()
+    sim.setCurrentFrame(frame)
+    return sim
+
+
+def solid_phi_at(orc, sc, pos):
+    """Trilinear solid level set (the oracle's nodal one) at the positions."""
+    phi = orc.solid_phi().astype(np.float64)
+    g = np.asarray(pos, np.float64) / sc.dx
+    i0 = np.clip(np.floor(g).astype(np.int64), 0, [sc.isize - 1, sc.jsize - 1, sc.ksize - 1])
+    f = g - i0
+    v = np.zeros(len(g))
+    for di in (0, 1):
+        for dj in (0, 1):
+            for dk in (0, 1):
+                w = (f[:, 0] if di else 1 - f[:, 0]) * (f[:, 1] if dj else 1 - f[:, 1]) * (f[:, 2] if dk else 1 - f[:, 2])
+                v += w * phi[i0[:, 2] + dk, i0[:, 1] + dj, i0[:, 0] + di]
+    return v
+
+
+def check_advected(pos, rpos, orc, sc, label):
+    assert pos.shape == rpos.shape, f"{label}: advected particle count"
+    scale = max(float(np.abs(rpos).max()), 1e-30)
+    d = np.abs(pos.astype(np.float64) - rpos).max(axis=1) / scale
+    off = np.flatnonzero(d > RTOL)
+    assert len(off) <= BOUNDARY_SKIPS, f"{label}: {len(off)} advected positions beyond {RTOL:g}"
+    if len(off):
+        near = np.minimum(np.abs(solid_phi_at(orc, sc, pos[off])), np.abs(solid_phi_at(orc, sc, rpos[off])))
+        assert (near <= 2 * sc.dx).all(), f"{label}: a position off by {d[off].max():.3g} away from the solid surface"
+
+
+def survivors_match(sim, orc, label):
+    pos = sim.getMarkerParticlePositionData()
+    rpos, _ = orc.particles()
+    err, skips = aligned_rel_err(pos, rpos, max_skips=BOUNDARY_SKIPS)
+    assert skips <= BOUNDARY_SKIPS and err <= RTOL, f"{label}: survivors {err:.3g} with {skips} boundary particles"
+
+
+@pytest.mark.parametrize("which", range(4))
+def test_scene_set_frames_match_oracle(gpu, which):
+    sc = chosen_scenes()[which]
+    label = f"{sc.name} (tol {sc.tolerance:g})"
+    orc = refsim.OracleSimulation(sc.isize, sc.jsize, sc.ksize, sc.dx, threads=THREADS).setup(sc)
+    with FluidSimulation.from_scene(sc) as sim:
+        st = sim.update_staged(sc.frame_dt)
+        ref = orc.update_staged(sc.frame_dt)
+        assert np.array_equal(st["phi"], ref["phi"]), f"{label}: liquid SDF not bit-exact"
+        assert rel_err(st["pressure"], ref["pressure"]) <= RTOL, f"{label}: pressure"
+        assert rel_err(st["vel_g2p"], ref["vel_g2p"]) <= RTOL, f"{label}: PIC/FLIP velocities"
+        check_advected(st["pos_adv"], ref["pos_adv"], orc, sc, label)
+        assert int(st["pcg_iters"][0]) == int(ref["pcg_iters"][0]), f"{label}: PCG iterations"
+        survivors_match(sim, orc, f"{label} frame 1")
+    rpos, rvel = orc.particles()
+    with resumed(sc, rpos, rvel, 1) as sim:
+        sim.update(sc.frame_dt)
+        orc.update(sc.frame_dt)
+        gi, oi = sim.getFrameStatsData().pressure_iterations, orc.L.ref_last_pcg_iters(orc.h)
+        assert abs(gi - oi) <= 1, f"{label} frame 2: PCG iterations {gi} vs the oracle's {oi}"
+        survivors_match(sim, orc, f"{label} frame 2")
+    orc.close()
+
+
+def test_scene_sets_in_the_runtime_match_alone(gpu):
     scs = chosen_scenes()
     alone = []
     for sc in scs:
-        orc = refsim.OracleSimulation(sc.isize, sc.jsize, sc.ksize, sc.dx, threads=THREADS).setup(sc)
         with FluidSimulation.from_scene(sc) as sim:
-            for f in range(FRAMES):
+            for _ in range(FRAMES):
                 sim.update(sc.frame_dt)
-                orc.update(sc.frame_dt)
-                pos = sim.getMarkerParticlePositionData()
-                rpos, _ = orc.particles()
-                label = f"{sc.name} (tol {sc.tolerance:g}) frame {f + 1}"
-                assert pos.shape == rpos.shape, f"{label}: particle count"
-                assert rel_err(pos, rpos) <= (RTOL if f == 0 else RTOL_MULTI), f"{label}: positions"
-                gi = sim.getFrameStatsData().pressure_iterations
-                oi = orc.L.ref_last_pcg_iters(orc.h)
-                assert abs(gi - oi) <= 1, f"{label}: PCG iterations {gi} vs the oracle's {oi}"
             alone.append((sim.getMarkerParticlePositionData(), sim.getMarkerParticleVelocityData()))
-        orc.close()
     sims = [FluidSimulation.from_scene(sc) for sc in scs]
     try:
         with FluidRuntime(workers=4) as rt:
