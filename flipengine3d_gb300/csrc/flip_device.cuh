@@ -144,7 +144,7 @@ struct PressureBuffers {
     float4 *A2;            // per cell {hi, lo}: the rows as exact float pairs (hi + lo = the FP64 value to 48 bits)
     float2 *x, *r, *q;     // solution, residual, A s: exact float pairs {hi, lo} (hi + lo to ~48 bits)
     float *z;              // preconditioned residual, sweep layout
-    float *s;              // search direction
+    float *s, *s2;         // search direction, double-buffered: an iteration reads one and writes the other
     float *rf;             // r rounded to FP32, the forward sweep's right-hand side, sweep layout
     SweepLayout sl;        // the orientation of the current solve
     long long nsl;         // entries allocated for the sweep layout
@@ -203,7 +203,7 @@ struct SweepState {
     int2 *range;             // per tile [first, last] step holding a system cell
     unsigned long long *xchg;  // tile edge exchange words {epoch, value}
     long long xchgWords;       // words allocated for xchg
-    unsigned int *ticket;    // [0] tile tickets of the running sweep, [1] its epoch
+    unsigned int *ticket;    // [0] forward tile tickets, [1] the sweep pair's epoch, [2] backward tile tickets
     int *err;                // set when a bounded wait gave up
     unsigned int epoch;      // host count of the epochs issued (wrap guard)
     unsigned int spinLimit = 0;   // poll rounds of the factor's and sweeps' waits (0: DEFAULT_SPIN_LIMIT)
@@ -213,10 +213,21 @@ int sweep_tiles_max(int I, int J, int K);           // tiles of the larger orien
 long long sweep_exchange_words(int I, int J, int K);   // for the larger orientation
 void launch_sweep_ranges(const StepConsts &c, const SweepLayout &g, const uint8_t *fluid, SweepState &sw,
                          cudaStream_t s);
+// Before each sweep pair, by one thread of a kernel that runs before it:
+// tile tickets from zero for both sweeps and a fresh epoch for each (the
+// forward sweep publishes under ticket[1], the backward under ticket[1]+1).
+// Kept on the device so that a captured sequence of pairs replays with new
+// epochs.
+__device__ __forceinline__ void sweep_prep(unsigned int *ticket) {
+    ticket[0] = 0u;
+    ticket[2] = 0u;
+    ticket[1] += 2u;
+}
 // z = M^-1 r with the MIC(0) factor L: forward then backward sweep
 // The launches return at once when *skip is set (a converged solve).
+// `prepped`: a kernel ahead of them on the stream already ran sweep_prep.
 void launch_sweeps(const StepConsts &c, const SweepLayout &g, const float4 *L, const float *rf, float *z,
-                   SweepState &sw, const int *skip, cudaStream_t s);
+                   SweepState &sw, const int *skip, cudaStream_t s, bool prepped = false);
 void sweep_epoch_guard(const StepConsts &c, SweepState &sw, long long upcoming, cudaStream_t s);
 
 void mic0_factor(const StepConsts &c, const uint8_t *fluid, const double4_32a *Ad, double *invD, double *W0,

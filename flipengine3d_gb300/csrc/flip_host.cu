@@ -204,7 +204,8 @@ int alloc_grids(flip_ctx *x) {
         (rc = x->alloc(&p.b, nc)) || (rc = x->alloc(&p.invdiagD, nc)) || (rc = x->alloc(&p.x, nc)) ||
         (rc = x->alloc(&p.r, nc)) || (rc = x->alloc(&p.q, nc)) || (rc = x->alloc(&p.z, nsl)) ||
         (rc = x->alloc(&p.A2, 2 * nc)) ||
-        (rc = x->alloc(&p.s, nc)) || (rc = x->alloc(&p.rf, nsl)) || (rc = x->alloc(&p.pressure, nc)))
+        (rc = x->alloc(&p.s, nc)) || (rc = x->alloc(&p.s2, nc)) || (rc = x->alloc(&p.rf, nsl)) ||
+        (rc = x->alloc(&p.pressure, nc)))
         return rc;
     if ((rc = x->alloc(&p.fluidFlag, nc + 1)) || (rc = x->alloc(&p.fluidPos, nc + 1)) ||
         (rc = x->alloc(&p.fluidScan, scan_scratch_ints((int)nc) + 4)) || (rc = x->alloc(&p.nFluid, 4)) ||
@@ -981,7 +982,7 @@ int flip_estimate_device_bytes(int isize, int jsize, int ksize, int particles, l
     b += 5 * (nc + 1) * 4 + (scan_scratch_ints((int)nc) + 4) * 4 + 16;   // binning
     b += nc * 4 + (I + 1) * (J + 1) * (K + 1) * 4 + nc;                  // phi, solid phi, solid cells
     b += faces * (4 * 3 + 1 + 1);                                        // weights, velocity, saved, valid, status
-    b += nc * (1 + 32 + 32 + 8 * 5 + 4 + 4) + nsl * (16 + 4 + 4);         // pressure system
+    b += nc * (1 + 32 + 32 + 8 * 5 + 4 * 2 + 4) + nsl * (16 + 4 + 4);     // pressure system
     b += (nc + 1) * 4 * 2 + nc * 4 * 2 + (scan_scratch_ints((int)nc) + 8) * 4;   // row list
     b += (pressure_partials_for(isize, jsize, ksize) + 32) * 8 + 64 + 16 + 32;
     b += (mic0_factor_tiles(jsize, ksize) + 1) * 4 + 64;                  // factor tiles, ticket, control

@@ -148,6 +148,7 @@ __global__ void k_build(StepConsts c, const float *phi, const float *wu, const f
         pb.r[t] = make_float2(0.0f, 0.0f);
         pb.q[t] = make_float2(0.0f, 0.0f);
         pb.s[t] = 0.0f;
+        pb.s2[t] = 0.0f;
         pb.invdiagD[t] = 0.0;
         if (!pb.fluid[t]) {
             pb.Ad[t] = make_double4_32a(0.0, 0.0, 0.0, 0.0);
@@ -526,30 +527,54 @@ __device__ __forceinline__ void df_mul_add(float ah, float al, float sv, float &
     sh = t;
 }
 
+// s = z + beta s (pcgsolver.h:295-298, beta rounded to float) fused with
 // q = A s over the rows in double-float, stored as a pair; s.q summed in
-// double-float per thread and in FP64 across threads.  The last CTA sums s.q
-// and sets alpha = rho / s.q, rounded to float as BLAS::addScaled takes it
+// double-float per thread and in FP64 across threads.  The new s of a row's
+// stencil is formed from the previous iteration's buffer sIn (so no row
+// reads a value another thread is writing) and the row's own goes to sOut.
+// In the first iteration beta = 0 and sIn = 0, so s = z.  A neighbour that
+// is not a row couples with 0 and takes s = 0.  The last CTA sums s.q and
+// sets alpha = rho / s.q, rounded to float as BLAS::addScaled takes it
 // (blaswrapper.h:129-158), and clears the iteration's residual norms.
-__global__ void k_spmv(StepConsts c, const int *__restrict__ rows, const int *nRows, const float4 *__restrict__ A2,
-                       const float *__restrict__ s, float2 *__restrict__ q, double *partials, double *scal,
-                       unsigned long long *rmaxBits, PcgCtl *ctl) {
+__global__ void k_spmv_s(StepConsts c, SweepLayout g, const int *__restrict__ rows, const int *__restrict__ rowsSk,
+                         const int *nRows, const float4 *__restrict__ A2, const float *__restrict__ z,
+                         const float *__restrict__ sIn, float *__restrict__ sOut, float2 *__restrict__ q,
+                         double *partials, double *scal, unsigned long long *rmaxBits, PcgCtl *ctl) {
     __shared__ double sh[32];
     if (ctl->done) return;
     const int n = *nRows;
+    const float beta = (float)scal[5];   // exact: beta is a float value
     const long long sy = c.I, sz = (long long)c.I * c.J;
     float2 dot = make_float2(0.0f, 0.0f);
     for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
         const long long t = rows[e];
+        const int sk = rowsSk[e];
+        int i, j, k;
+        unflatten(t, c.I, c.J, i, j, k);
         const float4 hi = A2[2 * t], lo = A2[2 * t + 1];
-        const float st = s[t];
+        const float4 hxm = A2[2 * (t - 1)], lxm = A2[2 * (t - 1) + 1];
+        const float4 hym = A2[2 * (t - sy)], lym = A2[2 * (t - sy) + 1];
+        const float4 hzm = A2[2 * (t - sz)], lzm = A2[2 * (t - sz) + 1];
+        // the search direction over the stencil's rows
+        auto snew = [&](bool row, long long tn, long long skn) {
+            return row ? __fmaf_rn(beta, sIn[tn], z[skn]) : 0.0f;
+        };
+        const float st = snew(true, t, sk);
+        const float sxp = snew(hi.y != 0.0f || lo.y != 0.0f, t + 1, sweep_index(g, i + 1, j, k));
+        const float syp = snew(hi.z != 0.0f || lo.z != 0.0f, t + sy, sweep_index(g, i, j + 1, k));
+        const float szp = snew(hi.w != 0.0f || lo.w != 0.0f, t + sz, sweep_index(g, i, j, k + 1));
+        const float sxm = snew(hxm.y != 0.0f || lxm.y != 0.0f, t - 1, sweep_index(g, i - 1, j, k));
+        const float sym = snew(hym.z != 0.0f || lym.z != 0.0f, t - sy, sweep_index(g, i, j - 1, k));
+        const float szm = snew(hzm.w != 0.0f || lzm.w != 0.0f, t - sz, sweep_index(g, i, j, k - 1));
+        sOut[t] = st;
         float accH = 0.0f, accL = 0.0f;
         df_mul_add(hi.x, lo.x, st, accH, accL);
-        df_mul_add(hi.y, lo.y, s[t + 1], accH, accL);
-        df_mul_add(hi.z, lo.z, s[t + sy], accH, accL);
-        df_mul_add(hi.w, lo.w, s[t + sz], accH, accL);
-        df_mul_add(A2[2 * (t - 1)].y, A2[2 * (t - 1) + 1].y, s[t - 1], accH, accL);
-        df_mul_add(A2[2 * (t - sy)].z, A2[2 * (t - sy) + 1].z, s[t - sy], accH, accL);
-        df_mul_add(A2[2 * (t - sz)].w, A2[2 * (t - sz) + 1].w, s[t - sz], accH, accL);
+        df_mul_add(hi.y, lo.y, sxp, accH, accL);
+        df_mul_add(hi.z, lo.z, syp, accH, accL);
+        df_mul_add(hi.w, lo.w, szp, accH, accL);
+        df_mul_add(hxm.y, lxm.y, sxm, accH, accL);
+        df_mul_add(hym.z, lym.z, sym, accH, accL);
+        df_mul_add(hzm.w, lzm.w, szm, accH, accL);
         const float2 qt = df_norm(accH, accL);
         q[t] = qt;
         dot = df_add(dot, df_scale(st, qt));
@@ -645,7 +670,9 @@ __global__ void k_update_xr(const int *__restrict__ rows, const int *__restrict_
 __global__ void k_true_residual(StepConsts c, const int *__restrict__ rows, const int *__restrict__ rowsSk,
                                 const int *nRows, const double4_32a *__restrict__ Ad, const double *__restrict__ b,
                                 const float2 *__restrict__ x, float2 *__restrict__ r, float *__restrict__ rf,
-                                unsigned long long *rmaxBits, const double *scal, PcgCtl *ctl) {
+                                unsigned long long *rmaxBits, const double *scal, PcgCtl *ctl,
+                                unsigned int *sweepTicket) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) sweep_prep(sweepTicket);   // for the sweep pair that follows
     if (ctl->done) return;
     if ((ctl->it + 1) % 25 != 0 && !ctl->claim) return;
     const int n = *nRows;
@@ -674,8 +701,9 @@ __global__ void k_true_residual(StepConsts c, const int *__restrict__ rows, cons
 
 // r = b (and its FP32 copy in the sweep layout), x = 0, |b|inf
 __global__ void k_init_r(StepConsts c, SweepLayout g, const double *b, float2 *r, float *rf, float2 *x,
-                         unsigned long long *rmaxBits) {
+                         unsigned long long *rmaxBits, unsigned int *sweepTicket) {
     const long long n = (long long)c.I * c.J * c.K;
+    if (blockIdx.x == 0 && threadIdx.x == 0) sweep_prep(sweepTicket);   // for the first sweep pair
     double m = 0.0;
 #pragma unroll 4
     for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
@@ -689,25 +717,6 @@ __global__ void k_init_r(StepConsts c, SweepLayout g, const double *b, float2 *r
         m = (av != av || av > m) ? av : m;
     }
     block_max_to(m, rmaxBits);
-}
-
-// s = z + beta s, beta = rho_new / rho as float (pcgsolver.h:295-298)
-__global__ void k_update_s(const int *__restrict__ rows, const int *__restrict__ rowsSk, const int *nRows,
-                           const float *__restrict__ z, float *__restrict__ s, const double *scal, const PcgCtl *ctl) {
-    if (ctl->done) return;
-    const int n = *nRows;
-    const float beta = (float)scal[5];
-    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
-        const int t = rows[e];
-        s[t] = __fmaf_rn(beta, s[t], z[rowsSk[e]]);
-    }
-}
-
-// s = z on the rows (s is zero elsewhere)
-__global__ void k_copy_zs(const int *__restrict__ rows, const int *__restrict__ rowsSk, const int *nRows,
-                          const float *__restrict__ z, float *__restrict__ s) {
-    const int n = *nRows;
-    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) s[rows[e]] = z[rowsSk[e]];
 }
 
 __global__ void k_x_to_float(long long n, const float2 *x, float *p) {
@@ -925,26 +934,31 @@ int pressure_project(const StepConsts &c, const PressureArgs &a, PressureBuffers
     // event pair q (recorded as graph nodes when captured)
     auto precondition = [&](int q, bool timed) {
         if (timed) record(tm->ev[2 * q]);
-        launch_sweeps(c, pb.sl, pb.L, pb.rf, pb.z, sw, &pb.ctl->done, s);
+        launch_sweeps(c, pb.sl, pb.L, pb.rf, pb.z, sw, &pb.ctl->done, s, true);   // prepared by the kernel before
         if (timed) record(tm->ev[2 * q + 1]);
         { FLIP_COUNT(1); k_dot_zr<<<rb, TPB, 0, s>>>(pb.fluidIdx, pb.fluidSk, pb.nFluid, pb.z, pb.r, pb.partials, pb.scal, pb.ctl, q > 0); }
     };
     // one PCG iteration (pcgsolver.h:263-300); every launch is the same for
-    // every iteration, the iteration index lives on the device
+    // every iteration but the search direction's two buffers, which swap
+    // roles each iteration (a batch of PCG_BATCH, an even count, ends where
+    // it began); the iteration index lives on the device
+    int sPar = 0;
     auto iteration = [&](int k, bool timed) {
-        { FLIP_COUNT(1); k_spmv<<<rb, TPB, 0, s>>>(c, pb.fluidIdx, pb.nFluid, pb.A2, pb.s, pb.q, pb.partials, pb.scal, rmax, pb.ctl); }
-        { FLIP_COUNT(1); k_update_xr<<<rb, TPB, 0, s>>>(pb.fluidIdx, pb.fluidSk, pb.nFluid, pb.x, pb.r, pb.rf, pb.s, pb.q, pb.scal, rmax, pb.ctl); }
-        { FLIP_COUNT(1); k_true_residual<<<rb, TPB, 0, s>>>(c, pb.fluidIdx, pb.fluidSk, pb.nFluid, pb.Ad, pb.b, pb.x, pb.r, pb.rf, rmax + 1, pb.scal, pb.ctl); }
+        float *sIn = sPar ? pb.s2 : pb.s, *sOut = sPar ? pb.s : pb.s2;
+        { FLIP_COUNT(1); k_spmv_s<<<rb, TPB, 0, s>>>(c, pb.sl, pb.fluidIdx, pb.fluidSk, pb.nFluid, pb.A2, pb.z, sIn, sOut, pb.q, pb.partials, pb.scal, rmax, pb.ctl); }
+        { FLIP_COUNT(1); k_update_xr<<<rb, TPB, 0, s>>>(pb.fluidIdx, pb.fluidSk, pb.nFluid, pb.x, pb.r, pb.rf, sOut, pb.q, pb.scal, rmax, pb.ctl); }
+        { FLIP_COUNT(1); k_true_residual<<<rb, TPB, 0, s>>>(c, pb.fluidIdx, pb.fluidSk, pb.nFluid, pb.Ad, pb.b, pb.x, pb.r, pb.rf, rmax + 1, pb.scal, pb.ctl, sw.ticket); }
         precondition(1 + k, timed);
-        { FLIP_COUNT(1); k_update_s<<<rb, TPB, 0, s>>>(pb.fluidIdx, pb.fluidSk, pb.nFluid, pb.z, pb.s, pb.scal, pb.ctl); }
+        sPar ^= 1;
     };
+    static_assert(PCG_BATCH % 2 == 0, "a batch must leave the search direction in the buffer it started from");
 
     mail->ptol = ptol;
     PCK(cudaMemsetAsync(pb.ctl, 0, sizeof(PcgCtl), s));
     PCK(cudaMemsetAsync(rmax, 0, 2 * sizeof(unsigned long long), s));
     PCK(cudaMemcpyAsync(pb.scal + 6, &mail->ptol, sizeof(double), cudaMemcpyHostToDevice, s));
-    { FLIP_COUNT(1); k_init_r<<<rb, TPB, 0, s>>>(c, pb.sl, pb.b, pb.r, pb.rf, pb.x, rmax); }
     sweep_epoch_guard(c, sw, 2, s);
+    { FLIP_COUNT(1); k_init_r<<<rb, TPB, 0, s>>>(c, pb.sl, pb.b, pb.r, pb.rf, pb.x, rmax, sw.ticket); }
     precondition(0, tm != nullptr);
     PCK(cudaMemcpyAsync(&mail->rho, pb.scal + 1, sizeof(double), cudaMemcpyDeviceToHost, s));
     PCK(cudaMemcpyAsync(&mail->sweepErr, sw.err, sizeof(int), cudaMemcpyDeviceToHost, s));
@@ -956,7 +970,6 @@ int pressure_project(const StepConsts &c, const PressureArgs &a, PressureBuffers
     double resid = bmax;
     int sweepErr = mail->sweepErr;   // the factor's or the first sweep's bounded wait gave up
     if (!sweepErr && !(rho0 == 0 || rho0 != rho0)) {
-        { FLIP_COUNT(1); k_copy_zs<<<rb, TPB, 0, s>>>(pb.fluidIdx, pb.fluidSk, pb.nFluid, pb.z, pb.s); }
         // Iterations go to the device PCG_BATCH at a time, as one CUDA graph
         // (captured on first use, per context): the convergence test runs
         // there and the kernels of iterations after convergence return at
@@ -1014,7 +1027,7 @@ int pressure_project(const StepConsts &c, const PressureArgs &a, PressureBuffers
     if (sweepErr) {
         cudaMemsetAsync(sw.err, 0, sizeof(int), s);
         cudaMemsetAsync(sw.xchg, 0, sweep_exchange_words(c.I, c.J, c.K) * sizeof(unsigned long long), s);
-        cudaMemsetAsync(sw.ticket, 0, 2 * sizeof(unsigned int), s);
+        cudaMemsetAsync(sw.ticket, 0, 3 * sizeof(unsigned int), s);
         sw.epoch = 0;
         sync();
         if (errMsg) *errMsg = "a wavefront (factor or sweep) gave up waiting for a neighbouring tile";

@@ -71,7 +71,8 @@ struct SweepArgs {
     int ntj, ntk;
     const int2 *range;             // per tile: first/last step (forward numbering) holding a system cell
     unsigned long long *xchg;      // per tile: T x TK j-edge words, then T x TJ k-edge words
-    unsigned int *ticket;          // [0] tile tickets of this launch, [1] its epoch (set by k_sweep_prep)
+    unsigned int *ticket;          // [0] forward tile tickets, [1] the pair's epoch, [2] backward tile tickets
+                                   // (set by sweep_prep before each pair)
     int *err;
     const int *skip;   // nonzero: return at once
     unsigned int spinLimit;    // poll rounds before a wait gives up
@@ -166,11 +167,11 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_wavefront(SweepArgs a) {
         if (*(volatile const int *)a.skip || *(volatile int *)a.err) {
             sm.tile = -1;   // converged, or an earlier sweep gave up: nothing to do
         } else {
-            int t = (int)atomicAdd(&a.ticket[0], 1u);
+            int t = (int)atomicAdd(&a.ticket[FWD ? 0 : 2], 1u);
             sm.tile = FWD ? t : ntiles - 1 - t;
         }
         sm.abort = 0;
-        sm.epoch = *(volatile unsigned int *)&a.ticket[1];
+        sm.epoch = *(volatile unsigned int *)&a.ticket[1] + (FWD ? 0u : 1u);   // forward e, backward e + 1
         for (int b = 0; b < NBUF; b++) {
             mb_init(&sm.full[b], 32);      // the helper warp's lanes, plus the bytes of the chunk
             mb_init(&sm.done[b], NCOMP);
@@ -386,13 +387,8 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_wavefront(SweepArgs a) {
     }
 }
 
-// Before each sweep launch: a fresh epoch for its exchange words and the
-// tile tickets from zero.  Kept on the device so that a captured sequence of
-// sweeps replays with new epochs.
-__global__ void k_sweep_prep(unsigned int *ticket) {
-    ticket[0] = 0u;
-    ticket[1] += 1u;
-}
+// Before a sweep pair without a kernel that prepares it (sweep_prep).
+__global__ void k_sweep_prep(unsigned int *ticket) { sweep_prep(ticket); }
 
 __global__ void k_tile_range_init(int2 *range, int n) {
     int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -447,7 +443,7 @@ void launch_sweep_ranges(const StepConsts &c, const SweepLayout &g, const uint8_
 }
 
 void launch_sweeps(const StepConsts &c, const SweepLayout &g, const float4 *L, const float *rf, float *z,
-                   SweepState &sw, const int *skip, cudaStream_t s) {
+                   SweepState &sw, const int *skip, cudaStream_t s, bool prepped) {
     const int n = g.ntj * g.ntk;
     static std::atomic<unsigned long long> smemSet{0};   // devices on which the slots' shared memory is opted in
     int dev = 0;
@@ -468,12 +464,11 @@ void launch_sweeps(const StepConsts &c, const SweepLayout &g, const float4 *L, c
     a.epochSkew = sw.stall ? 1u : 0u;
     // forward: y from r
     a.rin = rf; a.out = z;
-    { FLIP_COUNT(1); k_sweep_prep<<<1, 1, 0, s>>>(sw.ticket); }
+    if (!prepped) { FLIP_COUNT(1); k_sweep_prep<<<1, 1, 0, s>>>(sw.ticket); }
     if (g.swap) { FLIP_COUNT(1); k_wavefront<true, true><<<n, NTHREADS, sizeof(SweepSmem), s>>>(a); }
     else { FLIP_COUNT(1); k_wavefront<true, false><<<n, NTHREADS, sizeof(SweepSmem), s>>>(a); }
     // backward: z from y, in place
     a.rin = z; a.out = z;
-    { FLIP_COUNT(1); k_sweep_prep<<<1, 1, 0, s>>>(sw.ticket); }
     if (g.swap) { FLIP_COUNT(1); k_wavefront<false, true><<<n, NTHREADS, sizeof(SweepSmem), s>>>(a); }
     else { FLIP_COUNT(1); k_wavefront<false, false><<<n, NTHREADS, sizeof(SweepSmem), s>>>(a); }
     sw.epoch += 2;
@@ -484,7 +479,7 @@ void launch_sweeps(const StepConsts &c, const SweepLayout &g, const float4 *L, c
 void sweep_epoch_guard(const StepConsts &c, SweepState &sw, long long upcoming, cudaStream_t s) {
     if ((long long)sw.epoch + upcoming < 0xfffffff0LL) return;
     cudaMemsetAsync(sw.xchg, 0, sweep_exchange_words(c.I, c.J, c.K) * sizeof(unsigned long long), s);
-    cudaMemsetAsync(sw.ticket, 0, 2 * sizeof(unsigned int), s);
+    cudaMemsetAsync(sw.ticket, 0, 3 * sizeof(unsigned int), s);
     sw.epoch = 0;
 }
 
