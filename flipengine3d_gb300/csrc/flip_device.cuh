@@ -62,7 +62,8 @@ void launch_extrapolate(const StepConsts &c, float *u, float *v, float *w, const
 void launch_save_and_force(const StepConsts &c, float *u, float *v, float *w, float *su, float *sv, float *sw,
                            float fx, float fy, float fz, bool ax, bool ay, bool az, cudaStream_t s);
 void launch_constrain(const StepConsts &c, float *u, float *v, float *w, float *su, float *sv, float *sw,
-                      const float *wu, const float *wv, const float *ww, cudaStream_t s);
+                      const float *wu, const float *wv, const float *ww, const float *fu, const float *fv,
+                      const float *fw, cudaStream_t s);
 
 // -- particle update: PIC/FLIP, RK3, collision, removal tests, new keys
 void launch_advect(ParticleSoA p, int n, const StepConsts &c, const float *u, const float *v, const float *w,

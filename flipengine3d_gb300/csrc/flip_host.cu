@@ -82,6 +82,8 @@ struct flip_ctx {
     double maxSpeed = 0.0;
 
     DomainBox box;
+    std::vector<MeshObstacle> obstacles;   // static mesh obstacles (addMeshObstacle)
+    float *fu = nullptr, *fv = nullptr, *fw = nullptr;   // face friction, when an obstacle has some
     StepConsts c{};
 
     // device buffers
@@ -329,15 +331,23 @@ int collect_stage_times(flip_ctx *x) {
 }
 
 int build_solid(flip_ctx *x) {
-    x->box.compute(x->I, x->J, x->K, x->dx, x->cfl);
+    x->box.compute(x->I, x->J, x->K, x->dx, x->cfl, x->obstacles);
     cudaStream_t s = x->stream;
     CK(cudaMemcpyAsync(x->solidPhi, x->box.nodal.data(), x->box.nodal.size() * 4, cudaMemcpyHostToDevice, s));
     CK(cudaMemcpyAsync(x->wu, x->box.wu.data(), x->box.wu.size() * 4, cudaMemcpyHostToDevice, s));
     CK(cudaMemcpyAsync(x->wv, x->box.wv.data(), x->box.wv.size() * 4, cudaMemcpyHostToDevice, s));
     CK(cudaMemcpyAsync(x->ww, x->box.ww.data(), x->box.ww.size() * 4, cudaMemcpyHostToDevice, s));
     CK(cudaMemcpyAsync(x->solidCC, x->box.solidCentre.data(), x->box.solidCentre.size(), cudaMemcpyHostToDevice, s));
-    int rc = x->alloc(&x->nearSolid, x->box.near.size());
+    int rc = x->nearSolid ? FLIP_OK : x->alloc(&x->nearSolid, x->box.near.size());
     if (rc) return rc;
+    if (x->box.anyFriction) {
+        if (!x->fu && ((rc = x->alloc(&x->fu, x->nu())) || (rc = x->alloc(&x->fv, x->nv())) ||
+                       (rc = x->alloc(&x->fw, x->nw()))))
+            return rc;
+        CK(cudaMemcpyAsync(x->fu, x->box.fu.data(), x->box.fu.size() * 4, cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(x->fv, x->box.fv.data(), x->box.fv.size() * 4, cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(x->fw, x->box.fw.data(), x->box.fw.size() * 4, cudaMemcpyHostToDevice, s));
+    }
     CK(cudaMemcpyAsync(x->nearSolid, x->box.near.data(), x->box.near.size(), cudaMemcpyHostToDevice, s));
     StepConsts &c = x->c;
     c.nsi = x->box.nsi; c.nsj = x->box.nsj; c.nsk = x->box.nsk;
@@ -481,7 +491,9 @@ int step_fluid(flip_ctx *x, double dt, flip_stage_dump *d) {
     launch_extrapolate(c, x->u, x->v, x->w, x->vu, x->vv, x->vw, x->status, layers, s);
     if (d && (rc = dump_mac(x, d->u_press, d->v_press, d->w_press, x->u, x->v, x->w))) return rc;
     // constrain saved and current fields (fluidsimulation.cpp:3937-3950)
-    launch_constrain(c, x->u, x->v, x->w, x->su, x->sv, x->sw, x->wu, x->wv, x->ww, s);
+    const bool fr = x->box.anyFriction;
+    launch_constrain(c, x->u, x->v, x->w, x->su, x->sv, x->sw, x->wu, x->wv, x->ww, fr ? x->fu : nullptr,
+                     fr ? x->fv : nullptr, fr ? x->fw : nullptr, s);
     if (d && (rc = dump_mac(x, d->u_final, d->v_final, d->w_final, x->u, x->v, x->w))) return rc;
     if (d && (rc = dump_mac(x, d->u_saved, d->v_saved, d->w_saved, x->su, x->sv, x->sw))) return rc;
     if (x->n == 0) {
@@ -904,6 +916,67 @@ int flip_get_face_weights(flip_ctx *x, float *wu, float *wv, float *ww) {
     std::memcpy(ww, x->box.ww.data(), x->box.ww.size() * 4);
     return FLIP_OK;
 }
+namespace {
+// Obstacles given as plain arrays: obstacle q has nverts[q] vertices (xyz,
+// consecutive in verts) and ntris[q] triangles (vertex indices local to it,
+// consecutive in tris).
+int obstacles_from_arrays(int n, const int *nverts, const float *verts, const int *ntris, const int *tris,
+                          const float *friction, std::vector<MeshObstacle> &out) {
+    if (n < 0) return fail(FLIP_E_DOMAIN, "negative obstacle count");
+    if (n > 0 && (!nverts || !verts || !ntris || !tris)) return fail(FLIP_E_NULL, "null obstacle array");
+    size_t vo = 0, to = 0;
+    for (int q = 0; q < n; q++) {
+        if (nverts[q] < 0 || ntris[q] < 0) return fail(FLIP_E_DOMAIN, "negative vertex or triangle count");
+        MeshObstacle m;
+        m.verts.assign(verts + 3 * vo, verts + 3 * (vo + nverts[q]));
+        m.tris.assign(tris + 3 * to, tris + 3 * (to + ntris[q]));
+        for (int t : m.tris)
+            if (t < 0 || t >= nverts[q]) return fail(FLIP_E_DOMAIN, "triangle vertex index out of range");
+        for (float v : m.verts)
+            if (!std::isfinite(v)) return fail(FLIP_E_DOMAIN, "non-finite obstacle vertex");
+        m.friction = friction ? friction[q] : 0.0f;
+        if (!(m.friction >= 0.0f && m.friction <= 1.0f)) return fail(FLIP_E_DOMAIN, "friction must be in [0, 1]");
+        vo += nverts[q];
+        to += ntris[q];
+        out.push_back(std::move(m));
+    }
+    return FLIP_OK;
+}
+}  // namespace
+
+int flip_add_mesh_obstacle(flip_ctx *x, int nverts, const float *verts, int ntris, const int *tris, float friction) {
+    if (!x) return FLIP_E_NULL;
+    std::vector<MeshObstacle> one;
+    int rc = obstacles_from_arrays(1, &nverts, verts, &ntris, tris, &friction, one);
+    if (rc) return rc;
+    x->obstacles.push_back(std::move(one[0]));
+    x->solidBuilt = false;   // rebuilt before the next step (_isSolidLevelSetUpToDate, fluidsimulation.cpp:2007)
+    return FLIP_OK;
+}
+
+int flip_compute_solid(int isize, int jsize, int ksize, double dx, int cfl, int nobstacles, const int *nverts,
+                       const float *verts, const int *ntris, const int *tris, const float *friction, float *nodal,
+                       float *wu, float *wv, float *ww, int *nearDims, uint8_t *nearOut, float *fu, float *fv,
+                       float *fw) {
+    if (isize <= 0 || jsize <= 0 || ksize <= 0 || !(dx > 0.0) || cfl < 1)
+        return fail(FLIP_E_DOMAIN, "bad grid or CFL number");
+    std::vector<MeshObstacle> obs;
+    int rc = obstacles_from_arrays(nobstacles, nverts, verts, ntris, tris, friction, obs);
+    if (rc) return rc;
+    DomainBox b;
+    b.compute(isize, jsize, ksize, dx, cfl, obs);
+    if (nodal) std::memcpy(nodal, b.nodal.data(), b.nodal.size() * 4);
+    if (wu) std::memcpy(wu, b.wu.data(), b.wu.size() * 4);
+    if (wv) std::memcpy(wv, b.wv.data(), b.wv.size() * 4);
+    if (ww) std::memcpy(ww, b.ww.data(), b.ww.size() * 4);
+    if (nearDims) { nearDims[0] = b.nsi; nearDims[1] = b.nsj; nearDims[2] = b.nsk; }
+    if (nearOut) std::memcpy(nearOut, b.near.data(), b.near.size());
+    if (fu) std::memcpy(fu, b.fu.data(), b.fu.size() * 4);
+    if (fv) std::memcpy(fv, b.fv.data(), b.fv.size() * 4);
+    if (fw) std::memcpy(fw, b.fw.data(), b.fw.size() * 4);
+    return FLIP_OK;
+}
+
 int flip_compute_domain_solid(int isize, int jsize, int ksize, double dx, int cfl, float *nodal, float *wu,
                               float *wv, float *ww, int *nearDims, uint8_t *nearOut) {
     if (isize <= 0 || jsize <= 0 || ksize <= 0 || !(dx > 0.0) || cfl < 1)

@@ -488,21 +488,30 @@ __global__ void k_save_force(long long nu, long long nv, long long nw, float *u,
     }
 }
 
-// Faces with zero fluid weight take the solid velocity, which is zero for the
-// static domain walls; partly solid faces blend with the wall friction (zero
-// for the domain), which leaves them unchanged
-// (src/engine/fluidsimulation.cpp:3884-3950).
+// Faces with zero fluid weight take the solid velocity, which is zero for
+// static solids; partly solid faces blend it with their own velocity by the
+// mean friction of the solid objects closest to their four corners
+// (src/engine/fluidsimulation.cpp:3785-3846, 3884-3950).  The domain walls
+// have no friction: without friction arrays those faces stay as they are.
 __global__ void k_constrain(long long nu, long long nv, long long nw, float *u, float *v, float *w, float *su,
-                            float *sv, float *sw, const float *wu, const float *wv, const float *ww) {
+                            float *sv, float *sw, const float *wu, const float *wv, const float *ww, const float *fu,
+                            const float *fv, const float *fw) {
     long long f = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (f < nu) {
-        if (wu[f] == 0.0f) { u[f] = 0.0f; su[f] = 0.0f; }
-    } else if (f < nu + nv) {
-        long long l = f - nu;
-        if (wv[l] == 0.0f) { v[l] = 0.0f; sv[l] = 0.0f; }
-    } else if (f < nu + nv + nw) {
-        long long l = f - nu - nv;
-        if (ww[l] == 0.0f) { w[l] = 0.0f; sw[l] = 0.0f; }
+    float *G, *S;
+    const float *W, *F;
+    long long l;
+    if (f < nu) { G = u; S = su; W = wu; F = fu; l = f; }
+    else if (f < nu + nv) { G = v; S = sv; W = wv; F = fv; l = f - nu; }
+    else if (f < nu + nv + nw) { G = w; S = sw; W = ww; F = fw; l = f - nu - nv; }
+    else return;
+    const float wt = W[l];
+    if (wt == 0.0f) {   // inside the solid: the solid's velocity (zero for static solids)
+        G[l] = 0.0f;
+        S[l] = 0.0f;
+    } else if (wt < 1.0f && F) {   // part solid: f usolid + (1 - f) u, usolid = 0
+        const float fr = F[l], keep = __fsub_rn(1.0f, fr), us = __fmul_rn(fr, 0.0f);
+        G[l] = __fadd_rn(us, __fmul_rn(keep, G[l]));
+        S[l] = __fadd_rn(us, __fmul_rn(keep, S[l]));
     }
 }
 
@@ -804,10 +813,11 @@ void launch_save_and_force(const StepConsts &c, float *u, float *v, float *w, fl
     { FLIP_COUNT(1); k_save_force<<<div_up(nu + nv + nw, TPB), TPB, 0, s>>>(nu, nv, nw, u, v, w, su, sv, sw, fx, fy, fz, ax, ay, az); }
 }
 void launch_constrain(const StepConsts &c, float *u, float *v, float *w, float *su, float *sv, float *sw,
-                      const float *wu, const float *wv, const float *ww, cudaStream_t s) {
+                      const float *wu, const float *wv, const float *ww, const float *fu, const float *fv,
+                      const float *fw, cudaStream_t s) {
     long long nu = (long long)(c.I + 1) * c.J * c.K, nv = (long long)c.I * (c.J + 1) * c.K,
               nw = (long long)c.I * c.J * (c.K + 1);
-    { FLIP_COUNT(1); k_constrain<<<div_up(nu + nv + nw, TPB), TPB, 0, s>>>(nu, nv, nw, u, v, w, su, sv, sw, wu, wv, ww); }
+    { FLIP_COUNT(1); k_constrain<<<div_up(nu + nv + nw, TPB), TPB, 0, s>>>(nu, nv, nw, u, v, w, su, sv, sw, wu, wv, ww, fu, fv, fw); }
 }
 void launch_advect(ParticleSoA p, int n, const StepConsts &c, const float *u, const float *v, const float *w,
                    const float *su, const float *sv, const float *sw, const float *solidPhi,

@@ -1,4 +1,5 @@
-// Static solid set-up for the domain walls (host, once per simulation).
+// Static solid set-up: the domain walls and static mesh obstacles (host,
+// once per solid configuration).
 //
 // The reference builds its solid level set from the domain box mesh: the
 // AABB (0,0,0)-(I dx, J dx, K dx) shrunk by 3 dx + 1e-4
@@ -11,7 +12,15 @@
 // "solid at cell centre" flags the liquid SDF post-process uses
 // (particlelevelset.cpp:172-196, meshlevelset.cpp:152-162), and the coarse
 // near-solid grid of the collision test (fluidsimulation.cpp:3083-3126).
-// The walls are static, so this runs once; the per-step work is on the GPU.
+// Each static mesh obstacle adds a level set over the sub-grid that its
+// bounding box spans (meshobject.cpp:239-265, 515-553): the exact band in
+// the same block frame, signs from the parity of z-ray crossings through the
+// nodes (meshutils.cpp:99-215, 347-428), unioned into the walls' level set
+// through a temporary one (fluidsimulation.cpp:2927-2966, meshlevelset.cpp:
+// 603-638, 1758-1790).  The union also records, per node, which object is
+// closest: its friction blends the velocity of part-solid faces in the
+// constrain step (fluidsimulation.cpp:3785-3846, 3884-3935).
+// The solids are static, so this runs once; the per-step work is on the GPU.
 #include "solid_setup.h"
 
 #include <algorithm>
@@ -107,16 +116,151 @@ float frac4(float bl, float br, float tl, float tr) {
     return area;
 }
 
+inline V cross(V a, V b) {
+    return V{a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+inline int floor_index(float p, double dx) { return (int)std::floor((double)p * (1.0 / dx)); }
+
+// Collision::lineIntersectsTriangle (collision.cpp:79-118) for the ray
+// direction (0, 0, 1), in its float arithmetic: the z of the crossing.
+bool ray_z_crossing(V p, V v0, V v1, V v2, float *z) {
+    const V dir{0.0f, 0.0f, 1.0f};
+    const V e1 = vsub(v1, v0), e2 = vsub(v2, v0);
+    const V h = cross(dir, e2);
+    const float a = vdot(e1, h);
+    if (std::fabs(a) < 10e-9) return false;
+    const float f = 1 / a;
+    const V s = vsub(p, v0);
+    const float u = f * vdot(s, h);
+    if (u < 0.0 || u > 1.0) return false;
+    const V q = cross(s, e1);
+    const float v = f * vdot(dir, q);
+    if (v < 0.0 || u + v > 1.0) return false;
+    const double t = f * vdot(e2, q);
+    *z = p.z + (float)t * dir.z;
+    return true;
+}
+
+// The level set of one mesh over a sub-grid of nI x nJ x nK nodes whose
+// first node sits at `origin` (float position): the exact band in the block
+// frame and the signs from z-ray parity (meshlevelset.cpp:572-601,
+// 781-1158, 1298-1316).  Vertices are already relative to `origin`.
+void mesh_level_set(const std::vector<V> &vtx, const std::vector<int> &tris, int nI, int nJ, int nK, double dx,
+                    int band, std::vector<float> &phi, std::vector<int> &tri) {
+    const float upper = (float)((double)(nI + nJ + nK) * dx);
+    auto nid = [&](int i, int j, int k) { return (size_t)i + (size_t)nI * ((size_t)j + (size_t)nJ * k); };
+    phi.assign((size_t)nI * nJ * nK, upper);
+    tri.assign(phi.size(), -1);
+    const int bw = 10;
+    const int ntri = (int)tris.size() / 3;
+    for (int t = 0; t < ntri; t++) {
+        const V a = vtx[tris[3 * t]], b = vtx[tris[3 * t + 1]], e = vtx[tris[3 * t + 2]];
+        // AABB of the triangle: float minimum, double extent (aabb.cpp:84-110)
+        const float mn[3] = {std::min(a.x, std::min(b.x, e.x)), std::min(a.y, std::min(b.y, e.y)), std::min(a.z, std::min(b.z, e.z))};
+        const double ext[3] = {(double)std::max(a.x, std::max(b.x, e.x)) - mn[0], (double)std::max(a.y, std::max(b.y, e.y)) - mn[1],
+                               (double)std::max(a.z, std::max(b.z, e.z)) - mn[2]};
+        int lo[3], hi[3];
+        const int n[3] = {nI, nJ, nK};
+        bool outside = false;
+        for (int q = 0; q < 3; q++) {
+            lo[q] = floor_index(mn[q], dx) - band;
+            hi[q] = floor_index(mn[q] + (float)ext[q], dx) + band + 1;
+            if (hi[q] < 0 || lo[q] >= n[q]) outside = true;
+            lo[q] = std::max(lo[q], 0);
+            hi[q] = std::min(hi[q], n[q] - 1);
+        }
+        if (outside) continue;
+        for (int k = lo[2]; k <= hi[2]; k++)
+            for (int j = lo[1]; j <= hi[1]; j++)
+                for (int i = lo[0]; i <= hi[0]; i++) {
+                    const V off{gpos(i / bw, (double)bw * dx), gpos(j / bw, (double)bw * dx), gpos(k / bw, (double)bw * dx)};
+                    const V g{gpos(i % bw, dx), gpos(j % bw, dx), gpos(k % bw, dx)};
+                    const float dist = vlen(vsub(closest_point(g, vsub(a, off), vsub(b, off), vsub(e, off)), g));
+                    const size_t id = nid(i, j, k);
+                    if (dist < phi[id]) {
+                        phi[id] = dist;
+                        tri[id] = t;
+                    }
+                }
+    }
+    // Signs: the nodes become the cell centres of a grid shifted by half a
+    // cell, and a node is inside when the z-ray through it crosses the mesh
+    // an even number of times in all and an odd number of times below it
+    // (meshutils.cpp:156-215, 347-371).  The reference jitters the ray
+    // origins by a random amount below 0.001 dx against rays that graze an
+    // edge; here the jitter is a fixed amount in that range.
+    const float half = (float)(0.5 * dx);
+    std::vector<V> m(vtx.size());
+    for (size_t q = 0; q < vtx.size(); q++) m[q] = vadd(vtx[q], V{half, half, half});
+    if (m.empty()) return;
+    float bmin[3] = {m[0].x, m[0].y, m[0].z}, bmax[3] = {m[0].x, m[0].y, m[0].z};
+    for (const V &v : m) {
+        bmin[0] = std::min(bmin[0], v.x); bmin[1] = std::min(bmin[1], v.y); bmin[2] = std::min(bmin[2], v.z);
+        bmax[0] = std::max(bmax[0], v.x); bmax[1] = std::max(bmax[1], v.y); bmax[2] = std::max(bmax[2], v.z);
+    }
+    const double bext[3] = {(double)bmax[0] - bmin[0], (double)bmax[1] - bmin[1], (double)bmax[2] - bmin[2]};
+    const int go[3] = {floor_index(bmin[0], dx), floor_index(bmin[1], dx), floor_index(bmin[2], dx)};
+    const V offset{gpos(go[0], dx), gpos(go[1], dx), gpos(go[2], dx)};
+    const V noff{-offset.x, -offset.y, -offset.z};
+    for (V &v : m) v = vadd(v, noff);
+    float bpos[3] = {bmin[0] - offset.x, bmin[1] - offset.y, bmin[2] - offset.z};
+    const int cI = floor_index(bpos[0] + (float)bext[0], dx) + 1;
+    const int cJ = floor_index(bpos[1] + (float)bext[1], dx) + 1;
+    const int cK = floor_index(bpos[2] + (float)bext[2], dx) + 1;
+    if (cI <= 0 || cJ <= 0 || cK <= 0) return;
+    // triangles of each z-column (in triangle order)
+    std::vector<std::vector<int>> column((size_t)cI * cJ);
+    for (int t = 0; t < ntri; t++) {
+        const V a = m[tris[3 * t]], b = m[tris[3 * t + 1]], e = m[tris[3 * t + 2]];
+        const float mn[2] = {std::min(a.x, std::min(b.x, e.x)), std::min(a.y, std::min(b.y, e.y))};
+        const double ext[2] = {(double)std::max(a.x, std::max(b.x, e.x)) - mn[0], (double)std::max(a.y, std::max(b.y, e.y)) - mn[1]};
+        const int i0 = std::max(floor_index(mn[0], dx), 0), j0 = std::max(floor_index(mn[1], dx), 0);
+        const int i1 = std::min(floor_index(mn[0] + (float)ext[0], dx), cI - 1);
+        const int j1 = std::min(floor_index(mn[1] + (float)ext[1], dx), cJ - 1);
+        for (int j = j0; j <= j1; j++)
+            for (int i = i0; i <= i1; i++) column[(size_t)i + (size_t)cI * j].push_back(t);
+    }
+    const V jitter{(float)(0.00031 * dx), (float)(-0.00047 * dx), (float)(0.00023 * dx)};
+    const double hw = 0.5 * dx;
+    std::vector<float> zc;
+    for (int j = 0; j < cJ; j++)
+        for (int i = 0; i < cI; i++) {
+            const std::vector<int> &ts = column[(size_t)i + (size_t)cI * j];
+            if (ts.empty()) continue;
+            const V gp = vadd(V{(float)((float)i * dx + hw), (float)((float)j * dx + hw), (float)((float)-1 * dx + hw)}, jitter);
+            zc.clear();
+            for (int t : ts) {
+                float z;
+                if (ray_z_crossing(gp, m[tris[3 * t]], m[tris[3 * t + 1]], m[tris[3 * t + 2]], &z)) zc.push_back(z);
+            }
+            if (zc.size() % 2 != 0) continue;
+            for (int k = 0; k < cK; k++) {
+                const float zk = (float)((float)k * dx + hw);
+                int less = 0;
+                for (float z : zc) less += z < zk;
+                if (less % 2 == 1) {   // node (i, j, k) + goffset is inside
+                    const int ni = i + go[0], nj = j + go[1], nk = k + go[2];
+                    if (ni >= 0 && nj >= 0 && nk >= 0 && ni < nI && nj < nJ && nk < nK) {
+                        float &v = phi[nid(ni, nj, nk)];
+                        v = -v;
+                    }
+                }
+            }
+        }
+}
+
 }  // namespace
 
-void DomainBox::compute(int I_, int J_, int K_, double dx_, double cfl) {
+void DomainBox::compute(int I_, int J_, int K_, double dx_, double cfl, const std::vector<MeshObstacle> &obstacles) {
     I = I_; J = J_; K = K_; dx = dx_;
     // boundary box: AABB::expand(-3dx - 1e-4): position -= h, extent += v
     double v = -3 * dx - 1e-4, h = 0.5 * v;
     px = 0.0f - (float)h; py = 0.0f - (float)h; pz = 0.0f - (float)h;
     ex = I * dx + v; ey = J * dx + v; ez = K * dx + v;
     const int ni = I + 1, nj = J + 1, nk = K + 1;
-    nodal.assign((size_t)ni * nj * nk, (float)((double)(ni + nj + nk) * dx));
+    const float upper = (float)((double)(ni + nj + nk) * dx);
+    nodal.assign((size_t)ni * nj * nk, upper);
+    nodeObject.assign(nodal.size(), -1);
     auto nidx = [&](int i, int j, int k) { return (size_t)i + (size_t)ni * ((size_t)j + (size_t)nj * k); };
     float X1 = (float)(px + ex), Y1 = (float)(py + ey), Z1 = (float)(pz + ez);
     V c[8] = {{px, py, pz}, {X1, py, pz}, {X1, py, Z1}, {px, py, Z1}, {px, Y1, pz}, {X1, Y1, pz}, {X1, Y1, Z1}, {px, Y1, Z1}};
@@ -139,7 +283,10 @@ void DomainBox::compute(int I_, int J_, int K_, double dx_, double cfl) {
                     V g{gpos(i % bw, dx), gpos(j % bw, dx), gpos(k % bw, dx)};
                     float dist = vlen(vsub(closest_point(g, vsub(a, off), vsub(b, off), vsub(e, off)), g));
                     float &cur = nodal[nidx(i, j, k)];
-                    if (dist < cur) cur = dist;
+                    if (dist < cur) {
+                        cur = dist;
+                        nodeObject[nidx(i, j, k)] = 0;   // the domain walls
+                    }
                 }
     }
     // inside the box -> negative, then negate: the fluid region is positive
@@ -151,6 +298,66 @@ void DomainBox::compute(int I_, int J_, int K_, double dx_, double cfl) {
                 float &val = nodal[nidx(i, j, k)];
                 val = inside ? val : -val;
             }
+
+    // static mesh obstacles: each one's level set over its sub-grid, unioned
+    // into a temporary full-grid level set, which is unioned into the walls'
+    // (a node takes the smaller value; its closest object changes only where
+    // the new value is also smaller in magnitude and came from the band)
+    for (size_t q = 0; q < obstacles.size(); q++) {
+        const MeshObstacle &ob = obstacles[q];
+        const int nv = (int)ob.verts.size() / 3;
+        if (nv == 0 || ob.tris.empty()) continue;
+        std::vector<V> wv(nv);
+        for (int v = 0; v < nv; v++) wv[v] = V{ob.verts[3 * v], ob.verts[3 * v + 1], ob.verts[3 * v + 2]};
+        float lo[3] = {wv[0].x, wv[0].y, wv[0].z}, hi[3] = {wv[0].x, wv[0].y, wv[0].z};
+        for (const V &v : wv) {
+            lo[0] = std::min(lo[0], v.x); lo[1] = std::min(lo[1], v.y); lo[2] = std::min(lo[2], v.z);
+            hi[0] = std::max(hi[0], v.x); hi[1] = std::max(hi[1], v.y); hi[2] = std::max(hi[2], v.z);
+        }
+        const double ext[3] = {(double)hi[0] - lo[0], (double)hi[1] - lo[1], (double)hi[2] - lo[2]};
+        const int cells[3] = {I, J, K};
+        int g0[3], g1[3];
+        for (int a = 0; a < 3; a++) {   // meshobject.cpp:528-536
+            g0[a] = std::max(floor_index(lo[a], dx) - band, 0);
+            g1[a] = std::min(floor_index(lo[a] + (float)ext[a], dx) + band + 1, cells[a] - 1);
+        }
+        const int gw = g1[0] - g0[0], gh = g1[1] - g0[1], gd = g1[2] - g0[2];
+        if (gw <= 0 || gh <= 0 || gd <= 0) continue;   // outside the domain
+        const V origin{gpos(g0[0], dx), gpos(g0[1], dx), gpos(g0[2], dx)};
+        std::vector<V> rel(nv);
+        for (int v = 0; v < nv; v++) rel[v] = vsub(wv[v], origin);
+        std::vector<float> iphi;
+        std::vector<int> itri;
+        mesh_level_set(rel, ob.tris, gw + 1, gh + 1, gd + 1, dx, band, iphi, itri);
+        // island -> temporary level set -> solid level set
+        std::vector<float> tphi(nodal.size(), upper);
+        std::vector<int> tobj(nodal.size(), -1);
+        for (int k = 0; k <= gd; k++)
+            for (int j = 0; j <= gh; j++)
+                for (int i = 0; i <= gw; i++) {
+                    const int a = i + g0[0], b = j + g0[1], c = k + g0[2];
+                    if (a > I || b > J || c > K) continue;
+                    const size_t s = (size_t)i + (size_t)(gw + 1) * ((size_t)j + (size_t)(gh + 1) * k);
+                    const size_t d = nidx(a, b, c);
+                    if (iphi[s] < tphi[d]) {
+                        if (std::fabs(iphi[s]) < std::fabs(tphi[d]) && itri[s] != -1) tobj[d] = (int)q + 1;
+                        tphi[d] = iphi[s];
+                    }
+                }
+        for (size_t d = 0; d < nodal.size(); d++) {
+            if (tphi[d] < nodal[d]) {
+                if (std::fabs(tphi[d]) < std::fabs(nodal[d]) && tobj[d] != -1) nodeObject[d] = tobj[d];
+                nodal[d] = tphi[d];
+            }
+        }
+    }
+    nodeFriction.assign(nodal.size(), 0.0f);
+    anyFriction = false;
+    for (size_t d = 0; d < nodal.size(); d++) {
+        const int o = nodeObject[d];
+        nodeFriction[d] = o > 0 ? obstacles[o - 1].friction : 0.0f;   // the walls have no friction
+        anyFriction = anyFriction || nodeFriction[d] != 0.0f;
+    }
 
     wu.assign((size_t)(I + 1) * J * K, 0.0f);
     wv.assign((size_t)I * (J + 1) * K, 0.0f);
@@ -172,6 +379,37 @@ void DomainBox::compute(int I_, int J_, int K_, double dx_, double cfl) {
             for (int i = 0; i < I; i++)
                 ww[(size_t)i + (size_t)I * ((size_t)j + (size_t)J * k)] =
                     wclamp(frac4(S(i, j, k), S(i, j + 1, k), S(i + 1, j, k), S(i + 1, j + 1, k)));
+
+    // face friction: the mean of its four nodes' (fluidsimulation.cpp:3785-3846)
+    auto F = [&](int i, int j, int k) { return nodeFriction[nidx(i, j, k)]; };
+    auto mean4 = [](float a, float b, float c, float d) {
+        float f = 0.0f;
+        f += a;
+        f += b;
+        f += c;
+        f += d;
+        return 0.25f * f;
+    };
+    fu.assign(wu.size(), 0.0f);
+    fv.assign(wv.size(), 0.0f);
+    fw.assign(ww.size(), 0.0f);
+    if (anyFriction) {
+        for (int k = 0; k < K; k++)
+            for (int j = 0; j < J; j++)
+                for (int i = 0; i <= I; i++)
+                    fu[(size_t)i + (size_t)(I + 1) * ((size_t)j + (size_t)J * k)] =
+                        mean4(F(i, j, k), F(i, j + 1, k), F(i, j, k + 1), F(i, j + 1, k + 1));
+        for (int k = 0; k < K; k++)
+            for (int j = 0; j <= J; j++)
+                for (int i = 0; i < I; i++)
+                    fv[(size_t)i + (size_t)I * ((size_t)j + (size_t)(J + 1) * k)] =
+                        mean4(F(i, j, k), F(i + 1, j, k), F(i, j, k + 1), F(i + 1, j, k + 1));
+        for (int k = 0; k <= K; k++)
+            for (int j = 0; j < J; j++)
+                for (int i = 0; i < I; i++)
+                    fw[(size_t)i + (size_t)I * ((size_t)j + (size_t)J * k)] =
+                        mean4(F(i, j, k), F(i + 1, j, k), F(i, j + 1, k), F(i + 1, j + 1, k));
+    }
 
     solidCentre.assign((size_t)I * J * K, 0);
     for (int k = 0; k < K; k++)

@@ -1,9 +1,20 @@
-// Static solid set-up for the domain walls (host, once per simulation).
+// Static solid set-up: the domain walls and static mesh obstacles (host,
+// once per solid configuration).
 #pragma once
 #include <cstdint>
 #include <vector>
 
 namespace flip {
+
+// A static triangle-mesh obstacle (addMeshObstacle, fluidsimulation.cpp:
+// 1994-2008): world-space vertices, triangles as vertex index triples, and
+// the friction its faces apply in the constrain step (MeshObject::setFriction,
+// meshobject.cpp:301-309).
+struct MeshObstacle {
+    std::vector<float> verts;   // x, y, z per vertex
+    std::vector<int> tris;      // three vertex indices per triangle
+    float friction = 0.0f;
+};
 
 struct DomainBox {
     int I = 0, J = 0, K = 0;
@@ -17,8 +28,15 @@ struct DomainBox {
     std::vector<uint8_t> near;             // coarse near-solid grid
     int nsi = 0, nsj = 0, nsk = 0;
     double nearCell = 0;
+    // per node: the solid object closest to it (-1 none, 0 the domain walls,
+    // q + 1 obstacle q) and that object's friction; per face the mean friction
+    // of its four nodes (fluidsimulation.cpp:3785-3846)
+    std::vector<int> nodeObject;
+    std::vector<float> nodeFriction;
+    std::vector<float> fu, fv, fw;
+    bool anyFriction = false;
 
-    void compute(int I, int J, int K, double dx, double cfl);
+    void compute(int I, int J, int K, double dx, double cfl, const std::vector<MeshObstacle> &obstacles = {});
 };
 
 }  // namespace flip

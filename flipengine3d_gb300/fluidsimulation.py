@@ -92,6 +92,8 @@ SIGNATURES = {
     "flip_get_mac_velocity": [_P, _P, _P, _P],
     "flip_get_face_weights": [_P, _P, _P, _P],
     "flip_compute_domain_solid": [_I, _I, _I, _D, _I, _P, _P, _P, _P, _P, _P],
+    "flip_add_mesh_obstacle": [_P, _I, _P, _I, _P, C.c_float],
+    "flip_compute_solid": [_I, _I, _I, _D, _I, _I] + [_P] * 5 + [_P] * 9,
     "flip_set_stage_timing": [_P, _I],
     "flip_get_stage_times": [_P, _P, C.POINTER(C.c_longlong)],
     "flip_get_launch_count": [_P, C.POINTER(C.c_longlong)],
@@ -170,6 +172,39 @@ def compute_domain_solid(isize, jsize, ksize, dx, cfl=5):
     _check(lib, lib.flip_compute_domain_solid(I, J, K, dx, cfl, _ptr(nodal), _ptr(wu), _ptr(wv), _ptr(ww),
                                               _ptr(dims), _ptr(near)))
     return nodal, (wu, wv, ww), near
+
+
+def _obstacle_arrays(obstacles):
+    """(n, nverts, verts, ntris, tris, friction) arrays of [(verts (m, 3),
+    tris (t, 3), friction), ...]."""
+    nv = np.array([len(o[0]) for o in obstacles], np.int32)
+    nt = np.array([len(o[1]) for o in obstacles], np.int32)
+    verts = np.ascontiguousarray(np.concatenate([np.asarray(o[0], np.float32).reshape(-1, 3) for o in obstacles])
+                                 if obstacles else np.zeros((0, 3), np.float32), np.float32)
+    tris = np.ascontiguousarray(np.concatenate([np.asarray(o[1], np.int32).reshape(-1, 3) for o in obstacles])
+                                if obstacles else np.zeros((0, 3), np.int32), np.int32)
+    fr = np.array([float(o[2]) if len(o) > 2 else 0.0 for o in obstacles], np.float32)
+    return len(obstacles), nv, verts, nt, tris, fr
+
+
+def compute_solid(isize, jsize, ksize, dx, cfl=5, obstacles=()):
+    """Static solid set-up with mesh obstacles [(verts, tris, friction), ...]
+    (no device needed): nodal solid SDF, face weights (wu, wv, ww), the
+    near-solid grid and the face friction (fu, fv, fw), arrays shaped (k, j, i)."""
+    lib = load_library()
+    I, J, K = isize, jsize, ksize
+    n, nv, verts, nt, tris, fr = _obstacle_arrays(list(obstacles))
+    nodal = np.zeros((K + 1, J + 1, I + 1), np.float32)
+    wu, fu = np.zeros((K, J, I + 1), np.float32), np.zeros((K, J, I + 1), np.float32)
+    wv, fv = np.zeros((K, J + 1, I), np.float32), np.zeros((K, J + 1, I), np.float32)
+    ww, fw = np.zeros((K + 1, J, I), np.float32), np.zeros((K + 1, J, I), np.float32)
+    dims = np.zeros(3, np.int32)
+    args = (I, J, K, dx, cfl, n, _ptr(nv), _ptr(verts), _ptr(nt), _ptr(tris), _ptr(fr))
+    _check(lib, lib.flip_compute_solid(*args, None, None, None, None, _ptr(dims), None, None, None, None))
+    near = np.zeros((dims[2], dims[1], dims[0]), np.uint8)
+    _check(lib, lib.flip_compute_solid(*args, _ptr(nodal), _ptr(wu), _ptr(wv), _ptr(ww), _ptr(dims), _ptr(near),
+                                       _ptr(fu), _ptr(fv), _ptr(fw)))
+    return nodal, (wu, wv, ww), near, (fu, fv, fw)
 
 
 def order_particles_by_id_noalloc(d_px: int, d_py: int, d_pz: int, d_ids: int, n: int, id_space: int,
@@ -342,6 +377,15 @@ class FluidSimulation:
 
     def setMaxPressureSolveIterations(self, n: int):
         self._c(self._lib.flip_set_max_pressure_iterations(self._h, int(n)))
+
+    def addMeshObstacle(self, vertices, triangles, friction: float = 0.0):
+        """addMeshObstacle (fluidsimulation.cpp:1994-2008) for a static mesh
+        obstacle: vertices (m, 3), triangles (t, 3) vertex indices, surface
+        friction in [0, 1]; copied on the call."""
+        v = np.ascontiguousarray(vertices, np.float32).reshape(-1, 3)
+        t = np.ascontiguousarray(triangles, np.int32).reshape(-1, 3)
+        self._c(self._lib.flip_add_mesh_obstacle(self._h, v.shape[0], _ptr(v), t.shape[0], _ptr(t),
+                                                 float(friction)))
 
     def loadMarkerParticleData(self, positions, velocities):
         pos = np.ascontiguousarray(positions, dtype=np.float32).reshape(-1, 3)
@@ -548,6 +592,8 @@ class FluidSimulation:
         sim.addBodyForce(*scene.gravity)
         sim.setCFLConditionNumber(scene.cfl)
         sim.setPressureSolveTolerance(scene.tolerance if tolerance is None else tolerance)
+        for ob in getattr(scene, "obstacles", ()):
+            sim.addMeshObstacle(*ob)
         sim.loadMarkerParticleData(scene.positions, scene.velocities)
         sim.initialize()
         return sim

@@ -31,6 +31,8 @@ class Scene:
     steps: int = 10
     name: str = ""
     meta: dict = field(default_factory=dict)
+    # static mesh obstacles: (vertices (m, 3) float32, triangles (t, 3) int32, friction)
+    obstacles: list = field(default_factory=list)
 
     @property
     def num_particles(self) -> int:
@@ -97,6 +99,68 @@ def dam_break(n: int = 64, *, seed: int = 0, fill=(0.4, 0.6, 1.0), sphere: bool 
         vel = np.concatenate([vel, sv])
     return Scene(n, jsize, ksize, dx, pos, vel, steps=steps, pic_ratio=pic_ratio,
                  tolerance=tolerance, name=f"dam{'+sphere' if sphere else ''}_{n}x{jsize}x{ksize}")
+
+
+def box_mesh(lo, hi):
+    """A closed box mesh from corner lo to corner hi: 8 vertices, 12
+    triangles (two per face, outward winding)."""
+    x0, y0, z0 = lo
+    x1, y1, z1 = hi
+    v = np.array([[x0, y0, z0], [x1, y0, z0], [x1, y1, z0], [x0, y1, z0],
+                  [x0, y0, z1], [x1, y0, z1], [x1, y1, z1], [x0, y1, z1]], np.float32)
+    t = np.array([[0, 2, 1], [0, 3, 2], [4, 5, 6], [4, 6, 7], [0, 1, 5], [0, 5, 4],
+                  [3, 7, 6], [3, 6, 2], [0, 4, 7], [0, 7, 3], [1, 2, 6], [1, 6, 5]], np.int32)
+    return v, t
+
+
+def icosphere_mesh(centre, radius, subdivisions=2):
+    """A closed sphere mesh: an icosahedron subdivided `subdivisions` times,
+    vertices pushed to the sphere (20 * 4^subdivisions triangles)."""
+    g = (1.0 + 5.0 ** 0.5) / 2.0
+    verts = [(-1, g, 0), (1, g, 0), (-1, -g, 0), (1, -g, 0), (0, -1, g), (0, 1, g), (0, -1, -g), (0, 1, -g),
+             (g, 0, -1), (g, 0, 1), (-g, 0, -1), (-g, 0, 1)]
+    verts = [np.array(v, np.float64) / np.linalg.norm(v) for v in verts]
+    tris = [(0, 11, 5), (0, 5, 1), (0, 1, 7), (0, 7, 10), (0, 10, 11), (1, 5, 9), (5, 11, 4), (11, 10, 2),
+            (10, 7, 6), (7, 1, 8), (3, 9, 4), (3, 4, 2), (3, 2, 6), (3, 6, 8), (3, 8, 9), (4, 9, 5), (2, 4, 11),
+            (6, 2, 10), (8, 6, 7), (9, 8, 1)]
+    for _ in range(subdivisions):
+        mid = {}
+
+        def midpoint(a, b):
+            key = (min(a, b), max(a, b))
+            if key not in mid:
+                m = verts[a] + verts[b]
+                verts.append(m / np.linalg.norm(m))
+                mid[key] = len(verts) - 1
+            return mid[key]
+        new = []
+        for a, b, c in tris:
+            ab, bc, ca = midpoint(a, b), midpoint(b, c), midpoint(c, a)
+            new += [(a, ab, ca), (b, bc, ab), (c, ca, bc), (ab, bc, ca)]
+        tris = new
+    v = (np.array(verts) * radius + np.asarray(centre, np.float64)).astype(np.float32)
+    return v, np.array(tris, np.int32)
+
+
+def dam_with_obstacles(n: int = 24, *, seed: int = 0, which: str = "box", **kw) -> Scene:
+    """A dam break (as dam_break) with a static mesh obstacle inside the fluid
+    block: `box` (a box of friction 0.3 on its faces) or `sphere` (an
+    icosphere, no friction), placed off the grid's node planes."""
+    sc = dam_break(n, seed=seed, **kw)
+    if which == "box":
+        v, t = box_mesh((0.253, 0.0817, 0.3113), (0.371, 0.3929, 0.5471))
+        sc.obstacles = [(v, t, 0.3)]
+    elif which == "sphere":
+        v, t = icosphere_mesh((0.2231, 0.3327, 0.5119), 0.1307, subdivisions=2)
+        sc.obstacles = [(v, t, 0.0)]
+    elif which == "both":
+        v, t = box_mesh((0.253, 0.0817, 0.3113), (0.371, 0.3929, 0.5471))
+        v2, t2 = icosphere_mesh((0.2131, 0.3327, 0.7519), 0.1107, subdivisions=2)
+        sc.obstacles = [(v, t, 0.3), (v2, t2, 0.6)]
+    else:
+        raise ValueError(which)
+    sc.name += f"+{which}"
+    return sc
 
 
 def plain_64(seed: int = 0) -> Scene:

@@ -63,6 +63,27 @@ struct TriangleMesh {
     std::vector<int> triangles;
 };
 
+// A static obstacle mesh: the part of the reference's MeshObject
+// (meshobject.h, meshobject.cpp:32-59, 301-309) that addMeshObstacle uses.
+// The caller keeps it alive while the simulation uses it, as with the
+// reference (fluidsimulation.cpp:1994-2008).
+class MeshObject {
+public:
+    MeshObject() = default;
+    MeshObject(int, int, int, double) {}
+    void updateMeshStatic(const TriangleMesh &m) { mesh_ = m; }
+    void setFriction(float f) {
+        if (f < 0.0f || f > 1.0f) throw std::domain_error("Error: friction must be in range [0.0, 1.0].");
+        friction_ = f;
+    }
+    float getFriction() const { return friction_; }
+    const TriangleMesh &getMesh() const { return mesh_; }
+
+private:
+    TriangleMesh mesh_;
+    float friction_ = 0.0f;
+};
+
 class FluidSimulation {
 public:
     FluidSimulation(int isize, int jsize, int ksize, double dx) { check(flip_create(isize, jsize, ksize, dx, &ctx_)); }
@@ -99,6 +120,16 @@ public:
     void setMaxThreadCount(int) {}
     void disableSurfaceReconstruction() {}
     TriangleMesh &getIsomesh() { return mesh_; }
+
+    // addMeshObstacle (fluidsimulation.cpp:1994-2008): static obstacles only.
+    void addMeshObstacle(MeshObject *obstacle) {
+        for (MeshObject *o : obstacles_)
+            if (o == obstacle) throw std::runtime_error("Error: mesh obstacle has already been added.\n");
+        const TriangleMesh &m = obstacle->getMesh();
+        check(flip_add_mesh_obstacle(ctx_, (int)(m.vertices.size() / 3), m.vertices.data(),
+                                     (int)(m.triangles.size() / 3), m.triangles.data(), obstacle->getFriction()));
+        obstacles_.push_back(obstacle);
+    }
 
     void loadMarkerParticleData(FluidSimulationMarkerParticleData data) {
         check(flip_load_marker_particle_data(ctx_, data.size, reinterpret_cast<const float *>(data.positions),
@@ -142,6 +173,7 @@ public:
 private:
     flip_ctx *ctx_ = nullptr;
     TriangleMesh mesh_;
+    std::vector<MeshObject *> obstacles_;
 };
 
 }  // namespace flip3d

@@ -162,6 +162,30 @@ int flip_get_solid_sdf(flip_ctx *ctx, float *nodal_phi);   /* (I+1)*(J+1)*(K+1) 
 int flip_get_mac_velocity(flip_ctx *ctx, float *u, float *v, float *w);
 int flip_get_face_weights(flip_ctx *ctx, float *wu, float *wv, float *ww);
 
+/* addMeshObstacle(MeshObject *) (fluidsimulation.cpp:1994-2008) for a static
+ * obstacle: a triangle mesh of nverts vertices (xyz floats, world space) and
+ * ntris triangles (three vertex indices each), and the friction of its
+ * surface (MeshObject::setFriction, meshobject.cpp:301-309; in [0, 1]),
+ * copied on the call.  The solid level set, face weights and near-solid grid
+ * are rebuilt before the next step: the obstacle's level set over the
+ * sub-grid its bounding box spans, unioned with the domain walls'
+ * (fluidsimulation.cpp:2927-2966).  Animated and inverted obstacles are not
+ * supported.  FLIP_E_DOMAIN for a bad index, count, vertex or friction. */
+int flip_add_mesh_obstacle(flip_ctx *ctx, int nverts, const float *verts, int ntris, const int *tris,
+                           float friction);
+
+/* The solid set-up of the first step with static mesh obstacles, without a
+ * device: nodal solid level set, fluid face weights, near-solid grid (as in
+ * flip_compute_domain_solid) and the face friction of the constrain step
+ * (fu/fv/fw, face grids; fluidsimulation.cpp:3785-3846).  Obstacle q has
+ * nverts[q] vertices, consecutive in verts, and ntris[q] triangles with
+ * indices local to it, consecutive in tris; friction may be NULL (none).
+ * Any output may be NULL. */
+int flip_compute_solid(int isize, int jsize, int ksize, double dx, int cfl, int nobstacles, const int *nverts,
+                       const float *verts, const int *ntris, const int *tris, const float *friction,
+                       float *nodal_phi, float *wu, float *wv, float *ww, int *near_dims, uint8_t *near,
+                       float *fu, float *fv, float *fw);
+
 /* Static wall set-up of initialize()/the first step, without a device: the
  * domain-box solid level set on the (I+1)*(J+1)*(K+1) nodes, the fluid face
  * weights and the coarse near-solid grid (dims written to near_dims[3];

@@ -14,6 +14,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
+#include <cstdlib>
 #include <cstring>
 #include <fstream>
 #include <iostream>
@@ -34,11 +35,13 @@
 #include "pressuresolver.h"
 #include "pcgsolver/pcgsolver.h"
 #include "pcgsolver/sparsematrix.h"
+#include "meshobject.h"
 
 namespace {
 
 struct RefSim {
     FluidSimulation *sim = nullptr;
+    std::vector<MeshObject *> obstacles;   // owned here, registered with the simulation
     std::string status;
     unsigned int particleFragmentBytes = 0;   // 0: the reference's default fragments
 };
@@ -89,6 +92,7 @@ void *ref_create(int isize, int jsize, int ksize, double dx) {
 void ref_destroy(void *h) {
     RefSim *r = (RefSim *)h;
     delete r->sim;
+    for (MeshObject *o : r->obstacles) delete o;
     delete r;
 }
 
@@ -138,8 +142,25 @@ void ref_load_particles(void *h, int n, const float *pos, const float *vel) {
     r->sim->_isMarkerParticleLoadPending = true;
 }
 
-void ref_initialize(void *h) { ((RefSim *)h)->sim->initialize(); }
-void ref_update(void *h, double dt) { ((RefSim *)h)->sim->update(dt); }
+// The reference builds its static solid level sets (the domain box and static
+// obstacles) on initialisation, with ray origins jittered by the C library's
+// rand() (meshutils.cpp:95-122).  Which rays graze an edge, and so the signs
+// of some nodes, depends on that jitter: the generator is reseeded to its
+// start-of-process state (seed 1) first, so that a simulation set up after
+// other rand() users in the same process builds the same level set as one
+// set up in a fresh process.
+static void seed_like_a_fresh_process(FluidSimulation *s) {
+    if (!s->isInitialized()) std::srand(1);
+}
+
+void ref_initialize(void *h) {
+    seed_like_a_fresh_process(((RefSim *)h)->sim);
+    ((RefSim *)h)->sim->initialize();
+}
+void ref_update(void *h, double dt) {
+    seed_like_a_fresh_process(((RefSim *)h)->sim);
+    ((RefSim *)h)->sim->update(dt);
+}
 
 int ref_num_particles(void *h) { return (int)((RefSim *)h)->sim->getNumMarkerParticles(); }
 
@@ -430,6 +451,44 @@ int ref_mic0_precondition_f32(int I, int J, int K, const uint8_t *fluid, const f
     solveLowerTransposeInPlace(F, res);
     for (int c = 0; c < n; c++) z[cellOf[c]] = res[c];
     return n;
+}
+
+
+// addMeshObstacle with a static MeshObject built from plain arrays
+// (fluidsimulation.cpp:1994-2008, meshobject.cpp:50-59, 301-309).
+void ref_add_mesh_obstacle(void *h, int nverts, const float *verts, int ntris, const int *tris, float friction) {
+    RefSim *r = (RefSim *)h;
+    TriangleMesh m;
+    for (int v = 0; v < nverts; v++) m.vertices.push_back(vmath::vec3(verts[3 * v], verts[3 * v + 1], verts[3 * v + 2]));
+    for (int t = 0; t < ntris; t++) {
+        Triangle tri;
+        tri.tri[0] = tris[3 * t];
+        tri.tri[1] = tris[3 * t + 1];
+        tri.tri[2] = tris[3 * t + 2];
+        m.triangles.push_back(tri);
+    }
+    int I, J, K;
+    r->sim->getGridDimensions(&I, &J, &K);
+    MeshObject *o = new MeshObject(I, J, K, r->sim->getCellSize());
+    o->updateMeshStatic(m);
+    o->setFriction(friction);
+    r->obstacles.push_back(o);
+    r->sim->addMeshObstacle(o);
+}
+
+// Per node of the solid level set, the friction of the closest mesh object
+// (0 where none): what the constrain step averages per face
+// (fluidsimulation.cpp:3785-3846).
+void ref_get_node_friction(void *h, float *out) {
+    FluidSimulation *s = ((RefSim *)h)->sim;
+    int I, J, K;
+    s->getGridDimensions(&I, &J, &K);
+    for (int k = 0; k <= K; k++)
+        for (int j = 0; j <= J; j++)
+            for (int i = 0; i <= I; i++) {
+                MeshObject *m = s->_solidSDF.getClosestMeshObject(i, j, k);
+                out[i + (size_t)(I + 1) * (j + (size_t)(J + 1) * k)] = m == nullptr ? 0.0f : m->getFriction();
+            }
 }
 
 }  // extern "C"

@@ -68,6 +68,10 @@ def lib(prefix: str = "ref"):
         if prefix == "ref":
             L.ref_set_particle_fragment_bytes.argtypes = [C.c_void_p, C.c_uint]
             L.ref_set_particle_fragment_bytes.restype = None
+            L.ref_add_mesh_obstacle.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_float]
+            L.ref_add_mesh_obstacle.restype = None
+            L.ref_get_node_friction.argtypes = [C.c_void_p, C.c_void_p]
+            L.ref_get_node_friction.restype = None
         L.ref_num_particles.argtypes = [C.c_void_p]
         L.ref_num_particles.restype = C.c_int
         L.ref_frame_substeps.argtypes = [C.c_void_p]
@@ -217,6 +221,14 @@ class RefSimulation:
             pass
 
     def setup(self, scene, tolerance=None):
+        obstacles = getattr(scene, "obstacles", [])
+        if obstacles and self.PREFIX != "ref":
+            raise NotImplementedError("the oracle port restates the domain walls only; obstacle scenes are "
+                                      "pinned by fixtures from the reference")
+        for v, t, fr in obstacles:
+            v = np.ascontiguousarray(v, np.float32)
+            t = np.ascontiguousarray(t, np.int32)
+            self.L.ref_add_mesh_obstacle(self.h, len(v), _p(v), len(t), _p(t), float(fr))
         self.L.ref_set_pic_ratio(self.h, scene.pic_ratio)
         self.L.ref_add_body_force(self.h, *scene.gravity)
         self.L.ref_set_cfl(self.h, scene.cfl)
@@ -270,6 +282,12 @@ class RefSimulation:
 
     def pressure_status(self):
         return self.L.ref_pressure_status(self.h).decode()
+
+    def node_friction(self):
+        I, J, K = self.dims
+        a = np.zeros((K + 1, J + 1, I + 1), np.float32)
+        self.L.ref_get_node_friction(self.h, _p(a))
+        return a
 
     def update_staged(self, dt):
         """One single-substep frame with the state between stages returned."""

@@ -59,6 +59,13 @@ def golden_cases():
     return sorted(p.stem for p in GOLDEN.glob("*.npz"))
 
 
+def golden_scene(meta):
+    """The scene a fixture was made from (scenes.dam_break, or the builder
+    the fixture names, with its recorded arguments)."""
+    from flipengine3d_gb300 import scenes
+    return getattr(scenes, meta.get("builder", "dam_break"))(**meta["scene"])
+
+
 def load_golden(name):
     z = np.load(GOLDEN / f"{name}.npz")
     meta = json.loads(str(z["meta"]))

@@ -6,7 +6,7 @@ scenes and stores the state after each stage of the first frame plus the
 particles after later frames.  Inputs are not stored: the scenes are
 regenerated from flipengine3d_gb300.scenes with the recorded arguments.
 
-    python tests/golden/make_golden.py        # needs the reference sources
+    python tests/golden/make_golden.py [name ...]   # needs the reference sources
 """
 from __future__ import annotations
 
@@ -19,7 +19,7 @@ import numpy as np
 ROOT = Path(__file__).resolve().parents[2]
 sys.path.insert(0, str(ROOT))
 
-from flipengine3d_gb300.scenes import dam_break  # noqa: E402
+from flipengine3d_gb300 import scenes  # noqa: E402
 from oracle.refsim import RefSimulation  # noqa: E402
 
 OUT = Path(__file__).resolve().parent
@@ -30,15 +30,26 @@ CASES = {
     "sphere13x17x11": (dict(n=13, jsize=17, ksize=11, dx=1.0 / 13, seed=5, sphere=True, fill=(0.5, 0.5, 0.6)), 3, 1, 1e-9),
     "dam12_loose": (dict(n=12, seed=2, fill=(0.6, 0.9, 1.0)), 2, 1, 1e-6),
 }
+# scenes with static mesh obstacles (scenes.dam_with_obstacles): the solid
+# level set, face weights and per-node closest-object friction are stored too
+OBSTACLE_CASES = {
+    "dam24_box": (dict(n=24, seed=3, which="box"), 3, 1, 1e-9),
+    "dam20_sphere": (dict(n=20, seed=5, which="sphere"), 3, 1, 1e-9),
+    "dam20_both": (dict(n=20, seed=7, which="both"), 2, 1, 1e-9),
+}
 STAGE_KEYS = ("phi", "vu_p2g", "vv_p2g", "vw_p2g", "u_p2g", "v_p2g", "w_p2g", "pressure", "u_final", "v_final",
               "w_final", "vel_g2p", "pos_adv")
 
 
-def make(name, kwargs, frames, threads, tol):
-    sc = dam_break(**kwargs)
+def make(name, kwargs, frames, threads, tol, builder="dam_break"):
+    sc = getattr(scenes, builder)(**kwargs)
     ref = RefSimulation(sc.isize, sc.jsize, sc.ksize, sc.dx, threads=threads).setup(sc, tolerance=tol)
     st = ref.update_staged(sc.frame_dt)
     data = {k: st[k] for k in STAGE_KEYS}
+    if builder != "dam_break":   # the solid set-up of the first step
+        data["solid_phi"] = ref.solid_phi()
+        data["wu"], data["wv"], data["ww"] = ref.weights()
+        data["node_friction"] = ref.node_friction()
     data["pcg_iters"] = st["pcg_iters"]
     data["pcg_error"] = st["pcg_error"]
     data["positions_1"], data["velocities_1"] = st["positions"], st["velocities"]
@@ -46,7 +57,7 @@ def make(name, kwargs, frames, threads, tol):
         ref.update(sc.frame_dt)
     pos, vel = ref.particles()
     data[f"positions_{frames}"], data[f"velocities_{frames}"] = pos, vel
-    meta = dict(scene=kwargs, frames=frames, threads=threads, tolerance=tol, dt=sc.frame_dt,
+    meta = dict(scene=kwargs, builder=builder, frames=frames, threads=threads, tolerance=tol, dt=sc.frame_dt,
                 gravity=list(sc.gravity), pic_ratio=sc.pic_ratio, cfl=sc.cfl,
                 seeded=int(sc.num_particles), source="jklae/FLIPEngine3D src/engine via oracle/build_ref.sh")
     np.savez_compressed(OUT / f"{name}.npz", meta=np.array(json.dumps(meta)), **data)
@@ -55,5 +66,10 @@ def make(name, kwargs, frames, threads, tol):
 
 
 if __name__ == "__main__":
+    only = set(sys.argv[1:])   # names to (re)generate; all by default
     for name, (kw, frames, thr, tol) in CASES.items():
-        make(name, kw, frames, thr, tol)
+        if not only or name in only:
+            make(name, kw, frames, thr, tol)
+    for name, (kw, frames, thr, tol) in OBSTACLE_CASES.items():
+        if not only or name in only:
+            make(name, kw, frames, thr, tol, builder="dam_with_obstacles")

@@ -64,10 +64,27 @@ int main(int argc, char **argv) {
     std::vector<float> pos(3 * (size_t)n), vel(3 * (size_t)n);
     if (std::fread(pos.data(), 4, pos.size(), in) != pos.size() || std::fread(vel.data(), 4, vel.size(), in) != vel.size())
         return 2;
+    int nobs = 0;
+    if (std::fread(&nobs, 4, 1, in) != 1) return 2;
+    std::vector<flip3d::MeshObject> obstacles(nobs);
+    for (int q = 0; q < nobs; q++) {   // vertex count, triangle count, friction, vertices, triangles
+        int nv, nt;
+        float fr;
+        if (std::fread(&nv, 4, 1, in) != 1 || std::fread(&nt, 4, 1, in) != 1 || std::fread(&fr, 4, 1, in) != 1) return 2;
+        flip3d::TriangleMesh m;
+        m.vertices.resize(3 * (size_t)nv);
+        m.triangles.resize(3 * (size_t)nt);
+        if (std::fread(m.vertices.data(), 4, m.vertices.size(), in) != m.vertices.size() ||
+            std::fread(m.triangles.data(), 4, m.triangles.size(), in) != m.triangles.size())
+            return 2;
+        obstacles[q].updateMeshStatic(m);
+        obstacles[q].setFriction(fr);
+    }
     std::fclose(in);
     flip3d::FluidSimulation fluidsim(I, J, K, dx);
     fluidsim.setPICFLIPRatio(pic);
     fluidsim.addBodyForce(0.0, -9.81, 0.0);
+    for (auto &o : obstacles) fluidsim.addMeshObstacle(&o);
     flip3d::FluidSimulationMarkerParticleData data;
     data.size = n;
     data.positions = reinterpret_cast<char *>(pos.data());
@@ -88,26 +105,31 @@ int main(int argc, char **argv) {
 """
 
 
-@pytest.mark.gpu
-def test_cpp_drop_in_steps_a_scene_like_the_oracle(gpu, tmp_path):
-    """The C++ face drives the GPU the way FluidManager drives the reference:
-    its three frames match the oracle's (reference defaults: tolerance 1e-9)."""
+def _write_scene(path, sc):
     import numpy as np
-
-    from conftest import rel_err
-    from flipengine3d_gb300.scenes import dam_break
-    from oracle import refsim
-    gxx = shutil.which("g++")
-    if not gxx:
-        pytest.skip("g++ not available")
-    sc = dam_break(20, seed=31, sphere=True)
-    inp = tmp_path / "scene.bin"
-    with open(inp, "wb") as f:
+    with open(path, "wb") as f:
         np.array([sc.isize, sc.jsize, sc.ksize], np.int32).tofile(f)
         np.array([sc.dx, sc.pic_ratio], np.float64).tofile(f)
         np.array([len(sc.positions)], np.int32).tofile(f)
         np.ascontiguousarray(sc.positions, np.float32).tofile(f)
         np.ascontiguousarray(sc.velocities, np.float32).tofile(f)
+        np.array([len(sc.obstacles)], np.int32).tofile(f)
+        for v, t, fr in sc.obstacles:
+            np.array([len(v), len(t)], np.int32).tofile(f)
+            np.array([fr], np.float32).tofile(f)
+            np.ascontiguousarray(v, np.float32).tofile(f)
+            np.ascontiguousarray(t, np.int32).tofile(f)
+
+
+def _run_driver(tmp_path, sc):
+    """Compile the driver against the header, run it on the scene; the
+    positions after three frames."""
+    import numpy as np
+    gxx = shutil.which("g++")
+    if not gxx:
+        pytest.skip("g++ not available")
+    inp = tmp_path / "scene.bin"
+    _write_scene(inp, sc)
     src = tmp_path / "driver.cpp"
     src.write_text(DRIVER)
     exe = tmp_path / "driver"
@@ -122,9 +144,34 @@ def test_cpp_drop_in_steps_a_scene_like_the_oracle(gpu, tmp_path):
     raw = np.fromfile(out, dtype=np.uint32, count=1)
     pos = np.fromfile(out, dtype=np.float32, offset=4).reshape(-1, 3)
     assert int(raw[0]) == m == len(pos)
+    return pos
+
+
+@pytest.mark.gpu
+def test_cpp_drop_in_steps_a_scene_like_the_oracle(gpu, tmp_path):
+    """The C++ face drives the GPU the way FluidManager drives the reference:
+    its three frames match the oracle's (reference defaults: tolerance 1e-9)."""
+    from conftest import rel_err
+    from flipengine3d_gb300.scenes import dam_break
+    from oracle import refsim
+    sc = dam_break(20, seed=31, sphere=True)
+    pos = _run_driver(tmp_path, sc)
     orc = refsim.OracleSimulation(sc.isize, sc.jsize, sc.ksize, sc.dx).setup(sc, tolerance=1e-9)
     for _ in range(3):
         orc.update(sc.frame_dt)
     rpos, _ = orc.particles()
     assert pos.shape == rpos.shape
     assert rel_err(pos, rpos) <= 1e-4
+
+
+@pytest.mark.gpu
+def test_cpp_drop_in_with_a_mesh_obstacle_matches_the_reference(gpu, tmp_path):
+    """MeshObject + addMeshObstacle through the C++ face: a box obstacle with
+    friction in a dam break; after three frames the positions are the
+    reference engine's (its fixture dam24_box) within 1e-4."""
+    from conftest import golden_scene, load_golden, rel_err
+    meta, g = load_golden("dam24_box")
+    assert meta["tolerance"] == 1e-9 and meta["frames"] == 3
+    pos = _run_driver(tmp_path, golden_scene(meta))
+    assert pos.shape == g["positions_3"].shape
+    assert rel_err(pos, g["positions_3"]) <= 1e-4

@@ -10,7 +10,7 @@ from __future__ import annotations
 import numpy as np
 import pytest
 
-from conftest import golden_cases, load_golden, rel_err
+from conftest import golden_cases, golden_scene, load_golden, rel_err
 from flipengine3d_gb300 import FluidSimulation
 from flipengine3d_gb300.scenes import dam_break
 from oracle import refsim
@@ -36,9 +36,11 @@ def check_first_frame(st, ref, label):
 @pytest.mark.parametrize("case", golden_cases())
 def test_first_frame_matches_reference_golden(gpu, case):
     meta, g = load_golden(case)
-    sc = dam_break(**meta["scene"])
+    sc = golden_scene(meta)   # with static mesh obstacles for the obstacle fixtures
     with FluidSimulation.from_scene(sc, tolerance=meta["tolerance"]) as sim:
         st = sim.update_staged(meta["dt"])
+        if "solid_phi" in g:   # the solid set-up the obstacles make, bit for bit
+            assert np.array_equal(sim.solid_sdf(), g["solid_phi"]), f"{case}: solid level set"
         check_first_frame(st, g, case)
         assert int(st["pcg_iters"][0]) == int(g["pcg_iters"][0]), "PCG iterations differ from the reference's"
         assert st["positions"].shape == g["positions_1"].shape

@@ -6,7 +6,7 @@ from __future__ import annotations
 import numpy as np
 import pytest
 
-from conftest import golden_cases, load_golden
+from conftest import golden_cases, golden_scene, load_golden
 from flipengine3d_gb300.scenes import dam_break
 from oracle import refsim
 
@@ -14,10 +14,16 @@ STAGES = ("phi", "vu_p2g", "vv_p2g", "vw_p2g", "u_p2g", "v_p2g", "w_p2g", "press
           "w_final", "vel_g2p", "pos_adv")
 
 
-@pytest.mark.parametrize("case", golden_cases())
+def wall_cases():
+    """Fixtures of scenes with the domain walls only: the oracle port restates
+    the walls; obstacle scenes are pinned by the reference's fixtures alone."""
+    return [c for c in golden_cases() if load_golden(c)[0].get("builder", "dam_break") == "dam_break"]
+
+
+@pytest.mark.parametrize("case", wall_cases())
 def test_oracle_matches_golden_bit_exact(built, case):
     meta, g = load_golden(case)
-    sc = dam_break(**meta["scene"])
+    sc = golden_scene(meta)
     orc = refsim.OracleSimulation(sc.isize, sc.jsize, sc.ksize, sc.dx, threads=meta["threads"])
     orc.setup(sc, tolerance=meta["tolerance"])
     st = orc.update_staged(meta["dt"])
