@@ -41,6 +41,16 @@ struct StepConsts {
     const float *blockPosF;
 };
 
+// -- seeding from fluid meshes (flip_seed.cu); mask: one 8-bit sub-cell
+// mask per cell, four cells to a word; owner: 8 I J K words, all ones
+void launch_mask_particles(const ParticleSoA &p, int n, const StepConsts &c, unsigned int *mask, cudaStream_t s);
+void launch_seed_candidates(const StepConsts &c, const int *cells, long long ncells, const float *meshPhi,
+                            const float *solidPhi, double jitter, bool jitterSurface, unsigned long long seed,
+                            const unsigned int *mask, float4 *cand, unsigned int *owner, int *keep, cudaStream_t s);
+void launch_seed_scatter(const StepConsts &c, long long ncand, const float4 *cand, const int *keep, const int *rank,
+                         const ParticleSoA &p, int n0, unsigned int id0, float vx, float vy, float vz,
+                         unsigned int *mask, cudaStream_t s);
+
 // -- binning (flip_kernels.cu)
 void launch_keys_from_positions(const ParticleSoA &p, int n, const StepConsts &c, unsigned int *keys, cudaStream_t s);
 void launch_bin_count(const unsigned int *keys, int n, int *cellCount, cudaStream_t s);
@@ -81,12 +91,22 @@ void launch_mark_fast(const ParticleSoA &p, int n, const float *maxSpeedSq, unsi
 // into tiles of SWEEP_TJ x SWEEP_TK: SWEEP_TJ along the tile's lane axis a
 // and SWEEP_TK along its warp axis b, where (a, b) = (j, k), or (k, j) when
 // `swap` is set (the orientation is chosen per solve).  Pencil (l, w) of a
-// tile holds cell i at forward step tf = i - 1 + l + w, and entry
-// (tile, tf, w, l) lives at ((tile * T + tf) * SWEEP_NP + w * SWEEP_TJ + l),
-// T = I - 2 + SWEEP_TJ - 1 + SWEEP_TK - 1.  A chunk of consecutive steps of a
-// tile is one contiguous block, in either sweep direction.  Entries that hold
-// no interior cell stay zero.
+// tile holds cell i at forward step tf = i - 1 + SWEEP_SL * l + SWEEP_SW * w:
+// a pencil runs SWEEP_SL steps behind its lane neighbour and SWEEP_SW steps
+// behind its warp neighbour, so a term crosses lanes SWEEP_SL steps and warps
+// SWEEP_SW steps after it is formed.  Entry (tile, tf, w, l) lives at
+// ((tile * T + tf) * SWEEP_NP + w * SWEEP_TJ + l),
+// T = I - 2 + SWEEP_SL * (SWEEP_TJ - 1) + SWEEP_SW * (SWEEP_TK - 1).  A chunk of
+// consecutive steps of a tile is one contiguous block, in either sweep
+// direction.  Entries that hold no interior cell stay zero.
+#ifndef SWEEP_SL
+#define SWEEP_SL 1
+#endif
+#ifndef SWEEP_SW
+#define SWEEP_SW 1
+#endif
 constexpr int SWEEP_TJ = 32, SWEEP_TK = 8, SWEEP_NP = SWEEP_TJ * SWEEP_TK;
+static_assert(SWEEP_SL >= 1 && SWEEP_SL <= 4 && SWEEP_SW >= 1 && SWEEP_SW <= 4, "sweep skews");
 struct SweepLayout {
     int ntj, ntk, T;   // tiles along the lane and warp axes, steps per tile
     int swap;          // 0: lanes along j, warps along k; 1: lanes along k, warps along j
@@ -99,7 +119,7 @@ inline SweepLayout sweep_layout(int I, int J, int K, int swap = 0) {
     g.EB = swap ? J : K;
     g.ntj = (g.EA - 2 + SWEEP_TJ - 1) / SWEEP_TJ;
     g.ntk = (g.EB - 2 + SWEEP_TK - 1) / SWEEP_TK;
-    g.T = (I - 2) + (SWEEP_TJ - 1) + (SWEEP_TK - 1);
+    g.T = (I - 2) + SWEEP_SL * (SWEEP_TJ - 1) + SWEEP_SW * (SWEEP_TK - 1);
     return g;
 }
 // entries of either orientation: the arrays are allocated for the larger
@@ -116,7 +136,7 @@ __host__ __device__ __forceinline__ long long sweep_index(const SweepLayout &g, 
     const int aa = (g.swap ? k : j) - 1, bb = (g.swap ? j : k) - 1;
     const int l = aa % SWEEP_TJ, w = bb % SWEEP_TK;
     const int tile = aa / SWEEP_TJ + g.ntj * (bb / SWEEP_TK);
-    return ((long long)tile * g.T + (i - 1 + l + w)) * SWEEP_NP + w * SWEEP_TJ + l;
+    return ((long long)tile * g.T + (i - 1 + SWEEP_SL * l + SWEEP_SW * w)) * SWEEP_NP + w * SWEEP_TJ + l;
 }
 
 // Device-side control of the PCG loop: the convergence test runs on the

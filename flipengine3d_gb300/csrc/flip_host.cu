@@ -83,6 +83,17 @@ struct flip_ctx {
 
     DomainBox box;
     std::vector<MeshObstacle> obstacles;   // static mesh obstacles (addMeshObstacle)
+    // fluid meshes queued by addMeshFluid, seeded at the end of the next substep
+    struct FluidMesh {
+        std::vector<float> verts;
+        std::vector<int> tris;
+        float vx, vy, vz;
+    };
+    std::vector<FluidMesh> fluidQueue;
+    double jitterFactor = 0.0;      // _markerParticleJitterFactor
+    bool jitterSurface = false;     // _isJitterSurfaceMarkerParticlesEnabled
+    unsigned long long seedCalls = 0;
+    unsigned int idNext = 0;        // ids handed out so far (loaded, then seeded)
     float *fu = nullptr, *fv = nullptr, *fw = nullptr;   // face friction, when an obstacle has some
     StepConsts c{};
 
@@ -113,6 +124,7 @@ struct flip_ctx {
     } *mail = nullptr;
     PressureMail *pmail = nullptr;
     std::vector<void *> allocations;
+    std::vector<size_t> allocationBytes;
 
     long long launches = 0;      // kernel launches of this context's calls
     long long deviceBytes = 0;   // device memory allocated for this context
@@ -139,9 +151,20 @@ struct flip_ctx {
         int rc = dalloc(p, count);
         if (rc == FLIP_OK) {
             allocations.push_back((void *)*p);
-            deviceBytes += (long long)(count * sizeof(T));
+            allocationBytes.push_back(std::max<size_t>(count, 1) * sizeof(T));
+            deviceBytes += (long long)allocationBytes.back();
         }
         return rc;
+    }
+    void release(void *p) {
+        for (size_t q = 0; q < allocations.size(); q++)
+            if (allocations[q] == p) {
+                cudaFree(p);
+                deviceBytes -= (long long)allocationBytes[q];
+                allocations.erase(allocations.begin() + q);
+                allocationBytes.erase(allocationBytes.begin() + q);
+                return;
+            }
     }
 };
 
@@ -279,6 +302,97 @@ int alloc_particles(flip_ctx *x, int cap) {
         (rc = x->alloc(&x->idScratch, scan_scratch_ints(cap) + 4)) || (rc = x->alloc(&x->idTotal, 4)))
         return rc;
     return FLIP_OK;
+}
+
+int rebin(flip_ctx *x);
+
+// Larger particle storage, keeping the n particles of `pa` (seeding adds
+// particles after initialize; the stream is idle when this is called).
+int grow_particles(flip_ctx *x, int cap) {
+    if (cap <= x->capacity) return FLIP_OK;
+    ParticleSoA keep = x->pa;
+    const int oldCap = x->capacity;
+    void *old[] = {x->pa.px, x->pb.px, x->keys, x->slots, x->idFlags, x->idRank, x->idScratch, x->idTotal};
+    int rc = alloc_particles(x, cap);
+    if (rc) return rc;
+    cudaStream_t s = x->stream;
+    if (x->n > 0) {   // the six float planes and the ids of pa
+        for (int q = 0; q < 7; q++)
+            CK(cudaMemcpyAsync(x->pa.px + (size_t)q * cap, keep.px + (size_t)q * oldCap, (size_t)x->n * 4,
+                               cudaMemcpyDeviceToDevice, s));
+    }
+    if ((rc = sync(x))) return rc;
+    for (void *p : old) x->release(p);
+    return FLIP_OK;
+}
+
+// Fill the queued fluid meshes (_updateAddedFluidMeshObjectQueue,
+// fluidsimulation.cpp:4724-4759) after a substep: the cells and level set of
+// each mesh on the host, the particles on the device (flip_seed.cu), then
+// one binning of all particles.
+int seed_fluid_meshes(flip_ctx *x) {
+    if (x->fluidQueue.empty()) return FLIP_OK;
+    cudaStream_t s = x->stream;
+    const long long nc = x->nc();
+    std::vector<std::vector<int>> cells(x->fluidQueue.size());
+    std::vector<std::vector<float>> phi(x->fluidQueue.size());
+    long long ncand = 0, maxCand = 0;
+    for (size_t m = 0; m < x->fluidQueue.size(); m++) {
+        mesh_fluid_cells(x->I, x->J, x->K, x->dx, x->fluidQueue[m].verts, x->fluidQueue[m].tris, cells[m], phi[m]);
+        ncand += 8 * (long long)cells[m].size();
+        maxCand = std::max(maxCand, 8 * (long long)cells[m].size());
+    }
+    if ((long long)x->idNext + ncand >= 0x7fffffffLL) return fail(FLIP_E_OUT_OF_RANGE, "too many particles");
+    int rc;
+    if ((rc = grow_particles(x, std::max(x->capacity, (int)(x->idNext + ncand))))) return rc;
+    // scratch of this call only: seeding runs once per added mesh
+    struct Scratch {
+        std::vector<void *> p;
+        ~Scratch() { for (void *q : p) cudaFree(q); }
+    } sc;
+    auto get = [&](auto **ptr, long long count) {
+        if (dalloc(ptr, (size_t)std::max(count, 1LL))) return false;
+        sc.p.push_back((void *)*ptr);
+        return true;
+    };
+    unsigned int *mask, *owner;
+    float4 *cand;
+    int *dcells, *keep, *rank, *scratch, *total;
+    float *dphi;
+    const long long nphi = (long long)(x->I + 1) * (x->J + 1) * (x->K + 1);
+    if (!get(&mask, (nc + 3) / 4) || !get(&owner, 8 * nc) || !get(&cand, maxCand) || !get(&dcells, maxCand / 8) ||
+        !get(&keep, maxCand) || !get(&rank, maxCand + 1) || !get(&scratch, scan_scratch_ints((int)maxCand) + 4) ||
+        !get(&total, 4) || !get(&dphi, nphi))
+        return fail(FLIP_E_NOMEM, "cudaMalloc failed (seeding)");
+    CK(cudaMemsetAsync(mask, 0, (size_t)((nc + 3) / 4) * 4, s));
+    launch_mask_particles(x->pa, x->n, x->c, mask, s);
+    const double jitter = 0.25 * (x->jitterFactor - 1e-3) * x->dx;   // _getMarkerParticleJitter
+    for (size_t m = 0; m < x->fluidQueue.size(); m++) {
+        const long long nm = 8 * (long long)cells[m].size();
+        if (nm == 0) continue;
+        const auto &fm = x->fluidQueue[m];
+        CK(cudaMemcpyAsync(dcells, cells[m].data(), cells[m].size() * 4, cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(dphi, phi[m].data(), (size_t)nphi * 4, cudaMemcpyHostToDevice, s));
+        CK(cudaMemsetAsync(owner, 0xff, (size_t)(8 * nc) * 4, s));
+        const unsigned long long seed = 0x5eed5eed5eed5eedull ^ (++x->seedCalls * 0x2545f4914f6cdd1dull);
+        launch_seed_candidates(x->c, dcells, (long long)cells[m].size(), dphi, x->solidPhi, jitter, x->jitterSurface,
+                               seed, mask, cand, owner, keep, s);
+        launch_scan_cells(keep, (int)nm, rank, scratch, total, s);
+        CK(cudaMemcpyAsync(&x->mail->total, total, sizeof(int), cudaMemcpyDeviceToHost, s));
+        if ((rc = sync(x))) return rc;   // the cells and level set buffers are reused for the next mesh
+        const int added = x->mail->total;
+        launch_seed_scatter(x->c, nm, cand, keep, rank, x->pa, x->n, x->idNext, fm.vx, fm.vy, fm.vz, mask, s);
+        x->n += added;
+        x->idNext += (unsigned int)added;
+    }
+    x->fluidQueue.clear();
+    // bin everything (every particle kept, as loading does)
+    launch_keys_from_positions(x->pa, x->n, x->c, x->keys, s);
+    const int saveMax = x->maxPerCell;
+    x->maxPerCell = 0x7fffffff;
+    rc = rebin(x);
+    x->maxPerCell = saveMax;
+    return rc;
 }
 
 // Counting sort of the particles in `pa` by cell, with removal flags in
@@ -500,7 +614,8 @@ int step_fluid(flip_ctx *x, double dt, flip_stage_dump *d) {
         x->mark(FLIP_STAGE_ADVECT);
         x->mark(FLIP_STAGE_BINNING);
         x->mark(FLIP_NUM_STAGES);
-        return collect_stage_times(x);
+        if ((rc = collect_stage_times(x))) return rc;
+        return seed_fluid_meshes(x);   // _updateFluidObjects (fluidsimulation.cpp:5505)
     }
     // particle velocities, advection, removal (fluidsimulation.cpp:4172-4390)
     x->mark(FLIP_STAGE_ADVECT);
@@ -520,16 +635,22 @@ int step_fluid(flip_ctx *x, double dt, flip_stage_dump *d) {
     x->mark(FLIP_STAGE_BINNING);
     rc = rebin_marked(x);
     if (rc) return rc;
-    return collect_stage_times(x);
+    if ((rc = collect_stage_times(x))) return rc;
+    return seed_fluid_meshes(x);   // _updateFluidObjects (fluidsimulation.cpp:5505)
 }
 
 // _calculateNextTimeStep (fluidsimulation.cpp:5593-5613)
 double next_time_step(flip_ctx *x, double dt) {
     double maxu;
     if (x->frame == 0 && x->stepNumber == 0) {
+        // _predictMaximumMarkerParticleSpeed (:5529-5550): the queued fluid
+        // meshes' speeds, plus the body force over one frame
+        maxu = 0.0;
+        for (const auto &fm : x->fluidQueue)
+            maxu = std::fmax((double)std::sqrt(fm.vx * fm.vx + fm.vy * fm.vy + fm.vz * fm.vz), maxu);
         float3 bf = body_force(x);
         float len = std::sqrt(bf.x * bf.x + bf.y * bf.y + bf.z * bf.z);
-        maxu = 0.0 + len * dt;
+        maxu += len * dt;
     } else {
         maxu = x->maxSpeed;
     }
@@ -604,6 +725,7 @@ int do_initialize(flip_ctx *x) {
     }
     x->queuePos.clear(); x->queueVel.clear(); x->queueDevN = 0;
     x->n = (int)sx.size();
+    x->idNext = (unsigned int)x->n;
     if ((rc = alloc_particles(x, std::max(x->n, 1)))) return rc;
     if (x->n > 0) {
         std::vector<unsigned int> ids(x->n);
@@ -951,6 +1073,59 @@ int flip_add_mesh_obstacle(flip_ctx *x, int nverts, const float *verts, int ntri
     if (rc) return rc;
     x->obstacles.push_back(std::move(one[0]));
     x->solidBuilt = false;   // rebuilt before the next step (_isSolidLevelSetUpToDate, fluidsimulation.cpp:2007)
+    return FLIP_OK;
+}
+
+int flip_add_mesh_fluid(flip_ctx *x, int nverts, const float *verts, int ntris, const int *tris, double vx, double vy,
+                        double vz) {
+    if (!x) return FLIP_E_NULL;
+    std::vector<MeshObstacle> one;   // the same checks as an obstacle's arrays
+    int rc = obstacles_from_arrays(1, &nverts, verts, &ntris, tris, nullptr, one);
+    if (rc) return rc;
+    if (!std::isfinite(vx) || !std::isfinite(vy) || !std::isfinite(vz)) return fail(FLIP_E_DOMAIN, "non-finite velocity");
+    flip_ctx::FluidMesh fm;
+    fm.verts = std::move(one[0].verts);
+    fm.tris = std::move(one[0].tris);
+    fm.vx = (float)vx; fm.vy = (float)vy; fm.vz = (float)vz;   // vmath::vec3
+    x->fluidQueue.push_back(std::move(fm));
+    return FLIP_OK;
+}
+
+int flip_set_marker_particle_jitter_factor(flip_ctx *x, double jit) {
+    if (!x) return FLIP_E_NULL;
+    if (!(jit >= 0.0)) return fail(FLIP_E_DOMAIN, "Error: marker particle jitter must be greater than or equal to 0.");
+    x->jitterFactor = jit;
+    return FLIP_OK;
+}
+int flip_get_marker_particle_jitter_factor(flip_ctx *x, double *jit) {
+    if (!x || !jit) return FLIP_E_NULL;
+    *jit = x->jitterFactor;
+    return FLIP_OK;
+}
+int flip_set_jitter_surface_marker_particles(flip_ctx *x, int enable) {
+    if (!x) return FLIP_E_NULL;
+    x->jitterSurface = enable != 0;
+    return FLIP_OK;
+}
+int flip_is_jitter_surface_marker_particles_enabled(flip_ctx *x, int *enabled) {
+    if (!x || !enabled) return FLIP_E_NULL;
+    *enabled = x->jitterSurface ? 1 : 0;
+    return FLIP_OK;
+}
+
+int flip_mesh_fluid_cells(int isize, int jsize, int ksize, double dx, int nverts, const float *verts, int ntris,
+                          const int *tris, int *ncells, int *cells, float *phi) {
+    if (!ncells) return FLIP_E_NULL;
+    if (isize <= 0 || jsize <= 0 || ksize <= 0 || !(dx > 0.0)) return fail(FLIP_E_DOMAIN, "bad grid");
+    std::vector<MeshObstacle> one;
+    int rc = obstacles_from_arrays(1, &nverts, verts, &ntris, tris, nullptr, one);
+    if (rc) return rc;
+    std::vector<int> c;
+    std::vector<float> p;
+    mesh_fluid_cells(isize, jsize, ksize, dx, one[0].verts, one[0].tris, c, p);
+    *ncells = (int)c.size();
+    if (cells) std::copy(c.begin(), c.end(), cells);
+    if (phi) std::copy(p.begin(), p.end(), phi);
     return FLIP_OK;
 }
 

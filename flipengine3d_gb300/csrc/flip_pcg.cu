@@ -880,13 +880,13 @@ int pressure_project(const StepConsts &c, const PressureArgs &a, PressureBuffers
     }
     // Sweep tile orientation for this solve: the one whose tiles the rows'
     // extent crosses with the shorter chain of hops.  A hop across the lane
-    // axis delays the next tile by about TJ + chunk + handoff steps, across
-    // the warp axis by about TK + chunk + handoff.
+    // axis delays the next tile by about SL TJ + chunk + handoff steps, across
+    // the warp axis by about SW TK + chunk + handoff.
     {
         const int jlo = mail->levelRange[3], jhi = mail->levelRange[4];
         const int klo = mail->levelRange[5], khi = mail->levelRange[6];
         auto hops = [](int lo_, int hi_, int w) { return (hi_ - 1) / w - (lo_ - 1) / w; };
-        const int lagA = SWEEP_TJ + 8 + 14, lagB = SWEEP_TK + 8 + 14;
+        const int lagA = SWEEP_SL * SWEEP_TJ + 8 + 14, lagB = SWEEP_SW * SWEEP_TK + 8 + 14;
         const long long cost0 = (long long)hops(jlo, jhi, SWEEP_TJ) * lagA + (long long)hops(klo, khi, SWEEP_TK) * lagB;
         const long long cost1 = (long long)hops(klo, khi, SWEEP_TJ) * lagA + (long long)hops(jlo, jhi, SWEEP_TK) * lagB;
         int want = cost1 < cost0 ? 1 : (cost0 < cost1 ? 0 : pb.sl.swap);

@@ -11,27 +11,38 @@
 //
 // Mapping.  A CTA owns a tile of 32 (j) x 8 (k) pencils along i.  Its eight
 // compute warps hold one pencil per thread (lane = j, warp = k); in the
-// forward sweep thread (l, w) processes i = 1 + t - l - w at step t, so its
-// j-1 neighbour (lane l-1) and k-1 neighbour (warp w-1) finished that i at
-// step t-1: j terms arrive by warp shuffle, k terms through shared memory
-// after the per-step barrier (the backward sweep is the mirror image).  In
-// the forward sweep a cell hands its neighbours the finished products
-// L_c * y_c rather than y_c: each product is rounded once, by whichever
-// thread forms it, so the bits are the reference's.
+// forward sweep thread (l, w) processes i = 1 + t - SL l - SW w at step t, so
+// its j-1 neighbour (lane l-1) finished that i at step t - SL and its k-1
+// neighbour (warp w-1) at step t - SW: j terms arrive by warp shuffle, k terms
+// through shared memory, and the compute warps meet at a barrier once every
+// SW steps (the backward sweep is the mirror image).  In the forward sweep a
+// cell hands its neighbours the finished products L_c * y_c rather than y_c:
+// each product is rounded once, by whichever thread forms it, so the bits
+// are the reference's.
 //
-// Data movement.  The factor rows, the right-hand side and the result live
-// in the step-major sweep layout (flip_device.cuh), so the 8 steps of a
-// chunk of a tile are one contiguous block in either direction.  A helper
-// warp moves whole chunks with bulk asynchronous copies into a ring of
-// shared-memory slots (an mbarrier per slot counts the bytes in), writes
-// finished chunks back with bulk stores, and fetches the terms that the
-// neighbouring tiles publish for the chunk's edge cells.  The compute warps
-// only read operands from the slot and run the arithmetic; cells outside
-// the grid read zero rows, so a step is unpredicated.
+// Data movement.  The factor rows and the right-hand side live in the
+// step-major sweep layout (flip_device.cuh), so the 8 steps of a chunk of a
+// tile are one contiguous block in either direction.  A loader warp moves
+// whole chunks with bulk asynchronous copies into a ring of five
+// shared-memory slots as soon as a slot is free (an mbarrier per slot counts
+// the bytes in) and prefetches the chunk one ring further ahead into L2; an
+// edge warp fetches the terms that the neighbouring tiles publish for the
+// chunk's edge cells.  The two run independently, so a tile waiting for its
+// neighbours still has its operands on the way.  The compute warps read
+// operands from the slot, run the arithmetic and store each result straight
+// to global memory (a warp writes 128 contiguous bytes per step); cells
+// outside the grid read zero rows, so a step is unpredicated.
+//
+// The sweep is bound by how many operand bytes a tile keeps in flight: with
+// the compute loop stripped of every barrier, shuffle and shared-memory
+// exchange a one-tile sweep ran as long as with them, and with results
+// staged through shared memory (a bulk store per chunk, four slots) or
+// operands loaded into registers one chunk ahead, a tile was limited by the
+// latency of refilling its few chunks in flight.
 //
 // Tile edges.  The threads on a tile's downstream edges publish each term
 // they form as one 64-bit word {sweep epoch, value}, indexed by step, in an
-// exchange array; the neighbour's helper warp polls exactly the words its
+// exchange array; the neighbour's edge warp polls exactly the words its
 // chunk needs until their epoch is the current sweep's.  A single naturally
 // aligned 64-bit store is seen whole or not at all, so no fence, flag or
 // progress counter sits between the producing step and the consuming one.
@@ -48,17 +59,23 @@ namespace flip {
 
 namespace {
 
-constexpr int TJ = SWEEP_TJ, TK = SWEEP_TK, NP = SWEEP_NP, CH = 8;
+#ifndef SWEEP_CH
+#define SWEEP_CH 8   // steps per chunk
+#endif
+constexpr int TJ = SWEEP_TJ, TK = SWEEP_TK, NP = SWEEP_NP, CH = SWEEP_CH, SL = SWEEP_SL, SW = SWEEP_SW;
+// a chunk holds whole blocks of SW steps and whole rounds of the SL-deep lane
+// history, and the shared-memory ring of warp terms (2 SW steps) divides it
+static_assert(CH % SL == 0 && CH % (2 * SW) == 0, "sweep skews must divide the chunk");
 #ifndef SWEEP_NBUF
-#define SWEEP_NBUF (SWEEP_TK <= 8 ? 4 : 2)   // ring slots that fit in shared memory
+#define SWEEP_NBUF 5   // ring slots that fit in shared memory
 #endif
 constexpr int NBUF = SWEEP_NBUF;
 static_assert(NBUF >= 2, "the ring needs a slot in flight beside the one in use");
-// the helper warp's lanes take the CH x TK j-edge words JQ at a time and the
+// the edge warp's lanes take the CH x TK j-edge words JQ at a time and the
 // CH x TJ k-edge words one step each
 constexpr int JQ = CH * TK / 32;
-static_assert((CH * TK) % 32 == 0 && TJ == 32 && JQ <= 32, "edge-word mapping of the helper warp");
-constexpr int NCOMP = NP, NTHREADS = NCOMP + 32;
+static_assert((CH * TK) % 32 == 0 && TJ == 32 && JQ <= 32, "edge-word mapping of the edge warp");
+constexpr int NCOMP = NP, LOADER = NCOMP / 32, EDGE = LOADER + 1, NTHREADS = NCOMP + 64;
 // Waiting for this CTA's own bulk copies in flight (they complete by
 // themselves) keeps the default limit, whatever limit the edge waits have.
 constexpr unsigned int DRAIN_SPIN_LIMIT = DEFAULT_SPIN_LIMIT;
@@ -82,14 +99,15 @@ struct SweepArgs {
 struct Slot {
     float4 L[CH][NP];   // rows in layout order: forward row q = step q, backward row q = step CH-1-q
     float r[CH][NP];
-    float o[CH][NP];
     float eJ[CH][TK];   // by step: term from the j neighbour tile for the edge lane of each warp
     float eK[CH][TJ];   // by step: term from the k neighbour tile for each lane of the edge warp
 };
 struct SweepSmem {
     Slot slot[NBUF];
-    float p[2][TK][TJ];   // forward: L_w y of each pencil's last cell; backward: its z
-    unsigned long long full[NBUF], done[NBUF];
+    float p[2 * SW][TK][TJ];   // by step mod 2 SW: forward L_w y of each pencil's cell; backward its z
+    // per slot: operand bytes in (the loader), edge terms in (the edge warp),
+    // chunk done (the compute warps)
+    unsigned long long loaded[NBUF], edges[NBUF], done[NBUF];
     int abort;
     int tile;
     unsigned int epoch;
@@ -113,8 +131,9 @@ __device__ __forceinline__ void mb_init(unsigned long long *b, unsigned count) {
 __device__ __forceinline__ void mb_arrive(unsigned long long *b) {
     asm volatile("{\n .reg .b64 st;\n mbarrier.arrive.shared::cta.b64 st, [%0];\n}" ::"r"(smem_addr(b)) : "memory");
 }
-__device__ __forceinline__ void mb_expect_tx(unsigned long long *b, unsigned bytes) {
-    asm volatile("mbarrier.expect_tx.relaxed.cta.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(b)), "r"(bytes) : "memory");
+__device__ __forceinline__ void mb_arrive_expect_tx(unsigned long long *b, unsigned bytes) {
+    asm volatile("{\n .reg .b64 st;\n mbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n}" ::"r"(smem_addr(b)),
+                 "r"(bytes) : "memory");
 }
 __device__ __forceinline__ bool mb_test(unsigned long long *b, unsigned parity) {
     unsigned ok;
@@ -122,12 +141,21 @@ __device__ __forceinline__ bool mb_test(unsigned long long *b, unsigned parity) 
                  : "=r"(ok) : "r"(smem_addr(b)), "r"(parity) : "memory");
     return ok != 0;
 }
-// Bounded wait for a phase of an mbarrier; false on abort or timeout.
+// One round of waiting for a phase: the thread is suspended until the phase
+// completes or about `ns` nanoseconds pass, so waiting warps take no issue
+// slots from the warps that compute on the same scheduler.
+__device__ __forceinline__ bool mb_try(unsigned long long *b, unsigned parity, unsigned ns) {
+    unsigned ok;
+    asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n selp.u32 %0, 1, 0, p;\n}"
+                 : "=r"(ok) : "r"(smem_addr(b)), "r"(parity), "r"(ns) : "memory");
+    return ok != 0;
+}
+// Bounded wait for a phase of an mbarrier; false on abort or timeout (which
+// raises the abort and error flags).
 __device__ bool mb_wait(unsigned long long *b, unsigned parity, int *abortFlag, int *err, unsigned int limit) {
     for (unsigned int spin = 0; spin < limit; spin++) {
-        if (mb_test(b, parity)) return true;
+        if (mb_try(b, parity, 256)) return true;
         if (*(volatile int *)abortFlag) return false;
-        if (spin > 1024) __nanosleep(32);
     }
     *(volatile int *)abortFlag = 1;
     atomicExch(err, 1);
@@ -138,14 +166,9 @@ __device__ __forceinline__ void bulk_load(void *dst, const void *src, unsigned b
     asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
                  ::"r"(smem_addr(dst)), "l"(src), "r"(bytes), "r"(smem_addr(b)) : "memory");
 }
-__device__ __forceinline__ void bulk_store(void *dst, const void *src, unsigned bytes) {
-    asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(dst), "r"(smem_addr(src)),
-                 "r"(bytes) : "memory");
+__device__ __forceinline__ void prefetch_l2(const void *src, unsigned bytes) {
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(src), "r"(bytes) : "memory");
 }
-__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
-__device__ __forceinline__ void bulk_wait_read_all() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
-__device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
-__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 // named barrier of the compute warps, plain and with an OR vote
 __device__ __forceinline__ bool compute_sync_or(bool v) {
     unsigned r;
@@ -173,7 +196,8 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_wavefront(SweepArgs a) {
         sm.abort = 0;
         sm.epoch = *(volatile unsigned int *)&a.ticket[1] + (FWD ? 0u : 1u);   // forward e, backward e + 1
         for (int b = 0; b < NBUF; b++) {
-            mb_init(&sm.full[b], 32);      // the helper warp's lanes, plus the bytes of the chunk
+            mb_init(&sm.loaded[b], 1);      // the loader's arrival, plus the bytes of the chunk
+            mb_init(&sm.edges[b], 32);      // the edge warp's lanes
             mb_init(&sm.done[b], NCOMP);
         }
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -194,7 +218,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_wavefront(SweepArgs a) {
     const int j0 = 1 + tj * TJ, k0 = 1 + tk * TK;
     // cell of pencil (lane lr, warp ww) at step t
     auto cell = [&](int lr, int ww, int t) {
-        return FWD ? 1 + t - lr - ww : NI - t + (TJ - 1 - lr) + (TK - 1 - ww);
+        return FWD ? 1 + t - SL * lr - SW * ww : NI - t + SL * (TJ - 1 - lr) + SW * (TK - 1 - ww);
     };
     auto pencil_in = [&](int lr, int ww) { return j0 + lr <= a.J - 2 && k0 + ww <= a.K - 2; };
     const size_t wordsPerTile = (size_t)T * (TJ + TK);
@@ -205,10 +229,49 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_wavefront(SweepArgs a) {
     auto chunk_row0 = [&](int rows) { return FWD ? 0 : CH - rows; };
     auto chunk_tf0 = [&](int tb, int rows) { return FWD ? tb : T - tb - rows; };
     const size_t tileBase = (size_t)tile * T * NP;
+    const int warp = threadIdx.x >> 5;
 
-    if (threadIdx.x >= NCOMP) {
-        // ================================================== helper warp
-        const int lane = threadIdx.x - NCOMP;
+    if (warp == LOADER) {
+        // ================================================== loader warp
+        if ((threadIdx.x & 31) != 0) return;
+        auto issue = [&](int m, int b) {   // operands of chunk m into slot b
+            Slot &sl = sm.slot[b];
+            const int tb = tlo + m * CH, rows = chunk_rows(m);
+            const unsigned bl = (unsigned)(rows * NP * sizeof(float4)), br = (unsigned)(rows * NP * sizeof(float));
+            const size_t e0 = tileBase + (size_t)chunk_tf0(tb, rows) * NP;
+            mb_arrive_expect_tx(&sm.loaded[b], bl + br);
+            bulk_load(&sl.L[chunk_row0(rows)][0], a.L + e0, bl, &sm.loaded[b]);
+            bulk_load(&sl.r[chunk_row0(rows)][0], a.rin + e0, br, &sm.loaded[b]);
+        };
+        auto prefetch = [&](int m) {   // chunk m into L2, for its copy one ring later
+            if (m >= nChunks) return;
+            const int tb = tlo + m * CH, rows = chunk_rows(m);
+            const size_t e0 = tileBase + (size_t)chunk_tf0(tb, rows) * NP;
+            prefetch_l2(a.L + e0, (unsigned)(rows * NP * sizeof(float4)));
+            prefetch_l2(a.rin + e0, (unsigned)(rows * NP * sizeof(float)));
+        };
+        int issued = 0;
+        for (; issued < nChunks; issued++) {
+            const int b = issued % NBUF;
+            if (issued >= NBUF &&
+                !mb_wait(&sm.done[b], ((issued - NBUF) / NBUF) & 1, &sm.abort, a.err, a.spinLimit))
+                break;
+            issue(issued, b);
+            prefetch(issued + NBUF);
+        }
+        // The copies started must land before the CTA's shared memory is
+        // released, also when the compute warps stop early: each slot's
+        // phase completes once its bytes are in.
+        for (int m = max(0, issued - NBUF); m < issued; m++)
+            for (unsigned int spin = 0;
+                 spin < DRAIN_SPIN_LIMIT && !mb_test(&sm.loaded[m % NBUF], (m / NBUF) & 1); spin++)
+                __nanosleep(32);
+        return;
+    }
+
+    if (warp == EDGE) {
+        // ==================================================== edge warp
+        const int lane = threadIdx.x & 31;
         const int srcJ = FWD ? (tj > 0 ? tile - 1 : -1) : (tj < a.ntj - 1 ? tile + 1 : -1);
         const int srcK = FWD ? (tk > 0 ? tile - a.ntj : -1) : (tk < a.ntk - 1 ? tile + a.ntj : -1);
         const int2 rgJ = srcJ >= 0 ? steps_of(srcJ) : make_int2(1, 0);
@@ -216,33 +279,14 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_wavefront(SweepArgs a) {
         const int laneJ = FWD ? 0 : TJ - 1, warpK = FWD ? 0 : TK - 1;
         const unsigned long long *srcJw = a.xchg + (srcJ >= 0 ? srcJ : 0) * wordsPerTile;
         const unsigned long long *srcKw = a.xchg + (srcK >= 0 ? srcK : 0) * wordsPerTile + (size_t)T * TK;
-        bool ok = true;
-        int lastIssued = -1;   // last chunk whose operand copies were started
-        for (int m = 0; m < nChunks + NBUF && ok; m++) {
+        for (int m = 0; m < nChunks; m++) {
             const int b = m % NBUF;
             Slot &sl = sm.slot[b];
-            if (m >= NBUF) {   // write chunk m - NBUF back once its results are in
-                const int n = m - NBUF;
-                if (!mb_wait(&sm.done[b], (n / NBUF) & 1, &sm.abort, a.err, a.spinLimit)) { ok = false; break; }
-                if (lane == 0) {
-                    const int rows = chunk_rows(n), tb = tlo + n * CH;
-                    bulk_store(a.out + tileBase + (size_t)chunk_tf0(tb, rows) * NP, &sl.o[chunk_row0(rows)][0],
-                               (unsigned)(rows * NP * sizeof(float)));
-                    bulk_commit();
-                }
-            }
-            if (m >= nChunks) continue;
+            if (m >= NBUF && !mb_wait(&sm.done[b], ((m - NBUF) / NBUF) & 1, &sm.abort, a.err, a.spinLimit))
+                return;   // aborting
             const int tb = tlo + m * CH, rows = chunk_rows(m);
-            if (lane == 0) {   // operands of chunk m
-                const unsigned bl = (unsigned)(rows * NP * sizeof(float4)), br = (unsigned)(rows * NP * sizeof(float));
-                const size_t e0 = tileBase + (size_t)chunk_tf0(tb, rows) * NP;
-                mb_expect_tx(&sm.full[b], bl + br);
-                bulk_load(&sl.L[chunk_row0(rows)][0], a.L + e0, bl, &sm.full[b]);
-                bulk_load(&sl.r[chunk_row0(rows)][0], a.rin + e0, br, &sm.full[b]);
-            }
-            lastIssued = m;
             // edge terms: the consumer cell is computed and the producer's
-            // cell (TJ-1 or TK-1 steps later there) too
+            // cell (SL (TJ-1) or SW (TK-1) steps later there) too
             float vK[CH], vJ[JQ];
             unsigned long long wK[CH], wJ[JQ];
             unsigned int needK = 0, needJ = 0;
@@ -250,18 +294,19 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_wavefront(SweepArgs a) {
             for (int s = 0; s < CH; s++) {
                 const int te = tb + s, i = cell(lane, warpK, te);
                 const bool need = srcK >= 0 && s < rows && pencil_in(lane, warpK) && i >= 1 && i <= NI &&
-                                  te + (TK - 1) >= rgK.x && te + (TK - 1) <= rgK.y;
-                wK[s] = need ? ld_word(srcKw + (size_t)(te + TK - 1) * TJ + lane) : 0ull;
+                                  te + SW * (TK - 1) >= rgK.x && te + SW * (TK - 1) <= rgK.y;
+                wK[s] = need ? ld_word(srcKw + (size_t)(te + SW * (TK - 1)) * TJ + lane) : 0ull;
                 needK |= need ? 1u << s : 0u;
             }
 #pragma unroll
             for (int q = 0; q < JQ; q++) {
                 const int e = lane + 32 * q, es = e / TK, ew = e % TK, te = tb + es, i = cell(laneJ, ew, te);
                 const bool need = srcJ >= 0 && es < rows && pencil_in(laneJ, ew) && i >= 1 && i <= NI &&
-                                  te + (TJ - 1) >= rgJ.x && te + (TJ - 1) <= rgJ.y;
-                wJ[q] = need ? ld_word(srcJw + (size_t)(te + TJ - 1) * TK + ew) : 0ull;
+                                  te + SL * (TJ - 1) >= rgJ.x && te + SL * (TJ - 1) <= rgJ.y;
+                wJ[q] = need ? ld_word(srcJw + (size_t)(te + SL * (TJ - 1)) * TK + ew) : 0ull;
                 needJ |= need ? 1u << q : 0u;
             }
+            bool ok = true;
             for (unsigned int spin = 0;; spin++) {
                 unsigned int missK = 0, missJ = 0;
 #pragma unroll
@@ -272,21 +317,25 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_wavefront(SweepArgs a) {
                     missJ |= ((needJ >> q) & 1u) && (unsigned int)(wJ[q] >> 32) != epWait ? 1u << q : 0u;
                 if (!(missK | missJ)) break;
                 if (spin >= a.spinLimit) {
-                    *(volatile int *)&sm.abort = 1;
                     atomicExch(a.err, 1);
-                    ok = false;   // still arrive below, so that the chunk's copies can be waited for
+                    ok = false;
                     break;
                 }
                 if (*(volatile int *)&sm.abort || *(volatile int *)a.err) { ok = false; break; }
-                if (spin > 1024) __nanosleep(64);
+                if (spin > 64) __nanosleep(32);
 #pragma unroll
                 for (int s = 0; s < CH; s++)
-                    if ((missK >> s) & 1u) wK[s] = ld_word(srcKw + (size_t)(tb + s + TK - 1) * TJ + lane);
+                    if ((missK >> s) & 1u) wK[s] = ld_word(srcKw + (size_t)(tb + s + SW * (TK - 1)) * TJ + lane);
 #pragma unroll
                 for (int q = 0; q < JQ; q++) {
                     const int e = lane + 32 * q, es = e / TK, ew = e % TK;
-                    if ((missJ >> q) & 1u) wJ[q] = ld_word(srcJw + (size_t)(tb + es + TJ - 1) * TK + ew);
+                    if ((missJ >> q) & 1u) wJ[q] = ld_word(srcJw + (size_t)(tb + es + SL * (TJ - 1)) * TK + ew);
                 }
+            }
+            if (!__all_sync(0xffffffffu, ok)) {
+                // the compute warps and the loader see the flag in their waits
+                *(volatile int *)&sm.abort = 1;
+                return;
             }
 #pragma unroll
             for (int s = 0; s < CH; s++) vK[s] = __uint_as_float((unsigned int)wK[s]);
@@ -299,25 +348,15 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_wavefront(SweepArgs a) {
                 const int e = lane + 32 * q;
                 sl.eJ[e / TK][e % TK] = vJ[q];
             }
-            if (lane == 0) bulk_wait_read_all();   // the slot's results of chunk m - NBUF are out
             __syncwarp();
-            mb_arrive(&sm.full[b]);
+            mb_arrive(&sm.edges[b]);
         }
-        if (!ok) {
-            // Stopping early: the operand copies already started must land
-            // before the CTA's shared memory is released.  Their phases have
-            // all arrivals, so each completes once its bytes are in.
-            for (int m = max(0, lastIssued - NBUF + 1); m <= lastIssued; m++)
-                for (unsigned int spin = 0; spin < DRAIN_SPIN_LIMIT && !mb_test(&sm.full[m % NBUF], (m / NBUF) & 1); spin++)
-                    __nanosleep(32);
-        }
-        if (lane == 0) bulk_wait_all();   // every write-back complete before the CTA ends
         return;
     }
 
     // ====================================================== compute warps
-    const int l = threadIdx.x & 31, w = threadIdx.x >> 5;
-    int v0 = FWD ? l + w : (TJ - 1 - l) + (TK - 1 - w);   // steps at which the own cell is interior
+    const int l = threadIdx.x & 31, w = warp;
+    int v0 = FWD ? SL * l + SW * w : SL * (TJ - 1 - l) + SW * (TK - 1 - w);   // steps at which the own cell is interior
     int v1 = v0 + NI - 1;
     if (!pencil_in(l, w)) { v0 = 1; v1 = 0; }
     v0 = max(v0, tlo);
@@ -326,25 +365,34 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_wavefront(SweepArgs a) {
     const bool pubK = FWD ? (w == TK - 1 && tk < a.ntk - 1) : (w == 0 && tk > 0);
     unsigned long long *pubJw = a.xchg + tile * wordsPerTile + w;                     // [t][TK]
     unsigned long long *pubKw = a.xchg + tile * wordsPerTile + (size_t)T * TK + l;    // [t][TJ]
-    sm.p[0][w][l] = 0.0f;
-    sm.p[1][w][l] = 0.0f;
-    // forward: this pencil's terms from its last cell, L_x y (own next cell)
-    // and L_y y (lane l+1); backward: z of its last cell
-    float px = 0.0f, pz = 0.0f, zPrev = 0.0f;
+#pragma unroll
+    for (int q = 0; q < 2 * SW; q++) sm.p[q][w][l] = 0.0f;
+    // forward: L_x y of this pencil's last cell (for its next cell) and the
+    // L_y y terms of its last SL cells (for lane l+1), by step mod SL;
+    // backward: z of its last cell and of its last SL cells
+    float px = 0.0f, zPrev = 0.0f;
+    float hist[SL];
+#pragma unroll
+    for (int q = 0; q < SL; q++) hist[q] = 0.0f;
     for (int n = 0; n < nChunks; n++) {
         const int b = n % NBUF, tb = tlo + n * CH;
-        const bool fine = mb_wait(&sm.full[b], (n / NBUF) & 1, &sm.abort, a.err, a.spinLimit);
+        const unsigned par = (n / NBUF) & 1;
+        const bool fine = mb_wait(&sm.loaded[b], par, &sm.abort, a.err, a.spinLimit) &&
+                          mb_wait(&sm.edges[b], par, &sm.abort, a.err, a.spinLimit);
         if (compute_sync_or(!fine)) {
             *(volatile int *)&sm.abort = 1;
             return;
         }
-        Slot &sl = sm.slot[b];
-        const int par = tb & 1;
+        const Slot &sl = sm.slot[b];
+        // the results of chunk n: row of step tb + s at out0 + s * step
+        float *out0 = a.out + tileBase + (size_t)(FWD ? tb : T - 1 - tb) * NP + threadIdx.x;
+        const long long ostep = FWD ? NP : -NP;
 #pragma unroll
         for (int s = 0; s < CH; s++) {
+            // (tb - tlo) is a multiple of CH, so step t's ring positions are s's
             const int t = tb + s;
             const int q = FWD ? s : CH - 1 - s;
-            const int cb = (s & 1) ^ par, pb = cb ^ 1;   // buffers of steps t and t-1
+            const int cur = s % (2 * SW), prev = (s + SW) % (2 * SW);   // steps t and t - SW
             const float4 Lc = sl.L[q][threadIdx.x];
             const float rr = sl.r[q][threadIdx.x];
             const bool valid = t >= v0 && t <= v1;
@@ -352,38 +400,41 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_wavefront(SweepArgs a) {
             if (FWD) {
                 // terms from the lane and warp neighbours: L of the neighbour
                 // towards this cell times its y (y-axis coupling L.z, z-axis L.w)
-                float pL = __shfl_up_sync(0xffffffffu, pz, 1);
+                float pL = __shfl_up_sync(0xffffffffu, hist[s % SL], 1);
                 if (l == 0) pL = sl.eJ[s][w];
-                const float pW = w > 0 ? sm.p[pb][w - 1][l] : sl.eK[s][l];
+                const float pW = w > 0 ? sm.p[prev][w - 1][l] : sl.eK[s][l];
                 float acc = __fsub_rn(rr, SWAP ? pL : pW);   // -z
                 acc = __fsub_rn(acc, SWAP ? pW : pL);        // -y
                 acc = __fsub_rn(acc, px);                    // -x
                 res = __fmul_rn(acc, Lc.x);
                 px = __fmul_rn(Lc.y, res);
-                pz = __fmul_rn(SWAP ? Lc.w : Lc.z, res);     // for the next lane
+                const float pz = __fmul_rn(SWAP ? Lc.w : Lc.z, res);   // for the next lane
                 const float pw = __fmul_rn(SWAP ? Lc.z : Lc.w, res);   // for the next warp
-                sm.p[cb][w][l] = pw;
+                hist[s % SL] = pz;
+                sm.p[cur][w][l] = pw;
                 if (valid && pubJ) st_word(pubJw + (size_t)t * TK, pack(ep, pz));
                 if (valid && pubK) st_word(pubKw + (size_t)t * TJ, pack(ep, pw));
             } else {
-                float zL = __shfl_down_sync(0xffffffffu, zPrev, 1);
+                float zL = __shfl_down_sync(0xffffffffu, hist[s % SL], 1);
                 if (l == TJ - 1) zL = sl.eJ[s][w];
-                const float zW = w < TK - 1 ? sm.p[pb][w + 1][l] : sl.eK[s][l];
+                const float zW = w < TK - 1 ? sm.p[prev][w + 1][l] : sl.eK[s][l];
                 float acc = __fsub_rn(rr, __fmul_rn(Lc.y, zPrev));          // +x
                 acc = __fsub_rn(acc, __fmul_rn(Lc.z, SWAP ? zW : zL));      // +y
                 acc = __fsub_rn(acc, __fmul_rn(Lc.w, SWAP ? zL : zW));      // +z
                 res = __fmul_rn(acc, Lc.x);
                 zPrev = res;
-                sm.p[cb][w][l] = res;
+                hist[s % SL] = res;
+                sm.p[cur][w][l] = res;
                 if (valid && pubJ) st_word(pubJw + (size_t)t * TK, pack(ep, res));
                 if (valid && pubK) st_word(pubKw + (size_t)t * TJ, pack(ep, res));
             }
-            sl.o[q][threadIdx.x] = res;
+            __stcg(out0 + s * ostep, res);
             if (t == thi) break;
-            compute_sync();
+            // the warp terms of a block of SW steps are read in the next block;
+            // the chunk's last block meets the next chunk's opening barrier
+            if (s % SW == SW - 1 && s != CH - 1) compute_sync();
         }
-        fence_proxy_async();   // the results are read by the bulk store
-        mb_arrive(&sm.done[b]);
+        mb_arrive(&sm.done[b]);   // the slot may be refilled
     }
 }
 
@@ -406,7 +457,7 @@ __global__ void k_tile_range(const uint8_t *fluid, int I, int J, int K, SweepLay
         unflatten(t, I, J, i, j, k);
         const int aa = (g.swap ? k : j) - 1, bb = (g.swap ? j : k) - 1;
         tile = aa / TJ + g.ntj * (bb / TK);
-        step = (i - 1) + aa % TJ + bb % TK;
+        step = (i - 1) + SL * (aa % TJ) + SW * (bb % TK);
     }
     unsigned int grp = __match_any_sync(0xffffffffu, tile);
     int mn = __reduce_min_sync(grp, f ? step : 0x7fffffff);

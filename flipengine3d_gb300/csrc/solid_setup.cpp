@@ -141,58 +141,21 @@ bool ray_z_crossing(V p, V v0, V v1, V v2, float *z) {
     return true;
 }
 
-// The level set of one mesh over a sub-grid of nI x nJ x nK nodes whose
-// first node sits at `origin` (float position): the exact band in the block
-// frame and the signs from z-ray parity (meshlevelset.cpp:572-601,
-// 781-1158, 1298-1316).  Vertices are already relative to `origin`.
-void mesh_level_set(const std::vector<V> &vtx, const std::vector<int> &tris, int nI, int nJ, int nK, double dx,
-                    int band, std::vector<float> &phi, std::vector<int> &tri) {
-    const float upper = (float)((double)(nI + nJ + nK) * dx);
-    auto nid = [&](int i, int j, int k) { return (size_t)i + (size_t)nI * ((size_t)j + (size_t)nJ * k); };
-    phi.assign((size_t)nI * nJ * nK, upper);
-    tri.assign(phi.size(), -1);
-    const int bw = 10;
+// MeshUtils::getGridNodesInsideTriangleMesh for one mesh (meshutils.cpp:
+// 347-371, 156-215): the nodes become the cell centres of a grid shifted by
+// half a cell, and a node is inside when the z-ray through it crosses the
+// mesh an even number of times in all and an odd number of times below it.
+// `mark(i, j, k)` is called for each inside node (any index; the caller
+// keeps those in range).  The reference jitters the ray origins by a random
+// amount below 0.001 dx against rays that graze an edge; here the jitter is
+// a fixed amount in that range.
+template <class Mark>
+void inside_nodes_of(const std::vector<V> &vtx, const std::vector<int> &tris, double dx, Mark &&mark) {
     const int ntri = (int)tris.size() / 3;
-    for (int t = 0; t < ntri; t++) {
-        const V a = vtx[tris[3 * t]], b = vtx[tris[3 * t + 1]], e = vtx[tris[3 * t + 2]];
-        // AABB of the triangle: float minimum, double extent (aabb.cpp:84-110)
-        const float mn[3] = {std::min(a.x, std::min(b.x, e.x)), std::min(a.y, std::min(b.y, e.y)), std::min(a.z, std::min(b.z, e.z))};
-        const double ext[3] = {(double)std::max(a.x, std::max(b.x, e.x)) - mn[0], (double)std::max(a.y, std::max(b.y, e.y)) - mn[1],
-                               (double)std::max(a.z, std::max(b.z, e.z)) - mn[2]};
-        int lo[3], hi[3];
-        const int n[3] = {nI, nJ, nK};
-        bool outside = false;
-        for (int q = 0; q < 3; q++) {
-            lo[q] = floor_index(mn[q], dx) - band;
-            hi[q] = floor_index(mn[q] + (float)ext[q], dx) + band + 1;
-            if (hi[q] < 0 || lo[q] >= n[q]) outside = true;
-            lo[q] = std::max(lo[q], 0);
-            hi[q] = std::min(hi[q], n[q] - 1);
-        }
-        if (outside) continue;
-        for (int k = lo[2]; k <= hi[2]; k++)
-            for (int j = lo[1]; j <= hi[1]; j++)
-                for (int i = lo[0]; i <= hi[0]; i++) {
-                    const V off{gpos(i / bw, (double)bw * dx), gpos(j / bw, (double)bw * dx), gpos(k / bw, (double)bw * dx)};
-                    const V g{gpos(i % bw, dx), gpos(j % bw, dx), gpos(k % bw, dx)};
-                    const float dist = vlen(vsub(closest_point(g, vsub(a, off), vsub(b, off), vsub(e, off)), g));
-                    const size_t id = nid(i, j, k);
-                    if (dist < phi[id]) {
-                        phi[id] = dist;
-                        tri[id] = t;
-                    }
-                }
-    }
-    // Signs: the nodes become the cell centres of a grid shifted by half a
-    // cell, and a node is inside when the z-ray through it crosses the mesh
-    // an even number of times in all and an odd number of times below it
-    // (meshutils.cpp:156-215, 347-371).  The reference jitters the ray
-    // origins by a random amount below 0.001 dx against rays that graze an
-    // edge; here the jitter is a fixed amount in that range.
     const float half = (float)(0.5 * dx);
     std::vector<V> m(vtx.size());
     for (size_t q = 0; q < vtx.size(); q++) m[q] = vadd(vtx[q], V{half, half, half});
-    if (m.empty()) return;
+    if (m.empty() || ntri == 0) return;
     float bmin[3] = {m[0].x, m[0].y, m[0].z}, bmax[3] = {m[0].x, m[0].y, m[0].z};
     for (const V &v : m) {
         bmin[0] = std::min(bmin[0], v.x); bmin[1] = std::min(bmin[1], v.y); bmin[2] = std::min(bmin[2], v.z);
@@ -238,15 +201,146 @@ void mesh_level_set(const std::vector<V> &vtx, const std::vector<int> &tris, int
                 const float zk = (float)((float)k * dx + hw);
                 int less = 0;
                 for (float z : zc) less += z < zk;
-                if (less % 2 == 1) {   // node (i, j, k) + goffset is inside
-                    const int ni = i + go[0], nj = j + go[1], nk = k + go[2];
-                    if (ni >= 0 && nj >= 0 && nk >= 0 && ni < nI && nj < nJ && nk < nK) {
-                        float &v = phi[nid(ni, nj, nk)];
-                        v = -v;
-                    }
-                }
+                if (less % 2 == 1) mark(i + go[0], j + go[1], k + go[2]);
             }
         }
+}
+
+// MeshUtils::getGridNodesInsideTriangleMesh(mesh, dx, Array3d<bool>)
+// (meshutils.cpp:373-428) over nI x nJ x nK nodes: a mesh inside the grid's
+// box [0, (nI-1) dx) x ... is tested whole; otherwise it is cut into its
+// connected islands (_splitInsideOutsideMesh, :430-452; _splitIntoMeshIslands,
+// :454-557): the islands inside the box together, each island that reaches
+// into the box on its own, the rest not at all.
+void grid_nodes_inside(const std::vector<V> &vtx, const std::vector<int> &tris, int nI, int nJ, int nK, double dx,
+                       std::vector<uint8_t> &inside) {
+    inside.assign((size_t)nI * nJ * nK, 0);
+    auto mark = [&](int i, int j, int k) {
+        if (i >= 0 && j >= 0 && k >= 0 && i < nI && j < nJ && k < nK)
+            inside[(size_t)i + (size_t)nI * ((size_t)j + (size_t)nJ * k)] = 1;
+    };
+    const double W = (double)(nI - 1) * dx, H = (double)(nJ - 1) * dx, D = (double)(nK - 1) * dx;
+    auto in_box = [&](V p) {   // AABB::isPointInside (aabb.cpp:130-133), position 0
+        return p.x >= 0.0f && p.y >= 0.0f && p.z >= 0.0f && (double)p.x < W && (double)p.y < H && (double)p.z < D;
+    };
+    bool contained = true;
+    for (const V &v : vtx) contained = contained && in_box(v);
+    if (contained) {
+        inside_nodes_of(vtx, tris, dx, mark);
+        return;
+    }
+    // islands: vertices connected through triangle edges
+    const int nv = (int)vtx.size(), ntri = (int)tris.size() / 3;
+    std::vector<int> root(nv);
+    for (int q = 0; q < nv; q++) root[q] = q;
+    auto find = [&](int q) {
+        while (root[q] != q) q = root[q] = root[root[q]];
+        return q;
+    };
+    for (int t = 0; t < ntri; t++)
+        for (int e = 1; e < 3; e++) {
+            const int a = find(tris[3 * t]), b = find(tris[3 * t + e]);
+            if (a != b) root[std::max(a, b)] = std::min(a, b);
+        }
+    std::vector<int> island(nv), count;
+    for (int q = 0; q < nv; q++) {
+        const int r = find(q);
+        if (r == q) { island[q] = (int)count.size(); count.push_back(0); }
+        else island[q] = island[r];
+        count[island[q]]++;
+    }
+    const int ni = (int)count.size();
+    std::vector<std::vector<V>> iv(ni);
+    std::vector<std::vector<int>> it(ni);
+    std::vector<int> local(nv);
+    for (int q = 0; q < nv; q++) {
+        local[q] = (int)iv[island[q]].size();
+        iv[island[q]].push_back(vtx[q]);
+    }
+    for (int t = 0; t < ntri; t++) {
+        std::vector<int> &d = it[island[tris[3 * t]]];
+        for (int e = 0; e < 3; e++) d.push_back(local[tris[3 * t + e]]);
+    }
+    std::vector<V> inV;
+    std::vector<int> inT;
+    for (int g = 0; g < ni; g++) {
+        const std::vector<V> &v = iv[g];
+        float lo[3] = {v[0].x, v[0].y, v[0].z}, hi[3] = {v[0].x, v[0].y, v[0].z};
+        for (const V &p : v) {
+            lo[0] = std::min(lo[0], p.x); lo[1] = std::min(lo[1], p.y); lo[2] = std::min(lo[2], p.z);
+            hi[0] = std::max(hi[0], p.x); hi[1] = std::max(hi[1], p.y); hi[2] = std::max(hi[2], p.z);
+        }
+        // AABB of the island: float position, double extent; its max point in float
+        const V mn{lo[0], lo[1], lo[2]};
+        const V mx{(float)((double)lo[0] + ((double)hi[0] - lo[0])), (float)((double)lo[1] + ((double)hi[1] - lo[1])),
+                   (float)((double)lo[2] + ((double)hi[2] - lo[2]))};
+        if (in_box(mn) && in_box(mx)) {
+            const int base = (int)inV.size();
+            inV.insert(inV.end(), v.begin(), v.end());
+            for (int idx : it[g]) inT.push_back(base + idx);
+        } else {
+            // AABB::getIntersection with the grid's box (aabb.cpp:170-190)
+            const double bmax[3] = {W, H, D};
+            const float vmn[3] = {mn.x, mn.y, mn.z}, vmx[3] = {mx.x, mx.y, mx.z};
+            bool apart = false, some = false;
+            for (int a = 0; a < 3; a++) {
+                const float bx = (float)bmax[a];
+                if (vmn[a] > bx || vmx[a] < 0.0f) apart = true;
+                const double w = (double)std::min(vmx[a], bx) - (double)std::max(vmn[a], 0.0f);
+                some = some || w > 0.0;
+            }
+            if (!apart && some) inside_nodes_of(v, it[g], dx, mark);
+        }
+    }
+    if (!inV.empty()) inside_nodes_of(inV, inT, dx, mark);
+}
+
+// The level set of one mesh over a sub-grid of nI x nJ x nK nodes whose
+// first node sits at `origin` (float position): the exact band in the block
+// frame and the signs from the nodes inside (meshlevelset.cpp:572-601,
+// 781-1158, 1298-1316).  Vertices are already relative to `origin`.
+void mesh_level_set(const std::vector<V> &vtx, const std::vector<int> &tris, int nI, int nJ, int nK, double dx,
+                    int band, std::vector<float> &phi, std::vector<int> &tri) {
+    const float upper = (float)((double)(nI + nJ + nK) * dx);
+    auto nid = [&](int i, int j, int k) { return (size_t)i + (size_t)nI * ((size_t)j + (size_t)nJ * k); };
+    phi.assign((size_t)nI * nJ * nK, upper);
+    tri.assign(phi.size(), -1);
+    const int bw = 10;
+    const int ntri = (int)tris.size() / 3;
+    for (int t = 0; t < ntri; t++) {
+        const V a = vtx[tris[3 * t]], b = vtx[tris[3 * t + 1]], e = vtx[tris[3 * t + 2]];
+        // AABB of the triangle: float minimum, double extent (aabb.cpp:84-110)
+        const float mn[3] = {std::min(a.x, std::min(b.x, e.x)), std::min(a.y, std::min(b.y, e.y)), std::min(a.z, std::min(b.z, e.z))};
+        const double ext[3] = {(double)std::max(a.x, std::max(b.x, e.x)) - mn[0], (double)std::max(a.y, std::max(b.y, e.y)) - mn[1],
+                               (double)std::max(a.z, std::max(b.z, e.z)) - mn[2]};
+        int lo[3], hi[3];
+        const int n[3] = {nI, nJ, nK};
+        bool outside = false;
+        for (int q = 0; q < 3; q++) {
+            lo[q] = floor_index(mn[q], dx) - band;
+            hi[q] = floor_index(mn[q] + (float)ext[q], dx) + band + 1;
+            if (hi[q] < 0 || lo[q] >= n[q]) outside = true;
+            lo[q] = std::max(lo[q], 0);
+            hi[q] = std::min(hi[q], n[q] - 1);
+        }
+        if (outside) continue;
+        for (int k = lo[2]; k <= hi[2]; k++)
+            for (int j = lo[1]; j <= hi[1]; j++)
+                for (int i = lo[0]; i <= hi[0]; i++) {
+                    const V off{gpos(i / bw, (double)bw * dx), gpos(j / bw, (double)bw * dx), gpos(k / bw, (double)bw * dx)};
+                    const V g{gpos(i % bw, dx), gpos(j % bw, dx), gpos(k % bw, dx)};
+                    const float dist = vlen(vsub(closest_point(g, vsub(a, off), vsub(b, off), vsub(e, off)), g));
+                    const size_t id = nid(i, j, k);
+                    if (dist < phi[id]) {
+                        phi[id] = dist;
+                        tri[id] = t;
+                    }
+                }
+    }
+    std::vector<uint8_t> inside;
+    grid_nodes_inside(vtx, tris, nI, nJ, nK, dx, inside);
+    for (size_t q = 0; q < phi.size(); q++)
+        if (inside[q]) phi[q] = -phi[q];
 }
 
 }  // namespace
@@ -447,6 +541,38 @@ void DomainBox::compute(int I_, int J_, int K_, double dx_, double cfl, const st
                             near[cidx(q[0], q[1], q[2])] = 1;
                 }
     }
+}
+
+// The inputs of seeding a fluid mesh (_updateAddedFluidMeshObjectQueue,
+// fluidsimulation.cpp:4724-4759): the cells around the grid nodes inside the
+// mesh (MeshObject::getCells, meshobject.cpp:101-140; the eight cells that
+// share a node, grid3d.h getVertexGridIndexNeighbours) and the mesh's level
+// set over the whole grid's nodes, exact in a band of 3
+// (MeshLevelSet::fastCalculateSignedDistanceField, meshlevelset.cpp:572-601;
+// outside the band the upper bound, negated inside).
+void mesh_fluid_cells(int I, int J, int K, double dx, const std::vector<float> &verts, const std::vector<int> &tris,
+                      std::vector<int> &cells, std::vector<float> &phi) {
+    const int nv = (int)verts.size() / 3;
+    std::vector<V> wv(nv);
+    for (int v = 0; v < nv; v++) wv[v] = V{verts[3 * v], verts[3 * v + 1], verts[3 * v + 2]};
+    std::vector<uint8_t> nodes;
+    grid_nodes_inside(wv, tris, I + 1, J + 1, K + 1, dx, nodes);
+    std::vector<uint8_t> mark((size_t)I * J * K, 0);
+    for (int k = 0; k <= K; k++)
+        for (int j = 0; j <= J; j++)
+            for (int i = 0; i <= I; i++) {
+                if (!nodes[(size_t)i + (size_t)(I + 1) * ((size_t)j + (size_t)(J + 1) * k)]) continue;
+                for (int c = k - 1; c <= k; c++)
+                    for (int b = j - 1; b <= j; b++)
+                        for (int a = i - 1; a <= i; a++)
+                            if (a >= 0 && b >= 0 && c >= 0 && a < I && b < J && c < K)
+                                mark[(size_t)a + (size_t)I * ((size_t)b + (size_t)J * c)] = 1;
+            }
+    cells.clear();
+    for (size_t q = 0; q < mark.size(); q++)
+        if (mark[q]) cells.push_back((int)q);
+    std::vector<int> tri;
+    mesh_level_set(wv, tris, I + 1, J + 1, K + 1, dx, 3, phi, tri);
 }
 
 }  // namespace flip

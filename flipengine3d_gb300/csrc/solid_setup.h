@@ -39,4 +39,10 @@ struct DomainBox {
     void compute(int I, int J, int K, double dx, double cfl, const std::vector<MeshObstacle> &obstacles = {});
 };
 
+// A fluid mesh's seeding inputs (addMeshFluid): the cells of the grid nodes
+// inside the mesh, ascending flat index, and its (I+1)(J+1)(K+1) nodal level
+// set, negative inside.
+void mesh_fluid_cells(int I, int J, int K, double dx, const std::vector<float> &verts, const std::vector<int> &tris,
+                      std::vector<int> &cells, std::vector<float> &phi);
+
 }  // namespace flip

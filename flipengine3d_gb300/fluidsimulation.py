@@ -93,6 +93,12 @@ SIGNATURES = {
     "flip_get_face_weights": [_P, _P, _P, _P],
     "flip_compute_domain_solid": [_I, _I, _I, _D, _I, _P, _P, _P, _P, _P, _P],
     "flip_add_mesh_obstacle": [_P, _I, _P, _I, _P, C.c_float],
+    "flip_add_mesh_fluid": [_P, _I, _P, _I, _P, _D, _D, _D],
+    "flip_set_marker_particle_jitter_factor": [_P, _D],
+    "flip_get_marker_particle_jitter_factor": [_P, C.POINTER(C.c_double)],
+    "flip_set_jitter_surface_marker_particles": [_P, _I],
+    "flip_is_jitter_surface_marker_particles_enabled": [_P, C.POINTER(C.c_int)],
+    "flip_mesh_fluid_cells": [_I, _I, _I, _D, _I, _P, _I, _P, C.POINTER(C.c_int), _P, _P],
     "flip_compute_solid": [_I, _I, _I, _D, _I, _I] + [_P] * 5 + [_P] * 9,
     "flip_set_stage_timing": [_P, _I],
     "flip_get_stage_times": [_P, _P, C.POINTER(C.c_longlong)],
@@ -185,6 +191,21 @@ def _obstacle_arrays(obstacles):
                                 if obstacles else np.zeros((0, 3), np.int32), np.int32)
     fr = np.array([float(o[2]) if len(o) > 2 else 0.0 for o in obstacles], np.float32)
     return len(obstacles), nv, verts, nt, tris, fr
+
+
+def mesh_fluid_cells(isize, jsize, ksize, dx, vertices, triangles):
+    """Seeding inputs of a fluid mesh (no device needed): the flat indices of
+    the cells around grid nodes inside the mesh (MeshObject::getCells), and
+    the mesh's nodal level set (k+1, j+1, i+1), negative inside."""
+    lib = load_library()
+    v = np.ascontiguousarray(vertices, np.float32).reshape(-1, 3)
+    t = np.ascontiguousarray(triangles, np.int32).reshape(-1, 3)
+    n = C.c_int()
+    cells = np.zeros(isize * jsize * ksize, np.int32)
+    phi = np.zeros((ksize + 1, jsize + 1, isize + 1), np.float32)
+    _check(lib, lib.flip_mesh_fluid_cells(isize, jsize, ksize, dx, v.shape[0], _ptr(v), t.shape[0], _ptr(t),
+                                          C.byref(n), _ptr(cells), _ptr(phi)))
+    return cells[:n.value].copy(), phi
 
 
 def compute_solid(isize, jsize, ksize, dx, cfl=5, obstacles=()):
@@ -386,6 +407,35 @@ class FluidSimulation:
         t = np.ascontiguousarray(triangles, np.int32).reshape(-1, 3)
         self._c(self._lib.flip_add_mesh_obstacle(self._h, v.shape[0], _ptr(v), t.shape[0], _ptr(t),
                                                  float(friction)))
+
+    def addMeshFluid(self, vertices, triangles, velocity=(0.0, 0.0, 0.0)):
+        """addMeshFluid (fluidsimulation.cpp:2038-2047): a static mesh,
+        vertices (m, 3) and triangles (t, 3), filled with marker particles
+        moving at `velocity` at the end of the next substep; copied on the
+        call."""
+        v = np.ascontiguousarray(vertices, np.float32).reshape(-1, 3)
+        t = np.ascontiguousarray(triangles, np.int32).reshape(-1, 3)
+        vx, vy, vz = (float(a) for a in velocity)
+        self._c(self._lib.flip_add_mesh_fluid(self._h, v.shape[0], _ptr(v), t.shape[0], _ptr(t), vx, vy, vz))
+
+    def setMarkerParticleJitterFactor(self, jitter: float):
+        self._c(self._lib.flip_set_marker_particle_jitter_factor(self._h, float(jitter)))
+
+    def getMarkerParticleJitterFactor(self) -> float:
+        v = C.c_double()
+        self._c(self._lib.flip_get_marker_particle_jitter_factor(self._h, C.byref(v)))
+        return v.value
+
+    def enableJitterSurfaceMarkerParticles(self):
+        self._c(self._lib.flip_set_jitter_surface_marker_particles(self._h, 1))
+
+    def disableJitterSurfaceMarkerParticles(self):
+        self._c(self._lib.flip_set_jitter_surface_marker_particles(self._h, 0))
+
+    def isJitterSurfaceMarkerParticlesEnabled(self) -> bool:
+        v = C.c_int()
+        self._c(self._lib.flip_is_jitter_surface_marker_particles_enabled(self._h, C.byref(v)))
+        return bool(v.value)
 
     def loadMarkerParticleData(self, positions, velocities):
         pos = np.ascontiguousarray(positions, dtype=np.float32).reshape(-1, 3)
@@ -594,6 +644,11 @@ class FluidSimulation:
         sim.setPressureSolveTolerance(scene.tolerance if tolerance is None else tolerance)
         for ob in getattr(scene, "obstacles", ()):
             sim.addMeshObstacle(*ob)
-        sim.loadMarkerParticleData(scene.positions, scene.velocities)
+        if getattr(scene, "jitter_factor", None) is not None:
+            sim.setMarkerParticleJitterFactor(scene.jitter_factor)
+        for fm in getattr(scene, "fluid_meshes", []):
+            sim.addMeshFluid(*fm)
+        if len(scene.positions):
+            sim.loadMarkerParticleData(scene.positions, scene.velocities)
         sim.initialize()
         return sim

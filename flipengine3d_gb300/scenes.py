@@ -33,6 +33,9 @@ class Scene:
     meta: dict = field(default_factory=dict)
     # static mesh obstacles: (vertices (m, 3) float32, triangles (t, 3) int32, friction)
     obstacles: list = field(default_factory=list)
+    # fluid meshes added with addMeshFluid: (vertices, triangles, velocity xyz)
+    fluid_meshes: list = field(default_factory=list)
+    jitter_factor: float | None = None   # setMarkerParticleJitterFactor, when set
 
     @property
     def num_particles(self) -> int:
@@ -160,6 +163,54 @@ def dam_with_obstacles(n: int = 24, *, seed: int = 0, which: str = "box", **kw) 
     else:
         raise ValueError(which)
     sc.name += f"+{which}"
+    return sc
+
+
+def fluid_manager_box(n: int = 32, dx: float = 0.125):
+    """The fluid box FluidManager::initialize adds (src/FluidManager.cpp:
+    47-68): a third of the domain on each axis, centred; vertices and
+    triangles as its getTriangleMeshFromAABB (:20-44)."""
+    x = y = z = n * dx
+    w, h, d = x / 3.0, y / 3.0, z / 3.0
+    p = np.array([0.5 * (x - w), 0.5 * (y - h), 0.5 * (z - d)], np.float32).astype(np.float64)
+    # float position plus double extent, rounded to float (vmath::vec3)
+    v = np.array([[p[0], p[1], p[2]], [p[0] + w, p[1], p[2]], [p[0] + w, p[1], p[2] + d], [p[0], p[1], p[2] + d],
+                  [p[0], p[1] + h, p[2]], [p[0] + w, p[1] + h, p[2]], [p[0] + w, p[1] + h, p[2] + d],
+                  [p[0], p[1] + h, p[2] + d]], np.float64).astype(np.float32)
+    t = np.array([[0, 1, 2], [0, 2, 3], [4, 7, 6], [4, 6, 5], [0, 3, 7], [0, 7, 4],
+                  [1, 5, 6], [1, 6, 2], [0, 4, 5], [0, 5, 1], [3, 2, 6], [3, 6, 7]], np.int32)
+    return v, t
+
+
+def mesh_fluid(n: int = 32, *, which: str = "box", dx: float = 0.125, jitter_factor: float | None = 0.001,
+               steps: int = 3, seed: int = 0) -> Scene:
+    """Fluid added as meshes, the way FluidManager sets up its scene: an
+    n^3 grid (FluidManager's demo: 30^3, dx 0.125, 1/30 s frames, gravity
+    -25), fluid from addMeshFluid, no loaded particles.
+
+    `box`: FluidManager's box (a third of the domain, centred; with n = 32 its
+    faces lie off the grid nodes).  `both`: that box, a moving icosphere of
+    fluid, and a loaded block of particles overlapping the sphere, so that
+    seeding skips the sub-cells the loaded particles hold.  `jitter_factor`
+    0.001 makes the seeding jitter exactly zero; None keeps the reference's
+    default (0: jitter of up to 0.00025 dx)."""
+    v, t = fluid_manager_box(n, dx)
+    pos = np.zeros((0, 3), np.float32)
+    vel = np.zeros((0, 3), np.float32)
+    meshes = [(v, t, (0.0, 0.0, 0.0))]
+    if which == "both":
+        L = n * dx
+        sv, st = icosphere_mesh((0.71 * L, 0.62 * L, 0.43 * L), 0.17 * L, subdivisions=2)
+        meshes.append((sv, st, (-0.5, -1.0, 0.25)))
+        rng = np.random.default_rng(seed)
+        cells = _box_cells(n, n, n, dx, (0.6 * L, 0.55 * L, 0.3 * L), (0.8 * L, 0.7 * L, 0.5 * L))
+        pos = _jittered_cells(cells, dx, rng, 8)
+        vel = np.zeros_like(pos)
+        vel[:, 0] = 0.3
+    elif which != "box":
+        raise ValueError(which)
+    sc = Scene(n, n, n, dx, pos, vel, gravity=(0.0, -25.0, 0.0), frame_dt=1.0 / 30.0, tolerance=1e-9,
+               steps=steps, name=f"mesh_fluid_{which}_{n}", fluid_meshes=meshes, jitter_factor=jitter_factor)
     return sc
 
 

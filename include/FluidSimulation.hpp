@@ -63,6 +63,13 @@ struct TriangleMesh {
     std::vector<int> triangles;
 };
 
+// vmath::vec3 as addMeshFluid takes it (float components)
+struct vec3 {
+    float x = 0.0f, y = 0.0f, z = 0.0f;
+    vec3() = default;
+    vec3(double a, double b, double c) : x((float)a), y((float)b), z((float)c) {}
+};
+
 // A static obstacle mesh: the part of the reference's MeshObject
 // (meshobject.h, meshobject.cpp:32-59, 301-309) that addMeshObstacle uses.
 // The caller keeps it alive while the simulation uses it, as with the
@@ -86,12 +93,23 @@ private:
 
 class FluidSimulation {
 public:
-    FluidSimulation(int isize, int jsize, int ksize, double dx) { check(flip_create(isize, jsize, ksize, dx, &ctx_)); }
+    FluidSimulation(int isize, int jsize, int ksize, double dx) : isize_(isize), jsize_(jsize), ksize_(ksize), dx_(dx) {
+        check(flip_create(isize, jsize, ksize, dx, &ctx_));
+    }
     ~FluidSimulation() { flip_destroy(ctx_); }
     FluidSimulation(const FluidSimulation &) = delete;
     FluidSimulation &operator=(const FluidSimulation &) = delete;
 
     void initialize() { check(flip_initialize(ctx_)); }
+    // getGridDimensions / getCellSize / getSimulationDimensions
+    // (fluidsimulation.cpp:109-133)
+    void getGridDimensions(int *i, int *j, int *k) const { *i = isize_; *j = jsize_; *k = ksize_; }
+    double getCellSize() const { return dx_; }
+    void getSimulationDimensions(double *w, double *h, double *d) const {
+        *w = (double)isize_ * dx_;
+        *h = (double)jsize_ * dx_;
+        *d = (double)ksize_ * dx_;
+    }
     bool isInitialized() {
         int v = 0;
         check(flip_is_initialized(ctx_, &v));
@@ -129,6 +147,28 @@ public:
         check(flip_add_mesh_obstacle(ctx_, (int)(m.vertices.size() / 3), m.vertices.data(),
                                      (int)(m.triangles.size() / 3), m.triangles.data(), obstacle->getFriction()));
         obstacles_.push_back(obstacle);
+    }
+
+    // addMeshFluid (fluidsimulation.cpp:2038-2047): the mesh is copied and
+    // filled with marker particles at the end of the next substep.
+    void addMeshFluid(const MeshObject &fluid) { addMeshFluid(fluid, vec3(0.0, 0.0, 0.0)); }
+    void addMeshFluid(const MeshObject &fluid, vec3 velocity) {
+        const TriangleMesh &m = fluid.getMesh();
+        check(flip_add_mesh_fluid(ctx_, (int)(m.vertices.size() / 3), m.vertices.data(), (int)(m.triangles.size() / 3),
+                                  m.triangles.data(), velocity.x, velocity.y, velocity.z));
+    }
+    void setMarkerParticleJitterFactor(double jit) { check(flip_set_marker_particle_jitter_factor(ctx_, jit)); }
+    double getMarkerParticleJitterFactor() {
+        double v = 0.0;
+        check(flip_get_marker_particle_jitter_factor(ctx_, &v));
+        return v;
+    }
+    void enableJitterSurfaceMarkerParticles() { check(flip_set_jitter_surface_marker_particles(ctx_, 1)); }
+    void disableJitterSurfaceMarkerParticles() { check(flip_set_jitter_surface_marker_particles(ctx_, 0)); }
+    bool isJitterSurfaceMarkerParticlesEnabled() {
+        int v = 0;
+        check(flip_is_jitter_surface_marker_particles_enabled(ctx_, &v));
+        return v != 0;
     }
 
     void loadMarkerParticleData(FluidSimulationMarkerParticleData data) {
@@ -171,6 +211,8 @@ public:
     flip_ctx *handle() { return ctx_; }
 
 private:
+    int isize_, jsize_, ksize_;
+    double dx_;
     flip_ctx *ctx_ = nullptr;
     TriangleMesh mesh_;
     std::vector<MeshObject *> obstacles_;

@@ -174,6 +174,40 @@ int flip_get_face_weights(flip_ctx *ctx, float *wu, float *wv, float *ww);
 int flip_add_mesh_obstacle(flip_ctx *ctx, int nverts, const float *verts, int ntris, const int *tris,
                            float friction);
 
+/* addMeshFluid(MeshObject, vec3 velocity) (fluidsimulation.cpp:2038-2047):
+ * queue a static triangle mesh (arrays as flip_add_mesh_obstacle) to be
+ * filled with marker particles moving at (vx, vy, vz), copied on the call.
+ * The queue is filled at the end of the next substep
+ * (_updateAddedFluidMeshObjectQueue, :4724-4759): every cell around a grid
+ * node inside the mesh gets a particle at the centre of each of its eight
+ * sub-cells where the mesh's level set is <= 0 and the solid level set is
+ * positive, unless a particle already holds that sub-cell; particles deeper
+ * than one cell (all of them with surface jitter on) are jittered by up to
+ * 0.25 (jitter factor - 0.001) dx per axis.  On frame 0 the first substep's
+ * length uses the queued meshes' speeds (_predictMaximumMarkerParticleSpeed,
+ * :5529-5550).  The reference draws the jitter from rand(); here it is a
+ * counter-based hash, so runs repeat; at jitter factor 0.001 it is zero and
+ * the particles are the reference's.  FLIP_E_DOMAIN for a bad index, count,
+ * vertex or velocity. */
+int flip_add_mesh_fluid(flip_ctx *ctx, int nverts, const float *verts, int ntris, const int *tris, double vx,
+                        double vy, double vz);
+/* setMarkerParticleJitterFactor / getMarkerParticleJitterFactor
+ * (fluidsimulation.cpp:180-195; >= 0, default 0) and
+ * enable/disableJitterSurfaceMarkerParticles (:197-210; default off). */
+int flip_set_marker_particle_jitter_factor(flip_ctx *ctx, double jitter);
+int flip_get_marker_particle_jitter_factor(flip_ctx *ctx, double *jitter);
+int flip_set_jitter_surface_marker_particles(flip_ctx *ctx, int enable);
+int flip_is_jitter_surface_marker_particles_enabled(flip_ctx *ctx, int *enabled);
+
+/* The seeding inputs of one fluid mesh, without a device: the cells around
+ * the grid nodes inside the mesh (MeshObject::getCells, meshobject.cpp:
+ * 101-140), ascending flat index i + I (j + J k), and the mesh's level set on
+ * the (I+1)*(J+1)*(K+1) nodes (exact within 3 cells, negative inside;
+ * MeshLevelSet::fastCalculateSignedDistanceField, meshlevelset.cpp:572-601).
+ * cells holds up to I*J*K entries; cells and phi may be NULL. */
+int flip_mesh_fluid_cells(int isize, int jsize, int ksize, double dx, int nverts, const float *verts, int ntris,
+                          const int *tris, int *ncells, int *cells, float *phi);
+
 /* The solid set-up of the first step with static mesh obstacles, without a
  * device: nodal solid level set, fluid face weights, near-solid grid (as in
  * flip_compute_domain_solid) and the face friction of the constrain step

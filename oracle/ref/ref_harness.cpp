@@ -454,6 +454,55 @@ int ref_mic0_precondition_f32(int I, int J, int K, const uint8_t *fluid, const f
 }
 
 
+static TriangleMesh mesh_from_arrays(int nverts, const float *verts, int ntris, const int *tris) {
+    TriangleMesh m;
+    for (int v = 0; v < nverts; v++) m.vertices.push_back(vmath::vec3(verts[3 * v], verts[3 * v + 1], verts[3 * v + 2]));
+    for (int t = 0; t < ntris; t++) {
+        Triangle tri;
+        tri.tri[0] = tris[3 * t];
+        tri.tri[1] = tris[3 * t + 1];
+        tri.tri[2] = tris[3 * t + 2];
+        m.triangles.push_back(tri);
+    }
+    return m;
+}
+
+// addMeshFluid(MeshObject, vec3) with a static MeshObject built from plain
+// arrays (fluidsimulation.cpp:2038-2047); the queue copies the object.
+void ref_add_mesh_fluid(void *h, int nverts, const float *verts, int ntris, const int *tris, double vx, double vy,
+                        double vz) {
+    RefSim *r = (RefSim *)h;
+    int I, J, K;
+    r->sim->getGridDimensions(&I, &J, &K);
+    MeshObject o(I, J, K, r->sim->getCellSize());
+    o.updateMeshStatic(mesh_from_arrays(nverts, verts, ntris, tris));
+    r->sim->addMeshFluid(o, vmath::vec3(vx, vy, vz));
+}
+void ref_set_jitter_factor(void *h, double f) { ((RefSim *)h)->sim->setMarkerParticleJitterFactor(f); }
+
+// The seeding inputs of one fluid mesh: MeshObject::getCells
+// (meshobject.cpp:101-140) as flat indices, and the mesh's level set as
+// _updateAddedFluidMeshObjectQueue computes it (fluidsimulation.cpp:
+// 4731-4750: MeshLevelSet over the grid, exact band 3).  rand() is reseeded
+// as at the start of a process (the ray jitter draws from it).
+void ref_mesh_fluid_cells(int I, int J, int K, double dx, int nverts, const float *verts, int ntris, const int *tris,
+                          int *ncells, int *cells, float *phi) {
+    std::srand(1);
+    TriangleMesh m = mesh_from_arrays(nverts, verts, ntris, tris);
+    MeshObject o(I, J, K, dx);
+    o.updateMeshStatic(m);
+    std::vector<GridIndex> cs;
+    o.getCells(cs);
+    *ncells = (int)cs.size();
+    if (cells)
+        for (size_t q = 0; q < cs.size(); q++) cells[q] = cs[q].i + I * (cs[q].j + J * cs[q].k);
+    MeshLevelSet sdf(I, J, K, dx);
+    sdf.disableVelocityData();
+    TriangleMesh mm = o.getMesh();
+    sdf.fastCalculateSignedDistanceField(mm, 3);
+    if (phi) copyArray(sdf._phi, phi);
+}
+
 // addMeshObstacle with a static MeshObject built from plain arrays
 // (fluidsimulation.cpp:1994-2008, meshobject.cpp:50-59, 301-309).
 void ref_add_mesh_obstacle(void *h, int nverts, const float *verts, int ntris, const int *tris, float friction) {

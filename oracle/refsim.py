@@ -72,6 +72,14 @@ def lib(prefix: str = "ref"):
             L.ref_add_mesh_obstacle.restype = None
             L.ref_get_node_friction.argtypes = [C.c_void_p, C.c_void_p]
             L.ref_get_node_friction.restype = None
+            L.ref_add_mesh_fluid.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_double,
+                                             C.c_double, C.c_double]
+            L.ref_add_mesh_fluid.restype = None
+            L.ref_set_jitter_factor.argtypes = [C.c_void_p, C.c_double]
+            L.ref_set_jitter_factor.restype = None
+            L.ref_mesh_fluid_cells.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, C.c_int, C.c_void_p, C.c_int,
+                                               C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+            L.ref_mesh_fluid_cells.restype = None
         L.ref_num_particles.argtypes = [C.c_void_p]
         L.ref_num_particles.restype = C.c_int
         L.ref_frame_substeps.argtypes = [C.c_void_p]
@@ -141,6 +149,20 @@ def _hash_uniform(seed, stream, shape):
         x = (x ^ (x >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
         x = x ^ (x >> np.uint64(31))
     return ((x >> np.uint64(11)).astype(np.float64) * (1.0 / (1 << 53))).reshape(shape)
+
+
+def mesh_fluid_cells(isize, jsize, ksize, dx, vertices, triangles):
+    """The reference's seeding inputs of a fluid mesh (ref_mesh_fluid_cells):
+    flat cell indices of MeshObject::getCells and the mesh's nodal level set
+    (k+1, j+1, i+1)."""
+    L = lib("ref")
+    v = np.ascontiguousarray(vertices, np.float32).reshape(-1, 3)
+    t = np.ascontiguousarray(triangles, np.int32).reshape(-1, 3)
+    n = C.c_int()
+    cells = np.zeros(isize * jsize * ksize, np.int32)
+    phi = np.zeros((ksize + 1, jsize + 1, isize + 1), np.float32)
+    L.ref_mesh_fluid_cells(isize, jsize, ksize, dx, len(v), _p(v), len(t), _p(t), C.byref(n), _p(cells), _p(phi))
+    return cells[:n.value].copy(), phi
 
 
 def random_mic0_system(shape, seed, weak_fraction=0.05, null_rows=2):
@@ -222,9 +244,16 @@ class RefSimulation:
 
     def setup(self, scene, tolerance=None):
         obstacles = getattr(scene, "obstacles", [])
-        if obstacles and self.PREFIX != "ref":
-            raise NotImplementedError("the oracle port restates the domain walls only; obstacle scenes are "
-                                      "pinned by fixtures from the reference")
+        fluids = getattr(scene, "fluid_meshes", [])
+        if (obstacles or fluids) and self.PREFIX != "ref":
+            raise NotImplementedError("the oracle port restates the domain walls and loaded particles only; "
+                                      "obstacle and fluid-mesh scenes are pinned by fixtures from the reference")
+        if getattr(scene, "jitter_factor", None) is not None:
+            self.L.ref_set_jitter_factor(self.h, float(scene.jitter_factor))
+        for v, t, vel in fluids:
+            v = np.ascontiguousarray(v, np.float32)
+            t = np.ascontiguousarray(t, np.int32)
+            self.L.ref_add_mesh_fluid(self.h, len(v), _p(v), len(t), _p(t), *(float(a) for a in vel))
         for v, t, fr in obstacles:
             v = np.ascontiguousarray(v, np.float32)
             t = np.ascontiguousarray(t, np.int32)

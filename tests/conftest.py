@@ -55,8 +55,13 @@ def gpu(built):
     return True
 
 
-def golden_cases():
-    return sorted(p.stem for p in GOLDEN.glob("*.npz"))
+def golden_cases(stages=False):
+    """Fixture names; with stages, only those holding the first frame stage
+    by stage (the fluid-mesh fixtures hold the particles after each frame)."""
+    names = sorted(p.stem for p in GOLDEN.glob("*.npz"))
+    if stages:
+        names = [n for n in names if json.loads(str(np.load(GOLDEN / f"{n}.npz")["meta"])).get("builder") != "mesh_fluid"]
+    return names
 
 
 def golden_scene(meta):

@@ -37,6 +37,13 @@ OBSTACLE_CASES = {
     "dam20_sphere": (dict(n=20, seed=5, which="sphere"), 3, 1, 1e-9),
     "dam20_both": (dict(n=20, seed=7, which="both"), 2, 1, 1e-9),
 }
+# fluid added with addMeshFluid (scenes.mesh_fluid): the particles after
+# every frame (the first frame seeds them at the end of its first substep)
+MESH_FLUID_CASES = {
+    "mf32_box": (dict(n=32, which="box"), 3, 4),
+    "mf32_both": (dict(n=32, which="both"), 3, 4),
+    "mf32_box_jitter": (dict(n=32, which="box", jitter_factor=None), 1, 4),
+}
 STAGE_KEYS = ("phi", "vu_p2g", "vv_p2g", "vw_p2g", "u_p2g", "v_p2g", "w_p2g", "pressure", "u_final", "v_final",
               "w_final", "vel_g2p", "pos_adv")
 
@@ -65,6 +72,21 @@ def make(name, kwargs, frames, threads, tol, builder="dam_break"):
           f"{(OUT / f'{name}.npz').stat().st_size / 1024:.0f} KB")
 
 
+def make_mesh_fluid(name, kwargs, frames, threads):
+    sc = scenes.mesh_fluid(**kwargs)
+    ref = RefSimulation(sc.isize, sc.jsize, sc.ksize, sc.dx, threads=threads).setup(sc)
+    data = {}
+    for f in range(1, frames + 1):
+        ref.update(sc.frame_dt)
+        data[f"positions_{f}"], data[f"velocities_{f}"] = ref.particles()
+    meta = dict(scene=kwargs, builder="mesh_fluid", frames=frames, threads=threads, tolerance=sc.tolerance,
+                dt=sc.frame_dt, gravity=list(sc.gravity), pic_ratio=sc.pic_ratio, cfl=sc.cfl,
+                loaded=int(sc.num_particles), source="jklae/FLIPEngine3D src/engine via oracle/build_ref.sh")
+    np.savez_compressed(OUT / f"{name}.npz", meta=np.array(json.dumps(meta)), **data)
+    print(name, "loaded", sc.num_particles, "->", [data[f"positions_{f}"].shape[0] for f in range(1, frames + 1)],
+          f"{(OUT / f'{name}.npz').stat().st_size / 1024:.0f} KB")
+
+
 if __name__ == "__main__":
     only = set(sys.argv[1:])   # names to (re)generate; all by default
     for name, (kw, frames, thr, tol) in CASES.items():
@@ -73,3 +95,6 @@ if __name__ == "__main__":
     for name, (kw, frames, thr, tol) in OBSTACLE_CASES.items():
         if not only or name in only:
             make(name, kw, frames, thr, tol, builder="dam_with_obstacles")
+    for name, (kw, frames, thr) in MESH_FLUID_CASES.items():
+        if not only or name in only:
+            make_mesh_fluid(name, kw, frames, thr)

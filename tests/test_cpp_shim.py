@@ -175,3 +175,79 @@ def test_cpp_drop_in_with_a_mesh_obstacle_matches_the_reference(gpu, tmp_path):
     pos = _run_driver(tmp_path, golden_scene(meta))
     assert pos.shape == g["positions_3"].shape
     assert rel_err(pos, g["positions_3"]) <= 1e-4
+
+
+MESH_FLUID_DRIVER = r"""
+// FluidManager::initialize (src/FluidManager.cpp:47-68) verbatim in its
+// calls, on a 32^3 grid of dx 0.125 with the jitter factor at 0.001 (the
+// seeding jitter exactly zero), then three 1/30 s frames.
+#include <cstdio>
+#include <vector>
+#include "FluidSimulation.hpp"
+
+int main(int argc, char **argv) {
+    const int isize = 32, jsize = 32, ksize = 32;
+    const double dx = 0.125;
+    flip3d::FluidSimulation fluidsim(isize, jsize, ksize, dx);
+    double x, y, z;
+    fluidsim.getSimulationDimensions(&x, &y, &z);
+    double boxWidth = (1.0 / 3.0) * x, boxHeight = (1.0 / 3.0) * y, boxDepth = (1.0 / 3.0) * z;
+    flip3d::vec3 p(0.5 * (x - boxWidth), 0.5 * (y - boxHeight), 0.5 * (z - boxDepth));
+    // getTriangleMeshFromAABB (src/FluidManager.cpp:20-44)
+    flip3d::TriangleMesh boxMesh;
+    boxMesh.vertices = {p.x, p.y, p.z,
+                        (float)(p.x + boxWidth), p.y, p.z,
+                        (float)(p.x + boxWidth), p.y, (float)(p.z + boxDepth),
+                        p.x, p.y, (float)(p.z + boxDepth),
+                        p.x, (float)(p.y + boxHeight), p.z,
+                        (float)(p.x + boxWidth), (float)(p.y + boxHeight), p.z,
+                        (float)(p.x + boxWidth), (float)(p.y + boxHeight), (float)(p.z + boxDepth),
+                        p.x, (float)(p.y + boxHeight), (float)(p.z + boxDepth)};
+    boxMesh.triangles = {0, 1, 2, 0, 2, 3, 4, 7, 6, 4, 6, 5, 0, 3, 7, 0, 7, 4,
+                         1, 5, 6, 1, 6, 2, 0, 4, 5, 0, 5, 1, 3, 2, 6, 3, 6, 7};
+    flip3d::MeshObject boxFluidObject(isize, jsize, ksize, dx);
+    boxFluidObject.updateMeshStatic(boxMesh);
+    fluidsim.setMarkerParticleJitterFactor(0.001);
+    fluidsim.addMeshFluid(boxFluidObject);
+    fluidsim.addBodyForce(0.0, -25.0, 0.0);
+    fluidsim.initialize();
+    for (int f = 0; f < 3; f++) fluidsim.update(1.0 / 30.0);
+    unsigned int m = fluidsim.getNumMarkerParticles();
+    std::vector<char> buf(12 * (size_t)m);
+    fluidsim.getMarkerParticlePositionData(buf.data());
+    std::FILE *out = std::fopen(argv[1], "wb");
+    std::fwrite(&m, 4, 1, out);
+    std::fwrite(buf.data(), 1, buf.size(), out);
+    std::fclose(out);
+    std::printf("%d %u\n", fluidsim.getCurrentFrame(), m);
+    return 0;
+}
+"""
+
+
+@pytest.mark.gpu
+def test_cpp_fluid_manager_initialize_matches_reference(gpu, tmp_path):
+    """FluidManager's own set-up through the C++ face: addMeshFluid of its
+    centred box, gravity -25, three 1/30 s frames; the particles are the
+    reference engine's (fixture mf32_box) within 1e-4."""
+    import numpy as np
+    from conftest import load_golden, rel_err
+    gxx = shutil.which("g++")
+    if not gxx:
+        pytest.skip("g++ not available")
+    src = tmp_path / "fm.cpp"
+    src.write_text(MESH_FLUID_DRIVER)
+    exe = tmp_path / "fm"
+    libdir = build.library_path().parent
+    subprocess.run([gxx, "-std=c++17", "-O2", "-I", str(ROOT / "include"), str(src), "-o", str(exe),
+                    "-L", str(libdir), "-lflip3d_gb300", f"-Wl,-rpath,{libdir}"], check=True)
+    out = tmp_path / "positions.bin"
+    r = subprocess.run([str(exe), str(out)], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, (r.stdout, r.stderr)
+    frame, m = (int(v) for v in r.stdout.split())
+    assert frame == 3
+    pos = np.fromfile(out, dtype=np.float32, offset=4).reshape(-1, 3)
+    meta, g = load_golden("mf32_box")
+    assert meta["scene"] == {"n": 32, "which": "box"}
+    assert pos.shape == g["positions_3"].shape == (m, 3)
+    assert rel_err(pos, g["positions_3"]) <= 1e-4

@@ -33,7 +33,7 @@ def check_first_frame(st, ref, label):
     assert rel_err(st["pos_adv"], ref["pos_adv"]) <= RTOL, f"{label}: advected positions"
 
 
-@pytest.mark.parametrize("case", golden_cases())
+@pytest.mark.parametrize("case", golden_cases(stages=True))
 def test_first_frame_matches_reference_golden(gpu, case):
     meta, g = load_golden(case)
     sc = golden_scene(meta)   # with static mesh obstacles for the obstacle fixtures
