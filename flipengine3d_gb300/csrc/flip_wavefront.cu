@@ -33,12 +33,13 @@
 // to global memory (a warp writes 128 contiguous bytes per step); cells
 // outside the grid read zero rows, so a step is unpredicated.
 //
-// The sweep is bound by how many operand bytes a tile keeps in flight: with
-// the compute loop stripped of every barrier, shuffle and shared-memory
-// exchange a one-tile sweep ran as long as with them, and with results
-// staged through shared memory (a bulk store per chunk, four slots) or
-// operands loaded into registers one chunk ahead, a tile was limited by the
-// latency of refilling its few chunks in flight.
+// Where a tile's time goes (one tile of 128 cells along i, measured): about
+// 5 us per launch plus 115 ns per step.  Stripping the compute loop of every
+// barrier, shuffle and shared-memory exchange leaves 96 ns per step; loading
+// the operands into registers 8-24 steps ahead instead of through the ring,
+// splitting the bulk copies per step, more or fewer slots, and suspending
+// waiting warps instead of polling did not shorten it; 16-step chunks gave
+// 96 ns, 4-step chunks 141 ns.
 //
 // Tile edges.  The threads on a tile's downstream edges publish each term
 // they form as one 64-bit word {sweep epoch, value}, indexed by step, in an
@@ -233,15 +234,17 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_wavefront(SweepArgs a) {
 
     if (warp == LOADER) {
         // ================================================== loader warp
-        if ((threadIdx.x & 31) != 0) return;
+        const int lane = threadIdx.x & 31;
+        if (lane != 0) return;
         auto issue = [&](int m, int b) {   // operands of chunk m into slot b
             Slot &sl = sm.slot[b];
             const int tb = tlo + m * CH, rows = chunk_rows(m);
             const unsigned bl = (unsigned)(rows * NP * sizeof(float4)), br = (unsigned)(rows * NP * sizeof(float));
             const size_t e0 = tileBase + (size_t)chunk_tf0(tb, rows) * NP;
+            const int r0 = chunk_row0(rows);
             mb_arrive_expect_tx(&sm.loaded[b], bl + br);
-            bulk_load(&sl.L[chunk_row0(rows)][0], a.L + e0, bl, &sm.loaded[b]);
-            bulk_load(&sl.r[chunk_row0(rows)][0], a.rin + e0, br, &sm.loaded[b]);
+            bulk_load(&sl.L[r0][0], a.L + e0, bl, &sm.loaded[b]);
+            bulk_load(&sl.r[r0][0], a.rin + e0, br, &sm.loaded[b]);
         };
         auto prefetch = [&](int m) {   // chunk m into L2, for its copy one ring later
             if (m >= nChunks) return;
@@ -277,41 +280,82 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_wavefront(SweepArgs a) {
         const int2 rgJ = srcJ >= 0 ? steps_of(srcJ) : make_int2(1, 0);
         const int2 rgK = srcK >= 0 ? steps_of(srcK) : make_int2(1, 0);
         const int laneJ = FWD ? 0 : TJ - 1, warpK = FWD ? 0 : TK - 1;
-        const unsigned long long *srcJw = a.xchg + (srcJ >= 0 ? srcJ : 0) * wordsPerTile;
-        const unsigned long long *srcKw = a.xchg + (srcK >= 0 ? srcK : 0) * wordsPerTile + (size_t)T * TK;
+        // Each lane's words: for the k edge, the one of its own lane of the
+        // upstream tile's edge warp at each step; for the j edge, JQ (step,
+        // warp) pairs of each chunk.  A word is needed at step te when the
+        // consumer cell is interior (te in [base, base + NI - 1]) and the
+        // producer tile computes its cell (te + skew in the producer's
+        // range): a window of steps fixed per lane, computed once.
+        auto base_of = [&](int lr, int ww) {
+            return FWD ? SL * lr + SW * ww : SL * (TJ - 1 - lr) + SW * (TK - 1 - ww);
+        };
+        int kLo = 1, kHi = 0;
+        if (srcK >= 0 && pencil_in(lane, warpK)) {
+            const int bs = base_of(lane, warpK);
+            kLo = max(bs, rgK.x - SW * (TK - 1));
+            kHi = min(min(bs + NI - 1, rgK.y - SW * (TK - 1)), thi);
+        }
+        const unsigned long long *pK = a.xchg + (srcK >= 0 ? srcK : 0) * wordsPerTile + (size_t)T * TK +
+                                       (size_t)SW * (TK - 1) * TJ + lane;   // + te * TJ
+        int jLo[JQ], jHi[JQ], jes[JQ];
+        const unsigned long long *pJ[JQ];
+#pragma unroll
+        for (int q = 0; q < JQ; q++) {
+            const int e = lane + 32 * q, es = e / TK, ew = e % TK;
+            jes[q] = es;
+            jLo[q] = 1;
+            jHi[q] = 0;
+            if (srcJ >= 0 && pencil_in(laneJ, ew)) {
+                const int bs = base_of(laneJ, ew);
+                jLo[q] = max(bs, rgJ.x - SL * (TJ - 1));
+                jHi[q] = min(min(bs + NI - 1, rgJ.y - SL * (TJ - 1)), thi);
+            }
+            pJ[q] = a.xchg + (srcJ >= 0 ? srcJ : 0) * wordsPerTile + (size_t)SL * (TJ - 1) * TK + ew;   // + te * TK
+        }
+        bool mine = kLo <= kHi;
+#pragma unroll
+        for (int q = 0; q < JQ; q++) mine = mine || jLo[q] <= jHi[q];
+        const bool anyEdge = __any_sync(0xffffffffu, mine);
         for (int m = 0; m < nChunks; m++) {
             const int b = m % NBUF;
             Slot &sl = sm.slot[b];
             if (m >= NBUF && !mb_wait(&sm.done[b], ((m - NBUF) / NBUF) & 1, &sm.abort, a.err, a.spinLimit))
                 return;   // aborting
-            const int tb = tlo + m * CH, rows = chunk_rows(m);
-            // edge terms: the consumer cell is computed and the producer's
-            // cell (SL (TJ-1) or SW (TK-1) steps later there) too
+            const int tb = tlo + m * CH;
+            if (!anyEdge) {   // no upstream tile: the edge terms are zero
+                if (m < NBUF) {
+#pragma unroll
+                    for (int q2 = 0; q2 < CH; q2++) sl.eK[q2][lane] = 0.0f;
+#pragma unroll
+                    for (int q = 0; q < JQ; q++) sl.eJ[jes[q]][(lane + 32 * q) % TK] = 0.0f;
+                }
+                __syncwarp();
+                mb_arrive(&sm.edges[b]);
+                continue;
+            }
             float vK[CH], vJ[JQ];
             unsigned long long wK[CH], wJ[JQ];
             unsigned int needK = 0, needJ = 0;
 #pragma unroll
-            for (int s = 0; s < CH; s++) {
-                const int te = tb + s, i = cell(lane, warpK, te);
-                const bool need = srcK >= 0 && s < rows && pencil_in(lane, warpK) && i >= 1 && i <= NI &&
-                                  te + SW * (TK - 1) >= rgK.x && te + SW * (TK - 1) <= rgK.y;
-                wK[s] = need ? ld_word(srcKw + (size_t)(te + SW * (TK - 1)) * TJ + lane) : 0ull;
-                needK |= need ? 1u << s : 0u;
+            for (int s2 = 0; s2 < CH; s2++) {
+                const int te = tb + s2;
+                const bool need = te >= kLo && te <= kHi;
+                wK[s2] = need ? ld_word(pK + (size_t)te * TJ) : 0ull;
+                needK |= need ? 1u << s2 : 0u;
             }
 #pragma unroll
             for (int q = 0; q < JQ; q++) {
-                const int e = lane + 32 * q, es = e / TK, ew = e % TK, te = tb + es, i = cell(laneJ, ew, te);
-                const bool need = srcJ >= 0 && es < rows && pencil_in(laneJ, ew) && i >= 1 && i <= NI &&
-                                  te + SL * (TJ - 1) >= rgJ.x && te + SL * (TJ - 1) <= rgJ.y;
-                wJ[q] = need ? ld_word(srcJw + (size_t)(te + SL * (TJ - 1)) * TK + ew) : 0ull;
+                const int te = tb + jes[q];
+                const bool need = te >= jLo[q] && te <= jHi[q];
+                wJ[q] = need ? ld_word(pJ[q] + (size_t)te * TK) : 0ull;
                 needJ |= need ? 1u << q : 0u;
             }
             bool ok = true;
             for (unsigned int spin = 0;; spin++) {
                 unsigned int missK = 0, missJ = 0;
 #pragma unroll
-                for (int s = 0; s < CH; s++)
-                    missK |= ((needK >> s) & 1u) && (unsigned int)(wK[s] >> 32) != epWait ? 1u << s : 0u;
+                for (int s2 = 0; s2 < CH; s2++)
+                    missK |= ((needK >> s2) & 1u) && (unsigned int)(wK[s2] >> 32) != epWait ? 1u << s2 : 0u;
 #pragma unroll
                 for (int q = 0; q < JQ; q++)
                     missJ |= ((needJ >> q) & 1u) && (unsigned int)(wJ[q] >> 32) != epWait ? 1u << q : 0u;
@@ -324,13 +368,11 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_wavefront(SweepArgs a) {
                 if (*(volatile int *)&sm.abort || *(volatile int *)a.err) { ok = false; break; }
                 if (spin > 64) __nanosleep(32);
 #pragma unroll
-                for (int s = 0; s < CH; s++)
-                    if ((missK >> s) & 1u) wK[s] = ld_word(srcKw + (size_t)(tb + s + SW * (TK - 1)) * TJ + lane);
+                for (int s2 = 0; s2 < CH; s2++)
+                    if ((missK >> s2) & 1u) wK[s2] = ld_word(pK + (size_t)(tb + s2) * TJ);
 #pragma unroll
-                for (int q = 0; q < JQ; q++) {
-                    const int e = lane + 32 * q, es = e / TK, ew = e % TK;
-                    if ((missJ >> q) & 1u) wJ[q] = ld_word(srcJw + (size_t)(tb + es + SL * (TJ - 1)) * TK + ew);
-                }
+                for (int q = 0; q < JQ; q++)
+                    if ((missJ >> q) & 1u) wJ[q] = ld_word(pJ[q] + (size_t)(tb + jes[q]) * TK);
             }
             if (!__all_sync(0xffffffffu, ok)) {
                 // the compute warps and the loader see the flag in their waits
@@ -338,16 +380,13 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_wavefront(SweepArgs a) {
                 return;
             }
 #pragma unroll
-            for (int s = 0; s < CH; s++) vK[s] = __uint_as_float((unsigned int)wK[s]);
+            for (int s2 = 0; s2 < CH; s2++) vK[s2] = __uint_as_float((unsigned int)wK[s2]);
 #pragma unroll
             for (int q = 0; q < JQ; q++) vJ[q] = __uint_as_float((unsigned int)wJ[q]);
 #pragma unroll
-            for (int s = 0; s < CH; s++) sl.eK[s][lane] = vK[s];
+            for (int s2 = 0; s2 < CH; s2++) sl.eK[s2][lane] = vK[s2];
 #pragma unroll
-            for (int q = 0; q < JQ; q++) {
-                const int e = lane + 32 * q;
-                sl.eJ[e / TK][e % TK] = vJ[q];
-            }
+            for (int q = 0; q < JQ; q++) sl.eJ[jes[q]][(lane + 32 * q) % TK] = vJ[q];
             __syncwarp();
             mb_arrive(&sm.edges[b]);
         }
@@ -374,15 +413,9 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_wavefront(SweepArgs a) {
     float hist[SL];
 #pragma unroll
     for (int q = 0; q < SL; q++) hist[q] = 0.0f;
-    for (int n = 0; n < nChunks; n++) {
+    // Chunk n with its operands in Lr[s], Rr[s] (step tb + s).
+    auto run_chunk = [&](int n, const float4 (&Lr)[CH], const float (&Rr)[CH]) -> bool {
         const int b = n % NBUF, tb = tlo + n * CH;
-        const unsigned par = (n / NBUF) & 1;
-        const bool fine = mb_wait(&sm.loaded[b], par, &sm.abort, a.err, a.spinLimit) &&
-                          mb_wait(&sm.edges[b], par, &sm.abort, a.err, a.spinLimit);
-        if (compute_sync_or(!fine)) {
-            *(volatile int *)&sm.abort = 1;
-            return;
-        }
         const Slot &sl = sm.slot[b];
         // the results of chunk n: row of step tb + s at out0 + s * step
         float *out0 = a.out + tileBase + (size_t)(FWD ? tb : T - 1 - tb) * NP + threadIdx.x;
@@ -391,10 +424,9 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_wavefront(SweepArgs a) {
         for (int s = 0; s < CH; s++) {
             // (tb - tlo) is a multiple of CH, so step t's ring positions are s's
             const int t = tb + s;
-            const int q = FWD ? s : CH - 1 - s;
             const int cur = s % (2 * SW), prev = (s + SW) % (2 * SW);   // steps t and t - SW
-            const float4 Lc = sl.L[q][threadIdx.x];
-            const float rr = sl.r[q][threadIdx.x];
+            const float4 Lc = Lr[s];
+            const float rr = Rr[s];
             const bool valid = t >= v0 && t <= v1;
             float res;
             if (FWD) {
@@ -435,6 +467,31 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_wavefront(SweepArgs a) {
             if (s % SW == SW - 1 && s != CH - 1) compute_sync();
         }
         mb_arrive(&sm.done[b]);   // the slot may be refilled
+        return true;
+    };
+    auto wait_chunk = [&](int n) -> bool {   // the chunk's slot is filled
+        const int b = n % NBUF;
+        const unsigned par = (n / NBUF) & 1;
+        const bool fine = mb_wait(&sm.loaded[b], par, &sm.abort, a.err, a.spinLimit) &&
+                          mb_wait(&sm.edges[b], par, &sm.abort, a.err, a.spinLimit);
+        if (compute_sync_or(!fine)) {
+            *(volatile int *)&sm.abort = 1;
+            return false;
+        }
+        return true;
+    };
+    for (int n = 0; n < nChunks; n++) {
+        if (!wait_chunk(n)) return;
+        const Slot &sl = sm.slot[n % NBUF];
+        float4 Lr[CH];
+        float Rr[CH];
+#pragma unroll
+        for (int s = 0; s < CH; s++) {
+            const int q = FWD ? s : CH - 1 - s;
+            Lr[s] = sl.L[q][threadIdx.x];
+            Rr[s] = sl.r[q][threadIdx.x];
+        }
+        if (!run_chunk(n, Lr, Rr)) return;
     }
 }
 
