@@ -225,6 +225,7 @@ def run_gpu(args, rank, world):
     # into one pinned host buffer, as a caller of the reference's
     # getMarkerParticlePositionData(char *) passes its own buffer
     e2e_sim = fg.FluidSimulation(sc.isize, sc.jsize, sc.ksize, sc.dx)
+    e2e_sim.disableSurfaceReconstruction()   # as the reference arm and `value`: the FLIP step alone
     e2e_sim.setPICFLIPRatio(sc.pic_ratio)
     e2e_sim.addBodyForce(*sc.gravity)
     e2e_sim.setCFLConditionNumber(sc.cfl)

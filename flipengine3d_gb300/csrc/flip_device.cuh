@@ -266,6 +266,59 @@ int pressure_project(const StepConsts &c, const PressureArgs &a, PressureBuffers
 }  // namespace flip
 
 namespace flip {
+// -- surface reconstruction (flip_mesh.cu)
+// The frame of the mesher's one compute chunk: the subdivided grid, its
+// blocks of 10^3 nodes, the chunk's nodes and offset, and the particle radii.
+struct MeshFrame {
+    int I, J, K;
+    double dx, invdx, subdx, invsub;
+    float invsubf;
+    double blockdx, invBlock;      // 10 subdx, occupancy pass
+    float invBlockf;
+    float blockdxF;                // (float)(10 subdx), the count pass's block size
+    double invBlockF;
+    float invBlockFf;
+    int nbI, nbJ, nbK;             // blocks of the subdivided grid
+    int ni, nj, nk;                // chunk nodes
+    int cbI, cbJ, cbK;             // chunk blocks
+    float offx, offy, offz;        // chunk offset
+    float r, sr, maxd;             // radius, search radius, initial distance
+    float bbx, bby, bbz;           // the chunk's expanded box
+    double bbw, bbh, bbd;
+    int solidMode;                 // 0 interpolated, 1 subdivision 2 at offset 0, 2 same grid
+    float scalef, invscalef;
+};
+struct MeshJob {
+    StepConsts c;
+    ParticleSoA p;
+    int n;
+    const int *cellStart;
+    const float *solidPhi;
+    int subdivisions;
+    double radius;                 // marker particle radius x marker particle scale
+    double smoothValue;
+    int smoothIterations;
+};
+// Device buffers of the mesher, grown on demand; the mesh is verts[cur]
+// (nverts xyz floats) and tris (ntris vertex triples).
+struct MeshBuffers {
+    long long bytes = 0;
+    uint8_t *occ = nullptr, *active = nullptr, *cube = nullptr;
+    float *field = nullptr;
+    int *vstart = nullptr, *tstart = nullptr, *totals = nullptr;
+    int2 *tiles = nullptr, *adj = nullptr, *adjStart = nullptr;
+    int *adjCursor = nullptr, *adjList = nullptr, *tris = nullptr;
+    float *verts[2] = {nullptr, nullptr};
+    long long occCap = 0, activeCap = 0, cubeCap = 0, fieldCap = 0, vstartCap = 0, tstartCap = 0, totalsCap = 0,
+              tilesCap = 0, adjCap = 0, adjStartCap = 0, adjCursorCap = 0, adjListCap = 0, trisCap = 0;
+    long long vertsCap[2] = {0, 0};
+    int nverts = 0, ntris = 0, cur = 0;
+};
+// Mesh the particles of `job` into mb (synchronises the stream twice).
+int mesh_surface(const MeshJob &job, MeshBuffers &mb, cudaStream_t s);
+void mesh_release(MeshBuffers &mb);
+int record_error(int code, const std::string &msg);   // sets flip_last_error()
+
 // Packed xyz positions/velocities (either may be null) of the n particles in
 // the reference's order; flags/rank hold idSpace+1 ints, scratch
 // scan_scratch_ints(idSpace) ints.

@@ -96,6 +96,14 @@ struct flip_ctx {
     unsigned int idNext = 0;        // ids handed out so far (loaded, then seeded)
     float *fu = nullptr, *fv = nullptr, *fw = nullptr;   // face friction, when an obstacle has some
     StepConsts c{};
+    // surface reconstruction (fluidsimulation.h:1586-1611: on, subdivision
+    // 1, smoothing 0.5 x 2, marker particle scale 3)
+    bool meshEnabled = true;
+    int meshSubdivisions = 1;
+    double meshSmoothValue = 0.5;
+    int meshSmoothIterations = 2;
+    double markerParticleScale = 3.0;
+    MeshBuffers mesh;
 
     // device buffers
     ParticleSoA pa{}, pb{};
@@ -639,6 +647,29 @@ int step_fluid(flip_ctx *x, double dt, flip_stage_dump *d) {
     return seed_fluid_meshes(x);   // _updateFluidObjects (fluidsimulation.cpp:5505)
 }
 
+// The surface mesh of the current particles (_launchOutputSurfaceMeshThread
+// and _outputSurfaceMeshThread, fluidsimulation.cpp:5150-5239): radius =
+// marker particle radius (_initializeParticleRadii, :2643-2649) x marker
+// particle scale; the solid level set as the step uses it.
+int build_isomesh(flip_ctx *x) {
+    MeshJob job{};
+    job.c = x->c;
+    job.p = x->pa;
+    job.n = x->n;
+    job.cellStart = x->cellStart;
+    job.solidPhi = x->solidPhi;
+    job.subdivisions = x->meshSubdivisions;
+    const double volume = x->dx * x->dx * x->dx / 8.0, pi = 3.141592653;
+    job.radius = std::pow(3 * volume / (4 * pi), 1.0 / 3.0) * x->markerParticleScale;
+    job.smoothValue = x->meshSmoothValue;
+    job.smoothIterations = x->meshSmoothIterations;
+    if (x->n > 0 && !x->solidBuilt) {
+        int rc = build_solid(x);
+        if (rc) return rc;
+    }
+    return mesh_surface(job, x->mesh, x->stream);
+}
+
 // _calculateNextTimeStep (fluidsimulation.cpp:5593-5613)
 double next_time_step(flip_ctx *x, double dt) {
     double maxu;
@@ -684,6 +715,9 @@ int do_update(flip_ctx *x, double dt, flip_stage_dump *d) {
             if (rc == FLIP_E_SOLVER_NOCONV) worst = rc;
             else if (rc != FLIP_OK) return rc;
             if (x->stats.pressure_status == FLIP_E_SOLVER_NOCONV) worst = FLIP_E_SOLVER_NOCONV;
+            // _outputSimulationData (fluidsimulation.cpp:5444-5464): the
+            // frame's mesh comes from the state after its first substep
+            if (x->stepNumber == 0 && x->meshEnabled && (rc = build_isomesh(x))) return rc;
         }
         d = nullptr;
         x->stepNumber++;
@@ -820,6 +854,7 @@ int flip_destroy(flip_ctx *x) {
     for (int q = 0; q < 2 * (PCG_BATCH + 1); q++)
         if (x->sweepTiming.ev[q]) cudaEventDestroy(x->sweepTiming.ev[q]);
     for (void *p : x->allocations) cudaFree(p);
+    mesh_release(x->mesh);
     if (x->mail) cudaFreeHost(x->mail);
     if (x->pmail) cudaFreeHost(x->pmail);
     if (x->ownStream) cudaStreamDestroy(x->stream);
@@ -1213,7 +1248,7 @@ int flip_get_stage_times(flip_ctx *x, double *ms, long long *substeps) {
 
 int flip_get_device_bytes(flip_ctx *x, long long *bytes) {
     if (!x || !bytes) return FLIP_E_NULL;
-    *bytes = x->deviceBytes;
+    *bytes = x->deviceBytes + x->mesh.bytes;
     return FLIP_OK;
 }
 
@@ -1244,6 +1279,80 @@ int flip_get_launch_count(flip_ctx *x, long long *count) {
     if (!x || !count) return FLIP_E_NULL;
     *count = x->launches;
     return FLIP_OK;
+}
+
+int flip_enable_surface_reconstruction(flip_ctx *x, int enable) {
+    if (!x) return FLIP_E_NULL;
+    x->meshEnabled = enable != 0;
+    return FLIP_OK;
+}
+int flip_is_surface_reconstruction_enabled(flip_ctx *x, int *enabled) {
+    if (!x || !enabled) return FLIP_E_NULL;
+    *enabled = x->meshEnabled ? 1 : 0;
+    return FLIP_OK;
+}
+int flip_set_surface_subdivision_level(flip_ctx *x, int n) {
+    if (!x) return FLIP_E_NULL;
+    if (n < 1) return fail(FLIP_E_DOMAIN, "Error: subdivision level must be greater than or equal to 1.");
+    x->meshSubdivisions = n;
+    return FLIP_OK;
+}
+int flip_get_surface_subdivision_level(flip_ctx *x, int *n) {
+    if (!x || !n) return FLIP_E_NULL;
+    *n = x->meshSubdivisions;
+    return FLIP_OK;
+}
+int flip_set_surface_smoothing_value(flip_ctx *x, double s) {
+    if (!x) return FLIP_E_NULL;
+    x->meshSmoothValue = s;
+    return FLIP_OK;
+}
+int flip_get_surface_smoothing_value(flip_ctx *x, double *s) {
+    if (!x || !s) return FLIP_E_NULL;
+    *s = x->meshSmoothValue;
+    return FLIP_OK;
+}
+int flip_set_surface_smoothing_iterations(flip_ctx *x, int n) {
+    if (!x) return FLIP_E_NULL;
+    if (n < 0) return fail(FLIP_E_DOMAIN, "Error: number of smoothing iterations must be positive.");
+    x->meshSmoothIterations = n;
+    return FLIP_OK;
+}
+int flip_get_surface_smoothing_iterations(flip_ctx *x, int *n) {
+    if (!x || !n) return FLIP_E_NULL;
+    *n = x->meshSmoothIterations;
+    return FLIP_OK;
+}
+int flip_set_marker_particle_scale(flip_ctx *x, double s) {
+    if (!x) return FLIP_E_NULL;
+    if (!(s >= 0.0)) return fail(FLIP_E_DOMAIN, "Error: marker particle scale must be greater than or equal to 0.");
+    x->markerParticleScale = s;
+    return FLIP_OK;
+}
+int flip_get_marker_particle_scale(flip_ctx *x, double *s) {
+    if (!x || !s) return FLIP_E_NULL;
+    *s = x->markerParticleScale;
+    return FLIP_OK;
+}
+int flip_build_isomesh(flip_ctx *x) {
+    if (!x) return FLIP_E_NULL;
+    if (!x->initialized) return fail(FLIP_E_RUNTIME, "Error: FluidSimulation must be initialized before meshing.");
+    LaunchTally tally(x);
+    int rc = build_isomesh(x);
+    if (rc) return rc;
+    return sync(x);
+}
+int flip_get_isomesh(flip_ctx *x, int *nverts, int *ntris, float *verts, int *tris) {
+    if (!x || !nverts || !ntris) return FLIP_E_NULL;
+    *nverts = x->mesh.nverts;
+    *ntris = x->mesh.ntris;
+    if (verts && x->mesh.nverts > 0)
+        CK(cudaMemcpyAsync(verts, x->mesh.verts[x->mesh.cur], 3 * sizeof(float) * (size_t)x->mesh.nverts,
+                           cudaMemcpyDeviceToHost, x->stream));
+    if (tris && x->mesh.ntris > 0)
+        CK(cudaMemcpyAsync(tris, x->mesh.tris, 3 * sizeof(int) * (size_t)x->mesh.ntris, cudaMemcpyDeviceToHost,
+                           x->stream));
+    return sync(x);
 }
 
 }  // extern "C"

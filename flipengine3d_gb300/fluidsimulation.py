@@ -118,6 +118,18 @@ SIGNATURES = {
     "flip_runtime_update_all": [_P, C.POINTER(C.c_void_p), _I, _D],
     "flip_runtime_admit": [_P, C.c_longlong, C.POINTER(C.c_int)],
     "flip_runtime_pending": [_P, C.POINTER(C.c_int), C.POINTER(C.c_int)],
+    "flip_enable_surface_reconstruction": [_P, _I],
+    "flip_is_surface_reconstruction_enabled": [_P, C.POINTER(C.c_int)],
+    "flip_set_surface_subdivision_level": [_P, _I],
+    "flip_get_surface_subdivision_level": [_P, C.POINTER(C.c_int)],
+    "flip_set_surface_smoothing_value": [_P, _D],
+    "flip_get_surface_smoothing_value": [_P, C.POINTER(C.c_double)],
+    "flip_set_surface_smoothing_iterations": [_P, _I],
+    "flip_get_surface_smoothing_iterations": [_P, C.POINTER(C.c_int)],
+    "flip_set_marker_particle_scale": [_P, _D],
+    "flip_get_marker_particle_scale": [_P, C.POINTER(C.c_double)],
+    "flip_build_isomesh": [_P],
+    "flip_get_isomesh": [_P, C.POINTER(C.c_int), C.POINTER(C.c_int), _P, _P],
 }
 
 
@@ -516,9 +528,62 @@ class FluidSimulation:
         self._c(self._lib.flip_get_frame_stats(self._h, C.byref(s)))
         return s
 
+    # -- surface reconstruction (fluidsimulation.cpp:216-300, 367-380, 2543-2546)
+    def enableSurfaceReconstruction(self):
+        self._c(self._lib.flip_enable_surface_reconstruction(self._h, 1))
+
+    def disableSurfaceReconstruction(self):
+        self._c(self._lib.flip_enable_surface_reconstruction(self._h, 0))
+
+    def isSurfaceReconstructionEnabled(self) -> bool:
+        v = C.c_int()
+        self._c(self._lib.flip_is_surface_reconstruction_enabled(self._h, C.byref(v)))
+        return bool(v.value)
+
+    def setSurfaceSubdivisionLevel(self, n: int):
+        self._c(self._lib.flip_set_surface_subdivision_level(self._h, int(n)))
+
+    def getSurfaceSubdivisionLevel(self) -> int:
+        v = C.c_int()
+        self._c(self._lib.flip_get_surface_subdivision_level(self._h, C.byref(v)))
+        return v.value
+
+    def setSurfaceSmoothingValue(self, s: float):
+        self._c(self._lib.flip_set_surface_smoothing_value(self._h, float(s)))
+
+    def getSurfaceSmoothingValue(self) -> float:
+        v = C.c_double()
+        self._c(self._lib.flip_get_surface_smoothing_value(self._h, C.byref(v)))
+        return v.value
+
+    def setSurfaceSmoothingIterations(self, n: int):
+        self._c(self._lib.flip_set_surface_smoothing_iterations(self._h, int(n)))
+
+    def getSurfaceSmoothingIterations(self) -> int:
+        v = C.c_int()
+        self._c(self._lib.flip_get_surface_smoothing_iterations(self._h, C.byref(v)))
+        return v.value
+
+    def setMarkerParticleScale(self, s: float):
+        self._c(self._lib.flip_set_marker_particle_scale(self._h, float(s)))
+
+    def getMarkerParticleScale(self) -> float:
+        v = C.c_double()
+        self._c(self._lib.flip_get_marker_particle_scale(self._h, C.byref(v)))
+        return v.value
+
+    def buildIsomesh(self):
+        """Mesh the current particles now, as the first substep of a frame does."""
+        self._c(self._lib.flip_build_isomesh(self._h))
+
     def getIsomesh(self):
-        """Surface meshing is outside this library: an empty (vertices, triangles) pair."""
-        return np.zeros((0, 3), np.float32), np.zeros((0, 3), np.int32)
+        """The last frame's surface mesh: (vertices (n, 3) float32, triangles (m, 3) int32)."""
+        nv, nt = C.c_int(), C.c_int()
+        self._c(self._lib.flip_get_isomesh(self._h, C.byref(nv), C.byref(nt), None, None))
+        v = np.zeros((nv.value, 3), np.float32)
+        t = np.zeros((nt.value, 3), np.int32)
+        self._c(self._lib.flip_get_isomesh(self._h, C.byref(nv), C.byref(nt), _ptr(v), _ptr(t)))
+        return v, t
 
     # -- state readback for tests
     def liquid_sdf(self) -> np.ndarray:
@@ -633,11 +698,16 @@ class FluidSimulation:
         return out
 
     @classmethod
-    def from_scene(cls, scene, tolerance=None):
+    def from_scene(cls, scene, tolerance=None, surface_subdivisions=None):
         """Set up a seeded scene (flipengine3d_gb300.scenes) the way the
-        reference's headless driver does: PIC ratio, gravity, CFL,
-        tolerance, particles, initialize."""
+        reference's headless driver does: surface reconstruction off (or on
+        at the given subdivision level), PIC ratio, gravity, CFL, tolerance,
+        particles, initialize."""
         sim = cls(scene.isize, scene.jsize, scene.ksize, scene.dx)
+        if surface_subdivisions is None:
+            sim.disableSurfaceReconstruction()
+        else:
+            sim.setSurfaceSubdivisionLevel(surface_subdivisions)
         sim.setPICFLIPRatio(scene.pic_ratio)
         sim.addBodyForce(*scene.gravity)
         sim.setCFLConditionNumber(scene.cfl)

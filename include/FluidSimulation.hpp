@@ -56,18 +56,25 @@ struct FluidSimulationFrameStats {
     int pressureStatus = FLIP_OK;
 };
 
-// Surface reconstruction is not part of this library: getIsomesh() returns
-// an empty mesh, as the reference does with reconstruction disabled.
-struct TriangleMesh {
-    std::vector<float> vertices;
-    std::vector<int> triangles;
-};
-
-// vmath::vec3 as addMeshFluid takes it (float components)
+// vmath::vec3 (vmath.h): three float components
 struct vec3 {
     float x = 0.0f, y = 0.0f, z = 0.0f;
     vec3() = default;
     vec3(double a, double b, double c) : x((float)a), y((float)b), z((float)c) {}
+};
+// Triangle (triangle.h): three vertex indices
+struct Triangle {
+    int tri[3] = {0, 0, 0};
+    Triangle() = default;
+    Triangle(int a, int b, int c) : tri{a, b, c} {}
+};
+static_assert(sizeof(vec3) == 3 * sizeof(float) && sizeof(Triangle) == 3 * sizeof(int),
+              "vertices and triangles pass to the C ABI as packed arrays");
+
+// TriangleMesh (trianglemesh.h): the members the driver reads and writes
+struct TriangleMesh {
+    std::vector<vec3> vertices;
+    std::vector<Triangle> triangles;
 };
 
 // A static obstacle mesh: the part of the reference's MeshObject
@@ -134,18 +141,62 @@ public:
         check(flip_get_pic_flip_ratio(ctx_, &r));
         return r;
     }
-    // No effect: the step runs on the GPU; kept for drivers that call them.
+    // No effect: the step runs on the GPU; kept for drivers that call it.
     void setMaxThreadCount(int) {}
-    void disableSurfaceReconstruction() {}
-    TriangleMesh &getIsomesh() { return mesh_; }
+
+    // Surface reconstruction (fluidsimulation.cpp:216-300, 367-380): on by
+    // default; the mesh of the last frame's first substep.
+    void enableSurfaceReconstruction() { check(flip_enable_surface_reconstruction(ctx_, 1)); }
+    void disableSurfaceReconstruction() { check(flip_enable_surface_reconstruction(ctx_, 0)); }
+    bool isSurfaceReconstructionEnabled() {
+        int v = 0;
+        check(flip_is_surface_reconstruction_enabled(ctx_, &v));
+        return v != 0;
+    }
+    void setSurfaceSubdivisionLevel(int n) { check(flip_set_surface_subdivision_level(ctx_, n)); }
+    int getSurfaceSubdivisionLevel() {
+        int v = 0;
+        check(flip_get_surface_subdivision_level(ctx_, &v));
+        return v;
+    }
+    void setSurfaceSmoothingValue(double s) { check(flip_set_surface_smoothing_value(ctx_, s)); }
+    double getSurfaceSmoothingValue() {
+        double v = 0.0;
+        check(flip_get_surface_smoothing_value(ctx_, &v));
+        return v;
+    }
+    void setSurfaceSmoothingIterations(int n) { check(flip_set_surface_smoothing_iterations(ctx_, n)); }
+    int getSurfaceSmoothingIterations() {
+        int v = 0;
+        check(flip_get_surface_smoothing_iterations(ctx_, &v));
+        return v;
+    }
+    void setMarkerParticleScale(double s) { check(flip_set_marker_particle_scale(ctx_, s)); }
+    double getMarkerParticleScale() {
+        double v = 0.0;
+        check(flip_get_marker_particle_scale(ctx_, &v));
+        return v;
+    }
+    // getIsomesh (fluidsimulation.cpp:2543-2546): copied from the device on
+    // each call into the object returned.
+    TriangleMesh &getIsomesh() {
+        int nv = 0, nt = 0;
+        check(flip_get_isomesh(ctx_, &nv, &nt, nullptr, nullptr));
+        mesh_.vertices.resize((size_t)nv);
+        mesh_.triangles.resize((size_t)nt);
+        check(flip_get_isomesh(ctx_, &nv, &nt, reinterpret_cast<float *>(mesh_.vertices.data()),
+                               reinterpret_cast<int *>(mesh_.triangles.data())));
+        return mesh_;
+    }
 
     // addMeshObstacle (fluidsimulation.cpp:1994-2008): static obstacles only.
     void addMeshObstacle(MeshObject *obstacle) {
         for (MeshObject *o : obstacles_)
             if (o == obstacle) throw std::runtime_error("Error: mesh obstacle has already been added.\n");
         const TriangleMesh &m = obstacle->getMesh();
-        check(flip_add_mesh_obstacle(ctx_, (int)(m.vertices.size() / 3), m.vertices.data(),
-                                     (int)(m.triangles.size() / 3), m.triangles.data(), obstacle->getFriction()));
+        check(flip_add_mesh_obstacle(ctx_, (int)m.vertices.size(), reinterpret_cast<const float *>(m.vertices.data()),
+                                     (int)m.triangles.size(), reinterpret_cast<const int *>(m.triangles.data()),
+                                     obstacle->getFriction()));
         obstacles_.push_back(obstacle);
     }
 
@@ -154,8 +205,9 @@ public:
     void addMeshFluid(const MeshObject &fluid) { addMeshFluid(fluid, vec3(0.0, 0.0, 0.0)); }
     void addMeshFluid(const MeshObject &fluid, vec3 velocity) {
         const TriangleMesh &m = fluid.getMesh();
-        check(flip_add_mesh_fluid(ctx_, (int)(m.vertices.size() / 3), m.vertices.data(), (int)(m.triangles.size() / 3),
-                                  m.triangles.data(), velocity.x, velocity.y, velocity.z));
+        check(flip_add_mesh_fluid(ctx_, (int)m.vertices.size(), reinterpret_cast<const float *>(m.vertices.data()),
+                                  (int)m.triangles.size(), reinterpret_cast<const int *>(m.triangles.data()),
+                                  velocity.x, velocity.y, velocity.z));
     }
     void setMarkerParticleJitterFactor(double jit) { check(flip_set_marker_particle_jitter_factor(ctx_, jit)); }
     double getMarkerParticleJitterFactor() {

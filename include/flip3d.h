@@ -289,6 +289,40 @@ int flip_mic0_precondition(int isize, int jsize, int ksize, const uint8_t *fluid
 /* Number of this library's kernel launches issued so far on the context. */
 int flip_get_launch_count(flip_ctx *ctx, long long *count);
 
+/* Surface reconstruction, the mesh getIsomesh() returns (fluidsimulation.cpp:
+ * 2543-2546).  As in the reference, it is on by default and runs after the
+ * first substep of every frame (_outputSimulationData, :5444-5464): the
+ * marker particles' surface by marching cubes on the grid subdivided
+ * `subdivision level` times, then smoothed (_outputSurfaceMeshThread,
+ * :5150-5219; ParticleMesher, Polygonizer3d, TriangleMesh::smooth).  Vertices
+ * and triangles are those the reference makes from the same particles.  Not
+ * restated: polygonizer slices other than 1, the preview mesh, meshing
+ * volumes, surface motion blur, inverted contact normals and removal near
+ * the domain (all off by default in the reference); the domain offset and
+ * scale are the identity.
+ *   enable/disable/isSurfaceReconstructionEnabled (:367-380);
+ *   set/getSurfaceSubdivisionLevel (:216-231; FLIP_E_DOMAIN below 1);
+ *   set/getSurfaceSmoothingValue (:250-259) and ...Iterations (:261-276;
+ *   FLIP_E_DOMAIN below 0); set/getMarkerParticleScale (:163-179; the mesher's
+ *   particle radius is the marker particle radius times this, default 3;
+ *   FLIP_E_DOMAIN below 0).
+ * flip_build_isomesh meshes the current particles now, as the first substep
+ * of a frame would (FLIP_E_RUNTIME before initialize).  flip_get_isomesh
+ * writes the counts and, where the pointers are not NULL, the vertices (3
+ * floats each) and triangles (3 vertex indices each). */
+int flip_enable_surface_reconstruction(flip_ctx *ctx, int enable);
+int flip_is_surface_reconstruction_enabled(flip_ctx *ctx, int *enabled);
+int flip_set_surface_subdivision_level(flip_ctx *ctx, int n);
+int flip_get_surface_subdivision_level(flip_ctx *ctx, int *n);
+int flip_set_surface_smoothing_value(flip_ctx *ctx, double value);
+int flip_get_surface_smoothing_value(flip_ctx *ctx, double *value);
+int flip_set_surface_smoothing_iterations(flip_ctx *ctx, int n);
+int flip_get_surface_smoothing_iterations(flip_ctx *ctx, int *n);
+int flip_set_marker_particle_scale(flip_ctx *ctx, double scale);
+int flip_get_marker_particle_scale(flip_ctx *ctx, double *scale);
+int flip_build_isomesh(flip_ctx *ctx);
+int flip_get_isomesh(flip_ctx *ctx, int *nverts, int *ntris, float *verts, int *tris);
+
 /* Device memory of a context (flip_get_device_bytes), and the same figure
  * for a scene not yet created (flip_estimate_device_bytes: grids, pressure
  * system, particle storage for `particles`), for admission decisions.  No

@@ -525,6 +525,46 @@ void ref_add_mesh_obstacle(void *h, int nverts, const float *verts, int ntris, c
     r->sim->addMeshObstacle(o);
 }
 
+// Surface reconstruction settings (fluidsimulation.cpp:216-300, 367-376):
+// enabled or not, subdivision level, smoothing value and iterations.  The
+// mesher thread is joined at once (disableAsynchronousMeshing, :390-394), so
+// getIsomesh() holds the mesh when update() returns.
+void ref_set_surface_reconstruction(void *h, int enable, int subdivisions, double smooth_value, int smooth_iters) {
+    FluidSimulation *s = ((RefSim *)h)->sim;
+    if (enable) s->enableSurfaceReconstruction(); else s->disableSurfaceReconstruction();
+    s->setSurfaceSubdivisionLevel(subdivisions);
+    s->setSurfaceSmoothingValue(smooth_value);
+    s->setSurfaceSmoothingIterations(smooth_iters);
+    s->disableAsynchronousMeshing();
+}
+
+// The mesh of the simulation's current marker particles, as the first
+// substep of a frame makes it (_launchOutputSurfaceMeshThread,
+// fluidsimulation.cpp:5221-5239, and _outputSurfaceMeshThread, :5150-5219),
+// run now on the current particles and solid level set.
+void ref_mesh_now(void *h) {
+    FluidSimulation *s = ((RefSim *)h)->sim;
+    s->_launchOutputSurfaceMeshThread();
+    if (s->_mesherThread.joinable()) s->_mesherThread.join();
+}
+
+// getIsomesh() (fluidsimulation.cpp:2543-2546): counts, and the vertices
+// (xyz floats) and triangles (three ints) where the pointers are not null.
+void ref_get_isomesh(void *h, int *nverts, int *ntris, float *verts, int *tris) {
+    TriangleMesh &m = ((RefSim *)h)->sim->getIsomesh();
+    *nverts = (int)m.vertices.size();
+    *ntris = (int)m.triangles.size();
+    if (verts)
+        for (size_t v = 0; v < m.vertices.size(); v++) {
+            verts[3 * v] = m.vertices[v].x;
+            verts[3 * v + 1] = m.vertices[v].y;
+            verts[3 * v + 2] = m.vertices[v].z;
+        }
+    if (tris)
+        for (size_t t = 0; t < m.triangles.size(); t++)
+            for (int q = 0; q < 3; q++) tris[3 * t + q] = m.triangles[t].tri[q];
+}
+
 // Per node of the solid level set, the friction of the closest mesh object
 // (0 where none): what the constrain step averages per face
 // (fluidsimulation.cpp:3785-3846).

@@ -72,6 +72,12 @@ def lib(prefix: str = "ref"):
             L.ref_add_mesh_obstacle.restype = None
             L.ref_get_node_friction.argtypes = [C.c_void_p, C.c_void_p]
             L.ref_get_node_friction.restype = None
+            L.ref_set_surface_reconstruction.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_double, C.c_int]
+            L.ref_set_surface_reconstruction.restype = None
+            L.ref_mesh_now.argtypes = [C.c_void_p]
+            L.ref_mesh_now.restype = None
+            L.ref_get_isomesh.argtypes = [C.c_void_p] + [C.c_void_p] * 4
+            L.ref_get_isomesh.restype = None
             L.ref_add_mesh_fluid.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_double,
                                              C.c_double, C.c_double]
             L.ref_add_mesh_fluid.restype = None
@@ -317,6 +323,25 @@ class RefSimulation:
         a = np.zeros((K + 1, J + 1, I + 1), np.float32)
         self.L.ref_get_node_friction(self.h, _p(a))
         return a
+
+    def set_surface_reconstruction(self, enable=True, subdivisions=1, smooth_value=0.5, smooth_iterations=2):
+        """Surface reconstruction on or off, with the mesher's settings
+        (the reference's defaults: subdivision 1, smoothing 0.5 x 2)."""
+        self.L.ref_set_surface_reconstruction(self.h, int(enable), int(subdivisions), float(smooth_value),
+                                              int(smooth_iterations))
+
+    def mesh_now(self):
+        """Mesh the current particles as the first substep of a frame does."""
+        self.L.ref_mesh_now(self.h)
+
+    def isomesh(self):
+        """getIsomesh(): (vertices (n, 3) float32, triangles (m, 3) int32)."""
+        nv, nt = C.c_int(), C.c_int()
+        self.L.ref_get_isomesh(self.h, C.byref(nv), C.byref(nt), None, None)
+        v = np.zeros((nv.value, 3), np.float32)
+        t = np.zeros((nt.value, 3), np.int32)
+        self.L.ref_get_isomesh(self.h, C.byref(nv), C.byref(nt), _p(v), _p(t))
+        return v, t
 
     def update_staged(self, dt):
         """One single-substep frame with the state between stages returned."""

@@ -55,10 +55,16 @@ def gpu(built):
     return True
 
 
+def surface_cases():
+    """Fixtures of the reference's surface meshes (iso_*.npz)."""
+    return sorted(p.stem for p in GOLDEN.glob("iso_*.npz"))
+
+
 def golden_cases(stages=False):
-    """Fixture names; with stages, only those holding the first frame stage
-    by stage (the fluid-mesh fixtures hold the particles after each frame)."""
-    names = sorted(p.stem for p in GOLDEN.glob("*.npz"))
+    """Fixture names of simulation states (not the surface meshes); with
+    stages, only those holding the first frame stage by stage (the
+    fluid-mesh fixtures hold the particles after each frame)."""
+    names = sorted(p.stem for p in GOLDEN.glob("*.npz") if not p.stem.startswith("iso_"))
     if stages:
         names = [n for n in names if json.loads(str(np.load(GOLDEN / f"{n}.npz")["meta"])).get("builder") != "mesh_fluid"]
     return names

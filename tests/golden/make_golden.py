@@ -44,6 +44,14 @@ MESH_FLUID_CASES = {
     "mf32_both": (dict(n=32, which="both"), 3, 4),
     "mf32_box_jitter": (dict(n=32, which="box", jitter_factor=None), 1, 4),
 }
+# surface meshes (getIsomesh): the reference's mesher run on the particles
+# after frame 1 at each subdivision level (default smoothing), and the mesh
+# the reference made during frame 1 itself at the last level
+SURFACE_CASES = {
+    "iso_dam16": ("dam_break", dict(n=16, seed=0), (1, 2), 1e-9),
+    "iso_dam24_box": ("dam_with_obstacles", dict(n=24, seed=3, which="box"), (2,), 1e-9),
+    "iso_mf32_box": ("mesh_fluid", dict(n=32, which="box"), (1, 2), None),
+}
 STAGE_KEYS = ("phi", "vu_p2g", "vv_p2g", "vw_p2g", "u_p2g", "v_p2g", "w_p2g", "pressure", "u_final", "v_final",
               "w_final", "vel_g2p", "pos_adv")
 
@@ -87,6 +95,28 @@ def make_mesh_fluid(name, kwargs, frames, threads):
           f"{(OUT / f'{name}.npz').stat().st_size / 1024:.0f} KB")
 
 
+def make_surface(name, builder, kwargs, levels, tol):
+    sc = getattr(scenes, builder)(**kwargs)
+    ref = RefSimulation(sc.isize, sc.jsize, sc.ksize, sc.dx, threads=1).setup(sc, tolerance=tol)
+    ref.set_surface_reconstruction(True, levels[-1])
+    ref.update(sc.frame_dt)
+    data = {"frame_verts": None, "frame_tris": None}
+    data["frame_verts"], data["frame_tris"] = ref.isomesh()
+    data["positions"], data["velocities"] = ref.particles()
+    for s in levels:
+        ref.set_surface_reconstruction(True, s)
+        ref.mesh_now()
+        data[f"verts_s{s}"], data[f"tris_s{s}"] = ref.isomesh()
+    meta = dict(scene=kwargs, builder=builder, levels=list(levels), tolerance=tol, dt=sc.frame_dt,
+                gravity=list(sc.gravity), pic_ratio=sc.pic_ratio, cfl=sc.cfl, smoothing=[0.5, 2],
+                substeps=int(ref.L.ref_frame_substeps(ref.h)),
+                source="jklae/FLIPEngine3D src/engine via oracle/build_ref.sh")
+    np.savez_compressed(OUT / f"{name}.npz", meta=np.array(json.dumps(meta)), **data)
+    print(name, "particles", data["positions"].shape[0],
+          {s: (len(data[f"verts_s{s}"]), len(data[f"tris_s{s}"])) for s in levels},
+          f"{(OUT / f'{name}.npz').stat().st_size / 1024:.0f} KB")
+
+
 if __name__ == "__main__":
     only = set(sys.argv[1:])   # names to (re)generate; all by default
     for name, (kw, frames, thr, tol) in CASES.items():
@@ -98,3 +128,6 @@ if __name__ == "__main__":
     for name, (kw, frames, thr) in MESH_FLUID_CASES.items():
         if not only or name in only:
             make_mesh_fluid(name, kw, frames, thr)
+    for name, (builder, kw, levels, tol) in SURFACE_CASES.items():
+        if not only or name in only:
+            make_surface(name, builder, kw, levels, tol)

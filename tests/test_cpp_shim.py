@@ -72,16 +72,17 @@ int main(int argc, char **argv) {
         float fr;
         if (std::fread(&nv, 4, 1, in) != 1 || std::fread(&nt, 4, 1, in) != 1 || std::fread(&fr, 4, 1, in) != 1) return 2;
         flip3d::TriangleMesh m;
-        m.vertices.resize(3 * (size_t)nv);
-        m.triangles.resize(3 * (size_t)nt);
-        if (std::fread(m.vertices.data(), 4, m.vertices.size(), in) != m.vertices.size() ||
-            std::fread(m.triangles.data(), 4, m.triangles.size(), in) != m.triangles.size())
+        m.vertices.resize((size_t)nv);
+        m.triangles.resize((size_t)nt);
+        if (std::fread(m.vertices.data(), 12, m.vertices.size(), in) != m.vertices.size() ||
+            std::fread(m.triangles.data(), 12, m.triangles.size(), in) != m.triangles.size())
             return 2;
         obstacles[q].updateMeshStatic(m);
         obstacles[q].setFriction(fr);
     }
     std::fclose(in);
     flip3d::FluidSimulation fluidsim(I, J, K, dx);
+    fluidsim.disableSurfaceReconstruction();
     fluidsim.setPICFLIPRatio(pic);
     fluidsim.addBodyForce(0.0, -9.81, 0.0);
     for (auto &o : obstacles) fluidsim.addMeshObstacle(&o);
@@ -180,7 +181,8 @@ def test_cpp_drop_in_with_a_mesh_obstacle_matches_the_reference(gpu, tmp_path):
 MESH_FLUID_DRIVER = r"""
 // FluidManager::initialize (src/FluidManager.cpp:47-68) verbatim in its
 // calls, on a 32^3 grid of dx 0.125 with the jitter factor at 0.001 (the
-// seeding jitter exactly zero), then three 1/30 s frames.
+// seeding jitter exactly zero), then three 1/30 s frames; the particles and
+// the surface mesh FluidManager draws (getIsomesh, :100-166) written out.
 #include <cstdio>
 #include <vector>
 #include "FluidSimulation.hpp"
@@ -189,22 +191,28 @@ int main(int argc, char **argv) {
     const int isize = 32, jsize = 32, ksize = 32;
     const double dx = 0.125;
     flip3d::FluidSimulation fluidsim(isize, jsize, ksize, dx);
+    fluidsim.setSurfaceSubdivisionLevel(2);
     double x, y, z;
     fluidsim.getSimulationDimensions(&x, &y, &z);
     double boxWidth = (1.0 / 3.0) * x, boxHeight = (1.0 / 3.0) * y, boxDepth = (1.0 / 3.0) * z;
     flip3d::vec3 p(0.5 * (x - boxWidth), 0.5 * (y - boxHeight), 0.5 * (z - boxDepth));
     // getTriangleMeshFromAABB (src/FluidManager.cpp:20-44)
+    std::vector<flip3d::vec3> verts{
+        flip3d::vec3(p.x, p.y, p.z),
+        flip3d::vec3(p.x + boxWidth, p.y, p.z),
+        flip3d::vec3(p.x + boxWidth, p.y, p.z + boxDepth),
+        flip3d::vec3(p.x, p.y, p.z + boxDepth),
+        flip3d::vec3(p.x, p.y + boxHeight, p.z),
+        flip3d::vec3(p.x + boxWidth, p.y + boxHeight, p.z),
+        flip3d::vec3(p.x + boxWidth, p.y + boxHeight, p.z + boxDepth),
+        flip3d::vec3(p.x, p.y + boxHeight, p.z + boxDepth)};
+    std::vector<flip3d::Triangle> tris{
+        flip3d::Triangle(0, 1, 2), flip3d::Triangle(0, 2, 3), flip3d::Triangle(4, 7, 6), flip3d::Triangle(4, 6, 5),
+        flip3d::Triangle(0, 3, 7), flip3d::Triangle(0, 7, 4), flip3d::Triangle(1, 5, 6), flip3d::Triangle(1, 6, 2),
+        flip3d::Triangle(0, 4, 5), flip3d::Triangle(0, 5, 1), flip3d::Triangle(3, 2, 6), flip3d::Triangle(3, 6, 7)};
     flip3d::TriangleMesh boxMesh;
-    boxMesh.vertices = {p.x, p.y, p.z,
-                        (float)(p.x + boxWidth), p.y, p.z,
-                        (float)(p.x + boxWidth), p.y, (float)(p.z + boxDepth),
-                        p.x, p.y, (float)(p.z + boxDepth),
-                        p.x, (float)(p.y + boxHeight), p.z,
-                        (float)(p.x + boxWidth), (float)(p.y + boxHeight), p.z,
-                        (float)(p.x + boxWidth), (float)(p.y + boxHeight), (float)(p.z + boxDepth),
-                        p.x, (float)(p.y + boxHeight), (float)(p.z + boxDepth)};
-    boxMesh.triangles = {0, 1, 2, 0, 2, 3, 4, 7, 6, 4, 6, 5, 0, 3, 7, 0, 7, 4,
-                         1, 5, 6, 1, 6, 2, 0, 4, 5, 0, 5, 1, 3, 2, 6, 3, 6, 7};
+    boxMesh.vertices = verts;
+    boxMesh.triangles = tris;
     flip3d::MeshObject boxFluidObject(isize, jsize, ksize, dx);
     boxFluidObject.updateMeshStatic(boxMesh);
     fluidsim.setMarkerParticleJitterFactor(0.001);
@@ -215,11 +223,19 @@ int main(int argc, char **argv) {
     unsigned int m = fluidsim.getNumMarkerParticles();
     std::vector<char> buf(12 * (size_t)m);
     fluidsim.getMarkerParticlePositionData(buf.data());
+    flip3d::TriangleMesh isomesh = fluidsim.getIsomesh();
     std::FILE *out = std::fopen(argv[1], "wb");
     std::fwrite(&m, 4, 1, out);
     std::fwrite(buf.data(), 1, buf.size(), out);
     std::fclose(out);
-    std::printf("%d %u\n", fluidsim.getCurrentFrame(), m);
+    out = std::fopen(argv[2], "wb");
+    unsigned int nv = (unsigned int)isomesh.vertices.size(), nt = (unsigned int)isomesh.triangles.size();
+    std::fwrite(&nv, 4, 1, out);
+    std::fwrite(&nt, 4, 1, out);
+    std::fwrite(isomesh.vertices.data(), 12, nv, out);
+    std::fwrite(isomesh.triangles.data(), 12, nt, out);
+    std::fclose(out);
+    std::printf("%d %u %u\n", fluidsim.getCurrentFrame(), m, nt);
     return 0;
 }
 """
@@ -227,9 +243,11 @@ int main(int argc, char **argv) {
 
 @pytest.mark.gpu
 def test_cpp_fluid_manager_initialize_matches_reference(gpu, tmp_path):
-    """FluidManager's own set-up through the C++ face: addMeshFluid of its
-    centred box, gravity -25, three 1/30 s frames; the particles are the
-    reference engine's (fixture mf32_box) within 1e-4."""
+    """FluidManager's own set-up through the C++ face: subdivision level 2,
+    addMeshFluid of its centred box, gravity -25, three 1/30 s frames; the
+    particles are the reference engine's (fixture mf32_box) within 1e-4, and
+    getIsomesh returns the mesh of the last frame, the one the Python face
+    returns for the same calls."""
     import numpy as np
     from conftest import load_golden, rel_err
     gxx = shutil.which("g++")
@@ -242,12 +260,32 @@ def test_cpp_fluid_manager_initialize_matches_reference(gpu, tmp_path):
     subprocess.run([gxx, "-std=c++17", "-O2", "-I", str(ROOT / "include"), str(src), "-o", str(exe),
                     "-L", str(libdir), "-lflip3d_gb300", f"-Wl,-rpath,{libdir}"], check=True)
     out = tmp_path / "positions.bin"
-    r = subprocess.run([str(exe), str(out)], capture_output=True, text=True, timeout=300)
+    mesh = tmp_path / "isomesh.bin"
+    r = subprocess.run([str(exe), str(out), str(mesh)], capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, (r.stdout, r.stderr)
-    frame, m = (int(v) for v in r.stdout.split())
-    assert frame == 3
+    frame, m, nt = (int(v) for v in r.stdout.split())
+    assert frame == 3 and nt > 0
     pos = np.fromfile(out, dtype=np.float32, offset=4).reshape(-1, 3)
     meta, g = load_golden("mf32_box")
     assert meta["scene"] == {"n": 32, "which": "box"}
     assert pos.shape == g["positions_3"].shape == (m, 3)
     assert rel_err(pos, g["positions_3"]) <= 1e-4
+    counts = np.fromfile(mesh, dtype=np.uint32, count=2)
+    verts = np.fromfile(mesh, dtype=np.float32, count=3 * int(counts[0]), offset=8).reshape(-1, 3)
+    tris = np.fromfile(mesh, dtype=np.int32, offset=8 + 12 * int(counts[0])).reshape(-1, 3)
+    assert len(tris) == nt
+    # the same sequence through the Python face gives the same mesh (the
+    # mesher's parity with the reference is tests/test_surface.py's)
+    from flipengine3d_gb300 import fluidsimulation as fs
+    from flipengine3d_gb300 import scenes
+    with fs.FluidSimulation(32, 32, 32, 0.125) as sim:
+        sim.setSurfaceSubdivisionLevel(2)
+        sim.setMarkerParticleJitterFactor(0.001)
+        sim.addMeshFluid(*scenes.fluid_manager_box(32, 0.125))
+        sim.addBodyForce(0.0, -25.0, 0.0)
+        sim.initialize()
+        for _ in range(3):
+            sim.update(1.0 / 30.0)
+        ov, ot = sim.getIsomesh()
+    assert np.array_equal(tris, ot) and np.array_equal(verts, ov)
+    assert (verts >= 0).all() and (verts <= 4.0).all()
