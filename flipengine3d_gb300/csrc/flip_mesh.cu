@@ -224,76 +224,128 @@ __global__ void __launch_bounds__(MESH_TPB) k_mesh_field(ParticleSoA p, const in
                                                          float *field) {
     __shared__ unsigned int smin[MB * MB * MB];
     __shared__ float npos[MB];
+    __shared__ float4 recs[MESH_TPB / 32][32];   // per warp: a pass's particles {lx, ly, lz, box}
     const int bx = blockIdx.x, by = blockIdx.y, bz = blockIdx.z;
     for (int q = threadIdx.x; q < MB * MB * MB; q += blockDim.x) smin[q] = 0x7f800000u;   // +inf
     if (threadIdx.x < MB) npos[threadIdx.x] = (float)((double)(float)threadIdx.x * m.subdx);
     __syncthreads();
     if (active[bx + m.cbI * (by + m.cbJ * bz)]) {
         // block frame (_scalarFieldProducerThread, particlemesher.cpp:498-549)
-        const float box = (float)((double)(float)bx * m.blockdx), boy = (float)((double)(float)by * m.blockdx),
-                    boz = (float)((double)(float)bz * m.blockdx);
-        // candidate cells: every particle that can reach one of this block's
-        // nodes, with a cell of margin for rounding
-        const double reach = (double)m.sr + 2.0 * m.subdx;
+        const float bofx = (float)((double)(float)bx * m.blockdx), bofy = (float)((double)(float)by * m.blockdx),
+                    bofz = (float)((double)(float)bz * m.blockdx);
+        // candidate cells: every particle whose search box can overlap the
+        // block (its list holds no other), with slack for rounding
+        const double reach = (double)m.sr + 0.01 * m.dx;
         const double lox = (double)m.offx + bx * m.blockdx - reach, hix = (double)m.offx + (bx + 1) * m.blockdx + reach;
         const double loy = (double)m.offy + by * m.blockdx - reach, hiy = (double)m.offy + (by + 1) * m.blockdx + reach;
         const double loz = (double)m.offz + bz * m.blockdx - reach, hiz = (double)m.offz + (bz + 1) * m.blockdx + reach;
-        const int x0 = max((int)floor(lox * m.invdx) - 1, 0), x1 = min((int)floor(hix * m.invdx) + 1, m.I - 1);
-        const int y0 = max((int)floor(loy * m.invdx) - 1, 0), y1 = min((int)floor(hiy * m.invdx) + 1, m.J - 1);
-        const int z0 = max((int)floor(loz * m.invdx) - 1, 0), z1 = min((int)floor(hiz * m.invdx) + 1, m.K - 1);
+        const int x0 = max((int)floor(lox * m.invdx), 0), x1 = min((int)floor(hix * m.invdx), m.I - 1);
+        const int y0 = max((int)floor(loy * m.invdx), 0), y1 = min((int)floor(hiy * m.invdx), m.J - 1);
+        const int z0 = max((int)floor(loz * m.invdx), 0), z1 = min((int)floor(hiz * m.invdx), m.K - 1);
         const int ny = y1 - y0 + 1, nrows = x1 >= x0 ? ny * (z1 - z0 + 1) : 0;
         const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
         const float sr = m.sr;
+        float4 *wrec = recs[warp];
+        // col / n = (col * ceil(2^11 / n)) >> 11, exact for n <= MB and
+        // col < n * MB; lane n holds the multiplier
+        const int divLane = lane > 0 ? (2048 + lane - 1) / lane : 0;
         for (int row = warp; row < nrows; row += nwarps) {
             const int cy = y0 + row % ny, cz = z0 + row / ny;
             const long long rbase = (long long)m.I * (cy + (long long)m.J * cz);
             const int pb = cellStart[rbase + x0], pe = cellStart[rbase + x1 + 1];
-            for (int t = pb + lane; t < pe; t += 32) {
-                const float px = p.px[t], py = p.py[t], pz = p.pz[t];
-                // the chunk's box, expanded (particlemesher.cpp:287-301, aabb.cpp:122-133)
-                if (!(px >= m.bbx && py >= m.bby && pz >= m.bbz && (double)px < (double)m.bbx + m.bbw &&
-                      (double)py < (double)m.bby + m.bbh && (double)pz < (double)m.bbz + m.bbd))
-                    continue;
-                const float cx = __fsub_rn(px, m.offx), cy2 = __fsub_rn(py, m.offy), cz2 = __fsub_rn(pz, m.offz);
-                // the count pass's block lists (particlemesher.cpp:400-446)
-                const int oi = exact_floor(cx, m.invBlockF, m.invBlockFf), oj = exact_floor(cy2, m.invBlockF, m.invBlockFf),
-                          ok = exact_floor(cz2, m.invBlockF, m.invBlockFf);
-                const float bpx = (float)((double)(float)oi * (double)m.blockdxF),
-                            bpy = (float)((double)(float)oj * (double)m.blockdxF),
-                            bpz = (float)((double)(float)ok * (double)m.blockdxF);
-                bool mine;
-                if (__fsub_rn(cx, sr) > bpx && __fsub_rn(cy2, sr) > bpy && __fsub_rn(cz2, sr) > bpz &&
-                    __fadd_rn(cx, sr) < __fadd_rn(bpx, m.blockdxF) && __fadd_rn(cy2, sr) < __fadd_rn(bpy, m.blockdxF) &&
-                    __fadd_rn(cz2, sr) < __fadd_rn(bpz, m.blockdxF)) {
-                    mine = oi == bx && oj == by && ok == bz;
-                } else {
-                    const int i0 = exact_floor(__fsub_rn(cx, sr), m.invBlockF, m.invBlockFf),
-                              i1 = exact_floor(__fadd_rn(cx, sr), m.invBlockF, m.invBlockFf);
-                    const int j0 = exact_floor(__fsub_rn(cy2, sr), m.invBlockF, m.invBlockFf),
-                              j1 = exact_floor(__fadd_rn(cy2, sr), m.invBlockF, m.invBlockFf);
-                    const int k0 = exact_floor(__fsub_rn(cz2, sr), m.invBlockF, m.invBlockFf),
-                              k1 = exact_floor(__fadd_rn(cz2, sr), m.invBlockF, m.invBlockFf);
-                    mine = bx >= i0 && bx <= i1 && by >= j0 && by <= j1 && bz >= k0 && bz <= k1;
-                }
-                if (!mine) continue;
-                const float lx = __fsub_rn(cx, box), ly = __fsub_rn(cy2, boy), lz = __fsub_rn(cz2, boz);
-                const int a0 = max(exact_floor(__fsub_rn(lx, sr), m.invsub, m.invsubf), 0);
-                const int b0 = max(exact_floor(__fsub_rn(ly, sr), m.invsub, m.invsubf), 0);
-                const int c0 = max(exact_floor(__fsub_rn(lz, sr), m.invsub, m.invsubf), 0);
-                const int a1 = min(exact_floor(__fadd_rn(lx, sr), m.invsub, m.invsubf) + 1, MB - 1);
-                const int b1 = min(exact_floor(__fadd_rn(ly, sr), m.invsub, m.invsubf) + 1, MB - 1);
-                const int c1 = min(exact_floor(__fadd_rn(lz, sr), m.invsub, m.invsubf) + 1, MB - 1);
-                for (int cc = c0; cc <= c1; cc++) {
-                    const float dz = __fsub_rn(npos[cc], lz), dz2 = __fmul_rn(dz, dz);
-                    for (int bb = b0; bb <= b1; bb++) {
-                        const float dy = __fsub_rn(npos[bb], ly), dy2 = __fmul_rn(dy, dy);
-                        unsigned int *row2 = &smin[MB * (bb + MB * cc)];
-                        for (int aa = a0; aa <= a1; aa++) {
-                            const float dx = __fsub_rn(npos[aa], lx);
-                            atomicMin(&row2[aa], __float_as_uint(__fadd_rn(__fadd_rn(__fmul_rn(dx, dx), dy2), dz2)));
+            for (int base = pb; base < pe; base += 32) {
+                // phase 1, a lane per particle: is it in this block's list,
+                // and which of the block's nodes does its box cover
+                const int t = base + lane;
+                int ncol = 0, na = 0;
+                float4 rec = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                unsigned packed = 0;
+                if (t < pe) {
+                    const float px = p.px[t], py = p.py[t], pz = p.pz[t];
+                    // the chunk's box, expanded (particlemesher.cpp:287-301, aabb.cpp:122-133)
+                    const bool in = px >= m.bbx && py >= m.bby && pz >= m.bbz && (double)px < (double)m.bbx + m.bbw &&
+                                    (double)py < (double)m.bby + m.bbh && (double)pz < (double)m.bbz + m.bbd;
+                    const float cx = __fsub_rn(px, m.offx), cy2 = __fsub_rn(py, m.offy), cz2 = __fsub_rn(pz, m.offz);
+                    // the count pass's block lists (particlemesher.cpp:400-446)
+                    const int oi = exact_floor(cx, m.invBlockF, m.invBlockFf),
+                              oj = exact_floor(cy2, m.invBlockF, m.invBlockFf),
+                              ok = exact_floor(cz2, m.invBlockF, m.invBlockFf);
+                    const float bpx = (float)((double)(float)oi * (double)m.blockdxF),
+                                bpy = (float)((double)(float)oj * (double)m.blockdxF),
+                                bpz = (float)((double)(float)ok * (double)m.blockdxF);
+                    bool mine;
+                    if (__fsub_rn(cx, sr) > bpx && __fsub_rn(cy2, sr) > bpy && __fsub_rn(cz2, sr) > bpz &&
+                        __fadd_rn(cx, sr) < __fadd_rn(bpx, m.blockdxF) &&
+                        __fadd_rn(cy2, sr) < __fadd_rn(bpy, m.blockdxF) &&
+                        __fadd_rn(cz2, sr) < __fadd_rn(bpz, m.blockdxF)) {
+                        mine = oi == bx && oj == by && ok == bz;
+                    } else {
+                        const int i0 = exact_floor(__fsub_rn(cx, sr), m.invBlockF, m.invBlockFf),
+                                  i1 = exact_floor(__fadd_rn(cx, sr), m.invBlockF, m.invBlockFf);
+                        const int j0 = exact_floor(__fsub_rn(cy2, sr), m.invBlockF, m.invBlockFf),
+                                  j1 = exact_floor(__fadd_rn(cy2, sr), m.invBlockF, m.invBlockFf);
+                        const int k0 = exact_floor(__fsub_rn(cz2, sr), m.invBlockF, m.invBlockFf),
+                                  k1 = exact_floor(__fadd_rn(cz2, sr), m.invBlockF, m.invBlockFf);
+                        mine = bx >= i0 && bx <= i1 && by >= j0 && by <= j1 && bz >= k0 && bz <= k1;
+                    }
+                    if (in && mine) {
+                        const float lx = __fsub_rn(cx, bofx), ly = __fsub_rn(cy2, bofy), lz = __fsub_rn(cz2, bofz);
+                        const int a0 = max(exact_floor(__fsub_rn(lx, sr), m.invsub, m.invsubf), 0);
+                        const int b0 = max(exact_floor(__fsub_rn(ly, sr), m.invsub, m.invsubf), 0);
+                        const int c0 = max(exact_floor(__fsub_rn(lz, sr), m.invsub, m.invsubf), 0);
+                        const int a1 = min(exact_floor(__fadd_rn(lx, sr), m.invsub, m.invsubf) + 1, MB - 1);
+                        const int b1 = min(exact_floor(__fadd_rn(ly, sr), m.invsub, m.invsubf) + 1, MB - 1);
+                        const int c1 = min(exact_floor(__fadd_rn(lz, sr), m.invsub, m.invsubf) + 1, MB - 1);
+                        if (a1 >= a0 && b1 >= b0 && c1 >= c0) {
+                            na = a1 - a0 + 1;
+                            ncol = na * (b1 - b0 + 1);
+                            packed = (unsigned)a0 | (unsigned)na << 4 | (unsigned)b0 << 8 | (unsigned)c0 << 12 |
+                                     (unsigned)c1 << 16;
+                            rec = make_float4(lx, ly, lz, 0.0f);
                         }
                     }
                 }
+                const unsigned div = (unsigned)__shfl_sync(0xffffffffu, divLane, na);
+                if (ncol > 0) {
+                    rec.w = __uint_as_float(packed | div << 20);
+                    wrec[lane] = rec;
+                }
+                int incl = ncol;   // inclusive prefix sum of the column counts over the lanes
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const int v = __shfl_up_sync(0xffffffffu, incl, o);
+                    if (lane >= o) incl += v;
+                }
+                const int total = __shfl_sync(0xffffffffu, incl, 31);
+                __syncwarp();
+                // phase 2, a lane per (particle, column of its box along k):
+                // the lanes of one step walk distinct columns
+                for (int first = 0; first < total; first += 32) {
+                    const int item = first + lane;
+                    int L = 0;   // the smallest lane whose inclusive sum exceeds item
+#pragma unroll
+                    for (int step = 16; step > 0; step >>= 1)
+                        if (__shfl_sync(0xffffffffu, incl, L + step - 1) <= item) L += step;
+                    const int startL = __shfl_sync(0xffffffffu, incl, L) - __shfl_sync(0xffffffffu, ncol, L);
+                    if (item < total) {
+                        const float4 pr = wrec[L];
+                        const unsigned w = __float_as_uint(pr.w);
+                        const int a0 = w & 15, nA = (w >> 4) & 15, b0 = (w >> 8) & 15;
+                        const int c0 = (w >> 12) & 15, c1 = (w >> 16) & 15;
+                        const int col = item - startL;
+                        const int bq = (col * (int)(w >> 20)) >> 11;   // col / nA
+                        const int aa = a0 + col - bq * nA, bb = b0 + bq;
+                        const float ddx = __fsub_rn(npos[aa], pr.x);
+                        const float dy = __fsub_rn(npos[bb], pr.y);
+                        const float dxy = __fadd_rn(__fmul_rn(ddx, ddx), __fmul_rn(dy, dy));
+                        unsigned int *dst = &smin[aa + MB * (bb + MB * c0)];
+                        for (int cc = c0; cc <= c1; cc++, dst += MB * MB) {
+                            const float dz = __fsub_rn(npos[cc], pr.z);
+                            atomicMin(dst, __float_as_uint(__fadd_rn(dxy, __fmul_rn(dz, dz))));
+                        }
+                    }
+                }
+                __syncwarp();
             }
         }
     }
