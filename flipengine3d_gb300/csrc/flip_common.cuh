@@ -72,6 +72,48 @@ __host__ __device__ __forceinline__ void unflatten(long long t, int ni, int nj, 
     k = (int)(q / b);
 }
 
+// The level set of a mesh fluid source over its sub-grid: ni x nj x nk
+// nodes, the first at (ox, oy, oz).
+struct SourceGridView {
+    const float *phi;
+    int ni, nj, nk;
+    float ox, oy, oz;
+    double dx;
+};
+// MeshLevelSet::trilinearInterpolate (meshlevelset.cpp:261-263, through
+// Interpolation::trilinearInterpolate, interpolation.cpp:61-113) at a point
+// in the grid's own frame: FP64 weights, corners outside the grid read 0,
+// the result rounded to float as the reference returns it.
+__device__ __forceinline__ float source_phi(const SourceGridView &g, float px, float py, float pz) {
+    const double inv = 1.0 / g.dx;
+    const int i = (int)floor((double)px * inv), j = (int)floor((double)py * inv), k = (int)floor((double)pz * inv);
+    const float gx = (float)((double)(float)i * g.dx), gy = (float)((double)(float)j * g.dx),
+                gz = (float)((double)(float)k * g.dx);
+    const double x = (double)__fsub_rn(px, gx) * inv, y = (double)__fsub_rn(py, gy) * inv,
+                 z = (double)__fsub_rn(pz, gz) * inv;
+    auto at = [&](int a, int b, int c) -> double {
+        return (a >= 0 && b >= 0 && c >= 0 && a < g.ni && b < g.nj && c < g.nk)
+                   ? (double)g.phi[(long long)a + (long long)g.ni * ((long long)b + (long long)g.nj * c)]
+                   : 0.0;
+    };
+    const double p0 = at(i, j, k), p1 = at(i + 1, j, k), p2 = at(i, j + 1, k), p3 = at(i, j, k + 1),
+                 p4 = at(i + 1, j, k + 1), p5 = at(i, j + 1, k + 1), p6 = at(i + 1, j + 1, k),
+                 p7 = at(i + 1, j + 1, k + 1);
+    return (float)(p0 * (1 - x) * (1 - y) * (1 - z) + p1 * x * (1 - y) * (1 - z) + p2 * (1 - x) * y * (1 - z) +
+                   p3 * (1 - x) * (1 - y) * z + p4 * x * (1 - y) * z + p5 * (1 - x) * y * z +
+                   p6 * x * y * (1 - z) + p7 * x * y * z);
+}
+// Inflow sources that constrain the fluid velocity, in registration order
+// (fluidsimulation.cpp:3372-3440, 4109-4170).  cellBits: per cell, bit s
+// set when the cell is one of source s's cells.
+constexpr int MAX_CONSTRAINED_INFLOWS = 8;
+struct InflowConstraint {
+    int count = 0;
+    const uint8_t *cellBits = nullptr;
+    SourceGridView g[MAX_CONSTRAINED_INFLOWS];
+    float vx[MAX_CONSTRAINED_INFLOWS], vy[MAX_CONSTRAINED_INFLOWS], vz[MAX_CONSTRAINED_INFLOWS];
+};
+
 // Count of kernel launches issued by this library (all contexts); each
 // launcher adds the number of kernels it enqueues.
 long long &launch_counter();

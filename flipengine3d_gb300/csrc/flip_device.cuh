@@ -44,7 +44,8 @@ struct StepConsts {
 // -- seeding from fluid meshes (flip_seed.cu); mask: one 8-bit sub-cell
 // mask per cell, four cells to a word; owner: 8 I J K words, all ones
 void launch_mask_particles(const ParticleSoA &p, int n, const StepConsts &c, unsigned int *mask, cudaStream_t s);
-void launch_seed_candidates(const StepConsts &c, const int *cells, long long ncells, const float *meshPhi,
+// meshPhi: the mesh's level set, sampled at p minus its first node's position
+void launch_seed_candidates(const StepConsts &c, const int *cells, long long ncells, const SourceGridView &meshPhi,
                             const float *solidPhi, double jitter, bool jitterSurface, unsigned long long seed,
                             const unsigned int *mask, float4 *cand, unsigned int *owner, int *keep, cudaStream_t s);
 void launch_seed_scatter(const StepConsts &c, long long ncand, const float4 *cand, const int *keep, const int *rank,
@@ -70,7 +71,8 @@ void launch_p2g(const ParticleSoA &p, const int *cellStart, const StepConsts &c,
 void launch_extrapolate(const StepConsts &c, float *u, float *v, float *w, const uint8_t *vu, const uint8_t *vv,
                         const uint8_t *vw, uint8_t *status, int layers, cudaStream_t s);
 void launch_save_and_force(const StepConsts &c, float *u, float *v, float *w, float *su, float *sv, float *sw,
-                           float fx, float fy, float fz, bool ax, bool ay, bool az, cudaStream_t s);
+                           float fx, float fy, float fz, bool ax, bool ay, bool az, const uint8_t *ex,
+                           cudaStream_t s);
 void launch_constrain(const StepConsts &c, float *u, float *v, float *w, float *su, float *sv, float *sw,
                       const float *wu, const float *wv, const float *ww, const float *fu, const float *fv,
                       const float *fw, cudaStream_t s);
@@ -79,7 +81,20 @@ void launch_constrain(const StepConsts &c, float *u, float *v, float *w, float *
 void launch_advect(ParticleSoA p, int n, const StepConsts &c, const float *u, const float *v, const float *w,
                    const float *su, const float *sv, const float *sw, const float *solidPhi,
                    const uint8_t *nearSolid, float picRatio, float flipRatio, double dt, unsigned int *keys,
-                   unsigned int *speedHist, double speedStep, cudaStream_t s);
+                   unsigned int *speedHist, double speedStep, const InflowConstraint &ic, cudaStream_t s);
+
+// -- mesh fluid sources (flip_sources.cu)
+// Faces (u, v, w, one byte each) that enabled inflow sources constraining the
+// fluid velocity keep out of the body force: P2G-valid faces where a
+// source's level set, read at the face's position in its own frame, is
+// negative (fluidsimulation.cpp:3372-3440).
+void launch_inflow_faces(const StepConsts &c, const InflowConstraint &ic, const uint8_t *vu, const uint8_t *vv,
+                         const uint8_t *vw, uint8_t *ex, cudaStream_t s);
+// Outflow (fluidsimulation.cpp:4608-4650): particles in the source's cells
+// (or outside them, inversed) where its level set at p - offset is negative
+// (non-negative, inversed) are flagged for removal in keys.
+void launch_outflow_mark(const ParticleSoA &p, int n, const StepConsts &c, const uint8_t *cellMask, int inversed,
+                         const SourceGridView &g, unsigned int *keys, cudaStream_t s);
 void launch_speed_limit(const unsigned int *hist, int n, int bins, double speedStep, double maxPct, int maxAbs,
                         float *maxSpeedSq, cudaStream_t s);
 void launch_mark_fast(const ParticleSoA &p, int n, const float *maxSpeedSq, unsigned int *keys, cudaStream_t s);
@@ -324,4 +339,6 @@ int record_error(int code, const std::string &msg);   // sets flip_last_error()
 // scan_scratch_ints(idSpace) ints.
 void launch_readback_order(const ParticleSoA &p, int n, int idSpace, int *flags, int *rank, int *scratch,
                            int *total, float *pos, float *vel, cudaStream_t s);
+void launch_compact_ids(const ParticleSoA &p, int n, int idSpace, int *flags, int *rank, int *scratch, int *total,
+                        cudaStream_t s);
 }  // namespace flip

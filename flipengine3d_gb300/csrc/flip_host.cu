@@ -90,6 +90,23 @@ struct flip_ctx {
         float vx, vy, vz;
     };
     std::vector<FluidMesh> fluidQueue;
+    // mesh fluid sources (addMeshFluidSource), static meshes
+    struct FluidSource {
+        int id = 0;
+        std::vector<float> verts;
+        std::vector<int> tris;
+        flip_fluid_source_params prm{};
+        SourceGrid grid;           // host set-up, once
+        bool built = false;
+        float *dphi = nullptr;     // the level set on the device
+        int *dcells = nullptr;     // the cells, ascending
+        uint8_t *dmask = nullptr;  // one byte per grid cell: 1 for the source's cells
+    };
+    std::vector<FluidSource> sources;
+    int nextSourceId = 0;
+    uint8_t *inflowFaces = nullptr;      // faces kept out of the body force (u, v, w)
+    uint8_t *inflowCellBits = nullptr;   // per cell: bit q for constraining inflow q
+    std::vector<int> cellBitsIds;        // the sources inflowCellBits was built for, in order
     double jitterFactor = 0.0;      // _markerParticleJitterFactor
     bool jitterSurface = false;     // _isJitterSurfaceMarkerParticlesEnabled
     unsigned long long seedCalls = 0;
@@ -318,6 +335,9 @@ int rebin(flip_ctx *x);
 // particles after initialize; the stream is idle when this is called).
 int grow_particles(flip_ctx *x, int cap) {
     if (cap <= x->capacity) return FLIP_OK;
+    // a quarter more than asked for, so that steady emission grows the
+    // storage rarely
+    cap = (int)std::min<long long>(std::max<long long>(cap, (long long)x->capacity * 5 / 4), 0x7ffffff0LL);
     ParticleSoA keep = x->pa;
     const int oldCap = x->capacity;
     void *old[] = {x->pa.px, x->pb.px, x->keys, x->slots, x->idFlags, x->idRank, x->idScratch, x->idTotal};
@@ -334,26 +354,129 @@ int grow_particles(flip_ctx *x, int cap) {
     return FLIP_OK;
 }
 
-// Fill the queued fluid meshes (_updateAddedFluidMeshObjectQueue,
-// fluidsimulation.cpp:4724-4759) after a substep: the cells and level set of
-// each mesh on the host, the particles on the device (flip_seed.cu), then
-// one binning of all particles.
-int seed_fluid_meshes(flip_ctx *x) {
-    if (x->fluidQueue.empty()) return FLIP_OK;
+// The device copies of each source's set-up (cells, level set), made once.
+int prepare_sources(flip_ctx *x) {
+    for (auto &src : x->sources) {
+        if (src.built) continue;
+        fluid_source_setup(x->I, x->J, x->K, x->dx, src.verts, src.tris, src.grid);
+        int rc;
+        if ((rc = x->alloc(&src.dphi, src.grid.phi.size())) || (rc = x->alloc(&src.dcells, src.grid.cells.size())) ||
+            (rc = x->alloc(&src.dmask, (size_t)x->nc())))
+            return rc;
+        std::vector<uint8_t> mask((size_t)x->nc(), 0);
+        for (int q : src.grid.cells) mask[q] = 1;
+        CK(cudaMemcpy(src.dphi, src.grid.phi.data(), src.grid.phi.size() * 4, cudaMemcpyHostToDevice));
+        if (!src.grid.cells.empty())
+            CK(cudaMemcpy(src.dcells, src.grid.cells.data(), src.grid.cells.size() * 4, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(src.dmask, mask.data(), mask.size(), cudaMemcpyHostToDevice));
+        src.built = true;
+    }
+    return FLIP_OK;
+}
+
+SourceGridView source_view(const flip_ctx *x, const flip_ctx::FluidSource &src) {
+    SourceGridView g;
+    g.phi = src.dphi;
+    g.ni = src.grid.nodes[0];
+    g.nj = src.grid.nodes[1];
+    g.nk = src.grid.nodes[2];
+    g.ox = src.grid.offset[0];
+    g.oy = src.grid.offset[1];
+    g.oz = src.grid.offset[2];
+    g.dx = x->dx;
+    return g;
+}
+
+// The enabled inflow sources that constrain the fluid velocity, in
+// registration order, with the per-cell bits of their cells.
+int inflow_constraint(flip_ctx *x, InflowConstraint *ic) {
+    *ic = InflowConstraint{};
+    std::vector<int> ids;
+    for (auto &src : x->sources)
+        if (src.prm.enabled && src.prm.inflow && src.prm.constrained_velocity) ids.push_back(src.id);
+    if (ids.empty()) return FLIP_OK;
+    int rc;
+    if ((rc = prepare_sources(x))) return rc;
+    if (!x->inflowFaces && (rc = x->alloc(&x->inflowFaces, (size_t)(x->nu() + x->nv() + x->nw())))) return rc;
+    if (!x->inflowCellBits && (rc = x->alloc(&x->inflowCellBits, (size_t)x->nc()))) return rc;
+    if (ids != x->cellBitsIds) {
+        std::vector<uint8_t> bits((size_t)x->nc(), 0);
+        int q = 0;
+        for (auto &src : x->sources)
+            if (src.prm.enabled && src.prm.inflow && src.prm.constrained_velocity) {
+                for (int cell : src.grid.cells) bits[cell] |= (uint8_t)(1u << q);
+                q++;
+            }
+        CK(cudaMemcpyAsync(x->inflowCellBits, bits.data(), bits.size(), cudaMemcpyHostToDevice, x->stream));
+        CK(cudaStreamSynchronize(x->stream));
+        x->cellBitsIds = ids;
+    }
+    ic->cellBits = x->inflowCellBits;
+    for (auto &src : x->sources)
+        if (src.prm.enabled && src.prm.inflow && src.prm.constrained_velocity) {
+            const int q = ic->count++;
+            ic->g[q] = source_view(x, src);
+            ic->vx[q] = (float)src.prm.velocity[0];
+            ic->vy[q] = (float)src.prm.velocity[1];
+            ic->vz[q] = (float)src.prm.velocity[2];
+        }
+    return FLIP_OK;
+}
+
+// _updateFluidObjects (fluidsimulation.cpp:4794-4806) after a substep: the
+// queued fluid meshes (_updateAddedFluidMeshObjectQueue, :4724-4759), then
+// the inflow sources' emission (_updateInflowMeshFluidSources, :4676-4698,
+// 4564-4606) and the outflow sources' removal (_updateOutflowMeshFluidSources,
+// :4700-4717, 4608-4674).  Cells and level sets come from the host set-up;
+// particles are seeded on the device (flip_seed.cu) into one sub-cell mask
+// shared by every emission, outflow removal flags the particles in their
+// keys, and one binning orders everything.
+int update_fluid_objects(flip_ctx *x) {
+    int rc;
+    std::vector<const flip_ctx::FluidSource *> emit;
+    bool outflow = false;
+    for (auto &src : x->sources) {
+        if (!src.prm.enabled) continue;
+        if (!src.prm.inflow) {
+            outflow = outflow || src.prm.fluid_outflow;
+            continue;
+        }
+        int e = src.prm.substep_emissions;
+        if (e == 0) {   // only at a frame's first substep
+            if (x->stepNumber != 0) continue;
+            e = 1;
+        }
+        for (int q = 0; q < e; q++) emit.push_back(&src);
+    }
+    if (x->fluidQueue.empty() && emit.empty() && !outflow) return FLIP_OK;
+    if ((rc = prepare_sources(x))) return rc;
     cudaStream_t s = x->stream;
     const long long nc = x->nc();
     std::vector<std::vector<int>> cells(x->fluidQueue.size());
     std::vector<std::vector<float>> phi(x->fluidQueue.size());
-    long long ncand = 0, maxCand = 0;
+    long long ncand = 0, maxCand = 0, queueCand = 0;
     for (size_t m = 0; m < x->fluidQueue.size(); m++) {
         mesh_fluid_cells(x->I, x->J, x->K, x->dx, x->fluidQueue[m].verts, x->fluidQueue[m].tris, cells[m], phi[m]);
         ncand += 8 * (long long)cells[m].size();
-        maxCand = std::max(maxCand, 8 * (long long)cells[m].size());
+        queueCand = std::max(queueCand, 8 * (long long)cells[m].size());
     }
-    if ((long long)x->idNext + ncand >= 0x7fffffffLL) return fail(FLIP_E_OUT_OF_RANGE, "too many particles");
-    int rc;
-    if ((rc = grow_particles(x, std::max(x->capacity, (int)(x->idNext + ncand))))) return rc;
-    // scratch of this call only: seeding runs once per added mesh
+    maxCand = queueCand;
+    for (const auto *src : emit) {
+        ncand += 8 * (long long)src->grid.cells.size();
+        maxCand = std::max(maxCand, 8 * (long long)src->grid.cells.size());
+    }
+    if ((long long)x->n + ncand >= 0x7fffffffLL || (long long)x->idNext + ncand >= 0x7fffffffLL)
+        return fail(FLIP_E_OUT_OF_RANGE, "too many particles");
+    if (ncand > 0) {
+        // ids are ranks below the id space, which is the storage's capacity:
+        // once emission and removal have spread them out, renumber them
+        if ((long long)x->idNext + ncand > x->capacity && x->idNext > (unsigned int)x->n) {
+            launch_compact_ids(x->pa, x->n, x->idSpace, x->idFlags, x->idRank, x->idScratch, x->idTotal, s);
+            x->idNext = (unsigned int)x->n;
+        }
+        if ((rc = grow_particles(x, std::max(x->capacity, (int)(x->idNext + ncand))))) return rc;
+    }
+    // scratch of this call only
     struct Scratch {
         std::vector<void *> p;
         ~Scratch() { for (void *q : p) cudaFree(q); }
@@ -363,39 +486,62 @@ int seed_fluid_meshes(flip_ctx *x) {
         sc.p.push_back((void *)*ptr);
         return true;
     };
-    unsigned int *mask, *owner;
-    float4 *cand;
-    int *dcells, *keep, *rank, *scratch, *total;
-    float *dphi;
-    const long long nphi = (long long)(x->I + 1) * (x->J + 1) * (x->K + 1);
-    if (!get(&mask, (nc + 3) / 4) || !get(&owner, 8 * nc) || !get(&cand, maxCand) || !get(&dcells, maxCand / 8) ||
-        !get(&keep, maxCand) || !get(&rank, maxCand + 1) || !get(&scratch, scan_scratch_ints((int)maxCand) + 4) ||
-        !get(&total, 4) || !get(&dphi, nphi))
-        return fail(FLIP_E_NOMEM, "cudaMalloc failed (seeding)");
-    CK(cudaMemsetAsync(mask, 0, (size_t)((nc + 3) / 4) * 4, s));
-    launch_mask_particles(x->pa, x->n, x->c, mask, s);
-    const double jitter = 0.25 * (x->jitterFactor - 1e-3) * x->dx;   // _getMarkerParticleJitter
-    for (size_t m = 0; m < x->fluidQueue.size(); m++) {
-        const long long nm = 8 * (long long)cells[m].size();
-        if (nm == 0) continue;
-        const auto &fm = x->fluidQueue[m];
-        CK(cudaMemcpyAsync(dcells, cells[m].data(), cells[m].size() * 4, cudaMemcpyHostToDevice, s));
-        CK(cudaMemcpyAsync(dphi, phi[m].data(), (size_t)nphi * 4, cudaMemcpyHostToDevice, s));
-        CK(cudaMemsetAsync(owner, 0xff, (size_t)(8 * nc) * 4, s));
-        const unsigned long long seed = 0x5eed5eed5eed5eedull ^ (++x->seedCalls * 0x2545f4914f6cdd1dull);
-        launch_seed_candidates(x->c, dcells, (long long)cells[m].size(), dphi, x->solidPhi, jitter, x->jitterSurface,
-                               seed, mask, cand, owner, keep, s);
-        launch_scan_cells(keep, (int)nm, rank, scratch, total, s);
-        CK(cudaMemcpyAsync(&x->mail->total, total, sizeof(int), cudaMemcpyDeviceToHost, s));
-        if ((rc = sync(x))) return rc;   // the cells and level set buffers are reused for the next mesh
-        const int added = x->mail->total;
-        launch_seed_scatter(x->c, nm, cand, keep, rank, x->pa, x->n, x->idNext, fm.vx, fm.vy, fm.vz, mask, s);
-        x->n += added;
-        x->idNext += (unsigned int)added;
+    if (ncand > 0) {
+        unsigned int *mask, *owner;
+        float4 *cand;
+        int *dcells, *keep, *rank, *scratch, *total;
+        float *dphi = nullptr;
+        const long long nphi = (long long)(x->I + 1) * (x->J + 1) * (x->K + 1);
+        if (!get(&mask, (nc + 3) / 4) || !get(&owner, 8 * nc) || !get(&cand, maxCand) ||
+            !get(&dcells, queueCand / 8) || !get(&keep, maxCand) || !get(&rank, maxCand + 1) ||
+            !get(&scratch, scan_scratch_ints((int)maxCand) + 4) || !get(&total, 4) ||
+            (!x->fluidQueue.empty() && !get(&dphi, nphi)))
+            return fail(FLIP_E_NOMEM, "cudaMalloc failed (seeding)");
+        CK(cudaMemsetAsync(mask, 0, (size_t)((nc + 3) / 4) * 4, s));
+        launch_mask_particles(x->pa, x->n, x->c, mask, s);
+        const double jitter = 0.25 * (x->jitterFactor - 1e-3) * x->dx;   // _getMarkerParticleJitter
+        const size_t jobs = x->fluidQueue.size() + emit.size();
+        for (size_t m = 0; m < jobs; m++) {
+            const bool queued = m < x->fluidQueue.size();
+            const flip_ctx::FluidSource *src = queued ? nullptr : emit[m - x->fluidQueue.size()];
+            const long long ncells = queued ? (long long)cells[m].size() : (long long)src->grid.cells.size();
+            const long long nm = 8 * ncells;
+            if (nm == 0) continue;
+            SourceGridView g;
+            const int *dc;
+            float vx, vy, vz;
+            if (queued) {
+                const auto &fm = x->fluidQueue[m];
+                CK(cudaMemcpyAsync(dcells, cells[m].data(), cells[m].size() * 4, cudaMemcpyHostToDevice, s));
+                CK(cudaMemcpyAsync(dphi, phi[m].data(), (size_t)nphi * 4, cudaMemcpyHostToDevice, s));
+                g = SourceGridView{dphi, x->I + 1, x->J + 1, x->K + 1, 0.0f, 0.0f, 0.0f, x->dx};
+                dc = dcells;
+                vx = fm.vx; vy = fm.vy; vz = fm.vz;
+            } else {
+                g = source_view(x, *src);
+                dc = src->dcells;
+                vx = (float)src->prm.velocity[0]; vy = (float)src->prm.velocity[1]; vz = (float)src->prm.velocity[2];
+            }
+            CK(cudaMemsetAsync(owner, 0xff, (size_t)(8 * nc) * 4, s));
+            const unsigned long long seed = 0x5eed5eed5eed5eedull ^ (++x->seedCalls * 0x2545f4914f6cdd1dull);
+            launch_seed_candidates(x->c, dc, ncells, g, x->solidPhi, jitter, x->jitterSurface, seed, mask, cand,
+                                   owner, keep, s);
+            launch_scan_cells(keep, (int)nm, rank, scratch, total, s);
+            CK(cudaMemcpyAsync(&x->mail->total, total, sizeof(int), cudaMemcpyDeviceToHost, s));
+            if ((rc = sync(x))) return rc;   // the cells and level set buffers are reused for the next mesh
+            const int added = x->mail->total;
+            launch_seed_scatter(x->c, nm, cand, keep, rank, x->pa, x->n, x->idNext, vx, vy, vz, mask, s);
+            x->n += added;
+            x->idNext += (unsigned int)added;
+        }
     }
     x->fluidQueue.clear();
-    // bin everything (every particle kept, as loading does)
+    // bin everything (every particle kept, as loading does), less the outflows
     launch_keys_from_positions(x->pa, x->n, x->c, x->keys, s);
+    for (auto &src : x->sources)
+        if (src.prm.enabled && !src.prm.inflow && src.prm.fluid_outflow)
+            launch_outflow_mark(x->pa, x->n, x->c, src.dmask, src.prm.outflow_inversed ? 1 : 0, source_view(x, src),
+                                x->keys, s);
     const int saveMax = x->maxPerCell;
     x->maxPerCell = 0x7fffffff;
     rc = rebin(x);
@@ -595,8 +741,13 @@ int step_fluid(flip_ctx *x, double dt, flip_stage_dump *d) {
     x->mark(FLIP_STAGE_FORCE);
     float3 bf = body_force(x);
     const float feps = 1e-6f;
+    // inflow sources that constrain the fluid velocity keep the force off their faces
+    InflowConstraint ic;
+    if ((rc = inflow_constraint(x, &ic))) return rc;
+    if (ic.count) launch_inflow_faces(c, ic, x->vu, x->vv, x->vw, x->inflowFaces, s);
     launch_save_and_force(c, x->u, x->v, x->w, x->su, x->sv, x->sw, (float)(bf.x * dt), (float)(bf.y * dt),
-                          (float)(bf.z * dt), std::fabs(bf.x) > feps, std::fabs(bf.y) > feps, std::fabs(bf.z) > feps, s);
+                          (float)(bf.z * dt), std::fabs(bf.x) > feps, std::fabs(bf.y) > feps, std::fabs(bf.z) > feps,
+                          ic.count ? x->inflowFaces : nullptr, s);
     if (d && (rc = dump_mac(x, d->u_force, d->v_force, d->w_force, x->u, x->v, x->w))) return rc;
     // pressure (fluidsimulation.cpp:3732-3773)
     if (!x->solidBuilt) {
@@ -623,14 +774,14 @@ int step_fluid(flip_ctx *x, double dt, flip_stage_dump *d) {
         x->mark(FLIP_STAGE_BINNING);
         x->mark(FLIP_NUM_STAGES);
         if ((rc = collect_stage_times(x))) return rc;
-        return seed_fluid_meshes(x);   // _updateFluidObjects (fluidsimulation.cpp:5505)
+        return update_fluid_objects(x);   // _updateFluidObjects (fluidsimulation.cpp:5505)
     }
     // particle velocities, advection, removal (fluidsimulation.cpp:4172-4390)
     x->mark(FLIP_STAGE_ADVECT);
     double speedStep = x->cfl * x->dx / x->frameDt;
     CK(cudaMemsetAsync(x->speedHist, 0, 8 * sizeof(unsigned int), s));
     launch_advect(x->pa, x->n, c, x->u, x->v, x->w, x->su, x->sv, x->sw, x->solidPhi, x->nearSolid,
-                  (float)x->picRatio, (float)(1 - x->picRatio), dt, x->keys, x->speedHist, speedStep, s);
+                  (float)x->picRatio, (float)(1 - x->picRatio), dt, x->keys, x->speedHist, speedStep, ic, s);
     if (d && (d->vel_g2p || d->pos_adv)) {
         std::vector<float> pos, vel;
         if ((rc = particles_in_order(x, &pos, &vel))) return rc;
@@ -644,7 +795,7 @@ int step_fluid(flip_ctx *x, double dt, flip_stage_dump *d) {
     rc = rebin_marked(x);
     if (rc) return rc;
     if ((rc = collect_stage_times(x))) return rc;
-    return seed_fluid_meshes(x);   // _updateFluidObjects (fluidsimulation.cpp:5505)
+    return update_fluid_objects(x);   // _updateFluidObjects (fluidsimulation.cpp:5505)
 }
 
 // The surface mesh of the current particles (_launchOutputSurfaceMeshThread
@@ -679,6 +830,11 @@ double next_time_step(flip_ctx *x, double dt) {
         maxu = 0.0;
         for (const auto &fm : x->fluidQueue)
             maxu = std::fmax((double)std::sqrt(fm.vx * fm.vx + fm.vy * fm.vy + fm.vz * fm.vz), maxu);
+        for (const auto &src : x->sources) {   // enabled inflow sources (:5537-5546)
+            if (!src.prm.enabled || !src.prm.inflow) continue;
+            const float vx = (float)src.prm.velocity[0], vy = (float)src.prm.velocity[1], vz = (float)src.prm.velocity[2];
+            maxu = std::fmax((double)std::sqrt(vx * vx + vy * vy + vz * vz), maxu);
+        }
         float3 bf = body_force(x);
         float len = std::sqrt(bf.x * bf.x + bf.y * bf.y + bf.z * bf.z);
         maxu += len * dt;
@@ -1278,6 +1434,107 @@ int flip_estimate_device_bytes(int isize, int jsize, int ksize, int particles, l
 int flip_get_launch_count(flip_ctx *x, long long *count) {
     if (!x || !count) return FLIP_E_NULL;
     *count = x->launches;
+    return FLIP_OK;
+}
+
+static flip_fluid_source_params default_source_params() {
+    flip_fluid_source_params p{};
+    p.inflow = 1;
+    p.enabled = 1;
+    p.substep_emissions = 1;
+    p.constrained_velocity = 1;
+    p.fluid_outflow = 1;
+    p.outflow_inversed = 0;
+    return p;
+}
+static int check_source_params(const flip_fluid_source_params *p) {
+    for (double v : p->velocity)
+        if (!std::isfinite(v)) return fail(FLIP_E_DOMAIN, "Error: fluid source velocity must be finite.");
+    return FLIP_OK;
+}
+static flip_ctx::FluidSource *find_source(flip_ctx *x, int id) {
+    for (auto &src : x->sources)
+        if (src.id == id) return &src;
+    return nullptr;
+}
+int flip_add_mesh_fluid_source(flip_ctx *x, int nverts, const float *verts, int ntris, const int *tris,
+                               const flip_fluid_source_params *params, int *id) {
+    if (!x || !id) return FLIP_E_NULL;
+    std::vector<MeshObstacle> ms;
+    int rc = obstacles_from_arrays(1, &nverts, verts, &ntris, tris, nullptr, ms);
+    if (rc) return rc;
+    MeshObstacle &m = ms[0];
+    flip_fluid_source_params p = params ? *params : default_source_params();
+    if ((rc = check_source_params(&p))) return rc;
+    if (p.substep_emissions < 0) p.substep_emissions = 0;   // MeshFluidSource::setSubstepEmissions
+    int constraining = 0;
+    for (auto &src : x->sources) constraining += src.prm.inflow && src.prm.constrained_velocity;
+    if (p.inflow && p.constrained_velocity && constraining >= MAX_CONSTRAINED_INFLOWS)
+        return fail(FLIP_E_DOMAIN, "at most 8 inflow sources may constrain the fluid velocity");
+    flip_ctx::FluidSource src;
+    src.id = x->nextSourceId++;
+    src.verts = std::move(m.verts);
+    src.tris = std::move(m.tris);
+    src.prm = p;
+    x->sources.push_back(std::move(src));
+    *id = x->sources.back().id;
+    return FLIP_OK;
+}
+int flip_set_mesh_fluid_source_params(flip_ctx *x, int id, const flip_fluid_source_params *params) {
+    if (!x || !params) return FLIP_E_NULL;
+    flip_ctx::FluidSource *src = find_source(x, id);
+    if (!src) return fail(FLIP_E_DOMAIN, "no mesh fluid source with this id");
+    int rc = check_source_params(params);
+    if (rc) return rc;
+    flip_fluid_source_params p = *params;
+    if (p.substep_emissions < 0) p.substep_emissions = 0;
+    if (p.inflow && p.constrained_velocity && !(src->prm.inflow && src->prm.constrained_velocity)) {
+        int constraining = 0;
+        for (auto &o : x->sources) constraining += o.prm.inflow && o.prm.constrained_velocity;
+        if (constraining >= MAX_CONSTRAINED_INFLOWS)
+            return fail(FLIP_E_DOMAIN, "at most 8 inflow sources may constrain the fluid velocity");
+    }
+    src->prm = p;
+    return FLIP_OK;
+}
+int flip_get_mesh_fluid_source_params(flip_ctx *x, int id, flip_fluid_source_params *params) {
+    if (!x || !params) return FLIP_E_NULL;
+    flip_ctx::FluidSource *src = find_source(x, id);
+    if (!src) return fail(FLIP_E_DOMAIN, "no mesh fluid source with this id");
+    *params = src->prm;
+    return FLIP_OK;
+}
+int flip_remove_mesh_fluid_source(flip_ctx *x, int id) {
+    if (!x) return FLIP_E_NULL;
+    for (size_t q = 0; q < x->sources.size(); q++)
+        if (x->sources[q].id == id) {
+            cudaStreamSynchronize(x->stream);
+            x->release(x->sources[q].dphi);
+            x->release(x->sources[q].dcells);
+            x->release(x->sources[q].dmask);
+            x->sources.erase(x->sources.begin() + q);
+            x->cellBitsIds.clear();
+            return FLIP_OK;
+        }
+    return fail(FLIP_E_DOMAIN, "no mesh fluid source with this id");
+}
+int flip_fluid_source_setup(int isize, int jsize, int ksize, double dx, int nverts, const float *verts, int ntris,
+                            const int *tris, int *nodes, float *offset, float *phi, int *ncells, int *cells) {
+    if (isize <= 0 || jsize <= 0 || ksize <= 0 || !(dx > 0.0)) return fail(FLIP_E_DOMAIN, "bad grid");
+    if (!nodes || !offset || !ncells) return FLIP_E_NULL;
+    std::vector<MeshObstacle> ms;
+    int rc = obstacles_from_arrays(1, &nverts, verts, &ntris, tris, nullptr, ms);
+    if (rc) return rc;
+    const MeshObstacle &m = ms[0];
+    SourceGrid g;
+    fluid_source_setup(isize, jsize, ksize, dx, m.verts, m.tris, g);
+    for (int a = 0; a < 3; a++) {
+        nodes[a] = g.nodes[a];
+        offset[a] = g.offset[a];
+    }
+    *ncells = (int)g.cells.size();
+    if (phi) std::memcpy(phi, g.phi.data(), g.phi.size() * sizeof(float));
+    if (cells) std::memcpy(cells, g.cells.data(), g.cells.size() * sizeof(int));
     return FLIP_OK;
 }
 

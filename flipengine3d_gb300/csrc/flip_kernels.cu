@@ -476,15 +476,19 @@ __global__ void k_extrap_layer(StepConsts c, float *u, float *v, float *w, uint8
 }
 
 // -------------------------------------------------- save + body force, constrain
+// `ex` (optional, one byte per face over u, v, w): faces an inflow source
+// constrains, which the body force skips (fluidsimulation.cpp:3450-3489).
 __global__ void k_save_force(long long nu, long long nv, long long nw, float *u, float *v, float *w, float *su,
-                             float *sv, float *sw, float fx, float fy, float fz, int ax, int ay, int az) {
+                             float *sv, float *sw, float fx, float fy, float fz, int ax, int ay, int az,
+                             const uint8_t *ex) {
     long long f = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const bool skip = ex && f < nu + nv + nw && ex[f];
     if (f < nu) {
-        float x = u[f]; su[f] = x; if (ax) u[f] = __fadd_rn(x, fx);
+        float x = u[f]; su[f] = x; if (ax && !skip) u[f] = __fadd_rn(x, fx);
     } else if (f < nu + nv) {
-        long long l = f - nu; float x = v[l]; sv[l] = x; if (ay) v[l] = __fadd_rn(x, fy);
+        long long l = f - nu; float x = v[l]; sv[l] = x; if (ay && !skip) v[l] = __fadd_rn(x, fy);
     } else if (f < nu + nv + nw) {
-        long long l = f - nu - nv; float x = w[l]; sw[l] = x; if (az) w[l] = __fadd_rn(x, fz);
+        long long l = f - nu - nv; float x = w[l]; sw[l] = x; if (az && !skip) w[l] = __fadd_rn(x, fz);
     }
 }
 
@@ -692,7 +696,8 @@ __device__ F3 resolve_collision(const StepConsts &c, const float *S, const uint8
 __global__ void __launch_bounds__(TPB) k_advect(ParticleSoA p, int n, StepConsts c, const float *u, const float *v,
                                                 const float *w, const float *su, const float *sv, const float *sw,
                                                 const float *S, const uint8_t *ns, float picRatio, float flipRatio,
-                                                double dt, unsigned int *keys, unsigned int *hist, double speedStep) {
+                                                double dt, unsigned int *keys, unsigned int *hist, double speedStep,
+                                                const InflowConstraint ic) {
     __shared__ unsigned int shist[8];
     if (threadIdx.x < 8) shist[threadIdx.x] = 0;
     __syncthreads();
@@ -704,6 +709,20 @@ __global__ void __launch_bounds__(TPB) k_advect(ParticleSoA p, int n, StepConsts
         F3 vold = eval_vel(c, su, sv, sw, p0);
         F3 vflip = sub(add(v0, vpic), vold);
         F3 vn = add(mul(picRatio, vpic), mul(flipRatio, vflip));
+        if (ic.count > 0) {
+            // _constrainMarkerParticleVelocities (fluidsimulation.cpp:4109-4170):
+            // a particle in a cell of the source where the source's level set,
+            // read at the particle's position in the level set's own frame (the
+            // reference passes the position without the level set's offset), is
+            // not positive takes the source's velocity; later sources win
+            const int ci = exact_floor(p0.x, c.invdx, c.invdxf), cj = exact_floor(p0.y, c.invdx, c.invdxf),
+                      ck = exact_floor(p0.z, c.invdx, c.invdxf);
+            const Dims d{c.I, c.J, c.K};
+            const unsigned bits = d.in(ci, cj, ck) ? ic.cellBits[d.idx(ci, cj, ck)] : 0u;
+            for (int q = 0; q < ic.count; q++)
+                if ((bits >> q & 1u) && !(source_phi(ic.g[q], p0.x, p0.y, p0.z) > 0.0f))
+                    vn = f3(ic.vx[q], ic.vy[q], ic.vz[q]);
+        }
         F3 k1 = vpic;
         F3 k2 = eval_vel(c, u, v, w, add(p0, mul((float)(0.5 * dt), k1)));
         F3 k3 = eval_vel(c, u, v, w, add(p0, mul((float)(0.75 * dt), k2)));
@@ -807,10 +826,11 @@ void launch_extrapolate(const StepConsts &c, float *u, float *v, float *w, const
     for (int l = 0; l < layers; l++) { FLIP_COUNT(1); k_extrap_layer<<<div_up(tot, TPB), TPB, 0, s>>>(c, u, v, w, status, l); }
 }
 void launch_save_and_force(const StepConsts &c, float *u, float *v, float *w, float *su, float *sv, float *sw,
-                           float fx, float fy, float fz, bool ax, bool ay, bool az, cudaStream_t s) {
+                           float fx, float fy, float fz, bool ax, bool ay, bool az, const uint8_t *ex,
+                           cudaStream_t s) {
     long long nu = (long long)(c.I + 1) * c.J * c.K, nv = (long long)c.I * (c.J + 1) * c.K,
               nw = (long long)c.I * c.J * (c.K + 1);
-    { FLIP_COUNT(1); k_save_force<<<div_up(nu + nv + nw, TPB), TPB, 0, s>>>(nu, nv, nw, u, v, w, su, sv, sw, fx, fy, fz, ax, ay, az); }
+    { FLIP_COUNT(1); k_save_force<<<div_up(nu + nv + nw, TPB), TPB, 0, s>>>(nu, nv, nw, u, v, w, su, sv, sw, fx, fy, fz, ax, ay, az, ex); }
 }
 void launch_constrain(const StepConsts &c, float *u, float *v, float *w, float *su, float *sv, float *sw,
                       const float *wu, const float *wv, const float *ww, const float *fu, const float *fv,
@@ -822,11 +842,11 @@ void launch_constrain(const StepConsts &c, float *u, float *v, float *w, float *
 void launch_advect(ParticleSoA p, int n, const StepConsts &c, const float *u, const float *v, const float *w,
                    const float *su, const float *sv, const float *sw, const float *solidPhi,
                    const uint8_t *nearSolid, float picRatio, float flipRatio, double dt, unsigned int *keys,
-                   unsigned int *speedHist, double speedStep, cudaStream_t s) {
+                   unsigned int *speedHist, double speedStep, const InflowConstraint &ic, cudaStream_t s) {
     if (n <= 0) return;
     FLIP_COUNT(1);
     k_advect<<<div_up(n, TPB), TPB, 0, s>>>(p, n, c, u, v, w, su, sv, sw, solidPhi, nearSolid, picRatio,
-                                            flipRatio, dt, keys, speedHist, speedStep);
+                                            flipRatio, dt, keys, speedHist, speedStep, ic);
 }
 void launch_speed_limit(const unsigned int *hist, int n, int bins, double speedStep, double maxPct, int maxAbs,
                         float *maxSpeedSq, cudaStream_t s) {

@@ -96,7 +96,7 @@ __global__ void k_mask_particles(ParticleSoA p, int n, StepConsts c, unsigned in
 struct SeedArgs {
     const int *cells;       // flat cell indices, ascending
     long long ncand;        // 8 per cell
-    const float *meshPhi;   // nodal level set of the mesh
+    SourceGridView mesh;    // nodal level set of the mesh and its first node's position
     const float *solidPhi;  // nodal solid level set
     double jitter;          // _getMarkerParticleJitter()
     int jitterSurface;      // _isJitterSurfaceMarkerParticlesEnabled
@@ -118,8 +118,9 @@ __global__ void k_seed_candidates(StepConsts c, SeedArgs a, const unsigned int *
     float px = __fadd_rn(cell_centre(i, c.dx), ox), py = __fadd_rn(cell_centre(j, c.dx), oy),
           pz = __fadd_rn(cell_centre(k, c.dx), oz);
     cand[q] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-    // MeshLevelSet::trilinearInterpolate returns float
-    const double d = (double)(float)nodal_at(a.meshPhi, c.I, c.J, c.K, c.dx, px, py, pz);
+    // meshSDF.trilinearInterpolate(p - sdfoffset), a float (fluidsimulation.cpp:4548)
+    const double d = (double)source_phi(a.mesh, __fsub_rn(px, a.mesh.ox), __fsub_rn(py, a.mesh.oy),
+                                        __fsub_rn(pz, a.mesh.oz));
     if (d > 0) return;
     if (a.jitterSurface || d < -c.dx) {
         const double lo = -a.jitter, hi = a.jitter;
@@ -166,12 +167,12 @@ void launch_mask_particles(const ParticleSoA &p, int n, const StepConsts &c, uns
     k_mask_particles<<<div_up(n, TPB), TPB, 0, s>>>(p, n, c, mask);
 }
 
-void launch_seed_candidates(const StepConsts &c, const int *cells, long long ncells, const float *meshPhi,
+void launch_seed_candidates(const StepConsts &c, const int *cells, long long ncells, const SourceGridView &meshPhi,
                             const float *solidPhi, double jitter, bool jitterSurface, unsigned long long seed,
                             const unsigned int *mask, float4 *cand, unsigned int *owner, int *keep, cudaStream_t s) {
     if (ncells <= 0) return;
     SeedArgs a;
-    a.cells = cells; a.ncand = 8 * ncells; a.meshPhi = meshPhi; a.solidPhi = solidPhi;
+    a.cells = cells; a.ncand = 8 * ncells; a.mesh = meshPhi; a.solidPhi = solidPhi;
     a.jitter = jitter; a.jitterSurface = jitterSurface ? 1 : 0; a.seed = seed;
     const long long nb = div_up(a.ncand, TPB);
     { FLIP_COUNT(1); k_seed_candidates<<<(unsigned)nb, TPB, 0, s>>>(c, a, mask, cand, owner); }

@@ -575,4 +575,81 @@ void mesh_fluid_cells(int I, int J, int K, double dx, const std::vector<float> &
     mesh_level_set(wv, tris, I + 1, J + 1, K + 1, dx, 3, phi, tri);
 }
 
+// MeshFluidSource::update for a static mesh (meshfluidsource.cpp:171-214)
+// with _getGridBoundsFromTriangleMesh (:300-318): the mesh's AABB (double
+// extent plus 1e-9, aabb.cpp:54-82), expanded by 4 dx, its corners' cells
+// clamped to the grid give the sub-grid; a mesh whose box meets the domain
+// box (I+1, J+1, K+1 cells) in less than dx^3 / 8 leaves an empty level set.
+void fluid_source_setup(int I, int J, int K, double dx, const std::vector<float> &verts, const std::vector<int> &tris,
+                        SourceGrid &g) {
+    const int nv = (int)verts.size() / 3;
+    std::vector<V> wv(nv);
+    for (int v = 0; v < nv; v++) wv[v] = V{verts[3 * v], verts[3 * v + 1], verts[3 * v + 2]};
+    // MeshObject::getCells (meshobject.cpp:101-140)
+    std::vector<uint8_t> nodes;
+    grid_nodes_inside(wv, tris, I + 1, J + 1, K + 1, dx, nodes);
+    std::vector<uint8_t> mark((size_t)I * J * K, 0);
+    for (int k = 0; k <= K; k++)
+        for (int j = 0; j <= J; j++)
+            for (int i = 0; i <= I; i++) {
+                if (!nodes[(size_t)i + (size_t)(I + 1) * ((size_t)j + (size_t)(J + 1) * k)]) continue;
+                for (int c = k - 1; c <= k; c++)
+                    for (int b = j - 1; b <= j; b++)
+                        for (int a = i - 1; a <= i; a++)
+                            if (a >= 0 && b >= 0 && c >= 0 && a < I && b < J && c < K)
+                                mark[(size_t)a + (size_t)I * ((size_t)b + (size_t)J * c)] = 1;
+            }
+    g.cells.clear();
+    for (size_t q = 0; q < mark.size(); q++)
+        if (mark[q]) g.cells.push_back((int)q);
+    // the mesh's AABB
+    double mn[3] = {0, 0, 0}, mx[3] = {0, 0, 0};
+    for (int v = 0; v < nv; v++) {
+        const double p[3] = {wv[v].x, wv[v].y, wv[v].z};
+        for (int a = 0; a < 3; a++) {
+            mn[a] = v == 0 ? p[a] : std::fmin(p[a], mn[a]);
+            mx[a] = v == 0 ? p[a] : std::fmax(p[a], mx[a]);
+        }
+    }
+    float pos[3];
+    double ext[3];
+    for (int a = 0; a < 3; a++) {
+        pos[a] = (float)mn[a];
+        ext[a] = nv > 0 ? mx[a] - mn[a] + 1e-9 : 0.0;
+    }
+    // expand(4 dx), corners, cells
+    const double pad = 4.0 * dx, h = 0.5 * pad;
+    const int n[3] = {I, J, K};
+    int gmax[3];
+    for (int a = 0; a < 3; a++) {
+        const float lo = pos[a] - (float)h;
+        const float hi = lo + (float)(ext[a] + pad);
+        const int g0 = floor_index(lo, dx), g1 = floor_index(hi, dx);
+        g.gmin[a] = (int)std::fmax(g0, 0);
+        gmax[a] = (int)std::fmin(g1, n[a] - 1);
+        g.offset[a] = gpos(g.gmin[a], dx);
+        g.nodes[a] = std::max(gmax[a] - g.gmin[a] + 1, 1) + 1;
+    }
+    // AABB::isIntersecting(domain box, dx^3 / 8) (aabb.cpp:170-195)
+    bool meets = true;
+    double vol = 1.0;
+    for (int a = 0; a < 3; a++) {
+        const float lo1 = pos[a], hi1 = pos[a] + (float)ext[a];
+        const float lo2 = 0.0f, hi2 = (float)((n[a] + 1) * dx);
+        if (lo1 > hi2 || hi1 < lo2) meets = false;
+        vol *= (double)std::fmin(hi1, hi2) - (double)std::fmax(lo1, lo2);
+    }
+    meets = meets && vol > (dx * dx * dx) * 0.125;
+    std::vector<V> local;
+    std::vector<int> ltris;
+    if (meets) {
+        local.resize(nv);
+        for (int v = 0; v < nv; v++)
+            local[v] = V{wv[v].x + (-g.offset[0]), wv[v].y + (-g.offset[1]), wv[v].z + (-g.offset[2])};
+        ltris = tris;
+    }
+    std::vector<int> tri;
+    mesh_level_set(local, ltris, g.nodes[0], g.nodes[1], g.nodes[2], dx, 2, g.phi, tri);
+}
+
 }  // namespace flip

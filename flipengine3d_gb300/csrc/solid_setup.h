@@ -45,4 +45,19 @@ struct DomainBox {
 void mesh_fluid_cells(int I, int J, int K, double dx, const std::vector<float> &verts, const std::vector<int> &tris,
                       std::vector<int> &cells, std::vector<float> &phi);
 
+// The host set-up of a static mesh fluid source (MeshFluidSource::update,
+// meshfluidsource.cpp:171-214, 300-318): the cells of the grid nodes inside
+// the mesh (MeshObject::getCells), and the mesh's level set over the
+// sub-grid its bounding box spans, padded by 4 cells and clamped to the
+// domain, exact in a band of 2, with its first node at `offset`.
+struct SourceGrid {
+    int gmin[3] = {0, 0, 0};     // first cell of the sub-grid
+    int nodes[3] = {1, 1, 1};    // nodes of the level set (cells + 1)
+    float offset[3] = {0, 0, 0}; // position of its first node
+    std::vector<float> phi;      // negative inside
+    std::vector<int> cells;      // flat indices, ascending
+};
+void fluid_source_setup(int I, int J, int K, double dx, const std::vector<float> &verts, const std::vector<int> &tris,
+                        SourceGrid &g);
+
 }  // namespace flip

@@ -45,6 +45,13 @@ class FrameStats(C.Structure):
 STAGE_NAMES = ("liquid_sdf", "p2g", "force", "pressure", "constrain", "advect", "binning")
 
 
+class FluidSourceParams(C.Structure):
+    """flip_fluid_source_params (include/flip3d.h)."""
+    _fields_ = [("inflow", C.c_int), ("enabled", C.c_int), ("substep_emissions", C.c_int),
+                ("constrained_velocity", C.c_int), ("fluid_outflow", C.c_int), ("outflow_inversed", C.c_int),
+                ("velocity", C.c_double * 3)]
+
+
 class StageDump(C.Structure):
     _fields_ = [(n, C.c_void_p) for n in (
         "phi", "u_p2g", "v_p2g", "w_p2g", "vu_p2g", "vv_p2g", "vw_p2g",
@@ -118,6 +125,11 @@ SIGNATURES = {
     "flip_runtime_update_all": [_P, C.POINTER(C.c_void_p), _I, _D],
     "flip_runtime_admit": [_P, C.c_longlong, C.POINTER(C.c_int)],
     "flip_runtime_pending": [_P, C.POINTER(C.c_int), C.POINTER(C.c_int)],
+    "flip_add_mesh_fluid_source": [_P, _I, _P, _I, _P, C.POINTER(FluidSourceParams), C.POINTER(C.c_int)],
+    "flip_set_mesh_fluid_source_params": [_P, _I, C.POINTER(FluidSourceParams)],
+    "flip_get_mesh_fluid_source_params": [_P, _I, C.POINTER(FluidSourceParams)],
+    "flip_remove_mesh_fluid_source": [_P, _I],
+    "flip_fluid_source_setup": [_I, _I, _I, _D, _I, _P, _I, _P, _P, _P, _P, C.POINTER(C.c_int), _P],
     "flip_enable_surface_reconstruction": [_P, _I],
     "flip_is_surface_reconstruction_enabled": [_P, C.POINTER(C.c_int)],
     "flip_set_surface_subdivision_level": [_P, _I],
@@ -218,6 +230,25 @@ def mesh_fluid_cells(isize, jsize, ksize, dx, vertices, triangles):
     _check(lib, lib.flip_mesh_fluid_cells(isize, jsize, ksize, dx, v.shape[0], _ptr(v), t.shape[0], _ptr(t),
                                           C.byref(n), _ptr(cells), _ptr(phi)))
     return cells[:n.value].copy(), phi
+
+
+def fluid_source_setup(isize, jsize, ksize, dx, vertices, triangles):
+    """A static mesh fluid source's set-up without a device: (nodes (i, j, k),
+    offset xyz, level set (k, j, i) nodal, cells as flat indices)."""
+    lib = load_library()
+    v = np.ascontiguousarray(vertices, np.float32).reshape(-1, 3)
+    t = np.ascontiguousarray(triangles, np.int32).reshape(-1, 3)
+    nodes = np.zeros(3, np.int32)
+    off = np.zeros(3, np.float32)
+    n = C.c_int()
+    _check(lib, lib.flip_fluid_source_setup(isize, jsize, ksize, dx, len(v), _ptr(v), len(t), _ptr(t), _ptr(nodes),
+                                            _ptr(off), None, C.byref(n), None))
+    ni, nj, nk = (int(a) for a in nodes)
+    phi = np.zeros((nk, nj, ni), np.float32)
+    cells = np.zeros(max(n.value, 1), np.int32)
+    _check(lib, lib.flip_fluid_source_setup(isize, jsize, ksize, dx, len(v), _ptr(v), len(t), _ptr(t), _ptr(nodes),
+                                            _ptr(off), _ptr(phi), C.byref(n), _ptr(cells)))
+    return (ni, nj, nk), off, phi, cells[: n.value].copy()
 
 
 def compute_solid(isize, jsize, ksize, dx, cfl=5, obstacles=()):
@@ -528,6 +559,36 @@ class FluidSimulation:
         self._c(self._lib.flip_get_frame_stats(self._h, C.byref(s)))
         return s
 
+    # -- mesh fluid sources (fluidsimulation.cpp:1953-1992)
+    @staticmethod
+    def _source_params(inflow=True, enabled=True, substep_emissions=1, constrained=True, fluid_outflow=True,
+                       inversed=False, velocity=(0.0, 0.0, 0.0)):
+        p = FluidSourceParams()
+        p.inflow, p.enabled, p.substep_emissions = int(inflow), int(enabled), int(substep_emissions)
+        p.constrained_velocity, p.fluid_outflow, p.outflow_inversed = int(constrained), int(fluid_outflow), int(inversed)
+        for a in range(3):
+            p.velocity[a] = float(velocity[a])
+        return p
+
+    def addMeshFluidSource(self, vertices, triangles, **params) -> int:
+        """A static mesh fluid source; keyword settings as the reference's
+        MeshFluidSource setters (inflow, enabled, substep_emissions,
+        constrained, fluid_outflow, inversed, velocity).  Returns its id."""
+        v = np.ascontiguousarray(vertices, np.float32).reshape(-1, 3)
+        t = np.ascontiguousarray(triangles, np.int32).reshape(-1, 3)
+        sid = C.c_int()
+        p = self._source_params(**params)
+        self._c(self._lib.flip_add_mesh_fluid_source(self._h, len(v), _ptr(v), len(t), _ptr(t), C.byref(p),
+                                                     C.byref(sid)))
+        return sid.value
+
+    def setMeshFluidSource(self, source_id: int, **params):
+        p = self._source_params(**params)
+        self._c(self._lib.flip_set_mesh_fluid_source_params(self._h, int(source_id), C.byref(p)))
+
+    def removeMeshFluidSource(self, source_id: int):
+        self._c(self._lib.flip_remove_mesh_fluid_source(self._h, int(source_id)))
+
     # -- surface reconstruction (fluidsimulation.cpp:216-300, 367-380, 2543-2546)
     def enableSurfaceReconstruction(self):
         self._c(self._lib.flip_enable_surface_reconstruction(self._h, 1))
@@ -718,6 +779,9 @@ class FluidSimulation:
             sim.setMarkerParticleJitterFactor(scene.jitter_factor)
         for fm in getattr(scene, "fluid_meshes", []):
             sim.addMeshFluid(*fm)
+        for src in getattr(scene, "sources", []):
+            sim.addMeshFluidSource(src["vertices"], src["triangles"],
+                                   **{k: v for k, v in src.items() if k not in ("vertices", "triangles")})
         if len(scene.positions):
             sim.loadMarkerParticleData(scene.positions, scene.velocities)
         sim.initialize()

@@ -36,6 +36,10 @@ class Scene:
     # fluid meshes added with addMeshFluid: (vertices, triangles, velocity xyz)
     fluid_meshes: list = field(default_factory=list)
     jitter_factor: float | None = None   # setMarkerParticleJitterFactor, when set
+    # mesh fluid sources (addMeshFluidSource): dicts with vertices, triangles,
+    # inflow (bool), velocity xyz, substep_emissions, constrained,
+    # fluid_outflow, inversed
+    sources: list = field(default_factory=list)
 
     @property
     def num_particles(self) -> int:
@@ -212,6 +216,49 @@ def mesh_fluid(n: int = 32, *, which: str = "box", dx: float = 0.125, jitter_fac
     sc = Scene(n, n, n, dx, pos, vel, gravity=(0.0, -25.0, 0.0), frame_dt=1.0 / 30.0, tolerance=1e-9,
                steps=steps, name=f"mesh_fluid_{which}_{n}", fluid_meshes=meshes, jitter_factor=jitter_factor)
     return sc
+
+
+def fluid_sources(n: int = 24, *, which: str = "inflow", seed: int = 0, steps: int = 4) -> Scene:
+    """Mesh fluid sources in an n^3 box (dx 1/n, 1/60 s frames, gravity
+    -9.81, jitter factor 0.001 so that emitted particles are exactly the
+    sub-cell centres):
+
+    `inflow`: an inflow box high up near the -x wall emitting fluid moving at
+    (1.5, 0, 0.2) every substep, its velocity constrained, over a small
+    loaded pool; `outflow`: a dam break whose fluid runs into an outflow box
+    on the floor at the far wall; `both`: the inflow, the outflow, and a
+    second inflow (a sphere) that emits only at a frame's first substep and
+    does not constrain velocities; `inversed`: a dam break inside an
+    inversed outflow box, which removes fluid that leaves the box."""
+    L = 1.0
+    dx = L / n
+    rng = np.random.default_rng(seed)
+    inflow = dict(inflow=True, velocity=(1.5, 0.0, 0.2), substep_emissions=1, constrained=True)
+    inflow["vertices"], inflow["triangles"] = box_mesh((0.0913, 0.6131, 0.3217), (0.2389, 0.7523, 0.5431))
+    outflow = dict(inflow=False)
+    outflow["vertices"], outflow["triangles"] = box_mesh((0.5217, -0.05, 0.2013), (1.05, 0.2311, 0.8219))
+    pos = np.zeros((0, 3), np.float32)
+    if which in ("inflow", "both"):
+        cells = _box_cells(n, n, n, dx, (0.0, 0.0, 0.0), (0.5, 0.12, 1.0))
+    else:
+        cells = _box_cells(n, n, n, dx, (0.0, 0.0, 0.0), (0.45, 0.55, 0.5))
+    pos = _jittered_cells(cells, dx, rng, 8)
+    if which == "inflow":
+        sources = [inflow]
+    elif which == "outflow":
+        sources = [outflow]
+    elif which == "both":
+        sphere = dict(inflow=True, velocity=(0.0, -0.5, 1.0), substep_emissions=0, constrained=False)
+        sphere["vertices"], sphere["triangles"] = icosphere_mesh((0.6121, 0.7013, 0.3117), 0.0913, subdivisions=2)
+        sources = [inflow, outflow, sphere]
+    elif which == "inversed":
+        inv = dict(inflow=False, inversed=True)
+        inv["vertices"], inv["triangles"] = box_mesh((-0.05, -0.05, -0.05), (0.4913, 0.7219, 1.05))
+        sources = [inv]
+    else:
+        raise ValueError(which)
+    return Scene(n, n, n, dx, pos, np.zeros_like(pos), frame_dt=1.0 / 60.0, tolerance=1e-9, steps=steps,
+                 name=f"fluid_sources_{which}_{n}", sources=sources, jitter_factor=0.001)
 
 
 def plain_64(seed: int = 0) -> Scene:

@@ -16,6 +16,7 @@
 
 #include <stdexcept>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "flip3d.h"
@@ -98,6 +99,55 @@ private:
     float friction_ = 0.0f;
 };
 
+// A static mesh fluid source: the part of the reference's MeshFluidSource
+// (meshfluidsource.h, meshfluidsource.cpp:30-166) the simulation reads.  The
+// caller keeps it alive while it is added; its settings are read at every
+// update(), as the reference reads them.
+class MeshFluidSource {
+public:
+    MeshFluidSource() { prm_ = defaults(); }
+    MeshFluidSource(int, int, int, double) { prm_ = defaults(); }
+    void updateMeshStatic(const TriangleMesh &m) { mesh_ = m; }
+    const TriangleMesh &getMesh() const { return mesh_; }
+    void enable() { prm_.enabled = 1; }
+    void disable() { prm_.enabled = 0; }
+    bool isEnabled() const { return prm_.enabled != 0; }
+    void setSubstepEmissions(int n) { prm_.substep_emissions = n < 0 ? 0 : n; }
+    int getSubstepEmissions() const { return prm_.substep_emissions; }
+    void setInflow() { prm_.inflow = 1; }
+    bool isInflow() const { return prm_.inflow != 0; }
+    void setOutflow() { prm_.inflow = 0; }
+    bool isOutflow() const { return prm_.inflow == 0; }
+    void enableFluidOutflow() { prm_.fluid_outflow = 1; }
+    void disableFluidOutflow() { prm_.fluid_outflow = 0; }
+    bool isFluidOutflowEnabled() const { return prm_.fluid_outflow != 0; }
+    void setVelocity(vec3 v) {
+        prm_.velocity[0] = v.x;
+        prm_.velocity[1] = v.y;
+        prm_.velocity[2] = v.z;
+    }
+    vec3 getVelocity() const { return vec3(prm_.velocity[0], prm_.velocity[1], prm_.velocity[2]); }
+    void enableConstrainedFluidVelocity() { prm_.constrained_velocity = 1; }
+    void disableConstrainedFluidVelocity() { prm_.constrained_velocity = 0; }
+    bool isConstrainedFluidVelocityEnabled() const { return prm_.constrained_velocity != 0; }
+    void outflowInverse() { prm_.outflow_inversed = !prm_.outflow_inversed; }
+    bool isOutflowInversed() const { return prm_.outflow_inversed != 0; }
+    const flip_fluid_source_params &params() const { return prm_; }
+
+private:
+    static flip_fluid_source_params defaults() {
+        flip_fluid_source_params p{};
+        p.inflow = 1;
+        p.enabled = 1;
+        p.substep_emissions = 1;
+        p.constrained_velocity = 1;
+        p.fluid_outflow = 1;
+        return p;
+    }
+    TriangleMesh mesh_;
+    flip_fluid_source_params prm_;
+};
+
 class FluidSimulation {
 public:
     FluidSimulation(int isize, int jsize, int ksize, double dx) : isize_(isize), jsize_(jsize), ksize_(ksize), dx_(dx) {
@@ -123,6 +173,7 @@ public:
         return v != 0;
     }
     void update(double dt) {
+        for (auto &src : sources_) check(flip_set_mesh_fluid_source_params(ctx_, src.second, &src.first->params()));
         int rc = flip_update(ctx_, dt);
         if (rc != FLIP_E_SOLVER_NOCONV) check(rc);
     }
@@ -200,6 +251,32 @@ public:
         obstacles_.push_back(obstacle);
     }
 
+    // addMeshFluidSource / removeMeshFluidSource / removeMeshFluidSources
+    // (fluidsimulation.cpp:1953-1992): static meshes; the pointer is kept.
+    void addMeshFluidSource(MeshFluidSource *source) {
+        for (auto &src : sources_)
+            if (src.first == source) throw std::runtime_error("Error: Mesh fluid source has already been added.\n");
+        const TriangleMesh &m = source->getMesh();
+        int id = 0;
+        check(flip_add_mesh_fluid_source(ctx_, (int)m.vertices.size(), reinterpret_cast<const float *>(m.vertices.data()),
+                                         (int)m.triangles.size(), reinterpret_cast<const int *>(m.triangles.data()),
+                                         &source->params(), &id));
+        sources_.push_back({source, id});
+    }
+    void removeMeshFluidSource(MeshFluidSource *source) {
+        for (size_t q = 0; q < sources_.size(); q++)
+            if (sources_[q].first == source) {
+                check(flip_remove_mesh_fluid_source(ctx_, sources_[q].second));
+                sources_.erase(sources_.begin() + q);
+                return;
+            }
+        throw std::invalid_argument("Error: could not find mesh fluid source to remove.\n");
+    }
+    void removeMeshFluidSources() {
+        for (auto &src : sources_) check(flip_remove_mesh_fluid_source(ctx_, src.second));
+        sources_.clear();
+    }
+
     // addMeshFluid (fluidsimulation.cpp:2038-2047): the mesh is copied and
     // filled with marker particles at the end of the next substep.
     void addMeshFluid(const MeshObject &fluid) { addMeshFluid(fluid, vec3(0.0, 0.0, 0.0)); }
@@ -268,6 +345,7 @@ private:
     flip_ctx *ctx_ = nullptr;
     TriangleMesh mesh_;
     std::vector<MeshObject *> obstacles_;
+    std::vector<std::pair<MeshFluidSource *, int>> sources_;
 };
 
 }  // namespace flip3d

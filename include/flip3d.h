@@ -289,6 +289,52 @@ int flip_mic0_precondition(int isize, int jsize, int ksize, const uint8_t *fluid
 /* Number of this library's kernel launches issued so far on the context. */
 int flip_get_launch_count(flip_ctx *ctx, long long *count);
 
+/* Mesh fluid sources: addMeshFluidSource / removeMeshFluidSource
+ * (fluidsimulation.cpp:1953-1992) with a static MeshFluidSource
+ * (meshfluidsource.h).  The mesh (arrays as flip_add_mesh_obstacle) is
+ * copied; `params` NULL gives the reference's defaults (meshfluidsource.h:
+ * 111-124): an enabled inflow emitting once per substep at velocity 0 and
+ * constraining the fluid velocity, fluid outflow on, not inversed.  Per
+ * substep, as the reference:
+ *   - an enabled inflow that constrains the fluid velocity keeps the body
+ *     force off the faces where its level set is negative, and gives its
+ *     velocity to the particles in its cells where the level set is not
+ *     positive (:3372-3440, 4109-4170; like the reference, these two read
+ *     the level set at the world position without the level set's offset);
+ *   - an enabled inflow emits particles into its cells as addMeshFluid does,
+ *     `substep_emissions` times per substep, or only at a frame's first
+ *     substep when 0 (:4564-4606, 4676-4698);
+ *   - an enabled outflow with fluid outflow on removes the particles in its
+ *     cells where its level set is negative, or with outflow_inversed those
+ *     outside its cells or where the level set is not negative (:4608-4674);
+ *   - frame 0's first substep length counts the enabled inflows' speeds
+ *     (:5529-5551).
+ * The source's level set covers the cells its bounding box spans, padded by 4
+ * cells, exact in a band of 2 (meshfluidsource.cpp:171-214, 300-318).  Animated
+ * sources, appended object velocity and diffuse outflow are not restated.
+ * `id` identifies the source in the other calls; at most 8 inflows may
+ * constrain the fluid velocity at once (FLIP_E_DOMAIN). */
+typedef struct flip_fluid_source_params {
+    int inflow;                 /* 1 inflow, 0 outflow (setInflow / setOutflow)          */
+    int enabled;                /* enable / disable                                      */
+    int substep_emissions;      /* setSubstepEmissions: negative counts as 0             */
+    int constrained_velocity;   /* enable/disableConstrainedFluidVelocity                */
+    int fluid_outflow;          /* enable/disableFluidOutflow                            */
+    int outflow_inversed;       /* outflowInverse toggles it                              */
+    double velocity[3];         /* setVelocity                                           */
+} flip_fluid_source_params;
+int flip_add_mesh_fluid_source(flip_ctx *ctx, int nverts, const float *verts, int ntris, const int *tris,
+                               const flip_fluid_source_params *params, int *id);
+int flip_set_mesh_fluid_source_params(flip_ctx *ctx, int id, const flip_fluid_source_params *params);
+int flip_get_mesh_fluid_source_params(flip_ctx *ctx, int id, flip_fluid_source_params *params);
+int flip_remove_mesh_fluid_source(flip_ctx *ctx, int id);
+/* A source's set-up without a device: the nodes and first-node position of
+ * its level set, the level set (nodes[0]*nodes[1]*nodes[2] floats, flat i
+ * fastest), and its cells (ascending flat indices, up to I*J*K).  phi and
+ * cells may be NULL. */
+int flip_fluid_source_setup(int isize, int jsize, int ksize, double dx, int nverts, const float *verts, int ntris,
+                            const int *tris, int *nodes, float *offset, float *phi, int *ncells, int *cells);
+
 /* Surface reconstruction, the mesh getIsomesh() returns (fluidsimulation.cpp:
  * 2543-2546).  As in the reference, it is on by default and runs after the
  * first substep of every frame (_outputSimulationData, :5444-5464): the

@@ -36,12 +36,14 @@
 #include "pcgsolver/pcgsolver.h"
 #include "pcgsolver/sparsematrix.h"
 #include "meshobject.h"
+#include "meshfluidsource.h"
 
 namespace {
 
 struct RefSim {
     FluidSimulation *sim = nullptr;
     std::vector<MeshObject *> obstacles;   // owned here, registered with the simulation
+    std::vector<MeshFluidSource *> sources;   // owned here, registered with the simulation
     std::string status;
     unsigned int particleFragmentBytes = 0;   // 0: the reference's default fragments
 };
@@ -93,6 +95,7 @@ void ref_destroy(void *h) {
     RefSim *r = (RefSim *)h;
     delete r->sim;
     for (MeshObject *o : r->obstacles) delete o;
+    for (MeshFluidSource *q : r->sources) delete q;
     delete r;
 }
 
@@ -523,6 +526,54 @@ void ref_add_mesh_obstacle(void *h, int nverts, const float *verts, int ntris, c
     o->setFriction(friction);
     r->obstacles.push_back(o);
     r->sim->addMeshObstacle(o);
+}
+
+// addMeshFluidSource (fluidsimulation.cpp:1953-1965) with a static
+// MeshFluidSource built from plain arrays (meshfluidsource.cpp:30-49):
+// inflow or outflow, velocity, substep emissions, constrained fluid velocity,
+// fluid outflow and an inversed outflow as its setters make them.
+void ref_add_mesh_fluid_source(void *h, int nverts, const float *verts, int ntris, const int *tris, int inflow,
+                               double vx, double vy, double vz, int substep_emissions, int constrained,
+                               int fluid_outflow, int inversed) {
+    RefSim *r = (RefSim *)h;
+    int I, J, K;
+    r->sim->getGridDimensions(&I, &J, &K);
+    MeshFluidSource *src = new MeshFluidSource(I, J, K, r->sim->getCellSize());
+    src->updateMeshStatic(mesh_from_arrays(nverts, verts, ntris, tris));
+    if (inflow) src->setInflow(); else src->setOutflow();
+    src->setVelocity(vmath::vec3(vx, vy, vz));
+    src->setSubstepEmissions(substep_emissions);
+    if (constrained) src->enableConstrainedFluidVelocity(); else src->disableConstrainedFluidVelocity();
+    if (fluid_outflow) src->enableFluidOutflow(); else src->disableFluidOutflow();
+    if (inversed) src->outflowInverse();
+    r->sources.push_back(src);
+    r->sim->addMeshFluidSource(src);
+}
+
+// MeshFluidSource::update for a static mesh (meshfluidsource.cpp:171-214):
+// the source's level set (its nodes, the position of its first node, the
+// values) and MeshObject::getCells as flat indices.  rand() is reseeded as
+// at the start of a process (the inside test's ray jitter draws from it).
+void ref_fluid_source_setup(int I, int J, int K, double dx, int nverts, const float *verts, int ntris,
+                            const int *tris, int *nodes, float *offset, float *phi, int *ncells, int *cells) {
+    std::srand(1);
+    MeshFluidSource src(I, J, K, dx);
+    src.updateMeshStatic(mesh_from_arrays(nverts, verts, ntris, tris));
+    src.update(1.0 / 60.0);
+    MeshLevelSet *sdf = src.getMeshLevelSet();
+    nodes[0] = sdf->_phi.width;
+    nodes[1] = sdf->_phi.height;
+    nodes[2] = sdf->_phi.depth;
+    vmath::vec3 o = src.getMeshLevelSetOffset();
+    offset[0] = o.x;
+    offset[1] = o.y;
+    offset[2] = o.z;
+    if (phi) copyArray(sdf->_phi, phi);
+    std::vector<GridIndex> cs;
+    src.getCells(cs);
+    *ncells = (int)cs.size();
+    if (cells)
+        for (size_t q = 0; q < cs.size(); q++) cells[q] = cs[q].i + I * (cs[q].j + J * cs[q].k);
 }
 
 // Surface reconstruction settings (fluidsimulation.cpp:216-300, 367-376):

@@ -72,6 +72,13 @@ def lib(prefix: str = "ref"):
             L.ref_add_mesh_obstacle.restype = None
             L.ref_get_node_friction.argtypes = [C.c_void_p, C.c_void_p]
             L.ref_get_node_friction.restype = None
+            L.ref_add_mesh_fluid_source.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_int,
+                                                    C.c_double, C.c_double, C.c_double, C.c_int, C.c_int, C.c_int,
+                                                    C.c_int]
+            L.ref_add_mesh_fluid_source.restype = None
+            L.ref_fluid_source_setup.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, C.c_int, C.c_void_p, C.c_int,
+                                                 C.c_void_p] + [C.c_void_p] * 5
+            L.ref_fluid_source_setup.restype = None
             L.ref_set_surface_reconstruction.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_double, C.c_int]
             L.ref_set_surface_reconstruction.restype = None
             L.ref_mesh_now.argtypes = [C.c_void_p]
@@ -171,6 +178,23 @@ def mesh_fluid_cells(isize, jsize, ksize, dx, vertices, triangles):
     return cells[:n.value].copy(), phi
 
 
+def fluid_source_setup(isize, jsize, ksize, dx, vertices, triangles):
+    """The reference's set-up of a static mesh fluid source: (nodes (i, j, k),
+    offset xyz, level set (k, j, i) nodal, cells as flat indices)."""
+    L = lib("ref")
+    v = np.ascontiguousarray(vertices, np.float32).reshape(-1, 3)
+    t = np.ascontiguousarray(triangles, np.int32).reshape(-1, 3)
+    nodes = np.zeros(3, np.int32)
+    off = np.zeros(3, np.float32)
+    n = C.c_int()
+    phi = np.zeros((ksize + 2) * (jsize + 2) * (isize + 2), np.float32)
+    cells = np.zeros(isize * jsize * ksize, np.int32)
+    L.ref_fluid_source_setup(isize, jsize, ksize, dx, len(v), _p(v), len(t), _p(t), _p(nodes), _p(off), _p(phi),
+                             C.byref(n), _p(cells))
+    ni, nj, nk = (int(a) for a in nodes)
+    return (ni, nj, nk), off, phi[: ni * nj * nk].reshape(nk, nj, ni).copy(), cells[: n.value].copy()
+
+
 def random_mic0_system(shape, seed, weak_fraction=0.05, null_rows=2):
     """A random 7-point system of the pressure solve's shape: flagged cells
     (a union of balls, with holes) strictly inside the grid, negative
@@ -251,7 +275,7 @@ class RefSimulation:
     def setup(self, scene, tolerance=None):
         obstacles = getattr(scene, "obstacles", [])
         fluids = getattr(scene, "fluid_meshes", [])
-        if (obstacles or fluids) and self.PREFIX != "ref":
+        if (obstacles or fluids or getattr(scene, "sources", [])) and self.PREFIX != "ref":
             raise NotImplementedError("the oracle port restates the domain walls and loaded particles only; "
                                       "obstacle and fluid-mesh scenes are pinned by fixtures from the reference")
         if getattr(scene, "jitter_factor", None) is not None:
@@ -264,6 +288,13 @@ class RefSimulation:
             v = np.ascontiguousarray(v, np.float32)
             t = np.ascontiguousarray(t, np.int32)
             self.L.ref_add_mesh_obstacle(self.h, len(v), _p(v), len(t), _p(t), float(fr))
+        for src in getattr(scene, "sources", []):
+            v = np.ascontiguousarray(src["vertices"], np.float32)
+            t = np.ascontiguousarray(src["triangles"], np.int32)
+            self.L.ref_add_mesh_fluid_source(self.h, len(v), _p(v), len(t), _p(t), int(src.get("inflow", True)),
+                                             *(float(a) for a in src.get("velocity", (0.0, 0.0, 0.0))),
+                                             int(src.get("substep_emissions", 1)), int(src.get("constrained", True)),
+                                             int(src.get("fluid_outflow", True)), int(src.get("inversed", False)))
         self.L.ref_set_pic_ratio(self.h, scene.pic_ratio)
         self.L.ref_add_body_force(self.h, *scene.gravity)
         self.L.ref_set_cfl(self.h, scene.cfl)

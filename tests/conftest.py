@@ -66,7 +66,9 @@ def golden_cases(stages=False):
     fluid-mesh fixtures hold the particles after each frame)."""
     names = sorted(p.stem for p in GOLDEN.glob("*.npz") if not p.stem.startswith("iso_"))
     if stages:
-        names = [n for n in names if json.loads(str(np.load(GOLDEN / f"{n}.npz")["meta"])).get("builder") != "mesh_fluid"]
+        names = [n for n in names
+                 if json.loads(str(np.load(GOLDEN / f"{n}.npz")["meta"])).get("builder") not in ("mesh_fluid",
+                                                                                                 "fluid_sources")]
     return names
 
 

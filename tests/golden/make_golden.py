@@ -44,6 +44,13 @@ MESH_FLUID_CASES = {
     "mf32_both": (dict(n=32, which="both"), 3, 4),
     "mf32_box_jitter": (dict(n=32, which="box", jitter_factor=None), 1, 4),
 }
+# mesh fluid sources (scenes.fluid_sources): the particles after every frame
+SOURCE_CASES = {
+    "src24_inflow": (dict(n=24, which="inflow"), 6, 4),
+    "src24_outflow": (dict(n=24, which="outflow"), 9, 4),
+    "src24_both": (dict(n=24, which="both"), 8, 4),
+    "src24_inversed": (dict(n=24, which="inversed"), 9, 4),
+}
 # surface meshes (getIsomesh): the reference's mesher run on the particles
 # after frame 1 at each subdivision level (default smoothing), and the mesh
 # the reference made during frame 1 itself at the last level
@@ -80,18 +87,26 @@ def make(name, kwargs, frames, threads, tol, builder="dam_break"):
           f"{(OUT / f'{name}.npz').stat().st_size / 1024:.0f} KB")
 
 
-def make_mesh_fluid(name, kwargs, frames, threads):
-    sc = scenes.mesh_fluid(**kwargs)
+def make_mesh_fluid(name, kwargs, frames, threads, builder="mesh_fluid", keep=None):
+    """The particles after each frame (after the frames in `keep` only, and
+    the particle count after every frame, when given)."""
+    sc = getattr(scenes, builder)(**kwargs)
     ref = RefSimulation(sc.isize, sc.jsize, sc.ksize, sc.dx, threads=threads).setup(sc)
     data = {}
+    counts = []
     for f in range(1, frames + 1):
         ref.update(sc.frame_dt)
-        data[f"positions_{f}"], data[f"velocities_{f}"] = ref.particles()
-    meta = dict(scene=kwargs, builder="mesh_fluid", frames=frames, threads=threads, tolerance=sc.tolerance,
+        pos, vel = ref.particles()
+        counts.append(len(pos))
+        if keep is None or f in keep:
+            data[f"positions_{f}"], data[f"velocities_{f}"] = pos, vel
+    if keep is not None:
+        data["counts"] = np.array(counts, np.int32)
+    meta = dict(scene=kwargs, builder=builder, frames=frames, threads=threads, tolerance=sc.tolerance,
                 dt=sc.frame_dt, gravity=list(sc.gravity), pic_ratio=sc.pic_ratio, cfl=sc.cfl,
                 loaded=int(sc.num_particles), source="jklae/FLIPEngine3D src/engine via oracle/build_ref.sh")
     np.savez_compressed(OUT / f"{name}.npz", meta=np.array(json.dumps(meta)), **data)
-    print(name, "loaded", sc.num_particles, "->", [data[f"positions_{f}"].shape[0] for f in range(1, frames + 1)],
+    print(name, "loaded", sc.num_particles, "->", counts,
           f"{(OUT / f'{name}.npz').stat().st_size / 1024:.0f} KB")
 
 
@@ -128,6 +143,9 @@ if __name__ == "__main__":
     for name, (kw, frames, thr) in MESH_FLUID_CASES.items():
         if not only or name in only:
             make_mesh_fluid(name, kw, frames, thr)
+    for name, (kw, frames, thr) in SOURCE_CASES.items():
+        if not only or name in only:
+            make_mesh_fluid(name, kw, frames, thr, builder="fluid_sources", keep=(1, frames - 1, frames))
     for name, (builder, kw, levels, tol) in SURFACE_CASES.items():
         if not only or name in only:
             make_surface(name, builder, kw, levels, tol)
