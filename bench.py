@@ -358,7 +358,7 @@ def resident_scenes(rt, make, count, threads=16):
                 if not rt.admit(need):
                     rejected += 1
                     continue
-                sims.append(fg.FluidSimulation.from_scene(sc))
+                sims.append(fg.FluidSimulation.from_scene(sc, tuned=True))
     return sims, rejected
 
 

@@ -64,8 +64,9 @@ void launch_gather_particles(const ParticleSoA &src, ParticleSoA dst, const int 
                              const int *newStart, int ncells, unsigned int *maxSpeedSqBits, cudaStream_t s);
 
 // -- grid stages
+// threads: the CTA size, 256, 512 (default) or 1024
 void launch_liquid_sdf(const ParticleSoA &p, const int *cellStart, const StepConsts &c, const uint8_t *solidCC,
-                       float *phi, cudaStream_t s);
+                       float *phi, int threads, cudaStream_t s);
 void launch_p2g(const ParticleSoA &p, const int *cellStart, const StepConsts &c, float *u, float *v, float *w,
                 uint8_t *vu, uint8_t *vv, uint8_t *vw, cudaStream_t s);
 void launch_extrapolate(const StepConsts &c, float *u, float *v, float *w, const uint8_t *vu, const uint8_t *vv,
@@ -269,8 +270,10 @@ void sweep_epoch_guard(const StepConsts &c, SweepState &sw, long long upcoming, 
 void mic0_factor(const StepConsts &c, const uint8_t *fluid, const double4_32a *Ad, double *invD, double *W0,
                  double *W1, double *W2, int *progress, unsigned int *ticket, int *err, unsigned int spinLimit,
                  int lo, int hi, cudaStream_t s);
-int pressure_partials(const StepConsts &c);
-int pressure_partials_for(int I, int J, int K);
+// The reduction grid of the PCG row kernels: one CTA per `cellsPerCta` grid
+// cells (a tuning knob, default 4096), at most PCG_MAX_PARTIALS.
+constexpr int PCG_MAX_PARTIALS = 152 * 8;
+int pressure_partials_for(int I, int J, int K, int cellsPerCta = 4096);
 int mic0_factor_tiles(int J, int K);   // tiles of the wavefront factorisation
 // PressureSolver::solve (pressuresolver.cpp:44-76) on the device.  Returns
 // FLIP_OK (velocities updated, or nothing to solve), FLIP_E_SOLVER_NOCONV
@@ -281,6 +284,24 @@ int pressure_project(const StepConsts &c, const PressureArgs &a, PressureBuffers
 }  // namespace flip
 
 namespace flip {
+// -- viscosity (flip_viscosity.cu)
+struct ViscosityBuffers {
+    uint8_t *fluidFace, *valid, *valid2, *inSys;   // per face; per node (two); per face
+    float *node;                                   // corner values of one control-volume grid
+    float *vol[7];                                 // control-volume fractions
+    float4 *fac, *dr;                              // per face: six factors (two float4); {diag, rhs}
+    double *x, *r, *z, *p, *q, *part, *scal;       // CG vectors, partials (3 x blocks), scalars (8)
+};
+struct ViscosityResult {
+    long long rows;
+    int iterations;
+    double residual;   // |r|inf / |b|inf
+};
+void viscosity_buffer_sizes(int I, int J, int K, long long *nf, long long *nn, long long *ncorner,
+                            long long vol[7], int *reductionBlocks);
+int viscosity_apply(const StepConsts &c, const ViscosityBuffers &vb, const float *liquidPhi, const float *solidPhi,
+                    float *u, float *v, float *w, double visc, double dt, ViscosityResult *res, cudaStream_t s);
+
 // -- surface reconstruction (flip_mesh.cu)
 // The frame of the mesher's one compute chunk: the subdivided grid, its
 // blocks of 10^3 nodes, the chunk's nodes and offset, and the particle radii.

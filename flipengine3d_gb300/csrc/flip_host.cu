@@ -121,6 +121,16 @@ struct flip_ctx {
     int meshSmoothIterations = 2;
     double markerParticleScale = 3.0;
     MeshBuffers mesh;
+    // viscosity (setViscosity, fluidsimulation.cpp:1654-1670): off until set
+    bool viscosityEnabled = false;
+    double viscosity = 0.0;
+    ViscosityBuffers vb{};
+    bool vbReady = false;
+    ViscosityResult viscResult{};
+    // tuning knobs (flip_set_tuning): liquid-SDF CTA size, grid cells per
+    // CTA of the PCG row kernels; neither changes the results' meaning
+    int sdfThreads = 512;
+    int pcgCellsPerCta = 4096;
 
     // device buffers
     ParticleSoA pa{}, pb{};
@@ -265,8 +275,8 @@ int alloc_grids(flip_ctx *x) {
     CK(cudaMemsetAsync(p.L, 0, nsl * sizeof(float4), x->stream));
     CK(cudaMemsetAsync(p.rf, 0, nsl * sizeof(float), x->stream));
     CK(cudaMemsetAsync(p.z, 0, nsl * sizeof(float), x->stream));
-    p.nPartials = pressure_partials(x->c);
-    if ((rc = x->alloc(&p.partials, p.nPartials + 32)) || (rc = x->alloc(&p.scal, 8)) ||
+    p.nPartials = pressure_partials_for(x->I, x->J, x->K, x->pcgCellsPerCta);
+    if ((rc = x->alloc(&p.partials, PCG_MAX_PARTIALS + 32)) || (rc = x->alloc(&p.scal, 8)) ||
         (rc = x->alloc(&p.rmaxBits, 2)) || (rc = x->alloc(&p.levelRange, 8)) || (rc = x->alloc(&p.ctl, 1)) ||
         (rc = x->alloc(&p.factorProgress, mic0_factor_tiles(x->J, x->K))) || (rc = x->alloc(&p.factorTicket, 1)))
         return rc;
@@ -692,6 +702,40 @@ int dump_mac(flip_ctx *x, float *a, float *b, float *e, const float *u, const fl
     return FLIP_OK;
 }
 
+// The viscosity solve's device buffers, made with the first viscous step.
+int alloc_viscosity(flip_ctx *x) {
+    if (x->vbReady) return FLIP_OK;
+    long long nf, nn, ncorner, vol[7];
+    int rb;
+    viscosity_buffer_sizes(x->I, x->J, x->K, &nf, &nn, &ncorner, vol, &rb);
+    ViscosityBuffers &b = x->vb;
+    int rc;
+    if ((rc = x->alloc(&b.fluidFace, nf)) || (rc = x->alloc(&b.valid, nn)) || (rc = x->alloc(&b.valid2, nn)) ||
+        (rc = x->alloc(&b.inSys, nf)) || (rc = x->alloc(&b.node, ncorner)) || (rc = x->alloc(&b.fac, 2 * nf)) ||
+        (rc = x->alloc(&b.dr, nf)) || (rc = x->alloc(&b.x, nf)) || (rc = x->alloc(&b.r, nf)) ||
+        (rc = x->alloc(&b.z, nf)) || (rc = x->alloc(&b.p, nf)) || (rc = x->alloc(&b.q, nf)) ||
+        (rc = x->alloc(&b.part, 3 * (long long)rb)) || (rc = x->alloc(&b.scal, 8)))
+        return rc;
+    for (int g = 0; g < 7; g++)
+        if ((rc = x->alloc(&b.vol[g], vol[g]))) return rc;
+    x->vbReady = true;
+    return FLIP_OK;
+}
+
+// _applyViscosityToVelocityField (fluidsimulation.cpp:3592-3640): the field
+// constrained first, then the viscosity solve (flip_viscosity.cu).
+int apply_viscosity(flip_ctx *x, double dt) {
+    x->viscResult = ViscosityResult{};
+    if (!x->viscosityEnabled || x->n == 0 || !(x->viscosity > 0.0)) return FLIP_OK;
+    int rc = alloc_viscosity(x);
+    if (rc) return rc;
+    const bool fr = x->box.anyFriction;
+    launch_constrain(x->c, x->u, x->v, x->w, nullptr, nullptr, nullptr, x->wu, x->wv, x->ww, fr ? x->fu : nullptr,
+                     fr ? x->fv : nullptr, fr ? x->fw : nullptr, x->stream);
+    return viscosity_apply(x->c, x->vb, x->phi, x->solidPhi, x->u, x->v, x->w, x->viscosity, dt, &x->viscResult,
+                           x->stream);
+}
+
 // _stepFluid (fluidsimulation.cpp:5471-5508)
 int step_fluid(flip_ctx *x, double dt, flip_stage_dump *d) {
     cudaStream_t s = x->stream;
@@ -705,7 +749,7 @@ int step_fluid(flip_ctx *x, double dt, flip_stage_dump *d) {
     x->mark(FLIP_STAGE_LIQUID_SDF);
     // liquid level set (particlelevelset.cpp:161-196)
     if (x->n > 0 && x->solidBuilt) {
-        launch_liquid_sdf(x->pa, x->cellStart, c, x->solidCC, x->phi, s);
+        launch_liquid_sdf(x->pa, x->cellStart, c, x->solidCC, x->phi, x->sdfThreads, s);
     } else {
         std::vector<float> fill(x->nc(), (float)(3.0 * x->dx));
         float eps = (float)(0.005 * x->dx);
@@ -749,6 +793,7 @@ int step_fluid(flip_ctx *x, double dt, flip_stage_dump *d) {
                           (float)(bf.z * dt), std::fabs(bf.x) > feps, std::fabs(bf.y) > feps, std::fabs(bf.z) > feps,
                           ic.count ? x->inflowFaces : nullptr, s);
     if (d && (rc = dump_mac(x, d->u_force, d->v_force, d->w_force, x->u, x->v, x->w))) return rc;
+    if ((rc = apply_viscosity(x, dt))) return rc;
     // pressure (fluidsimulation.cpp:3732-3773)
     if (!x->solidBuilt) {
         if ((rc = build_solid(x))) return rc;
@@ -937,6 +982,10 @@ int do_initialize(flip_ctx *x) {
         CK(cudaMemsetAsync(x->cellStart, 0, (x->nc() + 1) * sizeof(int), s));
     }
     x->initialized = true;
+    // the static solid set-up, as the reference makes it on initialisation
+    // (it is redone before the next step if an obstacle or the CFL number
+    // changes)
+    if (!x->solidBuilt && (rc = build_solid(x))) return rc;
     return sync(x);
 }
 
@@ -1055,7 +1104,8 @@ int flip_reset_body_force(flip_ctx *x) {
 int flip_set_cfl_condition_number(flip_ctx *x, int n) {
     if (!x) return FLIP_E_NULL;
     if (n < 1) return fail(FLIP_E_DOMAIN, "Error: CFL must be greater than or equal to 1.");
-    if (x->solidBuilt) return fail(FLIP_E_RUNTIME, "CFL number is fixed once the simulation has stepped");
+    if (x->outputInitialized) return fail(FLIP_E_RUNTIME, "CFL number is fixed once the simulation has stepped");
+    if (n != (int)x->cfl) x->solidBuilt = false;   // the near-solid grid depends on it
     x->cfl = n;
     x->c.cfl = n;
     return FLIP_OK;
@@ -1423,7 +1473,7 @@ int flip_estimate_device_bytes(int isize, int jsize, int ksize, int particles, l
     b += faces * (4 * 3 + 1 + 1);                                        // weights, velocity, saved, valid, status
     b += nc * (1 + 32 + 32 + 8 * 5 + 4 * 2 + 4) + nsl * (16 + 4 + 4);     // pressure system
     b += (nc + 1) * 4 * 2 + nc * 4 * 2 + (scan_scratch_ints((int)nc) + 8) * 4;   // row list
-    b += (pressure_partials_for(isize, jsize, ksize) + 32) * 8 + 64 + 16 + 32;
+    b += (PCG_MAX_PARTIALS + 32) * 8 + 64 + 16 + 32;
     b += (mic0_factor_tiles(jsize, ksize) + 1) * 4 + 64;                  // factor tiles, ticket, control
     b += sweep_exchange_words(isize, jsize, ksize) * 8 + 4096;           // sweep exchange, ranges, tables
     b += cap * (7 * 4 * 2 + 4 * 4) + (scan_scratch_ints((int)cap) + 4) * 4 + 64;   // particles
@@ -1535,6 +1585,57 @@ int flip_fluid_source_setup(int isize, int jsize, int ksize, double dx, int nver
     *ncells = (int)g.cells.size();
     if (phi) std::memcpy(phi, g.phi.data(), g.phi.size() * sizeof(float));
     if (cells) std::memcpy(cells, g.cells.data(), g.cells.size() * sizeof(int));
+    return FLIP_OK;
+}
+
+int flip_set_viscosity(flip_ctx *x, double v) {
+    if (!x) return FLIP_E_NULL;
+    if (!(v >= 0.0)) return fail(FLIP_E_DOMAIN, "Error: viscosity must be greater than or equal to 0.");
+    x->viscosityEnabled = true;
+    x->viscosity = v;
+    return FLIP_OK;
+}
+int flip_get_viscosity(flip_ctx *x, double *v) {
+    if (!x || !v) return FLIP_E_NULL;
+    *v = x->viscosity;
+    return FLIP_OK;
+}
+int flip_get_viscosity_solve(flip_ctx *x, long long *rows, int *iterations, double *residual) {
+    if (!x) return FLIP_E_NULL;
+    if (rows) *rows = x->viscResult.rows;
+    if (iterations) *iterations = x->viscResult.iterations;
+    if (residual) *residual = x->viscResult.residual;
+    return FLIP_OK;
+}
+
+int flip_set_tuning(flip_ctx *x, const flip_tuning *t) {
+    if (!x || !t) return FLIP_E_NULL;
+    if (t->sdf_threads != 256 && t->sdf_threads != 512 && t->sdf_threads != 1024)
+        return fail(FLIP_E_DOMAIN, "sdf_threads must be 256, 512 or 1024");
+    if (t->pcg_cells_per_cta < 256 || t->pcg_cells_per_cta > (1 << 20))
+        return fail(FLIP_E_DOMAIN, "pcg_cells_per_cta must be in [256, 2^20]");
+    if (t->sweep_orientation < -1 || t->sweep_orientation > 1)
+        return fail(FLIP_E_DOMAIN, "sweep_orientation must be -1, 0 or 1");
+    cudaStreamSynchronize(x->stream);
+    x->sdfThreads = t->sdf_threads;
+    x->sweepOrientation = t->sweep_orientation;
+    if (t->pcg_cells_per_cta != x->pcgCellsPerCta) {
+        x->pcgCellsPerCta = t->pcg_cells_per_cta;
+        x->pr.nPartials = pressure_partials_for(x->I, x->J, x->K, x->pcgCellsPerCta);
+        for (int q = 0; q < 2; q++)   // the captured iteration batches hold the old grid
+            for (int o = 0; o < 2; o++)
+                if (x->pr.batchGraph[q][o]) {
+                    cudaGraphExecDestroy(x->pr.batchGraph[q][o]);
+                    x->pr.batchGraph[q][o] = nullptr;
+                }
+    }
+    return FLIP_OK;
+}
+int flip_get_tuning(flip_ctx *x, flip_tuning *t) {
+    if (!x || !t) return FLIP_E_NULL;
+    t->sdf_threads = x->sdfThreads;
+    t->pcg_cells_per_cta = x->pcgCellsPerCta;
+    t->sweep_orientation = x->sweepOrientation;
     return FLIP_OK;
 }
 

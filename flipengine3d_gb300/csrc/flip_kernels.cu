@@ -227,9 +227,8 @@ __device__ __forceinline__ bool in_block_list(float px, float py, float pz, floa
 // 16 warps per 10^3 block: the block's ~200 rows of candidate particles
 // then take about 6 passes per warp, where 8 warps leave the blocks of a
 // small scene (one wave of CTAs) bound by the latency of their atomics.
-#ifndef SDF_TPB
-#define SDF_TPB 512
-#endif
+// The CTA size is a tuning knob (256, 512 or 1024 threads; default 512).
+template <int SDF_TPB>
 __global__ void __launch_bounds__(SDF_TPB) k_liquid_sdf(ParticleSoA p, const int *cellStart, StepConsts c,
                                                         const uint8_t *solidCC, float *phi) {
     __shared__ unsigned int smin[BW * BW * BW];   // bits of the smallest squared distance (>= 0)
@@ -511,11 +510,11 @@ __global__ void k_constrain(long long nu, long long nv, long long nw, float *u, 
     const float wt = W[l];
     if (wt == 0.0f) {   // inside the solid: the solid's velocity (zero for static solids)
         G[l] = 0.0f;
-        S[l] = 0.0f;
+        if (S) S[l] = 0.0f;
     } else if (wt < 1.0f && F) {   // part solid: f usolid + (1 - f) u, usolid = 0
         const float fr = F[l], keep = __fsub_rn(1.0f, fr), us = __fmul_rn(fr, 0.0f);
         G[l] = __fadd_rn(us, __fmul_rn(keep, G[l]));
-        S[l] = __fadd_rn(us, __fmul_rn(keep, S[l]));
+        if (S) S[l] = __fadd_rn(us, __fmul_rn(keep, S[l]));
     }
 }
 
@@ -806,9 +805,12 @@ void launch_gather_particles(const ParticleSoA &src, ParticleSoA dst, const int 
     { FLIP_COUNT(1); k_gather<<<div_up(ncells, TPB), TPB, 0, s>>>(src, dst, cellStart, slots, newStart, ncells, maxSpeedSqBits); }
 }
 void launch_liquid_sdf(const ParticleSoA &p, const int *cellStart, const StepConsts &c, const uint8_t *solidCC,
-                       float *phi, cudaStream_t s) {
+                       float *phi, int threads, cudaStream_t s) {
     dim3 grid(div_up(c.I, BW), div_up(c.J, BW), div_up(c.K, BW));
-    { FLIP_COUNT(1); k_liquid_sdf<<<grid, SDF_TPB, 0, s>>>(p, cellStart, c, solidCC, phi); }
+    FLIP_COUNT(1);
+    if (threads == 256) k_liquid_sdf<256><<<grid, 256, 0, s>>>(p, cellStart, c, solidCC, phi);
+    else if (threads == 1024) k_liquid_sdf<1024><<<grid, 1024, 0, s>>>(p, cellStart, c, solidCC, phi);
+    else k_liquid_sdf<512><<<grid, 512, 0, s>>>(p, cellStart, c, solidCC, phi);
 }
 void launch_p2g(const ParticleSoA &p, const int *cellStart, const StepConsts &c, float *u, float *v, float *w,
                 uint8_t *vu, uint8_t *vv, uint8_t *vw, cudaStream_t s) {

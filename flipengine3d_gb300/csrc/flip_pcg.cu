@@ -785,16 +785,14 @@ int cuda_fail(cudaError_t e, const char *what, std::string *msg) {
 
 }  // namespace
 
-int pressure_partials(const StepConsts &c) { return pressure_partials_for(c.I, c.J, c.K); }
 int mic0_factor_tiles(int J, int K) { return std::max(1, (J - 2 + FT - 1) / FT) * std::max(1, (K - 2 + FT - 1) / FT); }
-int pressure_partials_for(int I, int J, int K) {
-// One reduction CTA per 4096 grid cells, at most RBLOCKS.  A liquid fills a
-// fraction of the grid, so a thread takes a few rows; a smaller grid spares
-// the GPU's CTA dispatch, which many scenes running at once share.
-#ifndef PCG_CELLS_PER_CTA
-#define PCG_CELLS_PER_CTA 4096
-#endif
-    return std::min((int)div_up((long long)I * J * K, PCG_CELLS_PER_CTA), RBLOCKS);
+// One reduction CTA per `cellsPerCta` grid cells (4096 by default), at most
+// RBLOCKS.  A liquid fills a fraction of the grid, so a thread takes a few
+// rows; a smaller grid spares the GPU's CTA dispatch, which many scenes
+// running at once share.
+int pressure_partials_for(int I, int J, int K, int cellsPerCta) {
+    static_assert(RBLOCKS == PCG_MAX_PARTIALS, "the partials buffer holds RBLOCKS sums");
+    return std::min((int)div_up((long long)I * J * K, std::max(cellsPerCta, 256)), RBLOCKS);
 }
 
 #define PCK(call)                                               \

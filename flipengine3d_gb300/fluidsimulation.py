@@ -52,6 +52,11 @@ class FluidSourceParams(C.Structure):
                 ("velocity", C.c_double * 3)]
 
 
+class Tuning(C.Structure):
+    """flip_tuning (include/flip3d.h)."""
+    _fields_ = [("sdf_threads", C.c_int), ("pcg_cells_per_cta", C.c_int), ("sweep_orientation", C.c_int)]
+
+
 class StageDump(C.Structure):
     _fields_ = [(n, C.c_void_p) for n in (
         "phi", "u_p2g", "v_p2g", "w_p2g", "vu_p2g", "vv_p2g", "vw_p2g",
@@ -130,6 +135,11 @@ SIGNATURES = {
     "flip_get_mesh_fluid_source_params": [_P, _I, C.POINTER(FluidSourceParams)],
     "flip_remove_mesh_fluid_source": [_P, _I],
     "flip_fluid_source_setup": [_I, _I, _I, _D, _I, _P, _I, _P, _P, _P, _P, C.POINTER(C.c_int), _P],
+    "flip_set_viscosity": [_P, _D],
+    "flip_get_viscosity": [_P, C.POINTER(C.c_double)],
+    "flip_get_viscosity_solve": [_P, C.POINTER(C.c_longlong), C.POINTER(C.c_int), C.POINTER(C.c_double)],
+    "flip_set_tuning": [_P, C.POINTER(Tuning)],
+    "flip_get_tuning": [_P, C.POINTER(Tuning)],
     "flip_enable_surface_reconstruction": [_P, _I],
     "flip_is_surface_reconstruction_enabled": [_P, C.POINTER(C.c_int)],
     "flip_set_surface_subdivision_level": [_P, _I],
@@ -559,6 +569,39 @@ class FluidSimulation:
         self._c(self._lib.flip_get_frame_stats(self._h, C.byref(s)))
         return s
 
+    # -- viscosity (fluidsimulation.cpp:1650-1670, 3592-3640)
+    def setViscosity(self, v: float):
+        self._c(self._lib.flip_set_viscosity(self._h, float(v)))
+
+    def getViscosity(self) -> float:
+        v = C.c_double()
+        self._c(self._lib.flip_get_viscosity(self._h, C.byref(v)))
+        return v.value
+
+    def viscosity_solve(self):
+        """(rows, iterations, relative residual) of the last substep's viscosity solve."""
+        rows, it, res = C.c_longlong(), C.c_int(), C.c_double()
+        self._c(self._lib.flip_get_viscosity_solve(self._h, C.byref(rows), C.byref(it), C.byref(res)))
+        return rows.value, it.value, res.value
+
+    # -- tuning knobs (flip_set_tuning; flipengine3d_gb300.autotune)
+    def setTuning(self, sdf_threads: int = 512, pcg_cells_per_cta: int = 4096, sweep_orientation: int = -1):
+        t = Tuning(int(sdf_threads), int(pcg_cells_per_cta), int(sweep_orientation))
+        self._c(self._lib.flip_set_tuning(self._h, C.byref(t)))
+
+    def getTuning(self) -> dict:
+        t = Tuning()
+        self._c(self._lib.flip_get_tuning(self._h, C.byref(t)))
+        return {"sdf_threads": t.sdf_threads, "pcg_cells_per_cta": t.pcg_cells_per_cta,
+                "sweep_orientation": t.sweep_orientation}
+
+    def applyTunedSettings(self):
+        """The autotuner's settings for this grid (the nearest edge of
+        flipengine3d_gb300/tuning_gb300.json; defaults without a table)."""
+        from .autotune import lookup
+        I, J, K = self.dims
+        self.setTuning(**lookup(I, J, K))
+
     # -- mesh fluid sources (fluidsimulation.cpp:1953-1992)
     @staticmethod
     def _source_params(inflow=True, enabled=True, substep_emissions=1, constrained=True, fluid_outflow=True,
@@ -759,12 +802,14 @@ class FluidSimulation:
         return out
 
     @classmethod
-    def from_scene(cls, scene, tolerance=None, surface_subdivisions=None):
+    def from_scene(cls, scene, tolerance=None, surface_subdivisions=None, tuned=False):
         """Set up a seeded scene (flipengine3d_gb300.scenes) the way the
         reference's headless driver does: surface reconstruction off (or on
         at the given subdivision level), PIC ratio, gravity, CFL, tolerance,
-        particles, initialize."""
+        particles, initialize; `tuned` applies the autotuner's settings."""
         sim = cls(scene.isize, scene.jsize, scene.ksize, scene.dx)
+        if tuned:
+            sim.applyTunedSettings()
         if surface_subdivisions is None:
             sim.disableSurfaceReconstruction()
         else:
@@ -777,6 +822,8 @@ class FluidSimulation:
             sim.addMeshObstacle(*ob)
         if getattr(scene, "jitter_factor", None) is not None:
             sim.setMarkerParticleJitterFactor(scene.jitter_factor)
+        if getattr(scene, "viscosity", None) is not None:
+            sim.setViscosity(scene.viscosity)
         for fm in getattr(scene, "fluid_meshes", []):
             sim.addMeshFluid(*fm)
         for src in getattr(scene, "sources", []):

@@ -40,6 +40,7 @@ class Scene:
     # inflow (bool), velocity xyz, substep_emissions, constrained,
     # fluid_outflow, inversed
     sources: list = field(default_factory=list)
+    viscosity: float | None = None       # setViscosity, when set
 
     @property
     def num_particles(self) -> int:

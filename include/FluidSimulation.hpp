@@ -192,6 +192,14 @@ public:
         check(flip_get_pic_flip_ratio(ctx_, &r));
         return r;
     }
+    // setViscosity / getViscosity (fluidsimulation.cpp:1650-1670)
+    void setViscosity(double v) { check(flip_set_viscosity(ctx_, v)); }
+    double getViscosity() {
+        double v = 0.0;
+        check(flip_get_viscosity(ctx_, &v));
+        return v;
+    }
+
     // No effect: the step runs on the GPU; kept for drivers that call it.
     void setMaxThreadCount(int) {}
 

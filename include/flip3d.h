@@ -289,6 +289,36 @@ int flip_mic0_precondition(int isize, int jsize, int ksize, const uint8_t *fluid
 /* Number of this library's kernel launches issued so far on the context. */
 int flip_get_launch_count(flip_ctx *ctx, long long *count);
 
+/* setViscosity / getViscosity (fluidsimulation.cpp:1650-1670): a constant
+ * viscosity >= 0 (FLIP_E_DOMAIN otherwise) turns the viscosity step on;
+ * each substep then constrains the field and solves Batty's variational
+ * viscosity system after the body force (_applyViscosityToVelocityField,
+ * :3592-3640).  The system's set-up (face states, liquid volume fractions,
+ * rows) is the reference's; it is solved by Jacobi-preconditioned CG in
+ * FP64 to a relative residual of 1e-9, where the reference runs an FP32
+ * MIC(0)-PCG to 1e-4, so velocities agree to the reference's own solver
+ * tolerance.  flip_get_viscosity_solve reports the last substep's system
+ * size, iterations and relative residual (rows 0: the solve did not run). */
+int flip_set_viscosity(flip_ctx *ctx, double viscosity);
+int flip_get_viscosity(flip_ctx *ctx, double *viscosity);
+int flip_get_viscosity_solve(flip_ctx *ctx, long long *rows, int *iterations, double *residual);
+
+/* Tuning knobs of the device kernels, no counterpart in the reference: the
+ * liquid-SDF CTA size (256, 512 or 1024 threads), the grid cells per CTA of
+ * the PCG row kernels' reduction grid (256 .. 2^20), and the preconditioner
+ * sweep orientation (as flip_set_sweep_orientation).  A different reduction
+ * grid sums the PCG's dot products in another order, so results move in the
+ * last bits; the others leave them as they are.  Defaults 512, 4096, -1.
+ * flipengine3d_gb300/autotune.py measures them per grid size and writes the
+ * table the Python face applies. */
+typedef struct flip_tuning {
+    int sdf_threads;
+    int pcg_cells_per_cta;
+    int sweep_orientation;
+} flip_tuning;
+int flip_set_tuning(flip_ctx *ctx, const flip_tuning *tuning);
+int flip_get_tuning(flip_ctx *ctx, flip_tuning *tuning);
+
 /* Mesh fluid sources: addMeshFluidSource / removeMeshFluidSource
  * (fluidsimulation.cpp:1953-1992) with a static MeshFluidSource
  * (meshfluidsource.h).  The mesh (arrays as flip_add_mesh_obstacle) is

@@ -264,6 +264,7 @@ int ref_update_staged(void *h, double dt, RefStageDump *d) {
     s->_saveVelocityField();
     s->_applyBodyForcesToVelocityField(step);
     if (d->u_force) ref_get_mac(h, d->u_force, d->v_force, d->w_force);
+    s->_applyViscosityToVelocityField(step);   // no-op unless setViscosity was called
 
     // _pressureSolve with PressureSolver::solve expanded so the solution
     // vector is visible (src/engine/pressuresolver.cpp:44-76)
@@ -574,6 +575,15 @@ void ref_fluid_source_setup(int I, int J, int K, double dx, int nverts, const fl
     *ncells = (int)cs.size();
     if (cells)
         for (size_t q = 0; q < cs.size(); q++) cells[q] = cs[q].i + I * (cs[q].j + J * cs[q].k);
+}
+
+// setViscosity (fluidsimulation.cpp:1654-1670)
+void ref_set_viscosity(void *h, double v) { ((RefSim *)h)->sim->setViscosity(v); }
+// the viscosity solver's status line of the last substep (empty when it did not run)
+const char *ref_viscosity_status(void *h) {
+    RefSim *r = (RefSim *)h;
+    r->status = r->sim->_viscositySolverStatus;
+    return r->status.c_str();
 }
 
 // Surface reconstruction settings (fluidsimulation.cpp:216-300, 367-376):

@@ -79,6 +79,10 @@ def lib(prefix: str = "ref"):
             L.ref_fluid_source_setup.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, C.c_int, C.c_void_p, C.c_int,
                                                  C.c_void_p] + [C.c_void_p] * 5
             L.ref_fluid_source_setup.restype = None
+            L.ref_set_viscosity.argtypes = [C.c_void_p, C.c_double]
+            L.ref_set_viscosity.restype = None
+            L.ref_viscosity_status.argtypes = [C.c_void_p]
+            L.ref_viscosity_status.restype = C.c_char_p
             L.ref_set_surface_reconstruction.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_double, C.c_int]
             L.ref_set_surface_reconstruction.restype = None
             L.ref_mesh_now.argtypes = [C.c_void_p]
@@ -280,6 +284,8 @@ class RefSimulation:
                                       "obstacle and fluid-mesh scenes are pinned by fixtures from the reference")
         if getattr(scene, "jitter_factor", None) is not None:
             self.L.ref_set_jitter_factor(self.h, float(scene.jitter_factor))
+        if getattr(scene, "viscosity", None) is not None:
+            self.L.ref_set_viscosity(self.h, float(scene.viscosity))
         for v, t, vel in fluids:
             v = np.ascontiguousarray(v, np.float32)
             t = np.ascontiguousarray(t, np.int32)

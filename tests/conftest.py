@@ -55,6 +55,11 @@ def gpu(built):
     return True
 
 
+def viscosity_cases():
+    """Fixtures of scenes with viscosity (visc*.npz)."""
+    return sorted(p.stem for p in GOLDEN.glob("visc*.npz"))
+
+
 def surface_cases():
     """Fixtures of the reference's surface meshes (iso_*.npz)."""
     return sorted(p.stem for p in GOLDEN.glob("iso_*.npz"))
@@ -64,7 +69,7 @@ def golden_cases(stages=False):
     """Fixture names of simulation states (not the surface meshes); with
     stages, only those holding the first frame stage by stage (the
     fluid-mesh fixtures hold the particles after each frame)."""
-    names = sorted(p.stem for p in GOLDEN.glob("*.npz") if not p.stem.startswith("iso_"))
+    names = sorted(p.stem for p in GOLDEN.glob("*.npz") if not p.stem.startswith(("iso_", "visc")))
     if stages:
         names = [n for n in names
                  if json.loads(str(np.load(GOLDEN / f"{n}.npz")["meta"])).get("builder") not in ("mesh_fluid",
