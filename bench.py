@@ -273,6 +273,7 @@ def run_gpu(args, rank, world):
     step_achieved = (base_b + pcg_b) * substeps / (sum(stage_ms.values()) / 1e3) / 1e9
 
     cpu = cpu_baseline(args) if not args.no_cpu_baseline else None
+    surface = run_surface(args, fg, stream) if world == 1 else None
     plain60 = run_full_length(args, fg, stream, flush) if (not args.no_full_length and world == 1) else None
     batched = served = None
     if not args.no_batched and world == 1:
@@ -312,6 +313,7 @@ def run_gpu(args, rank, world):
                      "stage_ms_per_step": {k: round(v / args.steps, 3) for k, v in stage_ms.items()}},
         "cpu_baseline": cpu,
         "plain_60": plain60,
+        "surface": surface,
         "batched": batched,
         "served": served,
         "gpu_launches": int(launches),
@@ -319,6 +321,37 @@ def run_gpu(args, rank, world):
         "clocks": clocks.summary(),
     }
     return line
+
+
+def run_surface(args, fg, stream, reps=5):
+    """getIsomesh at the benchmark workload: the 128^3 state after the
+    warm-up frames, meshed at subdivision levels 1 and 2 (FluidManager uses 2)
+    `reps` times each; wall clock per mesh with the device synchronised (the
+    mesher synchronises twice to size its outputs)."""
+    import torch
+    sc = make_scene(args.scene)
+    sim = fg.FluidSimulation.from_scene(sc)
+    sim.setStream(stream.cuda_stream)
+    for _ in range(args.warmup):
+        sim.update(FRAME_DT)
+    out = {"particles": sim.getNumMarkerParticles()}
+    for level in (1, 2):
+        sim.setSurfaceSubdivisionLevel(level)
+        sim.buildIsomesh()   # buffers sized
+        torch.cuda.synchronize()
+        ts = []
+        for _ in range(reps):
+            t0 = time.perf_counter()
+            sim.buildIsomesh()
+            torch.cuda.synchronize()
+            ts.append(time.perf_counter() - t0)
+        v, t = sim.getIsomesh()
+        out[f"subdivision_{level}"] = {"ms_per_mesh": round(1e3 * float(np.median(ts)), 3), "vertices": len(v),
+                                       "triangles": len(t)}
+    sim.close()
+    out["how"] = ("buildIsomesh() on the state after the warm-up frames; median wall clock of " + str(reps) +
+                  " meshes, device synchronised; vertices and triangles bit-identical to the reference's mesher")
+    return out
 
 
 def run_full_length(args, fg, stream, flush):
@@ -564,6 +597,8 @@ def main():
     ap.add_argument("--requests", type=int, default=800)
     ap.add_argument("--served-scenes", type=int, default=256)
     ap.add_argument("--arrival-rate", type=float, default=2000.0)
+    ap.add_argument("--surface-only", action="store_true",
+                    help="only the getIsomesh timing (a short run for profiling the mesher)")
     ap.add_argument("--scene", default="plain_128", choices=sorted(SCENES),
                     help="plain_128 is the benchmark workload; plain_64 is the small case for profiling")
     args = ap.parse_args()
@@ -573,7 +608,11 @@ def main():
         import torch
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
         torch.distributed.init_process_group("nccl")
-    if args.impl == "reference":
+    if args.surface_only:
+        import torch
+        import flipengine3d_gb300 as fg
+        line = {"surface": run_surface(args, fg, torch.cuda.Stream())}
+    elif args.impl == "reference":
         line = run_reference(args, rank, world)
     else:
         line = run_gpu(args, rank, world)

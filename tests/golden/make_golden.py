@@ -54,8 +54,9 @@ SOURCE_CASES = {
 # viscosity (setViscosity): dam break + sphere with a constant viscosity;
 # the particles after every frame and the viscosity solver's status
 VISCOSITY_CASES = {
-    "visc20": (dict(n=20, seed=1, sphere=True), 0.1, 3),
-    "visc16_thin": (dict(n=16, seed=4), 0.01, 2),
+    "visc20": ("dam_break", dict(n=20, seed=1, sphere=True), 0.1, 3),
+    "visc16_thin": ("dam_break", dict(n=16, seed=4), 0.01, 2),
+    "visc20_box": ("dam_with_obstacles", dict(n=20, seed=6, which="box"), 0.05, 2),
 }
 # surface meshes (getIsomesh): the reference's mesher run on the particles
 # after frame 1 at each subdivision level (default smoothing), and the mesh
@@ -138,8 +139,8 @@ def make_surface(name, builder, kwargs, levels, tol):
           f"{(OUT / f'{name}.npz').stat().st_size / 1024:.0f} KB")
 
 
-def make_viscosity(name, kwargs, viscosity, frames):
-    sc = scenes.dam_break(**kwargs)
+def make_viscosity(name, builder, kwargs, viscosity, frames):
+    sc = getattr(scenes, builder)(**kwargs)
     sc.viscosity = viscosity
     ref = RefSimulation(sc.isize, sc.jsize, sc.ksize, sc.dx, threads=1).setup(sc, tolerance=1e-9)
     data, status = {}, []
@@ -147,7 +148,7 @@ def make_viscosity(name, kwargs, viscosity, frames):
         ref.update(sc.frame_dt)
         data[f"positions_{f}"], data[f"velocities_{f}"] = ref.particles()
         status.append(ref.L.ref_viscosity_status(ref.h).decode())
-    meta = dict(scene=kwargs, builder="dam_break", viscosity=viscosity, frames=frames, tolerance=1e-9,
+    meta = dict(scene=kwargs, builder=builder, viscosity=viscosity, frames=frames, tolerance=1e-9,
                 dt=sc.frame_dt, gravity=list(sc.gravity), pic_ratio=sc.pic_ratio, cfl=sc.cfl, status=status,
                 source="jklae/FLIPEngine3D src/engine via oracle/build_ref.sh")
     np.savez_compressed(OUT / f"{name}.npz", meta=np.array(json.dumps(meta)), **data)
@@ -169,9 +170,9 @@ if __name__ == "__main__":
     for name, (kw, frames, thr) in SOURCE_CASES.items():
         if not only or name in only:
             make_mesh_fluid(name, kw, frames, thr, builder="fluid_sources", keep=(1, frames - 1, frames))
-    for name, (kw, visc, frames) in VISCOSITY_CASES.items():
+    for name, (builder, kw, visc, frames) in VISCOSITY_CASES.items():
         if not only or name in only:
-            make_viscosity(name, kw, visc, frames)
+            make_viscosity(name, builder, kw, visc, frames)
     for name, (builder, kw, levels, tol) in SURFACE_CASES.items():
         if not only or name in only:
             make_surface(name, builder, kw, levels, tol)

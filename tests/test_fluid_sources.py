@@ -116,3 +116,32 @@ def test_gpu_source_calls(gpu):
         sim.setMeshFluidSource(ids[0], enabled=False)
         sim.update(1.0 / 60.0)
         assert sim.getNumMarkerParticles() <= n   # nothing emitted while disabled
+
+
+@pytest.mark.gpu
+def test_gpu_source_emissions_and_removal(gpu):
+    """With the seeding jitter at zero, emitting twice per substep adds
+    nothing (every sub-cell the second emission would fill is taken, as in
+    the reference's mask); removing the source mid-run stops emission."""
+    sc = scenes.fluid_sources(24, which="inflow")
+    counts = {}
+    for emissions in (1, 2):
+        sc.sources[0]["substep_emissions"] = emissions
+        with fs.FluidSimulation.from_scene(sc) as sim:
+            for _ in range(3):
+                sim.update(sc.frame_dt)
+            counts[emissions] = sim.getNumMarkerParticles()
+            pos = sim.getMarkerParticlePositionData()
+            if emissions == 1:
+                first = pos
+            else:
+                assert np.array_equal(pos, first)
+    assert counts[1] == counts[2]
+    sc.sources[0]["substep_emissions"] = 1
+    with fs.FluidSimulation.from_scene(sc) as sim:
+        sim.update(sc.frame_dt)
+        sim.removeMeshFluidSource(0)
+        n = sim.getNumMarkerParticles()
+        for _ in range(2):
+            sim.update(sc.frame_dt)
+        assert sim.getNumMarkerParticles() <= n

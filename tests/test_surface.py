@@ -179,3 +179,18 @@ def test_gpu_surface_settings(gpu):
         ov, ot = mesh_particles(sim.getMarkerParticlePositionData(), sc.isize, sc.jsize, sc.ksize, sc.dx,
                                 sim.solid_sdf(), 1, smooth_iterations=0)
         assert np.array_equal(v3, ov) and np.array_equal(t3, ot)
+
+
+@pytest.mark.gpu
+def test_gpu_isomesh_subdivision_three_with_an_obstacle(gpu):
+    """Subdivision 3 (no aligned shortcut for the solid nodes, interpolated
+    solid samples everywhere) around a sphere obstacle, against the oracle."""
+    sc = scenes.dam_with_obstacles(20, seed=5, which="sphere")
+    with fs.FluidSimulation.from_scene(sc, surface_subdivisions=3) as sim:
+        for _ in range(2):
+            sim.update(sc.frame_dt)
+        v, t = sim.getIsomesh()
+        pos = sim.getMarkerParticlePositionData()
+        ov, ot = mesh_particles(pos, sc.isize, sc.jsize, sc.ksize, sc.dx, sim.solid_sdf(), 3)
+    assert len(t) > 0
+    assert np.array_equal(t, ot) and np.array_equal(v, ov)
