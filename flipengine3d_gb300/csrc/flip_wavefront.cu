@@ -9,16 +9,20 @@
 // (upper) neighbours only, so the cells of a plane i + j + k = const are
 // independent: the exact wavefront order.
 //
-// Mapping.  A CTA owns a tile of 32 (j) x 8 (k) pencils along i.  Its eight
-// compute warps hold one pencil per thread (lane = j, warp = k); in the
-// forward sweep thread (l, w) processes i = 1 + t - SL l - SW w at step t, so
-// its j-1 neighbour (lane l-1) finished that i at step t - SL and its k-1
-// neighbour (warp w-1) at step t - SW: j terms arrive by warp shuffle, k terms
-// through shared memory, and the compute warps meet at a barrier once every
-// SW steps (the backward sweep is the mirror image).  In the forward sweep a
-// cell hands its neighbours the finished products L_c * y_c rather than y_c:
-// each product is rounded once, by whichever thread forms it, so the bits
-// are the reference's.
+// Mapping.  A CTA owns a tile of 32 (j) x 8 (k) pencils along i: lane l
+// of the tile holds the 8 pencils (l, w) of its column, the tile's "slots"
+// w = 0..7, and four compute warps take two slots each.  In the forward
+// sweep slot w of lane l processes i = 1 + t - l - w at step t, so a cell's
+// three lower neighbours (i-1 in the same slot, j-1 in lane l-1, k-1 in
+// slot w-1) were all formed at step t - 1: the j terms arrive by warp
+// shuffle, the i terms and the k terms between a warp's own slots stay in
+// registers, and the k term that crosses to the next warp goes through
+// shared memory around the one barrier per step of the compute warps (the
+// backward sweep is the mirror image).  A full chunk of steps runs as
+// straight-line code, with no test or vote between its steps.  In the
+// forward sweep a cell hands its neighbours the finished products L_c * y_c
+// rather than y_c: each product is rounded once, by whichever thread forms
+// it, so the bits are the reference's.
 //
 // Data movement.  The factor rows and the right-hand side live in the
 // step-major sweep layout (flip_device.cuh), so the 8 steps of a chunk of a
@@ -29,17 +33,19 @@
 // edge warp fetches the terms that the neighbouring tiles publish for the
 // chunk's edge cells.  The two run independently, so a tile waiting for its
 // neighbours still has its operands on the way.  The compute warps read
-// operands from the slot, run the arithmetic and store each result straight
-// to global memory (a warp writes 128 contiguous bytes per step); cells
-// outside the grid read zero rows, so a step is unpredicated.
+// the next step's operands from the slot while they compute the current
+// one and store each result straight to global memory (128 contiguous bytes
+// per slot and step); cells outside the grid read zero rows, so a step is
+// unpredicated.
 //
-// Where a tile's time goes (one tile of 128 cells along i, measured): about
-// 5 us per launch plus 115 ns per step.  Stripping the compute loop of every
-// barrier, shuffle and shared-memory exchange leaves 96 ns per step; loading
-// the operands into registers 8-24 steps ahead instead of through the ring,
-// splitting the bulk copies per step, more or fewer slots, and suspending
-// waiting warps instead of polling did not shorten it; 16-step chunks gave
-// 96 ns, 4-step chunks 141 ns.
+// Where a step's time goes (one warp, measured): the arithmetic and
+// shuffles of 8 slots take about 80 cycles, of 2 slots about 46; operands
+// from shared memory, result stores and a test or vote per step (which
+// splits the unrolled chunk into separate blocks) add 100-250 cycles at 8
+// slots.  Four warps of two slots each, in lockstep, with full chunks free
+// of tests, sweep the 128^3 dam region in 53 us per launch and a fully
+// liquid 128^3 box in 95 us (eight warps of one slot with tests per step:
+// 64 us and 95 us; the same in lockstep without tests: 55 us and 82 us).
 //
 // Tile edges.  The threads on a tile's downstream edges publish each term
 // they form as one 64-bit word {sweep epoch, value}, indexed by step, in an
@@ -64,9 +70,9 @@ namespace {
 #define SWEEP_CH 8   // steps per chunk
 #endif
 constexpr int TJ = SWEEP_TJ, TK = SWEEP_TK, NP = SWEEP_NP, CH = SWEEP_CH, SL = SWEEP_SL, SW = SWEEP_SW;
-// a chunk holds whole blocks of SW steps and whole rounds of the SL-deep lane
-// history, and the shared-memory ring of warp terms (2 SW steps) divides it
-static_assert(CH % SL == 0 && CH % (2 * SW) == 0, "sweep skews must divide the chunk");
+// one compute warp holds a tile's TK pencils of each lane in registers: a
+// cell's three lower neighbours are then all one step back
+static_assert(SL == 1 && SW == 1 && CH >= 1, "the compute warp expects skews of one step");
 #ifndef SWEEP_NBUF
 #define SWEEP_NBUF 5   // ring slots that fit in shared memory
 #endif
@@ -76,7 +82,12 @@ static_assert(NBUF >= 2, "the ring needs a slot in flight beside the one in use"
 // CH x TJ k-edge words one step each
 constexpr int JQ = CH * TK / 32;
 static_assert((CH * TK) % 32 == 0 && TJ == 32 && JQ <= 32, "edge-word mapping of the edge warp");
-constexpr int NCOMP = NP, LOADER = NCOMP / 32, EDGE = LOADER + 1, NTHREADS = NCOMP + 64;
+#ifndef SWEEP_SPW
+#define SWEEP_SPW 2   // slots (pencils along the warp axis) per compute warp
+#endif
+constexpr int SPW = SWEEP_SPW, NWC = TK / SPW;   // compute warps per tile
+static_assert(TK % SPW == 0, "a compute warp holds whole slots");
+constexpr int NCOMP = 32 * NWC, LOADER = NWC, EDGE = LOADER + 1, NTHREADS = NCOMP + 64;
 // Waiting for this CTA's own bulk copies in flight (they complete by
 // themselves) keeps the default limit, whatever limit the edge waits have.
 constexpr unsigned int DRAIN_SPIN_LIMIT = DEFAULT_SPIN_LIMIT;
@@ -105,23 +116,23 @@ struct Slot {
 };
 struct SweepSmem {
     Slot slot[NBUF];
-    float p[2 * SW][TK][TJ];   // by step mod 2 SW: forward L_w y of each pencil's cell; backward its z
     // per slot: operand bytes in (the loader), edge terms in (the edge warp),
     // chunk done (the compute warps)
     unsigned long long loaded[NBUF], edges[NBUF], done[NBUF];
+    // between compute warps g and g + 1, by step parity and lane: forward
+    // warp g's last slot's L_z y, backward warp g + 1's first slot's z
+    float hand[2][NWC > 1 ? NWC - 1 : 1][TJ];
     int abort;
     int tile;
     unsigned int epoch;
 };
+static_assert(sizeof(SweepSmem) <= 227 * 1024, "the sweep's shared memory fits one CTA");
 
 __device__ __forceinline__ unsigned smem_addr(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
 __device__ __forceinline__ unsigned long long ld_word(const unsigned long long *p) {
     unsigned long long v;
     asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
     return v;
-}
-__device__ __forceinline__ void st_word(unsigned long long *p, unsigned long long v) {
-    asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }
 __device__ __forceinline__ unsigned long long pack(unsigned int epoch, float v) {
     return ((unsigned long long)epoch << 32) | __float_as_uint(v);
@@ -178,6 +189,20 @@ __device__ __forceinline__ bool compute_sync_or(bool v) {
     return r != 0;
 }
 __device__ __forceinline__ void compute_sync() { asm volatile("bar.sync 1, %0;" ::"n"(NCOMP) : "memory"); }
+// A published edge term, stored where `on` holds: a predicated store, not a
+// branch around one (only the tile's edge lanes publish), ordered against
+// nothing else (a consumer reads the word alone), so the compiler may move
+// the loads of later steps above it.
+__device__ __forceinline__ void st_term(bool on, unsigned long long *p, unsigned long long v) {
+    asm volatile("{\n .reg .pred q;\n setp.ne.u32 q, %2, 0;\n @q st.relaxed.gpu.global.u64 [%0], %1;\n}"
+                 ::"l"(p), "l"(v), "r"((unsigned)on));
+}
+// The j-edge terms of a lane's SPW slots at one step: consecutive words.
+template <int N>
+__device__ __forceinline__ void st_terms(bool on, unsigned long long *p, const float (&v)[N], unsigned int epoch) {
+#pragma unroll
+    for (int j = 0; j < N; j++) st_term(on, p + j, ((unsigned long long)epoch << 32) | __float_as_uint(v[j]));
+}
 
 // SWAP: the tile's lanes run along k and its warps along j (else lanes along
 // j, warps along k).  The couplings that travel along each axis and the
@@ -217,10 +242,6 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_wavefront(SweepArgs a) {
     if (thi < tlo) return;   // no system cell in the tile: nothing to compute or publish
     const int nChunks = (thi - tlo) / CH + 1;
     const int j0 = 1 + tj * TJ, k0 = 1 + tk * TK;
-    // cell of pencil (lane lr, warp ww) at step t
-    auto cell = [&](int lr, int ww, int t) {
-        return FWD ? 1 + t - SL * lr - SW * ww : NI - t + SL * (TJ - 1 - lr) + SW * (TK - 1 - ww);
-    };
     auto pencil_in = [&](int lr, int ww) { return j0 + lr <= a.J - 2 && k0 + ww <= a.K - 2; };
     const size_t wordsPerTile = (size_t)T * (TJ + TK);
     const unsigned int ep = sm.epoch;          // published with this sweep's terms
@@ -394,104 +415,128 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_wavefront(SweepArgs a) {
     }
 
     // ====================================================== compute warps
-    const int l = threadIdx.x & 31, w = warp;
-    int v0 = FWD ? SL * l + SW * w : SL * (TJ - 1 - l) + SW * (TK - 1 - w);   // steps at which the own cell is interior
-    int v1 = v0 + NI - 1;
-    if (!pencil_in(l, w)) { v0 = 1; v1 = 0; }
-    v0 = max(v0, tlo);
-    v1 = min(v1, thi);
+    // Slot w of lane l is pencil (l, w) of the tile; in the forward sweep it
+    // meets cell i = 1 + t - l - w at step t.  The three lower neighbours of
+    // a cell (i-1 in the same slot, j-1 in lane l-1, k-1 in slot w-1) were
+    // all formed at step t - 1, so the slots of a step are independent: the
+    // x term stays in the slot's register, the y term comes from lane l-1 by
+    // shuffle, the z term from slot w-1.  Compute warp g holds the SPW slots
+    // g*SPW.. of every lane and the warps run in lockstep, one barrier per
+    // step: the z term that crosses from warp g-1 to warp g is written to
+    // shared memory before the barrier and read after it (the backward sweep
+    // is the mirror image, its terms handed from warp g+1 to warp g).  Full
+    // chunks run without a test per step; only a tile's last chunk checks
+    // for its end.
+    const int l = threadIdx.x & 31, g = warp;
+    const int w0 = g * SPW;   // first slot of this warp
+    const bool takes = FWD ? g > 0 : g < NWC - 1;    // receives the z term from a neighbouring warp
+    const bool hands = FWD ? g < NWC - 1 : g > 0;    // hands its edge slot's term on
+    const bool slotEdgeIn = FWD ? g == 0 : g == NWC - 1;   // reads the upstream tile's k-edge terms
+    constexpr int NB = NWC > 1 ? NWC - 1 : 1;
+    const int bIn = min(max(FWD ? g - 1 : g, 0), NB - 1), bOut = min(max(FWD ? g : g - 1, 0), NB - 1);
     const bool pubJ = FWD ? (l == TJ - 1 && tj < a.ntj - 1) : (l == 0 && tj > 0);
-    const bool pubK = FWD ? (w == TK - 1 && tk < a.ntk - 1) : (w == 0 && tk > 0);
-    unsigned long long *pubJw = a.xchg + tile * wordsPerTile + w;                     // [t][TK]
+    // the tile's k-edge slot (TK-1 forward, 0 backward) publishes for its lane
+    const bool pubK = (FWD ? tk < a.ntk - 1 && g == NWC - 1 : tk > 0 && g == 0);
+    unsigned long long *pubJw = a.xchg + tile * wordsPerTile + w0;                    // [t][TK]
     unsigned long long *pubKw = a.xchg + tile * wordsPerTile + (size_t)T * TK + l;    // [t][TJ]
+    // forward: per slot the L_x y (own next cell), L_y y (lane l+1) and
+    // L_z y (slot w+1) terms of its last cell, in the tile's orientation;
+    // backward: per slot the z of its last cell, which all three take
+    float tx[SPW], tl[SPW], tw[SPW];
 #pragma unroll
-    for (int q = 0; q < 2 * SW; q++) sm.p[q][w][l] = 0.0f;
-    // forward: L_x y of this pencil's last cell (for its next cell) and the
-    // L_y y terms of its last SL cells (for lane l+1), by step mod SL;
-    // backward: z of its last cell and of its last SL cells
-    float px = 0.0f, zPrev = 0.0f;
-    float hist[SL];
-#pragma unroll
-    for (int q = 0; q < SL; q++) hist[q] = 0.0f;
-    // Chunk n with its operands in Lr[s], Rr[s] (step tb + s).
-    auto run_chunk = [&](int n, const float4 (&Lr)[CH], const float (&Rr)[CH]) -> bool {
-        const int b = n % NBUF, tb = tlo + n * CH;
-        const Slot &sl = sm.slot[b];
-        // the results of chunk n: row of step tb + s at out0 + s * step
-        float *out0 = a.out + tileBase + (size_t)(FWD ? tb : T - 1 - tb) * NP + threadIdx.x;
-        const long long ostep = FWD ? NP : -NP;
-#pragma unroll
-        for (int s = 0; s < CH; s++) {
-            // (tb - tlo) is a multiple of CH, so step t's ring positions are s's
-            const int t = tb + s;
-            const int cur = s % (2 * SW), prev = (s + SW) % (2 * SW);   // steps t and t - SW
-            const float4 Lc = Lr[s];
-            const float rr = Rr[s];
-            const bool valid = t >= v0 && t <= v1;
-            float res;
-            if (FWD) {
-                // terms from the lane and warp neighbours: L of the neighbour
-                // towards this cell times its y (y-axis coupling L.z, z-axis L.w)
-                float pL = __shfl_up_sync(0xffffffffu, hist[s % SL], 1);
-                if (l == 0) pL = sl.eJ[s][w];
-                const float pW = w > 0 ? sm.p[prev][w - 1][l] : sl.eK[s][l];
-                float acc = __fsub_rn(rr, SWAP ? pL : pW);   // -z
-                acc = __fsub_rn(acc, SWAP ? pW : pL);        // -y
-                acc = __fsub_rn(acc, px);                    // -x
-                res = __fmul_rn(acc, Lc.x);
-                px = __fmul_rn(Lc.y, res);
-                const float pz = __fmul_rn(SWAP ? Lc.w : Lc.z, res);   // for the next lane
-                const float pw = __fmul_rn(SWAP ? Lc.z : Lc.w, res);   // for the next warp
-                hist[s % SL] = pz;
-                sm.p[cur][w][l] = pw;
-                if (valid && pubJ) st_word(pubJw + (size_t)t * TK, pack(ep, pz));
-                if (valid && pubK) st_word(pubKw + (size_t)t * TJ, pack(ep, pw));
-            } else {
-                float zL = __shfl_down_sync(0xffffffffu, hist[s % SL], 1);
-                if (l == TJ - 1) zL = sl.eJ[s][w];
-                const float zW = w < TK - 1 ? sm.p[prev][w + 1][l] : sl.eK[s][l];
-                float acc = __fsub_rn(rr, __fmul_rn(Lc.y, zPrev));          // +x
-                acc = __fsub_rn(acc, __fmul_rn(Lc.z, SWAP ? zW : zL));      // +y
-                acc = __fsub_rn(acc, __fmul_rn(Lc.w, SWAP ? zL : zW));      // +z
-                res = __fmul_rn(acc, Lc.x);
-                zPrev = res;
-                hist[s % SL] = res;
-                sm.p[cur][w][l] = res;
-                if (valid && pubJ) st_word(pubJw + (size_t)t * TK, pack(ep, res));
-                if (valid && pubK) st_word(pubKw + (size_t)t * TJ, pack(ep, res));
-            }
-            __stcg(out0 + s * ostep, res);
-            if (t == thi) break;
-            // the warp terms of a block of SW steps are read in the next block;
-            // the chunk's last block meets the next chunk's opening barrier
-            if (s % SW == SW - 1 && s != CH - 1) compute_sync();
-        }
-        mb_arrive(&sm.done[b]);   // the slot may be refilled
-        return true;
-    };
-    auto wait_chunk = [&](int n) -> bool {   // the chunk's slot is filled
+    for (int j = 0; j < SPW; j++) tx[j] = tl[j] = tw[j] = 0.0f;
+    float upNext = 0.0f;   // the neighbouring warp's term for the next step (none before the first)
+    for (int n = 0; n < nChunks; n++) {
         const int b = n % NBUF;
         const unsigned par = (n / NBUF) & 1;
         const bool fine = mb_wait(&sm.loaded[b], par, &sm.abort, a.err, a.spinLimit) &&
                           mb_wait(&sm.edges[b], par, &sm.abort, a.err, a.spinLimit);
-        if (compute_sync_or(!fine)) {
+        if (compute_sync_or(!fine)) {   // every compute warp stops, or none
             *(volatile int *)&sm.abort = 1;
-            return false;
+            return;
         }
-        return true;
-    };
-    for (int n = 0; n < nChunks; n++) {
-        if (!wait_chunk(n)) return;
-        const Slot &sl = sm.slot[n % NBUF];
-        float4 Lr[CH];
-        float Rr[CH];
-#pragma unroll
-        for (int s = 0; s < CH; s++) {
+        const Slot &sl = sm.slot[b];
+        const int tb = tlo + n * CH, rows = min(CH, thi + 1 - tb);
+        // the results of chunk n: row of step tb + s at out0 + s * ostep
+        float *out0 = a.out + tileBase + (size_t)(FWD ? tb : T - 1 - tb) * NP + w0 * TJ + l;
+        const long long ostep = FWD ? NP : -NP;
+        // operands of the next step, loaded while the current one computes
+        float4 Ln[SPW];
+        float rn[SPW], ejn[SPW], ekn = 0.0f;
+        auto load_step = [&](int s) {
             const int q = FWD ? s : CH - 1 - s;
-            Lr[s] = sl.L[q][threadIdx.x];
-            Rr[s] = sl.r[q][threadIdx.x];
+#pragma unroll
+            for (int j = 0; j < SPW; j++) {
+                Ln[j] = sl.L[q][(w0 + j) * TJ + l];
+                rn[j] = sl.r[q][(w0 + j) * TJ + l];
+                ejn[j] = sl.eJ[s][w0 + j];
+            }
+            if (slotEdgeIn) ekn = sl.eK[s][l];
+        };
+        auto step = [&](int s, bool more) {
+            const int t = tb + s;
+            float4 Lc[SPW];
+            float rr[SPW], ej[SPW];
+#pragma unroll
+            for (int j = 0; j < SPW; j++) { Lc[j] = Ln[j]; rr[j] = rn[j]; ej[j] = ejn[j]; }
+            const float up = slotEdgeIn ? ekn : upNext;   // the z term of the warp's edge slot
+            if (more) load_step(s + 1);
+            float nb[SPW];   // the lane neighbour's term of each slot
+#pragma unroll
+            for (int j = 0; j < SPW; j++) {
+                nb[j] = FWD ? __shfl_up_sync(0xffffffffu, tl[j], 1) : __shfl_down_sync(0xffffffffu, tx[j], 1);
+                if (l == (FWD ? 0 : TJ - 1)) nb[j] = ej[j];
+            }
+            float nx[SPW], nl[SPW], nw[SPW], res[SPW];
+#pragma unroll
+            for (int j = 0; j < SPW; j++) {
+                if (FWD) {
+                    // terms from the lane and slot neighbours: L of the
+                    // neighbour towards this cell times its y
+                    const float pL = nb[j];
+                    const float pW = j > 0 ? tw[j - 1] : up;
+                    float acc = __fsub_rn(rr[j], SWAP ? pL : pW);   // -z
+                    acc = __fsub_rn(acc, SWAP ? pW : pL);           // -y
+                    acc = __fsub_rn(acc, tx[j]);                    // -x
+                    res[j] = __fmul_rn(acc, Lc[j].x);
+                    nx[j] = __fmul_rn(Lc[j].y, res[j]);
+                    nl[j] = __fmul_rn(SWAP ? Lc[j].w : Lc[j].z, res[j]);   // for the next lane
+                    nw[j] = __fmul_rn(SWAP ? Lc[j].z : Lc[j].w, res[j]);   // for the next slot
+                } else {
+                    const float zL = nb[j];
+                    const float zW = j < SPW - 1 ? tx[j + 1] : up;
+                    float acc = __fsub_rn(rr[j], __fmul_rn(Lc[j].y, tx[j]));          // +x
+                    acc = __fsub_rn(acc, __fmul_rn(Lc[j].z, SWAP ? zW : zL));      // +y
+                    acc = __fsub_rn(acc, __fmul_rn(Lc[j].w, SWAP ? zL : zW));      // +z
+                    res[j] = __fmul_rn(acc, Lc[j].x);
+                    nx[j] = nl[j] = nw[j] = res[j];
+                }
+            }
+            // the edge slot's term for the neighbouring warp, by step parity:
+            // it reads it after this step's barrier, before the next one
+            if (hands) sm.hand[t & 1][bOut][l] = nw[FWD ? SPW - 1 : 0];
+#pragma unroll
+            for (int j = 0; j < SPW; j++) __stcg(out0 + s * ostep + j * TJ, res[j]);
+            // Edge terms of cells outside the grid are published too: a
+            // neighbour only polls the words of cells it needs.
+            st_terms(pubJ, pubJw + (size_t)t * TK, nl, ep);
+            st_term(pubK, pubKw + (size_t)t * TJ, pack(ep, nw[FWD ? SPW - 1 : 0]));
+#pragma unroll
+            for (int j = 0; j < SPW; j++) { tx[j] = nx[j]; tl[j] = nl[j]; tw[j] = nw[j]; }
+            if (NWC > 1) {
+                compute_sync();
+                if (takes) upNext = sm.hand[t & 1][bIn][l];
+            }
+        };
+        load_step(0);
+        if (rows == CH) {
+#pragma unroll
+            for (int s = 0; s < CH; s++) step(s, s + 1 < CH);
+        } else {
+#pragma unroll 1
+            for (int s = 0; s < rows; s++) step(s, s + 1 < rows);
         }
-        if (!run_chunk(n, Lr, Rr)) return;
+        mb_arrive(&sm.done[b]);   // the slot may be refilled
     }
 }
 
