@@ -238,6 +238,7 @@ def run_gpu(args, rank, world):
     d2h = 0
     e2e_parts, e2e_frames = [], []
     torch.cuda.synchronize()
+    syncs0 = e2e_sim.host_sync_count()
     t0 = time.perf_counter()
     for k in range(args.steps):
         e2e_parts.append(e2e_sim.getNumMarkerParticles())
@@ -248,6 +249,7 @@ def run_gpu(args, rank, world):
         e2e_frames.append((st.substeps, st.pressure_iterations, st.pressure_cells))
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t0
+    host_syncs = e2e_sim.host_sync_count() - syncs0
     e2e_sim.close()
     e2e_particles = sum(e2e_parts)
     same_window = e2e_parts == parts and e2e_frames == frames
@@ -318,6 +320,10 @@ def run_gpu(args, rank, world):
         "served": served,
         "gpu_launches": int(launches),
         "launches_per_frame": round(launches / args.steps, 1),
+        # the library's waits on the device per frame in the e2e pass (the
+        # API path, the positions' readback included), and per substep
+        "host_syncs_per_frame": round(host_syncs / args.steps, 1),
+        "host_syncs_per_substep": round(host_syncs / max(1, sum(f[0] for f in e2e_frames)), 1),
         "clocks": clocks.summary(),
     }
     return line

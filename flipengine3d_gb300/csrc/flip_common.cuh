@@ -118,5 +118,9 @@ struct InflowConstraint {
 // launcher adds the number of kernels it enqueues.
 long long &launch_counter();
 #define FLIP_COUNT(n) (::flip::launch_counter() += (n))
+// Host waits on the device (stream or event synchronisations) issued by the
+// calling thread, tallied per context like the launches.
+long long &host_sync_counter();
+#define FLIP_SYNC_COUNT() (++::flip::host_sync_counter())
 
 }  // namespace flip

@@ -21,6 +21,10 @@ long long &launch_counter() {
     static thread_local long long n = 0;
     return n;
 }
+long long &host_sync_counter() {
+    static thread_local long long n = 0;
+    return n;
+}
 }  // namespace flip
 
 using namespace flip;
@@ -162,6 +166,7 @@ struct flip_ctx {
     std::vector<size_t> allocationBytes;
 
     long long launches = 0;      // kernel launches of this context's calls
+    long long hostSyncs = 0;     // host waits on the device in this context's calls
     long long deviceBytes = 0;   // device memory allocated for this context
 
     // stage timing
@@ -203,19 +208,25 @@ struct flip_ctx {
     }
 };
 
-// adds the launches made during one call to the context's count
+// adds the launches and host synchronisations made during one call to the
+// context's counts
 struct LaunchTally {
     flip_ctx *x;
-    long long start;
-    explicit LaunchTally(flip_ctx *c) : x(c), start(flip::launch_counter()) {}
+    long long start, syncStart;
+    explicit LaunchTally(flip_ctx *c)
+        : x(c), start(flip::launch_counter()), syncStart(flip::host_sync_counter()) {}
     ~LaunchTally() {
-        if (x) x->launches += flip::launch_counter() - start;
+        if (x) {
+            x->launches += flip::launch_counter() - start;
+            x->hostSyncs += flip::host_sync_counter() - syncStart;
+        }
     }
 };
 
 namespace {
 
 int sync(flip_ctx *x) {
+    FLIP_SYNC_COUNT();
     cudaError_t e = cudaStreamSynchronize(x->stream);
     if (e != cudaSuccess) return fail(FLIP_E_CUDA, std::string("stream: ") + cudaGetErrorString(e));
     e = cudaGetLastError();
@@ -418,6 +429,7 @@ int inflow_constraint(flip_ctx *x, InflowConstraint *ic) {
                 q++;
             }
         CK(cudaMemcpyAsync(x->inflowCellBits, bits.data(), bits.size(), cudaMemcpyHostToDevice, x->stream));
+        FLIP_SYNC_COUNT();
         CK(cudaStreamSynchronize(x->stream));
         x->cellBitsIds = ids;
     }
@@ -598,6 +610,7 @@ int rebin_marked(flip_ctx *x) {
 
 int collect_stage_times(flip_ctx *x) {
     if (!x->timing) return FLIP_OK;
+    FLIP_SYNC_COUNT();
     CK(cudaEventSynchronize(x->ev[FLIP_NUM_STAGES]));
     for (int q = 0; q < FLIP_NUM_STAGES; q++) {
         float ms = 0.f;
@@ -755,6 +768,7 @@ int step_fluid(flip_ctx *x, double dt, flip_stage_dump *d) {
         float eps = (float)(0.005 * x->dx);
         for (auto &f : fill) if (std::abs(f) < eps) f = f > 0 ? eps : -eps;
         CK(cudaMemcpyAsync(x->phi, fill.data(), fill.size() * 4, cudaMemcpyHostToDevice, s));
+        FLIP_SYNC_COUNT();
         CK(cudaStreamSynchronize(s));
     }
     if (d && d->phi) {
@@ -1050,6 +1064,7 @@ int flip_create(int isize, int jsize, int ksize, double dx, flip_ctx **out) {
 
 int flip_destroy(flip_ctx *x) {
     if (!x) return FLIP_E_NULL;
+    FLIP_SYNC_COUNT();
     cudaStreamSynchronize(x->stream);
     for (int q = 0; q < 2; q++)   // the graphs refer to the timing events: first
         for (int o = 0; o < 2; o++)
@@ -1069,6 +1084,7 @@ int flip_destroy(flip_ctx *x) {
 
 int flip_set_stream(flip_ctx *x, void *stream) {
     if (!x) return FLIP_E_NULL;
+    FLIP_SYNC_COUNT();
     cudaStreamSynchronize(x->stream);
     if (stream) {
         if (x->ownStream) cudaStreamDestroy(x->stream);
@@ -1410,6 +1426,7 @@ int flip_compute_domain_solid(int isize, int jsize, int ksize, double dx, int cf
 
 int flip_set_stage_timing(flip_ctx *x, int enable) {
     if (!x) return FLIP_E_NULL;
+    FLIP_SYNC_COUNT();
     CK(cudaStreamSynchronize(x->stream));
     if (enable && !x->ev[0]) {
         for (int q = 0; q <= FLIP_NUM_STAGES; q++) CK(cudaEventCreate(&x->ev[q]));
@@ -1487,6 +1504,12 @@ int flip_get_launch_count(flip_ctx *x, long long *count) {
     return FLIP_OK;
 }
 
+int flip_get_host_sync_count(flip_ctx *x, long long *count) {
+    if (!x || !count) return FLIP_E_NULL;
+    *count = x->hostSyncs;
+    return FLIP_OK;
+}
+
 static flip_fluid_source_params default_source_params() {
     flip_fluid_source_params p{};
     p.inflow = 1;
@@ -1558,6 +1581,7 @@ int flip_remove_mesh_fluid_source(flip_ctx *x, int id) {
     if (!x) return FLIP_E_NULL;
     for (size_t q = 0; q < x->sources.size(); q++)
         if (x->sources[q].id == id) {
+            FLIP_SYNC_COUNT();
             cudaStreamSynchronize(x->stream);
             x->release(x->sources[q].dphi);
             x->release(x->sources[q].dcells);
@@ -1616,6 +1640,7 @@ int flip_set_tuning(flip_ctx *x, const flip_tuning *t) {
         return fail(FLIP_E_DOMAIN, "pcg_cells_per_cta must be in [256, 2^20]");
     if (t->sweep_orientation < -1 || t->sweep_orientation > 1)
         return fail(FLIP_E_DOMAIN, "sweep_orientation must be -1, 0 or 1");
+    FLIP_SYNC_COUNT();
     cudaStreamSynchronize(x->stream);
     x->sdfThreads = t->sdf_threads;
     x->sweepOrientation = t->sweep_orientation;

@@ -741,6 +741,7 @@ int mesh_surface(const MeshJob &job, MeshBuffers &mb, cudaStream_t s) {
     { FLIP_COUNT(1); k_mesh_occupancy<<<div_up(job.n, MESH_TPB), MESH_TPB, 0, s>>>(job.p, job.n, m, mb.occ); }
     std::vector<uint8_t> occ(nb), act(nb, 0);
     MCK(cudaMemcpyAsync(occ.data(), mb.occ, nb, cudaMemcpyDeviceToHost, s));
+    FLIP_SYNC_COUNT();
     MCK(cudaStreamSynchronize(s));
     auto bidx = [&](int a, int b, int e) { return a + (long long)m.nbI * (b + (long long)m.nbJ * e); };
     for (int e = 0; e < m.nbK; e++)
@@ -841,6 +842,7 @@ int mesh_surface(const MeshJob &job, MeshBuffers &mb, cudaStream_t s) {
     { FLIP_COUNT(1); k_mesh_scan_tiles<<<1, MESH_TPB, 0, s>>>(mb.tiles, (int)ntiles, mb.totals); }
     int totals[2];
     MCK(cudaMemcpyAsync(totals, mb.totals, sizeof(totals), cudaMemcpyDeviceToHost, s));
+    FLIP_SYNC_COUNT();
     MCK(cudaStreamSynchronize(s));
     const int nverts = totals[0], ntris = totals[1];
     if (nverts <= 0 || ntris <= 0) return FLIP_OK;

@@ -850,6 +850,7 @@ int pressure_project(const StepConsts &c, const PressureArgs &a, PressureBuffers
     res->applied = false;
     res->cells = 0;
     auto sync = [&]() -> cudaError_t {
+        FLIP_SYNC_COUNT();
         cudaError_t e = cudaStreamSynchronize(s);
         return e != cudaSuccess ? e : cudaGetLastError();
     };

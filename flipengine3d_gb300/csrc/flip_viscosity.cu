@@ -539,7 +539,7 @@ int viscosity_apply(const StepConsts &c, const ViscosityBuffers &vb, const float
     { FLIP_COUNT(1); k_cg_sum<<<1, 1024, 0, s>>>(a, 0); }
     double hs[8];
     cudaError_t e = cudaMemcpyAsync(hs, vb.scal, sizeof(hs), cudaMemcpyDeviceToHost, s);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e == cudaSuccess) { FLIP_SYNC_COUNT(); e = cudaStreamSynchronize(s); }
     if (e != cudaSuccess) return record_error(FLIP_E_CUDA, std::string("viscosity: ") + cudaGetErrorString(e));
     res->rows = (long long)hs[5];
     res->iterations = 0;
@@ -559,7 +559,7 @@ int viscosity_apply(const StepConsts &c, const ViscosityBuffers &vb, const float
         }
         it += batch;
         e = cudaMemcpyAsync(hs, vb.scal, sizeof(hs), cudaMemcpyDeviceToHost, s);
-        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        if (e == cudaSuccess) { FLIP_SYNC_COUNT(); e = cudaStreamSynchronize(s); }
         if (e != cudaSuccess) return record_error(FLIP_E_CUDA, std::string("viscosity: ") + cudaGetErrorString(e));
         rmax = hs[3];
     }

@@ -115,6 +115,7 @@ SIGNATURES = {
     "flip_set_stage_timing": [_P, _I],
     "flip_get_stage_times": [_P, _P, C.POINTER(C.c_longlong)],
     "flip_get_launch_count": [_P, C.POINTER(C.c_longlong)],
+    "flip_get_host_sync_count": [_P, C.POINTER(C.c_longlong)],
     "flip_get_sweep_times": [_P, C.POINTER(C.c_double), C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)],
     "flip_set_sweep_orientation": [_P, _I],
     "flip_get_sweep_orientation": [_P, C.POINTER(C.c_int)],
@@ -767,6 +768,12 @@ class FluidSimulation:
     def launch_count(self) -> int:
         v = C.c_longlong()
         self._c(self._lib.flip_get_launch_count(self._h, C.byref(v)))
+        return v.value
+
+    def host_sync_count(self) -> int:
+        """Times this simulation's calls waited on the device so far."""
+        v = C.c_longlong()
+        self._c(self._lib.flip_get_host_sync_count(self._h, C.byref(v)))
         return v.value
 
     def update_staged(self, dt: float) -> dict:

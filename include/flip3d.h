@@ -289,6 +289,10 @@ int flip_mic0_precondition(int isize, int jsize, int ksize, const uint8_t *fluid
 /* Number of this library's kernel launches issued so far on the context. */
 int flip_get_launch_count(flip_ctx *ctx, long long *count);
 
+/* Number of times this library's calls on the context waited on the device
+ * (stream or event synchronisations) so far. */
+int flip_get_host_sync_count(flip_ctx *ctx, long long *count);
+
 /* setViscosity / getViscosity (fluidsimulation.cpp:1650-1670): a constant
  * viscosity >= 0 (FLIP_E_DOMAIN otherwise) turns the viscosity step on;
  * each substep then constrains the field and solves Batty's variational
