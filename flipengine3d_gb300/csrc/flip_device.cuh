@@ -181,6 +181,7 @@ struct PressureBuffers {
     float4 *A2;            // per cell {hi, lo}: the rows as exact float pairs (hi + lo = the FP64 value to 48 bits)
     float2 *x, *r, *q;     // solution, residual, A s: exact float pairs {hi, lo} (hi + lo to ~48 bits)
     float *z;              // preconditioned residual, sweep layout
+    float *zc;             // the same at the rows in cell order (written by the z.r pass for the SpMV)
     float *s, *s2;         // search direction, double-buffered: an iteration reads one and writes the other
     float *rf;             // r rounded to FP32, the forward sweep's right-hand side, sweep layout
     SweepLayout sl;        // the orientation of the current solve

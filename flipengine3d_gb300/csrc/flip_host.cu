@@ -274,6 +274,7 @@ int alloc_grids(flip_ctx *x) {
     if ((rc = x->alloc(&p.fluid, nc)) || (rc = x->alloc(&p.Ad, nc)) || (rc = x->alloc(&p.L, nsl)) ||
         (rc = x->alloc(&p.b, nc)) || (rc = x->alloc(&p.invdiagD, nc)) || (rc = x->alloc(&p.x, nc)) ||
         (rc = x->alloc(&p.r, nc)) || (rc = x->alloc(&p.q, nc)) || (rc = x->alloc(&p.z, nsl)) ||
+        (rc = x->alloc(&p.zc, nc)) ||
         (rc = x->alloc(&p.A2, 2 * nc)) ||
         (rc = x->alloc(&p.s, nc)) || (rc = x->alloc(&p.s2, nc)) || (rc = x->alloc(&p.rf, nsl)) ||
         (rc = x->alloc(&p.pressure, nc)))
@@ -286,6 +287,7 @@ int alloc_grids(flip_ctx *x) {
     CK(cudaMemsetAsync(p.L, 0, nsl * sizeof(float4), x->stream));
     CK(cudaMemsetAsync(p.rf, 0, nsl * sizeof(float), x->stream));
     CK(cudaMemsetAsync(p.z, 0, nsl * sizeof(float), x->stream));
+    CK(cudaMemsetAsync(p.zc, 0, nc * sizeof(float), x->stream));
     p.nPartials = pressure_partials_for(x->I, x->J, x->K, x->pcgCellsPerCta);
     if ((rc = x->alloc(&p.partials, PCG_MAX_PARTIALS + 32)) || (rc = x->alloc(&p.scal, 8)) ||
         (rc = x->alloc(&p.rmaxBits, 2)) || (rc = x->alloc(&p.levelRange, 8)) || (rc = x->alloc(&p.ctl, 1)) ||

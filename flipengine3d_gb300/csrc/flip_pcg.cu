@@ -532,11 +532,12 @@ __device__ __forceinline__ void df_mul_add(float ah, float al, float sv, float &
 // double-float per thread and in FP64 across threads.  The new s of a row's
 // stencil is formed from the previous iteration's buffer sIn (so no row
 // reads a value another thread is writing) and the row's own goes to sOut.
-// In the first iteration beta = 0 and sIn = 0, so s = z.  A neighbour that
+// z is read in cell order (zc, written by the z.r pass before it).  In the
+// first iteration beta = 0 and sIn = 0, so s = z.  A neighbour that
 // is not a row couples with 0 and takes s = 0.  The last CTA sums s.q and
 // sets alpha = rho / s.q, rounded to float as BLAS::addScaled takes it
 // (blaswrapper.h:129-158), and clears the iteration's residual norms.
-__global__ void k_spmv_s(StepConsts c, SweepLayout g, const int *__restrict__ rows, const int *__restrict__ rowsSk,
+__global__ void k_spmv_s(StepConsts c, const int *__restrict__ rows,
                          const int *nRows, const float4 *__restrict__ A2, const float *__restrict__ z,
                          const float *__restrict__ sIn, float *__restrict__ sOut, float2 *__restrict__ q,
                          double *partials, double *scal, unsigned long long *rmaxBits, PcgCtl *ctl) {
@@ -548,24 +549,21 @@ __global__ void k_spmv_s(StepConsts c, SweepLayout g, const int *__restrict__ ro
     float2 dot = make_float2(0.0f, 0.0f);
     for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
         const long long t = rows[e];
-        const int sk = rowsSk[e];
-        int i, j, k;
-        unflatten(t, c.I, c.J, i, j, k);
         const float4 hi = A2[2 * t], lo = A2[2 * t + 1];
         const float4 hxm = A2[2 * (t - 1)], lxm = A2[2 * (t - 1) + 1];
         const float4 hym = A2[2 * (t - sy)], lym = A2[2 * (t - sy) + 1];
         const float4 hzm = A2[2 * (t - sz)], lzm = A2[2 * (t - sz) + 1];
         // the search direction over the stencil's rows
-        auto snew = [&](bool row, long long tn, long long skn) {
-            return row ? __fmaf_rn(beta, sIn[tn], z[skn]) : 0.0f;
+        auto snew = [&](bool row, long long tn) {
+            return row ? __fmaf_rn(beta, sIn[tn], z[tn]) : 0.0f;
         };
-        const float st = snew(true, t, sk);
-        const float sxp = snew(hi.y != 0.0f || lo.y != 0.0f, t + 1, sweep_index(g, i + 1, j, k));
-        const float syp = snew(hi.z != 0.0f || lo.z != 0.0f, t + sy, sweep_index(g, i, j + 1, k));
-        const float szp = snew(hi.w != 0.0f || lo.w != 0.0f, t + sz, sweep_index(g, i, j, k + 1));
-        const float sxm = snew(hxm.y != 0.0f || lxm.y != 0.0f, t - 1, sweep_index(g, i - 1, j, k));
-        const float sym = snew(hym.z != 0.0f || lym.z != 0.0f, t - sy, sweep_index(g, i, j - 1, k));
-        const float szm = snew(hzm.w != 0.0f || lzm.w != 0.0f, t - sz, sweep_index(g, i, j, k - 1));
+        const float st = snew(true, t);
+        const float sxp = snew(hi.y != 0.0f || lo.y != 0.0f, t + 1);
+        const float syp = snew(hi.z != 0.0f || lo.z != 0.0f, t + sy);
+        const float szp = snew(hi.w != 0.0f || lo.w != 0.0f, t + sz);
+        const float sxm = snew(hxm.y != 0.0f || lxm.y != 0.0f, t - 1);
+        const float sym = snew(hym.z != 0.0f || lym.z != 0.0f, t - sy);
+        const float szm = snew(hzm.w != 0.0f || lzm.w != 0.0f, t - sz);
         sOut[t] = st;
         float accH = 0.0f, accL = 0.0f;
         df_mul_add(hi.x, lo.x, st, accH, accL);
@@ -594,16 +592,23 @@ __global__ void k_spmv_s(StepConsts c, SweepLayout g, const int *__restrict__ ro
 
 // rho_new = z.r.  The last CTA sums it; inside the loop (inLoop) it also
 // sets beta = rho_new / rho as float (pcgsolver.h:295-298) and ends the
-// iteration: rho = rho_new, next iteration index.
+// iteration: rho = rho_new, next iteration index.  Each row's z, gathered
+// from the sweep layout, is also stored in cell order, so that the SpMV's
+// stencil reads of z are coalesced.
 __global__ void k_dot_zr(const int *__restrict__ rows, const int *__restrict__ rowsSk, const int *nRows,
-                         const float *__restrict__ z, const float2 *__restrict__ r, double *partials, double *scal,
+                         const float *__restrict__ z, float *__restrict__ zc, const float2 *__restrict__ r,
+                         double *partials, double *scal,
                          PcgCtl *ctl, int inLoop) {
     __shared__ double sh[32];
     if (ctl->done) return;
     const int n = *nRows;
     float2 dot = make_float2(0.0f, 0.0f);   // double-float per thread, FP64 across threads
-    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x)
-        dot = df_add(dot, df_scale(z[rowsSk[e]], r[rows[e]]));
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
+        const int t = rows[e];
+        const float zt = z[rowsSk[e]];
+        zc[t] = zt;   // z in cell order, where the SpMV reads its stencil
+        dot = df_add(dot, df_scale(zt, r[t]));
+    }
     double s = block_sum(df_to(dot), sh);
     if (threadIdx.x == 0) partials[blockIdx.x] = s;
     if (last_cta(&ctl->ticket[1])) {
@@ -935,7 +940,7 @@ int pressure_project(const StepConsts &c, const PressureArgs &a, PressureBuffers
         if (timed) record(tm->ev[2 * q]);
         launch_sweeps(c, pb.sl, pb.L, pb.rf, pb.z, sw, &pb.ctl->done, s, true);   // prepared by the kernel before
         if (timed) record(tm->ev[2 * q + 1]);
-        { FLIP_COUNT(1); k_dot_zr<<<rb, TPB, 0, s>>>(pb.fluidIdx, pb.fluidSk, pb.nFluid, pb.z, pb.r, pb.partials, pb.scal, pb.ctl, q > 0); }
+        { FLIP_COUNT(1); k_dot_zr<<<rb, TPB, 0, s>>>(pb.fluidIdx, pb.fluidSk, pb.nFluid, pb.z, pb.zc, pb.r, pb.partials, pb.scal, pb.ctl, q > 0); }
     };
     // one PCG iteration (pcgsolver.h:263-300); every launch is the same for
     // every iteration but the search direction's two buffers, which swap
@@ -944,7 +949,7 @@ int pressure_project(const StepConsts &c, const PressureArgs &a, PressureBuffers
     int sPar = 0;
     auto iteration = [&](int k, bool timed) {
         float *sIn = sPar ? pb.s2 : pb.s, *sOut = sPar ? pb.s : pb.s2;
-        { FLIP_COUNT(1); k_spmv_s<<<rb, TPB, 0, s>>>(c, pb.sl, pb.fluidIdx, pb.fluidSk, pb.nFluid, pb.A2, pb.z, sIn, sOut, pb.q, pb.partials, pb.scal, rmax, pb.ctl); }
+        { FLIP_COUNT(1); k_spmv_s<<<rb, TPB, 0, s>>>(c, pb.fluidIdx, pb.nFluid, pb.A2, pb.zc, sIn, sOut, pb.q, pb.partials, pb.scal, rmax, pb.ctl); }
         { FLIP_COUNT(1); k_update_xr<<<rb, TPB, 0, s>>>(pb.fluidIdx, pb.fluidSk, pb.nFluid, pb.x, pb.r, pb.rf, sOut, pb.q, pb.scal, rmax, pb.ctl); }
         { FLIP_COUNT(1); k_true_residual<<<rb, TPB, 0, s>>>(c, pb.fluidIdx, pb.fluidSk, pb.nFluid, pb.Ad, pb.b, pb.x, pb.r, pb.rf, rmax + 1, pb.scal, pb.ctl, sw.ticket); }
         precondition(1 + k, timed);
