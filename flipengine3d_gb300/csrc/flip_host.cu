@@ -1490,7 +1490,7 @@ int flip_estimate_device_bytes(int isize, int jsize, int ksize, int particles, l
     b += 5 * (nc + 1) * 4 + (scan_scratch_ints((int)nc) + 4) * 4 + 16;   // binning
     b += nc * 4 + (I + 1) * (J + 1) * (K + 1) * 4 + nc;                  // phi, solid phi, solid cells
     b += faces * (4 * 3 + 1 + 1);                                        // weights, velocity, saved, valid, status
-    b += nc * (1 + 32 + 32 + 8 * 5 + 4 * 2 + 4) + nsl * (16 + 4 + 4);     // pressure system
+    b += nc * (1 + 32 + 32 + 8 * 5 + 4 * 3 + 4) + nsl * (16 + 4 + 4);     // pressure system (s, s2, zc)
     b += (nc + 1) * 4 * 2 + nc * 4 * 2 + (scan_scratch_ints((int)nc) + 8) * 4;   // row list
     b += (PCG_MAX_PARTIALS + 32) * 8 + 64 + 16 + 32;
     b += (mic0_factor_tiles(jsize, ksize) + 1) * 4 + 64;                  // factor tiles, ticket, control
