@@ -111,6 +111,23 @@ def test_launches_are_counted(gpu):
         assert sim.launch_count() > before + 20
 
 
+def test_host_synchronisations_are_counted(gpu):
+    """A substep waits on the device after the binning, the system build,
+    the first sweep pair and each batch of PCG iterations; a readback waits
+    once more."""
+    sc = dam_break(12, seed=0)
+    with FluidSimulation.from_scene(sc) as sim:
+        sim.update(sc.frame_dt)
+        before = sim.host_sync_count()
+        sim.update(sc.frame_dt)
+        substeps = sim.getFrameStatsData().substeps
+        per_update = sim.host_sync_count() - before
+        assert per_update >= 4 * substeps
+        before = sim.host_sync_count()
+        sim.getMarkerParticlePositionData()
+        assert sim.host_sync_count() == before + 1
+
+
 def test_readback_into_a_caller_buffer(gpu):
     """getMarkerParticlePositionData(char *) writes into the caller's buffer;
     the Python mirror takes one as `out` and rejects one that is too small."""
