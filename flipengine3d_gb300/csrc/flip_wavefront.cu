@@ -96,7 +96,7 @@ struct SweepArgs {
     const float4 *L;               // factor rows, sweep layout
     const float *rin;              // right-hand side, sweep layout (backward: the forward result)
     float *out;                    // result, sweep layout (backward: in place over the forward result)
-    int J, K, NI, T;               // J, K: grid extents along the tile's lane and warp axes
+    int J, K, NI, T;               // J, K: grid extents along the tile's lane and slot axes
     int ntj, ntk;
     const int2 *range;             // per tile: first/last step (forward numbering) holding a system cell
     unsigned long long *xchg;      // per tile: T x TK j-edge words, then T x TJ k-edge words
@@ -111,8 +111,8 @@ struct SweepArgs {
 struct Slot {
     float4 L[CH][NP];   // rows in layout order: forward row q = step q, backward row q = step CH-1-q
     float r[CH][NP];
-    float eJ[CH][TK];   // by step: term from the j neighbour tile for the edge lane of each warp
-    float eK[CH][TJ];   // by step: term from the k neighbour tile for each lane of the edge warp
+    float eJ[CH][TK];   // by step: term from the neighbour tile along the lanes, for the edge lane of each slot
+    float eK[CH][TJ];   // by step: term from the neighbour tile along the slots, for each lane of the edge slot
 };
 struct SweepSmem {
     Slot slot[NBUF];
