@@ -165,8 +165,10 @@ struct PcgCtl {
     int it;        // index of the iteration being run
     unsigned int ticket[4];   // per reduction kernel (spmv, dot_zr, update_xr, true residual): CTAs done
     double resid;  // last residual norm tested
+    int batches;     // batches run by the device-side loop
+    int maxBatches;  // its limit (maximum iterations / PCG_BATCH)
 };
-constexpr int PCG_BATCH = 8;   // iterations enqueued between host checks
+constexpr int PCG_BATCH = 8;   // iterations of a captured batch
 
 struct PressureBuffers {
     uint8_t *fluid;        // interior cell with phi < 0 (a row of the system)
@@ -195,6 +197,11 @@ struct PressureBuffers {
     cudaGraphExec_t batchGraph[2][2] = {};   // [timed][orientation]
     long long batchKernels[2][2] = {};
     bool noGraphs = false;   // the stream cannot be captured: launch eagerly
+    // untimed solves: the batches inside a device-side loop (a conditional
+    // WHILE node), one launch and one host wait per solve
+    cudaGraphExec_t loopGraph[2] = {};   // [orientation]
+    long long loopKernels[2] = {};       // kernels per pass of the loop body
+    bool noLoopGraph = false;            // the loop could not be built: batches from the host
     int *levelRange;       // [0]=min(i+j+k) [1]=max(i+j+k) [2]=system size [3..6]=min/max j, min/max k
     int *factorProgress;   // per factor tile: the last level it finished
     unsigned int *factorTicket;
@@ -224,6 +231,7 @@ struct PressureMail {      // pinned host scalars
     double bmax, rho, ptol;
     PcgCtl ctl;
     int sweepErr;
+    int maxBatches;
 };
 struct PressureResult {
     int iterations;

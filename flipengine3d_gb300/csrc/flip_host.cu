@@ -1071,6 +1071,8 @@ int flip_destroy(flip_ctx *x) {
     for (int q = 0; q < 2; q++)   // the graphs refer to the timing events: first
         for (int o = 0; o < 2; o++)
             if (x->pr.batchGraph[q][o]) cudaGraphExecDestroy(x->pr.batchGraph[q][o]);
+    for (int o = 0; o < 2; o++)
+        if (x->pr.loopGraph[o]) cudaGraphExecDestroy(x->pr.loopGraph[o]);
     for (int q = 0; q <= FLIP_NUM_STAGES; q++)
         if (x->ev[q]) cudaEventDestroy(x->ev[q]);
     for (int q = 0; q < 2 * (PCG_BATCH + 1); q++)
@@ -1655,6 +1657,11 @@ int flip_set_tuning(flip_ctx *x, const flip_tuning *t) {
                     cudaGraphExecDestroy(x->pr.batchGraph[q][o]);
                     x->pr.batchGraph[q][o] = nullptr;
                 }
+        for (int o = 0; o < 2; o++)
+            if (x->pr.loopGraph[o]) {
+                cudaGraphExecDestroy(x->pr.loopGraph[o]);
+                x->pr.loopGraph[o] = nullptr;
+            }
     }
     return FLIP_OK;
 }

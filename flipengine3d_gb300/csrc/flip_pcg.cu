@@ -844,6 +844,16 @@ void mic0_factor(const StepConsts &c, const uint8_t *fluid, const double4_32a *A
     }
 }
 
+// The condition of the device-side loop over batches of PCG iterations: one
+// more batch while the solve has not converged, no wavefront has given up
+// and fewer than maxBatches batches have run (so the loop always ends).
+__global__ void k_pcg_loop(cudaGraphConditionalHandle h, PcgCtl *ctl, const int *err) {
+    const int ran = ctl->batches + 1;
+    ctl->batches = ran;
+    const bool more = !ctl->done && !*(volatile const int *)err && ran < ctl->maxBatches;
+    cudaGraphSetConditional(h, more ? 1u : 0u);
+}
+
 int pressure_project(const StepConsts &c, const PressureArgs &a, PressureBuffers &pb, SweepState &sw,
                      PressureMail *mail, cudaStream_t s, PressureResult *res, std::string *errMsg) {
     const long long n = (long long)c.I * c.J * c.K;
@@ -977,9 +987,73 @@ int pressure_project(const StepConsts &c, const PressureArgs &a, PressureBuffers
         // Iterations go to the device PCG_BATCH at a time, as one CUDA graph
         // (captured on first use, per context): the convergence test runs
         // there and the kernels of iterations after convergence return at
-        // once.  The host reads the outcome once per batch.
+        // once.  Untimed, the full batches run inside a device-side loop (a
+        // conditional WHILE node whose body is a batch and k_pcg_loop), so
+        // the host launches the solve once and waits once; timed, or where
+        // the loop cannot be built, the host reads the outcome once per
+        // batch.  The iterations after the last full batch run eagerly.
         const int gi = tm ? 1 : 0, go = pb.sl.swap;
-        for (int it0 = 0; it0 < a.maxIter;) {
+        int it0 = 0;
+        const int maxBatches = a.maxIter / PCG_BATCH;
+        if (!tm && !pb.noGraphs && !pb.noLoopGraph && maxBatches > 0) {
+            sweep_epoch_guard(c, sw, 2LL * PCG_BATCH * maxBatches, s);
+            if (!pb.loopGraph[go]) {
+                long long &counter = launch_counter();
+                const long long before = counter;
+                const unsigned int epochBefore = sw.epoch;
+                cudaGraph_t graph = nullptr;
+                cudaGraphConditionalHandle handle{};
+                bool built = false;
+                if (cudaGraphCreate(&graph, 0) == cudaSuccess &&
+                    cudaGraphConditionalHandleCreate(&handle, graph, 1, cudaGraphCondAssignDefault) == cudaSuccess) {
+                    cudaGraphNodeParams cp{};
+                    cp.type = cudaGraphNodeTypeConditional;
+                    cp.conditional.handle = handle;
+                    cp.conditional.type = cudaGraphCondTypeWhile;
+                    cp.conditional.size = 1;
+                    cudaGraphNode_t node;
+                    if (cudaGraphAddNode(&node, graph, nullptr, nullptr, 0, &cp) == cudaSuccess &&
+                        cudaStreamBeginCaptureToGraph(s, cp.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                                      cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+                        capturing = true;
+                        for (int k = 0; k < PCG_BATCH; k++) iteration(k, false);
+                        { FLIP_COUNT(1); k_pcg_loop<<<1, 1, 0, s>>>(handle, pb.ctl, sw.err); }
+                        capturing = false;
+                        cudaGraph_t body = nullptr;
+                        built = cudaStreamEndCapture(s, &body) == cudaSuccess &&
+                                cudaGraphInstantiate(&pb.loopGraph[go], graph, 0) == cudaSuccess;
+                    }
+                }
+                if (graph) cudaGraphDestroy(graph);
+                if (!built) {
+                    cudaGetLastError();   // no device-side loop here: batches from the host
+                    pb.loopGraph[go] = nullptr;
+                    pb.noLoopGraph = true;
+                }
+                pb.loopKernels[go] = counter - before;
+                counter = before;   // counted when run
+                sw.epoch = epochBefore;
+            }
+            if (pb.loopGraph[go]) {
+                mail->maxBatches = maxBatches;
+                PCK(cudaMemcpyAsync(&pb.ctl->maxBatches, &mail->maxBatches, sizeof(int), cudaMemcpyHostToDevice, s));
+                PCK(cudaGraphLaunch(pb.loopGraph[go], s));
+                PCK(cudaMemcpyAsync(&mail->ctl, pb.ctl, sizeof(PcgCtl), cudaMemcpyDeviceToHost, s));
+                PCK(cudaMemcpyAsync(&mail->sweepErr, sw.err, sizeof(int), cudaMemcpyDeviceToHost, s));
+                PCK(sync());
+                const int ran = mail->ctl.batches;
+                launch_counter() += ran * pb.loopKernels[go];
+                sw.epoch += 2u * PCG_BATCH * (unsigned int)ran;
+                sweepErr = mail->sweepErr;
+                resid = mail->ctl.resid;
+                if (!sweepErr && mail->ctl.done) {
+                    ok = true;
+                    iterations = mail->ctl.iters;
+                }
+                it0 = ran * PCG_BATCH;
+            }
+        }
+        while (!ok && !sweepErr && it0 < a.maxIter) {
             const int nit = std::min(PCG_BATCH, a.maxIter - it0);
             sweep_epoch_guard(c, sw, 2LL * nit, s);
             if (nit == PCG_BATCH && !pb.batchGraph[gi][go] && !pb.noGraphs) {
