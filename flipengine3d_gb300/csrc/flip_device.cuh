@@ -121,7 +121,10 @@ void launch_mark_fast(const ParticleSoA &p, int n, const float *maxSpeedSq, unsi
 #ifndef SWEEP_SW
 #define SWEEP_SW 1
 #endif
-constexpr int SWEEP_TJ = 32, SWEEP_TK = 8, SWEEP_NP = SWEEP_TJ * SWEEP_TK;
+#ifndef SWEEP_SLOTS
+#define SWEEP_SLOTS 8   // pencils of a tile along its slot axis
+#endif
+constexpr int SWEEP_TJ = 32, SWEEP_TK = SWEEP_SLOTS, SWEEP_NP = SWEEP_TJ * SWEEP_TK;
 static_assert(SWEEP_SL >= 1 && SWEEP_SL <= 4 && SWEEP_SW >= 1 && SWEEP_SW <= 4, "sweep skews");
 struct SweepLayout {
     int ntj, ntk, T;   // tiles along the lane and warp axes, steps per tile
