@@ -90,6 +90,32 @@ def test_pressure_non_convergence_is_reported_not_raised(gpu):
         assert sim.getNumMarkerParticles() > 0
 
 
+@pytest.mark.parametrize("max_iterations", [1000, 21])
+def test_device_side_pcg_loop_matches_host_batches(gpu, max_iterations):
+    """Untimed solves run the PCG batches inside a device-side loop; with
+    stage timing on, the host launches them batch by batch.  Both run the
+    same kernels in the same order: the results are bit-identical, also when
+    the iteration cap (21: two full batches and an eager tail of 5) stops the
+    solve before convergence."""
+    sc = dam_break(24, seed=3, sphere=True)
+    out = []
+    for timed in (False, True):
+        with FluidSimulation.from_scene(sc, tolerance=1e-9) as sim:
+            sim.setMaxPressureSolveIterations(max_iterations)
+            sim.set_stage_timing(timed)
+            stats = []
+            for _ in range(3):
+                sim.update(sc.frame_dt)
+                st = sim.getFrameStatsData()
+                stats.append((st.substeps, st.pressure_iterations, st.pressure_status))
+            out.append((sim.getMarkerParticlePositionData(), sim.getMarkerParticleVelocityData(), stats))
+    (p0, v0, s0), (p1, v1, s1) = out
+    assert s0 == s1
+    assert np.array_equal(p0, p1) and np.array_equal(v0, v1)
+    if max_iterations == 21:
+        assert max(it for _, it, _ in s0) == 21
+
+
 def test_nan_velocity_input_does_not_fault(gpu):
     sc = dam_break(12, seed=0)
     vel = sc.velocities.copy()
