@@ -105,11 +105,11 @@ void launch_mark_fast(const ParticleSoA &p, int n, const float *maxSpeedSq, unsi
 // Sweep layout: the vectors of the MIC(0) sweeps (factor rows, right-hand
 // side, result) are stored step-major.  The interior pencils along i are cut
 // into tiles of SWEEP_TJ x SWEEP_TK: SWEEP_TJ along the tile's lane axis a
-// and SWEEP_TK along its warp axis b, where (a, b) = (j, k), or (k, j) when
+// and SWEEP_TK along its slot axis b, where (a, b) = (j, k), or (k, j) when
 // `swap` is set (the orientation is chosen per solve).  Pencil (l, w) of a
 // tile holds cell i at forward step tf = i - 1 + SWEEP_SL * l + SWEEP_SW * w:
 // a pencil runs SWEEP_SL steps behind its lane neighbour and SWEEP_SW steps
-// behind its warp neighbour, so a term crosses lanes SWEEP_SL steps and warps
+// behind its slot neighbour, so a term crosses lanes SWEEP_SL steps and slots
 // SWEEP_SW steps after it is formed.  Entry (tile, tf, w, l) lives at
 // ((tile * T + tf) * SWEEP_NP + w * SWEEP_TJ + l),
 // T = I - 2 + SWEEP_SL * (SWEEP_TJ - 1) + SWEEP_SW * (SWEEP_TK - 1).  A chunk of
