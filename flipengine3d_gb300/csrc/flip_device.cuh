@@ -71,6 +71,16 @@ void launch_p2g(const ParticleSoA &p, const int *cellStart, const StepConsts &c,
                 uint8_t *vu, uint8_t *vv, uint8_t *vw, cudaStream_t s);
 void launch_extrapolate(const StepConsts &c, float *u, float *v, float *w, const uint8_t *vu, const uint8_t *vv,
                         const uint8_t *vw, uint8_t *status, int layers, cudaStream_t s);
+// The force-field grid on the device (flip_forces.cu): faces of an
+// ni x nj x nk grid of cell size dx, and the body force it reads outside them
+struct ForceFieldView {
+    const float *u, *v, *w;
+    int ni, nj, nk;
+    double dx;
+    float gx, gy, gz;
+};
+void launch_force_field(const StepConsts &c, float *u, float *v, float *w, const ForceFieldView &f, double dt,
+                        const uint8_t *ex, cudaStream_t s);
 void launch_save_and_force(const StepConsts &c, float *u, float *v, float *w, float *su, float *sv, float *sw,
                            float fx, float fy, float fz, bool ax, bool ay, bool az, const uint8_t *ex,
                            cudaStream_t s);

@@ -11,6 +11,7 @@
 
 #include "../../include/flip3d.h"
 #include "flip_device.cuh"
+#include "force_fields.h"
 #include "solid_setup.h"
 
 namespace flip {
@@ -131,6 +132,22 @@ struct flip_ctx {
     ViscosityBuffers vb{};
     bool vbReady = false;
     ViscosityResult viscResult{};
+    // force fields (enableForceFields, fluidsimulation.cpp:1605-1647): point
+    // fields; the grid is rebuilt on the host at the first substep of a frame
+    // after a change (ffDirty, or the body force moved) and uploaded
+    struct ForceFieldEntry {
+        int id;
+        flip::PointForceField f;
+    };
+    bool ffEnabled = false;
+    int ffReduction = 1;
+    std::vector<ForceFieldEntry> forceFields;
+    int nextForceFieldId = 0;
+    bool ffDirty = true;
+    bool ffGravitySet = false;
+    float ffGravity[3] = {0.f, 0.f, 0.f};
+    flip::ForceFieldGridHost ffHost;
+    float *ffU = nullptr, *ffV = nullptr, *ffW = nullptr;
     // tuning knobs (flip_set_tuning): liquid-SDF CTA size, grid cells per
     // CTA of the PCG row kernels; neither changes the results' meaning
     int sdfThreads = 512;
@@ -752,6 +769,42 @@ int apply_viscosity(flip_ctx *x, double dt) {
 }
 
 // _stepFluid (fluidsimulation.cpp:5471-5508)
+// _updateForceFieldGrid (fluidsimulation.cpp:3440-3448) without adaptive
+// force-field time stepping: at the first substep of a frame the grid takes
+// the body force (a change of more than 1e-6 in length, ForceFieldGrid::
+// setGravityVector, forcefieldgrid.cpp:103-110, or of a field rebuilds it);
+// the grid's dimensions are ceil(I / level) ... at a cell of level * dx
+// (_initializeForceFieldGrid, :2614-2621), fixed when it is first built.
+int update_force_field_grid(flip_ctx *x, float3 bf) {
+    if (x->stepNumber != 0 && x->ffU) return FLIP_OK;
+    const float g[3] = {bf.x, bf.y, bf.z};
+    const float dg[3] = {g[0] - x->ffGravity[0], g[1] - x->ffGravity[1], g[2] - x->ffGravity[2]};
+    if (std::sqrt(dg[0] * dg[0] + dg[1] * dg[1] + dg[2] * dg[2]) > 1e-6f) x->ffDirty = true;
+    for (int d = 0; d < 3; d++) x->ffGravity[d] = g[d];
+    if (!x->ffDirty && x->ffU) return FLIP_OK;
+    int rc;
+    if (!x->ffU) {
+        const int red = x->ffReduction;
+        const int ni = (int)std::ceil((double)x->I / (double)red), nj = (int)std::ceil((double)x->J / (double)red),
+                  nk = (int)std::ceil((double)x->K / (double)red);
+        x->ffHost.ni = ni;
+        x->ffHost.nj = nj;
+        x->ffHost.nk = nk;
+        x->ffHost.dx = x->dx * red;
+        if ((rc = x->alloc(&x->ffU, (size_t)(ni + 1) * nj * nk)) || (rc = x->alloc(&x->ffV, (size_t)ni * (nj + 1) * nk)) ||
+            (rc = x->alloc(&x->ffW, (size_t)ni * nj * (nk + 1))))
+            return rc;
+    }
+    std::vector<PointForceField> fields;
+    for (auto &e : x->forceFields) fields.push_back(e.f);
+    point_force_grid(x->ffHost.ni, x->ffHost.nj, x->ffHost.nk, x->ffHost.dx, fields, g, x->ffHost);
+    CK(cudaMemcpyAsync(x->ffU, x->ffHost.u.data(), x->ffHost.u.size() * 4, cudaMemcpyHostToDevice, x->stream));
+    CK(cudaMemcpyAsync(x->ffV, x->ffHost.v.data(), x->ffHost.v.size() * 4, cudaMemcpyHostToDevice, x->stream));
+    CK(cudaMemcpyAsync(x->ffW, x->ffHost.w.data(), x->ffHost.w.size() * 4, cudaMemcpyHostToDevice, x->stream));
+    x->ffDirty = false;
+    return FLIP_OK;
+}
+
 int step_fluid(flip_ctx *x, double dt, flip_stage_dump *d) {
     cudaStream_t s = x->stream;
     StepConsts &c = x->c;
@@ -805,9 +858,19 @@ int step_fluid(flip_ctx *x, double dt, flip_stage_dump *d) {
     InflowConstraint ic;
     if ((rc = inflow_constraint(x, &ic))) return rc;
     if (ic.count) launch_inflow_faces(c, ic, x->vu, x->vv, x->vw, x->inflowFaces, s);
-    launch_save_and_force(c, x->u, x->v, x->w, x->su, x->sv, x->sw, (float)(bf.x * dt), (float)(bf.y * dt),
-                          (float)(bf.z * dt), std::fabs(bf.x) > feps, std::fabs(bf.y) > feps, std::fabs(bf.z) > feps,
-                          ic.count ? x->inflowFaces : nullptr, s);
+    if (x->ffEnabled) {
+        // _applyBodyForcesToVelocityField with force fields (:3566-3583):
+        // save, then the force-field grid instead of the constant force
+        if ((rc = update_force_field_grid(x, bf))) return rc;
+        launch_save_and_force(c, x->u, x->v, x->w, x->su, x->sv, x->sw, 0.f, 0.f, 0.f, false, false, false, nullptr, s);
+        ForceFieldView fv{x->ffU, x->ffV, x->ffW, x->ffHost.ni, x->ffHost.nj, x->ffHost.nk, x->ffHost.dx,
+                          x->ffGravity[0], x->ffGravity[1], x->ffGravity[2]};
+        launch_force_field(c, x->u, x->v, x->w, fv, dt, ic.count ? x->inflowFaces : nullptr, s);
+    } else {
+        launch_save_and_force(c, x->u, x->v, x->w, x->su, x->sv, x->sw, (float)(bf.x * dt), (float)(bf.y * dt),
+                              (float)(bf.z * dt), std::fabs(bf.x) > feps, std::fabs(bf.y) > feps,
+                              std::fabs(bf.z) > feps, ic.count ? x->inflowFaces : nullptr, s);
+    }
     if (d && (rc = dump_mac(x, d->u_force, d->v_force, d->w_force, x->u, x->v, x->w))) return rc;
     if ((rc = apply_viscosity(x, dt))) return rc;
     // pressure (fluidsimulation.cpp:3732-3773)
@@ -1633,6 +1696,105 @@ int flip_get_viscosity_solve(flip_ctx *x, long long *rows, int *iterations, doub
     if (rows) *rows = x->viscResult.rows;
     if (iterations) *iterations = x->viscResult.iterations;
     if (residual) *residual = x->viscResult.residual;
+    return FLIP_OK;
+}
+
+static flip::PointForceField point_field_from(const flip_point_force_field_params &q, const float centroid[3]) {
+    flip::PointForceField f;
+    f.cx = centroid[0];
+    f.cy = centroid[1];
+    f.cz = centroid[2];
+    f.strength = q.strength;
+    f.falloffPower = q.falloff_power;
+    f.maxForceLimitFactor = q.max_force_limit_factor;
+    f.minDistanceEnabled = q.min_distance_enabled != 0;
+    f.minDistance = q.min_distance;
+    f.maxDistanceEnabled = q.max_distance_enabled != 0;
+    f.maxDistance = q.max_distance;
+    f.gravityScale = q.gravity_scale;
+    f.gravityScaleWidth = q.gravity_scale_width;
+    f.enabled = q.enabled != 0;
+    return f;
+}
+int flip_enable_force_fields(flip_ctx *x, int enable) {
+    if (!x) return FLIP_E_NULL;
+    x->ffEnabled = enable != 0;
+    return FLIP_OK;
+}
+int flip_is_force_fields_enabled(flip_ctx *x, int *enabled) {
+    if (!x || !enabled) return FLIP_E_NULL;
+    *enabled = x->ffEnabled ? 1 : 0;
+    return FLIP_OK;
+}
+int flip_set_force_field_reduction_level(flip_ctx *x, int level) {
+    if (!x) return FLIP_E_NULL;
+    if (level < 1) return fail(FLIP_E_DOMAIN, "Error: reduction level must be greater than or equal to 1.");
+    x->ffReduction = level;
+    return FLIP_OK;
+}
+int flip_get_force_field_reduction_level(flip_ctx *x, int *level) {
+    if (!x || !level) return FLIP_E_NULL;
+    *level = x->ffReduction;
+    return FLIP_OK;
+}
+int flip_add_point_force_field(flip_ctx *x, int nverts, const float *verts, const flip_point_force_field_params *q,
+                               int *id) {
+    if (!x || !q) return FLIP_E_NULL;
+    if (!x->ffEnabled) return fail(FLIP_E_RUNTIME, "Error: force fields are not enabled.");
+    if (nverts < 0) return fail(FLIP_E_DOMAIN, "negative vertex count");
+    if (nverts > 0 && !verts) return FLIP_E_NULL;
+    float centroid[3];
+    mesh_centroid(verts, nverts, centroid);
+    flip_ctx::ForceFieldEntry e{x->nextForceFieldId++, point_field_from(*q, centroid)};
+    x->forceFields.push_back(e);
+    x->ffDirty = true;
+    if (id) *id = e.id;
+    return FLIP_OK;
+}
+int flip_set_point_force_field_params(flip_ctx *x, int id, const flip_point_force_field_params *q) {
+    if (!x || !q) return FLIP_E_NULL;
+    for (auto &e : x->forceFields)
+        if (e.id == id) {
+            const float centroid[3] = {e.f.cx, e.f.cy, e.f.cz};
+            e.f = point_field_from(*q, centroid);
+            x->ffDirty = true;
+            return FLIP_OK;
+        }
+    return fail(FLIP_E_DOMAIN, "no force field with this id");
+}
+int flip_get_point_force_field_params(flip_ctx *x, int id, flip_point_force_field_params *q) {
+    if (!x || !q) return FLIP_E_NULL;
+    for (auto &e : x->forceFields)
+        if (e.id == id) {
+            const flip::PointForceField &f = e.f;
+            *q = flip_point_force_field_params{f.strength, f.falloffPower, f.maxForceLimitFactor,
+                                               f.minDistanceEnabled ? 1 : 0, f.minDistance,
+                                               f.maxDistanceEnabled ? 1 : 0, f.maxDistance, f.gravityScale,
+                                               f.gravityScaleWidth, f.enabled ? 1 : 0};
+            return FLIP_OK;
+        }
+    return fail(FLIP_E_DOMAIN, "no force field with this id");
+}
+int flip_point_force_grid(int ni, int nj, int nk, double dx, int nfields, const int *nverts, const float *verts,
+                          const flip_point_force_field_params *params, const float *gravity, float *u, float *v,
+                          float *w) {
+    if (!gravity || !u || !v || !w || (nfields > 0 && (!nverts || !params))) return FLIP_E_NULL;
+    if (ni < 1 || nj < 1 || nk < 1 || !(dx > 0.0) || nfields < 0) return fail(FLIP_E_DOMAIN, "bad grid or field count");
+    std::vector<flip::PointForceField> fields;
+    long long off = 0;
+    for (int q = 0; q < nfields; q++) {
+        if (nverts[q] < 0) return fail(FLIP_E_DOMAIN, "negative vertex count");
+        if (nverts[q] > 0 && !verts) return FLIP_E_NULL;
+        float centroid[3];
+        mesh_centroid(verts ? verts + 3 * off : nullptr, nverts[q], centroid);
+        off += nverts[q];
+        fields.push_back(point_field_from(params[q], centroid));
+    }
+    flip::ForceFieldGridHost g;
+    point_force_grid(ni, nj, nk, dx, fields, gravity, g);
+    std::memcpy(u, g.u.data(), g.u.size() * 4);
+    std::memcpy(v, g.v.data(), g.v.size() * 4);
+    std::memcpy(w, g.w.data(), g.w.size() * 4);
     return FLIP_OK;
 }
 

@@ -52,6 +52,31 @@ class FluidSourceParams(C.Structure):
                 ("velocity", C.c_double * 3)]
 
 
+class PointForceFieldParams(C.Structure):
+    """flip_point_force_field_params (include/flip3d.h); the defaults are
+    ForceField's (forcefield.h:107-118)."""
+    _fields_ = [("strength", C.c_float), ("falloff_power", C.c_float), ("max_force_limit_factor", C.c_float),
+                ("min_distance_enabled", C.c_int), ("min_distance", C.c_float),
+                ("max_distance_enabled", C.c_int), ("max_distance", C.c_float),
+                ("gravity_scale", C.c_float), ("gravity_scale_width", C.c_float), ("enabled", C.c_int)]
+
+    DEFAULTS = dict(strength=0.0, falloff_power=1.0, max_force_limit_factor=3.0, min_distance=None,
+                    max_distance=None, gravity_scale=1.0, gravity_scale_width=0.0, enabled=True)
+
+    @classmethod
+    def make(cls, **kw):
+        """From keyword arguments; min_distance / max_distance None keep the
+        limit off."""
+        unknown = set(kw) - set(cls.DEFAULTS)
+        if unknown:
+            raise TypeError(f"unknown force field parameters: {sorted(unknown)}")
+        a = dict(cls.DEFAULTS, **kw)
+        return cls(float(a["strength"]), float(a["falloff_power"]), float(a["max_force_limit_factor"]),
+                   int(a["min_distance"] is not None), float(a["min_distance"] or 0.0),
+                   int(a["max_distance"] is not None), float(a["max_distance"] or 0.0),
+                   float(a["gravity_scale"]), float(a["gravity_scale_width"]), int(bool(a["enabled"])))
+
+
 class Tuning(C.Structure):
     """flip_tuning (include/flip3d.h)."""
     _fields_ = [("sdf_threads", C.c_int), ("pcg_cells_per_cta", C.c_int), ("sweep_orientation", C.c_int)]
@@ -137,6 +162,14 @@ SIGNATURES = {
     "flip_remove_mesh_fluid_source": [_P, _I],
     "flip_fluid_source_setup": [_I, _I, _I, _D, _I, _P, _I, _P, _P, _P, _P, C.POINTER(C.c_int), _P],
     "flip_set_viscosity": [_P, _D],
+    "flip_enable_force_fields": [_P, _I],
+    "flip_is_force_fields_enabled": [_P, C.POINTER(C.c_int)],
+    "flip_set_force_field_reduction_level": [_P, _I],
+    "flip_get_force_field_reduction_level": [_P, C.POINTER(C.c_int)],
+    "flip_add_point_force_field": [_P, _I, _P, C.POINTER(PointForceFieldParams), C.POINTER(C.c_int)],
+    "flip_set_point_force_field_params": [_P, _I, C.POINTER(PointForceFieldParams)],
+    "flip_get_point_force_field_params": [_P, _I, C.POINTER(PointForceFieldParams)],
+    "flip_point_force_grid": [_I, _I, _I, _D, _I, _P, _P, _P, _P, _P, _P, _P],
     "flip_get_viscosity": [_P, C.POINTER(C.c_double)],
     "flip_get_viscosity_solve": [_P, C.POINTER(C.c_longlong), C.POINTER(C.c_int), C.POINTER(C.c_double)],
     "flip_set_tuning": [_P, C.POINTER(Tuning)],
@@ -241,6 +274,23 @@ def mesh_fluid_cells(isize, jsize, ksize, dx, vertices, triangles):
     _check(lib, lib.flip_mesh_fluid_cells(isize, jsize, ksize, dx, v.shape[0], _ptr(v), t.shape[0], _ptr(t),
                                           C.byref(n), _ptr(cells), _ptr(phi)))
     return cells[:n.value].copy(), phi
+
+
+def point_force_grid(ni, nj, nk, dx, fields, gravity):
+    """The force-field grid of point fields without a device: fields is a
+    list of (vertices, params dict); returns u, v, w as (k, j, i) arrays."""
+    lib = load_library()
+    verts = [np.ascontiguousarray(v, np.float32).reshape(-1, 3) for v, _ in fields]
+    nverts = np.array([len(v) for v in verts] or [0], np.int32)
+    allv = np.ascontiguousarray(np.concatenate(verts) if verts else np.zeros((1, 3), np.float32))
+    prm = (PointForceFieldParams * max(len(fields), 1))(*[PointForceFieldParams.make(**q) for _, q in fields])
+    g = np.ascontiguousarray(gravity, np.float32)
+    u = np.zeros((nk, nj, ni + 1), np.float32)
+    v = np.zeros((nk, nj + 1, ni), np.float32)
+    w = np.zeros((nk + 1, nj, ni), np.float32)
+    _check(lib, lib.flip_point_force_grid(ni, nj, nk, float(dx), len(fields), _ptr(nverts), _ptr(allv),
+                                          C.cast(prm, C.c_void_p), _ptr(g), _ptr(u), _ptr(v), _ptr(w)))
+    return u, v, w
 
 
 def fluid_source_setup(isize, jsize, ksize, dx, vertices, triangles):
@@ -571,6 +621,44 @@ class FluidSimulation:
         return s
 
     # -- viscosity (fluidsimulation.cpp:1650-1670, 3592-3640)
+    # -- force fields (enableForceFields, getForceFieldGrid()->addForceField)
+    def enableForceFields(self):
+        self._c(self._lib.flip_enable_force_fields(self._h, 1))
+
+    def disableForceFields(self):
+        self._c(self._lib.flip_enable_force_fields(self._h, 0))
+
+    def isForceFieldsEnabled(self) -> bool:
+        v = C.c_int()
+        self._c(self._lib.flip_is_force_fields_enabled(self._h, C.byref(v)))
+        return bool(v.value)
+
+    def setForceFieldReductionLevel(self, level: int):
+        self._c(self._lib.flip_set_force_field_reduction_level(self._h, int(level)))
+
+    def getForceFieldReductionLevel(self) -> int:
+        v = C.c_int()
+        self._c(self._lib.flip_get_force_field_reduction_level(self._h, C.byref(v)))
+        return v.value
+
+    def addPointForceField(self, vertices, **params) -> int:
+        """A ForceFieldPoint at the centroid of a static mesh's vertices;
+        params as PointForceFieldParams.make.  Returns the field's id."""
+        v = np.ascontiguousarray(vertices, np.float32).reshape(-1, 3)
+        prm = PointForceFieldParams.make(**params)
+        fid = C.c_int()
+        self._c(self._lib.flip_add_point_force_field(self._h, len(v), _ptr(v), C.byref(prm), C.byref(fid)))
+        return fid.value
+
+    def setPointForceField(self, field_id: int, **params):
+        prm = PointForceFieldParams.make(**params)
+        self._c(self._lib.flip_set_point_force_field_params(self._h, int(field_id), C.byref(prm)))
+
+    def getPointForceField(self, field_id: int) -> PointForceFieldParams:
+        prm = PointForceFieldParams()
+        self._c(self._lib.flip_get_point_force_field_params(self._h, int(field_id), C.byref(prm)))
+        return prm
+
     def setViscosity(self, v: float):
         self._c(self._lib.flip_set_viscosity(self._h, float(v)))
 
@@ -836,6 +924,11 @@ class FluidSimulation:
         for src in getattr(scene, "sources", []):
             sim.addMeshFluidSource(src["vertices"], src["triangles"],
                                    **{k: v for k, v in src.items() if k not in ("vertices", "triangles")})
+        if getattr(scene, "force_fields", []):
+            sim.enableForceFields()
+            sim.setForceFieldReductionLevel(getattr(scene, "force_field_reduction", 1))
+            for ff in scene.force_fields:
+                sim.addPointForceField(ff["vertices"], **ff["params"])
         if len(scene.positions):
             sim.loadMarkerParticleData(scene.positions, scene.velocities)
         sim.initialize()

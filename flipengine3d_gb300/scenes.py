@@ -41,6 +41,11 @@ class Scene:
     # fluid_outflow, inversed
     sources: list = field(default_factory=list)
     viscosity: float | None = None       # setViscosity, when set
+    # point force fields (enableForceFields + addForceField): dicts with
+    # vertices, triangles (the field sits at their centroid) and params (as
+    # PointForceFieldParams.make takes them); the grid's reduction level
+    force_fields: list = field(default_factory=list)
+    force_field_reduction: int = 1
 
     @property
     def num_particles(self) -> int:
@@ -313,3 +318,34 @@ def served_scene(q: int, seed: int = 2) -> Scene:
     scene), FLIP blend 0.95, PCG tolerance 1e-5."""
     edge, fill, ppc = served_scene_params(q, seed)
     return dam_break(edge, seed=seed * 100000 + q, fill=(fill, 0.6, 1.0), ppc=ppc, tolerance=1e-5)
+
+
+def force_fields(n: int = 24, *, which: str = "point", seed: int = 0, steps: int = 4) -> Scene:
+    """Point force fields over a dam break in an n^3 box (dx 1/n, 1/60 s
+    frames, gravity -9.81): `point`: one attracting point field with a
+    minimum and a maximum distance, and gravity scaled down around it;
+    `two`: that field, a repelling one of falloff power 1 near the floor,
+    and a disabled third, on a force-field grid of half the resolution."""
+    L = 1.0
+    dx = L / n
+    rng = np.random.default_rng(seed)
+    cells = _box_cells(n, n, n, dx, (0.0, 0.0, 0.0), (0.45, 0.55, 0.6))
+    pos = _jittered_cells(cells, dx, rng, 8)
+    attract = dict(params=dict(strength=-4.0, falloff_power=2.0, min_distance=0.1213, max_distance=0.6117,
+                               gravity_scale=0.25, gravity_scale_width=0.3319))
+    attract["vertices"], attract["triangles"] = icosphere_mesh((0.7013, 0.4121, 0.5217), 0.05, subdivisions=1)
+    fields = [attract]
+    reduction = 1
+    if which == "two":
+        repel = dict(params=dict(strength=1.5, falloff_power=1.0, max_force_limit_factor=2.0,
+                                 gravity_scale=1.5, gravity_scale_width=0.2113))
+        repel["vertices"], repel["triangles"] = box_mesh((0.2013, 0.0117, 0.7011), (0.3121, 0.0613, 0.8219))
+        off = dict(params=dict(strength=50.0, enabled=False))
+        off["vertices"], off["triangles"] = box_mesh((0.4, 0.4, 0.4), (0.5, 0.5, 0.5))
+        fields = [attract, repel, off]
+        reduction = 2
+    elif which != "point":
+        raise ValueError(which)
+    return Scene(n, n, n, dx, pos, np.zeros_like(pos), frame_dt=1.0 / 60.0, tolerance=1e-9, steps=steps,
+                 name=f"force_fields_{which}_{n}", force_fields=fields, force_field_reduction=reduction)
+

@@ -307,6 +307,53 @@ int flip_set_viscosity(flip_ctx *ctx, double viscosity);
 int flip_get_viscosity(flip_ctx *ctx, double *viscosity);
 int flip_get_viscosity_solve(flip_ctx *ctx, long long *rows, int *iterations, double *residual);
 
+/* Force fields (enableForceFields, setForceFieldReductionLevel,
+ * getForceFieldGrid()->addForceField; fluidsimulation.cpp:1605-1647,
+ * forcefieldgrid.cpp, forcefieldpoint.cpp): point fields at the centroid of a
+ * static mesh.  With force fields on, the body-force step adds the force-field
+ * grid instead of the constant body force (_applyBodyForcesToVelocityField,
+ * :3566-3583): every field's strength / r^falloff along the direction from the
+ * point (capped at max_force_limit_factor * |strength|; faces nearer than the
+ * minimum distance take it, faces beyond the maximum distance none), plus the
+ * body force scaled near each field by gravity_scale over gravity_scale_width,
+ * on a grid of ceil(I / level) x ... cells of size level * dx, interpolated at
+ * the faces (gravity outside it).  The grid is rebuilt at the first substep of
+ * a frame after a field or the body force changed (_updateForceFieldGrid,
+ * :3440-3448).  Fields are added once force fields are on (FLIP_E_RUNTIME
+ * otherwise, as getForceFieldGrid throws); the reduction level (>= 1,
+ * FLIP_E_DOMAIN otherwise) is taken when the grid is first built.  The
+ * reference's getForceFieldReductionLevel returns the current frame
+ * (fluidsimulation.cpp:1623-1625); flip_get_force_field_reduction_level
+ * returns the level. */
+typedef struct {
+    float strength;               /* ForceField defaults: 0 */
+    float falloff_power;          /* 1 */
+    float max_force_limit_factor; /* 3 */
+    int min_distance_enabled;     /* 0 */
+    float min_distance;           /* 0 */
+    int max_distance_enabled;     /* 0 */
+    float max_distance;           /* 0 */
+    float gravity_scale;          /* 1 */
+    float gravity_scale_width;    /* 0 */
+    int enabled;                  /* 1 */
+} flip_point_force_field_params;
+int flip_enable_force_fields(flip_ctx *ctx, int enable);
+int flip_is_force_fields_enabled(flip_ctx *ctx, int *enabled);
+int flip_set_force_field_reduction_level(flip_ctx *ctx, int level);
+int flip_get_force_field_reduction_level(flip_ctx *ctx, int *level);
+int flip_add_point_force_field(flip_ctx *ctx, int nverts, const float *verts,
+                               const flip_point_force_field_params *params, int *id);
+int flip_set_point_force_field_params(flip_ctx *ctx, int id, const flip_point_force_field_params *params);
+int flip_get_point_force_field_params(flip_ctx *ctx, int id, flip_point_force_field_params *params);
+/* The force-field grid without a device (ForceFieldGrid::update from a
+ * cleared grid): nfields point fields, field q's nverts[q] vertices
+ * consecutive in verts, under the body force gravity[3], on an ni x nj x nk
+ * grid of cell size dx; u, v, w receive (ni+1) nj nk, ni (nj+1) nk and
+ * ni nj (nk+1) floats, flat i fastest. */
+int flip_point_force_grid(int ni, int nj, int nk, double dx, int nfields, const int *nverts, const float *verts,
+                          const flip_point_force_field_params *params, const float *gravity, float *u, float *v,
+                          float *w);
+
 /* Tuning knobs of the device kernels, no counterpart in the reference: the
  * liquid-SDF CTA size (256, 512 or 1024 threads), the grid cells per CTA of
  * the PCG row kernels' reduction grid (256 .. 2^20), and the preconditioner

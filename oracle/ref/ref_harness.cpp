@@ -37,6 +37,8 @@
 #include "pcgsolver/sparsematrix.h"
 #include "meshobject.h"
 #include "meshfluidsource.h"
+#include "forcefieldgrid.h"
+#include "forcefieldpoint.h"
 
 namespace {
 
@@ -44,6 +46,7 @@ struct RefSim {
     FluidSimulation *sim = nullptr;
     std::vector<MeshObject *> obstacles;   // owned here, registered with the simulation
     std::vector<MeshFluidSource *> sources;   // owned here, registered with the simulation
+    std::vector<ForceField *> fields;          // owned here, registered with the force-field grid
     std::string status;
     unsigned int particleFragmentBytes = 0;   // 0: the reference's default fragments
 };
@@ -96,6 +99,7 @@ void ref_destroy(void *h) {
     delete r->sim;
     for (MeshObject *o : r->obstacles) delete o;
     for (MeshFluidSource *q : r->sources) delete q;
+    for (ForceField *f : r->fields) delete f;
     delete r;
 }
 
@@ -639,6 +643,63 @@ void ref_get_node_friction(void *h, float *out) {
                 MeshObject *m = s->_solidSDF.getClosestMeshObject(i, j, k);
                 out[i + (size_t)(I + 1) * (j + (size_t)(J + 1) * k)] = m == nullptr ? 0.0f : m->getFriction();
             }
+}
+
+// Force fields (forcefieldpoint.cpp, forcefieldgrid.cpp).  prm: strength,
+// falloff power, max force limit factor, min distance enabled, min distance,
+// max distance enabled, max distance, gravity scale, gravity scale width,
+// enabled.
+static ForceFieldPoint *point_field(int nverts, const float *verts, int ntris, const int *tris, const float *prm) {
+    ForceFieldPoint *f = new ForceFieldPoint();
+    f->updateMeshStatic(mesh_from_arrays(nverts, verts, ntris, tris));
+    f->setStrength(prm[0]);
+    f->setFalloffPower(prm[1]);
+    f->setMaxForceLimitFactor(prm[2]);
+    if (prm[3] != 0.0f) f->enableMinDistance(); else f->disableMinDistance();
+    f->setMinDistance(prm[4]);
+    if (prm[5] != 0.0f) f->enableMaxDistance(); else f->disableMaxDistance();
+    f->setMaxDistance(prm[6]);
+    f->setGravityScale(prm[7]);
+    f->setGravityScaleWidth(prm[8]);
+    if (prm[9] != 0.0f) f->enable(); else f->disable();
+    return f;
+}
+
+void ref_enable_force_fields(void *h, int reduction) {
+    RefSim *r = (RefSim *)h;
+    r->sim->enableForceFields();
+    r->sim->setForceFieldReductionLevel(reduction);
+}
+
+void ref_add_point_force_field(void *h, int nverts, const float *verts, int ntris, const int *tris, const float *prm) {
+    RefSim *r = (RefSim *)h;
+    ForceFieldPoint *f = point_field(nverts, verts, ntris, tris, prm);
+    r->fields.push_back(f);
+    r->sim->getForceFieldGrid()->addForceField(f);
+}
+
+// ForceFieldGrid::update of a fresh grid: fields q = 0..nfields-1 with
+// nverts[q] / ntris[q] consecutive vertices / triangles (indices local to the
+// field) and 10 parameters each; the grid's u, v, w faces.
+void ref_point_force_grid(int ni, int nj, int nk, double dx, int nfields, const int *nverts, const float *verts,
+                          const int *ntris, const int *tris, const float *prms, const float *gravity, float *u,
+                          float *v, float *w) {
+    ForceFieldGrid grid;
+    grid.initialize(ni, nj, nk, dx);
+    std::vector<ForceFieldPoint *> fields;
+    size_t vo = 0, to = 0;
+    for (int q = 0; q < nfields; q++) {
+        fields.push_back(point_field(nverts[q], verts + 3 * vo, ntris[q], tris + 3 * to, prms + 10 * q));
+        grid.addForceField(fields.back());
+        vo += nverts[q];
+        to += ntris[q];
+    }
+    grid.setGravityVector(vmath::vec3(gravity[0], gravity[1], gravity[2]));
+    grid.update(0.0, 0.0);
+    copyArray(grid._forceField._u, u);
+    copyArray(grid._forceField._v, v);
+    copyArray(grid._forceField._w, w);
+    for (ForceFieldPoint *f : fields) delete f;
 }
 
 }  // extern "C"

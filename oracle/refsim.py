@@ -97,6 +97,12 @@ def lib(prefix: str = "ref"):
             L.ref_mesh_fluid_cells.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, C.c_int, C.c_void_p, C.c_int,
                                                C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
             L.ref_mesh_fluid_cells.restype = None
+            L.ref_enable_force_fields.argtypes = [C.c_void_p, C.c_int]
+            L.ref_enable_force_fields.restype = None
+            L.ref_add_point_force_field.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]
+            L.ref_add_point_force_field.restype = None
+            L.ref_point_force_grid.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, C.c_int] + [C.c_void_p] * 9
+            L.ref_point_force_grid.restype = None
         L.ref_num_particles.argtypes = [C.c_void_p]
         L.ref_num_particles.restype = C.c_int
         L.ref_frame_substeps.argtypes = [C.c_void_p]
@@ -180,6 +186,37 @@ def mesh_fluid_cells(isize, jsize, ksize, dx, vertices, triangles):
     phi = np.zeros((ksize + 1, jsize + 1, isize + 1), np.float32)
     L.ref_mesh_fluid_cells(isize, jsize, ksize, dx, len(v), _p(v), len(t), _p(t), C.byref(n), _p(cells), _p(phi))
     return cells[:n.value].copy(), phi
+
+
+def force_field_params(q):
+    """The 10 floats of the harness's point-field parameters from a dict as
+    flipengine3d_gb300's PointForceFieldParams.make takes it."""
+    mn, mx = q.get("min_distance"), q.get("max_distance")
+    return np.array([q.get("strength", 0.0), q.get("falloff_power", 1.0), q.get("max_force_limit_factor", 3.0),
+                     float(mn is not None), mn or 0.0, float(mx is not None), mx or 0.0,
+                     q.get("gravity_scale", 1.0), q.get("gravity_scale_width", 0.0),
+                     float(q.get("enabled", True))], np.float32)
+
+
+def point_force_grid(ni, nj, nk, dx, fields, gravity):
+    """The reference's ForceFieldGrid (a fresh one, updated once) for point
+    fields given as (vertices, triangles, params dict): u, v, w (k, j, i)."""
+    L = lib("ref")
+    vs = [np.ascontiguousarray(v, np.float32).reshape(-1, 3) for v, _, _ in fields]
+    ts = [np.ascontiguousarray(t, np.int32).reshape(-1, 3) for _, t, _ in fields]
+    nv = np.array([len(v) for v in vs] or [0], np.int32)
+    nt = np.array([len(t) for t in ts] or [0], np.int32)
+    allv = np.ascontiguousarray(np.concatenate(vs) if vs else np.zeros((1, 3), np.float32))
+    allt = np.ascontiguousarray(np.concatenate(ts) if ts else np.zeros((1, 3), np.int32))
+    prm = np.ascontiguousarray(np.concatenate([force_field_params(q) for _, _, q in fields])
+                               if fields else np.zeros(10, np.float32))
+    g = np.ascontiguousarray(gravity, np.float32)
+    u = np.zeros((nk, nj, ni + 1), np.float32)
+    v = np.zeros((nk, nj + 1, ni), np.float32)
+    w = np.zeros((nk + 1, nj, ni), np.float32)
+    L.ref_point_force_grid(ni, nj, nk, float(dx), len(fields), _p(nv), _p(allv), _p(nt), _p(allt), _p(prm), _p(g),
+                           _p(u), _p(v), _p(w))
+    return u, v, w
 
 
 def fluid_source_setup(isize, jsize, ksize, dx, vertices, triangles):
@@ -279,7 +316,8 @@ class RefSimulation:
     def setup(self, scene, tolerance=None):
         obstacles = getattr(scene, "obstacles", [])
         fluids = getattr(scene, "fluid_meshes", [])
-        if (obstacles or fluids or getattr(scene, "sources", [])) and self.PREFIX != "ref":
+        if (obstacles or fluids or getattr(scene, "sources", []) or getattr(scene, "force_fields", [])) \
+                and self.PREFIX != "ref":
             raise NotImplementedError("the oracle port restates the domain walls and loaded particles only; "
                                       "obstacle and fluid-mesh scenes are pinned by fixtures from the reference")
         if getattr(scene, "jitter_factor", None) is not None:
@@ -301,6 +339,13 @@ class RefSimulation:
                                              *(float(a) for a in src.get("velocity", (0.0, 0.0, 0.0))),
                                              int(src.get("substep_emissions", 1)), int(src.get("constrained", True)),
                                              int(src.get("fluid_outflow", True)), int(src.get("inversed", False)))
+        if getattr(scene, "force_fields", []):
+            self.L.ref_enable_force_fields(self.h, int(getattr(scene, "force_field_reduction", 1)))
+            for ff in scene.force_fields:
+                v = np.ascontiguousarray(ff["vertices"], np.float32)
+                t = np.ascontiguousarray(ff["triangles"], np.int32)
+                self.L.ref_add_point_force_field(self.h, len(v), _p(v), len(t), _p(t),
+                                                 _p(force_field_params(ff["params"])))
         self.L.ref_set_pic_ratio(self.h, scene.pic_ratio)
         self.L.ref_add_body_force(self.h, *scene.gravity)
         self.L.ref_set_cfl(self.h, scene.cfl)

@@ -72,8 +72,8 @@ def golden_cases(stages=False):
     names = sorted(p.stem for p in GOLDEN.glob("*.npz") if not p.stem.startswith(("iso_", "visc")))
     if stages:
         names = [n for n in names
-                 if json.loads(str(np.load(GOLDEN / f"{n}.npz")["meta"])).get("builder") not in ("mesh_fluid",
-                                                                                                 "fluid_sources")]
+                 if json.loads(str(np.load(GOLDEN / f"{n}.npz")["meta"])).get("builder") not in (
+                     "mesh_fluid", "fluid_sources", "force_fields")]
     return names
 
 

@@ -51,6 +51,11 @@ SOURCE_CASES = {
     "src24_both": (dict(n=24, which="both"), 8, 4),
     "src24_inversed": (dict(n=24, which="inversed"), 9, 4),
 }
+# point force fields (scenes.force_fields): the particles after every frame
+FORCE_FIELD_CASES = {
+    "ff24_point": (dict(n=24, which="point"), 6, 4),
+    "ff24_two": (dict(n=24, which="two"), 6, 4),
+}
 # viscosity (setViscosity): dam break + sphere with a constant viscosity;
 # the particles after every frame and the viscosity solver's status
 VISCOSITY_CASES = {
@@ -170,6 +175,9 @@ if __name__ == "__main__":
     for name, (kw, frames, thr) in SOURCE_CASES.items():
         if not only or name in only:
             make_mesh_fluid(name, kw, frames, thr, builder="fluid_sources", keep=(1, frames - 1, frames))
+    for name, (kw, frames, thr) in FORCE_FIELD_CASES.items():
+        if not only or name in only:
+            make_mesh_fluid(name, kw, frames, thr, builder="force_fields", keep=(1, frames - 1, frames))
     for name, (builder, kw, visc, frames) in VISCOSITY_CASES.items():
         if not only or name in only:
             make_viscosity(name, builder, kw, visc, frames)
