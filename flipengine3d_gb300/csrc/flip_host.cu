@@ -1740,7 +1740,8 @@ int flip_get_force_field_reduction_level(flip_ctx *x, int *level) {
 int flip_add_point_force_field(flip_ctx *x, int nverts, const float *verts, const flip_point_force_field_params *q,
                                int *id) {
     if (!x || !q) return FLIP_E_NULL;
-    if (!x->ffEnabled) return fail(FLIP_E_RUNTIME, "Error: force fields are not enabled.");
+    // getForceFieldGrid (fluidsimulation.cpp:1640-1648) throws std::domain_error
+    if (!x->ffEnabled) return fail(FLIP_E_DOMAIN, "Error: force fields must be enabled before using this method.");
     if (nverts < 0) return fail(FLIP_E_DOMAIN, "negative vertex count");
     if (nverts > 0 && !verts) return FLIP_E_NULL;
     float centroid[3];

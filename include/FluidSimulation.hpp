@@ -148,6 +148,64 @@ private:
     flip_fluid_source_params prm_;
 };
 
+// ForceFieldPoint (forcefieldpoint.cpp, forcefield.cpp): a point field at the
+// centroid of a static mesh's vertices.  Its parameters are pushed to the
+// simulation at every update(), as the reference reads them there.
+class ForceFieldPoint {
+public:
+    ForceFieldPoint() { prm_ = defaults(); }
+    void updateMeshStatic(const TriangleMesh &m) { mesh_ = m; }
+    const TriangleMesh &getMesh() const { return mesh_; }
+    void enable() { prm_.enabled = 1; }
+    void disable() { prm_.enabled = 0; }
+    bool isEnabled() const { return prm_.enabled != 0; }
+    void setStrength(float s) { prm_.strength = s; }
+    float getStrength() const { return prm_.strength; }
+    void setFalloffPower(float p) { prm_.falloff_power = p; }
+    float getFalloffPower() const { return prm_.falloff_power; }
+    void setMaxForceLimitFactor(float f) { prm_.max_force_limit_factor = f; }
+    float getMaxForceLimitFactor() const { return prm_.max_force_limit_factor; }
+    void enableMinDistance() { prm_.min_distance_enabled = 1; }
+    void disableMinDistance() { prm_.min_distance_enabled = 0; }
+    bool isMinDistanceEnabled() const { return prm_.min_distance_enabled != 0; }
+    void setMinDistance(float d) { prm_.min_distance = d; }
+    float getMinDistance() const { return prm_.min_distance; }
+    void enableMaxDistance() { prm_.max_distance_enabled = 1; }
+    void disableMaxDistance() { prm_.max_distance_enabled = 0; }
+    bool isMaxDistanceEnabled() const { return prm_.max_distance_enabled != 0; }
+    void setMaxDistance(float d) { prm_.max_distance = d; }
+    float getMaxDistance() const { return prm_.max_distance; }
+    void setGravityScale(float s) { prm_.gravity_scale = s; }
+    float getGravityScale() const { return prm_.gravity_scale; }
+    void setGravityScaleWidth(float w) { prm_.gravity_scale_width = w; }
+    float getGravityScaleWidth() const { return prm_.gravity_scale_width; }
+    const flip_point_force_field_params &params() const { return prm_; }
+
+private:
+    static flip_point_force_field_params defaults() {
+        flip_point_force_field_params p{};
+        p.falloff_power = 1.0f;
+        p.max_force_limit_factor = 3.0f;
+        p.gravity_scale = 1.0f;
+        p.enabled = 1;
+        return p;
+    }
+    TriangleMesh mesh_;
+    flip_point_force_field_params prm_;
+};
+
+class FluidSimulation;
+// What getForceFieldGrid() returns: addForceField registers a point field
+// (the pointer is kept; the caller owns the field, as in the reference).
+class ForceFieldGrid {
+public:
+    void addForceField(ForceFieldPoint *field);
+
+private:
+    friend class FluidSimulation;
+    FluidSimulation *sim_ = nullptr;
+};
+
 class FluidSimulation {
 public:
     FluidSimulation(int isize, int jsize, int ksize, double dx) : isize_(isize), jsize_(jsize), ksize_(ksize), dx_(dx) {
@@ -174,6 +232,7 @@ public:
     }
     void update(double dt) {
         for (auto &src : sources_) check(flip_set_mesh_fluid_source_params(ctx_, src.second, &src.first->params()));
+        for (auto &f : fields_) check(flip_set_point_force_field_params(ctx_, f.second, &f.first->params()));
         int rc = flip_update(ctx_, dt);
         if (rc != FLIP_E_SOLVER_NOCONV) check(rc);
     }
@@ -191,6 +250,34 @@ public:
         double r = 0.0;
         check(flip_get_pic_flip_ratio(ctx_, &r));
         return r;
+    }
+    // enableForceFields / setForceFieldReductionLevel / getForceFieldGrid
+    // (fluidsimulation.cpp:1605-1648)
+    void enableForceFields() { check(flip_enable_force_fields(ctx_, 1)); }
+    void disableForceFields() { check(flip_enable_force_fields(ctx_, 0)); }
+    bool isForceFieldsEnabled() {
+        int v = 0;
+        check(flip_is_force_fields_enabled(ctx_, &v));
+        return v != 0;
+    }
+    void setForceFieldReductionLevel(int level) { check(flip_set_force_field_reduction_level(ctx_, level)); }
+    int getForceFieldReductionLevel() {
+        int v = 0;
+        check(flip_get_force_field_reduction_level(ctx_, &v));
+        return v;
+    }
+    ForceFieldGrid *getForceFieldGrid() {
+        if (!isForceFieldsEnabled())
+            throw std::domain_error("Error: force fields must be enabled before using this method.\n");
+        grid_.sim_ = this;
+        return &grid_;
+    }
+    void addPointForceField(ForceFieldPoint *field) {
+        const TriangleMesh &m = field->getMesh();
+        int id = 0;
+        check(flip_add_point_force_field(ctx_, (int)m.vertices.size(), reinterpret_cast<const float *>(m.vertices.data()),
+                                         &field->params(), &id));
+        fields_.push_back({field, id});
     }
     // setViscosity / getViscosity (fluidsimulation.cpp:1650-1670)
     void setViscosity(double v) { check(flip_set_viscosity(ctx_, v)); }
@@ -354,7 +441,11 @@ private:
     TriangleMesh mesh_;
     std::vector<MeshObject *> obstacles_;
     std::vector<std::pair<MeshFluidSource *, int>> sources_;
+    std::vector<std::pair<ForceFieldPoint *, int>> fields_;
+    ForceFieldGrid grid_;
 };
+
+inline void ForceFieldGrid::addForceField(ForceFieldPoint *field) { sim_->addPointForceField(field); }
 
 }  // namespace flip3d
 

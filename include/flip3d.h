@@ -319,8 +319,8 @@ int flip_get_viscosity_solve(flip_ctx *ctx, long long *rows, int *iterations, do
  * on a grid of ceil(I / level) x ... cells of size level * dx, interpolated at
  * the faces (gravity outside it).  The grid is rebuilt at the first substep of
  * a frame after a field or the body force changed (_updateForceFieldGrid,
- * :3440-3448).  Fields are added once force fields are on (FLIP_E_RUNTIME
- * otherwise, as getForceFieldGrid throws); the reduction level (>= 1,
+ * :3440-3448).  Fields are added once force fields are on (FLIP_E_DOMAIN
+ * otherwise, as getForceFieldGrid throws std::domain_error); the reduction level (>= 1,
  * FLIP_E_DOMAIN otherwise) is taken when the grid is first built.  The
  * reference's getForceFieldReductionLevel returns the current frame
  * (fluidsimulation.cpp:1623-1625); flip_get_force_field_reduction_level

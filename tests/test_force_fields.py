@@ -108,7 +108,7 @@ def test_gpu_force_field_calls(gpu):
     with fs.FluidSimulation(16, 16, 16, 1.0 / 16) as sim:
         sim.disableSurfaceReconstruction()
         assert not sim.isForceFieldsEnabled()
-        with pytest.raises(RuntimeError):   # getForceFieldGrid() throws while force fields are off
+        with pytest.raises(ValueError):   # getForceFieldGrid() throws std::domain_error while they are off
             sim.addPointForceField(ff["vertices"], **ff["params"])
         sim.enableForceFields()
         with pytest.raises(ValueError):
