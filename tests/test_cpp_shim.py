@@ -289,3 +289,117 @@ def test_cpp_fluid_manager_initialize_matches_reference(gpu, tmp_path):
         ov, ot = sim.getIsomesh()
     assert np.array_equal(tris, ot) and np.array_equal(verts, ov)
     assert (verts >= 0).all() and (verts <= 4.0).all()
+
+
+FORCE_FIELD_DRIVER = r"""
+// Point force fields through the C++ face: the reference's calls
+// (enableForceFields, setForceFieldReductionLevel, a ForceFieldPoint on a
+// static mesh added with getForceFieldGrid()->addForceField), then one 1/60 s
+// frame of the loaded particles under gravity; positions written out.
+#include <cstdio>
+#include <vector>
+#include "FluidSimulation.hpp"
+
+int main(int argc, char **argv) {
+    int I, J, K, n, red, nfields;
+    double dx, pic;
+    std::FILE *in = std::fopen(argv[1], "rb");
+    if (!in || std::fread(&I, 4, 1, in) != 1 || std::fread(&J, 4, 1, in) != 1 || std::fread(&K, 4, 1, in) != 1 ||
+        std::fread(&dx, 8, 1, in) != 1 || std::fread(&pic, 8, 1, in) != 1 || std::fread(&n, 4, 1, in) != 1)
+        return 2;
+    std::vector<float> pos(3 * (size_t)n), vel(3 * (size_t)n);
+    if (std::fread(pos.data(), 4, pos.size(), in) != pos.size() || std::fread(vel.data(), 4, vel.size(), in) != vel.size() ||
+        std::fread(&red, 4, 1, in) != 1 || std::fread(&nfields, 4, 1, in) != 1)
+        return 2;
+    std::vector<flip3d::ForceFieldPoint> fields(nfields);
+    for (int q = 0; q < nfields; q++) {   // vertex count, triangle count, 10 parameters, vertices, triangles
+        int nv, nt;
+        float p[10];
+        if (std::fread(&nv, 4, 1, in) != 1 || std::fread(&nt, 4, 1, in) != 1 || std::fread(p, 4, 10, in) != 10) return 2;
+        flip3d::TriangleMesh m;
+        m.vertices.resize((size_t)nv);
+        m.triangles.resize((size_t)nt);
+        if (std::fread(m.vertices.data(), 12, m.vertices.size(), in) != m.vertices.size() ||
+            std::fread(m.triangles.data(), 12, m.triangles.size(), in) != m.triangles.size())
+            return 2;
+        flip3d::ForceFieldPoint &f = fields[q];
+        f.updateMeshStatic(m);
+        f.setStrength(p[0]);
+        f.setFalloffPower(p[1]);
+        f.setMaxForceLimitFactor(p[2]);
+        if (p[3] != 0.0f) f.enableMinDistance();
+        f.setMinDistance(p[4]);
+        if (p[5] != 0.0f) f.enableMaxDistance();
+        f.setMaxDistance(p[6]);
+        f.setGravityScale(p[7]);
+        f.setGravityScaleWidth(p[8]);
+        if (p[9] == 0.0f) f.disable();
+    }
+    std::fclose(in);
+    flip3d::FluidSimulation fluidsim(I, J, K, dx);
+    fluidsim.disableSurfaceReconstruction();
+    fluidsim.setPICFLIPRatio(pic);
+    fluidsim.addBodyForce(0.0, -9.81, 0.0);
+    fluidsim.enableForceFields();
+    fluidsim.setForceFieldReductionLevel(red);
+    for (auto &f : fields) fluidsim.getForceFieldGrid()->addForceField(&f);
+    flip3d::FluidSimulationMarkerParticleData data;
+    data.size = n;
+    data.positions = reinterpret_cast<char *>(pos.data());
+    data.velocities = reinterpret_cast<char *>(vel.data());
+    fluidsim.loadMarkerParticleData(data);
+    fluidsim.initialize();
+    fluidsim.update(1.0 / 60.0);
+    std::vector<char> out(fluidsim.getMarkerParticlePositionDataSize());
+    fluidsim.getMarkerParticlePositionData(out.data());
+    std::FILE *o = std::fopen(argv[2], "wb");
+    unsigned int m = fluidsim.getNumMarkerParticles();
+    std::fwrite(&m, 4, 1, o);
+    std::fwrite(out.data(), 1, out.size(), o);
+    std::fclose(o);
+    std::printf("%d %u\n", fluidsim.getCurrentFrame(), m);
+    return 0;
+}
+"""
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", ["ff24_point", "ff24_two"])
+def test_cpp_force_fields_match_the_reference(gpu, tmp_path, case):
+    """The point-field scenes set up through the C++ face (ForceFieldPoint,
+    getForceFieldGrid()->addForceField) give the reference engine's
+    particles after the first frame (fixtures ff24_*) within 1e-5."""
+    import numpy as np
+    from conftest import golden_scene, load_golden, rel_err
+    from oracle import refsim
+    gxx = shutil.which("g++")
+    if not gxx:
+        pytest.skip("g++ not available")
+    meta, g = load_golden(case)
+    sc = golden_scene(meta)
+    inp = tmp_path / "scene.bin"
+    with open(inp, "wb") as f:
+        np.array([sc.isize, sc.jsize, sc.ksize], np.int32).tofile(f)
+        np.array([sc.dx, sc.pic_ratio], np.float64).tofile(f)
+        np.array([len(sc.positions)], np.int32).tofile(f)
+        np.ascontiguousarray(sc.positions, np.float32).tofile(f)
+        np.ascontiguousarray(sc.velocities, np.float32).tofile(f)
+        np.array([sc.force_field_reduction, len(sc.force_fields)], np.int32).tofile(f)
+        for ff in sc.force_fields:
+            np.array([len(ff["vertices"]), len(ff["triangles"])], np.int32).tofile(f)
+            refsim.force_field_params(ff["params"]).tofile(f)
+            np.ascontiguousarray(ff["vertices"], np.float32).tofile(f)
+            np.ascontiguousarray(ff["triangles"], np.int32).tofile(f)
+    src = tmp_path / "ff.cpp"
+    src.write_text(FORCE_FIELD_DRIVER)
+    exe = tmp_path / "ff"
+    libdir = build.library_path().parent
+    subprocess.run([gxx, "-std=c++17", "-O2", "-I", str(ROOT / "include"), str(src), "-o", str(exe),
+                    "-L", str(libdir), "-lflip3d_gb300", f"-Wl,-rpath,{libdir}"], check=True)
+    out = tmp_path / "positions.bin"
+    r = subprocess.run([str(exe), str(inp), str(out)], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, (r.stdout, r.stderr)
+    frame, m = (int(v) for v in r.stdout.split())
+    pos = np.fromfile(out, dtype=np.float32, offset=4).reshape(-1, 3)
+    assert frame == 1 and pos.shape == g["positions_1"].shape == (m, 3)
+    assert rel_err(pos, g["positions_1"]) <= 1e-5
